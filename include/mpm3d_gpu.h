@@ -1,0 +1,156 @@
+/*
+ * mpm3d_gpu.h -- C ABI of the GB300 explicit MPM time step.
+ *
+ * This library replaces the bodies of the argument-less step subroutines that
+ * MPM3D.f90's time loop calls (MPM3D.f90:66-160). A Fortran host binds these
+ * functions with ISO_C_BINDING (mpm3d-f90_gb300/fortran/mpm3d_gpu_shim.f90);
+ * any other host (C, C++, Python ctypes) binds them directly. Plain pointers,
+ * sizes and int status codes only; no exception or C++ type crosses the ABI.
+ *
+ * Ownership: after mpm_create the device owns the live particle and grid
+ * state. The host mirror is refreshed only by mpm_download / mpm_get_*.
+ * Threading: one host thread per context; contexts are independent.
+ * Errors: every function returns an mpm_status (mpm_deck.h). Device-side
+ * health checks (non-finite state, particle outside the grid) are written to a
+ * per-context status word and reported by mpm_check / mpm_sync.
+ */
+#ifndef MPM3D_GPU_H
+#define MPM3D_GPU_H
+
+#include <stdint.h>
+
+#include "mpm_deck.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* Arithmetic forms of the step. */
+enum mpm_precision {
+  MPM_FP64_STRICT = 0, /* FP64 throughout, reference summation order, no FMA,
+                          project libm: bit-identical to the CPU oracle      */
+  MPM_FP64_NATIVE = 1, /* as STRICT but CUDA libm for log/exp/pow           */
+  MPM_MIXED = 2        /* FP32 shape functions, velocity gradient and
+                          constitutive update; FP64 grid mass / momentum /
+                          force accumulation, positions, velocities, energy  */
+};
+
+/* Step phases: one per reference subroutine, same order semantics.
+ * A Fortran shim calls mpm_step_phase(ctx, MPM_PHASE_x) from the body of the
+ * subroutine of the same name. */
+enum mpm_phase {
+  MPM_PHASE_GRID_MOMENTUM_INITIAL = 1,    /* update_step.f90:288  GridMomentumInitial     */
+  MPM_PHASE_APPLY_BOUNDARY = 2,           /* update_step.f90:1795 ApplyBoundaryConditions */
+  MPM_PHASE_PARTICLE_STRESS_UPDATE = 3,   /* update_step.f90:456  ParticleStressUpdate    */
+  MPM_PHASE_GRID_MOMENTUM_UPDATE = 4,     /* update_step.f90:831  GridMomentumUpdate      */
+  MPM_PHASE_INTEGRATE_MOMENTUM = 5,       /* update_step.f90:1194 IntegrateMomentum       */
+  MPM_PHASE_PARTICLE_POSITION_UPDATE = 6, /* update_step.f90:1378 ParticlePositionUpdate  */
+  MPM_PHASE_GRID_MOMENTUM_MUSL = 7,       /* update_step.f90:1668 GridMomentumMUSL        */
+  MPM_PHASE_CALC_ENERGY = 8,              /* Particle.f90:204     calcEnergy              */
+  MPM_PHASE_UPDATE_DT = 9,                /* update_step.f90:1833 UpdateDT                */
+  MPM_PHASE_DR_DAMPING = 10,              /* Particle.f90:172     dynamicRelaxationDamping*/
+  MPM_PHASE_BEGIN_STEP = 11               /* MPM3D.f90:72-74: istep+1, time += DT         */
+};
+
+/* Field identifiers for mpm_download / oracle accessors. Particle fields are
+ * component-major arrays of nb_particle doubles per component, in the input
+ * particle order; grid fields are per node in the reference's flat order
+ * (x fastest, MPM3D Grid.f90:299). */
+enum mpm_field {
+  MPM_P_XP = 1,      /* 3 */
+  MPM_P_XX = 2,      /* 3 */
+  MPM_P_VXP = 3,     /* 3 */
+  MPM_P_FXP = 4,     /* 3 */
+  MPM_P_XN = 5,      /* 3 */
+  MPM_P_XXN = 6,     /* 3 */
+  MPM_P_VOL = 7,
+  MPM_P_VOL0 = 8,
+  MPM_P_SIG_Y = 9,
+  MPM_P_SM = 10,
+  MPM_P_SEQV = 11,
+  MPM_P_SD = 12,     /* 6: xx, yy, zz, xy, yz, xz */
+  MPM_P_FP = 13,     /* 9: Fp(i,j) at i*3+j (0-based), Fp - I on the diagonal */
+  MPM_P_EPEFF = 14,
+  MPM_P_CELSIUS = 15,
+  MPM_P_DMG = 16,
+  MPM_P_LT = 17,
+  MPM_P_IE = 18,
+  MPM_P_MASS = 19,
+  MPM_P_CP = 20,
+  MPM_P_Q = 21,
+  MPM_P_FAILURE = 22, /* 0 / 1 */
+  MPM_P_ICELL = 23,   /* 1-based cell id, -1 outside */
+  MPM_P_CENTERICELL = 24,
+  MPM_P_INODE = 25,
+  MPM_G_MG = 40,
+  MPM_G_PX = 41,     /* 3 */
+  MPM_G_FX = 42,     /* 3 */
+  MPM_C_MG = 50,     /* SGMP auxiliary (cell-centre) grid mass */
+  MPM_C_PX = 51      /* 3 */
+};
+
+/* Scalar block returned by mpm_get_scalars (16 doubles):
+ * 0 istep, 1 CurrentTime, 2 DT, 3 EngKinetic, 4 EngInternal, 5-7 Momentum,
+ * 8 EngKinetic_prev, 9 nb_gridnode, 10 nb_particle, 11 CutOff, 12 DCell,
+ * 13 active nodes (Mg > 0) after the last P2G, 14 status word, 15 reserved. */
+#define MPM_NSCALARS 16
+
+/* Number of components a field has (1, 3, 6 or 9); 0 for an unknown id. */
+int mpm_field_components(int field);
+
+/* ------------------------------------------------------------- lifecycle */
+/* Create a context from a parsed deck: derives the set-up (Initial,
+ * SetGridData, SetDT, calcEnergy; DataIn.f90:1211-1297, Grid.f90:222-418,
+ * MPM3D.f90:42) and uploads the particle state. device < 0 picks the
+ * current device. */
+int mpm_create(const mpm_deck* deck, int precision, int device, mpm_ctx** out);
+void mpm_destroy(mpm_ctx* ctx);
+/* Last error text of a context (or of the library when ctx is NULL). */
+const char* mpm_last_error(const mpm_ctx* ctx);
+
+/* ------------------------------------------------------------------ step */
+/* One phase of the step (see enum mpm_phase). */
+int mpm_step_phase(mpm_ctx* ctx, int phase);
+/* One full step in the order of MPM3D.f90:69-118 (USF / USL / MUSL chosen by
+ * the deck flags): begin-step, P2G, stress, forces, integration, G2P, MUSL
+ * re-map, energies and the next DT. */
+int mpm_step(mpm_ctx* ctx);
+/* nsteps full steps, launched back to back without host synchronisation
+ * (captured once into a CUDA graph when use_graph != 0). */
+int mpm_run(mpm_ctx* ctx, int nsteps, int use_graph);
+/* Wait for the context's stream and read the device status word. */
+int mpm_sync(mpm_ctx* ctx);
+
+/* -------------------------------------------------------------- data I/O */
+int mpm_get_scalars(mpm_ctx* ctx, double* out16);
+/* Copy a field to host memory (out holds components * count doubles). */
+int mpm_download(mpm_ctx* ctx, int field, double* out);
+/* Replace a particle field (component-major, nb_particle per component). */
+int mpm_upload(mpm_ctx* ctx, int field, const double* in);
+int64_t mpm_nb_particle(const mpm_ctx* ctx);
+int64_t mpm_nb_gridnode(const mpm_ctx* ctx);
+int64_t mpm_nb_cell(const mpm_ctx* ctx);
+
+/* ---------------------------------------------------- measurement hooks */
+/* Time nsteps full steps with CUDA events on the context's stream;
+ * returns milliseconds in *ms. */
+int mpm_time_steps(mpm_ctx* ctx, int nsteps, int use_graph, double* ms);
+/* Per-kernel event timing: when enabled, every launch of the step records a
+ * start/stop event pair on the context's stream. mpm_kernel_stats returns,
+ * for kernel index k, its name, launch count and total milliseconds. */
+int mpm_profile_enable(mpm_ctx* ctx, int on);
+int mpm_kernel_count(const mpm_ctx* ctx);
+int mpm_kernel_stats(mpm_ctx* ctx, int k, char* name, int namelen, int64_t* launches,
+                     double* total_ms);
+/* Algorithmic bytes moved by the last step (particle fields read once and
+ * modified fields written once, plus active-node grid traffic). */
+int mpm_algorithmic_bytes(mpm_ctx* ctx, double* bytes_per_step);
+/* Bytes of device memory the context holds. */
+int64_t mpm_device_bytes(const mpm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

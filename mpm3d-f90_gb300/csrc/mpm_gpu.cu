@@ -1,0 +1,922 @@
+// mpm_gpu.cu -- host side of the C ABI declared in include/mpm3d_gpu.h.
+//
+// mpm_create derives the reference set-up from a parsed deck
+// (Initial, DataIn.f90:1211-1267; SetGridData, Grid.f90:222-418; SetDT,
+// DataIn.f90:1269-1297), uploads the structure-of-arrays state and runs the
+// initial calcEnergy (MPM3D.f90:42). mpm_step enqueues one time step
+// (MPM3D.f90:69-118) on the context's stream without host synchronisation;
+// mpm_run replays it from a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mpm3d_gpu.h"
+#include "mpm_gpu_internal.cuh"
+
+using namespace mpm;
+
+namespace {
+
+thread_local std::string g_lib_error;
+
+struct ProfRec {
+  int kernel;
+  cudaEvent_t a, b;
+};
+
+struct MaxOp {
+  __host__ __device__ int operator()(int a, int b) const { return a > b ? a : b; }
+};
+
+}  // namespace
+
+struct mpm_ctx {
+  int precision = 0;
+  const StepOps* ops = nullptr;
+  Geometry g{};
+  int device = 0;
+  int flags = 0;
+  int drdamp = 0;
+  cudaStream_t stream = nullptr;
+  DevState<double, double> st{};  // pointer layout is the same for every form
+  std::vector<void*> allocs;
+  long long bytes = 0;
+  int nkeys = 0;
+  long long npairs = 0;
+  int key_bits = 1;
+  int red_blocks = 1;
+  void* cub_tmp = nullptr;
+  size_t cub_tmp_bytes = 0;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_steps = 0;
+  bool graph_prof = false;
+  std::vector<DevMaterial> mats;
+  std::vector<DevBody> bodies;
+  // profiling
+  bool prof = false;
+  bool capturing = false;
+  std::vector<ProfRec> recs;
+  std::vector<cudaEvent_t> event_pool;
+  size_t event_next = 0;
+  double kstat_ms[K_COUNT] = {};
+  long long kstat_n[K_COUNT] = {};
+  std::string err;
+};
+
+namespace {
+
+thread_local mpm_ctx* t_prof_ctx = nullptr;  // context whose launches are being timed
+
+int set_err(mpm_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  else g_lib_error = buf;
+  return code;
+}
+
+int cuda_err(mpm_ctx* c, cudaError_t e, const char* what) {
+  return set_err(c, MPM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t e__ = (call);                           \
+    if (e__ != cudaSuccess) return cuda_err(c, e__, #call); \
+  } while (0)
+
+template <class T>
+int dalloc(mpm_ctx* c, T** p, long long n) {
+  if (n <= 0) n = 1;
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, (size_t)n * sizeof(T));
+  if (e != cudaSuccess) return set_err(c, MPM_ERR_OOM, "cudaMalloc(%lld bytes): %s", (long long)(n * sizeof(T)),
+                                       cudaGetErrorString(e));
+  c->allocs.push_back(q);
+  c->bytes += n * (long long)sizeof(T);
+  *p = (T*)q;
+  return MPM_OK;
+}
+
+cudaEvent_t pool_event(mpm_ctx* c) {
+  if (c->event_next == c->event_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    c->event_pool.push_back(e);
+  }
+  return c->event_pool[c->event_next++];
+}
+
+}  // namespace
+
+namespace mpm {
+void prof_begin(int k, cudaStream_t s) {
+  mpm_ctx* c = t_prof_ctx;
+  if (!c || !c->prof) return;
+  ProfRec r{k, pool_event(c), pool_event(c)};
+  if (c->capturing) cudaEventRecordWithFlags(r.a, s, cudaEventRecordExternal);
+  else cudaEventRecord(r.a, s);
+  c->recs.push_back(r);
+}
+void prof_end(int k, cudaStream_t s) {
+  mpm_ctx* c = t_prof_ctx;
+  if (!c || !c->prof || c->recs.empty()) return;
+  ProfRec& r = c->recs.back();
+  if (r.kernel != k) return;
+  if (c->capturing) cudaEventRecordWithFlags(r.b, s, cudaEventRecordExternal);
+  else cudaEventRecord(r.b, s);
+}
+}  // namespace mpm
+
+namespace {
+
+struct ProfScope {
+  mpm_ctx* prev;
+  explicit ProfScope(mpm_ctx* c) : prev(t_prof_ctx) { t_prof_ctx = c; }
+  ~ProfScope() { t_prof_ctx = prev; }
+};
+
+// ------------------------------------------------------------- set-up
+
+int derive_setup(mpm_ctx* c, const mpm_deck* d, std::vector<double>& host_vol, std::vector<double>& sig_y,
+                 std::vector<double>& ie, std::vector<double>& cp, std::vector<double>& lt,
+                 std::vector<uint8_t>& fix, std::vector<uint8_t>& bd) {
+  Geometry& g = c->g;
+  const long long np = d->nb_particle;
+  // materials (Initial overrides cEos(1) of null materials with the wave speed)
+  c->mats.resize(d->nb_mat);
+  for (int m = 0; m < d->nb_mat; ++m) {
+    const mpm_material& s = d->mats[m];
+    DevMaterial& t = c->mats[m];
+    memset(&t, 0, sizeof t);
+    t.mat_type = s.mat_type;
+    t.eos_type = s.eos_type;
+    t.density = s.density; t.miu = s.miu; t.young = s.young; t.poisson = s.poisson;
+    t.yield0 = s.yield0; t.tangmod = s.tangmod; t.roomt = s.roomt; t.melt = s.melt; t.specheat = s.specheat;
+    t.B_jc = s.B_jc; t.n_jc = s.n_jc; t.C_jc = s.C_jc; t.m_jc = s.m_jc; t.epso = s.epso; t.epf = s.epf;
+    t.D = s.D;
+    for (int k = 0; k < 10; ++k) t.cEos[k] = s.cEos[k];
+    t.wavespd = s.wavespd; t.q_fai = s.q_fai; t.k_fai = s.k_fai; t.q_psi = s.q_psi; t.ten_f = s.ten_f;
+    if (t.mat_type < 1 || t.mat_type > 11) return set_err(c, MPM_ERR_ARG, "material %d has no type", m + 1);
+    bool needs_eos = t.mat_type == 5 || t.mat_type == 6 || t.mat_type == 7 || t.mat_type == 8 || t.mat_type == 9;
+    if (needs_eos && (t.eos_type < 1 || t.eos_type > 4))
+      return set_err(c, MPM_ERR_ARG, "material %d (type %d) needs an equation of state", m + 1, t.mat_type);
+    if (t.eos_type == 3 && t.mat_type != 8)
+      return set_err(c, MPM_ERR_UNSUPPORTED, "JWL EOS is only supported with the 'hiex' material");
+  }
+  for (int m = 0; m < d->nb_mat; ++m)
+    if (c->mats[m].mat_type == 9) c->mats[m].cEos[0] = c->mats[m].wavespd;
+  c->bodies.resize(d->nb_body);
+  for (int b = 0; b < d->nb_body; ++b) {
+    if (d->bodies[b].mat < 1 || d->bodies[b].mat > d->nb_mat)
+      return set_err(c, MPM_ERR_ARG, "body %d has no material", b + 1);
+    c->bodies[b].mat = d->bodies[b].mat - 1;
+    for (int k = 0; k < 3; ++k) c->bodies[b].gravp[k] = d->bodies[b].gravp[k];
+  }
+  // Initial: per-particle volume, yield stress, internal energy, sound speed,
+  // lighting time (sqrt(...)/D is a default-REAL temporary)
+  host_vol.assign(np, 0.0); sig_y.assign(np, 0.0); ie.assign(np, 0.0); cp.assign(np, 0.0);
+  lt.assign(np, 0.0);
+  for (int b = 0; b < d->nb_body; ++b) {
+    const DevMaterial& m = c->mats[c->bodies[b].mat];
+    if (m.mat_type == 12) continue;
+    for (long long p = d->bodies[b].par_begin; p < d->bodies[b].par_end; ++p) {
+      double vol = d->mass[p] / m.density;
+      host_vol[p] = vol;
+      sig_y[p] = m.yield0;
+      ie[p] = d->mats[c->bodies[b].mat].cEos[9] * vol;
+      if (m.mat_type == 1 || m.mat_type == 11) {
+        double E = m.young, nu = m.poisson, ro = m.density;
+        cp[p] = std::sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
+      }
+      if (m.mat_type == 9) cp[p] = m.wavespd;
+      double ltv = (double)10e6f;
+      for (int j = 0; j < d->n_deto; ++j) {
+        double dx = d->xp[p] - d->deto[j][0];
+        double dy = d->xp[np + p] - d->deto[j][1];
+        double dz = d->xp[2 * np + p] - d->deto[j][2];
+        float t = (float)(std::sqrt(dx * dx + dy * dy + dz * dz) / m.D);
+        if ((double)t < ltv) ltv = (double)t;
+      }
+      lt[p] = ltv;
+    }
+  }
+  // SetGridData
+  const double h = d->dcell;
+  if (h == 0) return set_err(c, MPM_ERR_ARG, "DCell must be defined");
+  double sp[3], s0[3];
+  for (int a = 0; a < 3; ++a) {
+    s0[a] = d->span[a][0];
+    sp[a] = d->span[a][1] - d->span[a][0];
+    if (sp[a] <= 0) return set_err(c, MPM_ERR_ARG, "computational region must be defined");
+  }
+  int NC[3], CNC[3];
+  for (int a = 0; a < 3; ++a) {
+    NC[a] = (int)(sp[a] / h + 0.5);
+    CNC[a] = NC[a] - 1 == 0 ? 1 : NC[a] - 1;
+  }
+  long long nn = (long long)(NC[0] + 1) * (NC[1] + 1) * (NC[2] + 1);
+  long long ncell = (long long)NC[0] * NC[1] * NC[2];
+  if (nn > 2000000000LL) return set_err(c, MPM_ERR_UNSUPPORTED, "grid too large for 32-bit node ids");
+  if (np >= (1LL << 27)) return set_err(c, MPM_ERR_UNSUPPORTED, "more than 2^27 particles per context");
+  g.np = np;
+  g.NCx = NC[0]; g.NCy = NC[1]; g.NCz = NC[2]; g.NCxy = NC[0] * NC[1];
+  g.CNCx = CNC[0]; g.CNCy = CNC[1]; g.CNCz = CNC[2]; g.CNCxy = CNC[0] * CNC[1]; g.CNC = g.CNCxy * CNC[2];
+  g.ncell = (int)ncell;
+  g.NGx = NC[0] + 1; g.NGy = NC[1] + 1; g.NGz = NC[2] + 1; g.NGxy = g.NGx * g.NGy;
+  g.nn = (int)nn;
+  for (int a = 0; a < 3; ++a) {
+    g.span0[a] = s0[a];
+    g.span1[a] = s0[a] + NC[a] * h;
+  }
+  g.dcell = h;
+  g.cutoff = d->cutoff;
+  g.iJacobi = 2.0 / h;
+  g.iJacobi4 = g.iJacobi * 0.125;
+  g.iDCell = 1.0 / h;
+  const int f = d->flags;
+  const bool gimp = f & MPM_F_GIMP, bsp = f & MPM_F_BSPLINE, sgmp = f & MPM_F_SGMP;
+  g.shape = sgmp ? 3 : (gimp ? 1 : (bsp ? 2 : 0));
+  g.K = (g.shape == 1 || g.shape == 2) ? 27 : 8;
+  for (int k = 0; k < 6; ++k) g.fixs[k] = d->fixs[k];
+  g.usf = !!(f & MPM_F_USF);
+  g.usl = !!(f & MPM_F_USL);
+  g.musl = !!(f & MPM_F_MUSL);
+  g.uvfp = !!(f & MPM_F_UVFP);
+  g.qload = !!(f & MPM_F_QUASILOAD);
+  g.qdamp = !!(f & MPM_F_QUASIDAMP);
+  g.gravity = !!(f & MPM_F_GRAVITY);
+  g.qload_time = d->quasi_load_time;
+  g.damp_factor = d->damp_factor;
+  g.bq1 = d->bq1;
+  g.bq2 = d->bq2;
+  g.dtscale = d->dtscale;
+  g.nb_mat = d->nb_mat;
+  g.nb_body = d->nb_body;
+  g.has_jc = 0;
+  for (auto& m : c->mats)
+    if (m.mat_type == 4 || m.mat_type == 7) g.has_jc = 1;
+  // fixities and SGMP boundary types (Grid.f90:291-359)
+  fix.assign(nn, 0);
+  bd.assign(nn, 0);
+  const int* F = d->fixs;
+  const int NGx = g.NGx, NGy = g.NGy, NGz = g.NGz;
+  for (int iz = 1; iz <= NGz; ++iz)
+    for (int iy = 1; iy <= NGy; ++iy)
+      for (int ix = 1; ix <= NGx; ++ix) {
+        long long i = (long long)(iz - 1) * g.NGxy + (long long)(iy - 1) * NGx + (ix - 1);
+        int bt[3] = {0, 0, 0};
+        int idx[3] = {ix, iy, iz}, NG[3] = {NGx, NGy, NGz};
+        for (int a = 0; a < 3; ++a) {
+          if (idx[a] == 1 && F[2 * a] != 0) bt[a] = 1;
+          if (idx[a] == NG[a] && F[2 * a + 1] != 0) bt[a] = 2;
+          if (sgmp) {
+            if (idx[a] == 2 && F[2 * a] != 0) bt[a] = 1;
+            if (idx[a] == NG[a] - 1 && F[2 * a + 1] != 0) bt[a] = 2;
+          }
+        }
+        bd[i] = (uint8_t)(bt[0] | (bt[1] << 2) | (bt[2] << 4));
+        uint8_t fx = 0;
+        bool all = false;
+        for (int a = 0; a < 3; ++a) {
+          bool lo1 = idx[a] == 1, hi1 = idx[a] == NG[a];
+          bool lo2 = lo1 || idx[a] == 2, hi2 = hi1 || idx[a] == NG[a] - 1;
+          bool two = gimp || bsp || sgmp;  // a second node layer is fixed too
+          bool lo = two ? lo2 : lo1, hi = two ? hi2 : hi1;
+          if ((lo && F[2 * a] == 1) || (hi && F[2 * a + 1] == 1)) all = true;
+          if ((lo && F[2 * a] == 2) || (hi && F[2 * a + 1] == 2)) fx |= (uint8_t)(1 << a);
+        }
+        if (all) fx = 7;
+        fix[i] = fx;
+      }
+  return MPM_OK;
+}
+
+double set_dt(const std::vector<DevMaterial>& mats, double dcell, double dtscale) {
+  double dt = (double)1.0e6f;
+  for (const auto& m : mats) {
+    if (m.mat_type == 12) continue;
+    double E = m.young, nu = m.poisson, ro = m.density;
+    double cp = std::sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
+    if (m.D > cp) cp = m.D;
+    if (m.wavespd > cp) cp = m.wavespd;
+    double t = dcell / cp;
+    if (t < dt) dt = t;
+  }
+  return dt * dtscale;
+}
+
+template <class T>
+int upload_as(mpm_ctx* c, void* dst, const double* src, long long n, size_t elem) {
+  if (elem == sizeof(double)) {
+    CK(cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return MPM_OK;
+  }
+  std::vector<float> tmp((size_t)n);
+  for (long long i = 0; i < n; ++i) tmp[i] = (float)src[i];
+  CK(cudaMemcpyAsync(dst, tmp.data(), (size_t)n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+// ------------------------------------------------------------ sorting
+int sort_pairs(mpm_ctx* c) {
+  DevState<double, double>& s = c->st;
+  prof_begin(K_SORT, c->stream);
+  size_t tmp = c->cub_tmp_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(c->cub_tmp, tmp, s.key, s.key_sorted, s.val, s.val_sorted,
+                                                  (int)c->npairs, 0, c->key_bits, c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "radix sort");
+  // per-node pair counts -> inclusive prefix sums (segment ends)
+  tmp = c->cub_tmp_bytes;
+  e = cub::DeviceScan::InclusiveSum(c->cub_tmp, tmp, s.seg, s.seg, c->nkeys, c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "segment scan");
+  prof_end(K_SORT, c->stream);
+  return MPM_OK;
+}
+
+int depeff_pass(mpm_ctx* c) {
+  if (!c->g.has_jc) return MPM_OK;
+  DevState<double, double>& s = c->st;
+  size_t tmp = c->cub_tmp_bytes;
+  cudaError_t e = cub::DeviceScan::InclusiveScan(c->cub_tmp, tmp, s.setter, s.setter_scan, MaxOp(),
+                                                 (int)c->g.np, c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "depeff scan");
+  c->ops->depeff_apply(&c->st, c->g, c->stream);
+  return MPM_OK;
+}
+
+int build_pairs(mpm_ctx* c) {
+  cudaError_t e = cudaMemsetAsync(c->st.seg, 0, sizeof(int) * ((size_t)c->nkeys + 1), c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "memset seg");
+  c->ops->locate(&c->st, c->g, c->stream);
+  return sort_pairs(c);
+}
+
+int stress_pass(mpm_ctx* c) {
+  c->ops->stress(&c->st, c->g, c->stream);
+  return depeff_pass(c);
+}
+
+// one full step, MPM3D.f90:69-118, enqueued without synchronisation
+int enqueue_step(mpm_ctx* c) {
+  const Geometry& g = c->g;
+  const StepOps* o = c->ops;
+  void* st = &c->st;
+  cudaStream_t s = c->stream;
+  int r;
+  o->begin_step(st, g, s);
+  if ((r = build_pairs(c))) return r;
+  o->p2g_mass(st, g, g.usf, g.usf, s);
+  if (g.usf)
+    if ((r = stress_pass(c))) return r;
+  o->force_prep(st, g, s);
+  o->p2g_force(st, g, 1, s);
+  o->position(st, g, s);
+  if (g.musl) o->p2g_momentum(st, g, !g.usf, s);
+  if (!g.usf)
+    if ((r = stress_pass(c))) return r;
+  o->reduce(st, g, 3, c->red_blocks, s);
+  if (c->drdamp) o->dr_damping(st, g, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "kernel launch");
+  return MPM_OK;
+}
+
+void free_ctx(mpm_ctx* c) {
+  if (!c) return;
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  for (void* p : c->allocs) cudaFree(p);
+  for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int harvest_profile(mpm_ctx* c) {
+  if (c->recs.empty()) return MPM_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  for (const ProfRec& r : c->recs) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      c->kstat_ms[r.kernel] += ms;
+      c->kstat_n[r.kernel] += 1;
+    }
+  }
+  c->recs.clear();
+  c->event_next = 0;
+  return MPM_OK;
+}
+
+const char* kKernelNames[K_COUNT] = {"begin_step", "locate",     "pair_sort",     "segments",  "p2g_mass",
+                                     "node_velocity", "apply_bc", "stress_update", "depeff_tail", "force_prep",
+                                     "p2g_force_integrate", "integrate", "g2p_position", "p2g_musl",
+                                     "reduce_energy_dt", "dr_damping"};
+
+}  // namespace
+
+// =================================================================== ABI
+
+extern "C" {
+
+int mpm_field_components(int f) {
+  switch (f) {
+    case MPM_P_XP: case MPM_P_XX: case MPM_P_VXP: case MPM_P_FXP: case MPM_P_XN: case MPM_P_XXN:
+    case MPM_G_PX: case MPM_G_FX: case MPM_C_PX:
+      return 3;
+    case MPM_P_SD: return 6;
+    case MPM_P_FP: return 9;
+    case MPM_P_VOL: case MPM_P_VOL0: case MPM_P_SIG_Y: case MPM_P_SM: case MPM_P_SEQV: case MPM_P_EPEFF:
+    case MPM_P_CELSIUS: case MPM_P_DMG: case MPM_P_LT: case MPM_P_IE: case MPM_P_MASS: case MPM_P_CP:
+    case MPM_P_Q: case MPM_P_FAILURE: case MPM_P_ICELL: case MPM_P_CENTERICELL: case MPM_P_INODE:
+    case MPM_G_MG: case MPM_C_MG:
+      return 1;
+    default: return 0;
+  }
+}
+
+const char* mpm_last_error(const mpm_ctx* c) { return c ? c->err.c_str() : g_lib_error.c_str(); }
+
+int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
+  if (!out) return set_err(nullptr, MPM_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (!d) return set_err(nullptr, MPM_ERR_ARG, "deck is NULL");
+  if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM))
+    return set_err(nullptr, MPM_ERR_UNSUPPORTED, "contact and TLMPM are outside the explicit-step path");
+  if (d->nb_component != 1) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "only one grid component");
+  if (d->nb_particle <= 0 || d->nb_body <= 0 || d->nb_mat <= 0)
+    return set_err(nullptr, MPM_ERR_ARG, "deck defines no particles / bodies / materials");
+  if (d->nb_body > 65535) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "more than 65535 bodies");
+  mpm_ctx* c = new mpm_ctx();
+  c->precision = precision;
+  switch (precision) {
+    case MPM_FP64_STRICT: c->ops = &kOpsStrict; break;
+    case MPM_FP64_NATIVE: c->ops = &kOpsNative; break;
+    case MPM_MIXED: c->ops = &kOpsMixed; break;
+    default:
+      delete c;
+      return set_err(nullptr, MPM_ERR_ARG, "unknown precision %d", precision);
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    delete c;
+    return set_err(nullptr, MPM_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (device >= 0) {
+    if (device >= ndev) {
+      delete c;
+      return set_err(nullptr, MPM_ERR_ARG, "device %d does not exist", device);
+    }
+    cudaSetDevice(device);
+  }
+  cudaGetDevice(&c->device);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    int r = set_err(nullptr, MPM_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+    delete c;
+    return r;
+  }
+  c->flags = d->flags;
+  c->drdamp = !!(d->flags & MPM_F_DRDAMP);
+  std::vector<double> vol, sig_y, ie, cp, lt;
+  std::vector<uint8_t> fix, bd;
+  int r = derive_setup(c, d, vol, sig_y, ie, cp, lt, fix, bd);
+  if (r) {
+    g_lib_error = c->err;
+    free_ctx(c);
+    return r;
+  }
+  Geometry& g = c->g;
+  const long long np = g.np, nn = g.nn, nc = g.ncell;
+  const int K = g.K;
+  c->nkeys = g.shape == 3 ? (int)nc : (int)nn;
+  c->npairs = np * K;
+  c->key_bits = 1;
+  while ((1LL << c->key_bits) <= (long long)c->nkeys) c->key_bits++;
+  c->red_blocks = (int)std::min<long long>(1024, (np + kBlock - 1) / kBlock);
+  const size_t B = c->ops->bulk_size, Rz = c->ops->real_size;
+  DevState<double, double>& s = c->st;
+  // particle arrays
+#define AL(ptr, T, n) \
+  if ((r = dalloc(c, (T**)&(ptr), (n)))) goto fail;
+#define ALB(ptr, n)                                                      \
+  if (B == sizeof(double)) { AL(ptr, double, n); } else { AL(ptr, float, n); }
+#define ALR(ptr, n)                                                      \
+  if (Rz == sizeof(double)) { AL(ptr, double, n); } else { AL(ptr, float, n); }
+  {
+    AL(s.xp, double, 3 * np); AL(s.xx, double, 3 * np); AL(s.vxp, double, 3 * np); AL(s.fxp, double, 3 * np);
+    AL(s.mass, double, np); AL(s.ie, double, np);
+    ALB(s.vol, np); ALB(s.sig_y, np); ALB(s.sm, np); ALB(s.seqv, np); ALB(s.sd, 6 * np);
+    ALB(s.fp, g.uvfp ? 9 * np : 1); ALB(s.epeff, np); ALB(s.celsius, np); ALB(s.dmg, np); ALB(s.lt, np);
+    ALB(s.cp, np); ALB(s.q, np); ALB(s.xn, 3 * np); ALB(s.xxn, 3 * np);
+    AL(s.icell, int, np); AL(s.centericell, int, np); AL(s.inode, int, np);
+    AL(s.failure, uint8_t, np); AL(s.body, uint16_t, np);
+    AL(s.fext, double, 3 * np); AL(s.sdiag, double, 3 * np);
+    AL(s.snode, int, (long long)K * np);
+    ALR(s.shp, (long long)K * np);
+    if (g.shape != 3) { ALR(s.dndx, (long long)K * np); ALR(s.dndy, (long long)K * np); ALR(s.dndz, (long long)K * np); }
+    AL(s.key, unsigned, c->npairs); AL(s.val, unsigned, c->npairs);
+    AL(s.key_sorted, unsigned, c->npairs); AL(s.val_sorted, unsigned, c->npairs);
+    AL(s.seg, int, (long long)c->nkeys + 1);
+    AL(s.mg, double, nn); AL(s.px, double, 3 * nn); AL(s.fx, double, 3 * nn); AL(s.vg, double, 3 * nn);
+    AL(s.fix, uint8_t, nn); AL(s.bd, uint8_t, nn);
+    if (g.shape == 3) {
+      AL(s.cmg, double, nc); AL(s.cpx, double, 3 * nc); AL(s.cfext, double, 3 * nc); AL(s.cfint, double, 6 * nc);
+      AL(s.co, double, 6 * nc); AL(s.cw, double, 3 * nc); AL(s.cdefp, double, 9 * nc);
+      AL(s.cvx, double, 3 * nc); AL(s.cax, double, 3 * nc);
+    }
+    if (g.has_jc) {
+      AL(s.setter, int, np); AL(s.setter_scan, int, np); AL(s.dep, double, np);
+      AL(s.jc_aux, double, 5 * np); AL(s.deferred, uint8_t, np);
+    }
+    AL(s.red_part, double, (long long)kRedVals * c->red_blocks); AL(s.red_count, unsigned, 1);
+    AL(s.mats, DevMaterial, (long long)c->mats.size()); AL(s.bodies, DevBody, (long long)c->bodies.size());
+    AL(s.sc, DevScalars, 1);
+  }
+#undef AL
+#undef ALB
+#undef ALR
+  {
+    // CUB temporary storage: the largest of the three primitives
+    size_t t1 = 0, t2 = 0, t3 = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, t1, s.key, s.key_sorted, s.val, s.val_sorted, (int)c->npairs, 0,
+                                    c->key_bits, c->stream);
+    cub::DeviceScan::InclusiveSum(nullptr, t2, s.seg, s.seg, c->nkeys, c->stream);
+    if (g.has_jc) cub::DeviceScan::InclusiveScan(nullptr, t3, s.setter, s.setter_scan, MaxOp(), (int)np, c->stream);
+    c->cub_tmp_bytes = std::max(t1, std::max(t2, t3));
+    if ((r = dalloc(c, (char**)&c->cub_tmp, (long long)c->cub_tmp_bytes))) goto fail;
+  }
+  // uploads
+  {
+#define UPB(dst, src, n) \
+  if ((r = upload_as<double>(c, (dst), (src), (n), B))) goto fail;
+#define CKF(call)                                              \
+  if ((e = (call)) != cudaSuccess) { r = cuda_err(c, e, #call); goto fail; }
+    CKF(cudaMemcpyAsync(s.xp, d->xp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.xx, d->xp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.vxp, d->vxp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.fxp, d->fxp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.mass, d->mass, sizeof(double) * np, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.ie, ie.data(), sizeof(double) * np, cudaMemcpyHostToDevice, c->stream));
+    std::vector<double> zeros((size_t)9 * np, 0.0), t293((size_t)np, (double)293.0f);
+    UPB(s.vol, vol.data(), np);
+    UPB(s.sig_y, sig_y.data(), np);
+    UPB(s.cp, cp.data(), np);
+    UPB(s.lt, lt.data(), np);
+    UPB(s.celsius, t293.data(), np);
+    UPB(s.sm, zeros.data(), np);
+    UPB(s.seqv, zeros.data(), np);
+    UPB(s.sd, zeros.data(), 6 * np);
+    if (g.uvfp) UPB(s.fp, zeros.data(), 9 * np);
+    UPB(s.epeff, zeros.data(), np);
+    UPB(s.dmg, zeros.data(), np);
+    UPB(s.q, zeros.data(), np);
+    UPB(s.xn, zeros.data(), 3 * np);
+    UPB(s.xxn, zeros.data(), 3 * np);
+    CKF(cudaMemsetAsync(s.failure, 0, np, c->stream));
+    std::vector<uint16_t> body((size_t)np, 0);
+    for (int b = 0; b < d->nb_body; ++b)
+      for (long long p = d->bodies[b].par_begin; p < d->bodies[b].par_end; ++p) body[p] = (uint16_t)b;
+    CKF(cudaMemcpyAsync(s.body, body.data(), sizeof(uint16_t) * np, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.fix, fix.data(), nn, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.bd, bd.data(), nn, cudaMemcpyHostToDevice, c->stream));
+    CKF(cudaMemcpyAsync(s.mats, c->mats.data(), sizeof(DevMaterial) * c->mats.size(), cudaMemcpyHostToDevice,
+                        c->stream));
+    CKF(cudaMemcpyAsync(s.bodies, c->bodies.data(), sizeof(DevBody) * c->bodies.size(), cudaMemcpyHostToDevice,
+                        c->stream));
+    CKF(cudaMemsetAsync(s.mg, 0, sizeof(double) * nn, c->stream));
+    CKF(cudaMemsetAsync(s.px, 0, sizeof(double) * 3 * nn, c->stream));
+    CKF(cudaMemsetAsync(s.fx, 0, sizeof(double) * 3 * nn, c->stream));
+    CKF(cudaMemsetAsync(s.vg, 0, sizeof(double) * 3 * nn, c->stream));
+    CKF(cudaMemsetAsync(s.red_count, 0, sizeof(unsigned), c->stream));
+    DevScalars sc0;
+    memset(&sc0, 0, sizeof sc0);
+    sc0.dt = set_dt(c->mats, g.dcell, g.dtscale);
+    CKF(cudaMemcpyAsync(s.sc, &sc0, sizeof sc0, cudaMemcpyHostToDevice, c->stream));
+    if (g.shape == 3) {
+      CKF(cudaMemsetAsync(s.cmg, 0, sizeof(double) * nc, c->stream));
+      CKF(cudaMemsetAsync(s.cpx, 0, sizeof(double) * 3 * nc, c->stream));
+    }
+    // calcEnergy before the loop (MPM3D.f90:42)
+    c->ops->reduce(&c->st, g, 1, c->red_blocks, c->stream);
+    CKF(cudaStreamSynchronize(c->stream));
+    CKF(cudaGetLastError());
+#undef UPB
+#undef CKF
+  }
+  *out = c;
+  return MPM_OK;
+fail:
+  g_lib_error = c->err;
+  free_ctx(c);
+  return r;
+}
+
+void mpm_destroy(mpm_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_ctx(c);
+}
+
+int mpm_step_phase(mpm_ctx* c, int phase) {
+  if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  ProfScope ps(c);
+  const Geometry& g = c->g;
+  const StepOps* o = c->ops;
+  void* st = &c->st;
+  cudaStream_t s = c->stream;
+  int r = MPM_OK;
+  switch (phase) {
+    case MPM_PHASE_BEGIN_STEP: o->begin_step(st, g, s); break;
+    case MPM_PHASE_GRID_MOMENTUM_INITIAL:
+      if ((r = build_pairs(c))) return r;
+      o->p2g_mass(st, g, 0, 0, s);
+      break;
+    case MPM_PHASE_APPLY_BOUNDARY: o->apply_bc(st, g, s); break;
+    case MPM_PHASE_PARTICLE_STRESS_UPDATE:
+      o->node_velocity(st, g, s);
+      if ((r = stress_pass(c))) return r;
+      break;
+    case MPM_PHASE_GRID_MOMENTUM_UPDATE:
+      o->force_prep(st, g, s);
+      o->p2g_force(st, g, 0, s);
+      break;
+    case MPM_PHASE_INTEGRATE_MOMENTUM: o->integrate(st, g, s); break;
+    case MPM_PHASE_PARTICLE_POSITION_UPDATE:
+      o->node_velocity(st, g, s);
+      o->position(st, g, s);
+      break;
+    case MPM_PHASE_GRID_MOMENTUM_MUSL: o->p2g_momentum(st, g, 0, s); break;
+    case MPM_PHASE_CALC_ENERGY: o->reduce(st, g, 1, c->red_blocks, s); break;
+    case MPM_PHASE_UPDATE_DT: o->reduce(st, g, 2, c->red_blocks, s); break;
+    case MPM_PHASE_DR_DAMPING: o->dr_damping(st, g, s); break;
+    default: return set_err(c, MPM_ERR_ARG, "unknown phase %d", phase);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "kernel launch");
+  return r;
+}
+
+int mpm_step(mpm_ctx* c) {
+  if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  ProfScope ps(c);
+  return enqueue_step(c);
+}
+
+static int ensure_graph(mpm_ctx* c, int nsteps) {
+  if (c->graph_exec && c->graph_steps == nsteps && c->graph_prof == c->prof) return MPM_OK;
+  if (c->graph_exec) {
+    cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+  }
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  c->capturing = true;
+  int r = MPM_OK;
+  for (int i = 0; i < nsteps && r == MPM_OK; ++i) r = enqueue_step(c);
+  c->capturing = false;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+  if (r) return r;
+  if (e != cudaSuccess) return cuda_err(c, e, "end capture");
+  e = cudaGraphInstantiate(&c->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_err(c, e, "graph instantiate");
+  c->graph_steps = nsteps;
+  c->graph_prof = c->prof;
+  return MPM_OK;
+}
+
+int mpm_run(mpm_ctx* c, int nsteps, int use_graph) {
+  if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  if (nsteps <= 0) return MPM_OK;
+  ProfScope ps(c);
+  if (!use_graph) {
+    for (int i = 0; i < nsteps; ++i) {
+      int r = enqueue_step(c);
+      if (r) return r;
+    }
+    return MPM_OK;
+  }
+  // a graph of one step, launched nsteps times (profiling records only the
+  // event nodes of the captured step, so profiled runs use a graph of all
+  // steps instead)
+  int gsteps = c->prof ? nsteps : 1;
+  if (c->prof) {
+    // re-capture so that the event records of this run are the live ones
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+    c->recs.clear();
+    c->event_next = 0;
+  }
+  int r = ensure_graph(c, gsteps);
+  if (r) return r;
+  for (int i = 0; i < nsteps / gsteps; ++i) CK(cudaGraphLaunch(c->graph_exec, c->stream));
+  return MPM_OK;
+}
+
+int mpm_sync(mpm_ctx* c) {
+  if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  CK(cudaStreamSynchronize(c->stream));
+  unsigned status = 0;
+  CK(cudaMemcpy(&status, &c->st.sc->status, sizeof status, cudaMemcpyDeviceToHost));
+  if (status & (ST_NONFINITE)) return set_err(c, MPM_ERR_NONFINITE, "non-finite particle state");
+  if (status & ST_BAD_EOS) return set_err(c, MPM_ERR_ARG, "a material without equation of state called one");
+  return MPM_OK;
+}
+
+int mpm_get_scalars(mpm_ctx* c, double* o) {
+  if (!c || !o) return set_err(c, MPM_ERR_ARG, "bad argument");
+  CK(cudaStreamSynchronize(c->stream));
+  DevScalars sc;
+  CK(cudaMemcpy(&sc, c->st.sc, sizeof sc, cudaMemcpyDeviceToHost));
+  memset(o, 0, sizeof(double) * MPM_NSCALARS);
+  o[0] = sc.istep; o[1] = sc.time; o[2] = sc.dt; o[3] = sc.ke; o[4] = sc.ie;
+  o[5] = sc.mom[0]; o[6] = sc.mom[1]; o[7] = sc.mom[2]; o[8] = sc.ke_prev;
+  o[9] = c->g.nn; o[10] = (double)c->g.np; o[11] = c->g.cutoff; o[12] = c->g.dcell;
+  o[13] = (double)sc.active_nodes; o[14] = sc.status;
+  return MPM_OK;
+}
+
+int64_t mpm_nb_particle(const mpm_ctx* c) { return c ? c->g.np : -1; }
+int64_t mpm_nb_gridnode(const mpm_ctx* c) { return c ? c->g.nn : -1; }
+int64_t mpm_nb_cell(const mpm_ctx* c) { return c ? c->g.ncell : -1; }
+int64_t mpm_device_bytes(const mpm_ctx* c) { return c ? c->bytes : -1; }
+
+static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long* count) {
+  DevState<double, double>& s = c->st;
+  const long long np = c->g.np, nn = c->g.nn, nc = c->g.ncell;
+  const size_t B = c->ops->bulk_size;
+  *elem = 8;
+  *count = np * mpm_field_components(field);
+  switch (field) {
+    case MPM_P_XP: *ptr = s.xp; break;
+    case MPM_P_XX: *ptr = s.xx; break;
+    case MPM_P_VXP: *ptr = s.vxp; break;
+    case MPM_P_FXP: *ptr = s.fxp; break;
+    case MPM_P_MASS: *ptr = s.mass; break;
+    case MPM_P_IE: *ptr = s.ie; break;
+    case MPM_P_XN: *ptr = s.xn; *elem = B; break;
+    case MPM_P_XXN: *ptr = s.xxn; *elem = B; break;
+    case MPM_P_VOL: *ptr = s.vol; *elem = B; break;
+    case MPM_P_SIG_Y: *ptr = s.sig_y; *elem = B; break;
+    case MPM_P_SM: *ptr = s.sm; *elem = B; break;
+    case MPM_P_SEQV: *ptr = s.seqv; *elem = B; break;
+    case MPM_P_SD: *ptr = s.sd; *elem = B; break;
+    case MPM_P_FP:
+      if (!c->g.uvfp) return set_err(c, MPM_ERR_ARG, "deformation gradient is not tracked (no UVFp)");
+      *ptr = s.fp; *elem = B; break;
+    case MPM_P_EPEFF: *ptr = s.epeff; *elem = B; break;
+    case MPM_P_CELSIUS: *ptr = s.celsius; *elem = B; break;
+    case MPM_P_DMG: *ptr = s.dmg; *elem = B; break;
+    case MPM_P_LT: *ptr = s.lt; *elem = B; break;
+    case MPM_P_CP: *ptr = s.cp; *elem = B; break;
+    case MPM_P_Q: *ptr = s.q; *elem = B; break;
+    case MPM_P_FAILURE: *ptr = s.failure; *elem = 1; break;
+    case MPM_P_ICELL: *ptr = s.icell; *elem = 4; break;
+    case MPM_P_CENTERICELL: *ptr = s.centericell; *elem = 4; break;
+    case MPM_P_INODE: *ptr = s.inode; *elem = 4; break;
+    case MPM_G_MG: *ptr = s.mg; *count = nn; break;
+    case MPM_G_PX: *ptr = s.px; *count = 3 * nn; break;
+    case MPM_G_FX: *ptr = s.fx; *count = 3 * nn; break;
+    case MPM_C_MG:
+      if (!s.cmg) return set_err(c, MPM_ERR_ARG, "no auxiliary grid (not SGMP)");
+      *ptr = s.cmg; *count = nc; break;
+    case MPM_C_PX:
+      if (!s.cpx) return set_err(c, MPM_ERR_ARG, "no auxiliary grid (not SGMP)");
+      *ptr = s.cpx; *count = 3 * nc; break;
+    default: return set_err(c, MPM_ERR_ARG, "field %d is not available", field);
+  }
+  return MPM_OK;
+}
+
+int mpm_download(mpm_ctx* c, int field, double* out) {
+  if (!c || !out) return set_err(c, MPM_ERR_ARG, "bad argument");
+  void* p = nullptr;
+  size_t elem = 0;
+  long long n = 0;
+  int r = field_ptr(c, field, &p, &elem, &n);
+  if (r) return r;
+  CK(cudaStreamSynchronize(c->stream));
+  if (elem == 8) {
+    CK(cudaMemcpy(out, p, (size_t)n * 8, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+  }
+  std::vector<unsigned char> tmp((size_t)n * elem);
+  CK(cudaMemcpy(tmp.data(), p, tmp.size(), cudaMemcpyDeviceToHost));
+  for (long long i = 0; i < n; ++i) {
+    if (elem == 4 && (field == MPM_P_ICELL || field == MPM_P_CENTERICELL || field == MPM_P_INODE))
+      out[i] = ((const int*)tmp.data())[i];
+    else if (elem == 4)
+      out[i] = ((const float*)tmp.data())[i];
+    else
+      out[i] = tmp[i];
+  }
+  return MPM_OK;
+}
+
+int mpm_upload(mpm_ctx* c, int field, const double* in) {
+  if (!c || !in) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (field >= MPM_G_MG || field == MPM_P_ICELL || field == MPM_P_CENTERICELL || field == MPM_P_INODE ||
+      field == MPM_P_FAILURE)
+    return set_err(c, MPM_ERR_ARG, "field %d cannot be uploaded", field);
+  void* p = nullptr;
+  size_t elem = 0;
+  long long n = 0;
+  int r = field_ptr(c, field, &p, &elem, &n);
+  if (r) return r;
+  CK(cudaStreamSynchronize(c->stream));
+  if (elem == 8) {
+    CK(cudaMemcpy(p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> tmp((size_t)n);
+    for (long long i = 0; i < n; ++i) tmp[i] = (float)in[i];
+    CK(cudaMemcpy(p, tmp.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+  }
+  if (c->graph_exec) {
+    cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+  }
+  return MPM_OK;
+}
+
+int mpm_time_steps(mpm_ctx* c, int nsteps, int use_graph, double* ms) {
+  if (!c || !ms) return set_err(c, MPM_ERR_ARG, "bad argument");
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaEventRecord(a, c->stream));
+  int r = mpm_run(c, nsteps, use_graph);
+  CK(cudaEventRecord(b, c->stream));
+  CK(cudaEventSynchronize(b));
+  float f = 0;
+  cudaEventElapsedTime(&f, a, b);
+  *ms = f;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (r) return r;
+  if (c->prof) harvest_profile(c);
+  return MPM_OK;
+}
+
+int mpm_profile_enable(mpm_ctx* c, int on) {
+  if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  if (c->prof) harvest_profile(c);
+  c->prof = on != 0;
+  for (int k = 0; k < K_COUNT; ++k) {
+    c->kstat_ms[k] = 0;
+    c->kstat_n[k] = 0;
+  }
+  return MPM_OK;
+}
+
+int mpm_kernel_count(const mpm_ctx*) { return K_COUNT; }
+
+int mpm_kernel_stats(mpm_ctx* c, int k, char* name, int namelen, int64_t* launches, double* total_ms) {
+  if (!c || k < 0 || k >= K_COUNT) return set_err(c, MPM_ERR_ARG, "bad kernel index");
+  harvest_profile(c);
+  if (name && namelen > 0) snprintf(name, (size_t)namelen, "%s", kKernelNames[k]);
+  if (launches) *launches = c->kstat_n[k];
+  if (total_ms) *total_ms = c->kstat_ms[k];
+  return MPM_OK;
+}
+
+int mpm_algorithmic_bytes(mpm_ctx* c, double* bytes) {
+  if (!c || !bytes) return set_err(c, MPM_ERR_ARG, "bad argument");
+  double sc[MPM_NSCALARS];
+  int r = mpm_get_scalars(c, sc);
+  if (r) return r;
+  const double Bw = (double)c->ops->bulk_size;
+  // per particle: read {Xp, VXp, mass, VOL, SM, SD, q, ie, cp},
+  // write {Xp, VXp, VOL, SM, SD, q, ie, seqv}
+  double per_p = (24 + 24 + 8 + 8) + Bw * (1 + 1 + 6 + 1 + 1) + (24 + 24 + 8) + Bw * (1 + 1 + 6 + 1 + 1);
+  bool jc = false, dp = false, neo = false, loads = false;
+  for (auto& m : c->mats) {
+    if (m.mat_type >= 4 && m.mat_type <= 7) jc = true;
+    if (m.mat_type == 10) dp = true;
+    if (m.mat_type == 11) neo = true;
+  }
+  if (c->g.qload || (c->flags & MPM_F_QUASILOAD)) loads = true;
+  if (jc) per_p += 2 * 3 * Bw;
+  if (dp) per_p += 2 * Bw;
+  if (neo) per_p += 2 * 9 * Bw;
+  if (loads) per_p += 24;
+  double per_node = 112 + (c->g.musl ? 48 : 0);
+  *bytes = per_p * (double)c->g.np + per_node * sc[13];
+  return MPM_OK;
+}
+
+}  // extern "C"

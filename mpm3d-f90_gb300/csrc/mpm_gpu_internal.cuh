@@ -1,0 +1,163 @@
+// mpm_gpu_internal.cuh -- device data layout and launch interface of the
+// GB300 explicit MPM step (internal to libmpm3d_gpu).
+//
+// Layout in HBM (structure of arrays, one allocation per field):
+//   particles, in input order (the reference's particle_list order):
+//     FP64 always : xp[3][Np], xx[3][Np], vxp[3][Np], fxp[3][Np], mass[Np], ie[Np]
+//     "bulk" type B (double for the FP64 forms, float for the mixed form):
+//                   vol, sig_y, sm, seqv, sd[6], fp[9], epeff, celsius, dmg, lt,
+//                   cp, q, xn[3], xxn[3]
+//     int32       : icell, centericell, inode; uint8 failure; uint16 body
+//   shape cache (recomputed every step by the locate kernel, reused by every
+//   particle pass of the step; type R = double / float):
+//     node[K][Np] int32 (0-based node, -1 = not an influence node),
+//     shp / dndx / dndy / dndz [K][Np]
+//   node-sorted pair list: key[K*Np] = node, val[K*Np] = (p << 5) | slot,
+//     stably radix-sorted by node so that each node's contributions appear in
+//     the reference's summation order (ascending particle, then slot);
+//     seg[n] = end of node n's slice (inclusive prefix sum of the counts).
+//   grid, FP64, flat reference node order: mg[Nn], px[3][Nn], fx[3][Nn],
+//     vg[3][Nn] (= px/mg), uint8 fix[Nn] (bit c = DOF c fixed), uint8 bd[Nn]
+//   SGMP auxiliary grid (one centre node per cell), FP64: cmg, cpx[3],
+//     cfext[3], cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3].
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpm3d_gpu.h"
+
+namespace mpm {
+
+constexpr int kMaxMat = 16;
+constexpr int kMaxBody = 64;
+constexpr int kBlock = 256;
+constexpr int kRedVals = 6;  // values reduced per step: ke, ie, momentum x/y/z, max |v| component
+
+// Device status bits (per context status word).
+enum StatusBits : unsigned {
+  ST_NONFINITE = 1u << 0,
+  ST_OUT_OF_GRID = 1u << 1,
+  ST_NEGATIVE_VOLUME = 1u << 2,
+  ST_BAD_EOS = 1u << 3
+};
+
+struct DevMaterial {
+  int mat_type, eos_type;
+  double density, miu, young, poisson, yield0, tangmod, roomt, melt, specheat;
+  double B_jc, n_jc, C_jc, m_jc, epso, epf, D;
+  double cEos[10];
+  double wavespd, q_fai, k_fai, q_psi, ten_f;
+};
+
+struct DevBody {
+  int mat;  // 0-based material index
+  double gravp[3];
+};
+
+// Scalars that stay on the device across steps (MPM3D.f90 loop state).
+struct DevScalars {
+  int istep;
+  int pad_;
+  double time;       // CurrentTime
+  double dt;         // DT
+  double ke, ie, mom[3], ke_prev;
+  double depeff_carry;  // MaterialModel's module-level depeff after the last particle
+  double max_vp;
+  unsigned long long active_nodes;
+  unsigned status;
+  unsigned pad2_;
+};
+
+// Everything a kernel needs besides the arrays.
+struct Geometry {
+  long long np;       // particles
+  int nn;             // grid nodes
+  int ncell;          // cells (= SGMP centre nodes)
+  int NGx, NGy, NGz, NGxy;
+  int NCx, NCy, NCz, NCxy;        // NumCellx..
+  int CNCx, CNCy, CNCz, CNCxy, CNC;  // CenterNumCell..
+  int K;              // influence slots per particle (8 or 27)
+  int shape;          // 0 linear, 1 GIMP, 2 B-spline, 3 SGMP
+  double span0[3], span1[3];
+  double dcell, cutoff, iJacobi, iJacobi4, iDCell;
+  double dtscale, qload_time, damp_factor, bq1, bq2;
+  int fixs[6];
+  int usf, usl, musl, uvfp, qload, qdamp, gravity;
+  int nb_mat, nb_body;
+  int has_jc;         // a Johnson-Cook material (types 4, 7) is present
+};
+
+template <class B, class R>
+struct DevState {
+  // particles
+  double *xp, *xx, *vxp, *fxp, *mass, *ie;
+  B *vol, *sig_y, *sm, *seqv, *sd, *fp, *epeff, *celsius, *dmg, *lt, *cp, *q, *xn, *xxn;
+  int *icell, *centericell, *inode;
+  uint8_t* failure;
+  uint16_t* body;
+  // force inputs prepared per particle before the force transfer
+  double *fext, *sdiag;  // fext[3][Np], sdiag[3][Np] = SM - q + SDii
+  // shape cache
+  int* snode;
+  R *shp, *dndx, *dndy, *dndz;
+  // pairs
+  unsigned *key, *val, *key_sorted, *val_sorted;
+  int* seg;
+  // grid
+  double *mg, *px, *fx, *vg;
+  uint8_t *fix, *bd;
+  // SGMP centre grid
+  double *cmg, *cpx, *cfext, *cfint, *co, *cw, *cdefp, *cvx, *cax;
+  // Johnson-Cook depeff carry
+  int *setter, *setter_scan;
+  double *dep;
+  double *jc_aux;  // [5][Np]: vold, ieinc, dvol, smold, vol_ of deferred particles
+  uint8_t* deferred;
+  // reductions
+  double* red_part;  // per-block partial sums
+  unsigned* red_count;
+  DevMaterial* mats;
+  DevBody* bodies;
+  DevScalars* sc;
+};
+
+// One launch table per arithmetic form; each form is compiled in its own
+// translation unit (FP64 forms without FMA contraction).
+struct StepOps {
+  const char* name;
+  size_t bulk_size, real_size;
+  void (*begin_step)(void* st, const Geometry& g, cudaStream_t s);
+  void (*locate)(void* st, const Geometry& g, cudaStream_t s);
+  void (*node_offsets)(void* st, const Geometry& g, long long npairs, cudaStream_t s);
+  // P2G of mass + momentum; bc: apply the fixed-DOF zeroing; vel: write vg
+  void (*p2g_mass)(void* st, const Geometry& g, int bc, int vel, cudaStream_t s);
+  void (*node_velocity)(void* st, const Geometry& g, cudaStream_t s);
+  void (*apply_bc)(void* st, const Geometry& g, cudaStream_t s);
+  void (*stress)(void* st, const Geometry& g, cudaStream_t s);
+  void (*depeff_apply)(void* st, const Geometry& g, cudaStream_t s);
+  void (*force_prep)(void* st, const Geometry& g, cudaStream_t s);
+  // force transfer; integ: also integrate momentum + BC + vg
+  void (*p2g_force)(void* st, const Geometry& g, int integ, cudaStream_t s);
+  void (*integrate)(void* st, const Geometry& g, cudaStream_t s);
+  void (*position)(void* st, const Geometry& g, cudaStream_t s);
+  void (*p2g_momentum)(void* st, const Geometry& g, int vel, cudaStream_t s);
+  // mode bit 0: energies and momentum (calcEnergy), bit 1: next DT (UpdateDT)
+  void (*reduce)(void* st, const Geometry& g, int mode, int nblocks, cudaStream_t s);
+  void (*dr_damping)(void* st, const Geometry& g, cudaStream_t s);
+};
+
+extern const StepOps kOpsStrict;   // MPM_FP64_STRICT
+extern const StepOps kOpsNative;   // MPM_FP64_NATIVE
+extern const StepOps kOpsMixed;    // MPM_MIXED
+
+// Kernel launch bookkeeping for per-kernel event timing.
+void prof_begin(int kernel_id, cudaStream_t s);
+void prof_end(int kernel_id, cudaStream_t s);
+
+enum KernelId {
+  K_BEGIN = 0, K_LOCATE, K_SORT, K_SEG, K_P2G_MASS, K_NODE_VEL, K_BC, K_STRESS, K_DEPEFF,
+  K_FORCE_PREP, K_P2G_FORCE, K_INTEGRATE, K_POSITION, K_P2G_MOM, K_REDUCE, K_DR, K_COUNT
+};
+
+}  // namespace mpm

@@ -1,0 +1,324 @@
+"""Python host binding of libmpm3d_gpu, the GB300 explicit MPM time step.
+
+The module mirrors the reference's step interface: a :class:`MpmStep` object
+owns one device context and exposes one method per reference subroutine
+(``GridMomentumInitial``, ``ApplyBoundaryConditions``, ``ParticleStressUpdate``,
+``GridMomentumUpdate``, ``IntegrateMomentum``, ``ParticlePositionUpdate``,
+``GridMomentumMUSL``, ``calcEnergy``, ``UpdateDT``,
+``dynamicRelaxationDamping`` -- update_step.f90 / Particle.f90), plus
+``step()`` for one whole pass of the MPM3D.f90 time loop.
+
+Errors raise :class:`MpmError` carrying the C status code; there is no CPU
+fallback: if the compiled library is missing, importing the binding fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_PKG)
+LIB_PATH = os.path.join(_ROOT, "_build", "libmpm3d_gpu.so")
+
+STATUS = {
+    0: "ok", 1: "bad argument", 2: "out of memory", 3: "parse error", 4: "unsupported",
+    5: "CUDA error", 6: "particle out of grid", 7: "non-finite state", 8: "timeout",
+    9: "bad state", 10: "I/O error",
+}
+
+PRECISION = {"fp64": 0, "strict": 0, "fp64-strict": 0, "native": 1, "fp64-native": 1, "mixed": 2}
+
+FIELDS = {
+    "Xp": 1, "XX": 2, "VXp": 3, "FXp": 4, "XN": 5, "XXN": 6, "VOL": 7, "VOL0": 8, "sig_y": 9,
+    "SM": 10, "Seqv": 11, "SD": 12, "Fp": 13, "epeff": 14, "celsius_t": 15, "DMG": 16, "LT": 17,
+    "ie": 18, "mass": 19, "cp": 20, "q": 21, "failure": 22, "icell": 23, "centericell": 24,
+    "inode": 25, "Mg": 40, "PXg": 41, "FXg": 42, "Cmg": 50, "Cpxg": 51,
+}
+COMPONENTS = {"Xp": 3, "XX": 3, "VXp": 3, "FXp": 3, "XN": 3, "XXN": 3, "SD": 6, "Fp": 9,
+              "PXg": 3, "FXg": 3, "Cpxg": 3}
+GRID_FIELDS = {"Mg", "PXg", "FXg"}
+CELL_FIELDS = {"Cmg", "Cpxg"}
+
+PHASES = {
+    "GridMomentumInitial": 1, "ApplyBoundaryConditions": 2, "ParticleStressUpdate": 3,
+    "GridMomentumUpdate": 4, "IntegrateMomentum": 5, "ParticlePositionUpdate": 6,
+    "GridMomentumMUSL": 7, "calcEnergy": 8, "UpdateDT": 9, "dynamicRelaxationDamping": 10,
+    "BeginStep": 11,
+}
+
+SCALARS = ("istep", "CurrentTime", "DT", "EngKinetic", "EngInternal", "Momentum_x",
+           "Momentum_y", "Momentum_z", "EngKinetic_prev", "nb_gridnode", "nb_particle",
+           "CutOff", "DCell", "active_nodes", "status", "reserved")
+
+FLAG_BITS = {"MUSL": 1 << 0, "USL": 1 << 1, "USF": 1 << 2, "GIMP": 1 << 3, "Bspline": 1 << 4,
+             "SGMP": 1 << 5, "QuasiLoad": 1 << 6, "QuasiDamp": 1 << 7, "SmoothStress": 1 << 8,
+             "UpdateVbyFp": 1 << 9, "TLMPM": 1 << 10, "contact": 1 << 11, "Gravity": 1 << 12,
+             "DR_DAMPING": 1 << 13}
+
+
+class MpmError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code} {STATUS.get(code, '?')}] {message}")
+        self.code = code
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library() -> ctypes.CDLL:
+    """Load libmpm3d_gpu.so (built in-tree by build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libmpm3d_gpu.so is not built ({LIB_PATH}); run build.py first")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i, i64, d, c = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_char_p
+    P = ctypes.POINTER
+    sig = {
+        "mpm_deck_load": (i, [c, P(vp), c, i]),
+        "mpm_deck_parse": (i, [c, P(vp), c, i]),
+        "mpm_deck_free": (None, [vp]),
+        "mpm_deck_nb_particle": (i64, [vp]),
+        "mpm_deck_flags": (ctypes.c_int32, [vp]),
+        "mpm_deck_get_particles": (i, [vp, P(d), P(d), P(d), P(d)]),
+        "mpm_deck_scalars": (i, [vp, P(d)]),
+        "mpm_field_components": (i, [i]),
+        "mpm_create": (i, [vp, i, i, P(vp)]),
+        "mpm_destroy": (None, [vp]),
+        "mpm_last_error": (c, [vp]),
+        "mpm_step_phase": (i, [vp, i]),
+        "mpm_step": (i, [vp]),
+        "mpm_run": (i, [vp, i, i]),
+        "mpm_sync": (i, [vp]),
+        "mpm_get_scalars": (i, [vp, P(d)]),
+        "mpm_download": (i, [vp, i, P(d)]),
+        "mpm_upload": (i, [vp, i, P(d)]),
+        "mpm_nb_particle": (i64, [vp]),
+        "mpm_nb_gridnode": (i64, [vp]),
+        "mpm_nb_cell": (i64, [vp]),
+        "mpm_time_steps": (i, [vp, i, i, P(d)]),
+        "mpm_profile_enable": (i, [vp, i]),
+        "mpm_kernel_count": (i, [vp]),
+        "mpm_kernel_stats": (i, [vp, i, c, i, P(i64), P(d)]),
+        "mpm_algorithmic_bytes": (i, [vp, P(d)]),
+        "mpm_device_bytes": (i64, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Deck:
+    """A parsed .mpm deck (the reference's input format, FFI.f90 / DataIn.f90)."""
+
+    def __init__(self, handle: int):
+        self._h = ctypes.c_void_p(handle)
+
+    @classmethod
+    def load(cls, path: str) -> "Deck":
+        lib = library()
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        st = lib.mpm_deck_load(path.encode(), ctypes.byref(h), err, 256)
+        if st:
+            raise MpmError(st, err.value.decode(errors="replace"))
+        return cls(h.value)
+
+    @classmethod
+    def parse(cls, text: str) -> "Deck":
+        lib = library()
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        st = lib.mpm_deck_parse(text.encode(), ctypes.byref(h), err, 256)
+        if st:
+            raise MpmError(st, err.value.decode(errors="replace"))
+        return cls(h.value)
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    @property
+    def nb_particle(self) -> int:
+        return int(library().mpm_deck_nb_particle(self._h))
+
+    @property
+    def flags(self) -> dict:
+        f = int(library().mpm_deck_flags(self._h))
+        return {k: bool(f & v) for k, v in FLAG_BITS.items()}
+
+    def particles(self) -> dict:
+        n = self.nb_particle
+        m = np.zeros(n)
+        x = np.zeros(3 * n)
+        v = np.zeros(3 * n)
+        f = np.zeros(3 * n)
+        library().mpm_deck_get_particles(self._h, _dptr(m), _dptr(x), _dptr(v), _dptr(f))
+        return {"mass": m, "Xp": x.reshape(3, n), "VXp": v.reshape(3, n), "FXp": f.reshape(3, n)}
+
+    def scalars(self) -> dict:
+        o = np.zeros(16)
+        library().mpm_deck_scalars(self._h, _dptr(o))
+        names = ("spx0", "spx1", "spy0", "spy1", "spz0", "spz1", "DCell", "CutOff", "DTScale",
+                 "EndTime", "OutTime", "ReportTime", "QuasiLoadTime", "DampFactor", "bq1", "bq2")
+        return dict(zip(names, o.tolist()))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            library().mpm_deck_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MpmStep:
+    """One device context: the explicit step of one scene on one GPU."""
+
+    def __init__(self, deck: Deck, precision: str = "fp64", device: int = -1):
+        lib = library()
+        h = ctypes.c_void_p()
+        st = lib.mpm_create(deck.handle, PRECISION[precision], device, ctypes.byref(h))
+        if st:
+            raise MpmError(st, lib.mpm_last_error(None).decode(errors="replace"))
+        self._h = h
+        self.precision = precision
+        self.nb_particle = int(lib.mpm_nb_particle(h))
+        self.nb_gridnode = int(lib.mpm_nb_gridnode(h))
+        self.nb_cell = int(lib.mpm_nb_cell(h))
+
+    # -- plumbing
+    def _check(self, st: int) -> None:
+        if st:
+            raise MpmError(st, library().mpm_last_error(self._h).decode(errors="replace"))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            library().mpm_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the reference's subroutines (one phase each)
+    def phase(self, name: str) -> None:
+        self._check(library().mpm_step_phase(self._h, PHASES[name]))
+
+    def BeginStep(self):
+        self.phase("BeginStep")
+
+    def GridMomentumInitial(self):
+        self.phase("GridMomentumInitial")
+
+    def ApplyBoundaryConditions(self):
+        self.phase("ApplyBoundaryConditions")
+
+    def ParticleStressUpdate(self):
+        self.phase("ParticleStressUpdate")
+
+    def GridMomentumUpdate(self):
+        self.phase("GridMomentumUpdate")
+
+    def IntegrateMomentum(self):
+        self.phase("IntegrateMomentum")
+
+    def ParticlePositionUpdate(self):
+        self.phase("ParticlePositionUpdate")
+
+    def GridMomentumMUSL(self):
+        self.phase("GridMomentumMUSL")
+
+    def calcEnergy(self):
+        self.phase("calcEnergy")
+
+    def UpdateDT(self):
+        self.phase("UpdateDT")
+
+    def dynamicRelaxationDamping(self):
+        self.phase("dynamicRelaxationDamping")
+
+    # -- whole steps
+    def step(self) -> None:
+        self._check(library().mpm_step(self._h))
+
+    def run(self, nsteps: int, graph: bool = True) -> None:
+        self._check(library().mpm_run(self._h, int(nsteps), int(bool(graph))))
+
+    def sync(self) -> None:
+        self._check(library().mpm_sync(self._h))
+
+    def time_steps(self, nsteps: int, graph: bool = True) -> float:
+        ms = ctypes.c_double()
+        self._check(library().mpm_time_steps(self._h, int(nsteps), int(bool(graph)), ctypes.byref(ms)))
+        return ms.value
+
+    # -- data
+    def scalars(self) -> dict:
+        o = np.zeros(16)
+        self._check(library().mpm_get_scalars(self._h, _dptr(o)))
+        return dict(zip(SCALARS, o.tolist()))
+
+    def download(self, field: str) -> np.ndarray:
+        ncomp = COMPONENTS.get(field, 1)
+        if field in GRID_FIELDS:
+            n = self.nb_gridnode
+        elif field in CELL_FIELDS:
+            n = self.nb_cell
+        else:
+            n = self.nb_particle
+        out = np.zeros(ncomp * n)
+        self._check(library().mpm_download(self._h, FIELDS[field], _dptr(out)))
+        return out.reshape(ncomp, n) if ncomp > 1 else out
+
+    def upload(self, field: str, values: np.ndarray) -> None:
+        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        self._check(library().mpm_upload(self._h, FIELDS[field], _dptr(a)))
+
+    # -- measurement
+    def profile(self, on: bool = True) -> None:
+        self._check(library().mpm_profile_enable(self._h, int(bool(on))))
+
+    def kernel_stats(self) -> list:
+        lib = library()
+        out = []
+        for k in range(lib.mpm_kernel_count(self._h)):
+            name = ctypes.create_string_buffer(64)
+            n = ctypes.c_int64()
+            ms = ctypes.c_double()
+            self._check(lib.mpm_kernel_stats(self._h, k, name, 64, ctypes.byref(n), ctypes.byref(ms)))
+            out.append({"kernel": name.value.decode(), "launches": n.value, "total_ms": ms.value})
+        return out
+
+    def algorithmic_bytes(self) -> float:
+        b = ctypes.c_double()
+        self._check(library().mpm_algorithmic_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def device_bytes(self) -> int:
+        return int(library().mpm_device_bytes(self._h))
+
+
+__all__ = ["Deck", "MpmStep", "MpmError", "library", "FIELDS", "PHASES", "PRECISION", "LIB_PATH"]

@@ -1,0 +1,301 @@
+"""Writers of .mpm decks for the benchmark workloads and the parity cases.
+
+Every deck is plain reference syntax (DataIn.f90 keyword table), so the
+reference itself could read it. Numbers are written as float32-representable
+decimals ('%.9g' of a float32), because the reference reads every real as a
+32-bit REAL (FFI.f90:110); the deck therefore states exactly the values both
+sides compute with. Random inputs use numpy's PCG64 generator with a fixed
+seed.
+
+Workloads (sizes as in the benchmark configurations):
+  taylor_bar   -- copper cylinder R 3.2 mm, L 32.4 mm, 0.4 mm spacing, 8 ppc,
+                  190 m/s onto a rigid wall; Johnson-Cook with failure ('jcf',
+                  type 7) + linear EOS; USF, linear shape functions.
+  soil_slope   -- 20 m high 45 degree slope, 0.1 m spacing jittered +-1%,
+                  Drucker-Prager (c 10 kPa, phi 20 deg), gravity; GIMP, USF.
+  dam_break    -- 4 x 2 x 2 m water column in a 10 x 2 x 4 m tank, 1 cm
+                  spacing; null material + weakly compressible EOS; B-spline,
+                  MUSL.
+  soft_beam    -- neo-Hookean cantilever; SGMP, MUSL (serving scenes).
+  cook_membrane-- the tapered Cook panel under a distributed tip shear.
+"""
+from __future__ import annotations
+
+import math
+from typing import Iterable, Optional
+
+import numpy as np
+
+
+def f32s(x: float) -> str:
+    """Decimal that reads back to the same float32 (tokens stay <= 20 chars)."""
+    return "%.9g" % float(np.float32(x))
+
+
+def _points_block(ids_start: int, mat: int, mass: np.ndarray, xyz: np.ndarray) -> str:
+    n = xyz.shape[0]
+    m = np.asarray(mass, dtype=np.float32)
+    p = xyz.astype(np.float32)
+    if m.ndim == 0:
+        m = np.full(n, m, dtype=np.float32)
+    lines = ["%d %d %.9g %.9g %.9g %.9g" % (ids_start + i, mat, m[i], p[i, 0], p[i, 1], p[i, 2])
+             for i in range(n)]
+    return "\n".join(lines)
+
+
+class DeckWriter:
+    """Accumulates the sections of a deck in the reference's keyword order."""
+
+    def __init__(self, title: str):
+        self.title = title
+        self.head: list[str] = []
+        self.bodies: list[str] = []
+        self.tail: list[str] = []
+        self.nbmp = 0
+        self.nbbo = 0
+
+    def kw(self, line: str) -> None:
+        self.head.append(line)
+
+    def points(self, mat: int, mass, xyz: np.ndarray, com: int = 1) -> tuple[int, int]:
+        n = xyz.shape[0]
+        first = self.nbmp + 1
+        self.bodies.append(f"part poin {com} {n}\n" + _points_block(first, mat, np.asarray(mass), xyz))
+        self.nbmp += n
+        self.nbbo += 1
+        return first, first + n - 1
+
+    def block(self, mat: int, density: float, dp: float, origin, counts, com: int = 1) -> tuple[int, int]:
+        nx, ny, nz = counts
+        first = self.nbmp + 1
+        self.bodies.append(
+            f"part bloc {com} {mat} {f32s(density)} {f32s(dp)} {f32s(origin[0])} {f32s(origin[1])} "
+            f"{f32s(origin[2])} {nx} {ny} {nz}")
+        self.nbmp += nx * ny * nz
+        self.nbbo += 1
+        return first, first + nx * ny * nz - 1
+
+    def text(self) -> str:
+        out = [f"mpm3d *** {self.title}", "nbco 1", f"nbbo {self.nbbo}", f"nbmp {self.nbmp}"]
+        out += self.head
+        out += self.bodies
+        out += self.tail
+        out.append("endi")
+        return "\n".join(out) + "\n"
+
+
+def _grid_lines(span, dcell) -> list[str]:
+    return [f"spx {f32s(span[0][0])} {f32s(span[0][1])}",
+            f"spy {f32s(span[1][0])} {f32s(span[1][1])}",
+            f"spz {f32s(span[2][0])} {f32s(span[2][1])}",
+            f"dcel {f32s(dcell)}"]
+
+
+def taylor_bar(dp: float = 4e-4, radius: float = 3.2e-3, length: float = 32.4e-3,
+               velocity: float = -190.0, dtscale: float = 0.1, epf: float = 100.0) -> str:
+    """Copper Taylor bar (8 particles per cell: cell = 2 dp)."""
+    h = 2 * dp
+    n = int(math.ceil(radius / dp))
+    ij = np.arange(-n, n)
+    cx = (ij + 0.5) * dp
+    X, Y = np.meshgrid(cx, cx, indexing="xy")
+    inside = X ** 2 + Y ** 2 < radius ** 2
+    xs, ys = X[inside], Y[inside]
+    nl = int(round(length / dp))
+    pts = []
+    for k in range(nl):
+        z = (k + 0.5) * dp
+        pts.append(np.stack([xs, ys, np.full(xs.shape, z)], axis=1))
+    xyz = np.concatenate(pts, axis=0)
+    rho, E, nu = 8930.0, 1.17e11, 0.35
+    K = E / (3 * (1 - 2 * nu))
+    half = 16 * h
+    w = DeckWriter("taylor bar, Johnson-Cook + linear EOS, USF")
+    w.kw("nmat 1")
+    w.head += _grid_lines(((-half, half), (-half, half), (0.0, 42 * h)), h)
+    w.kw(f"dtsc {f32s(dtscale)}")
+    w.kw("endt 1.0")
+    w.kw("usf on")
+    w.kw("fixe 0 0 0 0 1 0")
+    w.kw("mate")
+    # num jcf density E nu A B n C m roomt melt specheat epso epf
+    w.kw(f"1 jcf {f32s(rho)} {f32s(E)} {f32s(nu)} 9e7 2.92e8 0.31 0.025 1.09 293 1356 383 1 {f32s(epf)}")
+    w.kw(f"seos 1 1 0 {f32s(K)} 0 0 0 0 0 0")
+    w.points(1, rho * dp ** 3, xyz)
+    w.tail += ["velo", f"body 1 0 0 {f32s(velocity)}", "endv"]
+    return w.text()
+
+
+def dp_parameters(cohesion: float, phi_deg: float) -> tuple[float, float, float, float]:
+    """Drucker-Prager (q_phi, k_phi, q_psi, tension) matched to Mohr-Coulomb in
+    plane strain: q = 3 tan(phi)/sqrt(9 + 12 tan^2 phi), k = 3c/sqrt(...),
+    associated dilatancy off (q_psi = 0), tension cut-off at the cone apex k/q."""
+    t = math.tan(math.radians(phi_deg))
+    r = math.sqrt(9 + 12 * t * t)
+    q = 3 * t / r
+    k = 3 * cohesion / r
+    tens = k / q if q > 0 else 0.0
+    return q, k, 0.0, tens
+
+
+def soil_slope(dp: float = 0.1, width: float = 3.0, height: float = 20.0, crest: float = 10.0,
+               jitter: float = 0.01, seed: int = 0x5EED, dtscale: float = 0.3,
+               cohesion: float = 1e4, phi: float = 20.0) -> str:
+    """45 degree slope on a rigid base, GIMP (cell = 2 dp), gravity along -z."""
+    h = 2 * dp
+    nx = int(round((crest + height) / dp))
+    nz = int(round(height / dp))
+    ny = int(round(width / dp))
+    xi = (np.arange(nx) + 0.5) * dp
+    zk = (np.arange(nz) + 0.5) * dp
+    X, Z = np.meshgrid(xi, zk, indexing="xy")
+    top = np.where(X <= crest, height, height - (X - crest))
+    keep = Z < top
+    xs, zs = X[keep], Z[keep]
+    pts = []
+    for j in range(ny):
+        y = (j + 0.5) * dp
+        pts.append(np.stack([xs, np.full(xs.shape, y), zs], axis=1))
+    xyz = np.concatenate(pts, axis=0)
+    rng = np.random.default_rng(seed)
+    xyz = xyz + rng.uniform(-jitter * dp, jitter * dp, size=xyz.shape)
+    rho, E, nu = 2000.0, 5e7, 0.3
+    q, k, qpsi, tens = dp_parameters(cohesion, phi)
+    w = DeckWriter("soil slope, Drucker-Prager, GIMP, USF")
+    w.kw("nmat 1")
+    lx = crest + height + 0.3 * height
+    w.head += _grid_lines(((0.0, lx), (0.0, width), (0.0, height + 0.2 * height)), h)
+    w.kw(f"dtsc {f32s(dtscale)}")
+    w.kw("endt 100.0")
+    w.kw("usf on")
+    w.kw("gimp")
+    w.kw("fixe 2 0 2 2 1 0")
+    w.kw("mate")
+    w.kw(f"1 dpm {f32s(rho)} {f32s(E)} {f32s(nu)} {f32s(q)} {f32s(k)} {f32s(qpsi)} {f32s(tens)}")
+    w.points(1, rho * dp ** 3, xyz)
+    w.tail += ["load", "grav 1 0 0 -9.81", "endl"]
+    return w.text()
+
+
+def dam_break(dp: float = 0.01, h: float = 0.02, water=(4.0, 2.0, 2.0), tank=(10.0, 2.0, 4.0),
+              dtscale: float = 0.5, bulk: float = 2.2e6, viscosity: float = 1e-3) -> str:
+    """Water column in a tank with slip walls; quadratic B-spline, MUSL. The
+    grid has one extra cell outside each wall so that the wall is the second,
+    fixed node layer."""
+    rho = 1000.0
+    nx, ny, nz = (int(round(water[i] / dp)) for i in range(3))
+    w = DeckWriter("dam break, null material + weakly compressible EOS, B-spline, MUSL")
+    w.kw("nmat 1")
+    w.head += _grid_lines(((-h, tank[0] + h), (-h, tank[1] + h), (-h, tank[2] + h)), h)
+    w.kw(f"dtsc {f32s(dtscale)}")
+    w.kw("endt 100.0")
+    w.kw("musl on")
+    w.kw("bimp")
+    w.kw("bulk 1.5 0.06")
+    w.kw("fixe 2 2 2 2 2 0")
+    w.kw("mate")
+    w.kw(f"1 null {f32s(rho)} {f32s(bulk)} {f32s(viscosity)}")
+    w.kw(f"seos 1 4 {f32s(math.sqrt(bulk / rho))}")
+    w.block(1, rho, dp, (0.0, 0.0, 0.0), (nx, ny, nz))
+    w.tail += ["load", "grav 1 0 0 -9.81", "endl"]
+    return w.text()
+
+
+def soft_beam(dp: float = 0.25, length: float = 6.0, depth: float = 1.0, thick: float = 1.0,
+              young: float = 1e7, nu: float = 0.3, rho: float = 1000.0, dtscale: float = 0.5,
+              shape: str = "sgmp", scheme: str = "musl", gravity: float = -9.81) -> str:
+    """Cantilever soft beam clamped at x = 0 (neo-Hookean). With SGMP the grid
+    has one extra layer beyond the clamped face (the reference's rule for
+    fixed boundaries under SGMP)."""
+    h = 2 * dp
+    nx, ny, nz = int(round(length / dp)), int(round(thick / dp)), int(round(depth / dp))
+    w = DeckWriter(f"soft beam, neo-Hookean, {shape}, {scheme}")
+    w.kw("nmat 1")
+    pad = h if shape == "sgmp" else 0.0
+    z0 = 2.0
+    w.head += _grid_lines(((-pad, length + 2.0), (0.0, thick), (0.0, z0 + depth + 1.0)), h)
+    w.kw(f"dtsc {f32s(dtscale)}")
+    w.kw("endt 100.0")
+    w.kw(f"{scheme} on")
+    if shape in ("sgmp", "gimp", "bimp"):
+        w.kw(shape)
+    w.kw("fixe 1 0 2 2 0 0")
+    w.kw("mate")
+    w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
+    w.block(1, rho, dp, (0.0, 0.0, z0), (nx, ny, nz))
+    w.tail += ["load", f"grav 1 0 0 {f32s(gravity)}", "endl"]
+    return w.text()
+
+
+def generic_block(material_line: str, eos_line: Optional[str] = None, *, dp: float = 0.5,
+                  counts=(8, 4, 6), shape: Optional[str] = None, scheme: str = "usf",
+                  velocity=(0.0, 0.0, -5.0), gravity: Optional[float] = -9.81, dtscale: float = 0.5,
+                  fixed: str = "0 0 0 0 1 0", rho: float = 1000.0, extra: Iterable[str] = ()) -> str:
+    """Small block test case for any material line ('1 elas 1000 1e7 0.3')."""
+    h = 2 * dp
+    w = DeckWriter("block parity case")
+    w.kw("nmat 1")
+    pad = 2 * h
+    lx, ly, lz = (counts[i] * dp for i in range(3))
+    w.head += _grid_lines(((-pad, lx + pad), (-pad, ly + pad), (0.0, lz + 3 * pad)), h)
+    w.kw(f"dtsc {f32s(dtscale)}")
+    w.kw("endt 100.0")
+    w.kw(f"{scheme} on")
+    if shape:
+        w.kw(shape)
+    w.kw(f"fixe {fixed}")
+    for e in extra:
+        w.kw(e)
+    w.kw("mate")
+    w.kw(material_line)
+    if eos_line:
+        w.kw(eos_line)
+    w.block(1, rho, dp, (0.0, 0.0, h), counts)
+    w.tail += ["velo", "body 1 %s %s %s" % tuple(f32s(v) for v in velocity), "endv"]
+    if gravity is not None:
+        w.tail += ["load", f"grav 1 0 0 {f32s(gravity)}", "endl"]
+    return w.text()
+
+
+def cook_membrane(spacing: float = 0.5, young: float = 70.0, nu: float = 0.499, rho: float = 1.0,
+                  shape: Optional[str] = None, total_load: float = 1.0) -> str:
+    """Cook's tapered panel (corners (0,0), (48,44), (48,60), (0,44), unit
+    thickness, plane strain via roller z faces), clamped at x = 0, loaded by a
+    vertical shear on the x = 48 edge, run quasi-statically (load ramp 'QuLo'
+    and mass damping 'Damp'); neo-Hookean, MUSL."""
+    ds = spacing
+    xs = (np.arange(int(round(48 / ds))) + 0.5) * ds
+    ys = (np.arange(int(round(60 / ds))) + 0.5) * ds
+    pts = []
+    for y in ys:
+        for x in xs:
+            if y >= 44.0 / 48.0 * x and y <= 44.0 + 16.0 / 48.0 * x:
+                pts.append((x, y, 0.0))
+    xyz = np.array(pts)
+    n = xyz.shape[0]
+    area = 48.0 * (44.0 + 16.0) / 2.0
+    mass = rho * area / n
+    w = DeckWriter(f"Cook membrane, neo-Hookean, {shape or 'mpm'}")
+    w.kw("nmat 1")
+    pad = 1.0 if shape == "sgmp" else 0.0
+    w.head += _grid_lines(((0.0 - pad, 50.0), (0.0, 62.0), (-0.5, 0.5)), 1.0)
+    w.kw("fixe 1 0 0 0 2 2")
+    w.kw("dtsc 0.9")
+    w.kw("endt 30")
+    w.kw("musl on")
+    if shape:
+        w.kw(shape)
+    w.kw("QuLo 15")
+    w.kw("Damp 0.3")
+    w.kw("mate")
+    w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
+    w.points(1, mass, xyz)
+    right = np.where(np.isclose(xyz[:, 0], xs[-1]))[0]
+    per = total_load / max(1, len(right) - 1)
+    loads = ["load"]
+    for k, i in enumerate(right):
+        f = per * (0.5 if k in (0, len(right) - 1) else 1.0)
+        loads.append(f"part {i + 1} 0 {f32s(f)} 0")
+    loads.append("endl")
+    w.tail += loads
+    return w.text()

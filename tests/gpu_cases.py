@@ -1,0 +1,36 @@
+"""Parity cases shared by the GPU tests: small decks that the oracle runs in
+seconds, each exercising one shape family / scheme / material path."""
+import sys
+import os
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "mpm3d-f90_gb300"))
+
+from mpm3d_gb300 import decks  # noqa: E402
+
+# name -> (deck text factory, steps)
+CASES = {
+    "taylor_small_usf_jcf_linear": (lambda: decks.taylor_bar(dp=8e-4), 100),
+    "slope_small_usf_dp_gimp": (lambda: decks.soil_slope(dp=0.5, width=2.0), 60),
+    "dam_small_musl_null_bspline": (lambda: decks.dam_break(dp=0.1, h=0.2), 40),
+    "beam_musl_neoh_sgmp": (lambda: decks.soft_beam(), 60),
+    "beam_usl_neoh_linear": (lambda: decks.soft_beam(shape="mpm", scheme="usl"), 60),
+    "cook_musl_neoh_quasistatic": (lambda: decks.cook_membrane(), 60),
+    "block_usf_elastic": (lambda: decks.generic_block("1 elas 1000 1e7 0.3"), 60),
+    "block_musl_pla1_gimp": (lambda: decks.generic_block("1 pla1 1000 1e7 0.3 2e4", shape="gimp",
+                                                         scheme="musl", velocity=(1.0, 0.0, -20.0)), 60),
+    "block_usl_pla2_bspline": (lambda: decks.generic_block("1 pla2 1000 1e7 0.3 2e4 1e5", shape="bimp",
+                                                           scheme="usl", velocity=(0.0, 2.0, -20.0)), 60),
+    "block_usf_john": (lambda: decks.generic_block(
+        "1 john 8930 1.17e11 0.35 9e7 2.92e8 0.31 0.025 1.09 293 1356 383 1", dp=4e-4,
+        velocity=(0.0, 0.0, -150.0), rho=8930.0, dtscale=0.2, gravity=None), 80),
+    "block_musl_sjc_gruneisen": (lambda: decks.generic_block(
+        "1 sjc 8930 1.17e11 0.35 1.57e8 4.25e8 1.0 0.0 1e-3", "seos 1 2 3940 1.49 1.96 0", dp=4e-4,
+        velocity=(0.0, 0.0, -200.0), rho=8930.0, dtscale=0.2, gravity=None, scheme="musl"), 80),
+    "block_usf_sjcf_gruneisen": (lambda: decks.generic_block(
+        "1 sjcf 8930 1.17e11 0.35 9e7 2.92e8 0.31 0.025 1 0.02", "seos 1 2 3940 1.49 1.96 0", dp=4e-4,
+        velocity=(0.0, 0.0, -300.0), rho=8930.0, dtscale=0.2, gravity=None), 80),
+    "block_musl_hiex_jwl": (lambda: decks.generic_block(
+        "1 hiex 1630 6930", "seos 1 3 3.712e11 3.21e9 4.15 0.95 0.3 6.993e9", dp=5e-4,
+        velocity=(0.0, 0.0, 0.0), rho=1630.0, dtscale=0.1, gravity=None, scheme="musl",
+        extra=["deto 0 0 0"]), 60),
+}
