@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 explicit MPM step (one JSON line on stdout).
+
+Workload (default): the 3-D soil slope -- 20 m high, 45 degrees, 0.1 m
+particle spacing jittered by +-1% from a fixed seed (1.2 M particles), grid
+cell 0.2 m, Drucker-Prager (c = 10 kPa, phi = 20 deg), gravity, GIMP shape
+functions, USF. A "step" is one explicit time step of the whole scene.
+
+  value      particle-steps/s of the mixed-precision form, state resident in
+             HBM, CUDA-graph replay, timed with CUDA events on the library's
+             stream (inputs are larger than L2, no flush needed);
+  fp64       the plain FP64 form (bit-identical to the CPU oracle) on the same
+             steps, and the mixed form's error against it;
+  e2e        the same metric through the C ABI from host arrays: context
+             creation (host->device upload of the particle state), the steps
+             with the per-step scalar read-back the host loop needs for its
+             exit test, and the read-back of the particle state;
+  roofline   the dominant kernel's algorithmic bytes / its event-timed duration;
+  cpu_baseline  the CPU oracle (a restatement of the reference step) on a
+             bounded sample of the same workload on this host's cores.
+
+`--impl reference` times the reference's CPU step (the oracle port; the
+Fortran reference cannot be compiled on these machines) with one replica per
+host core.
+
+Multi-GPU: scenes are independent, so N GPUs run N replicas (weak scaling,
+no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mpm3d-f90_gb300"))
+
+WORKLOADS = {
+    # name: (deck factory kwargs, description)
+    "soil_slope": ("soil slope 20 m 45 deg, 0.1 m spacing, GIMP, Drucker-Prager, USF",),
+    "taylor_bar": ("Taylor bar R 3.2 mm L 32.4 mm, 0.4 mm spacing, linear, Johnson-Cook + EOS, USF",),
+    "dam_break": ("dam break 4x2x2 m in 10x2x4 m tank, 1 cm spacing, B-spline, null + EOS 4, MUSL",),
+}
+
+
+def make_deck(workload: str, scale: float = 1.0) -> str:
+    from mpm3d_gb300 import decks
+
+    if workload == "soil_slope":
+        return decks.soil_slope(dp=0.1 * scale, width=3.0)
+    if workload == "taylor_bar":
+        return decks.taylor_bar(dp=4e-4 * scale)
+    if workload == "dam_break":
+        return decks.dam_break(dp=0.01 * scale, h=0.02 * scale)
+    raise SystemExit(f"unknown workload {workload}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def rel_err(a, b) -> float:
+    import numpy as np
+
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    s = float(np.max(np.abs(b))) if b.size else 0.0
+    return float(np.max(np.abs(a - b)) / s) if s > 0 else float(np.max(np.abs(a - b)))
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def dominant_kernel(stats: list, steps: int) -> dict:
+    best = max(stats, key=lambda s: s["total_ms"])
+    return dict(best, avg_ms=best["total_ms"] / max(1, best["launches"]))
+
+
+def kernel_bytes(kernel: str, np_: int, nn_active: float, K: int, bulk: int, real: int) -> float:
+    """Algorithmic bytes of one launch of a kernel: each particle / node field it
+    must touch, read once and written once (no re-reads, no scratch)."""
+    if kernel == "stress_update":
+        # read: snode + dndx/y/z per slot, node vg + mg per active node, and the
+        # particle state; write: the updated state (+ Xp when not USF)
+        per_p = K * (4 + 3 * real) + bulk * (1 + 1 + 1 + 1 + 1 + 1 + 6 + 1 + 1) + 8 * 2 + 1 + 2
+        per_p += bulk * (1 + 1 + 1 + 6 + 1 + 1 + 1 + 1) + 8 + 1
+        return per_p * np_ + nn_active * 32
+    if kernel == "p2g_force_integrate":
+        per_p = K * (4 + 4 * real) + 8 * 3 + 8 * 3 + bulk * 4  # pairs, shape, fext, sdiag, sd + vol
+        return per_p * np_ + nn_active * (8 * 3 * 2 + 8 + 8 * 3 + 1)
+    if kernel == "locate":
+        return np_ * (24 + 8 * 4 + K * (4 + 4 * real) + K * 8)
+    if kernel == "g2p_position":
+        return np_ * (K * (4 + real) + 24 * 4) + nn_active * (8 + 48)
+    if kernel == "p2g_mass":
+        return np_ * (K * (4 + real) + 8 + 24) + nn_active * 32
+    if kernel == "pair_sort":
+        return np_ * K * 8 * 2 * 3
+    return np_ * 100.0
+
+
+def run_ours(args) -> dict:
+    import numpy as np
+    import mpm3d_gb300 as m
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # replicas only: barrier + max of times
+
+        dist.init_process_group("gloo", init_method="env://")
+    text = make_deck(args.workload, args.scale)
+    with tempfile.NamedTemporaryFile("w", suffix=".mpm", delete=False) as f:
+        f.write(text)
+        deck_path = f.name
+    deck = m.Deck.load(deck_path)
+    os.unlink(deck_path)
+    npart = deck.nb_particle
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if not dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    states = {}
+    for form in ("fp64", "mixed"):
+        s = m.MpmStep(deck, precision=form, device=local)
+        s.run(args.warmup, graph=True)
+        s.sync()
+        barrier()
+        sampler = ClockSampler(local) if form == "mixed" else None
+        if sampler:
+            sampler.start()
+        ms = s.time_steps(args.steps, graph=True)
+        s.sync()
+        clocks = sampler.stop() if sampler else None
+        ms = max_over_ranks(ms)
+        barrier()
+        results[form] = {"ms": ms, "clocks": clocks, "device_bytes": s.device_bytes(),
+                         "alg_bytes_step": s.algorithmic_bytes(), "scalars": s.scalars()}
+        states[form] = {f: s.download(f) for f in ("PXg", "Mg", "SM", "SD", "Xp", "VXp")}
+        # per-kernel timing over a second, profiled run of the same length
+        s.profile(True)
+        s.time_steps(args.steps, graph=True)
+        results[form]["kernels"] = s.kernel_stats()
+        s.profile(False)
+        s.close()
+    err = {"nodal_momentum_rel": rel_err(states["mixed"]["PXg"], states["fp64"]["PXg"]),
+           "particle_stress_rel": max(rel_err(states["mixed"]["SM"], states["fp64"]["SM"]),
+                                      rel_err(states["mixed"]["SD"], states["fp64"]["SD"])),
+           "position_rel": rel_err(states["mixed"]["Xp"], states["fp64"]["Xp"])}
+
+    # end to end through the C ABI from host buffers
+    t0 = time.perf_counter()
+    e2 = m.MpmStep(deck, precision="mixed", device=local)
+    h2d = npart * 8 * (1 + 3 + 3 + 3)  # mass, Xp, VXp, FXp uploaded
+    for _ in range(args.steps):
+        e2.step()
+        e2.scalars()  # the host loop's exit test needs CurrentTime every step
+    out = [e2.download(f) for f in ("Xp", "VXp", "SM", "SD")]
+    t_e2e = time.perf_counter() - t0
+    d2h = args.steps * 16 * 8 + sum(o.nbytes for o in out)
+    e2.close()
+    t_e2e = max_over_ranks(t_e2e)
+
+    mixed, fp64 = results["mixed"], results["fp64"]
+    value = npart * world * args.steps / (mixed["ms"] / 1e3)
+    fp64_value = npart * world * args.steps / (fp64["ms"] / 1e3)
+    peaks = measured_peaks()
+    dom = dominant_kernel(mixed["kernels"], args.steps)
+    nn_active = mixed["scalars"]["active_nodes"]
+    K = 27
+    kb = kernel_bytes(dom["kernel"], npart, nn_active, K, 4, 4)
+    achieved = kb / (dom["avg_ms"] / 1e3) / 1e9
+    line = {
+        "metric": "particle-steps/s (mixed precision vs plain FP64 GPU, stated error)",
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": mixed["ms"] / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 particle / f64 grid (mixed)",
+        "data": "synthetic (seeded deck generator)",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
+                   "grid_nodes": int(mixed["scalars"]["nb_gridnode"]), "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (no flush)", "graph": True},
+        "fp64": {"value": fp64_value, "ms_per_step": fp64["ms"] / args.steps, "dtype": "f64",
+                 "parity": "bit-identical to the CPU oracle (tests/test_gpu_parity.py)",
+                 "speedup_mixed_over_fp64": value / fp64_value},
+        "error_vs_fp64": err,
+        "e2e": {"value": npart * world * args.steps / t_e2e, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
+        "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                     "traffic": None, "avg_launch_ms": dom["avg_ms"]},
+        "step_alg_gbs": mixed["alg_bytes_step"] / (mixed["ms"] / args.steps / 1e3) / 1e9,
+        "kernels_mixed": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in mixed["kernels"] if k["launches"]},
+        "kernels_fp64": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in fp64["kernels"] if k["launches"]},
+        "gpu_launches": sum(k["launches"] for k in mixed["kernels"]),
+        "clocks": mixed["clocks"],
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(text, args.cpu_steps, npart)
+    if dist:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def cpu_baseline(text: str, steps: int, npart: int, cores: int = 1) -> dict:
+    """The oracle (a port of the reference step) on this host, bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    o = oracle.Oracle(deck_text=text)
+    o.run(1)
+    t0 = time.perf_counter()
+    o.run(steps)
+    t = time.perf_counter() - t0
+    o.close()
+    return {"value": npart * steps / t, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} steps of the full workload ({npart} particles) after 1 untimed step"}
+
+
+def _replica(args_tuple):
+    text, warm, steps = args_tuple
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    o = oracle.Oracle(deck_text=text)
+    o.run(warm)
+    t0 = time.perf_counter()
+    o.run(steps)
+    return time.perf_counter() - t0, o.nb_particle
+
+
+def run_reference(args) -> dict:
+    """Reference arm: the CPU step (oracle port), one replica per host core."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+
+    text = make_deck(args.workload, args.scale)
+    cores = args.ref_cores or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_replica, [(text, args.ref_warmup, args.ref_steps)] * cores)
+    t = max(r[0] for r in res)
+    npart = res[0][1]
+    value = npart * cores * args.ref_steps / t
+    return {
+        "impl": "reference",
+        "metric": "particle-steps/s (mixed precision vs plain FP64 GPU, stated error)",
+        "value": value, "unit": "particle-steps/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.ref_steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded deck generator)",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
+                   "parallelism": f"{cores} CPU replicas"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.ref_steps} steps per replica after {args.ref_warmup} warm-up steps, "
+                                   f"{cores} independent replicas of the full workload"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="soil_slope", choices=sorted(WORKLOADS))
+    ap.add_argument("--scale", type=float, default=1.0, help="particle spacing multiplier (1 = full size)")
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-steps", type=int, default=2)
+    ap.add_argument("--ref-warmup", type=int, default=1)
+    ap.add_argument("--ref-cores", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

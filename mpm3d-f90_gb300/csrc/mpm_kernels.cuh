@@ -1217,14 +1217,27 @@ __global__ void k_reduce(St<P> s, Geometry g, int mode) {
     last = (done == gridDim.x - 1);
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
+  // the last block combines the block partials: thread t takes blocks t,
+  // t + blockDim, ... in order, then the same fixed tree as above
   double tot[kRedVals] = {0, 0, 0, 0, 0, 0};
-  for (unsigned b = 0; b < gridDim.x; ++b) {
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
     for (int i = 0; i < 5; ++i) tot[i] = tot[i] + s.red_part[(long long)i * gridDim.x + b];
     double mv = s.red_part[5LL * gridDim.x + b];
     if (tot[5] < mv) tot[5] = mv;
   }
+  for (int i = 0; i < kRedVals; ++i) sh[i][threadIdx.x] = tot[i];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      for (int i = 0; i < 5; ++i) sh[i][threadIdx.x] = sh[i][threadIdx.x] + sh[i][threadIdx.x + w];
+      if (sh[5][threadIdx.x + w] > sh[5][threadIdx.x]) sh[5][threadIdx.x] = sh[5][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i < kRedVals; ++i) tot[i] = sh[i][0];
   DevScalars* sc = s.sc;
   if (mode & 1) {
     sc->ke_prev = sc->ke;

@@ -257,12 +257,18 @@ def generic_block(material_line: str, eos_line: Optional[str] = None, *, dp: flo
     return w.text()
 
 
-def cook_membrane(spacing: float = 0.5, young: float = 70.0, nu: float = 0.499, rho: float = 1.0,
-                  shape: Optional[str] = None, total_load: float = 1.0) -> str:
+def cook_membrane(variant: str = "mpm", spacing: float = 0.5, young: float = 70.0, nu: float = 0.499,
+                  rho: float = 1.0, total_load: float = 1.0) -> str:
     """Cook's tapered panel (corners (0,0), (48,44), (48,60), (0,44), unit
-    thickness, plane strain via roller z faces), clamped at x = 0, loaded by a
-    vertical shear on the x = 48 edge, run quasi-statically (load ramp 'QuLo'
-    and mass damping 'Damp'); neo-Hookean, MUSL."""
+    thickness, plane strain through roller z faces), clamped at x = 0 and
+    loaded by a vertical shear on the x = 48 edge, run quasi-statically (load
+    ramp 'QuLo 15', mass damping 'Damp 0.3'); neo-Hookean, MUSL.
+
+    variant: 'mpm' (linear), 'gimp', 'bimp' (B-spline) or 'sgmp'. Particles
+    sit on a regular lattice clipped to the panel, rows by increasing y; the
+    particle mass and the edge loads are written with six decimals (mass =
+    area/n; the edge particles carry 1/(m-1) of the load, the two corner
+    particles half of that)."""
     ds = spacing
     xs = (np.arange(int(round(48 / ds))) + 0.5) * ds
     ys = (np.arange(int(round(60 / ds))) + 0.5) * ds
@@ -274,28 +280,40 @@ def cook_membrane(spacing: float = 0.5, young: float = 70.0, nu: float = 0.499, 
     xyz = np.array(pts)
     n = xyz.shape[0]
     area = 48.0 * (44.0 + 16.0) / 2.0
-    mass = rho * area / n
-    w = DeckWriter(f"Cook membrane, neo-Hookean, {shape or 'mpm'}")
+    mass = "%.6f" % (rho * area / n)
+    spans = {"mpm": ((0, 50), (0, 62), (-0.5, 0.5)), "gimp": ((-1, 50), (-1, 62), (-1, 1)),
+             "bimp": ((-1, 50), (-1, 62), (-1, 1)), "sgmp": ((-1, 50), (-1, 62), (-0.5, 0.5))}[variant]
+    w = DeckWriter(f"Cook membrane, neo-Hookean, {variant}")
     w.kw("nmat 1")
-    pad = 1.0 if shape == "sgmp" else 0.0
-    w.head += _grid_lines(((0.0 - pad, 50.0), (0.0, 62.0), (-0.5, 0.5)), 1.0)
+    w.head += _grid_lines(spans, 1.0)
     w.kw("fixe 1 0 0 0 2 2")
     w.kw("dtsc 0.9")
     w.kw("endt 30")
     w.kw("musl on")
-    if shape:
-        w.kw(shape)
+    if variant != "mpm":
+        w.kw(variant)
+    w.kw("smoo")
     w.kw("QuLo 15")
     w.kw("Damp 0.3")
+    w.kw(f"curv disy {n}")
     w.kw("mate")
     w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
-    w.points(1, mass, xyz)
+    first = w.nbmp + 1
+    lines = ["%d 1 %s %.9g %.9g %.9g" % (first + i, mass, xyz[i, 0], xyz[i, 1], xyz[i, 2]) for i in range(n)]
+    w.bodies.append(f"part poin 1 {n}\n" + "\n".join(lines))
+    w.nbmp += n
+    w.nbbo += 1
     right = np.where(np.isclose(xyz[:, 0], xs[-1]))[0]
     per = total_load / max(1, len(right) - 1)
     loads = ["load"]
     for k, i in enumerate(right):
         f = per * (0.5 if k in (0, len(right) - 1) else 1.0)
-        loads.append(f"part {i + 1} 0 {f32s(f)} 0")
+        loads.append("part %d 0 %.6f 0" % (i + 1, f))
     loads.append("endl")
     w.tail += loads
     return w.text()
+
+
+# Published tip vertical displacement (m) of the Cook membrane with 5776
+# particles (VolumetricLockingEx/ExamplesResults.pdf, Table 1), by variant.
+COOK_TIP_PUBLISHED = {"mpm": 0.2489, "gimp": 0.2512, "bimp": 0.2620, "sgmp": 0.2678}
