@@ -1,0 +1,67 @@
+"""End-to-end pins on the GPU (marked gpu).
+
+1. The four Cook-membrane decks (linear, GIMP, B-spline, SGMP; 5776
+   particles), regenerated exactly, run in FP64 to the reference's quasi-static
+   exit test: the tip vertical displacement must round to the published value
+   (VolumetricLockingEx/ExamplesResults.pdf, Table 1).
+2. The spec case: the full Taylor bar (16 k particles, Johnson-Cook with
+   failure + linear EOS, USF) for 1000 steps. The strict FP64 form must be bit
+   identical to the oracle with the same libm; against the oracle on glibc the
+   nodal momentum and particle stress must agree to 1e-10 relative, or to the
+   spread the libm choice causes on the CPU alone if that is larger.
+"""
+import numpy as np
+import pytest
+
+
+def _tip(step_obj, x0):
+    return step_obj.download("Xp")[1, -1] - x0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["mpm", "gimp", "bimp", "sgmp"])
+def test_cook_membrane_published_tip_displacement(gpu_mod, variant):
+    from mpm3d_gb300 import decks
+
+    deck = gpu_mod.Deck.parse(decks.cook_membrane(variant))
+    s = gpu_mod.MpmStep(deck, precision="fp64", device=0)
+    x0 = s.download("Xp")[1, -1]
+    n = 0
+    while True:
+        s.step()
+        n += 1
+        sc = s.scalars()
+        if sc["CurrentTime"] > 30 and sc["EngKinetic"] / (sc["EngKinetic"] + sc["EngInternal"]) < 0.005 \
+                and sc["CurrentTime"] > 100:
+            break
+        assert n < 20000
+    tip = _tip(s, x0)
+    assert round(tip, 4) == decks.COOK_TIP_PUBLISHED[variant], (variant, tip, n)
+
+
+def _rel(a, b):
+    s = float(np.max(np.abs(b)))
+    return float(np.max(np.abs(a - b)) / s) if s > 0 else float(np.max(np.abs(a - b)))
+
+
+@pytest.mark.gpu
+def test_taylor_bar_1000_steps_north_star(gpu_mod, oracle_mod):
+    from mpm3d_gb300 import decks
+
+    text = decks.taylor_bar()
+    deck = gpu_mod.Deck.parse(text)
+    g = gpu_mod.MpmStep(deck, precision="fp64", device=0)
+    g.run(1000, graph=True)
+    g.sync()
+    op = oracle_mod.Oracle(deck_text=text, libm="project")
+    op.run(1000)
+    for f in ("PXg", "Mg", "FXg", "SM", "SD", "Xp", "VXp", "epeff", "celsius_t", "ie"):
+        assert np.array_equal(g.download(f), op.download(f)), f
+    assert float(np.max(op.download("epeff"))) > 0.05  # the bar has yielded
+    og = oracle_mod.Oracle(deck_text=text, libm="system")
+    og.run(1000)
+    for f in ("PXg", "SM", "SD"):
+        spread = _rel(op.download(f), og.download(f))
+        r = _rel(g.download(f), og.download(f))
+        print(f"taylor 1000 steps {f}: GPU vs glibc oracle {r:.2e}, libm spread {spread:.2e}")
+        assert r <= max(1e-10, 2 * spread), (f, r, spread)
