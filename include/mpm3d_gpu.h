@@ -150,6 +150,31 @@ int mpm_algorithmic_bytes(mpm_ctx* ctx, double* bytes_per_step);
 /* Bytes of device memory the context holds. */
 int64_t mpm_device_bytes(const mpm_ctx* ctx);
 
+/* ------------------------------------------------ allocation-free call */
+/* No counterpart in the reference: an extra entry point for hosts that may not
+ * allocate device memory inside a solver call (a Fortran code passing device
+ * arrays it manages itself, a host under a fixed memory pool, or a time loop
+ * that must not allocate mid-run). It is the step's calcEnergy reduction
+ * (Particle.f90:204-230) plus the maximum velocity component UpdateDT needs
+ * (update_step.f90:1852), over caller-owned device arrays:
+ *   vxp  : device, 3*np doubles, component-major (x block, y block, z block)
+ *   mass : device, np doubles;  ie : device, np doubles (internal energy)
+ *   out6 : device, 6 doubles written: kinetic energy, internal energy,
+ *          momentum x, y, z, max |velocity component|
+ *   stream : a cudaStream_t (NULL = default stream); the call is asynchronous.
+ * It allocates nothing: its block partial sums live in a fixed 64 KiB
+ * __device__ array that every GPU loading the library holds until the process
+ * exits. np must be in 1..MPM_NOALLOC_MAX_PARTICLES, else MPM_ERR_ARG. The
+ * first call on a device looks up that array's device address once (with that
+ * device current), so make the first call before any stream capture. All
+ * calls share the array: calls that overlap on the GPU (different streams or
+ * threads at the same time) race and must be serialised by the caller.
+ * It uses the block tree and combine order of the context path's calcEnergy
+ * (mpm_step_phase MPM_PHASE_CALC_ENERGY) on the same arrays. */
+#define MPM_NOALLOC_MAX_PARTICLES (1LL << 27)
+int mpm_energy_reduce_noalloc(const double* vxp, const double* mass, const double* ie, int64_t np,
+                              double* out6, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

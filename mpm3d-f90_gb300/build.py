@@ -71,6 +71,7 @@ def build_library(force: bool = False) -> str:
         ("mpm_fp64.cu", ["--fmad=false"]),
         ("mpm_mixed.cu", []),
         ("mpm_gpu.cu", []),
+        ("mpm_noalloc.cu", ["--fmad=false"]),
     ]
     jobs = []
     objs = []

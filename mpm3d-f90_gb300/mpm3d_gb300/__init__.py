@@ -106,6 +106,7 @@ def library() -> ctypes.CDLL:
         "mpm_kernel_stats": (i, [vp, i, c, i, P(i64), P(d)]),
         "mpm_algorithmic_bytes": (i, [vp, P(d)]),
         "mpm_device_bytes": (i64, [vp]),
+        "mpm_energy_reduce_noalloc": (i, [vp, vp, vp, i64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
