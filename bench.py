@@ -222,17 +222,20 @@ def run_ours(args) -> dict:
            "position_rel": rel_err(states["mixed"]["Xp"], states["fp64"]["Xp"])}
 
     # end to end through the C ABI from host buffers
+    if args.no_e2e:
+        t_e2e, h2d, d2h = float("nan"), 0, 0
     t0 = time.perf_counter()
-    e2 = m.MpmStep(deck, precision="mixed", device=local)
-    h2d = npart * 8 * (1 + 3 + 3 + 3)  # mass, Xp, VXp, FXp uploaded
-    for _ in range(args.steps):
-        e2.step()
-        e2.scalars()  # the host loop's exit test needs CurrentTime every step
-    out = [e2.download(f) for f in ("Xp", "VXp", "SM", "SD")]
-    t_e2e = time.perf_counter() - t0
-    d2h = args.steps * 16 * 8 + sum(o.nbytes for o in out)
-    e2.close()
-    t_e2e = max_over_ranks(t_e2e)
+    if not args.no_e2e:
+        e2 = m.MpmStep(deck, precision="mixed", device=local)
+        h2d = npart * 8 * (1 + 3 + 3 + 3)  # mass, Xp, VXp, FXp uploaded
+        for _ in range(args.steps):
+            e2.step()
+            e2.scalars()  # the host loop's exit test needs CurrentTime every step
+        out = [e2.download(f) for f in ("Xp", "VXp", "SM", "SD")]
+        t_e2e = time.perf_counter() - t0
+        d2h = args.steps * 16 * 8 + sum(o.nbytes for o in out)
+        e2.close()
+        t_e2e = max_over_ranks(t_e2e)
 
     mixed, fp64 = results["mixed"], results["fp64"]
     value = npart * world * args.steps / (mixed["ms"] / 1e3)
@@ -349,6 +352,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="particle spacing multiplier (1 = full size)")
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ref-steps", type=int, default=2)
     ap.add_argument("--ref-warmup", type=int, default=1)
     ap.add_argument("--ref-cores", type=int, default=0)

@@ -30,6 +30,28 @@ static __global__ void k_begin_step(DevScalars* sc) {
   sc->active_nodes = 0;
 }
 
+// cpGIMP 1-D weight and its derivative in units of the cell (NShape_GIMP,
+// Grid.f90:577-591): particle half-width h/4.
+template <class R>
+__device__ __forceinline__ void gimp_1d(R rr, R& sh, R& dn) {
+  R a = rr < (R)0 ? -rr : rr;
+  R sg = copysign((R)1.0, rr);
+  if (a < (R)0.25) {
+    sh = ((R)7 - (R)16 * a * a) * (R)0.125;
+    dn = -((R)4 * rr);
+  } else if (a < (R)0.75) {
+    sh = (R)1 - a;
+    dn = -sg;
+  } else if (a < (R)1.25) {
+    R t = ((R)5 - (R)4 * a) * (R)0.25;
+    sh = t * t;
+    dn = (R)2 * rr - sg * (R)2.5;
+  } else {
+    sh = (R)0.0;
+    dn = (R)0.0;
+  }
+}
+
 // ----------------------------------------------------------------- locate
 // ParticleInitial (update_step.f90:408-453) plus the shape functions of the
 // step (NShape / FindInflNode+NShape_GIMP / BFindInflNode+NShape_Bspline /
@@ -115,7 +137,6 @@ __global__ void k_locate(St<P> s, Geometry g, int nkeys) {
       }
       nvalid = 8;
     } else if (g.shape == 1) {  // cpGIMP
-      double rel[3];
       int i1[3];
       {
         int iz = n1 / g.NGxy, rem = n1 - iz * g.NGxy, iy = rem / g.NGx;
@@ -123,46 +144,56 @@ __global__ void k_locate(St<P> s, Geometry g, int nkeys) {
         i1[1] = iy;
         i1[2] = iz;
       }
+      double rel[3];
       for (int d = 0; d < 3; ++d) rel[d] = (x[d] - node_coord(g, n1, d)) * g.iDCell;
       int q[3];
       for (int d = 0; d < 3; ++d) q[d] = rel[d] < 0.25 ? 0 : (rel[d] > 0.75 ? 2 : 1);
       const GimpCase& gc = kGimp[q[2] * 9 + q[1] * 3 + q[0]];
       nvalid = gc.n;
       const R idc = (R)g.iDCell;
+      // 1-D shape values for the four node offsets -1..2 of each direction
+      // (NShape_GIMP, Grid.f90:577-591): every slot whose node is not a
+      // wrapped flat index uses these, so each r is computed once
+      R sh1[3][4], dn1[3][4];
+      for (int d = 0; d < 3; ++d)
+        for (int o = 0; o < 4; ++o) {
+          R rr;
+          if constexpr (P::kExact)
+            rr = (x[d] - ((double)(i1[d] + o - 1) * g.dcell + g.span0[d])) * g.iDCell;
+          else
+            rr = (R)rel[d] - (R)(o - 1);
+          gimp_1d<R>(rr, sh1[d][o], dn1[d][o]);
+        }
+      const int NGd[3] = {g.NGx, g.NGy, g.NGz};
       for (int k = 0; k < gc.n; ++k) {
         int off = gc.off[k];
-        int dx = (off & 3) - 1, dy = ((off >> 2) & 3) - 1, dz = (off >> 4) - 1;
-        int nd = n1 + dx + dy * g.NGx + dz * g.NGxy;  // flat arithmetic (may wrap rows)
+        int od[3] = {(off & 3), ((off >> 2) & 3), (off >> 4)};  // offset + 1
+        int nd = n1 + (od[0] - 1) + (od[1] - 1) * g.NGx + (od[2] - 1) * g.NGxy;  // flat arithmetic
         bool ok = nd >= 0 && nd < g.nn;
         slot_node[k] = ok ? nd : -1;
         if (!ok) continue;
-        R r[3];
-        if constexpr (P::kExact) {
-          for (int d = 0; d < 3; ++d) r[d] = (x[d] - node_coord(g, nd, d)) * g.iDCell;
-        } else {
-          int iz = nd / g.NGxy, rem = nd - iz * g.NGxy, iy = rem / g.NGx, ix = rem - iy * g.NGx;
-          r[0] = (R)rel[0] - (R)(ix - i1[0]);
-          r[1] = (R)rel[1] - (R)(iy - i1[1]);
-          r[2] = (R)rel[2] - (R)(iz - i1[2]);
-        }
         R sh[3], dn[3];
-        for (int d = 0; d < 3; ++d) {
-          R rr = r[d];
-          R a = rr < (R)0 ? -rr : rr;
-          R sg = copysign((R)1.0, rr);
-          if (a < (R)0.25) {
-            sh[d] = ((R)7 - (R)16 * a * a) * (R)0.125;
-            dn[d] = -((R)4 * rr);
-          } else if (a < (R)0.75) {
-            sh[d] = (R)1 - a;
-            dn[d] = -sg;
-          } else if (a < (R)1.25) {
-            R t = ((R)5 - (R)4 * a) * (R)0.25;
-            sh[d] = t * t;
-            dn[d] = (R)2 * rr - sg * (R)2.5;
-          } else {
-            sh[d] = (R)0.0;
-            dn[d] = (R)0.0;
+        bool wrapped = false;
+        for (int d = 0; d < 2; ++d) {
+          int id = i1[d] + od[d] - 1;
+          if (id < 0 || id >= NGd[d]) wrapped = true;
+        }
+        if (!wrapped) {
+          for (int d = 0; d < 3; ++d) {
+            sh[d] = sh1[d][od[d]];
+            dn[d] = dn1[d][od[d]];
+          }
+        } else {  // the +-1 / +-NGx offset crossed a grid row: the node lies elsewhere
+          int iz = nd / g.NGxy, rem = nd - iz * g.NGxy, iy = rem / g.NGx, ix = rem - iy * g.NGx;
+          for (int d = 0; d < 3; ++d) {
+            R rr;
+            if constexpr (P::kExact) {
+              rr = (x[d] - node_coord(g, nd, d)) * g.iDCell;
+            } else {
+              int id = d == 0 ? ix : (d == 1 ? iy : iz);
+              rr = (R)rel[d] - (R)(id - i1[d]);
+            }
+            gimp_1d<R>(rr, sh[d], dn[d]);
           }
         }
         s.shp[k * np + p] = sh[0] * sh[1] * sh[2];
