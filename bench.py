@@ -136,26 +136,28 @@ def dominant_kernel(stats: list, steps: int) -> dict:
     return dict(best, avg_ms=best["total_ms"] / max(1, best["launches"]))
 
 
-def kernel_bytes(kernel: str, np_: int, nn_active: float, K: int, bulk: int, real: int) -> float:
-    """Algorithmic bytes of one launch of a kernel: each particle / node field it
-    must touch, read once and written once (no re-reads, no scratch)."""
-    if kernel == "stress_update":
-        # read: snode + dndx/y/z per slot, node vg + mg per active node, and the
-        # particle state; write: the updated state (+ Xp when not USF)
-        per_p = K * (4 + 3 * real) + bulk * (1 + 1 + 1 + 1 + 1 + 1 + 6 + 1 + 1) + 8 * 2 + 1 + 2
-        per_p += bulk * (1 + 1 + 1 + 6 + 1 + 1 + 1 + 1) + 8 + 1
-        return per_p * np_ + nn_active * 32
-    if kernel == "p2g_force_integrate":
-        per_p = K * (4 + 4 * real) + 8 * 3 + 8 * 3 + bulk * 4  # pairs, shape, fext, sdiag, sd + vol
-        return per_p * np_ + nn_active * (8 * 3 * 2 + 8 + 8 * 3 + 1)
-    if kernel == "locate":
-        return np_ * (24 + 8 * 4 + K * (4 + 4 * real) + K * 8)
-    if kernel == "g2p_position":
-        return np_ * (K * (4 + real) + 24 * 4) + nn_active * (8 + 48)
+def kernel_bytes(kernel: str, np_: int, nn_active: float, usf: bool = True) -> float:
+    """Algorithmic bytes of one launch of a kernel of the mixed (batched) step:
+    the particle and node fields it must touch, each read once and written
+    once, at their stored widths (FP64 position, velocity, mass, energy, grid;
+    FP32 stress state). Sort keys, permutation and per-step scratch are
+    implementation overhead and are not counted."""
     if kernel == "p2g_mass":
-        return np_ * (K * (4 + real) + 8 + 24) + nn_active * 32
-    if kernel == "pair_sort":
-        return np_ * K * 8 * 2 * 3
+        # read x, mass, v; write node mass + momentum (+ velocity under USF)
+        return np_ * (24 + 8 + 24) + nn_active * (32 + (24 if usf else 0))
+    if kernel == "p2g_force_integrate":
+        # read sigma (SM, SD), vol, q, FXp, mass; node: read mass + momentum,
+        # write force, momentum, velocity, acceleration
+        return np_ * (4 * 7 + 4 + 4 + 24 + 8) + nn_active * (32 + 96)
+    if kernel == "stress_update":
+        # read x, vol, SM, SD, q, ie, cp, epeff, sig_y; write vol, SM, SD, q,
+        # ie, seqv, epeff; node velocity + mass read once
+        return np_ * (24 + 4 * 13 + 8) + np_ * (4 * 11 + 8) + nn_active * 32
+    if kernel == "g2p_position":
+        # read x, v; write x, v; node mass, velocity, acceleration read once
+        return np_ * 96 + nn_active * 56
+    if kernel == "permute":
+        return np_ * 2 * (6 * 8 + 6 * 8 + 16 * 4 + 1 + 2 + 2 + 4)
     return np_ * 100.0
 
 
@@ -243,8 +245,7 @@ def run_ours(args) -> dict:
     peaks = measured_peaks()
     dom = dominant_kernel(mixed["kernels"], args.steps)
     nn_active = mixed["scalars"]["active_nodes"]
-    K = 27
-    kb = kernel_bytes(dom["kernel"], npart, nn_active, K, 4, 4)
+    kb = kernel_bytes(dom["kernel"], npart, nn_active)
     achieved = kb / (dom["avg_ms"] / 1e3) / 1e9
     line = {
         "metric": "particle-steps/s (mixed precision vs plain FP64 GPU, stated error)",

@@ -150,6 +150,81 @@ int mpm_algorithmic_bytes(mpm_ctx* ctx, double* bytes_per_step);
 /* Bytes of device memory the context holds. */
 int64_t mpm_device_bytes(const mpm_ctx* ctx);
 
+/* --------------------------------------------------- batched scenes */
+/* No counterpart in the reference (which runs one scene per process): many
+ * independent scenes advanced together on one GPU in the mixed-precision form,
+ * one launch per kernel for the whole batch, indexed by per-scene offset
+ * tables. Each scene keeps its own DT, time, energies and step count, and its
+ * results do not depend on which other scenes share the batch.
+ * mpm_batch_add stages a scene (steps = number of steps it runs, 0 = no
+ * limit); mpm_batch_remove retires one; mpm_batch_commit lays the staged
+ * composition out in device memory (moving resident scenes' state on the
+ * device). Scene ids stay valid until removed. */
+typedef struct mpm_batch mpm_batch;
+int mpm_batch_create(int device, mpm_batch** out);
+void mpm_batch_destroy(mpm_batch* b);
+int mpm_batch_add(mpm_batch* b, const mpm_deck* deck, int steps, int* scene_id);
+int mpm_batch_remove(mpm_batch* b, int scene_id);
+int mpm_batch_commit(mpm_batch* b);
+/* Device bytes a deck needs as a scene of a batch (admission by HBM budget). */
+int64_t mpm_scene_device_bytes(const mpm_deck* deck);
+int64_t mpm_batch_device_bytes(const mpm_batch* b);
+int mpm_batch_scene_count(const mpm_batch* b);
+/* nsteps steps of every resident scene (a scene stops at its step count);
+ * use_graph replays a CUDA graph captured once per batch composition. */
+int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph);
+int mpm_batch_sync(mpm_batch* b);
+int mpm_batch_time_steps(mpm_batch* b, int nsteps, int use_graph, double* ms);
+int mpm_batch_scene_scalars(mpm_batch* b, int scene_id, double* out16);
+int mpm_batch_scene_download(mpm_batch* b, int scene_id, int field, double* out);
+const char* mpm_batch_last_error(const mpm_batch* b);
+/* Launch shape of the batch kernels (threads per block for particle and node
+ * kernels; 0 keeps the current value). */
+int mpm_batch_set_blocks(mpm_batch* b, int particle_block, int node_block);
+int mpm_batch_profile_enable(mpm_batch* b, int on);
+int mpm_batch_kernel_stats(mpm_batch* b, int k, char* name, int namelen, int64_t* launches, double* total_ms);
+
+/* ------------------------------------------------------ serving runtime */
+/* No counterpart in the reference (a serial one-scene program): a server owns
+ * one device and one batch (above). Client threads submit scenes; a server
+ * thread admits them first-come first-served while their estimated device
+ * bytes fit the budget, advances the batch in chunks of chunk_steps steps
+ * (one CUDA graph replay per step, recaptured when the composition changes),
+ * retires scenes that reached their step count (snapshotting the fields named
+ * in field_mask to host memory) and admits the next ones. A scene's results
+ * are the same as when it runs alone. */
+typedef struct mpm_server mpm_server;
+typedef struct mpm_serve_config {
+  int device;               /* CUDA device, -1 = current                        */
+  int chunk_steps;          /* steps between admission points (0 = 25)          */
+  int64_t hbm_budget_bytes; /* device bytes for resident scenes (0 = 80% of free) */
+  int max_scenes;           /* resident scene cap (0 = 4096)                     */
+  int autotune;             /* 1 = pick the batch launch shape on the first chunks */
+} mpm_serve_config;
+/* bit (1u << field) of field_mask snapshots particle field `field` (mpm_field
+ * ids 1..25) when the scene finishes */
+#define MPM_SERVE_FIELD(f) (1u << (f))
+int mpm_serve_create(const mpm_serve_config* cfg, mpm_server** out);
+void mpm_serve_destroy(mpm_server* s); /* drains nothing: running scenes are dropped */
+const char* mpm_serve_last_error(const mpm_server* s);
+/* queue a scene for `steps` steps (>= 1); the deck may be freed on return */
+int mpm_serve_submit(mpm_server* s, const mpm_deck* deck, int steps, uint32_t field_mask, int64_t* ticket);
+/* wait up to timeout_ms (< 0: no limit) for a ticket: MPM_OK once finished,
+ * MPM_ERR_TIMEOUT if still queued / running, MPM_ERR_OOM if the scene can
+ * never fit the budget, MPM_ERR_ARG for an unknown ticket */
+int mpm_serve_wait(mpm_server* s, int64_t ticket, int timeout_ms);
+/* a finished ticket: scalars as mpm_get_scalars; times_ms[3] = queue wait,
+ * time resident, total latency (submit to retirement) */
+int mpm_serve_result(mpm_server* s, int64_t ticket, double* scalars16, double* times_ms3);
+/* a snapshotted particle field of a finished ticket, in the deck's particle order */
+int mpm_serve_field(mpm_server* s, int64_t ticket, int field, double* out);
+int mpm_serve_release(mpm_server* s, int64_t ticket);
+/* out[10]: submitted, finished, queued, resident, chunks run, particle-steps
+ * run, device busy ms, particle block, node block, peak resident bytes */
+int mpm_serve_stats(mpm_server* s, double* out10);
+/* block until no scene is queued or resident (or timeout_ms passes) */
+int mpm_serve_drain(mpm_server* s, int timeout_ms);
+
 /* ------------------------------------------------ allocation-free call */
 /* No counterpart in the reference: an extra entry point for hosts that may not
  * allocate device memory inside a solver call (a Fortran code passing device

@@ -69,9 +69,11 @@ def build_library(force: bool = False) -> str:
     hdr = _headers()
     units = [
         ("mpm_fp64.cu", ["--fmad=false"]),
-        ("mpm_mixed.cu", []),
         ("mpm_gpu.cu", []),
         ("mpm_noalloc.cu", ["--fmad=false"]),
+        ("mpm_setup.cu", []),
+        ("mpm_batch.cu", []),
+        ("mpm_serve.cu", []),
     ]
     jobs = []
     objs = []

@@ -1,0 +1,1015 @@
+// mpm_batch.cu -- host side of the batched mixed-precision step (C ABI in
+// include/mpm3d_gpu.h, kernels in mpm_batch_kernels.cuh).
+//
+// A batch holds the scenes of one composition laid out back to back in device
+// memory. Changing the composition (mpm_batch_commit) builds a new layout:
+// resident scenes are moved on the device by a relocation kernel, new scenes
+// are uploaded, retired scenes are dropped. Every step sorts the particles of
+// all scenes by (scene, cell) and runs one launch per kernel for the batch.
+#include <cuda_runtime.h>
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "mpm3d_gpu.h"
+#include "mpm_batch_host.h"
+#include "mpm_batch_kernels.cuh"
+#include "mpm_setup.h"
+
+using namespace mpm;
+using namespace mpm::bm;
+
+namespace mpm {
+
+// a scene staged on the host: its set-up and input state (copied from the
+// deck, so the deck may be freed once the scene is staged)
+struct HostScene {
+  int id = 0;
+  int steps = 0;  // step count to run (INT_MAX = unlimited)
+  SceneSetup su;
+  long long np = 0, nn = 0, ncell = 0;
+  std::vector<double> mass, x, v, fxp;  // input state, component-major, input order
+  std::vector<uint16_t> body_local;     // body index per particle
+  bool resident = false;
+  long long p0 = 0, n0 = 0, k0 = 0, c0 = 0, r0 = 0, nr = 0;
+  int mat0 = 0, body0 = 0, index = 0;
+  SceneState st{};
+  int drdamp = 0;
+};
+
+}  // namespace mpm
+
+namespace {
+
+struct MaxOpB {
+  __host__ __device__ int operator()(int a, int b) const { return a > b ? a : b; }
+};
+
+// relocation of resident particles into a new layout
+__global__ void kb_relocate(BState src, BState dst, const int* map, const uint16_t* scene_map,
+                            const uint16_t* body_map) {
+  long long i = btid();
+  if (i >= dst.NP) return;
+  long long j = map[i];
+  if (j < 0) return;
+  const long long NP = dst.NP, SP = src.NP;
+  for (int a = 0; a < 3; ++a) {
+    dst.x[a * NP + i] = src.x[a * SP + j];
+    dst.xx[a * NP + i] = src.xx[a * SP + j];
+    dst.v[a * NP + i] = src.v[a * SP + j];
+    dst.fxp[a * NP + i] = src.fxp[a * SP + j];
+  }
+  dst.mass[i] = src.mass[j];
+  dst.ie[i] = src.ie[j];
+  dst.vol[i] = src.vol[j];
+  dst.sig_y[i] = src.sig_y[j];
+  dst.sm[i] = src.sm[j];
+  dst.seqv[i] = src.seqv[j];
+  for (int a = 0; a < 6; ++a) dst.sd[a * NP + i] = src.sd[a * SP + j];
+  if (src.any_uvfp && dst.any_uvfp)
+    for (int a = 0; a < 9; ++a) dst.fp[a * NP + i] = src.fp[a * SP + j];
+  dst.epeff[i] = src.epeff[j];
+  dst.celsius[i] = src.celsius[j];
+  dst.dmg[i] = src.dmg[j];
+  dst.lt[i] = src.lt[j];
+  dst.cp[i] = src.cp[j];
+  dst.q[i] = src.q[j];
+  dst.failure[i] = src.failure[j];
+  dst.body[i] = body_map[src.body[j]];
+  dst.scene[i] = scene_map[src.scene[j]];
+  dst.orig[i] = src.orig[j];
+}
+
+}  // namespace
+
+struct mpm_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<HostScene*> order;  // composition order
+  std::map<int, HostScene*> by_id;
+  int next_id = 1;
+  bool dirty = false;
+  // current layout
+  BState A{}, B{};
+  std::vector<void*> allocs;
+  long long bytes = 0;
+  int* d_target = nullptr;
+  void* cub_tmp = nullptr;
+  size_t cub_bytes = 0;
+  int key_bits = 1;
+  int any_sgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
+  const double* set0_x = nullptr;                   // identifies particle buffer set 0
+  int pblock = 256, nblock = 256;
+  Profiler prof;
+  std::string err;
+};
+
+namespace {
+
+int berr(mpm_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return code;
+}
+
+#define BCK(call)                                                                        \
+  do {                                                                                   \
+    cudaError_t e__ = (call);                                                            \
+    if (e__ != cudaSuccess) return berr(b, MPM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e__)); \
+  } while (0)
+
+struct Alloc {
+  std::vector<void*> ptrs;
+  long long bytes = 0;
+  bool fail = false;
+  template <class T>
+  T* get(long long n) {
+    if (n <= 0) n = 1;
+    void* p = nullptr;
+    if (cudaMalloc(&p, (size_t)n * sizeof(T)) != cudaSuccess) {
+      fail = true;
+      return nullptr;
+    }
+    ptrs.push_back(p);
+    bytes += n * (long long)sizeof(T);
+    return (T*)p;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+    bytes = 0;
+  }
+};
+
+void alloc_particles(Alloc& al, BState& s, long long NP, bool uvfp) {
+  s.x = al.get<double>(3 * NP);
+  s.xx = al.get<double>(3 * NP);
+  s.v = al.get<double>(3 * NP);
+  s.fxp = al.get<double>(3 * NP);
+  s.mass = al.get<double>(NP);
+  s.ie = al.get<double>(NP);
+  s.vol = al.get<float>(NP);
+  s.sig_y = al.get<float>(NP);
+  s.sm = al.get<float>(NP);
+  s.seqv = al.get<float>(NP);
+  s.sd = al.get<float>(6 * NP);
+  s.fp = al.get<float>(uvfp ? 9 * NP : 1);
+  s.epeff = al.get<float>(NP);
+  s.celsius = al.get<float>(NP);
+  s.dmg = al.get<float>(NP);
+  s.lt = al.get<float>(NP);
+  s.cp = al.get<float>(NP);
+  s.q = al.get<float>(NP);
+  s.failure = al.get<uint8_t>(NP);
+  s.body = al.get<uint16_t>(NP);
+  s.scene = al.get<uint16_t>(NP);
+  s.orig = al.get<int>(NP);
+}
+
+long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bool uvfp, bool jc) {
+  long long per_p = 2 * (16 * 8 + 16 * 4 + (uvfp ? 36 : 0) + 1 + 2 + 2 + 4);  // two particle buffer sets
+  per_p += 4 * 3 + 4 * 9 + 4 * 6 + 4 * 9;                                  // derived + force staging
+  per_p += 4 * 4;                                                         // sort keys / values
+  if (jc) per_p += 4 * 2 + 8 * 6 + 1;
+  long long per_n = 8 * 13 + 4;
+  long long per_k = 4;
+  long long per_c = sgmp ? 8 * 39 + 2 : 0;
+  return np * per_p + nn * per_n + (ncell + 1) * per_k + ncell * per_c + 4096;
+}
+
+void layout_flags(mpm_batch* b) {
+  b->any_sgmp = b->any_usf = b->any_later = b->any_musl = b->any_jc = b->any_dr = b->any_uvfp = 0;
+  for (HostScene* h : b->order) {
+    const Geometry& g = h->su.g;
+    if (g.shape == 3) b->any_sgmp = 1;
+    if (g.usf) b->any_usf = 1; else b->any_later = 1;
+    if (g.musl) b->any_musl = 1;
+    if (g.has_jc) b->any_jc = 1;
+    if (g.uvfp) b->any_uvfp = 1;
+    if (h->drdamp) b->any_dr = 1;
+  }
+}
+
+int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
+  const long long NP = s.NP, np = h->np, p0 = h->p0;
+  std::vector<float> f((size_t)np);
+  auto upd = [&](double* dst, const double* src, long long n) {
+    return cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream);
+  };
+  for (int a = 0; a < 3; ++a) {
+    BCK(upd(s.x + a * NP + p0, h->x.data() + a * np, np));
+    BCK(upd(s.xx + a * NP + p0, h->x.data() + a * np, np));
+    BCK(upd(s.v + a * NP + p0, h->v.data() + a * np, np));
+    BCK(upd(s.fxp + a * NP + p0, h->fxp.data() + a * np, np));
+  }
+  BCK(upd(s.mass + p0, h->mass.data(), np));
+  BCK(upd(s.ie + p0, h->su.ie.data(), np));
+  auto upf = [&](float* dst, const std::vector<double>& src) {
+    for (long long i = 0; i < np; ++i) f[i] = (float)src[i];
+    cudaError_t e = cudaMemcpyAsync(dst, f.data(), sizeof(float) * np, cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    return e;
+  };
+  BCK(upf(s.vol + p0, h->su.vol));
+  BCK(upf(s.sig_y + p0, h->su.sig_y));
+  BCK(upf(s.cp + p0, h->su.cp));
+  BCK(upf(s.lt + p0, h->su.lt));
+  std::vector<double> t293((size_t)np, (double)293.0f);
+  BCK(upf(s.celsius + p0, t293));
+  BCK(cudaMemsetAsync(s.sm + p0, 0, sizeof(float) * np, b->stream));
+  BCK(cudaMemsetAsync(s.seqv + p0, 0, sizeof(float) * np, b->stream));
+  for (int a = 0; a < 6; ++a) BCK(cudaMemsetAsync(s.sd + a * NP + p0, 0, sizeof(float) * np, b->stream));
+  if (s.any_uvfp)
+    for (int a = 0; a < 9; ++a) BCK(cudaMemsetAsync(s.fp + a * NP + p0, 0, sizeof(float) * np, b->stream));
+  BCK(cudaMemsetAsync(s.epeff + p0, 0, sizeof(float) * np, b->stream));
+  BCK(cudaMemsetAsync(s.dmg + p0, 0, sizeof(float) * np, b->stream));
+  BCK(cudaMemsetAsync(s.q + p0, 0, sizeof(float) * np, b->stream));
+  BCK(cudaMemsetAsync(s.failure + p0, 0, np, b->stream));
+  std::vector<uint16_t> body((size_t)np), scene((size_t)np, (uint16_t)h->index);
+  for (long long i = 0; i < np; ++i) body[i] = (uint16_t)(h->body0 + h->body_local[i]);
+  std::vector<int> orig((size_t)np);
+  for (long long i = 0; i < np; ++i) orig[i] = (int)i;
+  BCK(cudaMemcpyAsync(s.body + p0, body.data(), 2 * np, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(s.scene + p0, scene.data(), 2 * np, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(s.orig + p0, orig.data(), 4 * np, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return MPM_OK;
+}
+
+inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
+
+// one step of every live scene (MPM3D.f90:69-118 for each scene)
+int enqueue_step(mpm_batch* b) {
+  cudaStream_t st = b->stream;
+  BState& a = b->A;
+  const int pb = b->pblock, nb = b->nblock;
+  prof_begin(K_BEGIN, st);
+  kb_begin<<<gridn(a.nscene, 128), 128, 0, st>>>(a, b->d_target);
+  prof_end(K_BEGIN, st);
+  prof_begin(K_LOCATE, st);
+  cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
+  kb_keys<<<gridn(a.NP, pb), pb, 0, st>>>(a);
+  prof_end(K_LOCATE, st);
+  prof_begin(K_SORT, st);
+  size_t tmp = b->cub_bytes;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(b->cub_tmp, tmp, a.key, a.key_sorted, a.val, a.perm, (int)a.NP, 0,
+                                                  b->key_bits, st);
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "sort: %s", cudaGetErrorString(e));
+  tmp = b->cub_bytes;
+  e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
+  prof_end(K_SORT, st);
+  prof_begin(K_PERMUTE, st);
+  kb_permute<<<gridn(a.NP, pb), pb, 0, st>>>(a, b->B);
+  prof_end(K_PERMUTE, st);
+  // swap the particle buffer sets (node and scene arrays are shared)
+  std::swap(b->A, b->B);
+  BState& s = b->A;
+  prof_begin(K_P2G_MASS, st);
+  if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
+  kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
+  prof_end(K_P2G_MASS, st);
+  auto stress = [&](int usf_pass) -> int {
+    prof_begin(K_STRESS, st);
+    if (b->any_sgmp) kb_sg_centre_gradient<<<gridn(s.NC, nb), nb, 0, st>>>(s, usf_pass);
+    kb_stress<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass);
+    prof_end(K_STRESS, st);
+    if (b->any_jc) {
+      prof_begin(K_DEPEFF, st);
+      size_t t2 = b->cub_bytes;
+      cudaError_t e2 = cub::DeviceScan::InclusiveScan(b->cub_tmp, t2, s.setter, s.setter_scan, MaxOpB(), (int)s.NP, st);
+      if (e2 != cudaSuccess) return berr(b, MPM_ERR_CUDA, "depeff scan: %s", cudaGetErrorString(e2));
+      kb_depeff_apply<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass);
+      kb_depeff_carry<<<gridn(s.nscene, 128), 128, 0, st>>>(s, usf_pass);
+      prof_end(K_DEPEFF, st);
+    }
+    return MPM_OK;
+  };
+  int r;
+  if (b->any_usf && (r = stress(1))) return r;
+  prof_begin(K_FORCE_PREP, st);
+  kb_force_prep<<<gridn(s.NP, pb), pb, 0, st>>>(s);
+  prof_end(K_FORCE_PREP, st);
+  prof_begin(K_P2G_FORCE, st);
+  if (b->any_sgmp) kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
+  kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
+  prof_end(K_P2G_FORCE, st);
+  prof_begin(K_POSITION, st);
+  if (b->any_sgmp) kb_sg_centre_velocity<<<gridn(s.NC, nb), nb, 0, st>>>(s);
+  kb_position<<<gridn(s.NP, pb), pb, 0, st>>>(s);
+  prof_end(K_POSITION, st);
+  if (b->any_musl) {
+    prof_begin(K_P2G_MOM, st);
+    if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
+    kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
+    prof_end(K_P2G_MOM, st);
+  }
+  if (b->any_later && (r = stress(0))) return r;
+  prof_begin(K_REDUCE, st);
+  kb_reduce_chunks<<<(unsigned)s.NR, 256, 0, st>>>(s);
+  kb_reduce_scenes<<<(unsigned)s.nscene, 256, 0, st>>>(s, 3);
+  prof_end(K_REDUCE, st);
+  if (b->any_dr) {
+    prof_begin(K_DR, st);
+    kb_dr_damping<<<gridn(s.NP, pb), pb, 0, st>>>(s);
+    kb_dr_finish<<<gridn(s.nscene, 128), 128, 0, st>>>(s);
+    prof_end(K_DR, st);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "launch: %s", cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+void drop_graph(mpm_batch* b) {
+  for (auto& g : b->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
+// capture nsteps steps into an executable graph; the host-side buffer handles
+// end swapped nsteps times, as after running the steps eagerly
+int capture(mpm_batch* b, int nsteps, cudaGraphExec_t* out) {
+  cudaGraph_t g;
+  BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  b->prof.capturing = true;
+  int r = MPM_OK;
+  for (int i = 0; i < nsteps && r == MPM_OK; ++i) r = enqueue_step(b);
+  b->prof.capturing = false;
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (r) {
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "end capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+struct BProfScope {
+  Profiler* prev;
+  explicit BProfScope(mpm_batch* b) : prev(prof_current()) { prof_set_current(&b->prof); }
+  ~BProfScope() { prof_set_current(prev); }
+};
+
+int commit(mpm_batch* b) {
+  cudaStream_t st = b->stream;
+  if (b->order.empty()) {
+    drop_graph(b);
+    for (void* p : b->allocs) cudaFree(p);
+    b->allocs.clear();
+    b->bytes = 0;
+    b->A = BState{};
+    b->B = BState{};
+    b->set0_x = nullptr;
+    b->dirty = false;
+    return MPM_OK;
+  }
+  // scene states of resident scenes, read back before the layout changes
+  if (b->A.nscene > 0) {
+    std::vector<SceneState> old((size_t)b->A.nscene);
+    BCK(cudaMemcpy(old.data(), b->A.sst, sizeof(SceneState) * old.size(), cudaMemcpyDeviceToHost));
+    for (HostScene* h : b->order)
+      if (h->resident) h->st = old[h->index];
+  }
+  // new layout
+  long long NP = 0, NN = 0, NK = 0, NC = 0, NR = 0;
+  int nmat = 0, nbody = 0;
+  std::vector<int> old_index;
+  for (size_t k = 0; k < b->order.size(); ++k) {
+    HostScene* h = b->order[k];
+    old_index.push_back(h->resident ? h->index : -1);
+  }
+  std::vector<long long> old_p0, old_body0;
+  for (HostScene* h : b->order) {
+    old_p0.push_back(h->p0);
+    old_body0.push_back(h->body0);
+  }
+  for (size_t k = 0; k < b->order.size(); ++k) {
+    HostScene* h = b->order[k];
+    const Geometry& g = h->su.g;
+    h->index = (int)k;
+    h->p0 = NP;
+    h->n0 = NN;
+    h->k0 = NK;
+    h->c0 = NC;
+    h->r0 = NR;
+    h->nr = (h->np + kChunk - 1) / kChunk;
+    if (h->nr == 0) h->nr = 1;
+    h->mat0 = nmat;
+    h->body0 = nbody;
+    NP += h->np;
+    NN += h->nn;
+    NK += h->ncell + 1;
+    if (g.shape == 3) NC += h->ncell;
+    NR += h->nr;
+    nmat += (int)h->su.mats.size();
+    nbody += (int)h->su.bodies.size();
+  }
+  if (b->order.size() > 65535 || nbody > 65535) return berr(b, MPM_ERR_UNSUPPORTED, "too many scenes / bodies");
+  if (NP >= (1LL << 31) || NK >= (1LL << 31) || NN >= (1LL << 31))
+    return berr(b, MPM_ERR_UNSUPPORTED, "batch too large for 32-bit indices");
+  layout_flags(b);
+  Alloc al;
+  BState A{}, B{};
+  A.NP = B.NP = NP;
+  A.NN = B.NN = NN;
+  A.NK = B.NK = NK;
+  A.NC = B.NC = NC;
+  A.NR = B.NR = NR;
+  A.nscene = B.nscene = (int)b->order.size();
+  A.any_uvfp = B.any_uvfp = b->any_uvfp;
+  A.any_sgmp = B.any_sgmp = b->any_sgmp;
+  A.any_jc = B.any_jc = b->any_jc;
+  alloc_particles(al, A, NP, b->any_uvfp);
+  alloc_particles(al, B, NP, b->any_uvfp);
+  BState shared{};
+  shared.cell = al.get<int>(NP);
+  shared.dual = al.get<int>(NP);
+  shared.inode = al.get<int>(NP);
+  shared.off = al.get<float>(3 * NP);
+  shared.xxn = al.get<float>(3 * NP);
+  shared.xn = al.get<float>(3 * NP);
+  shared.fs = al.get<float>(9 * NP);
+  shared.key = al.get<unsigned>(NP);
+  shared.key_sorted = al.get<unsigned>(NP);
+  shared.val = al.get<int>(NP);
+  shared.perm = al.get<int>(NP);
+  shared.seg = al.get<int>(NK + 1);
+  shared.mg = al.get<double>(NN);
+  shared.px = al.get<double>(3 * NN);
+  shared.fx = al.get<double>(3 * NN);
+  shared.vg = al.get<double>(3 * NN);
+  shared.ag = al.get<double>(3 * NN);
+  shared.fix = al.get<uint8_t>(NN);
+  shared.bd = al.get<uint8_t>(NN);
+  shared.node_scene = al.get<uint16_t>(NN);
+  shared.cmg = al.get<double>(NC);
+  shared.cpx = al.get<double>(3 * NC);
+  shared.cfext = al.get<double>(3 * NC);
+  shared.cfint = al.get<double>(6 * NC);
+  shared.co = al.get<double>(6 * NC);
+  shared.cw = al.get<double>(3 * NC);
+  shared.cdefp = al.get<double>(9 * NC);
+  shared.cvx = al.get<double>(3 * NC);
+  shared.cax = al.get<double>(3 * NC);
+  shared.cscene = al.get<uint16_t>(NC);
+  if (b->any_jc) {
+    shared.setter = al.get<int>(NP);
+    shared.setter_scan = al.get<int>(NP);
+    shared.dep = al.get<double>(NP);
+    shared.jc_aux = al.get<double>(5 * NP);
+    shared.deferred = al.get<uint8_t>(NP);
+  }
+  shared.red_part = al.get<double>(6 * NR);
+  shared.rscene = al.get<uint16_t>(NR);
+  shared.scenes = al.get<Scene>((long long)b->order.size());
+  shared.sst = al.get<SceneState>((long long)b->order.size());
+  shared.mats = al.get<DevMaterial>(nmat);
+  shared.bodies = al.get<DevBody>(nbody);
+  int* d_target = al.get<int>((long long)b->order.size());
+  int* d_map = al.get<int>(NP);
+  uint16_t* d_smap = al.get<uint16_t>(b->A.nscene + 1);
+  uint16_t* d_bmap = al.get<uint16_t>(65536);
+  if (al.fail) {
+    al.release();
+    return berr(b, MPM_ERR_OOM, "device memory for a batch of %lld particles", NP);
+  }
+  auto share = [&](BState& s) {
+    s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
+    s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
+    s.perm = shared.perm; s.seg = shared.seg; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
+    s.vg = shared.vg; s.ag = shared.ag; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
+    s.cmg = shared.cmg; s.cpx = shared.cpx; s.cfext = shared.cfext; s.cfint = shared.cfint; s.co = shared.co;
+    s.cw = shared.cw; s.cdefp = shared.cdefp; s.cvx = shared.cvx; s.cax = shared.cax; s.cscene = shared.cscene;
+    s.setter = shared.setter; s.setter_scan = shared.setter_scan; s.dep = shared.dep; s.jc_aux = shared.jc_aux;
+    s.deferred = shared.deferred; s.red_part = shared.red_part; s.rscene = shared.rscene; s.scenes = shared.scenes;
+    s.sst = shared.sst; s.mats = shared.mats; s.bodies = shared.bodies;
+  };
+  share(A);
+  share(B);
+  // move resident scenes on the device
+  bool any_resident = false;
+  for (HostScene* h : b->order) any_resident |= h->resident;
+  if (any_resident) {
+    std::vector<int> map((size_t)NP, -1);
+    std::vector<uint16_t> smap((size_t)b->A.nscene + 1, 0);
+    std::vector<uint16_t> bmap(65536, 0);
+    for (size_t k = 0; k < b->order.size(); ++k) {
+      HostScene* h = b->order[k];
+      if (!h->resident) continue;
+      for (long long i = 0; i < h->np; ++i) map[h->p0 + i] = (int)(old_p0[k] + i);
+      smap[old_index[k]] = (uint16_t)h->index;
+      for (size_t q = 0; q < h->su.bodies.size(); ++q) bmap[old_body0[k] + q] = (uint16_t)(h->body0 + q);
+    }
+    BCK(cudaMemcpyAsync(d_map, map.data(), sizeof(int) * NP, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(d_smap, smap.data(), 2 * smap.size(), cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(d_bmap, bmap.data(), 2 * bmap.size(), cudaMemcpyHostToDevice, st));
+    kb_relocate<<<gridn(NP, 256), 256, 0, st>>>(b->A, A, d_map, d_smap, d_bmap);
+    BCK(cudaGetLastError());
+    BCK(cudaStreamSynchronize(st));
+  }
+  // static per-scene tables
+  std::vector<Scene> scenes;
+  std::vector<DevMaterial> mats;
+  std::vector<DevBody> bodies;
+  std::vector<uint16_t> nscene((size_t)NN), cscene((size_t)NC), rscene((size_t)NR);
+  std::vector<uint8_t> fix((size_t)NN), bd((size_t)NN);
+  std::vector<int> target;
+  std::vector<SceneState> sst;
+  for (HostScene* h : b->order) {
+    const Geometry& g = h->su.g;
+    Scene sc;
+    memset(&sc, 0, sizeof sc);
+    sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = h->ncell + 1;
+    sc.c0 = h->c0; sc.nc = g.shape == 3 ? h->ncell : 0; sc.r0 = h->r0; sc.nr = h->nr;
+    sc.NGx = g.NGx; sc.NGy = g.NGy; sc.NGz = g.NGz; sc.NGxy = g.NGxy;
+    sc.NCx = g.NCx; sc.NCy = g.NCy; sc.NCz = g.NCz; sc.NCxy = g.NCxy;
+    sc.CNCx = g.CNCx; sc.CNCy = g.CNCy; sc.CNCz = g.CNCz; sc.CNCxy = g.CNCxy; sc.CNC = g.CNC;
+    sc.shape = g.shape; sc.usf = g.usf; sc.musl = g.musl; sc.uvfp = g.uvfp; sc.qload = g.qload;
+    sc.qdamp = g.qdamp; sc.gravity = g.gravity; sc.drdamp = h->drdamp; sc.has_jc = g.has_jc;
+    for (int k = 0; k < 6; ++k) sc.fixs[k] = g.fixs[k];
+    sc.mat0 = h->mat0; sc.nmat = (int)h->su.mats.size();
+    for (int k = 0; k < 3; ++k) { sc.span0[k] = g.span0[k]; sc.span1[k] = g.span1[k]; }
+    sc.dcell = g.dcell; sc.idcell = g.iDCell; sc.cutoff = g.cutoff; sc.iJacobi = g.iJacobi; sc.iJacobi4 = g.iJacobi4;
+    sc.dtscale = g.dtscale; sc.qload_time = g.qload_time; sc.damp_factor = g.damp_factor; sc.bq1 = g.bq1; sc.bq2 = g.bq2;
+    scenes.push_back(sc);
+    for (auto m : h->su.mats) mats.push_back(m);
+    for (auto bo : h->su.bodies) {
+      bo.mat += h->mat0;
+      bodies.push_back(bo);
+    }
+    for (long long n = 0; n < h->nn; ++n) {
+      nscene[h->n0 + n] = (uint16_t)h->index;
+      fix[h->n0 + n] = h->su.fix[n];
+      bd[h->n0 + n] = h->su.bd[n];
+    }
+    if (g.shape == 3)
+      for (long long c = 0; c < h->ncell; ++c) cscene[h->c0 + c] = (uint16_t)h->index;
+    for (long long r = 0; r < h->nr; ++r) rscene[h->r0 + r] = (uint16_t)h->index;
+    target.push_back(h->steps);
+    SceneState s0;
+    if (h->resident) {
+      s0 = h->st;
+    } else {
+      memset(&s0, 0, sizeof s0);
+      s0.dt = set_dt(h->su.mats, g.dcell, g.dtscale);
+    }
+    s0.active = h->resident ? 0 : 1;  // the initial energy pass below runs for new scenes only
+    sst.push_back(s0);
+  }
+  BCK(cudaMemcpyAsync(shared.scenes, scenes.data(), sizeof(Scene) * scenes.size(), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.mats, mats.data(), sizeof(DevMaterial) * mats.size(), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.bodies, bodies.data(), sizeof(DevBody) * bodies.size(), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.node_scene, nscene.data(), 2 * NN, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.fix, fix.data(), NN, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.bd, bd.data(), NN, cudaMemcpyHostToDevice, st));
+  if (NC) BCK(cudaMemcpyAsync(shared.cscene, cscene.data(), 2 * NC, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.rscene, rscene.data(), 2 * NR, cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(d_target, target.data(), sizeof(int) * target.size(), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemcpyAsync(shared.sst, sst.data(), sizeof(SceneState) * sst.size(), cudaMemcpyHostToDevice, st));
+  BCK(cudaMemsetAsync(shared.mg, 0, sizeof(double) * NN, st));
+  BCK(cudaMemsetAsync(shared.px, 0, sizeof(double) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.fx, 0, sizeof(double) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.vg, 0, sizeof(double) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.ag, 0, sizeof(double) * 3 * NN, st));
+  // every depeff setter entry is -1 or its own index (the max-scan relies on
+  // it); only Johnson-Cook scenes rewrite theirs each step
+  if (b->any_jc) BCK(cudaMemsetAsync(shared.setter, 0xff, sizeof(int) * NP, st));
+  for (HostScene* h : b->order)
+    if (!h->resident) {
+      int r = upload_scene_particles(b, h, A);
+      if (r) {
+        al.release();
+        return r;
+      }
+    }
+  // CUB scratch for this layout
+  size_t t1 = 0, t2 = 0, t3 = 0;
+  int bits = 1;
+  while ((1LL << bits) <= NK) ++bits;
+  cub::DeviceRadixSort::SortPairs(nullptr, t1, A.key, A.key_sorted, A.val, A.perm, (int)NP, 0, bits, st);
+  cub::DeviceScan::InclusiveSum(nullptr, t2, A.seg, A.seg, (int)NK, st);
+  if (b->any_jc) cub::DeviceScan::InclusiveScan(nullptr, t3, A.setter, A.setter_scan, MaxOpB(), (int)NP, st);
+  size_t tb = std::max(t1, std::max(t2, t3));
+  void* tmp = al.get<char>((long long)tb);
+  if (al.fail) {
+    al.release();
+    return berr(b, MPM_ERR_OOM, "device memory for the sort scratch");
+  }
+  // calcEnergy of the new scenes (MPM3D.f90:42)
+  kb_reduce_chunks<<<(unsigned)NR, 256, 0, st>>>(A);
+  kb_reduce_scenes<<<(unsigned)A.nscene, 256, 0, st>>>(A, 1);
+  BCK(cudaGetLastError());
+  BCK(cudaStreamSynchronize(st));
+  // swap in the new layout
+  drop_graph(b);
+  for (void* p : b->allocs) cudaFree(p);
+  b->allocs = al.ptrs;
+  b->bytes = al.bytes;
+  b->A = A;
+  b->B = B;
+  b->set0_x = A.x;
+  b->d_target = d_target;
+  b->cub_tmp = tmp;
+  b->cub_bytes = tb;
+  b->key_bits = bits;
+  for (HostScene* h : b->order) h->resident = true;
+  b->dirty = false;
+  return MPM_OK;
+}
+
+int ensure_committed(mpm_batch* b) {
+  if (b->dirty) return commit(b);
+  return MPM_OK;
+}
+
+HostScene* find(mpm_batch* b, int id) {
+  auto it = b->by_id.find(id);
+  return it == b->by_id.end() ? nullptr : it->second;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_batch_create(int device, mpm_batch** out) {
+  if (!out) return MPM_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MPM_ERR_CUDA;
+  if (device >= ndev) return MPM_ERR_ARG;
+  if (device >= 0) cudaSetDevice(device);
+  mpm_batch* b = new mpm_batch();
+  cudaGetDevice(&b->device);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return MPM_ERR_CUDA;
+  }
+  *out = b;
+  return MPM_OK;
+}
+
+void mpm_batch_destroy(mpm_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  for (void* p : b->allocs) cudaFree(p);
+  for (auto& kv : b->by_id) delete kv.second;
+  prof_free(&b->prof);
+  cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+const char* mpm_batch_last_error(const mpm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int64_t mpm_scene_device_bytes(const mpm_deck* d) {
+  if (!d) return -1;
+  SceneSetup su;
+  if (scene_setup(d, su)) return -1;
+  return scene_bytes(d->nb_particle, su.g.nn, su.g.ncell, su.g.shape == 3, su.g.uvfp, su.g.has_jc);
+}
+
+int mpm_batch_add(mpm_batch* b, const mpm_deck* d, int steps, int* scene_id) {
+  if (!b || !d) return MPM_ERR_ARG;
+  int code = MPM_OK;
+  HostScene* h = scene_stage(d, steps, b->err, &code);
+  if (!h) return code;
+  return batch_insert(b, h, scene_id);
+}
+
+int mpm_batch_remove(mpm_batch* b, int id) {
+  if (!b) return MPM_ERR_ARG;
+  HostScene* h = find(b, id);
+  if (!h) return berr(b, MPM_ERR_ARG, "no scene %d", id);
+  if (h->resident && b->A.nscene > 0) {
+    // keep the other scenes' states: read them now (commit reads by index)
+    std::vector<SceneState> old((size_t)b->A.nscene);
+    BCK(cudaStreamSynchronize(b->stream));
+    BCK(cudaMemcpy(old.data(), b->A.sst, sizeof(SceneState) * old.size(), cudaMemcpyDeviceToHost));
+    for (HostScene* o : b->order)
+      if (o->resident) o->st = old[o->index];
+  }
+  b->order.erase(std::find(b->order.begin(), b->order.end(), h));
+  b->by_id.erase(id);
+  delete h;
+  b->dirty = true;
+  return MPM_OK;
+}
+
+int mpm_batch_commit(mpm_batch* b) {
+  if (!b) return MPM_ERR_ARG;
+  cudaSetDevice(b->device);
+  BCK(cudaStreamSynchronize(b->stream));
+  return commit(b);
+}
+
+int64_t mpm_batch_device_bytes(const mpm_batch* b) { return b ? b->bytes : -1; }
+int mpm_batch_scene_count(const mpm_batch* b) { return b ? (int)b->order.size() : -1; }
+
+int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph) {
+  if (!b) return MPM_ERR_ARG;
+  if (nsteps <= 0) return MPM_OK;
+  cudaSetDevice(b->device);
+  int r = ensure_committed(b);
+  if (r) return r;
+  if (b->order.empty()) return MPM_OK;
+  BProfScope ps(b);
+  if (!use_graph) {
+    for (int i = 0; i < nsteps; ++i)
+      if ((r = enqueue_step(b))) return r;
+    return MPM_OK;
+  }
+  if (b->prof.on) {
+    // one graph over all the steps, with event nodes around every kernel
+    drop_graph(b);
+    b->prof.nrec = 0;
+    b->prof.next = 0;
+    cudaGraphExec_t ge = nullptr;
+    if ((r = capture(b, nsteps, &ge))) return r;
+    cudaError_t e = cudaGraphLaunch(ge, b->stream);
+    cudaGraphExecDestroy(ge);
+    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
+    return MPM_OK;
+  }
+  // one graph of one step per buffer parity (the step swaps the two particle
+  // buffer sets, so the graph captured from either set is replayed alternately)
+  for (int i = 0; i < nsteps; ++i) {
+    const int par = b->A.x == b->set0_x ? 0 : 1;
+    if (!b->graph[par]) {
+      cudaGraphExec_t ge = nullptr;
+      if ((r = capture(b, 1, &ge))) return r;
+      b->graph[par] = ge;
+      std::swap(b->A, b->B);  // capture swapped the host handles; the launch below does the step
+    }
+    BCK(cudaGraphLaunch(b->graph[par], b->stream));
+    std::swap(b->A, b->B);
+  }
+  return MPM_OK;
+}
+
+int mpm_batch_sync(mpm_batch* b) {
+  if (!b) return MPM_ERR_ARG;
+  BCK(cudaStreamSynchronize(b->stream));
+  if (b->A.nscene == 0) return MPM_OK;
+  std::vector<SceneState> s((size_t)b->A.nscene);
+  BCK(cudaMemcpy(s.data(), b->A.sst, sizeof(SceneState) * s.size(), cudaMemcpyDeviceToHost));
+  for (auto& x : s)
+    if (x.status & ST_NONFINITE) return berr(b, MPM_ERR_NONFINITE, "non-finite particle state");
+  return MPM_OK;
+}
+
+int mpm_batch_time_steps(mpm_batch* b, int nsteps, int use_graph, double* ms) {
+  if (!b || !ms) return MPM_ERR_ARG;
+  int r = ensure_committed(b);
+  if (r) return r;
+  cudaEvent_t e0, e1;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  BCK(cudaStreamSynchronize(b->stream));
+  BCK(cudaEventRecord(e0, b->stream));
+  r = mpm_batch_run(b, nsteps, use_graph);
+  BCK(cudaEventRecord(e1, b->stream));
+  BCK(cudaEventSynchronize(e1));
+  float f = 0;
+  cudaEventElapsedTime(&f, e0, e1);
+  *ms = f;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (b->prof.on) prof_harvest(&b->prof, b->stream);
+  return r;
+}
+
+int mpm_batch_scene_scalars(mpm_batch* b, int id, double* o) {
+  if (!b || !o) return MPM_ERR_ARG;
+  HostScene* h = find(b, id);
+  if (!h) return berr(b, MPM_ERR_ARG, "no scene %d", id);
+  memset(o, 0, sizeof(double) * MPM_NSCALARS);
+  SceneState s = h->st;
+  if (h->resident && !b->dirty) {
+    BCK(cudaStreamSynchronize(b->stream));
+    BCK(cudaMemcpy(&s, b->A.sst + h->index, sizeof s, cudaMemcpyDeviceToHost));
+  }
+  o[0] = s.istep; o[1] = s.time; o[2] = s.dt; o[3] = s.ke; o[4] = s.ie;
+  o[5] = s.mom[0]; o[6] = s.mom[1]; o[7] = s.mom[2]; o[8] = s.ke_prev;
+  o[9] = (double)h->nn; o[10] = (double)h->np; o[11] = h->su.g.cutoff; o[12] = h->su.g.dcell;
+  o[13] = (double)s.active_nodes; o[14] = s.status;
+  return MPM_OK;
+}
+
+int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
+  if (!b || !out) return MPM_ERR_ARG;
+  int r = ensure_committed(b);
+  if (r) return r;
+  HostScene* h = find(b, id);
+  if (!h) return berr(b, MPM_ERR_ARG, "no scene %d", id);
+  BCK(cudaStreamSynchronize(b->stream));
+  const BState& s = b->A;
+  const long long NP = s.NP, np = h->np, p0 = h->p0;
+  const int nc = mpm_field_components(field);
+  if (field == MPM_G_MG || field == MPM_G_PX || field == MPM_G_FX) {
+    const double* src = field == MPM_G_MG ? s.mg : (field == MPM_G_PX ? s.px : s.fx);
+    for (int a = 0; a < nc; ++a)
+      BCK(cudaMemcpy(out + a * h->nn, src + a * s.NN + h->n0, sizeof(double) * h->nn, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+  }
+  if (field == MPM_C_MG || field == MPM_C_PX) {
+    if (h->su.g.shape != 3) return berr(b, MPM_ERR_ARG, "no auxiliary grid (not SGMP)");
+    const double* src = field == MPM_C_MG ? s.cmg : s.cpx;
+    for (int a = 0; a < nc; ++a)
+      BCK(cudaMemcpy(out + a * h->ncell, src + a * s.NC + h->c0, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+  }
+  std::vector<int> orig((size_t)np);
+  BCK(cudaMemcpy(orig.data(), s.orig + p0, sizeof(int) * np, cudaMemcpyDeviceToHost));
+  std::vector<double> dbuf((size_t)np);
+  std::vector<float> fbuf((size_t)np);
+  auto fetch_d = [&](const double* base, int a) -> cudaError_t {
+    cudaError_t e = cudaMemcpy(dbuf.data(), base + a * NP + p0, sizeof(double) * np, cudaMemcpyDeviceToHost);
+    for (long long i = 0; i < np; ++i) out[a * np + orig[i]] = dbuf[i];
+    return e;
+  };
+  auto fetch_f = [&](const float* base, int a) -> cudaError_t {
+    cudaError_t e = cudaMemcpy(fbuf.data(), base + a * NP + p0, sizeof(float) * np, cudaMemcpyDeviceToHost);
+    for (long long i = 0; i < np; ++i) out[a * np + orig[i]] = fbuf[i];
+    return e;
+  };
+  for (int a = 0; a < nc; ++a) {
+    cudaError_t e = cudaSuccess;
+    switch (field) {
+      case MPM_P_XP: e = fetch_d(s.x, a); break;
+      case MPM_P_XX: e = fetch_d(s.xx, a); break;
+      case MPM_P_VXP: e = fetch_d(s.v, a); break;
+      case MPM_P_FXP: e = fetch_d(s.fxp, a); break;
+      case MPM_P_MASS: e = fetch_d(s.mass, a); break;
+      case MPM_P_IE: e = fetch_d(s.ie, a); break;
+      case MPM_P_VOL: e = fetch_f(s.vol, a); break;
+      case MPM_P_SIG_Y: e = fetch_f(s.sig_y, a); break;
+      case MPM_P_SM: e = fetch_f(s.sm, a); break;
+      case MPM_P_SEQV: e = fetch_f(s.seqv, a); break;
+      case MPM_P_SD: e = fetch_f(s.sd, a); break;
+      case MPM_P_FP:
+        if (!b->any_uvfp) return berr(b, MPM_ERR_ARG, "deformation gradient is not tracked");
+        e = fetch_f(s.fp, a);
+        break;
+      case MPM_P_EPEFF: e = fetch_f(s.epeff, a); break;
+      case MPM_P_CELSIUS: e = fetch_f(s.celsius, a); break;
+      case MPM_P_DMG: e = fetch_f(s.dmg, a); break;
+      case MPM_P_LT: e = fetch_f(s.lt, a); break;
+      case MPM_P_CP: e = fetch_f(s.cp, a); break;
+      case MPM_P_Q: e = fetch_f(s.q, a); break;
+      case MPM_P_FAILURE: {
+        std::vector<uint8_t> u((size_t)np);
+        e = cudaMemcpy(u.data(), s.failure + p0, np, cudaMemcpyDeviceToHost);
+        for (long long i = 0; i < np; ++i) out[orig[i]] = u[i];
+        break;
+      }
+      default:
+        return berr(b, MPM_ERR_ARG, "field %d is not available for batched scenes", field);
+    }
+    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+  }
+  return MPM_OK;
+}
+
+int mpm_batch_set_blocks(mpm_batch* b, int pblock, int nblock) {
+  if (!b) return MPM_ERR_ARG;
+  auto ok = [](int x) { return x == 0 || (x >= 32 && x <= 512 && (x % 32) == 0); };
+  if (!ok(pblock) || !ok(nblock)) return berr(b, MPM_ERR_ARG, "block sizes must be multiples of 32 in 32..512");
+  if (pblock) b->pblock = pblock;
+  if (nblock) b->nblock = nblock;
+  drop_graph(b);
+  return MPM_OK;
+}
+
+int mpm_batch_profile_enable(mpm_batch* b, int on) {
+  if (!b) return MPM_ERR_ARG;
+  if (b->prof.on) prof_harvest(&b->prof, b->stream);
+  prof_reset(&b->prof);
+  b->prof.on = on != 0;
+  drop_graph(b);
+  return MPM_OK;
+}
+
+int mpm_batch_kernel_stats(mpm_batch* b, int k, char* name, int namelen, int64_t* launches, double* total_ms) {
+  if (!b || k < 0 || k >= K_COUNT) return MPM_ERR_ARG;
+  prof_harvest(&b->prof, b->stream);
+  if (name && namelen > 0) snprintf(name, (size_t)namelen, "%s", kKernelNames[k]);
+  if (launches) *launches = b->prof.n[k];
+  if (total_ms) *total_ms = b->prof.ms[k];
+  return MPM_OK;
+}
+
+}  // extern "C"
+
+namespace mpm {
+
+HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code) {
+  *code = MPM_OK;
+  if (!d) {
+    *code = MPM_ERR_ARG;
+    err = "deck is NULL";
+    return nullptr;
+  }
+  if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM)) {
+    *code = MPM_ERR_UNSUPPORTED;
+    err = "contact and TLMPM are outside the explicit-step path";
+    return nullptr;
+  }
+  if (d->nb_component != 1 || d->nb_particle <= 0 || d->nb_body <= 0) {
+    *code = d->nb_component != 1 ? MPM_ERR_UNSUPPORTED : MPM_ERR_ARG;
+    err = d->nb_component != 1 ? "only one grid component" : "deck defines no particles / bodies";
+    return nullptr;
+  }
+  HostScene* h = new HostScene();
+  int r = scene_setup(d, h->su);
+  if (r) {
+    *code = r;
+    err = h->su.err;
+    delete h;
+    return nullptr;
+  }
+  h->steps = steps > 0 ? steps : 0x7fffffff;
+  h->np = d->nb_particle;
+  h->nn = h->su.g.nn;
+  h->ncell = h->su.g.ncell;
+  h->drdamp = !!(d->flags & MPM_F_DRDAMP);
+  h->mass.assign(d->mass, d->mass + h->np);
+  h->x.assign(d->xp, d->xp + 3 * h->np);
+  h->v.assign(d->vxp, d->vxp + 3 * h->np);
+  h->fxp.assign(d->fxp, d->fxp + 3 * h->np);
+  h->body_local.assign((size_t)h->np, 0);
+  for (int bo = 0; bo < d->nb_body; ++bo)
+    for (long long p = d->bodies[bo].par_begin; p < d->bodies[bo].par_end; ++p) h->body_local[p] = (uint16_t)bo;
+  return h;
+}
+
+void scene_free(HostScene* h) { delete h; }
+
+long long scene_np(const HostScene* h) { return h->np; }
+
+long long scene_device_bytes(const HostScene* h) {
+  return scene_bytes(h->np, h->nn, h->ncell, h->su.g.shape == 3, h->su.g.uvfp, h->su.g.has_jc);
+}
+
+int batch_insert(mpm_batch* b, HostScene* h, int* scene_id) {
+  h->id = b->next_id++;
+  h->resident = false;
+  b->order.push_back(h);
+  b->by_id[h->id] = h;
+  b->dirty = true;
+  if (scene_id) *scene_id = h->id;
+  return MPM_OK;
+}
+
+int batch_progress(mpm_batch* b, std::vector<BatchProgress>& out) {
+  out.clear();
+  int r = ensure_committed(b);
+  if (r) return r;
+  if (b->order.empty()) return MPM_OK;
+  std::vector<SceneState> s((size_t)b->A.nscene);
+  BCK(cudaStreamSynchronize(b->stream));
+  BCK(cudaMemcpy(s.data(), b->A.sst, sizeof(SceneState) * s.size(), cudaMemcpyDeviceToHost));
+  for (HostScene* h : b->order) {
+    const SceneState& t = s[h->index];
+    out.push_back(BatchProgress{h->id, t.istep, h->steps, h->np, t.status});
+  }
+  return MPM_OK;
+}
+
+long long batch_particles(const mpm_batch* b) {
+  long long n = 0;
+  for (const HostScene* h : b->order) n += h->np;
+  return n;
+}
+
+void batch_remaining(mpm_batch*, const std::vector<BatchProgress>& p, int* min_left) {
+  int m = 0;
+  bool first = true;
+  for (const BatchProgress& q : p) {
+    int left = q.target - q.istep;
+    if (left <= 0) continue;
+    if (first || left < m) m = left;
+    first = false;
+  }
+  *min_left = m;
+}
+
+}  // namespace mpm

@@ -1,0 +1,98 @@
+// mpm_batch.cuh -- the batched mixed-precision step: many independent scenes
+// advanced together by one set of kernels indexed by per-scene offset tables.
+//
+// Layout (all scenes concatenated; scene s owns the ranges in its Scene entry):
+//   particles, kept physically sorted by (scene, cell) at the start of every
+//   step (stable sort of the previous order, then a permutation of every
+//   field), component-major over the total particle count NP:
+//     FP64: x[3], xx[3], v[3], fxp[3], mass, ie
+//     FP32: vol, sig_y, sm, seqv, sd[6], fp[9], epeff, celsius, dmg, lt, cp, q
+//     per step (written by the permutation): cell (scene-local cell, -1
+//     outside), off[3] (offset in the cell, in cells), SGMP dual cell, nearest
+//     node, xxn[3], xn[3]; body, scene, orig (scene-local input index)
+//   grid nodes concatenated: FP64 mg, px[3], fx[3], vg[3]; fix, bd, node scene
+//   SGMP centre nodes (one per cell) concatenated: FP64 cmg, cpx[3], cfext[3],
+//     cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3]
+//   sort keys: scene s owns keys [k0, k0 + ncell + 1), the last one collects
+//     particles outside its grid; seg[k] = end of key k's particle range.
+//
+// Transfers particle -> grid are node-centric gathers over the neighbouring
+// cells' particle ranges (fixed order: cells z, y, x; particles in storage
+// order), FP32 contributions summed per source cell and accumulated in FP64:
+// deterministic, no atomics, and the same for a scene alone or in a batch.
+// Transfers grid -> particle are particle-centric with shape functions
+// evaluated on the fly in FP32.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mpm_gpu_internal.cuh"
+
+namespace mpm {
+namespace bm {
+
+struct Scene {
+  long long p0, np;  // particles
+  long long n0, nn;  // grid nodes
+  long long k0, nk;  // sort keys (ncell + 1)
+  long long c0, nc;  // SGMP centre nodes
+  long long r0, nr;  // reduction chunks
+  int NGx, NGy, NGz, NGxy, NCx, NCy, NCz, NCxy, CNCx, CNCy, CNCz, CNCxy, CNC;
+  int shape, usf, musl, uvfp, qload, qdamp, gravity, drdamp, has_jc;
+  int fixs[6];
+  int mat0, nmat;
+  double span0[3], span1[3], dcell, idcell, cutoff, iJacobi, iJacobi4;
+  double dtscale, qload_time, damp_factor, bq1, bq2;
+};
+
+struct SceneState {
+  int istep;
+  int active;  // 0: the scene is parked (no work this step)
+  double time, dt, ke, ie, mom[3], ke_prev, max_vp, depeff_carry;
+  unsigned long long active_nodes;
+  unsigned status;
+  unsigned pad_;
+};
+
+struct BState {
+  long long NP, NN, NK, NC, NR;
+  int nscene;
+  int any_uvfp, any_sgmp, any_jc;
+  // particles (A = current, B = permutation target)
+  double *x, *xx, *v, *fxp, *mass, *ie;
+  float *vol, *sig_y, *sm, *seqv, *sd, *fp, *epeff, *celsius, *dmg, *lt, *cp, *q;
+  uint8_t* failure;
+  uint16_t *body, *scene;
+  int* orig;
+  // per-step derived (written by the permutation)
+  int *cell, *dual, *inode;
+  float *off, *xxn, *xn;
+  float* fs;  // force staging [9][NP]: sigma*vol (xx, yy, zz, xy, yz, xz), fext (3)
+  // sort
+  unsigned *key, *key_sorted;
+  int *val, *perm, *seg;
+  // grid
+  double *mg, *px, *fx, *vg, *ag;  // ag = fx / mg after the integration
+  uint8_t *fix, *bd;
+  uint16_t* node_scene;
+  // SGMP centre grid
+  double *cmg, *cpx, *cfext, *cfint, *co, *cw, *cdefp, *cvx, *cax;
+  uint16_t* cscene;
+  // Johnson-Cook depeff carry (indexed by scene particle range + orig)
+  int *setter, *setter_scan;
+  double *dep, *jc_aux;
+  uint8_t* deferred;
+  // reductions
+  double* red_part;  // [6][NR]
+  uint16_t* rscene;  // chunk -> scene
+  Scene* scenes;
+  SceneState* sst;
+  DevMaterial* mats;
+  DevBody* bodies;   // gravp; mat = global material index
+};
+
+constexpr int kChunk = 2048;  // particles per reduction chunk
+
+}  // namespace bm
+}  // namespace mpm

@@ -1,0 +1,38 @@
+// mpm_batch_host.h -- host-side access to a batch for the serving runtime
+// (internal to libmpm3d_gpu).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "mpm3d_gpu.h"
+
+namespace mpm {
+
+struct HostScene;
+// stage a scene from a deck on any thread (nullptr + code/err on failure)
+HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code);
+void scene_free(HostScene* h);
+long long scene_np(const HostScene* h);
+long long scene_device_bytes(const HostScene* h);
+// hand a staged scene to a batch (the batch owns it from then on)
+int batch_insert(mpm_batch* b, HostScene* h, int* scene_id);
+
+struct BatchProgress {
+  int id;         // scene id
+  int istep;      // steps done
+  int target;     // steps requested
+  long long np;   // particles
+  unsigned status;
+};
+
+// progress of every resident scene, read from the device in one copy
+// (synchronises the batch stream)
+int batch_progress(mpm_batch* b, std::vector<BatchProgress>& out);
+// particles of all resident scenes
+long long batch_particles(const mpm_batch* b);
+// particle-steps still to run over the resident scenes, and the smallest
+// number of steps until one of them finishes (0 when none is resident)
+void batch_remaining(mpm_batch* b, const std::vector<BatchProgress>& p, int* min_left);
+
+}  // namespace mpm

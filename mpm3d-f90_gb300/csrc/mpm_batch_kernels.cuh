@@ -1,0 +1,1059 @@
+// mpm_batch_kernels.cuh -- kernels of the batched mixed-precision step (see
+// mpm_batch.cuh for the layout). FP32 particle math, FP64 grid accumulation.
+#pragma once
+
+#include "mpm_batch.cuh"
+#include "mpm_kernels.cuh"
+
+namespace mpm {
+namespace bm {
+
+__device__ __forceinline__ long long btid() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
+
+__device__ __forceinline__ bool scene_live(const BState& b, int s) { return b.sst[s].active != 0; }
+
+// local node (jx, jy, jz) of a global node index
+__device__ __forceinline__ void node_xyz(const Scene& sc, long long ln, int& jx, int& jy, int& jz) {
+  jz = (int)(ln / sc.NGxy);
+  int rem = (int)(ln - (long long)jz * sc.NGxy);
+  jy = rem / sc.NGx;
+  jx = rem - jy * sc.NGx;
+}
+
+// -------------------------------------------------------------- 1-D shapes
+// Offsets are node index minus particle cell index (t) or the particle's
+// position relative to the node in cells (r); derivatives are per cell.
+__device__ __forceinline__ void lin1(int t, float off, float& w, float& d) {
+  w = t ? off : 1.f - off;
+  d = t ? 1.f : -1.f;
+}
+__device__ __forceinline__ void gimp1(float r, float& w, float& d) { gimp_1d<float>(r, w, d); }
+__device__ __forceinline__ void bsp1(int t, float off, float& w, float& d) {
+  // NShape_Bspline pieces (Grid.f90:927-962) with r = off * 0.2 + 0.4
+  float r = off * 0.2f + 0.4f;
+  if (t < 0) {
+    float a = 3.f - 5.f * r;
+    w = 0.5f * a * a;
+    d = (5.f * r - 3.f) * 5.f * 0.2f;
+  } else if (t == 0) {
+    w = -25.f * r * r + 25.f * r - 5.5f;
+    d = (-50.f * r + 25.f) * 0.2f;
+  } else {
+    float a = 5.f * r - 2.f;
+    w = 0.5f * a * a;
+    d = (5.f * r - 2.f) * 5.f * 0.2f;
+  }
+}
+
+// weight and gradient (per cell) of node j for a particle in cell c
+__device__ __forceinline__ bool weight3(int shape, const int c[3], const int j[3], const float off[3], float& w,
+                                        float g[3]) {
+  float wd[3], dd[3];
+  for (int a = 0; a < 3; ++a) {
+    int t = j[a] - c[a];
+    if (shape == 0) {
+      if (t < 0 || t > 1) return false;
+      lin1(t, off[a], wd[a], dd[a]);
+    } else if (shape == 1) {
+      gimp1((float)(c[a] - j[a]) + off[a], wd[a], dd[a]);
+      if (wd[a] == 0.f) return false;
+    } else {
+      if (t < -1 || t > 1) return false;
+      bsp1(t, off[a], wd[a], dd[a]);
+    }
+  }
+  w = wd[0] * wd[1] * wd[2];
+  g[0] = dd[0] * wd[1] * wd[2];
+  g[1] = wd[0] * dd[1] * wd[2];
+  g[2] = wd[0] * wd[1] * dd[2];
+  return true;
+}
+
+// neighbour cell window of a node: particles in cells j+lo .. j+hi reach it
+__device__ __forceinline__ void cell_window(int shape, int& lo, int& hi) {
+  if (shape == 0) { lo = -1; hi = 0; }
+  else if (shape == 1) { lo = -2; hi = 1; }
+  else { lo = -1; hi = 1; }
+}
+
+// influence node offsets of a particle in its cell (per direction)
+__device__ __forceinline__ int node_offsets(int shape, float off, int t[4]) {
+  if (shape == 0) { t[0] = 0; t[1] = 1; return 2; }
+  if (shape == 2) { t[0] = -1; t[1] = 0; t[2] = 1; return 3; }
+  int n = 0;  // cpGIMP: quarter rule of FindInflNode
+  if (off < 0.25f) t[n++] = -1;
+  t[n++] = 0;
+  t[n++] = 1;
+  if (off > 0.75f) t[n++] = 2;
+  return n;
+}
+
+__device__ __forceinline__ void key_range(const BState& b, long long key, int& i0, int& i1) {
+  i0 = key == 0 ? 0 : b.seg[key - 1];
+  i1 = b.seg[key];
+}
+
+// ------------------------------------------------------------- begin step
+__global__ void kb_begin(BState b, const int* target) {
+  int s = (int)btid();
+  if (s >= b.nscene) return;
+  SceneState& t = b.sst[s];
+  t.active = t.istep < target[s] ? 1 : 0;
+  if (!t.active) return;
+  t.istep = t.istep + 1;
+  t.time = t.time + t.dt;
+  t.ie = 0.0;
+  t.active_nodes = 0;
+}
+
+// SGMP dual (cell-centre) cell of a position, CenterInWhichCell
+// (Grid.f90:157-190): the flat index of the per-direction truncations, valid
+// when it lies in 0..CNC-1. Like the reference, a position within half a cell
+// of the upper grid faces yields a per-direction index past the last dual
+// cell, and the flat index then continues into the next row / layer.
+__device__ __forceinline__ long long dual_cell(const Scene& sc, const double x[3]) {
+  long long d = 0;
+  int dc[3];
+  for (int a = 0; a < 3; ++a) dc[a] = (int)((x[a] - sc.span0[a]) * sc.idcell - 0.5);
+  d = ((long long)dc[2] * sc.CNCy + dc[1]) * sc.CNCx + dc[0];
+  return (d >= 0 && d < sc.CNC) ? d : -1;
+}
+
+// ------------------------------------------------------------------ keys
+// Sort key of a particle: its scene's key base plus its cell (linear, GIMP,
+// B-spline) or its dual cell (SGMP); the scene's last key collects the
+// particles outside the grid.
+__global__ void kb_keys(BState b) {
+  long long i = btid();
+  if (i >= b.NP) return;
+  const long long NP = b.NP;
+  const Scene& sc = b.scenes[b.scene[i]];
+  double x[3] = {b.x[i], b.x[NP + i], b.x[2 * NP + i]};
+  long long c = -1;
+  if (sc.shape == 3) {
+    c = dual_cell(sc, x);
+  } else {
+    int cc[3];
+    bool in = true;
+    for (int a = 0; a < 3; ++a) {
+      if (x[a] < sc.span0[a] || x[a] > sc.span1[a]) in = false;
+      double u = (x[a] - sc.span0[a]) * sc.idcell;
+      cc[a] = (int)u;
+    }
+    if (in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz)
+      c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+  }
+  long long key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
+  b.key[i] = (unsigned)key;
+  b.val[i] = (int)i;
+  atomicAdd(&b.seg[key], 1);
+}
+
+// ---------------------------------------------------- permutation + derived
+// dst[i] = src[perm[i]] for every persistent particle field, then the per-step
+// derived data of the particle at its new position (ParticleInitial,
+// update_step.f90:408-453, in FP32 form).
+__global__ void kb_permute(BState src, BState dst) {
+  long long i = btid();
+  if (i >= src.NP) return;
+  const long long NP = src.NP;
+  const long long j = src.perm[i];
+  for (int a = 0; a < 3; ++a) {
+    dst.x[a * NP + i] = src.x[a * NP + j];
+    dst.v[a * NP + i] = src.v[a * NP + j];
+    dst.fxp[a * NP + i] = src.fxp[a * NP + j];
+  }
+  dst.mass[i] = src.mass[j];
+  dst.ie[i] = src.ie[j];
+  dst.vol[i] = src.vol[j];
+  dst.sig_y[i] = src.sig_y[j];
+  dst.sm[i] = src.sm[j];
+  dst.seqv[i] = src.seqv[j];
+  for (int a = 0; a < 6; ++a) dst.sd[a * NP + i] = src.sd[a * NP + j];
+  if (src.any_uvfp)
+    for (int a = 0; a < 9; ++a) dst.fp[a * NP + i] = src.fp[a * NP + j];
+  dst.epeff[i] = src.epeff[j];
+  dst.celsius[i] = src.celsius[j];
+  dst.dmg[i] = src.dmg[j];
+  dst.lt[i] = src.lt[j];
+  dst.cp[i] = src.cp[j];
+  dst.q[i] = src.q[j];
+  dst.failure[i] = src.failure[j];
+  dst.body[i] = src.body[j];
+  const int s = src.scene[j];
+  dst.scene[i] = (uint16_t)s;
+  dst.orig[i] = src.orig[j];
+  // derived
+  const Scene& sc = src.scenes[s];
+  double x[3] = {dst.x[i], dst.x[NP + i], dst.x[2 * NP + i]};
+  int cc[3];
+  bool in = true;
+  float off[3];
+  for (int a = 0; a < 3; ++a) {
+    if (x[a] < sc.span0[a] || x[a] > sc.span1[a]) in = false;
+    double u = (x[a] - sc.span0[a]) * sc.idcell;
+    cc[a] = (int)u;
+    off[a] = (float)(u - (double)cc[a]);
+    dst.off[a * NP + i] = off[a];
+  }
+  int c = -1;
+  if (in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz) c = (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+  dst.cell[i] = c;
+  if (sc.shape == 3) {
+    // dual (cell-centre) grid: CenterInWhichCell and the nearest node
+    int nd[3];
+    for (int a = 0; a < 3; ++a) nd[a] = (int)((x[a] - sc.span0[a]) * sc.idcell + 0.5);
+    dst.dual[i] = (int)dual_cell(sc, x);
+    bool nin = nd[0] >= 0 && nd[0] < sc.NGx && nd[1] >= 0 && nd[1] < sc.NGy && nd[2] >= 0 && nd[2] < sc.NGz;
+    int ln = nin ? (nd[2] * sc.NGy + nd[1]) * sc.NGx + nd[0] : -1;
+    dst.inode[i] = ln;
+    int bd = ln >= 0 ? src.bd[sc.n0 + ln] : 0;
+    for (int a = 0; a < 3; ++a) {
+      double u = (x[a] - sc.span0[a]) * sc.idcell;
+      float xxn = (float)((u - (double)nd[a]) * 2.0);
+      if ((bd >> (2 * a)) & 3) xxn = xxn > 0.f ? 1.f : (xxn < 0.f ? -1.f : 0.f);
+      dst.xxn[a * NP + i] = xxn;
+      dst.xn[a * NP + i] = off[a] * 2.f - 1.f;
+    }
+  }
+}
+
+// ------------------------------------------------- node-centric gathers
+// P2G of mass and momentum for linear / GIMP / B-spline scenes
+// (GridMomentumInitial); SGMP scenes take their values from the centre grid.
+__device__ __forceinline__ void node_finish(BState& b, const Scene& sc, long long n, int bc, int vel) {
+  const long long NN = b.NN;
+  if (bc) {
+    uint8_t f = b.fix[n];
+    for (int a = 0; a < 3; ++a)
+      if (f & (1 << a)) {
+        b.px[a * NN + n] = 0.0;
+        b.fx[a * NN + n] = 0.0;
+      }
+  }
+  if (vel) {
+    double m = b.mg[n];
+    if (m > sc.cutoff)
+      for (int a = 0; a < 3; ++a) b.vg[a * NN + n] = b.px[a * NN + n] / m;
+  }
+}
+
+__global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
+  long long n = btid();
+  bool act = false;
+  int s = -1;
+  if (n < b.NN) {
+    s = b.node_scene[n];
+    if (scene_live(b, s)) {
+      const Scene& sc = b.scenes[s];
+      const long long NN = b.NN, NP = b.NP;
+      double M = 0, P0 = 0, P1 = 0, P2 = 0;
+      int j[3];
+      node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
+      if (sc.shape == 3) {
+        // centre nodes -> node: adjacent cells in ascending order, cut-off on the cell mass
+        const long long nc0 = sc.c0;
+        for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
+          if (cz < 0 || cz >= sc.NCz) continue;
+          for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
+            if (cy < 0 || cy >= sc.NCy) continue;
+            for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
+              if (cx < 0 || cx >= sc.NCx) continue;
+              long long c = nc0 + (cz * sc.NCy + cy) * sc.NCx + cx;
+              double cm = b.cmg[c];
+              if (!(cm > sc.cutoff)) continue;
+              M += 0.125 * cm;
+              P0 += 0.125 * b.cpx[c];
+              P1 += 0.125 * b.cpx[b.NC + c];
+              P2 += 0.125 * b.cpx[2 * b.NC + c];
+            }
+          }
+        }
+      } else {
+        int lo, hi;
+        cell_window(sc.shape, lo, hi);
+        for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
+          for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
+            for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
+              int i0, i1;
+              key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
+              if (i0 == i1) continue;
+              const int c[3] = {cx, cy, cz};
+              float m = 0, p0 = 0, p1 = 0, p2 = 0;
+              for (int i = i0; i < i1; ++i) {
+                float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+                float w, g[3];
+                if (!weight3(sc.shape, c, j, off, w, g)) continue;
+                float wm = w * (float)b.mass[i];
+                m += wm;
+                p0 += wm * (float)b.v[i];
+                p1 += wm * (float)b.v[NP + i];
+                p2 += wm * (float)b.v[2 * NP + i];
+              }
+              M += m;
+              P0 += p0;
+              P1 += p1;
+              P2 += p2;
+            }
+      }
+      b.mg[n] = M;
+      b.px[n] = P0;
+      b.px[NN + n] = P1;
+      b.px[2 * NN + n] = P2;
+      act = M > 0.0;
+      node_finish(b, sc, n, bc_usf && sc.usf, vel_usf && sc.usf);
+    }
+  }
+  // per-scene active-node count: one atomic per (warp, scene) group
+  unsigned grp = __match_any_sync(0xffffffffu, s);
+  unsigned actg = __ballot_sync(0xffffffffu, act) & grp;
+  int lane = threadIdx.x & 31;
+  if (s >= 0 && actg && lane == __ffs(grp) - 1) atomicAdd(&b.sst[s].active_nodes, (unsigned long long)__popc(actg));
+}
+
+// SGMP: particles -> centre nodes. The centre node of cell q is corner k of
+// the dual cells q - kCorner[k]; a particle of such a dual cell contributes
+// with the SGNShape weight of that corner.
+__device__ __forceinline__ float sg_corner_weight(const BState& b, long long i, int k) {
+  const long long NP = b.NP;
+  float w = 0.125f;
+  for (int a = 0; a < 3; ++a) {
+    float xx = b.xxn[a * NP + i];
+    w *= kCorner[k][a] ? 1.f + xx : 1.f - xx;
+  }
+  return w;
+}
+
+// particle key range of the dual cell q - kCorner[k] (empty if it does not exist)
+__device__ __forceinline__ bool sg_dual_range(const BState& b, const Scene& sc, const int q[3], int k, int& i0,
+                                              int& i1) {
+  int d[3];
+  const int CN[3] = {sc.CNCx, sc.CNCy, sc.CNCz};
+  for (int a = 0; a < 3; ++a) {
+    d[a] = q[a] - kCorner[k][a];
+    if (d[a] < 0 || d[a] >= CN[a]) return false;
+  }
+  key_range(b, sc.k0 + ((long long)d[2] * sc.CNCy + d[1]) * sc.CNCx + d[0], i0, i1);
+  return i0 < i1;
+}
+
+__global__ void kb_sg_centre_mass(BState b, int momentum_only) {
+  long long c = btid();
+  if (c >= b.NC) return;
+  int s = b.cscene[c];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  const long long NP = b.NP, NC = b.NC;
+  long long lc = c - sc.c0;
+  int q[3];
+  q[2] = (int)(lc / sc.NCxy);
+  int rem = (int)(lc - (long long)q[2] * sc.NCxy);
+  q[1] = rem / sc.NCx;
+  q[0] = rem - q[1] * sc.NCx;
+  double M = 0, P0 = 0, P1 = 0, P2 = 0;
+  for (int k = 0; k < 8; ++k) {
+    int i0, i1;
+    if (!sg_dual_range(b, sc, q, k, i0, i1)) continue;
+    float m = 0, p0 = 0, p1 = 0, p2 = 0;
+    for (int i = i0; i < i1; ++i) {
+      float wm = sg_corner_weight(b, i, k) * (float)b.mass[i];
+      m += wm;
+      p0 += wm * (float)b.v[i];
+      p1 += wm * (float)b.v[NP + i];
+      p2 += wm * (float)b.v[2 * NP + i];
+    }
+    M += m;
+    P0 += p0;
+    P1 += p1;
+    P2 += p2;
+  }
+  if (!momentum_only) b.cmg[c] = M;
+  b.cpx[c] = P0;
+  b.cpx[NC + c] = P1;
+  b.cpx[2 * NC + c] = P2;
+}
+
+// -------------------------------------------------------------- stress
+// ParticleStressUpdate + Constitution for one particle (FP32). The stress pass
+// runs twice per step: before the force transfer for USF scenes (usf_pass 1)
+// and after the position update for USL / MUSL scenes (usf_pass 0).
+__global__ void kb_stress(BState b, int usf_pass) {
+  using P = PMixed;
+  using R = float;
+  long long i = btid();
+  if (i >= b.NP) return;
+  const int s = b.scene[i];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  if (sc.usf != usf_pass) return;
+  const long long NP = b.NP, NN = b.NN;
+  const long long o = sc.p0 + b.orig[i];  // position in the reference processing order
+  if (sc.has_jc) {
+    b.setter[o] = -1;
+    b.deferred[i] = 0;
+  }
+  R de[6] = {0, 0, 0, 0, 0, 0}, vort[3] = {0, 0, 0}, deFp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  if (sc.shape == 3) {
+    int d = b.dual[i];
+    if (d < 0) return;
+    int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+    float xx[3] = {b.xxn[i], b.xxn[NP + i], b.xxn[2 * NP + i]};
+    for (int k = 0; k < 8; ++k) {
+      int oc[3] = {kCorner[k][0], kCorner[k][1], kCorner[k][2]};
+      long long c = sc.c0 + ((dz + oc[2]) * sc.NCy + (dy + oc[1])) * sc.NCx + (dx + oc[0]);
+      float w = 0.125f;
+      for (int a = 0; a < 3; ++a) w *= oc[a] ? 1.f + xx[a] : 1.f - xx[a];
+      const long long NC = b.NC;
+      for (int a = 0; a < 6; ++a) de[a] += (R)b.co[a * NC + c] * w;
+      for (int a = 0; a < 3; ++a) vort[a] += (R)b.cw[a * NC + c] * w;
+      for (int a = 0; a < 9; ++a) deFp[a / 3][a % 3] += w * (R)b.cdefp[a * NC + c];
+    }
+  } else {
+    const int cl = b.cell[i];
+    if (cl < 0) return;
+    int c[3];
+    c[2] = cl / sc.NCxy;
+    int rem = cl - c[2] * sc.NCxy;
+    c[1] = rem / sc.NCx;
+    c[0] = rem - c[1] * sc.NCx;
+    float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+    int t[3][4], nt[3];
+    for (int a = 0; a < 3; ++a) nt[a] = node_offsets(sc.shape, off[a], t[a]);
+    const float idc = (float)sc.idcell;
+    for (int az = 0; az < nt[2]; ++az)
+      for (int ay = 0; ay < nt[1]; ++ay)
+        for (int ax = 0; ax < nt[0]; ++ax) {
+          int j[3] = {c[0] + t[0][ax], c[1] + t[1][ay], c[2] + t[2][az]};
+          if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
+          long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
+          if (!(b.mg[n] > sc.cutoff)) continue;
+          float w, g[3];
+          if (!weight3(sc.shape, c, j, off, w, g)) continue;
+          float dx = g[0] * idc, dy = g[1] * idc, dz = g[2] * idc;
+          float v[3] = {(float)b.vg[n], (float)b.vg[NN + n], (float)b.vg[2 * NN + n]};
+          de[0] += dx * v[0];
+          de[1] += dy * v[1];
+          de[2] += dz * v[2];
+          de[3] += dy * v[2] + dz * v[1];
+          de[4] += dz * v[0] + dx * v[2];
+          de[5] += dx * v[1] + dy * v[0];
+          vort[0] += dy * v[2] - dz * v[1];
+          vort[1] += dz * v[0] - dx * v[2];
+          vort[2] += dx * v[1] - dy * v[0];
+          for (int a = 0; a < 3; ++a) {
+            deFp[a][0] += dx * v[a];
+            deFp[a][1] += dy * v[a];
+            deFp[a][2] += dz * v[a];
+          }
+        }
+  }
+  const SceneState& st = b.sst[s];
+  const R DT = (R)st.dt;
+  for (int a = 0; a < 6; ++a) de[a] *= DT;
+  for (int a = 0; a < 3; ++a) vort[a] = vort[a] * DT / 2.f;
+  for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < 3; ++k) deFp[a][k] *= DT;
+  R Fpn[3][3];
+  if (sc.uvfp) {
+    R F0[3][3];
+    for (int a = 0; a < 9; ++a) F0[a / 3][a % 3] = b.fp[a * NP + i];
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < 3; ++k) {
+        Fpn[a][k] = F0[a][k] + deFp[a][k] + deFp[a][0] * F0[0][k] + deFp[a][1] * F0[1][k] + deFp[a][2] * F0[2][k];
+        b.fp[(a * 3 + k) * NP + i] = Fpn[a][k];
+      }
+  }
+  PState<R> ps;
+  ps.vol = b.vol[i];
+  ps.epeff = b.epeff[i];
+  ps.sig_y = b.sig_y[i];
+  ps.seqv = b.seqv[i];
+  ps.lt = b.lt[i];
+  ps.celsius = b.celsius[i];
+  ps.ie = (R)b.ie[i];
+  ps.mass = (R)b.mass[i];
+  ps.dmg = b.dmg[i];
+  ps.cp = b.cp[i];
+  ps.sm = b.sm[i];
+  ps.q = b.q[i];
+  for (int a = 0; a < 6; ++a) ps.sd[a] = b.sd[a * NP + i];
+  ps.failure = b.failure[i] != 0;
+  const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
+  CResult<R> res;
+  constitution<P>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2, res);
+  if (res.negative_volume) atomicOr(&b.sst[s].status, (unsigned)ST_NEGATIVE_VOLUME);
+  if (!res.eos_ok) atomicOr(&b.sst[s].status, (unsigned)ST_BAD_EOS);
+  if (sc.has_jc) {
+    if (res.dep_set) {
+      b.setter[o] = (int)o;
+      b.dep[o] = (double)res.depeff;
+    }
+    b.deferred[i] = res.defer ? (uint8_t)res.tail : 0;
+    if (res.defer && res.tail == 7) {
+      b.jc_aux[i] = res.vold;
+      b.jc_aux[NP + i] = res.ieinc;
+      b.jc_aux[2 * NP + i] = res.dvol;
+      b.jc_aux[3 * NP + i] = res.smold;
+      b.jc_aux[4 * NP + i] = res.vol_;
+    }
+  }
+  b.vol[i] = ps.vol;
+  b.sm[i] = ps.sm;
+  b.seqv[i] = ps.seqv;
+  for (int a = 0; a < 6; ++a) b.sd[a * NP + i] = ps.sd[a];
+  b.sig_y[i] = ps.sig_y;
+  b.epeff[i] = ps.epeff;
+  b.ie[i] = (double)ps.ie;
+  b.cp[i] = ps.cp;
+  b.q[i] = ps.q;
+  b.celsius[i] = ps.celsius;
+  b.failure[i] = ps.failure ? 1 : 0;
+  if (!isfinite(ps.sm) || !isfinite(ps.ie)) atomicOr(&b.sst[s].status, (unsigned)ST_NONFINITE);
+  if (!sc.usf)
+    for (int a = 0; a < 3; ++a) b.x[a * NP + i] = b.xx[a * NP + i];
+}
+
+// Johnson-Cook tails waiting for the depeff carried from the previous particle
+// in the reference order (scene-local input order)
+__global__ void kb_depeff_apply(BState b, int usf_pass) {
+  using P = PMixed;
+  using R = float;
+  long long i = btid();
+  if (i >= b.NP) return;
+  const int tail = b.deferred[i];
+  if (tail == 0) return;
+  const int s = b.scene[i];
+  const Scene& sc = b.scenes[s];
+  if (!scene_live(b, s) || sc.usf != usf_pass) return;
+  const long long NP = b.NP;
+  const long long o = sc.p0 + b.orig[i];
+  int last = b.setter_scan[o];
+  R D = (R)(last >= sc.p0 && last <= o ? b.dep[last] : b.sst[s].depeff_carry);
+  const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
+  if (tail == 4) {
+    R den_ = (R)b.mass[i] / b.vol[i];
+    b.celsius[i] = b.celsius[i] + b.seqv[i] * D / den_ / (R)mt.specheat;
+    return;
+  }
+  Mm<R> m;
+  m.epeff_ = b.epeff[i];
+  m.sm = b.sm[i];
+  m.bqf = b.q[i];
+  m.iener = (R)b.ie[i];
+  m.seqv = b.seqv[i];
+  m.sd[0] = b.sd[i];
+  m.sd[1] = b.sd[NP + i];
+  m.sd[2] = b.sd[2 * NP + i];
+  m.sd[3] = b.sd[4 * NP + i];
+  m.sd[4] = b.sd[5 * NP + i];
+  m.sd[5] = b.sd[3 * NP + i];
+  m.vold = (R)b.jc_aux[i];
+  m.ieinc = (R)b.jc_aux[NP + i];
+  m.dvol = (R)b.jc_aux[2 * NP + i];
+  m.smold = (R)b.jc_aux[3 * NP + i];
+  m.vol_ = (R)b.jc_aux[4 * NP + i];
+  m.DMG = b.dmg[i];
+  m.oldDMG = m.DMG;
+  bool failure = b.failure[i] != 0;
+  R vol_store = m.vol_;
+  jc7_tail<P>(m, mt, failure, D, vol_store);
+  R den_ = (R)b.mass[i] / m.vol_;
+  b.celsius[i] = b.celsius[i] + m.seqv * D / den_ / (R)mt.specheat;
+  b.vol[i] = vol_store;
+  b.sm[i] = m.sm;
+  b.q[i] = m.bqf;
+  b.ie[i] = (double)m.iener;
+  b.epeff[i] = m.epeff_;
+  b.sd[i] = m.sd[0];
+  b.sd[NP + i] = m.sd[1];
+  b.sd[2 * NP + i] = m.sd[2];
+  b.sd[4 * NP + i] = m.sd[3];
+  b.sd[5 * NP + i] = m.sd[4];
+  b.sd[3 * NP + i] = m.sd[5];
+  b.failure[i] = failure ? 1 : 0;
+}
+
+__global__ void kb_depeff_carry(BState b, int usf_pass) {
+  int s = (int)btid();
+  if (s >= b.nscene) return;
+  const Scene& sc = b.scenes[s];
+  if (!sc.has_jc || !scene_live(b, s) || sc.np == 0 || sc.usf != usf_pass) return;
+  int last = b.setter_scan[sc.p0 + sc.np - 1];
+  if (last >= sc.p0 && last < sc.p0 + sc.np) b.sst[s].depeff_carry = b.dep[last];
+}
+
+// ------------------------------------------------------------ force input
+// external force (QuLo ramp, Damp, gravity; update_step.f90:889-903) and
+// sigma * vol, staged per particle in FP32 for the force gather
+__global__ void kb_force_prep(BState b) {
+  long long i = btid();
+  if (i >= b.NP) return;
+  const int s = b.scene[i];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  const SceneState& st = b.sst[s];
+  const long long NP = b.NP;
+  double f[3];
+  for (int a = 0; a < 3; ++a) {
+    double fa = b.fxp[a * NP + i];
+    if (sc.qload && !(st.time >= sc.qload_time)) fa = fa / sc.qload_time * st.time;
+    f[a] = fa;
+  }
+  if (sc.qdamp)
+    for (int a = 0; a < 3; ++a) f[a] = f[a] - sc.damp_factor * b.mass[i] * b.v[a * NP + i];
+  if (sc.gravity) {
+    const DevBody& bd = b.bodies[b.body[i]];
+    for (int a = 0; a < 3; ++a) f[a] = f[a] + b.mass[i] * bd.gravp[a];
+  }
+  float vol = b.vol[i];
+  float smq = b.sm[i] - b.q[i];
+  b.fs[i] = (smq + b.sd[i]) * vol;
+  b.fs[NP + i] = (smq + b.sd[NP + i]) * vol;
+  b.fs[2 * NP + i] = (smq + b.sd[2 * NP + i]) * vol;
+  b.fs[3 * NP + i] = b.sd[3 * NP + i] * vol;
+  b.fs[4 * NP + i] = b.sd[4 * NP + i] * vol;
+  b.fs[5 * NP + i] = b.sd[5 * NP + i] * vol;
+  for (int a = 0; a < 3; ++a) b.fs[(6 + a) * NP + i] = (float)f[a];
+}
+
+// GridMomentumUpdate + IntegrateMomentum for one node
+__device__ __forceinline__ void node_integrate(BState& b, const Scene& sc, long long n, const double f[3]) {
+  const long long NN = b.NN;
+  const SceneState& st = b.sst[b.node_scene[n]];
+  const double dt = st.dt;
+  for (int a = 0; a < 3; ++a) {
+    b.fx[a * NN + n] = f[a];
+    double p = b.px[a * NN + n];
+    p = st.istep == 1 ? p + f[a] * dt * 0.5 : p + f[a] * dt;
+    b.px[a * NN + n] = p;
+  }
+  node_finish(b, sc, n, 1, 1);
+  double m = b.mg[n];
+  if (m > sc.cutoff)
+    for (int a = 0; a < 3; ++a) b.ag[a * NN + n] = b.fx[a * NN + n] / m;
+}
+
+__global__ void kb_p2g_force(BState b) {
+  long long n = btid();
+  if (n >= b.NN) return;
+  const int s = b.node_scene[n];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  const long long NP = b.NP;
+  int j[3];
+  node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
+  double F[3] = {0, 0, 0};
+  if (sc.shape == 3) {
+    const long long NC = b.NC;
+    const float j4 = (float)sc.iJacobi4;
+    for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
+      if (cz < 0 || cz >= sc.NCz) continue;
+      for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
+        if (cy < 0 || cy >= sc.NCy) continue;
+        for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
+          if (cx < 0 || cx >= sc.NCx) continue;
+          long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
+          int ox = j[0] - cx, oy = j[1] - cy, oz = j[2] - cz;
+          double dx = (ox ? 1.0 : -1.0) * sc.iJacobi4, dy = (oy ? 1.0 : -1.0) * sc.iJacobi4,
+                 dz = (oz ? 1.0 : -1.0) * sc.iJacobi4;
+          const double* ci = b.cfint;
+          double c0 = ci[c], c1 = ci[NC + c], c2 = ci[2 * NC + c], c3 = ci[3 * NC + c], c4 = ci[4 * NC + c],
+                 c5 = ci[5 * NC + c];
+          F[0] += 0.125 * b.cfext[c] - (c0 * dx + c3 * dy + c5 * dz);
+          F[1] += 0.125 * b.cfext[NC + c] - (c3 * dx + c1 * dy + c4 * dz);
+          F[2] += 0.125 * b.cfext[2 * NC + c] - (c5 * dx + c4 * dy + c2 * dz);
+          (void)j4;
+        }
+      }
+    }
+  } else {
+    int lo, hi;
+    cell_window(sc.shape, lo, hi);
+    const float idc = (float)sc.idcell;
+    for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
+      for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
+        for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
+          int i0, i1;
+          key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
+          if (i0 == i1) continue;
+          const int c[3] = {cx, cy, cz};
+          float f0 = 0, f1 = 0, f2 = 0;
+          for (int i = i0; i < i1; ++i) {
+            float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+            float w, g[3];
+            if (!weight3(sc.shape, c, j, off, w, g)) continue;
+            float dx = g[0] * idc, dy = g[1] * idc, dz = g[2] * idc;
+            float sxx = b.fs[i], syy = b.fs[NP + i], szz = b.fs[2 * NP + i];
+            float sxy = b.fs[3 * NP + i], syz = b.fs[4 * NP + i], sxz = b.fs[5 * NP + i];
+            f0 += -(sxx * dx + sxy * dy + sxz * dz) + b.fs[6 * NP + i] * w;
+            f1 += -(sxy * dx + syy * dy + syz * dz) + b.fs[7 * NP + i] * w;
+            f2 += -(sxz * dx + syz * dy + szz * dz) + b.fs[8 * NP + i] * w;
+          }
+          F[0] += f0;
+          F[1] += f1;
+          F[2] += f2;
+        }
+  }
+  node_integrate(b, sc, n, F);
+}
+
+// SGMP: particles -> centre nodes, force terms
+__global__ void kb_sg_centre_force(BState b) {
+  long long c = btid();
+  if (c >= b.NC) return;
+  int s = b.cscene[c];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  const long long NP = b.NP, NC = b.NC;
+  long long lc = c - sc.c0;
+  int q[3];
+  q[2] = (int)(lc / sc.NCxy);
+  int rem = (int)(lc - (long long)q[2] * sc.NCxy);
+  q[1] = rem / sc.NCx;
+  q[0] = rem - q[1] * sc.NCx;
+  double E[3] = {0, 0, 0}, I[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < 8; ++k) {
+    int i0, i1;
+    if (!sg_dual_range(b, sc, q, k, i0, i1)) continue;
+    float e[3] = {0, 0, 0}, t[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = i0; i < i1; ++i) {
+      float w = sg_corner_weight(b, i, k);
+      for (int a = 0; a < 3; ++a) e[a] += b.fs[(6 + a) * NP + i] * w;
+      for (int a = 0; a < 6; ++a) t[a] += w * b.fs[a * NP + i];
+    }
+    for (int a = 0; a < 3; ++a) E[a] += e[a];
+    for (int a = 0; a < 6; ++a) I[a] += t[a];
+  }
+  for (int a = 0; a < 3; ++a) b.cfext[a * NC + c] = E[a];
+  // Cfint order of the reference: xx, yy, zz, xy, yz, xz
+  for (int a = 0; a < 6; ++a) b.cfint[a * NC + c] = I[a];
+}
+
+// SGMP: strain rate / spin at the centre nodes from the 8 cell nodes
+__global__ void kb_sg_centre_gradient(BState b, int usf_pass) {
+  long long c = btid();
+  if (c >= b.NC) return;
+  int s = b.cscene[c];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  if (sc.usf != usf_pass) return;
+  const long long NN = b.NN, NC = b.NC;
+  long long lc = c - sc.c0;
+  int q[3];
+  q[2] = (int)(lc / sc.NCxy);
+  int rem = (int)(lc - (long long)q[2] * sc.NCxy);
+  q[1] = rem / sc.NCx;
+  q[0] = rem - q[1] * sc.NCx;
+  double co[6] = {0, 0, 0, 0, 0, 0}, cw[3] = {0, 0, 0}, cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < 8; ++k) {
+    long long n = sc.n0 + ((long long)(q[2] + kCorner[k][2]) * sc.NGy + q[1] + kCorner[k][1]) * sc.NGx + q[0] +
+                  kCorner[k][0];
+    if (!(b.mg[n] > sc.cutoff)) continue;
+    double v[3] = {b.vg[n], b.vg[NN + n], b.vg[2 * NN + n]};
+    double dx = kSN[0][k] * sc.iJacobi4, dy = kSN[1][k] * sc.iJacobi4, dz = kSN[2][k] * sc.iJacobi4;
+    co[0] += dx * v[0];
+    co[1] += dy * v[1];
+    co[2] += dz * v[2];
+    co[3] += dz * v[1] + dy * v[2];
+    co[4] += dz * v[0] + dx * v[2];
+    co[5] += dy * v[0] + dx * v[1];
+    cw[0] += dy * v[2] - dz * v[1];
+    cw[1] += dz * v[0] - dx * v[2];
+    cw[2] += dx * v[1] - dy * v[0];
+    for (int a = 0; a < 3; ++a) {
+      cf[a * 3 + 0] += dx * v[a];
+      cf[a * 3 + 1] += dy * v[a];
+      cf[a * 3 + 2] += dz * v[a];
+    }
+  }
+  for (int a = 0; a < 6; ++a) b.co[a * NC + c] = co[a];
+  for (int a = 0; a < 3; ++a) b.cw[a * NC + c] = cw[a];
+  for (int a = 0; a < 9; ++a) b.cdefp[a * NC + c] = cf[a];
+}
+
+// SGMP: centre-node velocity / acceleration (BoundaryAuxiliaryNodeUpdate on
+// the fixed / symmetric faces)
+__global__ void kb_sg_centre_velocity(BState b) {
+  long long c = btid();
+  if (c >= b.NC) return;
+  int s = b.cscene[c];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  const long long NN = b.NN, NC = b.NC;
+  long long lc = c - sc.c0;
+  int q[3];
+  q[2] = (int)(lc / sc.NCxy);
+  int rem = (int)(lc - (long long)q[2] * sc.NCxy);
+  q[1] = rem / sc.NCx;
+  q[0] = rem - q[1] * sc.NCx;
+  const int NCd[3] = {sc.NCx, sc.NCy, sc.NCz};
+  bool boundary = false;
+  for (int a = 0; a < 3; ++a)
+    if (NCd[a] > 1 && ((q[a] == 0 && sc.fixs[2 * a] != 0) || (q[a] == NCd[a] - 1 && sc.fixs[2 * a + 1] != 0)))
+      boundary = true;
+  double cxx[3] = {0, 0, 0};
+  if (boundary)
+    for (int a = 0; a < 3; ++a)
+      if (NCd[a] > 1) cxx[a] = q[a] == NCd[a] - 1 ? -1.0 : (q[a] == 0 ? 1.0 : 0.0);
+  double v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
+  for (int k = 0; k < 8; ++k) {
+    long long n = sc.n0 + ((long long)(q[2] + kCorner[k][2]) * sc.NGy + q[1] + kCorner[k][1]) * sc.NGx + q[0] +
+                  kCorner[k][0];
+    double m = b.mg[n];
+    if (!(m > sc.cutoff)) continue;
+    double w = 0.125;
+    if (boundary) w = (kSN[0][k] * cxx[0] + 1.0) * (kSN[1][k] * cxx[1] + 1.0) * (kSN[2][k] * cxx[2] + 1.0) * 0.125;
+    for (int a = 0; a < 3; ++a) {
+      v[a] += w * b.px[a * NN + n] / m;
+      acc[a] += w * b.fx[a * NN + n] / m;
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    b.cvx[a * NC + c] = v[a];
+    b.cax[a * NC + c] = acc[a];
+  }
+}
+
+// ---------------------------------------------------------- G2P position
+__global__ void kb_position(BState b) {
+  long long i = btid();
+  if (i >= b.NP) return;
+  const int s = b.scene[i];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  const SceneState& st = b.sst[s];
+  const long long NP = b.NP, NN = b.NN;
+  float v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
+  if (sc.shape == 3) {
+    int d = b.dual[i];
+    if (d < 0) return;
+    int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+    int ln = b.inode[i];
+    int bd = ln >= 0 ? b.bd[sc.n0 + ln] : 0;
+    float xx[3];
+    for (int a = 0; a < 3; ++a) {
+      if ((bd >> (2 * a)) & 3) {  // AuxiliaryGridSHP
+        float xn = b.xn[a * NP + i];
+        xx[a] = xn < 0.f ? 1.f + 2.f * xn : 2.f * xn - 1.f;
+      } else {
+        xx[a] = b.xxn[a * NP + i];
+      }
+    }
+    if (bd == 0)
+      for (int a = 0; a < 3; ++a) xx[a] = b.xxn[a * NP + i];
+    const long long NC = b.NC;
+    for (int k = 0; k < 8; ++k) {
+      int oc[3] = {kCorner[k][0], kCorner[k][1], kCorner[k][2]};
+      long long c = sc.c0 + ((dz + oc[2]) * sc.NCy + (dy + oc[1])) * sc.NCx + (dx + oc[0]);
+      float w = 0.125f;
+      for (int a = 0; a < 3; ++a) w *= oc[a] ? 1.f + xx[a] : 1.f - xx[a];
+      for (int a = 0; a < 3; ++a) {
+        v[a] += w * (float)b.cvx[a * NC + c];
+        acc[a] += w * (float)b.cax[a * NC + c];
+      }
+    }
+  } else {
+    const int cl = b.cell[i];
+    if (cl < 0) return;
+    int c[3];
+    c[2] = cl / sc.NCxy;
+    int rem = cl - c[2] * sc.NCxy;
+    c[1] = rem / sc.NCx;
+    c[0] = rem - c[1] * sc.NCx;
+    float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+    int t[3][4], nt[3];
+    for (int a = 0; a < 3; ++a) nt[a] = node_offsets(sc.shape, off[a], t[a]);
+    for (int az = 0; az < nt[2]; ++az)
+      for (int ay = 0; ay < nt[1]; ++ay)
+        for (int ax = 0; ax < nt[0]; ++ax) {
+          int j[3] = {c[0] + t[0][ax], c[1] + t[1][ay], c[2] + t[2][az]};
+          if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
+          long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
+          double m = b.mg[n];
+          if (!(m > sc.cutoff)) continue;
+          float w, g[3];
+          if (!weight3(sc.shape, c, j, off, w, g)) continue;
+          for (int a = 0; a < 3; ++a) {
+            v[a] += w * (float)b.vg[a * NN + n];
+            acc[a] += w * (float)b.ag[a * NN + n];
+          }
+        }
+  }
+  const double dt = st.dt;
+  for (int a = 0; a < 3; ++a) {
+    double xx = b.x[a * NP + i] + (double)v[a] * dt;
+    b.xx[a * NP + i] = xx;
+    double vv = b.v[a * NP + i];
+    vv = st.istep == 1 ? vv + (double)acc[a] * dt * 0.5 : vv + (double)acc[a] * dt;
+    b.v[a * NP + i] = vv;
+    if (sc.usf) b.x[a * NP + i] = xx;
+  }
+}
+
+// GridMomentumMUSL: momentum re-map with the new particle velocities
+__global__ void kb_p2g_momentum(BState b) {
+  long long n = btid();
+  if (n >= b.NN) return;
+  const int s = b.node_scene[n];
+  if (!scene_live(b, s)) return;
+  const Scene& sc = b.scenes[s];
+  if (!sc.musl) return;
+  const long long NN = b.NN, NP = b.NP;
+  int j[3];
+  node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
+  double P0 = 0, P1 = 0, P2 = 0;
+  if (sc.shape == 3) {
+    const long long NC = b.NC;
+    for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
+      if (cz < 0 || cz >= sc.NCz) continue;
+      for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
+        if (cy < 0 || cy >= sc.NCy) continue;
+        for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
+          if (cx < 0 || cx >= sc.NCx) continue;
+          long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
+          P0 += 0.125 * b.cpx[c];
+          P1 += 0.125 * b.cpx[NC + c];
+          P2 += 0.125 * b.cpx[2 * NC + c];
+        }
+      }
+    }
+  } else {
+    int lo, hi;
+    cell_window(sc.shape, lo, hi);
+    for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
+      for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
+        for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
+          int i0, i1;
+          key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
+          if (i0 == i1) continue;
+          const int c[3] = {cx, cy, cz};
+          float p0 = 0, p1 = 0, p2 = 0;
+          for (int i = i0; i < i1; ++i) {
+            float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+            float w, g[3];
+            if (!weight3(sc.shape, c, j, off, w, g)) continue;
+            float wm = w * (float)b.mass[i];
+            p0 += wm * (float)b.v[i];
+            p1 += wm * (float)b.v[NP + i];
+            p2 += wm * (float)b.v[2 * NP + i];
+          }
+          P0 += p0;
+          P1 += p1;
+          P2 += p2;
+        }
+  }
+  b.px[n] = P0;
+  b.px[NN + n] = P1;
+  b.px[2 * NN + n] = P2;
+  node_finish(b, sc, n, 1, !sc.usf);
+}
+
+// ------------------------------------------------------------ reductions
+// calcEnergy + UpdateDT per scene: a block per chunk of kChunk particles of
+// one scene (chunks are fixed relative to the scene start, so the sums of a
+// scene do not depend on the other scenes of the batch), then a block per
+// scene combining its chunks in order.
+__global__ void kb_reduce_chunks(BState b) {
+  __shared__ double sh[6][256];
+  const long long r = blockIdx.x;
+  const int s = b.rscene[r];
+  const Scene& sc = b.scenes[s];
+  const long long NP = b.NP;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  if (scene_live(b, s)) {
+    long long p_begin = sc.p0 + (r - sc.r0) * kChunk;
+    long long p_end = min(p_begin + kChunk, sc.p0 + sc.np);
+    for (long long i = p_begin + threadIdx.x; i < p_end; i += blockDim.x) {
+      double v0 = b.v[i], v1 = b.v[NP + i], v2 = b.v[2 * NP + i], m = b.mass[i];
+      acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5;
+      acc[1] += b.ie[i];
+      acc[2] += m * v0;
+      acc[3] += m * v1;
+      acc[4] += m * v2;
+      double a = fmax(fabs(v0), fmax(fabs(v1), fabs(v2)));
+      acc[5] = fmax(acc[5], a);
+    }
+  }
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      for (int k = 0; k < 5; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+      sh[5][threadIdx.x] = fmax(sh[5][threadIdx.x], sh[5][threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) b.red_part[k * b.NR + r] = sh[k][0];
+}
+
+__global__ void kb_reduce_scenes(BState b, int mode) {
+  __shared__ double sh[6][256];
+  const int s = blockIdx.x;
+  const Scene& sc = b.scenes[s];
+  if (!scene_live(b, s)) return;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (long long r = sc.r0 + threadIdx.x; r < sc.r0 + sc.nr; r += blockDim.x) {
+    for (int k = 0; k < 5; ++k) acc[k] += b.red_part[k * b.NR + r];
+    acc[5] = fmax(acc[5], b.red_part[5 * b.NR + r]);
+  }
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      for (int k = 0; k < 5; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+      sh[5][threadIdx.x] = fmax(sh[5][threadIdx.x], sh[5][threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  SceneState& st = b.sst[s];
+  if (mode & 1) {
+    st.ke_prev = st.ke;
+    st.ke = sh[0][0];
+    st.ie = sh[1][0];
+    st.mom[0] = sh[2][0];
+    st.mom[1] = sh[3][0];
+    st.mom[2] = sh[4][0];
+  }
+  st.max_vp = sh[5][0];
+  if (mode & 2) {
+    double dt = (double)1e6f;
+    for (int m = sc.mat0; m < sc.mat0 + sc.nmat; ++m) {
+      const DevMaterial& mt = b.mats[m];
+      if (mt.mat_type == 12) continue;
+      double E = mt.young, nu = mt.poisson, ro = mt.density;
+      double vv = sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
+      vv = fmax(vv, mt.D);
+      vv = fmax(vv, mt.wavespd);
+      vv = vv + sh[5][0];
+      dt = fmin(dt, sc.dcell / vv);
+    }
+    st.dt = dt * sc.dtscale;
+  }
+}
+
+__global__ void kb_dr_damping(BState b) {
+  long long i = btid();
+  if (i >= b.NP) return;
+  const int s = b.scene[i];
+  const Scene& sc = b.scenes[s];
+  if (!sc.drdamp || !scene_live(b, s)) return;
+  const SceneState& st = b.sst[s];
+  if (!(st.ke - st.ke_prev <= 0.0)) return;
+  const long long NP = b.NP;
+  b.v[i] = 0;
+  b.v[NP + i] = 0;
+  b.v[2 * NP + i] = 0;
+}
+
+__global__ void kb_dr_finish(BState b) {
+  int s = (int)btid();
+  if (s >= b.nscene) return;
+  if (!b.scenes[s].drdamp || !scene_live(b, s)) return;
+  SceneState& st = b.sst[s];
+  if (st.ke - st.ke_prev <= 0.0) st.ke = 0;
+}
+
+}  // namespace bm
+}  // namespace mpm

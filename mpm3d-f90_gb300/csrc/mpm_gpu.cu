@@ -22,17 +22,13 @@
 
 #include "mpm3d_gpu.h"
 #include "mpm_gpu_internal.cuh"
+#include "mpm_setup.h"
 
 using namespace mpm;
 
 namespace {
 
 thread_local std::string g_lib_error;
-
-struct ProfRec {
-  int kernel;
-  cudaEvent_t a, b;
-};
 
 struct MaxOp {
   __host__ __device__ int operator()(int a, int b) const { return a > b ? a : b; }
@@ -62,20 +58,13 @@ struct mpm_ctx {
   bool graph_prof = false;
   std::vector<DevMaterial> mats;
   std::vector<DevBody> bodies;
-  // profiling
-  bool prof = false;
-  bool capturing = false;
-  std::vector<ProfRec> recs;
-  std::vector<cudaEvent_t> event_pool;
-  size_t event_next = 0;
-  double kstat_ms[K_COUNT] = {};
-  long long kstat_n[K_COUNT] = {};
+  Profiler prof;
+  mpm_batch* batch = nullptr;  // the mixed form runs as a batch of one scene
+  int batch_scene = -1;
   std::string err;
 };
 
 namespace {
-
-thread_local mpm_ctx* t_prof_ctx = nullptr;  // context whose launches are being timed
 
 int set_err(mpm_ctx* c, int code, const char* fmt, ...) {
   char buf[512];
@@ -111,212 +100,126 @@ int dalloc(mpm_ctx* c, T** p, long long n) {
   return MPM_OK;
 }
 
-cudaEvent_t pool_event(mpm_ctx* c) {
-  if (c->event_next == c->event_pool.size()) {
-    cudaEvent_t e;
-    cudaEventCreate(&e);
-    c->event_pool.push_back(e);
-  }
-  return c->event_pool[c->event_next++];
-}
-
 }  // namespace
 
 namespace mpm {
-void prof_begin(int k, cudaStream_t s) {
-  mpm_ctx* c = t_prof_ctx;
-  if (!c || !c->prof) return;
-  ProfRec r{k, pool_event(c), pool_event(c)};
-  if (c->capturing) cudaEventRecordWithFlags(r.a, s, cudaEventRecordExternal);
-  else cudaEventRecord(r.a, s);
-  c->recs.push_back(r);
+
+const char* const kKernelNames[K_COUNT] = {
+    "begin_step", "locate", "pair_sort", "segments", "p2g_mass", "node_velocity", "apply_bc",
+    "stress_update", "depeff_tail", "force_prep", "p2g_force_integrate", "integrate", "g2p_position",
+    "p2g_musl", "reduce_energy_dt", "dr_damping", "permute"};
+
+static thread_local Profiler* t_prof = nullptr;
+void prof_set_current(Profiler* p) { t_prof = p; }
+Profiler* prof_current() { return t_prof; }
+
+static cudaEvent_t pool_event(Profiler* p) {
+  if (p->next == p->npool) {
+    int ncap = p->npool ? 2 * p->npool : 256;
+    cudaEvent_t* np = (cudaEvent_t*)realloc(p->pool, sizeof(cudaEvent_t) * ncap);
+    if (!np) return nullptr;
+    p->pool = np;
+    for (int k = p->npool; k < ncap; ++k) cudaEventCreate(&p->pool[k]);
+    p->npool = ncap;
+  }
+  return p->pool[p->next++];
 }
+
+void prof_begin(int k, cudaStream_t s) {
+  Profiler* p = t_prof;
+  if (!p || !p->on) return;
+  if (p->nrec == p->cap) {
+    int ncap = p->cap ? 2 * p->cap : 256;
+    Profiler::Rec* nr = (Profiler::Rec*)realloc(p->recs, sizeof(Profiler::Rec) * ncap);
+    if (!nr) return;
+    p->recs = nr;
+    p->cap = ncap;
+  }
+  Profiler::Rec& r = p->recs[p->nrec++];
+  r.kernel = k;
+  r.a = pool_event(p);
+  r.b = pool_event(p);
+  if (p->capturing) cudaEventRecordWithFlags(r.a, s, cudaEventRecordExternal);
+  else cudaEventRecord(r.a, s);
+}
+
 void prof_end(int k, cudaStream_t s) {
-  mpm_ctx* c = t_prof_ctx;
-  if (!c || !c->prof || c->recs.empty()) return;
-  ProfRec& r = c->recs.back();
+  Profiler* p = t_prof;
+  if (!p || !p->on || p->nrec == 0) return;
+  Profiler::Rec& r = p->recs[p->nrec - 1];
   if (r.kernel != k) return;
-  if (c->capturing) cudaEventRecordWithFlags(r.b, s, cudaEventRecordExternal);
+  if (p->capturing) cudaEventRecordWithFlags(r.b, s, cudaEventRecordExternal);
   else cudaEventRecord(r.b, s);
 }
+
+int prof_harvest(Profiler* p, cudaStream_t s) {
+  if (!p || p->nrec == 0) return MPM_OK;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MPM_ERR_CUDA;
+  for (int i = 0; i < p->nrec; ++i) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p->recs[i].a, p->recs[i].b) == cudaSuccess) {
+      p->ms[p->recs[i].kernel] += ms;
+      p->n[p->recs[i].kernel] += 1;
+    }
+  }
+  p->nrec = 0;
+  p->next = 0;
+  return MPM_OK;
+}
+
+void prof_reset(Profiler* p) {
+  for (int k = 0; k < K_COUNT; ++k) {
+    p->ms[k] = 0;
+    p->n[k] = 0;
+  }
+  p->nrec = 0;
+  p->next = 0;
+}
+
+void prof_free(Profiler* p) {
+  for (int k = 0; k < p->npool; ++k) cudaEventDestroy(p->pool[k]);
+  free(p->pool);
+  free(p->recs);
+  p->pool = nullptr;
+  p->recs = nullptr;
+  p->npool = p->cap = p->nrec = p->next = 0;
+}
+
 }  // namespace mpm
 
 namespace {
 
 struct ProfScope {
-  mpm_ctx* prev;
-  explicit ProfScope(mpm_ctx* c) : prev(t_prof_ctx) { t_prof_ctx = c; }
-  ~ProfScope() { t_prof_ctx = prev; }
+  Profiler* prev;
+  explicit ProfScope(mpm_ctx* c) : prev(prof_current()) { prof_set_current(&c->prof); }
+  ~ProfScope() { prof_set_current(prev); }
 };
+
+// status of a call delegated to the batched engine, with its message
+int batch_status(mpm_ctx* c, int r) {
+  if (r) set_err(c, r, "%s", mpm_batch_last_error(c->batch));
+  return r;
+}
 
 // ------------------------------------------------------------- set-up
 
 int derive_setup(mpm_ctx* c, const mpm_deck* d, std::vector<double>& host_vol, std::vector<double>& sig_y,
                  std::vector<double>& ie, std::vector<double>& cp, std::vector<double>& lt,
                  std::vector<uint8_t>& fix, std::vector<uint8_t>& bd) {
-  Geometry& g = c->g;
-  const long long np = d->nb_particle;
-  // materials (Initial overrides cEos(1) of null materials with the wave speed)
-  c->mats.resize(d->nb_mat);
-  for (int m = 0; m < d->nb_mat; ++m) {
-    const mpm_material& s = d->mats[m];
-    DevMaterial& t = c->mats[m];
-    memset(&t, 0, sizeof t);
-    t.mat_type = s.mat_type;
-    t.eos_type = s.eos_type;
-    t.density = s.density; t.miu = s.miu; t.young = s.young; t.poisson = s.poisson;
-    t.yield0 = s.yield0; t.tangmod = s.tangmod; t.roomt = s.roomt; t.melt = s.melt; t.specheat = s.specheat;
-    t.B_jc = s.B_jc; t.n_jc = s.n_jc; t.C_jc = s.C_jc; t.m_jc = s.m_jc; t.epso = s.epso; t.epf = s.epf;
-    t.D = s.D;
-    for (int k = 0; k < 10; ++k) t.cEos[k] = s.cEos[k];
-    t.wavespd = s.wavespd; t.q_fai = s.q_fai; t.k_fai = s.k_fai; t.q_psi = s.q_psi; t.ten_f = s.ten_f;
-    if (t.mat_type < 1 || t.mat_type > 11) return set_err(c, MPM_ERR_ARG, "material %d has no type", m + 1);
-    bool needs_eos = t.mat_type == 5 || t.mat_type == 6 || t.mat_type == 7 || t.mat_type == 8 || t.mat_type == 9;
-    if (needs_eos && (t.eos_type < 1 || t.eos_type > 4))
-      return set_err(c, MPM_ERR_ARG, "material %d (type %d) needs an equation of state", m + 1, t.mat_type);
-    if (t.eos_type == 3 && t.mat_type != 8)
-      return set_err(c, MPM_ERR_UNSUPPORTED, "JWL EOS is only supported with the 'hiex' material");
-  }
-  for (int m = 0; m < d->nb_mat; ++m)
-    if (c->mats[m].mat_type == 9) c->mats[m].cEos[0] = c->mats[m].wavespd;
-  c->bodies.resize(d->nb_body);
-  for (int b = 0; b < d->nb_body; ++b) {
-    if (d->bodies[b].mat < 1 || d->bodies[b].mat > d->nb_mat)
-      return set_err(c, MPM_ERR_ARG, "body %d has no material", b + 1);
-    c->bodies[b].mat = d->bodies[b].mat - 1;
-    for (int k = 0; k < 3; ++k) c->bodies[b].gravp[k] = d->bodies[b].gravp[k];
-  }
-  // Initial: per-particle volume, yield stress, internal energy, sound speed,
-  // lighting time (sqrt(...)/D is a default-REAL temporary)
-  host_vol.assign(np, 0.0); sig_y.assign(np, 0.0); ie.assign(np, 0.0); cp.assign(np, 0.0);
-  lt.assign(np, 0.0);
-  for (int b = 0; b < d->nb_body; ++b) {
-    const DevMaterial& m = c->mats[c->bodies[b].mat];
-    if (m.mat_type == 12) continue;
-    for (long long p = d->bodies[b].par_begin; p < d->bodies[b].par_end; ++p) {
-      double vol = d->mass[p] / m.density;
-      host_vol[p] = vol;
-      sig_y[p] = m.yield0;
-      ie[p] = d->mats[c->bodies[b].mat].cEos[9] * vol;
-      if (m.mat_type == 1 || m.mat_type == 11) {
-        double E = m.young, nu = m.poisson, ro = m.density;
-        cp[p] = std::sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
-      }
-      if (m.mat_type == 9) cp[p] = m.wavespd;
-      double ltv = (double)10e6f;
-      for (int j = 0; j < d->n_deto; ++j) {
-        double dx = d->xp[p] - d->deto[j][0];
-        double dy = d->xp[np + p] - d->deto[j][1];
-        double dz = d->xp[2 * np + p] - d->deto[j][2];
-        float t = (float)(std::sqrt(dx * dx + dy * dy + dz * dz) / m.D);
-        if ((double)t < ltv) ltv = (double)t;
-      }
-      lt[p] = ltv;
-    }
-  }
-  // SetGridData
-  const double h = d->dcell;
-  if (h == 0) return set_err(c, MPM_ERR_ARG, "DCell must be defined");
-  double sp[3], s0[3];
-  for (int a = 0; a < 3; ++a) {
-    s0[a] = d->span[a][0];
-    sp[a] = d->span[a][1] - d->span[a][0];
-    if (sp[a] <= 0) return set_err(c, MPM_ERR_ARG, "computational region must be defined");
-  }
-  int NC[3], CNC[3];
-  for (int a = 0; a < 3; ++a) {
-    NC[a] = (int)(sp[a] / h + 0.5);
-    CNC[a] = NC[a] - 1 == 0 ? 1 : NC[a] - 1;
-  }
-  long long nn = (long long)(NC[0] + 1) * (NC[1] + 1) * (NC[2] + 1);
-  long long ncell = (long long)NC[0] * NC[1] * NC[2];
-  if (nn > 2000000000LL) return set_err(c, MPM_ERR_UNSUPPORTED, "grid too large for 32-bit node ids");
-  if (np >= (1LL << 27)) return set_err(c, MPM_ERR_UNSUPPORTED, "more than 2^27 particles per context");
-  g.np = np;
-  g.NCx = NC[0]; g.NCy = NC[1]; g.NCz = NC[2]; g.NCxy = NC[0] * NC[1];
-  g.CNCx = CNC[0]; g.CNCy = CNC[1]; g.CNCz = CNC[2]; g.CNCxy = CNC[0] * CNC[1]; g.CNC = g.CNCxy * CNC[2];
-  g.ncell = (int)ncell;
-  g.NGx = NC[0] + 1; g.NGy = NC[1] + 1; g.NGz = NC[2] + 1; g.NGxy = g.NGx * g.NGy;
-  g.nn = (int)nn;
-  for (int a = 0; a < 3; ++a) {
-    g.span0[a] = s0[a];
-    g.span1[a] = s0[a] + NC[a] * h;
-  }
-  g.dcell = h;
-  g.cutoff = d->cutoff;
-  g.iJacobi = 2.0 / h;
-  g.iJacobi4 = g.iJacobi * 0.125;
-  g.iDCell = 1.0 / h;
-  const int f = d->flags;
-  const bool gimp = f & MPM_F_GIMP, bsp = f & MPM_F_BSPLINE, sgmp = f & MPM_F_SGMP;
-  g.shape = sgmp ? 3 : (gimp ? 1 : (bsp ? 2 : 0));
-  g.K = (g.shape == 1 || g.shape == 2) ? 27 : 8;
-  for (int k = 0; k < 6; ++k) g.fixs[k] = d->fixs[k];
-  g.usf = !!(f & MPM_F_USF);
-  g.usl = !!(f & MPM_F_USL);
-  g.musl = !!(f & MPM_F_MUSL);
-  g.uvfp = !!(f & MPM_F_UVFP);
-  g.qload = !!(f & MPM_F_QUASILOAD);
-  g.qdamp = !!(f & MPM_F_QUASIDAMP);
-  g.gravity = !!(f & MPM_F_GRAVITY);
-  g.qload_time = d->quasi_load_time;
-  g.damp_factor = d->damp_factor;
-  g.bq1 = d->bq1;
-  g.bq2 = d->bq2;
-  g.dtscale = d->dtscale;
-  g.nb_mat = d->nb_mat;
-  g.nb_body = d->nb_body;
-  g.has_jc = 0;
-  for (auto& m : c->mats)
-    if (m.mat_type == 4 || m.mat_type == 7) g.has_jc = 1;
-  // fixities and SGMP boundary types (Grid.f90:291-359)
-  fix.assign(nn, 0);
-  bd.assign(nn, 0);
-  const int* F = d->fixs;
-  const int NGx = g.NGx, NGy = g.NGy, NGz = g.NGz;
-  for (int iz = 1; iz <= NGz; ++iz)
-    for (int iy = 1; iy <= NGy; ++iy)
-      for (int ix = 1; ix <= NGx; ++ix) {
-        long long i = (long long)(iz - 1) * g.NGxy + (long long)(iy - 1) * NGx + (ix - 1);
-        int bt[3] = {0, 0, 0};
-        int idx[3] = {ix, iy, iz}, NG[3] = {NGx, NGy, NGz};
-        for (int a = 0; a < 3; ++a) {
-          if (idx[a] == 1 && F[2 * a] != 0) bt[a] = 1;
-          if (idx[a] == NG[a] && F[2 * a + 1] != 0) bt[a] = 2;
-          if (sgmp) {
-            if (idx[a] == 2 && F[2 * a] != 0) bt[a] = 1;
-            if (idx[a] == NG[a] - 1 && F[2 * a + 1] != 0) bt[a] = 2;
-          }
-        }
-        bd[i] = (uint8_t)(bt[0] | (bt[1] << 2) | (bt[2] << 4));
-        uint8_t fx = 0;
-        bool all = false;
-        for (int a = 0; a < 3; ++a) {
-          bool lo1 = idx[a] == 1, hi1 = idx[a] == NG[a];
-          bool lo2 = lo1 || idx[a] == 2, hi2 = hi1 || idx[a] == NG[a] - 1;
-          bool two = gimp || bsp || sgmp;  // a second node layer is fixed too
-          bool lo = two ? lo2 : lo1, hi = two ? hi2 : hi1;
-          if ((lo && F[2 * a] == 1) || (hi && F[2 * a + 1] == 1)) all = true;
-          if ((lo && F[2 * a] == 2) || (hi && F[2 * a + 1] == 2)) fx |= (uint8_t)(1 << a);
-        }
-        if (all) fx = 7;
-        fix[i] = fx;
-      }
+  SceneSetup su;
+  int r = scene_setup(d, su);
+  if (r) return set_err(c, r, "%s", su.err.c_str());
+  c->g = su.g;
+  c->mats = su.mats;
+  c->bodies = su.bodies;
+  host_vol.swap(su.vol);
+  sig_y.swap(su.sig_y);
+  ie.swap(su.ie);
+  cp.swap(su.cp);
+  lt.swap(su.lt);
+  fix.swap(su.fix);
+  bd.swap(su.bd);
   return MPM_OK;
-}
-
-double set_dt(const std::vector<DevMaterial>& mats, double dcell, double dtscale) {
-  double dt = (double)1.0e6f;
-  for (const auto& m : mats) {
-    if (m.mat_type == 12) continue;
-    double E = m.young, nu = m.poisson, ro = m.density;
-    double cp = std::sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
-    if (m.D > cp) cp = m.D;
-    if (m.wavespd > cp) cp = m.wavespd;
-    double t = dcell / cp;
-    if (t < dt) dt = t;
-  }
-  return dt * dtscale;
 }
 
 template <class T>
@@ -398,32 +301,15 @@ int enqueue_step(mpm_ctx* c) {
 
 void free_ctx(mpm_ctx* c) {
   if (!c) return;
+  if (c->batch) mpm_batch_destroy(c->batch);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   for (void* p : c->allocs) cudaFree(p);
-  for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+  prof_free(&c->prof);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
 
-int harvest_profile(mpm_ctx* c) {
-  if (c->recs.empty()) return MPM_OK;
-  CK(cudaStreamSynchronize(c->stream));
-  for (const ProfRec& r : c->recs) {
-    float ms = 0;
-    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
-      c->kstat_ms[r.kernel] += ms;
-      c->kstat_n[r.kernel] += 1;
-    }
-  }
-  c->recs.clear();
-  c->event_next = 0;
-  return MPM_OK;
-}
-
-const char* kKernelNames[K_COUNT] = {"begin_step", "locate",     "pair_sort",     "segments",  "p2g_mass",
-                                     "node_velocity", "apply_bc", "stress_update", "depeff_tail", "force_prep",
-                                     "p2g_force_integrate", "integrate", "g2p_position", "p2g_musl",
-                                     "reduce_energy_dt", "dr_damping"};
+int harvest_profile(mpm_ctx* c) { return prof_harvest(&c->prof, c->stream); }
 
 }  // namespace
 
@@ -464,7 +350,7 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
   switch (precision) {
     case MPM_FP64_STRICT: c->ops = &kOpsStrict; break;
     case MPM_FP64_NATIVE: c->ops = &kOpsNative; break;
-    case MPM_MIXED: c->ops = &kOpsMixed; break;
+    case MPM_MIXED: c->ops = nullptr; break;  // batched engine, one scene
     default:
       delete c;
       return set_err(nullptr, MPM_ERR_ARG, "unknown precision %d", precision);
@@ -497,6 +383,24 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     g_lib_error = c->err;
     free_ctx(c);
     return r;
+  }
+  if (precision == MPM_MIXED) {
+    // the mixed form is the batched engine running a batch of one scene
+    if ((r = mpm_batch_create(c->device, &c->batch))) {
+      set_err(c, r, "batch create failed");
+      g_lib_error = c->err;
+      free_ctx(c);
+      return r;
+    }
+    if ((r = mpm_batch_add(c->batch, d, 0, &c->batch_scene)) || (r = mpm_batch_commit(c->batch))) {
+      set_err(c, r, "%s", mpm_batch_last_error(c->batch));
+      g_lib_error = c->err;
+      free_ctx(c);
+      return r;
+    }
+    c->bytes = mpm_batch_device_bytes(c->batch);
+    *out = c;
+    return MPM_OK;
   }
   Geometry& g = c->g;
   const long long np = g.np, nn = g.nn, nc = g.ncell;
@@ -633,6 +537,7 @@ void mpm_destroy(mpm_ctx* c) {
 
 int mpm_step_phase(mpm_ctx* c, int phase) {
   if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "the mixed form runs whole steps only");
   ProfScope ps(c);
   const Geometry& g = c->g;
   const StepOps* o = c->ops;
@@ -672,22 +577,23 @@ int mpm_step_phase(mpm_ctx* c, int phase) {
 
 int mpm_step(mpm_ctx* c) {
   if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  if (c->batch) return batch_status(c, mpm_batch_run(c->batch, 1, 0));
   ProfScope ps(c);
   return enqueue_step(c);
 }
 
 static int ensure_graph(mpm_ctx* c, int nsteps) {
-  if (c->graph_exec && c->graph_steps == nsteps && c->graph_prof == c->prof) return MPM_OK;
+  if (c->graph_exec && c->graph_steps == nsteps && c->graph_prof == c->prof.on) return MPM_OK;
   if (c->graph_exec) {
     cudaGraphExecDestroy(c->graph_exec);
     c->graph_exec = nullptr;
   }
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  c->capturing = true;
+  c->prof.capturing = true;
   int r = MPM_OK;
   for (int i = 0; i < nsteps && r == MPM_OK; ++i) r = enqueue_step(c);
-  c->capturing = false;
+  c->prof.capturing = false;
   cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
   if (r) return r;
   if (e != cudaSuccess) return cuda_err(c, e, "end capture");
@@ -695,13 +601,14 @@ static int ensure_graph(mpm_ctx* c, int nsteps) {
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_err(c, e, "graph instantiate");
   c->graph_steps = nsteps;
-  c->graph_prof = c->prof;
+  c->graph_prof = c->prof.on;
   return MPM_OK;
 }
 
 int mpm_run(mpm_ctx* c, int nsteps, int use_graph) {
   if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
   if (nsteps <= 0) return MPM_OK;
+  if (c->batch) return batch_status(c, mpm_batch_run(c->batch, nsteps, use_graph));
   ProfScope ps(c);
   if (!use_graph) {
     for (int i = 0; i < nsteps; ++i) {
@@ -713,13 +620,13 @@ int mpm_run(mpm_ctx* c, int nsteps, int use_graph) {
   // a graph of one step, launched nsteps times (profiling records only the
   // event nodes of the captured step, so profiled runs use a graph of all
   // steps instead)
-  int gsteps = c->prof ? nsteps : 1;
-  if (c->prof) {
+  int gsteps = c->prof.on ? nsteps : 1;
+  if (c->prof.on) {
     // re-capture so that the event records of this run are the live ones
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     c->graph_exec = nullptr;
-    c->recs.clear();
-    c->event_next = 0;
+    c->prof.nrec = 0;
+    c->prof.next = 0;
   }
   int r = ensure_graph(c, gsteps);
   if (r) return r;
@@ -729,6 +636,7 @@ int mpm_run(mpm_ctx* c, int nsteps, int use_graph) {
 
 int mpm_sync(mpm_ctx* c) {
   if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
+  if (c->batch) return batch_status(c, mpm_batch_sync(c->batch));
   CK(cudaStreamSynchronize(c->stream));
   unsigned status = 0;
   CK(cudaMemcpy(&status, &c->st.sc->status, sizeof status, cudaMemcpyDeviceToHost));
@@ -739,6 +647,7 @@ int mpm_sync(mpm_ctx* c) {
 
 int mpm_get_scalars(mpm_ctx* c, double* o) {
   if (!c || !o) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return batch_status(c, mpm_batch_scene_scalars(c->batch, c->batch_scene, o));
   CK(cudaStreamSynchronize(c->stream));
   DevScalars sc;
   CK(cudaMemcpy(&sc, c->st.sc, sizeof sc, cudaMemcpyDeviceToHost));
@@ -753,7 +662,7 @@ int mpm_get_scalars(mpm_ctx* c, double* o) {
 int64_t mpm_nb_particle(const mpm_ctx* c) { return c ? c->g.np : -1; }
 int64_t mpm_nb_gridnode(const mpm_ctx* c) { return c ? c->g.nn : -1; }
 int64_t mpm_nb_cell(const mpm_ctx* c) { return c ? c->g.ncell : -1; }
-int64_t mpm_device_bytes(const mpm_ctx* c) { return c ? c->bytes : -1; }
+int64_t mpm_device_bytes(const mpm_ctx* c) { return c ? (c->batch ? mpm_batch_device_bytes(c->batch) : c->bytes) : -1; }
 
 static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long* count) {
   DevState<double, double>& s = c->st;
@@ -804,6 +713,7 @@ static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long*
 
 int mpm_download(mpm_ctx* c, int field, double* out) {
   if (!c || !out) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return batch_status(c, mpm_batch_scene_download(c->batch, c->batch_scene, field, out));
   void* p = nullptr;
   size_t elem = 0;
   long long n = 0;
@@ -829,6 +739,7 @@ int mpm_download(mpm_ctx* c, int field, double* out) {
 
 int mpm_upload(mpm_ctx* c, int field, const double* in) {
   if (!c || !in) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "the mixed form takes its state from the deck only");
   if (field >= MPM_G_MG || field == MPM_P_ICELL || field == MPM_P_CENTERICELL || field == MPM_P_INODE ||
       field == MPM_P_FAILURE)
     return set_err(c, MPM_ERR_ARG, "field %d cannot be uploaded", field);
@@ -854,6 +765,7 @@ int mpm_upload(mpm_ctx* c, int field, const double* in) {
 
 int mpm_time_steps(mpm_ctx* c, int nsteps, int use_graph, double* ms) {
   if (!c || !ms) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return batch_status(c, mpm_batch_time_steps(c->batch, nsteps, use_graph, ms));
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
@@ -868,18 +780,16 @@ int mpm_time_steps(mpm_ctx* c, int nsteps, int use_graph, double* ms) {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (r) return r;
-  if (c->prof) harvest_profile(c);
+  if (c->prof.on) harvest_profile(c);
   return MPM_OK;
 }
 
 int mpm_profile_enable(mpm_ctx* c, int on) {
   if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
-  if (c->prof) harvest_profile(c);
-  c->prof = on != 0;
-  for (int k = 0; k < K_COUNT; ++k) {
-    c->kstat_ms[k] = 0;
-    c->kstat_n[k] = 0;
-  }
+  if (c->batch) return batch_status(c, mpm_batch_profile_enable(c->batch, on));
+  if (c->prof.on) harvest_profile(c);
+  prof_reset(&c->prof);
+  c->prof.on = on != 0;
   return MPM_OK;
 }
 
@@ -887,10 +797,11 @@ int mpm_kernel_count(const mpm_ctx*) { return K_COUNT; }
 
 int mpm_kernel_stats(mpm_ctx* c, int k, char* name, int namelen, int64_t* launches, double* total_ms) {
   if (!c || k < 0 || k >= K_COUNT) return set_err(c, MPM_ERR_ARG, "bad kernel index");
+  if (c->batch) return batch_status(c, mpm_batch_kernel_stats(c->batch, k, name, namelen, launches, total_ms));
   harvest_profile(c);
   if (name && namelen > 0) snprintf(name, (size_t)namelen, "%s", kKernelNames[k]);
-  if (launches) *launches = c->kstat_n[k];
-  if (total_ms) *total_ms = c->kstat_ms[k];
+  if (launches) *launches = c->prof.n[k];
+  if (total_ms) *total_ms = c->prof.ms[k];
   return MPM_OK;
 }
 
@@ -899,7 +810,7 @@ int mpm_algorithmic_bytes(mpm_ctx* c, double* bytes) {
   double sc[MPM_NSCALARS];
   int r = mpm_get_scalars(c, sc);
   if (r) return r;
-  const double Bw = (double)c->ops->bulk_size;
+  const double Bw = c->batch ? 4.0 : (double)c->ops->bulk_size;
   // per particle: read {Xp, VXp, mass, VOL, SM, SD, q, ie, cp},
   // write {Xp, VXp, VOL, SM, SD, q, ie, seqv}
   double per_p = (24 + 24 + 8 + 8) + Bw * (1 + 1 + 6 + 1 + 1) + (24 + 24 + 8) + Bw * (1 + 1 + 6 + 1 + 1);

@@ -149,7 +149,6 @@ struct StepOps {
 
 extern const StepOps kOpsStrict;   // MPM_FP64_STRICT
 extern const StepOps kOpsNative;   // MPM_FP64_NATIVE
-extern const StepOps kOpsMixed;    // MPM_MIXED
 
 // Kernel launch bookkeeping for per-kernel event timing.
 void prof_begin(int kernel_id, cudaStream_t s);
@@ -157,7 +156,32 @@ void prof_end(int kernel_id, cudaStream_t s);
 
 enum KernelId {
   K_BEGIN = 0, K_LOCATE, K_SORT, K_SEG, K_P2G_MASS, K_NODE_VEL, K_BC, K_STRESS, K_DEPEFF,
-  K_FORCE_PREP, K_P2G_FORCE, K_INTEGRATE, K_POSITION, K_P2G_MOM, K_REDUCE, K_DR, K_COUNT
+  K_FORCE_PREP, K_P2G_FORCE, K_INTEGRATE, K_POSITION, K_P2G_MOM, K_REDUCE, K_DR, K_PERMUTE, K_COUNT
 };
+extern const char* const kKernelNames[K_COUNT];
+
+// Per-kernel CUDA-event timing shared by contexts and batches: while a
+// Profiler is current on the calling thread and enabled, every launch
+// bracketed by prof_begin / prof_end records an event pair on its stream
+// (event-record nodes when the stream is being captured into a graph).
+struct Profiler {
+  bool on = false;
+  bool capturing = false;
+  struct Rec {
+    int kernel;
+    cudaEvent_t a, b;
+  };
+  Rec* recs = nullptr;
+  int nrec = 0, cap = 0;
+  cudaEvent_t* pool = nullptr;
+  int npool = 0, next = 0;
+  double ms[K_COUNT] = {};
+  long long n[K_COUNT] = {};
+};
+void prof_set_current(Profiler* p);
+Profiler* prof_current();
+int prof_harvest(Profiler* p, cudaStream_t s);
+void prof_reset(Profiler* p);
+void prof_free(Profiler* p);
 
 }  // namespace mpm

@@ -352,88 +352,49 @@ __device__ __forceinline__ void jc7_tail(Mm<typename P::R>& m, const DevMaterial
   }
 }
 
-template <class P>
-__global__ void k_stress(St<P> s, Geometry g) {
-  using R = typename P::R;
-  using B = typename P::B;
-  const long long p = gtid();
-  if (p >= g.np) return;
-  const long long np = g.np;
-  const int nn = g.nn;
-  if (g.has_jc) {
-    s.setter[p] = -1;
-    s.deferred[p] = 0;
-  }
-  R de[6] = {0, 0, 0, 0, 0, 0}, vort[3] = {0, 0, 0}, deFp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  if (g.shape == 3) {
-    if (s.centericell[p] < 0) return;
-    const long long nc = g.ncell;
-    for (int k = 0; k < 8; ++k) {
-      int c = s.snode[k * np + p];
-      if (c < 0) continue;
-      R sk = s.shp[k * np + p];
-      for (int i = 0; i < 6; ++i) de[i] = de[i] + (R)s.co[i * nc + c] * sk;
-      for (int i = 0; i < 3; ++i) vort[i] = vort[i] + (R)s.cw[i * nc + c] * sk;
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] + sk * (R)s.cdefp[(i * 3 + j) * nc + c];
-    }
-  } else {
-    if (s.icell[p] < 0) return;
-    for (int k = 0; k < g.K; ++k) {
-      int n = s.snode[k * np + p];
-      if (n < 0) continue;
-      if (!(s.mg[n] > g.cutoff)) continue;
-      R v[3] = {(R)s.vg[n], (R)s.vg[nn + n], (R)s.vg[2LL * nn + n]};
-      const long long idx = k * np + p;
-      R dx = s.dndx[idx], dy = s.dndy[idx], dz = s.dndz[idx];
-      de[0] = de[0] + dx * v[0];
-      de[1] = de[1] + dy * v[1];
-      de[2] = de[2] + dz * v[2];
-      de[3] = de[3] + (dy * v[2] + dz * v[1]);
-      de[4] = de[4] + (dz * v[0] + dx * v[2]);
-      de[5] = de[5] + (dx * v[1] + dy * v[0]);
-      vort[0] = vort[0] + (dy * v[2] - dz * v[1]);
-      vort[1] = vort[1] + (dz * v[0] - dx * v[2]);
-      vort[2] = vort[2] + (dx * v[1] - dy * v[0]);
-      for (int i = 0; i < 3; ++i) {
-        deFp[i][0] = deFp[i][0] + dx * v[i];
-        deFp[i][1] = deFp[i][1] + dy * v[i];
-        deFp[i][2] = deFp[i][2] + dz * v[i];
-      }
-    }
-  }
-  const DevScalars& sc = *s.sc;
-  const R DT = (R)sc.dt;
-  for (int i = 0; i < 6; ++i) de[i] = de[i] * DT;
-  for (int i = 0; i < 3; ++i) vort[i] = vort[i] * DT / (R)2.0;
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] * DT;
-  R Fpn[3][3];
-  if (g.uvfp) {
-    R F0[3][3];
-    for (int i = 0; i < 9; ++i) F0[i / 3][i % 3] = (R)s.fp[i * np + p];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        Fpn[i][j] = F0[i][j] + deFp[i][j] + deFp[i][0] * F0[0][j] + deFp[i][1] * F0[1][j] + deFp[i][2] * F0[2][j];
-        s.fp[(i * 3 + j) * np + p] = (B)Fpn[i][j];
-      }
-  }
+// Particle state read and written by one Constitution call
+// (Constitution.f90:79-368); sd in storage order xx, yy, zz, xy, yz, xz.
+template <class R>
+struct PState {
+  R vol, epeff, sig_y, seqv, lt, celsius, ie, mass, dmg, cp, sm, q;
+  R sd[6];
+  bool failure;
+};
 
-  // ---- Constitution
-  const DevBody& bd = s.bodies[s.body[p]];
-  const DevMaterial& mt = s.mats[bd.mat];
+// What the caller must do after the call: the Johnson-Cook tail (tail 4 / 7)
+// deferred to the depeff carried from the previous particle, the value this
+// particle assigned to depeff, and health flags.
+template <class R>
+struct CResult {
+  int tail;
+  bool defer, dep_set, eos_ok, negative_volume;
+  R depeff, vold, ieinc, dvol, smold, vol_;
+};
+
+// Constitution (Constitution.f90:79-368) for one particle: volume update,
+// material constants, the material model of the particle's material and the
+// write-back of Constitution.f90:351-366.
+template <class P>
+__device__ __forceinline__ void constitution(PState<typename P::R>& ps, const DevMaterial& mt,
+                                             const typename P::R de[6], const typename P::R vort[3],
+                                             const typename P::R deFp[3][3], const typename P::R Fpn[3][3],
+                                             bool uvfp, typename P::R DT, double time, typename P::R dcell,
+                                             typename P::R bq1, typename P::R bq2,
+                                             CResult<typename P::R>& res) {
+  using R = typename P::R;
   Mm<R> m;
   m.dep_set = false;
   m.depeff = (R)0;
   m.bfac = (R)0;
   for (int i = 0; i < 6; ++i) m.dinc[i] = de[i];
-  m.vold = (R)s.vol[p];
-  if (g.uvfp) {
+  m.vold = ps.vol;
+  if (uvfp) {
     R dF[3][3];
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         dF[i][j] = deFp[i][j];
         m.Fp[i][j] = Fpn[i][j];
+        m.H[i][j] = Fpn[i][j];
       }
     for (int i = 0; i < 3; ++i) {
       dF[i][i] = dF[i][i] + (R)1.0;
@@ -442,18 +403,25 @@ __global__ void k_stress(St<P> s, Geometry g) {
     m.vol_ = m.vold * det3(dF);
   } else {
     m.vol_ = m.vold * ((R)1 + de[0] + de[1] + de[2]);
+    // without UpdateVbyFp the reference's module variable Fp is never set
+    // (zero from program start)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        m.Fp[i][j] = (R)0;
+        m.H[i][j] = i == j ? (R)-1 : (R)0;
+      }
   }
   R vol_store = m.vol_;
-  if (m.vol_ < (R)0) atomicOr(&s.sc->status, (unsigned)ST_NEGATIVE_VOLUME);
+  res.negative_volume = m.vol_ < (R)0;
   m.dvol = (R)0.5 * (m.vol_ - m.vold);
-  m.epeff_ = (R)s.epeff[p];
-  m.sig_y_ = (R)s.sig_y[p];
-  m.seqv = (R)s.seqv[p];
-  const R ltim = (R)s.lt[p];
-  m.tmprt = (R)s.celsius[p];
-  m.iener = (R)s.ie[p];
-  const R mp_ = (R)s.mass[p];
-  bool failure = s.failure[p] != 0;
+  m.epeff_ = ps.epeff;
+  m.sig_y_ = ps.sig_y;
+  m.seqv = ps.seqv;
+  const R ltim = ps.lt;
+  m.tmprt = ps.celsius;
+  m.iener = ps.ie;
+  const R mp_ = ps.mass;
+  bool failure = ps.failure;
   const bool was_failed = failure;
   m.miu2 = (R)2 * (R)mt.miu;
   m.young_ = (R)mt.young;
@@ -466,7 +434,7 @@ __global__ void k_stress(St<P> s, Geometry g) {
   m.mu = m.den_ / m.den0_ - (R)1;
   m.rv = m.vol_ / m.vol0_;
   m.specen = m.iener / m.vol0_;
-  m.DMG = (R)s.dmg[p];
+  m.DMG = ps.dmg;
   m.oldDMG = m.DMG;
   if constexpr (P::kExact)
     m.young_ = m.young_ * ((R)1.0 - m.DMG + (R)2.220446049250313e-16);
@@ -476,16 +444,16 @@ __global__ void k_stress(St<P> s, Geometry g) {
   m.K3 = m.young_ / ((R)1 - (R)2 * m.poisson_);
   m.lamda = (m.young_ * m.poisson_) / (((R)1 + m.poisson_) * ((R)1 - (R)2 * m.poisson_));
   m.PlaMod = m.young_ * tangmod_ / (m.young_ - tangmod_);
-  m.cp = (R)s.cp[p];
-  m.sm = (R)s.sm[p];
+  m.cp = ps.cp;
+  m.sm = ps.sm;
   m.smold = m.sm;
   // sd(1..6) = SDxx, SDyy, SDzz, SDyz, SDxz, SDxy (Constitution.f90:184-189)
-  m.sd[0] = (R)s.sd[p];
-  m.sd[1] = (R)s.sd[np + p];
-  m.sd[2] = (R)s.sd[2 * np + p];
-  m.sd[3] = (R)s.sd[4 * np + p];
-  m.sd[4] = (R)s.sd[5 * np + p];
-  m.sd[5] = (R)s.sd[3 * np + p];
+  m.sd[0] = ps.sd[0];
+  m.sd[1] = ps.sd[1];
+  m.sd[2] = ps.sd[2];
+  m.sd[3] = ps.sd[4];
+  m.sd[4] = ps.sd[5];
+  m.sd[5] = ps.sd[3];
   m.sig[0] = m.sd[0] + m.sm;
   m.sig[1] = m.sd[1] + m.sm;
   m.sig[2] = m.sd[2] + m.sm;
@@ -494,7 +462,6 @@ __global__ void k_stress(St<P> s, Geometry g) {
   m.sig[5] = m.sd[5];
   for (int i = 0; i < 6; ++i) m.sold[i] = m.sd[i];
   m.bqf = (R)0.0;
-  const R dcell = (R)g.dcell, bq1 = (R)g.bq1, bq2 = (R)g.bq2;
   bool eos_ok = true;
   bool defer = false;  // Johnson-Cook tail needs the carried depeff
   int tail = 0;        // 4: celsius update only, 7: failure + damage tail
@@ -598,7 +565,7 @@ __global__ void k_stress(St<P> s, Geometry g) {
       }
       break;
     case 8:
-      m.bfac = sc.time > (double)ltim ? (R)1.0 : (R)0.0;  // M3DM6
+      m.bfac = time > (double)ltim ? (R)1.0 : (R)0.0;  // M3DM6
       eos_ok = seleos<P>(m, mt, failure, DT, dcell, bq1, bq2);
       break;
     case 9:
@@ -617,42 +584,152 @@ __global__ void k_stress(St<P> s, Geometry g) {
     default:
       eos_ok = false;
   }
-  if (!eos_ok) atomicOr(&s.sc->status, (unsigned)ST_BAD_EOS);
+  res.eos_ok = eos_ok;
   if (tail != 0 && !defer) {
     // this particle assigned depeff itself: finish now with its own value
     if (tail == 7) jc7_tail<P>(m, mt, failure, m.depeff, vol_store);
     R den_ = m.den_;
-    s.celsius[p] = (B)((R)s.celsius[p] + m.seqv * m.depeff / den_ / (R)mt.specheat);
+    ps.celsius = ps.celsius + m.seqv * m.depeff / den_ / (R)mt.specheat;
   }
-  if (defer && tail == 7) {
+  res.tail = tail;
+  res.defer = defer;
+  res.dep_set = m.dep_set;
+  res.depeff = m.depeff;
+  res.vold = m.vold;
+  res.ieinc = m.ieinc;
+  res.dvol = m.dvol;
+  res.smold = m.smold;
+  res.vol_ = m.vol_;
+  ps.vol = vol_store;
+  ps.sm = m.sm;
+  ps.seqv = m.seqv;
+  ps.sd[0] = m.sd[0];
+  ps.sd[1] = m.sd[1];
+  ps.sd[2] = m.sd[2];
+  ps.sd[4] = m.sd[3];
+  ps.sd[5] = m.sd[4];
+  ps.sd[3] = m.sd[5];
+  ps.sig_y = m.sig_y_;
+  ps.epeff = m.epeff_;
+  ps.ie = m.iener;
+  ps.cp = m.cp;
+  ps.q = m.bqf;
+  ps.failure = failure;
+}
+
+template <class P>
+__global__ void k_stress(St<P> s, Geometry g) {
+  using R = typename P::R;
+  using B = typename P::B;
+  const long long p = gtid();
+  if (p >= g.np) return;
+  const long long np = g.np;
+  const int nn = g.nn;
+  if (g.has_jc) {
+    s.setter[p] = -1;
+    s.deferred[p] = 0;
+  }
+  R de[6] = {0, 0, 0, 0, 0, 0}, vort[3] = {0, 0, 0}, deFp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  if (g.shape == 3) {
+    if (s.centericell[p] < 0) return;
+    const long long nc = g.ncell;
+    for (int k = 0; k < 8; ++k) {
+      int c = s.snode[k * np + p];
+      if (c < 0) continue;
+      R sk = s.shp[k * np + p];
+      for (int i = 0; i < 6; ++i) de[i] = de[i] + (R)s.co[i * nc + c] * sk;
+      for (int i = 0; i < 3; ++i) vort[i] = vort[i] + (R)s.cw[i * nc + c] * sk;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] + sk * (R)s.cdefp[(i * 3 + j) * nc + c];
+    }
+  } else {
+    if (s.icell[p] < 0) return;
+    for (int k = 0; k < g.K; ++k) {
+      int n = s.snode[k * np + p];
+      if (n < 0) continue;
+      if (!(s.mg[n] > g.cutoff)) continue;
+      R v[3] = {(R)s.vg[n], (R)s.vg[nn + n], (R)s.vg[2LL * nn + n]};
+      const long long idx = k * np + p;
+      R dx = s.dndx[idx], dy = s.dndy[idx], dz = s.dndz[idx];
+      de[0] = de[0] + dx * v[0];
+      de[1] = de[1] + dy * v[1];
+      de[2] = de[2] + dz * v[2];
+      de[3] = de[3] + (dy * v[2] + dz * v[1]);
+      de[4] = de[4] + (dz * v[0] + dx * v[2]);
+      de[5] = de[5] + (dx * v[1] + dy * v[0]);
+      vort[0] = vort[0] + (dy * v[2] - dz * v[1]);
+      vort[1] = vort[1] + (dz * v[0] - dx * v[2]);
+      vort[2] = vort[2] + (dx * v[1] - dy * v[0]);
+      for (int i = 0; i < 3; ++i) {
+        deFp[i][0] = deFp[i][0] + dx * v[i];
+        deFp[i][1] = deFp[i][1] + dy * v[i];
+        deFp[i][2] = deFp[i][2] + dz * v[i];
+      }
+    }
+  }
+  const DevScalars& sc = *s.sc;
+  const R DT = (R)sc.dt;
+  for (int i = 0; i < 6; ++i) de[i] = de[i] * DT;
+  for (int i = 0; i < 3; ++i) vort[i] = vort[i] * DT / (R)2.0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] * DT;
+  R Fpn[3][3];
+  if (g.uvfp) {
+    R F0[3][3];
+    for (int i = 0; i < 9; ++i) F0[i / 3][i % 3] = (R)s.fp[i * np + p];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Fpn[i][j] = F0[i][j] + deFp[i][j] + deFp[i][0] * F0[0][j] + deFp[i][1] * F0[1][j] + deFp[i][2] * F0[2][j];
+        s.fp[(i * 3 + j) * np + p] = (B)Fpn[i][j];
+      }
+  }
+
+  // ---- Constitution
+  PState<R> ps;
+  ps.vol = (R)s.vol[p];
+  ps.epeff = (R)s.epeff[p];
+  ps.sig_y = (R)s.sig_y[p];
+  ps.seqv = (R)s.seqv[p];
+  ps.lt = (R)s.lt[p];
+  ps.celsius = (R)s.celsius[p];
+  ps.ie = (R)s.ie[p];
+  ps.mass = (R)s.mass[p];
+  ps.dmg = (R)s.dmg[p];
+  ps.cp = (R)s.cp[p];
+  ps.sm = (R)s.sm[p];
+  ps.q = (R)s.q[p];
+  for (int i = 0; i < 6; ++i) ps.sd[i] = (R)s.sd[i * np + p];
+  ps.failure = s.failure[p] != 0;
+  const DevMaterial& mt = s.mats[s.bodies[s.body[p]].mat];
+  CResult<R> res;
+  constitution<P>(ps, mt, de, vort, deFp, Fpn, g.uvfp != 0, DT, s.sc->time, (R)g.dcell, (R)g.bq1, (R)g.bq2, res);
+  if (res.negative_volume) atomicOr(&s.sc->status, (unsigned)ST_NEGATIVE_VOLUME);
+  if (!res.eos_ok) atomicOr(&s.sc->status, (unsigned)ST_BAD_EOS);
+  if (res.defer && res.tail == 7) {
     // park the values the tail needs (Constitution.f90:285-314)
-    s.jc_aux[p] = (double)m.vold;
-    s.jc_aux[np + p] = (double)m.ieinc;
-    s.jc_aux[2 * np + p] = (double)m.dvol;
-    s.jc_aux[3 * np + p] = (double)m.smold;
-    s.jc_aux[4 * np + p] = (double)m.vol_;
+    s.jc_aux[p] = (double)res.vold;
+    s.jc_aux[np + p] = (double)res.ieinc;
+    s.jc_aux[2 * np + p] = (double)res.dvol;
+    s.jc_aux[3 * np + p] = (double)res.smold;
+    s.jc_aux[4 * np + p] = (double)res.vol_;
   }
   if (g.has_jc) {
-    s.setter[p] = m.dep_set ? (int)p : -1;
-    if (m.dep_set) s.dep[p] = (double)m.depeff;
-    s.deferred[p] = defer ? (uint8_t)tail : 0;
+    s.setter[p] = res.dep_set ? (int)p : -1;
+    if (res.dep_set) s.dep[p] = (double)res.depeff;
+    s.deferred[p] = res.defer ? (uint8_t)res.tail : 0;
   }
-  s.vol[p] = (B)vol_store;
-  s.sm[p] = (B)m.sm;
-  s.seqv[p] = (B)m.seqv;
-  s.sd[p] = (B)m.sd[0];
-  s.sd[np + p] = (B)m.sd[1];
-  s.sd[2 * np + p] = (B)m.sd[2];
-  s.sd[4 * np + p] = (B)m.sd[3];
-  s.sd[5 * np + p] = (B)m.sd[4];
-  s.sd[3 * np + p] = (B)m.sd[5];
-  s.sig_y[p] = (B)m.sig_y_;
-  s.epeff[p] = (B)m.epeff_;
-  s.ie[p] = (double)m.iener;
-  s.cp[p] = (B)m.cp;
-  s.q[p] = (B)m.bqf;
-  s.failure[p] = failure ? 1 : 0;
-  if (!isfinite((double)m.sm) || !isfinite((double)m.iener)) atomicOr(&s.sc->status, (unsigned)ST_NONFINITE);
+  s.vol[p] = (B)ps.vol;
+  s.sm[p] = (B)ps.sm;
+  s.seqv[p] = (B)ps.seqv;
+  for (int i = 0; i < 6; ++i) s.sd[i * np + p] = (B)ps.sd[i];
+  s.sig_y[p] = (B)ps.sig_y;
+  s.epeff[p] = (B)ps.epeff;
+  s.ie[p] = (double)ps.ie;
+  s.cp[p] = (B)ps.cp;
+  s.q[p] = (B)ps.q;
+  s.celsius[p] = (B)ps.celsius;
+  s.failure[p] = ps.failure ? 1 : 0;
+  if (!isfinite((double)ps.sm) || !isfinite((double)ps.ie)) atomicOr(&s.sc->status, (unsigned)ST_NONFINITE);
   if (!g.usf) {
     s.xp[p] = s.xx[p];
     s.xp[np + p] = s.xx[np + p];

@@ -167,6 +167,7 @@ struct Mm {
   R dinc[6], sig[6], sd[6], sold[6], sm, smold, bqf, seqv, epeff_, sig_y_, depeff, ratio;
   R G2, K3, PlaMod, lamda, miu2, young_, poisson_, yield0_, tmprt, cp, DMG, oldDMG, bfac;
   R Fp[3][3];
+  R H[3][3];     // Fp - I as stored per particle (the mixed form works from it)
   bool dep_set;  // this particle assigned the module variable depeff
 };
 
@@ -410,17 +411,37 @@ __device__ __forceinline__ void m3dm10(Mm<typename P::R>& m) {
   using R = typename P::R;
   const R (*F)[3] = m.Fp;
   R G = (R)0.5 * m.G2;
-  R J = det3(m.Fp);
   R B[6];
-  B[0] = F[0][0] * F[0][0] + F[0][1] * F[0][1] + F[0][2] * F[0][2] - (R)1.0;
-  B[1] = F[1][0] * F[1][0] + F[1][1] * F[1][1] + F[1][2] * F[1][2] - (R)1.0;
-  B[2] = F[2][0] * F[2][0] + F[2][1] * F[2][1] + F[2][2] * F[2][2] - (R)1.0;
-  B[3] = F[0][0] * F[1][0] + F[0][1] * F[1][1] + F[0][2] * F[1][2];
-  B[4] = F[1][0] * F[2][0] + F[1][1] * F[2][1] + F[1][2] * F[2][2];
-  B[5] = F[0][0] * F[2][0] + F[0][1] * F[2][1] + F[0][2] * F[2][2];
+  R iJ, lj;
+  if constexpr (P::kExact) {
+    R J = det3(m.Fp);
+    B[0] = F[0][0] * F[0][0] + F[0][1] * F[0][1] + F[0][2] * F[0][2] - (R)1.0;
+    B[1] = F[1][0] * F[1][0] + F[1][1] * F[1][1] + F[1][2] * F[1][2] - (R)1.0;
+    B[2] = F[2][0] * F[2][0] + F[2][1] * F[2][1] + F[2][2] * F[2][2] - (R)1.0;
+    B[3] = F[0][0] * F[1][0] + F[0][1] * F[1][1] + F[0][2] * F[1][2];
+    B[4] = F[1][0] * F[2][0] + F[1][1] * F[2][1] + F[1][2] * F[2][2];
+    B[5] = F[0][0] * F[2][0] + F[0][1] * F[2][1] + F[0][2] * F[2][2];
+    iJ = (R)1.0 / J;
+    lj = m_log<P>(J);
+  } else {
+    // the same quantities from H = F - I without cancellation, which FP32
+    // needs for nearly incompressible materials (J - 1 and B - I ~ 1e-6):
+    // B - I = H + H^T + H H^T;  J - 1 = tr H + I2(H) + det H;  ln J = log1p(J - 1)
+    const R (*H)[3] = m.H;
+    auto hh = [&](int i, int j) { return H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2]; };
+    B[0] = (R)2 * H[0][0] + hh(0, 0);
+    B[1] = (R)2 * H[1][1] + hh(1, 1);
+    B[2] = (R)2 * H[2][2] + hh(2, 2);
+    B[3] = H[0][1] + H[1][0] + hh(0, 1);
+    B[4] = H[1][2] + H[2][1] + hh(1, 2);
+    B[5] = H[0][2] + H[2][0] + hh(0, 2);
+    R i2 = H[0][0] * H[1][1] + H[1][1] * H[2][2] + H[0][0] * H[2][2] - H[0][1] * H[1][0] - H[1][2] * H[2][1] -
+           H[0][2] * H[2][0];
+    R jm1 = (H[0][0] + H[1][1] + H[2][2]) + i2 + det3(H);
+    iJ = (R)1.0 / ((R)1.0 + jm1);
+    lj = log1pf(jm1);
+  }
   m.ieinc = sig_work(m);
-  R iJ = (R)1.0 / J;
-  R lj = m_log<P>(J);
   R* sig = m.sig;
   sig[0] = iJ * (G * B[0] + m.lamda * lj * (R)1.0);
   sig[1] = iJ * (G * B[1] + m.lamda * lj * (R)1.0);

@@ -1,0 +1,427 @@
+// mpm_serve.cu -- serving runtime over the batched step (C ABI in
+// include/mpm3d_gpu.h, mpm_serve_*).
+//
+// One server thread owns the device batch. Client threads only touch the
+// ticket table and the submission queue under the server mutex; staging a
+// scene (deck -> host set-up and input copy) runs on the client thread.
+//
+// Server loop:
+//   1. admit queued scenes first-come first-served while the estimated device
+//      bytes of the resident scenes stay within the budget;
+//   2. run min(chunk_steps, steps until the next scene finishes) steps of the
+//      batch (graph replays; the batch recaptures after a composition change);
+//   3. read every resident scene's progress in one copy, snapshot the fields
+//      of the finished ones, retire them and wake their waiters.
+// The launch shape autotuner times the candidate (particle block, node block)
+// pairs on the first chunks (a launch shape changes no result) and keeps the
+// fastest per particle-step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "mpm3d_gpu.h"
+#include "mpm_batch_host.h"
+
+using mpm::BatchProgress;
+using mpm::HostScene;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_since(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+enum TicketState { T_QUEUED, T_RESIDENT, T_DONE, T_FAILED };
+
+struct Ticket {
+  int64_t id = 0;
+  TicketState state = T_QUEUED;
+  int code = MPM_OK;
+  std::string err;
+  HostScene* scene = nullptr;  // owned while queued
+  long long bytes = 0, np = 0;
+  int steps = 0;
+  uint32_t mask = 0;
+  int scene_id = -1;
+  Clock::time_point t_submit, t_admit, t_done;
+  double scalars[MPM_NSCALARS] = {};
+  std::map<int, std::vector<double>> fields;
+};
+
+struct Tune {
+  int pb, nb;
+  double ms = 0, work = 0;  // accumulated time and particle-steps
+};
+
+}  // namespace
+
+struct mpm_server {
+  mpm_serve_config cfg{};
+  mpm_batch* batch = nullptr;
+  std::thread thr;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  bool stop = false;
+  std::deque<int64_t> queue;
+  std::map<int64_t, Ticket*> tickets;
+  std::map<int, int64_t> by_scene;  // resident scene id -> ticket
+  int64_t next_ticket = 1;
+  long long resident_bytes = 0, peak_bytes = 0;
+  // statistics
+  long long submitted = 0, finished = 0, chunks = 0;
+  double particle_steps = 0, busy_ms = 0;
+  int pb = 256, nb = 256;
+  std::vector<Tune> tune;
+  size_t tune_next = 0;
+  int tune_rounds = 0;
+  bool tuned = false;
+  std::string err;
+};
+
+namespace {
+
+int serr(mpm_server* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (s) s->err = buf;
+  return code;
+}
+
+// fail every ticket that is resident (after a batch error) -- caller holds mu
+void fail_resident(mpm_server* s, int code, const std::string& msg) {
+  for (auto& kv : s->by_scene) {
+    auto it = s->tickets.find(kv.second);
+    if (it == s->tickets.end()) continue;
+    Ticket* t = it->second;
+    t->state = T_FAILED;
+    t->code = code;
+    t->err = msg;
+    t->t_done = Clock::now();
+  }
+  s->by_scene.clear();
+  s->resident_bytes = 0;
+}
+
+void serve_loop(mpm_server* s) {
+  cudaSetDevice(s->cfg.device);
+  std::vector<BatchProgress> prog;
+  std::vector<int> retire;
+  for (;;) {
+    // 1. admission (under the lock: the queue and tickets are shared)
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      for (;;) {
+        if (s->stop) return;
+        while (!s->queue.empty()) {
+          Ticket* t = s->tickets[s->queue.front()];
+          if ((int)s->by_scene.size() >= s->cfg.max_scenes) break;
+          if (s->resident_bytes + t->bytes > s->cfg.hbm_budget_bytes) {
+            if (s->by_scene.empty()) {  // can never fit: fail it rather than block the queue
+              t->state = T_FAILED;
+              t->code = MPM_ERR_OOM;
+              t->err = "scene needs more device memory than the serving budget";
+              t->t_done = Clock::now();
+              delete t->scene;
+              t->scene = nullptr;
+              s->queue.pop_front();
+              s->cv_done.notify_all();
+              continue;
+            }
+            break;
+          }
+          int id = -1;
+          mpm::batch_insert(s->batch, t->scene, &id);
+          t->scene = nullptr;  // the batch owns it now
+          t->scene_id = id;
+          t->state = T_RESIDENT;
+          t->t_admit = Clock::now();
+          s->by_scene[id] = t->id;
+          s->resident_bytes += t->bytes;
+          s->peak_bytes = std::max(s->peak_bytes, s->resident_bytes);
+          s->queue.pop_front();
+        }
+        if (!s->by_scene.empty()) break;
+        s->cv_work.wait(lk);
+      }
+    }
+    // 2. a chunk of steps (server thread only touches the batch)
+    int r = mpm_batch_commit(s->batch);
+    if (r == MPM_OK) r = mpm::batch_progress(s->batch, prog);
+    int left = 0;
+    if (r == MPM_OK) mpm::batch_remaining(s->batch, prog, &left);
+    int k = std::max(1, std::min(s->cfg.chunk_steps, left > 0 ? left : 1));
+    double work = 0;  // particle-steps this chunk runs (parked scenes do no work)
+    for (const BatchProgress& q : prog) work += (double)q.np * std::max(0, std::min(k, q.target - q.istep));
+    Tune* trial = nullptr;
+    if (r == MPM_OK && s->cfg.autotune && !s->tuned) {
+      trial = &s->tune[s->tune_next];
+      r = mpm_batch_set_blocks(s->batch, trial->pb, trial->nb);
+    }
+    double ms = 0;
+    if (r == MPM_OK) r = mpm_batch_time_steps(s->batch, k, 1, &ms);
+    if (r == MPM_OK && trial) {
+      trial->ms += ms;
+      trial->work += work;
+      s->tune_next++;
+      if (s->tune_next == s->tune.size()) {
+        // two rounds over the candidates, then keep the best
+        bool measured = true;
+        for (auto& c : s->tune) measured = measured && c.work > 0;
+        if (measured && ++s->tune_rounds >= 2) {
+          const Tune* best = &s->tune[0];
+          for (auto& c : s->tune)
+            if (c.ms / c.work < best->ms / best->work) best = &c;
+          s->pb = best->pb;
+          s->nb = best->nb;
+          s->tuned = true;
+          r = mpm_batch_set_blocks(s->batch, s->pb, s->nb);
+        }
+        s->tune_next = 0;
+      }
+    }
+    // 3. retirement
+    if (r == MPM_OK) r = mpm::batch_progress(s->batch, prog);
+    retire.clear();
+    std::vector<Ticket*> done;
+    if (r == MPM_OK) {
+      for (const BatchProgress& q : prog)
+        if (q.istep >= q.target) retire.push_back(q.id);
+      std::vector<Ticket*> owners;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (int id : retire) owners.push_back(s->tickets[s->by_scene[id]]);
+      }
+      for (size_t i = 0; i < retire.size() && r == MPM_OK; ++i) {
+        Ticket* t = owners[i];
+        r = mpm_batch_scene_scalars(s->batch, retire[i], t->scalars);
+        for (int f = 1; f <= 25 && r == MPM_OK; ++f)
+          if (t->mask & (1u << f)) {
+            int nc = mpm_field_components(f);
+            std::vector<double> buf((size_t)(nc * t->np));
+            r = mpm_batch_scene_download(s->batch, retire[i], f, buf.data());
+            if (r == MPM_OK) t->fields[f].swap(buf);
+          }
+        if (r == MPM_OK) r = mpm_batch_remove(s->batch, retire[i]);
+        if (r == MPM_OK) done.push_back(t);
+      }
+    }
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (r == MPM_OK) {
+        s->chunks++;
+        s->particle_steps += work;
+        s->busy_ms += ms;
+        Clock::time_point now = Clock::now();
+        for (Ticket* t : done) {
+          t->state = T_DONE;
+          t->t_done = now;
+          s->by_scene.erase(t->scene_id);
+          s->resident_bytes -= t->bytes;
+          s->finished++;
+        }
+      } else {
+        std::string msg = mpm_batch_last_error(s->batch);
+        fail_resident(s, r, msg);
+        // start over with an empty batch
+        mpm_batch_destroy(s->batch);
+        s->batch = nullptr;
+        if (mpm_batch_create(s->cfg.device, &s->batch) != MPM_OK) {
+          s->stop = true;
+          s->err = "batch lost after error: " + msg;
+        } else {
+          mpm_batch_set_blocks(s->batch, s->pb, s->nb);
+        }
+      }
+    }
+    s->cv_done.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_serve_create(const mpm_serve_config* cfg, mpm_server** out) {
+  if (!out) return MPM_ERR_ARG;
+  *out = nullptr;
+  mpm_server* s = new mpm_server();
+  if (cfg) s->cfg = *cfg;
+  if (s->cfg.device < 0) cudaGetDevice(&s->cfg.device);
+  if (s->cfg.chunk_steps <= 0) s->cfg.chunk_steps = 25;
+  if (s->cfg.max_scenes <= 0) s->cfg.max_scenes = 4096;
+  int r = mpm_batch_create(s->cfg.device, &s->batch);
+  if (r) {
+    delete s;
+    return r;
+  }
+  if (s->cfg.hbm_budget_bytes <= 0) {
+    size_t fr = 0, tot = 0;
+    cudaSetDevice(s->cfg.device);
+    cudaMemGetInfo(&fr, &tot);
+    s->cfg.hbm_budget_bytes = (int64_t)(0.8 * (double)fr);
+  }
+  if (s->cfg.autotune) {
+    const int cand[3] = {128, 256, 512};
+    for (int a : cand)
+      for (int b2 : cand) s->tune.push_back(Tune{a, b2});
+  }
+  s->thr = std::thread(serve_loop, s);
+  *out = s;
+  return MPM_OK;
+}
+
+void mpm_serve_destroy(mpm_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->thr.joinable()) s->thr.join();
+  if (s->batch) mpm_batch_destroy(s->batch);
+  for (auto& kv : s->tickets) {
+    delete kv.second->scene;
+    delete kv.second;
+  }
+  delete s;
+}
+
+const char* mpm_serve_last_error(const mpm_server* s) { return s ? s->err.c_str() : "null server"; }
+
+int mpm_serve_submit(mpm_server* s, const mpm_deck* d, int steps, uint32_t field_mask, int64_t* ticket) {
+  if (!s || !d || !ticket || steps < 1) return serr(s, MPM_ERR_ARG, "bad argument");
+  Clock::time_point t0 = Clock::now();
+  std::string err;
+  int code = MPM_OK;
+  HostScene* h = mpm::scene_stage(d, steps, err, &code);
+  if (!h) return serr(s, code, "%s", err.c_str());
+  Ticket* t = new Ticket();
+  t->scene = h;
+  t->bytes = mpm::scene_device_bytes(h);
+  t->np = mpm::scene_np(h);
+  t->steps = steps;
+  t->mask = field_mask;
+  t->t_submit = t0;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) {
+      delete h;
+      delete t;
+      return serr(s, MPM_ERR_STATE, "server stopped: %s", s->err.c_str());
+    }
+    t->id = s->next_ticket++;
+    s->tickets[t->id] = t;
+    s->queue.push_back(t->id);
+    s->submitted++;
+    *ticket = t->id;
+  }
+  s->cv_work.notify_all();
+  return MPM_OK;
+}
+
+int mpm_serve_wait(mpm_server* s, int64_t ticket, int timeout_ms) {
+  if (!s) return MPM_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return serr(s, MPM_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  Ticket* t = it->second;
+  auto ready = [&] { return t->state == T_DONE || t->state == T_FAILED || s->stop; };
+  if (timeout_ms < 0)
+    s->cv_done.wait(lk, ready);
+  else
+    s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready);
+  if (t->state == T_DONE) return MPM_OK;
+  if (t->state == T_FAILED) return serr(s, t->code, "%s", t->err.c_str());
+  if (s->stop) return serr(s, MPM_ERR_STATE, "server stopped: %s", s->err.c_str());
+  return MPM_ERR_TIMEOUT;
+}
+
+int mpm_serve_result(mpm_server* s, int64_t ticket, double* scalars16, double* times_ms3) {
+  if (!s) return MPM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return serr(s, MPM_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  Ticket* t = it->second;
+  if (t->state == T_FAILED) return serr(s, t->code, "%s", t->err.c_str());
+  if (t->state != T_DONE) return serr(s, MPM_ERR_STATE, "ticket %lld has not finished", (long long)ticket);
+  if (scalars16) memcpy(scalars16, t->scalars, sizeof t->scalars);
+  if (times_ms3) {
+    times_ms3[0] = ms_since(t->t_submit, t->t_admit);
+    times_ms3[1] = ms_since(t->t_admit, t->t_done);
+    times_ms3[2] = ms_since(t->t_submit, t->t_done);
+  }
+  return MPM_OK;
+}
+
+int mpm_serve_field(mpm_server* s, int64_t ticket, int field, double* out) {
+  if (!s || !out) return MPM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return serr(s, MPM_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  Ticket* t = it->second;
+  if (t->state != T_DONE) return serr(s, MPM_ERR_STATE, "ticket %lld has not finished", (long long)ticket);
+  auto f = t->fields.find(field);
+  if (f == t->fields.end()) return serr(s, MPM_ERR_ARG, "field %d was not requested at submission", field);
+  memcpy(out, f->second.data(), sizeof(double) * f->second.size());
+  return MPM_OK;
+}
+
+int mpm_serve_release(mpm_server* s, int64_t ticket) {
+  if (!s) return MPM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return serr(s, MPM_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  Ticket* t = it->second;
+  if (t->state == T_QUEUED || t->state == T_RESIDENT)
+    return serr(s, MPM_ERR_STATE, "ticket %lld is still running", (long long)ticket);
+  delete t;
+  s->tickets.erase(it);
+  return MPM_OK;
+}
+
+int mpm_serve_stats(mpm_server* s, double* o) {
+  if (!s || !o) return MPM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  o[0] = (double)s->submitted;
+  o[1] = (double)s->finished;
+  o[2] = (double)s->queue.size();
+  o[3] = (double)s->by_scene.size();
+  o[4] = (double)s->chunks;
+  o[5] = s->particle_steps;
+  o[6] = s->busy_ms;
+  o[7] = s->pb;
+  o[8] = s->nb;
+  o[9] = (double)s->peak_bytes;
+  return MPM_OK;
+}
+
+int mpm_serve_drain(mpm_server* s, int timeout_ms) {
+  if (!s) return MPM_ERR_ARG;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto idle = [&] { return (s->queue.empty() && s->by_scene.empty()) || s->stop; };
+  if (timeout_ms < 0)
+    s->cv_done.wait(lk, idle);
+  else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle))
+    return MPM_ERR_TIMEOUT;
+  if (s->stop && !(s->queue.empty() && s->by_scene.empty()))
+    return serr(s, MPM_ERR_STATE, "server stopped: %s", s->err.c_str());
+  return MPM_OK;
+}
+
+}  // extern "C"

@@ -107,6 +107,33 @@ def library() -> ctypes.CDLL:
         "mpm_algorithmic_bytes": (i, [vp, P(d)]),
         "mpm_device_bytes": (i64, [vp]),
         "mpm_energy_reduce_noalloc": (i, [vp, vp, vp, i64, vp, vp]),
+        "mpm_batch_create": (i, [i, P(vp)]),
+        "mpm_batch_destroy": (None, [vp]),
+        "mpm_batch_add": (i, [vp, vp, i, P(i)]),
+        "mpm_batch_remove": (i, [vp, i]),
+        "mpm_batch_commit": (i, [vp]),
+        "mpm_scene_device_bytes": (i64, [vp]),
+        "mpm_batch_device_bytes": (i64, [vp]),
+        "mpm_batch_scene_count": (i, [vp]),
+        "mpm_batch_run": (i, [vp, i, i]),
+        "mpm_batch_sync": (i, [vp]),
+        "mpm_batch_time_steps": (i, [vp, i, i, P(d)]),
+        "mpm_batch_scene_scalars": (i, [vp, i, P(d)]),
+        "mpm_batch_scene_download": (i, [vp, i, i, P(d)]),
+        "mpm_batch_last_error": (c, [vp]),
+        "mpm_batch_set_blocks": (i, [vp, i, i]),
+        "mpm_batch_profile_enable": (i, [vp, i]),
+        "mpm_batch_kernel_stats": (i, [vp, i, c, i, P(i64), P(d)]),
+        "mpm_serve_create": (i, [vp, P(vp)]),
+        "mpm_serve_destroy": (None, [vp]),
+        "mpm_serve_last_error": (c, [vp]),
+        "mpm_serve_submit": (i, [vp, vp, i, ctypes.c_uint32, P(i64)]),
+        "mpm_serve_wait": (i, [vp, i64, i]),
+        "mpm_serve_result": (i, [vp, i64, P(d), P(d)]),
+        "mpm_serve_field": (i, [vp, i64, i, P(d)]),
+        "mpm_serve_release": (i, [vp, i64]),
+        "mpm_serve_stats": (i, [vp, P(d)]),
+        "mpm_serve_drain": (i, [vp, i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -322,4 +349,210 @@ class MpmStep:
         return int(library().mpm_device_bytes(self._h))
 
 
-__all__ = ["Deck", "MpmStep", "MpmError", "library", "FIELDS", "PHASES", "PRECISION", "LIB_PATH"]
+class Batch:
+    """Many independent scenes advanced together by the mixed-precision step.
+
+    Scenes are added (with a step count; 0 = until removed) and removed at any
+    time; the composition takes effect at the next :meth:`commit` or run.
+    Results of a scene do not depend on which other scenes share the batch.
+    """
+
+    def __init__(self, device: int = -1):
+        lib = library()
+        h = ctypes.c_void_p()
+        st = lib.mpm_batch_create(device, ctypes.byref(h))
+        if st:
+            raise MpmError(st, "mpm_batch_create failed")
+        self._h = h
+        self._scenes = {}
+
+    def _check(self, st: int) -> None:
+        if st:
+            raise MpmError(st, library().mpm_batch_last_error(self._h).decode(errors="replace"))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            library().mpm_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def scene_bytes(deck: Deck) -> int:
+        """Device memory a scene adds to a batch (admission estimate)."""
+        return int(library().mpm_scene_device_bytes(deck.handle))
+
+    def add(self, deck: Deck, steps: int = 0) -> int:
+        sid = ctypes.c_int()
+        self._check(library().mpm_batch_add(self._h, deck.handle, int(steps), ctypes.byref(sid)))
+        self._scenes[sid.value] = (deck.nb_particle, deck)
+        return sid.value
+
+    def remove(self, scene: int) -> None:
+        self._check(library().mpm_batch_remove(self._h, int(scene)))
+        self._scenes.pop(scene, None)
+
+    def commit(self) -> None:
+        self._check(library().mpm_batch_commit(self._h))
+
+    def run(self, nsteps: int, graph: bool = True) -> None:
+        self._check(library().mpm_batch_run(self._h, int(nsteps), int(bool(graph))))
+
+    def sync(self) -> None:
+        self._check(library().mpm_batch_sync(self._h))
+
+    def time_steps(self, nsteps: int, graph: bool = True) -> float:
+        ms = ctypes.c_double()
+        self._check(library().mpm_batch_time_steps(self._h, int(nsteps), int(bool(graph)), ctypes.byref(ms)))
+        return ms.value
+
+    def scalars(self, scene: int) -> dict:
+        o = np.zeros(16)
+        self._check(library().mpm_batch_scene_scalars(self._h, int(scene), _dptr(o)))
+        return dict(zip(SCALARS, o.tolist()))
+
+    def download(self, scene: int, field: str) -> np.ndarray:
+        ncomp = COMPONENTS.get(field, 1)
+        sc = self.scalars(scene)
+        if field in GRID_FIELDS:
+            n = int(sc["nb_gridnode"])
+        elif field in CELL_FIELDS:
+            raise MpmError(1, "cell fields are read per scene through MpmStep")
+        else:
+            n = int(sc["nb_particle"])
+        out = np.zeros(ncomp * n)
+        self._check(library().mpm_batch_scene_download(self._h, int(scene), FIELDS[field], _dptr(out)))
+        return out.reshape(ncomp, n) if ncomp > 1 else out
+
+    def set_blocks(self, particle_block: int = 0, node_block: int = 0) -> None:
+        self._check(library().mpm_batch_set_blocks(self._h, int(particle_block), int(node_block)))
+
+    def profile(self, on: bool = True) -> None:
+        self._check(library().mpm_batch_profile_enable(self._h, int(bool(on))))
+
+    def kernel_stats(self) -> list:
+        lib = library()
+        out = []
+        for k in range(lib.mpm_kernel_count(None)):
+            name = ctypes.create_string_buffer(64)
+            n = ctypes.c_int64()
+            ms = ctypes.c_double()
+            self._check(lib.mpm_batch_kernel_stats(self._h, k, name, 64, ctypes.byref(n), ctypes.byref(ms)))
+            out.append({"kernel": name.value.decode(), "launches": n.value, "total_ms": ms.value})
+        return out
+
+    def device_bytes(self) -> int:
+        return int(library().mpm_batch_device_bytes(self._h))
+
+    @property
+    def scene_count(self) -> int:
+        return int(library().mpm_batch_scene_count(self._h))
+
+
+class _ServeConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("chunk_steps", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_int64),
+                ("max_scenes", ctypes.c_int), ("autotune", ctypes.c_int)]
+
+
+SERVE_STATS = ("submitted", "finished", "queued", "resident", "chunks", "particle_steps", "busy_ms",
+               "particle_block", "node_block", "peak_resident_bytes")
+
+
+class Server:
+    """Serving runtime: scenes submitted from any thread are admitted into one
+    device-resident batch while they fit the device-memory budget, advanced in
+    chunks of steps and retired when they reach their step count."""
+
+    def __init__(self, device: int = -1, chunk_steps: int = 25, hbm_budget_bytes: int = 0,
+                 max_scenes: int = 0, autotune: bool = False):
+        lib = library()
+        cfg = _ServeConfig(device, chunk_steps, hbm_budget_bytes, max_scenes, int(bool(autotune)))
+        h = ctypes.c_void_p()
+        st = lib.mpm_serve_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st:
+            raise MpmError(st, "mpm_serve_create failed")
+        self._h = h
+        self._np = {}
+
+    def _check(self, st: int) -> None:
+        if st:
+            raise MpmError(st, library().mpm_serve_last_error(self._h).decode(errors="replace"))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            library().mpm_serve_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, deck: Deck, steps: int, fields=()) -> int:
+        mask = 0
+        for f in fields:
+            mask |= 1 << FIELDS[f]
+        t = ctypes.c_int64()
+        self._check(library().mpm_serve_submit(self._h, deck.handle, int(steps), mask, ctypes.byref(t)))
+        self._np[t.value] = deck.nb_particle
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> bool:
+        """True once the ticket finished, False on timeout; raises if it failed."""
+        st = library().mpm_serve_wait(self._h, int(ticket), int(timeout_ms))
+        if st == 8:
+            return False
+        self._check(st)
+        return True
+
+    def result(self, ticket: int) -> dict:
+        sc = np.zeros(16)
+        tm = np.zeros(3)
+        self._check(library().mpm_serve_result(self._h, int(ticket), _dptr(sc), _dptr(tm)))
+        out = dict(zip(SCALARS, sc.tolist()))
+        out.update({"queue_ms": tm[0], "resident_ms": tm[1], "latency_ms": tm[2]})
+        return out
+
+    def field(self, ticket: int, name: str) -> np.ndarray:
+        ncomp = COMPONENTS.get(name, 1)
+        n = self._np[ticket]
+        out = np.zeros(ncomp * n)
+        self._check(library().mpm_serve_field(self._h, int(ticket), FIELDS[name], _dptr(out)))
+        return out.reshape(ncomp, n) if ncomp > 1 else out
+
+    def release(self, ticket: int) -> None:
+        self._check(library().mpm_serve_release(self._h, int(ticket)))
+        self._np.pop(ticket, None)
+
+    def stats(self) -> dict:
+        o = np.zeros(10)
+        self._check(library().mpm_serve_stats(self._h, _dptr(o)))
+        return dict(zip(SERVE_STATS, o.tolist()))
+
+    def drain(self, timeout_ms: int = -1) -> bool:
+        st = library().mpm_serve_drain(self._h, int(timeout_ms))
+        if st == 8:
+            return False
+        self._check(st)
+        return True
+
+
+__all__ = ["Deck", "MpmStep", "Batch", "Server", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
+           "LIB_PATH"]

@@ -317,3 +317,89 @@ def cook_membrane(variant: str = "mpm", spacing: float = 0.5, young: float = 70.
 # Published tip vertical displacement (m) of the Cook membrane with 5776
 # particles (VolumetricLockingEx/ExamplesResults.pdf, Table 1), by variant.
 COOK_TIP_PUBLISHED = {"mpm": 0.2489, "gimp": 0.2512, "bimp": 0.2620, "sgmp": 0.2678}
+
+
+def _fast_points(ids_start: int, mat: int, mass: float, xyz: np.ndarray) -> str:
+    """'part poin' body lines for large point sets (vectorised formatting)."""
+    n = xyz.shape[0]
+    p = xyz.astype(np.float32).astype(np.float64)
+    ids = np.arange(ids_start, ids_start + n)
+    m = float(np.float32(mass))
+    cols = [ids.astype(str), np.full(n, str(mat)), np.full(n, "%.9g" % m)]
+    cols += [np.char.mod("%.9g", p[:, k]) for k in range(3)]
+    out = cols[0]
+    for c in cols[1:]:
+        out = np.char.add(np.char.add(out, " "), c)
+    return "\n".join(out.tolist())
+
+
+def serving_scene(rng: np.random.Generator, np_min: int = 2000, np_max: int = 400000,
+                  kind: Optional[str] = None) -> tuple[str, int, str]:
+    """One scene of the serving workload: a Cook membrane panel (extruded two
+    particles thick, plane strain through roller z faces) or a cantilever soft
+    beam, each with probability 1/2; particle count log-uniform in
+    [np_min, np_max]; cell size h = 2 x spacing (8 particles per cell);
+    neo-Hookean with E log-uniform in [1, 100] MPa, nu uniform in [0.3, 0.49],
+    rho 1000; SGMP with one extra grid layer beyond the clamped and roller
+    faces; MUSL. Returns (deck text, particle count, kind)."""
+    if kind is None:
+        kind = "cook" if rng.random() < 0.5 else "beam"
+    target = math.exp(rng.uniform(math.log(np_min), math.log(np_max)))
+    young = math.exp(rng.uniform(math.log(1e6), math.log(1e8)))
+    nu = rng.uniform(0.3, 0.49)
+    rho = 1000.0
+    if kind == "beam":
+        # 6 x 1 x 1 m beam clamped at x = 0
+        dp = (6.0 / target) ** (1.0 / 3.0)
+        nx, ny, nz = max(2, int(round(6.0 / dp))), max(2, int(round(1.0 / dp))), max(2, int(round(1.0 / dp)))
+        h = 2 * dp
+        w = DeckWriter("serving scene: soft beam, neo-Hookean, sgmp, musl")
+        w.kw("nmat 1")
+        lx, ly, lz = nx * dp, ny * dp, nz * dp
+        w.head += _grid_lines(((-h, lx + 2 * h), (0.0, ly), (0.0, lz + 4 * h)), h)
+        w.kw("dtsc 0.5")
+        w.kw("endt 100.0")
+        w.kw("musl on")
+        w.kw("sgmp")
+        w.kw("fixe 1 0 2 2 0 0")
+        w.kw("mate")
+        w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
+        w.block(1, rho, dp, (0.0, 0.0, 2 * h), (nx, ny, nz))
+        w.tail += ["load", f"grav 1 0 0 {f32s(-9.81)}", "endl"]
+        return w.text(), nx * ny * nz, kind
+    # Cook panel (48 x 44..60 m), two particles through the thickness
+    area = 48.0 * (44.0 + 16.0) / 2.0
+    dp = math.sqrt(2.0 * area / target)
+    xs = (np.arange(int(round(48 / dp))) + 0.5) * dp
+    ys = (np.arange(int(round(60 / dp))) + 0.5) * dp
+    X, Y = np.meshgrid(xs, ys)
+    X, Y = X.ravel(), Y.ravel()
+    keep = (Y >= 44.0 / 48.0 * X) & (Y <= 44.0 + 16.0 / 48.0 * X)
+    X, Y = X[keep], Y[keep]
+    h = 2 * dp
+    zs = np.array([0.5, 1.5]) * dp
+    xyz = np.concatenate([np.stack([X, Y, np.full_like(X, z)], axis=1) for z in zs])
+    n = xyz.shape[0]
+    mass = rho * area * (2 * dp) / n
+    w = DeckWriter("serving scene: Cook membrane, neo-Hookean, sgmp, musl")
+    w.kw("nmat 1")
+    w.head += _grid_lines(((-h, 48.0 + 2 * h), (-2 * h, 62.0 + 2 * h), (-h, 2 * dp + h)), h)
+    w.kw("fixe 1 0 0 0 2 2")
+    w.kw("dtsc 0.9")
+    w.kw("endt 30")
+    w.kw("musl on")
+    w.kw("sgmp")
+    w.kw("QuLo 15")
+    w.kw("Damp 0.3")
+    w.kw("mate")
+    w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
+    first = w.nbmp + 1
+    w.bodies.append(f"part poin 1 {n}\n" + _fast_points(first, 1, mass, xyz))
+    w.nbmp += n
+    w.nbbo += 1
+    right = np.where(np.isclose(xyz[:, 0], xs[-1]))[0]
+    total = young * 1e-3 * 16.0 * (2 * dp)  # shear traction 1e-3 E on the loaded edge
+    per = total / max(1, len(right))
+    loads = ["load"] + ["part %d 0 %s 0" % (i + 1, f32s(per)) for i in right] + ["endl"]
+    w.tail += loads
+    return w.text(), n, kind

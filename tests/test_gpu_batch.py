@@ -1,0 +1,175 @@
+"""Mixed-precision batched engine: accuracy against the FP64 GPU form, and the
+identity of a scene's results whatever else shares its batch (alone, mixed
+with other scenes, admitted mid-run, served by the serving runtime)."""
+import time
+
+import numpy as np
+import pytest
+
+from gpu_cases import CASES
+
+pytestmark = pytest.mark.gpu
+
+# Relative error bound of the mixed form against FP64 (max |a - b| / max |a|
+# per field) after the case's step count. Elastic, hyperelastic, Drucker-
+# Prager, J2-plastic and fluid cases stay near FP32 rounding (< 1e-4; most
+# are ~1e-6). Johnson-Cook cases amplify rounding through the plastic return
+# map and the rate term (the FP64 form itself moves by ~1e-2 in SD over 1000
+# Taylor steps when only the libm changes), so they get a looser bound.
+MIXED_TOL = {
+    "taylor_small_usf_jcf_linear": 0.1,
+    "block_musl_sjc_gruneisen": 2e-2,
+    "block_usf_sjcf_gruneisen": 2e-2,
+}
+DEFAULT_TOL = 1e-4
+FIELDS = ["PXg", "Mg", "SM", "SD", "Xp", "VXp"]
+
+
+def _rel(a, b):
+    s = float(np.max(np.abs(a))) if a.size else 0.0
+    d = float(np.max(np.abs(a - b))) if a.size else 0.0
+    return d / s if s > 0 else d
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_mixed_vs_fp64(built, name):
+    from mpm3d_gb300 import Deck, MpmStep
+    mk, steps = CASES[name]
+    d = Deck.parse(mk())
+    a = MpmStep(d, "fp64")
+    a.run(steps)
+    a.sync()
+    b = MpmStep(d, "mixed")
+    b.run(steps)
+    b.sync()
+    tol = MIXED_TOL.get(name, DEFAULT_TOL)
+    for f in FIELDS:
+        err = _rel(a.download(f), b.download(f))
+        assert err <= tol, f"{name} {f}: mixed vs FP64 relative error {err:.3g} > {tol}"
+    sa, sb = a.scalars(), b.scalars()
+    assert sa["istep"] == sb["istep"] == steps
+
+
+@pytest.mark.parametrize("variant", ["mpm", "gimp", "bimp", "sgmp"])
+def test_mixed_cook_vs_fp64(built, variant):
+    """Nearly incompressible neo-Hookean (nu = 0.499): the mixed form derives
+    J - 1 and B - I from Fp - I without cancellation."""
+    from mpm3d_gb300 import Deck, MpmStep, decks
+    d = Deck.parse(decks.cook_membrane(variant))
+    a = MpmStep(d, "fp64")
+    b = MpmStep(d, "mixed")
+    a.run(300)
+    b.run(300)
+    for f in FIELDS:
+        err = _rel(a.download(f), b.download(f))
+        assert err <= DEFAULT_TOL, f"cook {variant} {f}: {err:.3g}"
+
+
+MIX = ["slope_small_usf_dp_gimp", "beam_musl_neoh_sgmp", "block_usf_john", "dam_small_musl_null_bspline"]
+PFIELDS = ["Xp", "VXp", "SM", "SD", "PXg"]
+
+
+def _alone(deck, steps):
+    from mpm3d_gb300 import Batch
+    with Batch() as bt:
+        sid = bt.add(deck, steps=steps)
+        bt.run(steps)
+        bt.sync()
+        return {f: bt.download(sid, f) for f in PFIELDS}
+
+
+def test_batch_alone_vs_mix_identity(built):
+    """Four scenes of four shape families in one batch: each scene's state is
+    bit-identical to the scene run alone; scenes stop at their step count."""
+    from mpm3d_gb300 import Batch, Deck
+    decks_ = {n: Deck.parse(CASES[n][0]()) for n in MIX}
+    alone = {n: _alone(decks_[n], 30) for n in MIX}
+    with Batch() as bt:
+        ids = {n: bt.add(decks_[n], steps=30) for n in MIX}
+        bt.run(45)
+        bt.sync()
+        for n in MIX:
+            assert bt.scalars(ids[n])["istep"] == 30
+            for f in PFIELDS:
+                np.testing.assert_array_equal(bt.download(ids[n], f), alone[n][f], err_msg=f"{n} {f}")
+
+
+def test_batch_admission_mid_run_identity(built):
+    """Scenes admitted and retired while others run (the batch is re-laid out
+    on the device each time) keep bit-identical results; eager and graph
+    launches agree."""
+    from mpm3d_gb300 import Batch, Deck
+    decks_ = {n: Deck.parse(CASES[n][0]()) for n in MIX}
+    alone = {n: _alone(decks_[n], 30) for n in MIX[:3]}
+    with Batch() as bt:
+        i0 = bt.add(decks_[MIX[0]], steps=30)
+        bt.run(10)
+        i1 = bt.add(decks_[MIX[1]], steps=30)
+        bt.run(25, graph=False)
+        i2 = bt.add(decks_[MIX[2]], steps=30)
+        bt.remove(i0)
+        bt.run(7)
+        bt.run(33)
+        bt.sync()
+        for n, i in ((MIX[1], i1), (MIX[2], i2)):
+            for f in PFIELDS:
+                np.testing.assert_array_equal(bt.download(i, f), alone[n][f], err_msg=f"{n} {f}")
+
+
+def test_batch_block_shape_invariance(built):
+    """Launch shapes (the autotuner's knobs) change no result."""
+    from mpm3d_gb300 import Batch, Deck
+    d = Deck.parse(CASES[MIX[0]][0]())
+    ref = _alone(d, 20)
+    with Batch() as bt:
+        sid = bt.add(d, steps=20)
+        bt.set_blocks(128, 512)
+        bt.run(20)
+        for f in PFIELDS:
+            np.testing.assert_array_equal(bt.download(sid, f), ref[f], err_msg=f)
+
+
+def test_serving_runtime(built):
+    """Sixteen serving scenes (Cook panels and soft beams, SGMP, MUSL,
+    neo-Hookean) submitted from the host while earlier ones run: all finish
+    their step count, latencies are reported, and a served scene's fields are
+    bit-identical to the same scene run alone."""
+    from mpm3d_gb300 import Deck, Server, decks
+    rng = np.random.default_rng(3)
+    scenes = [Deck.parse(decks.serving_scene(rng, 2000, 40000)[0]) for _ in range(16)]
+    alone = _alone(scenes[5], 60)
+    with Server(chunk_steps=16, autotune=True) as srv:
+        tickets = []
+        for d in scenes:
+            tickets.append(srv.submit(d, 60, fields=["Xp", "SD", "VXp"]))
+            time.sleep(0.005)
+        for t in tickets:
+            assert srv.wait(t, 300000)
+        st = srv.stats()
+        assert st["finished"] == 16 and st["resident"] == 0 and st["queued"] == 0
+        for t in tickets:
+            r = srv.result(t)
+            assert r["istep"] == 60
+            assert 0 <= r["queue_ms"] <= r["latency_ms"]
+        for f in ["Xp", "SD", "VXp"]:
+            np.testing.assert_array_equal(srv.field(tickets[5], f), alone[f], err_msg=f)
+        srv.release(tickets[0])
+
+
+def test_serving_budget_admission(built):
+    """A budget that holds one scene at a time still runs every scene, and a
+    scene larger than the budget fails alone instead of blocking the queue."""
+    from mpm3d_gb300 import Batch, Deck, MpmError, Server, decks
+    rng = np.random.default_rng(5)
+    small = [Deck.parse(decks.serving_scene(rng, 3000, 6000)[0]) for _ in range(3)]
+    big = Deck.parse(decks.serving_scene(rng, 50000, 60000)[0])
+    budget = max(Batch.scene_bytes(d) for d in small) + 1
+    assert Batch.scene_bytes(big) > budget
+    with Server(hbm_budget_bytes=budget, chunk_steps=10) as srv:
+        t_big = srv.submit(big, 10)
+        ts = [srv.submit(d, 20) for d in small]
+        with pytest.raises(MpmError):
+            srv.wait(t_big, 60000)
+        for t in ts:
+            assert srv.wait(t, 60000)
+        assert srv.stats()["peak_resident_bytes"] <= budget
