@@ -110,6 +110,7 @@ struct mpm_batch {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
+  int gimp_split = 1;  // sort-key sub-cells per direction of GIMP scenes
   Profiler prof;
   std::string err;
 };
@@ -188,7 +189,7 @@ long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bo
   long long per_n = 8 * 13 + 4;
   long long per_k = 4;
   long long per_c = sgmp ? 8 * 39 + 2 : 0;
-  return np * per_p + nn * per_n + (ncell + 1) * per_k + ncell * per_c + 4096;
+  return np * per_p + nn * per_n + (27 * ncell + 1) * per_k + ncell * per_c + 4096;
 }
 
 void layout_flags(mpm_batch* b) {
@@ -248,6 +249,12 @@ int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
   BCK(cudaMemcpyAsync(s.orig + p0, orig.data(), 4 * np, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
   return MPM_OK;
+}
+
+// sort keys of a scene: its (sub-)cells plus one for particles off the grid
+long long scene_keys(const Geometry& g, int gimp_split) {
+  const long long k = g.shape == 1 ? gimp_split : 1;
+  return k * k * k * g.ncell + 1;
 }
 
 inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
@@ -416,7 +423,7 @@ int commit(mpm_batch* b) {
     h->body0 = nbody;
     NP += h->np;
     NN += h->nn;
-    NK += h->ncell + 1;
+    NK += scene_keys(h->su.g, b->gimp_split);
     if (g.shape == 3) NC += h->ncell;
     NR += h->nr;
     nmat += (int)h->su.mats.size();
@@ -537,11 +544,12 @@ int commit(mpm_batch* b) {
     const Geometry& g = h->su.g;
     Scene sc;
     memset(&sc, 0, sizeof sc);
-    sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = h->ncell + 1;
+    sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = scene_keys(g, b->gimp_split);
     sc.c0 = h->c0; sc.nc = g.shape == 3 ? h->ncell : 0; sc.r0 = h->r0; sc.nr = h->nr;
     sc.NGx = g.NGx; sc.NGy = g.NGy; sc.NGz = g.NGz; sc.NGxy = g.NGxy;
     sc.NCx = g.NCx; sc.NCy = g.NCy; sc.NCz = g.NCz; sc.NCxy = g.NCxy;
     sc.CNCx = g.CNCx; sc.CNCy = g.CNCy; sc.CNCz = g.CNCz; sc.CNCxy = g.CNCxy; sc.CNC = g.CNC;
+    sc.kdiv = g.shape == 1 ? b->gimp_split : 1;
     sc.shape = g.shape; sc.usf = g.usf; sc.musl = g.musl; sc.uvfp = g.uvfp; sc.qload = g.qload;
     sc.qdamp = g.qdamp; sc.gravity = g.gravity; sc.drdamp = h->drdamp; sc.has_jc = g.has_jc;
     for (int k = 0; k < 6; ++k) sc.fixs[k] = g.fixs[k];
@@ -591,7 +599,10 @@ int commit(mpm_batch* b) {
   BCK(cudaMemsetAsync(shared.ag, 0, sizeof(double) * 3 * NN, st));
   // every depeff setter entry is -1 or its own index (the max-scan relies on
   // it); only Johnson-Cook scenes rewrite theirs each step
-  if (b->any_jc) BCK(cudaMemsetAsync(shared.setter, 0xff, sizeof(int) * NP, st));
+  if (b->any_jc) {
+    BCK(cudaMemsetAsync(shared.setter, 0xff, sizeof(int) * NP, st));
+    BCK(cudaMemsetAsync(shared.deferred, 0, NP, st));
+  }
   for (HostScene* h : b->order)
     if (!h->resident) {
       int r = upload_scene_particles(b, h, A);
@@ -897,6 +908,33 @@ int mpm_batch_set_blocks(mpm_batch* b, int pblock, int nblock) {
   if (nblock) b->nblock = nblock;
   drop_graph(b);
   return MPM_OK;
+}
+
+int mpm_batch_set_option(mpm_batch* b, int option, int value) {
+  if (!b) return MPM_ERR_ARG;
+  switch (option) {
+    case MPM_BATCH_PARTICLE_BLOCK: return mpm_batch_set_blocks(b, value, 0);
+    case MPM_BATCH_NODE_BLOCK: return mpm_batch_set_blocks(b, 0, value);
+    case MPM_BATCH_GIMP_SPLIT:
+      if (value < 1 || value > 3) return berr(b, MPM_ERR_ARG, "GIMP key split must be 1, 2 or 3");
+      if (value != b->gimp_split) {
+        b->gimp_split = value;
+        drop_graph(b);
+        if (!b->order.empty()) b->dirty = true;  // re-lay out the keys
+      }
+      return MPM_OK;
+    default: return berr(b, MPM_ERR_ARG, "unknown batch option %d", option);
+  }
+}
+
+int mpm_batch_get_option(const mpm_batch* b, int option) {
+  if (!b) return -1;
+  switch (option) {
+    case MPM_BATCH_PARTICLE_BLOCK: return b->pblock;
+    case MPM_BATCH_NODE_BLOCK: return b->nblock;
+    case MPM_BATCH_GIMP_SPLIT: return b->gimp_split;
+    default: return -1;
+  }
 }
 
 int mpm_batch_profile_enable(mpm_batch* b, int on) {

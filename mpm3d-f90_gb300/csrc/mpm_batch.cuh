@@ -13,8 +13,12 @@
 //   grid nodes concatenated: FP64 mg, px[3], fx[3], vg[3]; fix, bd, node scene
 //   SGMP centre nodes (one per cell) concatenated: FP64 cmg, cpx[3], cfext[3],
 //     cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3]
-//   sort keys: scene s owns keys [k0, k0 + ncell + 1), the last one collects
+//   sort keys: scene s owns keys [k0, k0 + nk), the last one collects the
 //     particles outside its grid; seg[k] = end of key k's particle range.
+//     Linear / B-spline: one key per cell. SGMP: one key per dual cell.
+//     GIMP: 27 keys per cell -- the cell split per direction at 1/4 and 3/4
+//     (the cpGIMP quarter rule), ordered as a 3x finer grid, so that a node
+//     reads exactly the particle ranges its support reaches.
 //
 // Transfers particle -> grid are node-centric gathers over the neighbouring
 // cells' particle ranges (fixed order: cells z, y, x; particles in storage
@@ -40,6 +44,7 @@ struct Scene {
   long long r0, nr;  // reduction chunks
   int NGx, NGy, NGz, NGxy, NCx, NCy, NCz, NCxy, CNCx, CNCy, CNCz, CNCxy, CNC;
   int shape, usf, musl, uvfp, qload, qdamp, gravity, drdamp, has_jc;
+  int kdiv;  // sort-key sub-cells per direction and cell (3 for GIMP, else 1)
   int fixs[6];
   int mat0, nmat;
   double span0[3], span1[3], dcell, idcell, cutoff, iJacobi, iJacobi4;

@@ -106,6 +106,31 @@ __global__ void kb_begin(BState b, const int* target) {
   t.active_nodes = 0;
 }
 
+// cell of a position (InWhichCell, Grid.f90:123-155) and the offset in it, in
+// cells (FP32); false off the grid. The sort keys and the per-step particle
+// data use this one routine, so that a particle's key and its shape-function
+// offsets agree exactly.
+__device__ __forceinline__ bool cell_of(const Scene& sc, const double x[3], int cc[3], float off[3]) {
+  bool in = true;
+  for (int a = 0; a < 3; ++a) {
+    if (x[a] < sc.span0[a] || x[a] > sc.span1[a]) in = false;
+    double u = (x[a] - sc.span0[a]) * sc.idcell;
+    cc[a] = (int)u;
+    off[a] = (float)(u - (double)cc[a]);
+  }
+  return in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz;
+}
+
+// Sub-cell of an offset in a cell along one direction for a GIMP sort-key
+// split k: k = 3 splits at 1/4 and 3/4 (FindInflNode's quarter rule,
+// Grid.f90:602-849: below 1/4 the particle also reaches the node below its
+// cell, above 3/4 the second node above), k = 2 at 1/2, k = 1 not at all.
+__device__ __forceinline__ int gimp_sub(int k, float off) {
+  if (k == 3) return off < 0.25f ? 0 : (off > 0.75f ? 2 : 1);
+  if (k == 2) return off < 0.5f ? 0 : 1;
+  return 0;
+}
+
 // SGMP dual (cell-centre) cell of a position, CenterInWhichCell
 // (Grid.f90:157-190): the flat index of the per-direction truncations, valid
 // when it lies in 0..CNC-1. Like the reference, a position within half a cell
@@ -134,14 +159,17 @@ __global__ void kb_keys(BState b) {
     c = dual_cell(sc, x);
   } else {
     int cc[3];
-    bool in = true;
-    for (int a = 0; a < 3; ++a) {
-      if (x[a] < sc.span0[a] || x[a] > sc.span1[a]) in = false;
-      double u = (x[a] - sc.span0[a]) * sc.idcell;
-      cc[a] = (int)u;
+    float off[3];
+    if (cell_of(sc, x, cc, off)) {
+      if (sc.kdiv > 1) {
+        const int k = sc.kdiv;
+        int sk[3];
+        for (int a = 0; a < 3; ++a) sk[a] = k * cc[a] + gimp_sub(k, off[a]);
+        c = ((long long)sk[2] * (k * sc.NCy) + sk[1]) * (k * sc.NCx) + sk[0];
+      } else {
+        c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+      }
     }
-    if (in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz)
-      c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
   }
   long long key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
   b.key[i] = (unsigned)key;
@@ -187,18 +215,10 @@ __global__ void kb_permute(BState src, BState dst) {
   const Scene& sc = src.scenes[s];
   double x[3] = {dst.x[i], dst.x[NP + i], dst.x[2 * NP + i]};
   int cc[3];
-  bool in = true;
   float off[3];
-  for (int a = 0; a < 3; ++a) {
-    if (x[a] < sc.span0[a] || x[a] > sc.span1[a]) in = false;
-    double u = (x[a] - sc.span0[a]) * sc.idcell;
-    cc[a] = (int)u;
-    off[a] = (float)(u - (double)cc[a]);
-    dst.off[a * NP + i] = off[a];
-  }
-  int c = -1;
-  if (in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz) c = (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
-  dst.cell[i] = c;
+  const bool in = cell_of(sc, x, cc, off);
+  for (int a = 0; a < 3; ++a) dst.off[a * NP + i] = off[a];
+  dst.cell[i] = in ? (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0] : -1;
   if (sc.shape == 3) {
     // dual (cell-centre) grid: CenterInWhichCell and the nearest node
     int nd[3];
@@ -219,6 +239,36 @@ __global__ void kb_permute(BState src, BState dst) {
 }
 
 // ------------------------------------------------- node-centric gathers
+// Source particle ranges of node j of a GIMP scene with a key split k > 1, in
+// a fixed order: for each sub-row (sz, sy) of the k-times finer key grid
+// within the node's reach (from the sub-cell of cell j-2 holding offsets
+// above 3/4 to the sub-cell of cell j+1 holding offsets below 1/4), the cells
+// j-2 .. j+1 along x, each with the sub-cell range within that reach.
+// f(c, i0, i1) receives the cell and the particle range.
+template <class F>
+__device__ __forceinline__ void gimp_sources(const BState& b, const Scene& sc, const int j[3], F f) {
+  const int k = sc.kdiv;
+  const int lo = k - 1, hi = 0;  // sub-cells of offsets above 3/4 (cell j-2) and below 1/4 (cell j+1)
+  const int KX = k * sc.NCx, KY = k * sc.NCy, KZ = k * sc.NCz;
+  const int sx0 = max(0, k * (j[0] - 2) + lo), sx1 = min(KX - 1, k * (j[0] + 1) + hi);
+  const int sy0 = max(0, k * (j[1] - 2) + lo), sy1 = min(KY - 1, k * (j[1] + 1) + hi);
+  const int sz0 = max(0, k * (j[2] - 2) + lo), sz1 = min(KZ - 1, k * (j[2] + 1) + hi);
+  if (sx0 > sx1) return;
+  for (int sz = sz0; sz <= sz1; ++sz)
+    for (int sy = sy0; sy <= sy1; ++sy) {
+      const long long row = sc.k0 + ((long long)sz * KY + sy) * KX;
+      int i0 = row + sx0 == 0 ? 0 : b.seg[row + sx0 - 1];
+      for (int cx = sx0 / k; cx <= sx1 / k; ++cx) {
+        const int i1 = b.seg[row + min(sx1, k * cx + k - 1)];
+        if (i1 > i0) {
+          const int c[3] = {cx, sy / k, sz / k};
+          f(c, i0, i1);
+        }
+        i0 = i1;
+      }
+    }
+}
+
 // P2G of mass and momentum for linear / GIMP / B-spline scenes
 // (GridMomentumInitial); SGMP scenes take their values from the centre grid.
 __device__ __forceinline__ void node_finish(BState& b, const Scene& sc, long long n, int bc, int vel) {
@@ -270,31 +320,37 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
           }
         }
       } else {
-        int lo, hi;
-        cell_window(sc.shape, lo, hi);
-        for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
-          for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
-            for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
-              int i0, i1;
-              key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
-              if (i0 == i1) continue;
-              const int c[3] = {cx, cy, cz};
-              float m = 0, p0 = 0, p1 = 0, p2 = 0;
-              for (int i = i0; i < i1; ++i) {
-                float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-                float w, g[3];
-                if (!weight3(sc.shape, c, j, off, w, g)) continue;
-                float wm = w * (float)b.mass[i];
-                m += wm;
-                p0 += wm * (float)b.v[i];
-                p1 += wm * (float)b.v[NP + i];
-                p2 += wm * (float)b.v[2 * NP + i];
+        auto gather = [&](const int c[3], int i0, int i1) {
+          float m = 0, p0 = 0, p1 = 0, p2 = 0;
+          for (int i = i0; i < i1; ++i) {
+            float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+            float w, g[3];
+            if (!weight3(sc.shape, c, j, off, w, g)) continue;
+            float wm = w * (float)b.mass[i];
+            m += wm;
+            p0 += wm * (float)b.v[i];
+            p1 += wm * (float)b.v[NP + i];
+            p2 += wm * (float)b.v[2 * NP + i];
+          }
+          M += m;
+          P0 += p0;
+          P1 += p1;
+          P2 += p2;
+        };
+        if (sc.kdiv > 1) {
+          gimp_sources(b, sc, j, gather);
+        } else {
+          int lo, hi;
+          cell_window(sc.shape, lo, hi);
+          for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
+            for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
+              for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
+                int i0, i1;
+                key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
+                const int c[3] = {cx, cy, cz};
+                if (i0 < i1) gather(c, i0, i1);
               }
-              M += m;
-              P0 += p0;
-              P1 += p1;
-              P2 += p2;
-            }
+        }
       }
       b.mg[n] = M;
       b.px[n] = P0;
@@ -520,11 +576,11 @@ __global__ void kb_depeff_apply(BState b, int usf_pass) {
   using R = float;
   long long i = btid();
   if (i >= b.NP) return;
-  const int tail = b.deferred[i];
-  if (tail == 0) return;
   const int s = b.scene[i];
   const Scene& sc = b.scenes[s];
-  if (!scene_live(b, s) || sc.usf != usf_pass) return;
+  if (!sc.has_jc || !scene_live(b, s) || sc.usf != usf_pass) return;
+  const int tail = b.deferred[i];
+  if (tail == 0) return;
   const long long NP = b.NP;
   const long long o = sc.p0 + b.orig[i];
   int last = b.setter_scan[o];
@@ -667,32 +723,38 @@ __global__ void kb_p2g_force(BState b) {
       }
     }
   } else {
-    int lo, hi;
-    cell_window(sc.shape, lo, hi);
     const float idc = (float)sc.idcell;
-    for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
-      for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
-        for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
-          int i0, i1;
-          key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
-          if (i0 == i1) continue;
-          const int c[3] = {cx, cy, cz};
-          float f0 = 0, f1 = 0, f2 = 0;
-          for (int i = i0; i < i1; ++i) {
-            float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-            float w, g[3];
-            if (!weight3(sc.shape, c, j, off, w, g)) continue;
-            float dx = g[0] * idc, dy = g[1] * idc, dz = g[2] * idc;
-            float sxx = b.fs[i], syy = b.fs[NP + i], szz = b.fs[2 * NP + i];
-            float sxy = b.fs[3 * NP + i], syz = b.fs[4 * NP + i], sxz = b.fs[5 * NP + i];
-            f0 += -(sxx * dx + sxy * dy + sxz * dz) + b.fs[6 * NP + i] * w;
-            f1 += -(sxy * dx + syy * dy + syz * dz) + b.fs[7 * NP + i] * w;
-            f2 += -(sxz * dx + syz * dy + szz * dz) + b.fs[8 * NP + i] * w;
+    auto gather = [&](const int c[3], int i0, int i1) {
+      float f0 = 0, f1 = 0, f2 = 0;
+      for (int i = i0; i < i1; ++i) {
+        float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+        float w, g[3];
+        if (!weight3(sc.shape, c, j, off, w, g)) continue;
+        float dx = g[0] * idc, dy = g[1] * idc, dz = g[2] * idc;
+        float sxx = b.fs[i], syy = b.fs[NP + i], szz = b.fs[2 * NP + i];
+        float sxy = b.fs[3 * NP + i], syz = b.fs[4 * NP + i], sxz = b.fs[5 * NP + i];
+        f0 += -(sxx * dx + sxy * dy + sxz * dz) + b.fs[6 * NP + i] * w;
+        f1 += -(sxy * dx + syy * dy + syz * dz) + b.fs[7 * NP + i] * w;
+        f2 += -(sxz * dx + syz * dy + szz * dz) + b.fs[8 * NP + i] * w;
+      }
+      F[0] += f0;
+      F[1] += f1;
+      F[2] += f2;
+    };
+    if (sc.kdiv > 1) {
+      gimp_sources(b, sc, j, gather);
+    } else {
+      int lo, hi;
+      cell_window(sc.shape, lo, hi);
+      for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
+        for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
+          for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
+            int i0, i1;
+            key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
+            const int c[3] = {cx, cy, cz};
+            if (i0 < i1) gather(c, i0, i1);
           }
-          F[0] += f0;
-          F[1] += f1;
-          F[2] += f2;
-        }
+    }
   }
   node_integrate(b, sc, n, F);
 }
@@ -918,29 +980,35 @@ __global__ void kb_p2g_momentum(BState b) {
       }
     }
   } else {
-    int lo, hi;
-    cell_window(sc.shape, lo, hi);
-    for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
-      for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
-        for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
-          int i0, i1;
-          key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
-          if (i0 == i1) continue;
-          const int c[3] = {cx, cy, cz};
-          float p0 = 0, p1 = 0, p2 = 0;
-          for (int i = i0; i < i1; ++i) {
-            float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-            float w, g[3];
-            if (!weight3(sc.shape, c, j, off, w, g)) continue;
-            float wm = w * (float)b.mass[i];
-            p0 += wm * (float)b.v[i];
-            p1 += wm * (float)b.v[NP + i];
-            p2 += wm * (float)b.v[2 * NP + i];
+    auto gather = [&](const int c[3], int i0, int i1) {
+      float p0 = 0, p1 = 0, p2 = 0;
+      for (int i = i0; i < i1; ++i) {
+        float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+        float w, g[3];
+        if (!weight3(sc.shape, c, j, off, w, g)) continue;
+        float wm = w * (float)b.mass[i];
+        p0 += wm * (float)b.v[i];
+        p1 += wm * (float)b.v[NP + i];
+        p2 += wm * (float)b.v[2 * NP + i];
+      }
+      P0 += p0;
+      P1 += p1;
+      P2 += p2;
+    };
+    if (sc.kdiv > 1) {
+      gimp_sources(b, sc, j, gather);
+    } else {
+      int lo, hi;
+      cell_window(sc.shape, lo, hi);
+      for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
+        for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
+          for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
+            int i0, i1;
+            key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
+            const int c[3] = {cx, cy, cz};
+            if (i0 < i1) gather(c, i0, i1);
           }
-          P0 += p0;
-          P1 += p1;
-          P2 += p2;
-        }
+    }
   }
   b.px[n] = P0;
   b.px[NN + n] = P1;

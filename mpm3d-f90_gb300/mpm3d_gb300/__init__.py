@@ -122,6 +122,8 @@ def library() -> ctypes.CDLL:
         "mpm_batch_scene_download": (i, [vp, i, i, P(d)]),
         "mpm_batch_last_error": (c, [vp]),
         "mpm_batch_set_blocks": (i, [vp, i, i]),
+        "mpm_batch_set_option": (i, [vp, i, i]),
+        "mpm_batch_get_option": (i, [vp, i]),
         "mpm_batch_profile_enable": (i, [vp, i]),
         "mpm_batch_kernel_stats": (i, [vp, i, c, i, P(i64), P(d)]),
         "mpm_serve_create": (i, [vp, P(vp)]),
@@ -349,6 +351,9 @@ class MpmStep:
         return int(library().mpm_device_bytes(self._h))
 
 
+BATCH_OPTIONS = {"particle_block": 1, "node_block": 2, "gimp_split": 3}
+
+
 class Batch:
     """Many independent scenes advanced together by the mixed-precision step.
 
@@ -436,6 +441,12 @@ class Batch:
 
     def set_blocks(self, particle_block: int = 0, node_block: int = 0) -> None:
         self._check(library().mpm_batch_set_blocks(self._h, int(particle_block), int(node_block)))
+
+    def set_option(self, name: str, value: int) -> None:
+        self._check(library().mpm_batch_set_option(self._h, BATCH_OPTIONS[name], int(value)))
+
+    def option(self, name: str) -> int:
+        return int(library().mpm_batch_get_option(self._h, BATCH_OPTIONS[name]))
 
     def profile(self, on: bool = True) -> None:
         self._check(library().mpm_batch_profile_enable(self._h, int(bool(on))))
