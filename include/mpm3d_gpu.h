@@ -181,12 +181,8 @@ const char* mpm_batch_last_error(const mpm_batch* b);
 /* Launch shape of the batch kernels (threads per block for particle and node
  * kernels; 0 keeps the current value). */
 int mpm_batch_set_blocks(mpm_batch* b, int particle_block, int node_block);
-/* Batch options. The block sizes change no result. The GIMP key split is the
- * number of sort-key sub-cells per direction and cell of GIMP scenes (1, 2 or
- * 3; 3 = the cpGIMP quarter rule, so a node visits only particles its support
- * reaches); it groups the FP32 partial sums differently, so results depend on
- * it at rounding level: set it before adding scenes. */
-enum mpm_batch_option { MPM_BATCH_PARTICLE_BLOCK = 1, MPM_BATCH_NODE_BLOCK = 2, MPM_BATCH_GIMP_SPLIT = 3 };
+/* Batch options (launch shapes; they change no result). */
+enum mpm_batch_option { MPM_BATCH_PARTICLE_BLOCK = 1, MPM_BATCH_NODE_BLOCK = 2 };
 int mpm_batch_set_option(mpm_batch* b, int option, int value);
 int mpm_batch_get_option(const mpm_batch* b, int option);
 int mpm_batch_profile_enable(mpm_batch* b, int on);

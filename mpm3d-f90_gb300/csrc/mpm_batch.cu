@@ -106,11 +106,10 @@ struct mpm_batch {
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
   int key_bits = 1;
-  int any_sgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
+  int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
-  int gimp_split = 1;  // sort-key sub-cells per direction of GIMP scenes
   Profiler prof;
   std::string err;
 };
@@ -186,17 +185,17 @@ long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bo
   per_p += 4 * 3 + 4 * 9 + 4 * 6 + 4 * 9;                                  // derived + force staging
   per_p += 4 * 4;                                                         // sort keys / values
   if (jc) per_p += 4 * 2 + 8 * 6 + 1;
-  long long per_n = 8 * 13 + 4;
+  long long per_n = 8 * 13 + 4 + 8 * 4;
   long long per_k = 4;
   long long per_c = sgmp ? 8 * 39 + 2 : 0;
-  return np * per_p + nn * per_n + (27 * ncell + 1) * per_k + ncell * per_c + 4096;
+  return np * per_p + nn * per_n + (ncell + 1) * per_k + ncell * per_c + 4096;
 }
 
 void layout_flags(mpm_batch* b) {
-  b->any_sgmp = b->any_usf = b->any_later = b->any_musl = b->any_jc = b->any_dr = b->any_uvfp = 0;
+  b->any_sgmp = b->any_nonsgmp = b->any_usf = b->any_later = b->any_musl = b->any_jc = b->any_dr = b->any_uvfp = 0;
   for (HostScene* h : b->order) {
     const Geometry& g = h->su.g;
-    if (g.shape == 3) b->any_sgmp = 1;
+    if (g.shape == 3) b->any_sgmp = 1; else b->any_nonsgmp = 1;
     if (g.usf) b->any_usf = 1; else b->any_later = 1;
     if (g.musl) b->any_musl = 1;
     if (g.has_jc) b->any_jc = 1;
@@ -251,11 +250,9 @@ int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
   return MPM_OK;
 }
 
-// sort keys of a scene: its (sub-)cells plus one for particles off the grid
-long long scene_keys(const Geometry& g, int gimp_split) {
-  const long long k = g.shape == 1 ? gimp_split : 1;
-  return k * k * k * g.ncell + 1;
-}
+// sort keys of a scene: its cells (dual cells for SGMP) plus one for the
+// particles off the grid
+long long scene_keys(const Geometry& g) { return (long long)g.ncell + 1; }
 
 inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
 
@@ -268,7 +265,7 @@ int enqueue_step(mpm_batch* b) {
   kb_begin<<<gridn(a.nscene, 128), 128, 0, st>>>(a, b->d_target);
   prof_end(K_BEGIN, st);
   prof_begin(K_LOCATE, st);
-  cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
+  if (b->any_sgmp) cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
   kb_keys<<<gridn(a.NP, pb), pb, 0, st>>>(a);
   prof_end(K_LOCATE, st);
   prof_begin(K_SORT, st);
@@ -276,9 +273,11 @@ int enqueue_step(mpm_batch* b) {
   cudaError_t e = cub::DeviceRadixSort::SortPairs(b->cub_tmp, tmp, a.key, a.key_sorted, a.val, a.perm, (int)a.NP, 0,
                                                   b->key_bits, st);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "sort: %s", cudaGetErrorString(e));
-  tmp = b->cub_bytes;
-  e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
-  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
+  if (b->any_sgmp) {
+    tmp = b->cub_bytes;
+    e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
+    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
+  }
   prof_end(K_SORT, st);
   prof_begin(K_PERMUTE, st);
   kb_permute<<<gridn(a.NP, pb), pb, 0, st>>>(a, b->B);
@@ -286,8 +285,13 @@ int enqueue_step(mpm_batch* b) {
   // swap the particle buffer sets (node and scene arrays are shared)
   std::swap(b->A, b->B);
   BState& s = b->A;
+  const bool scatter = b->any_nonsgmp;
   prof_begin(K_P2G_MASS, st);
   if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
+  if (scatter) {
+    kb_bounds<<<gridn(s.NP, pb), pb, 0, st>>>(s, 0);
+    kb_scatter_momentum<0><<<gridn(s.NP, kScatterBlock), kScatterBlock, 0, st>>>(s);
+  }
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
   prof_end(K_P2G_MASS, st);
   auto stress = [&](int usf_pass) -> int {
@@ -313,6 +317,10 @@ int enqueue_step(mpm_batch* b) {
   prof_end(K_FORCE_PREP, st);
   prof_begin(K_P2G_FORCE, st);
   if (b->any_sgmp) kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
+  if (scatter) {
+    kb_bounds<<<gridn(s.NP, pb), pb, 0, st>>>(s, 1);
+    kb_scatter_force<<<gridn(s.NP, kScatterBlock), kScatterBlock, 0, st>>>(s);
+  }
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
   prof_end(K_P2G_FORCE, st);
   prof_begin(K_POSITION, st);
@@ -322,6 +330,10 @@ int enqueue_step(mpm_batch* b) {
   if (b->any_musl) {
     prof_begin(K_P2G_MOM, st);
     if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
+    if (scatter) {
+      kb_bounds<<<gridn(s.NP, pb), pb, 0, st>>>(s, 2);
+      kb_scatter_momentum<1><<<gridn(s.NP, kScatterBlock), kScatterBlock, 0, st>>>(s);
+    }
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
     prof_end(K_P2G_MOM, st);
   }
@@ -423,7 +435,7 @@ int commit(mpm_batch* b) {
     h->body0 = nbody;
     NP += h->np;
     NN += h->nn;
-    NK += scene_keys(h->su.g, b->gimp_split);
+    NK += scene_keys(h->su.g);
     if (g.shape == 3) NC += h->ncell;
     NR += h->nr;
     nmat += (int)h->su.mats.size();
@@ -462,8 +474,9 @@ int commit(mpm_batch* b) {
   shared.mg = al.get<double>(NN);
   shared.px = al.get<double>(3 * NN);
   shared.fx = al.get<double>(3 * NN);
-  shared.vg = al.get<double>(3 * NN);
-  shared.ag = al.get<double>(3 * NN);
+  shared.nvel = al.get<float4>(NN);
+  shared.nacc = al.get<float4>(NN);
+  shared.acc = al.get<unsigned long long>(4 * NN);
   shared.fix = al.get<uint8_t>(NN);
   shared.bd = al.get<uint8_t>(NN);
   shared.node_scene = al.get<uint16_t>(NN);
@@ -502,7 +515,7 @@ int commit(mpm_batch* b) {
     s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
     s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
     s.perm = shared.perm; s.seg = shared.seg; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
-    s.vg = shared.vg; s.ag = shared.ag; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
+    s.nvel = shared.nvel; s.nacc = shared.nacc; s.acc = shared.acc; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
     s.cmg = shared.cmg; s.cpx = shared.cpx; s.cfext = shared.cfext; s.cfint = shared.cfint; s.co = shared.co;
     s.cw = shared.cw; s.cdefp = shared.cdefp; s.cvx = shared.cvx; s.cax = shared.cax; s.cscene = shared.cscene;
     s.setter = shared.setter; s.setter_scan = shared.setter_scan; s.dep = shared.dep; s.jc_aux = shared.jc_aux;
@@ -544,12 +557,11 @@ int commit(mpm_batch* b) {
     const Geometry& g = h->su.g;
     Scene sc;
     memset(&sc, 0, sizeof sc);
-    sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = scene_keys(g, b->gimp_split);
+    sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = scene_keys(g);
     sc.c0 = h->c0; sc.nc = g.shape == 3 ? h->ncell : 0; sc.r0 = h->r0; sc.nr = h->nr;
     sc.NGx = g.NGx; sc.NGy = g.NGy; sc.NGz = g.NGz; sc.NGxy = g.NGxy;
     sc.NCx = g.NCx; sc.NCy = g.NCy; sc.NCz = g.NCz; sc.NCxy = g.NCxy;
     sc.CNCx = g.CNCx; sc.CNCy = g.CNCy; sc.CNCz = g.CNCz; sc.CNCxy = g.CNCxy; sc.CNC = g.CNC;
-    sc.kdiv = g.shape == 1 ? b->gimp_split : 1;
     sc.shape = g.shape; sc.usf = g.usf; sc.musl = g.musl; sc.uvfp = g.uvfp; sc.qload = g.qload;
     sc.qdamp = g.qdamp; sc.gravity = g.gravity; sc.drdamp = h->drdamp; sc.has_jc = g.has_jc;
     for (int k = 0; k < 6; ++k) sc.fixs[k] = g.fixs[k];
@@ -595,8 +607,9 @@ int commit(mpm_batch* b) {
   BCK(cudaMemsetAsync(shared.mg, 0, sizeof(double) * NN, st));
   BCK(cudaMemsetAsync(shared.px, 0, sizeof(double) * 3 * NN, st));
   BCK(cudaMemsetAsync(shared.fx, 0, sizeof(double) * 3 * NN, st));
-  BCK(cudaMemsetAsync(shared.vg, 0, sizeof(double) * 3 * NN, st));
-  BCK(cudaMemsetAsync(shared.ag, 0, sizeof(double) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.nvel, 0, sizeof(float4) * NN, st));
+  BCK(cudaMemsetAsync(shared.nacc, 0, sizeof(float4) * NN, st));
+  BCK(cudaMemsetAsync(shared.acc, 0, sizeof(unsigned long long) * 4 * NN, st));
   // every depeff setter entry is -1 or its own index (the max-scan relies on
   // it); only Johnson-Cook scenes rewrite theirs each step
   if (b->any_jc) {
@@ -915,14 +928,6 @@ int mpm_batch_set_option(mpm_batch* b, int option, int value) {
   switch (option) {
     case MPM_BATCH_PARTICLE_BLOCK: return mpm_batch_set_blocks(b, value, 0);
     case MPM_BATCH_NODE_BLOCK: return mpm_batch_set_blocks(b, 0, value);
-    case MPM_BATCH_GIMP_SPLIT:
-      if (value < 1 || value > 3) return berr(b, MPM_ERR_ARG, "GIMP key split must be 1, 2 or 3");
-      if (value != b->gimp_split) {
-        b->gimp_split = value;
-        drop_graph(b);
-        if (!b->order.empty()) b->dirty = true;  // re-lay out the keys
-      }
-      return MPM_OK;
     default: return berr(b, MPM_ERR_ARG, "unknown batch option %d", option);
   }
 }
@@ -932,7 +937,6 @@ int mpm_batch_get_option(const mpm_batch* b, int option) {
   switch (option) {
     case MPM_BATCH_PARTICLE_BLOCK: return b->pblock;
     case MPM_BATCH_NODE_BLOCK: return b->nblock;
-    case MPM_BATCH_GIMP_SPLIT: return b->gimp_split;
     default: return -1;
   }
 }

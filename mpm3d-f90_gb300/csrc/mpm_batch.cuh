@@ -10,20 +10,22 @@
 //     per step (written by the permutation): cell (scene-local cell, -1
 //     outside), off[3] (offset in the cell, in cells), SGMP dual cell, nearest
 //     node, xxn[3], xn[3]; body, scene, orig (scene-local input index)
-//   grid nodes concatenated: FP64 mg, px[3], fx[3], vg[3]; fix, bd, node scene
+//   grid nodes concatenated: FP64 mg, px[3], fx[3]; FP32 float4 velocity and
+//     acceleration (for the particle gathers); fix, bd, node scene
 //   SGMP centre nodes (one per cell) concatenated: FP64 cmg, cpx[3], cfext[3],
 //     cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3]
 //   sort keys: scene s owns keys [k0, k0 + nk), the last one collects the
-//     particles outside its grid; seg[k] = end of key k's particle range.
-//     Linear / B-spline: one key per cell. SGMP: one key per dual cell.
-//     GIMP: 27 keys per cell -- the cell split per direction at 1/4 and 3/4
-//     (the cpGIMP quarter rule), ordered as a 3x finer grid, so that a node
-//     reads exactly the particle ranges its support reaches.
+//     particles outside its grid; seg[k] = end of key k's particle range
+//     (kept for SGMP scenes). Linear / GIMP / B-spline: one key per cell;
+//     SGMP: one key per dual cell.
+//   P2G accumulators: acc[4][NN] 64-bit fixed point (see the scatter kernels).
 //
-// Transfers particle -> grid are node-centric gathers over the neighbouring
-// cells' particle ranges (fixed order: cells z, y, x; particles in storage
-// order), FP32 contributions summed per source cell and accumulated in FP64:
-// deterministic, no atomics, and the same for a scene alone or in a batch.
+// Transfers particle -> grid of linear / GIMP / B-spline scenes are
+// particle-centric scatters of FP32 contributions summed exactly in 64-bit
+// fixed point; SGMP particle -> centre-node transfers are node-centric
+// gathers over the dual cells' particle ranges with FP32 partial sums per
+// dual cell accumulated in FP64. Both are deterministic and give a scene the
+// same results alone or in a batch.
 // Transfers grid -> particle are particle-centric with shape functions
 // evaluated on the fly in FP32.
 #pragma once
@@ -44,7 +46,6 @@ struct Scene {
   long long r0, nr;  // reduction chunks
   int NGx, NGy, NGz, NGxy, NCx, NCy, NCz, NCxy, CNCx, CNCy, CNCz, CNCxy, CNC;
   int shape, usf, musl, uvfp, qload, qdamp, gravity, drdamp, has_jc;
-  int kdiv;  // sort-key sub-cells per direction and cell (3 for GIMP, else 1)
   int fixs[6];
   int mat0, nmat;
   double span0[3], span1[3], dcell, idcell, cutoff, iJacobi, iJacobi4;
@@ -57,6 +58,7 @@ struct SceneState {
   double time, dt, ke, ie, mom[3], ke_prev, max_vp, depeff_carry;
   unsigned long long active_nodes;
   unsigned status;
+  unsigned qmax[4];  // per-step contribution bounds of the P2G scatters (float bits)
   unsigned pad_;
 };
 
@@ -78,7 +80,9 @@ struct BState {
   unsigned *key, *key_sorted;
   int *val, *perm, *seg;
   // grid
-  double *mg, *px, *fx, *vg, *ag;  // ag = fx / mg after the integration
+  double *mg, *px, *fx;
+  float4 *nvel, *nacc;             // FP32 px / mg and fx / mg for the gathers (zero at or below the cut-off)
+  unsigned long long* acc;         // [4][NN] fixed-point P2G sums, zero between transfers
   uint8_t *fix, *bd;
   uint16_t* node_scene;
   // SGMP centre grid

@@ -45,49 +45,6 @@ __device__ __forceinline__ void bsp1(int t, float off, float& w, float& d) {
   }
 }
 
-// weight and gradient (per cell) of node j for a particle in cell c
-__device__ __forceinline__ bool weight3(int shape, const int c[3], const int j[3], const float off[3], float& w,
-                                        float g[3]) {
-  float wd[3], dd[3];
-  for (int a = 0; a < 3; ++a) {
-    int t = j[a] - c[a];
-    if (shape == 0) {
-      if (t < 0 || t > 1) return false;
-      lin1(t, off[a], wd[a], dd[a]);
-    } else if (shape == 1) {
-      gimp1((float)(c[a] - j[a]) + off[a], wd[a], dd[a]);
-      if (wd[a] == 0.f) return false;
-    } else {
-      if (t < -1 || t > 1) return false;
-      bsp1(t, off[a], wd[a], dd[a]);
-    }
-  }
-  w = wd[0] * wd[1] * wd[2];
-  g[0] = dd[0] * wd[1] * wd[2];
-  g[1] = wd[0] * dd[1] * wd[2];
-  g[2] = wd[0] * wd[1] * dd[2];
-  return true;
-}
-
-// neighbour cell window of a node: particles in cells j+lo .. j+hi reach it
-__device__ __forceinline__ void cell_window(int shape, int& lo, int& hi) {
-  if (shape == 0) { lo = -1; hi = 0; }
-  else if (shape == 1) { lo = -2; hi = 1; }
-  else { lo = -1; hi = 1; }
-}
-
-// influence node offsets of a particle in its cell (per direction)
-__device__ __forceinline__ int node_offsets(int shape, float off, int t[4]) {
-  if (shape == 0) { t[0] = 0; t[1] = 1; return 2; }
-  if (shape == 2) { t[0] = -1; t[1] = 0; t[2] = 1; return 3; }
-  int n = 0;  // cpGIMP: quarter rule of FindInflNode
-  if (off < 0.25f) t[n++] = -1;
-  t[n++] = 0;
-  t[n++] = 1;
-  if (off > 0.75f) t[n++] = 2;
-  return n;
-}
-
 __device__ __forceinline__ void key_range(const BState& b, long long key, int& i0, int& i1) {
   i0 = key == 0 ? 0 : b.seg[key - 1];
   i1 = b.seg[key];
@@ -104,6 +61,7 @@ __global__ void kb_begin(BState b, const int* target) {
   t.time = t.time + t.dt;
   t.ie = 0.0;
   t.active_nodes = 0;
+  for (int k = 0; k < 4; ++k) t.qmax[k] = 0u;
 }
 
 // cell of a position (InWhichCell, Grid.f90:123-155) and the offset in it, in
@@ -119,16 +77,6 @@ __device__ __forceinline__ bool cell_of(const Scene& sc, const double x[3], int 
     off[a] = (float)(u - (double)cc[a]);
   }
   return in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz;
-}
-
-// Sub-cell of an offset in a cell along one direction for a GIMP sort-key
-// split k: k = 3 splits at 1/4 and 3/4 (FindInflNode's quarter rule,
-// Grid.f90:602-849: below 1/4 the particle also reaches the node below its
-// cell, above 3/4 the second node above), k = 2 at 1/2, k = 1 not at all.
-__device__ __forceinline__ int gimp_sub(int k, float off) {
-  if (k == 3) return off < 0.25f ? 0 : (off > 0.75f ? 2 : 1);
-  if (k == 2) return off < 0.5f ? 0 : 1;
-  return 0;
 }
 
 // SGMP dual (cell-centre) cell of a position, CenterInWhichCell
@@ -147,7 +95,9 @@ __device__ __forceinline__ long long dual_cell(const Scene& sc, const double x[3
 // ------------------------------------------------------------------ keys
 // Sort key of a particle: its scene's key base plus its cell (linear, GIMP,
 // B-spline) or its dual cell (SGMP); the scene's last key collects the
-// particles outside the grid.
+// particles outside the grid. Sorting keeps the particles of a cell
+// contiguous, which the transfers rely on for locality (and the SGMP centre
+// gathers for their particle ranges).
 __global__ void kb_keys(BState b) {
   long long i = btid();
   if (i >= b.NP) return;
@@ -161,20 +111,13 @@ __global__ void kb_keys(BState b) {
     int cc[3];
     float off[3];
     if (cell_of(sc, x, cc, off)) {
-      if (sc.kdiv > 1) {
-        const int k = sc.kdiv;
-        int sk[3];
-        for (int a = 0; a < 3; ++a) sk[a] = k * cc[a] + gimp_sub(k, off[a]);
-        c = ((long long)sk[2] * (k * sc.NCy) + sk[1]) * (k * sc.NCx) + sk[0];
-      } else {
-        c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
-      }
+      c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
     }
   }
   long long key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
   b.key[i] = (unsigned)key;
   b.val[i] = (int)i;
-  atomicAdd(&b.seg[key], 1);
+  if (b.any_sgmp) atomicAdd(&b.seg[key], 1);  // per-key counts for the SGMP centre gathers
 }
 
 // ---------------------------------------------------- permutation + derived
@@ -239,38 +182,300 @@ __global__ void kb_permute(BState src, BState dst) {
 }
 
 // ------------------------------------------------- node-centric gathers
-// Source particle ranges of node j of a GIMP scene with a key split k > 1, in
-// a fixed order: for each sub-row (sz, sy) of the k-times finer key grid
-// within the node's reach (from the sub-cell of cell j-2 holding offsets
-// above 3/4 to the sub-cell of cell j+1 holding offsets below 1/4), the cells
-// j-2 .. j+1 along x, each with the sub-cell range within that reach.
-// f(c, i0, i1) receives the cell and the particle range.
-template <class F>
-__device__ __forceinline__ void gimp_sources(const BState& b, const Scene& sc, const int j[3], F f) {
-  const int k = sc.kdiv;
-  const int lo = k - 1, hi = 0;  // sub-cells of offsets above 3/4 (cell j-2) and below 1/4 (cell j+1)
-  const int KX = k * sc.NCx, KY = k * sc.NCy, KZ = k * sc.NCz;
-  const int sx0 = max(0, k * (j[0] - 2) + lo), sx1 = min(KX - 1, k * (j[0] + 1) + hi);
-  const int sy0 = max(0, k * (j[1] - 2) + lo), sy1 = min(KY - 1, k * (j[1] + 1) + hi);
-  const int sz0 = max(0, k * (j[2] - 2) + lo), sz1 = min(KZ - 1, k * (j[2] + 1) + hi);
-  if (sx0 > sx1) return;
-  for (int sz = sz0; sz <= sz1; ++sz)
-    for (int sy = sy0; sy <= sy1; ++sy) {
-      const long long row = sc.k0 + ((long long)sz * KY + sy) * KX;
-      int i0 = row + sx0 == 0 ? 0 : b.seg[row + sx0 - 1];
-      for (int cx = sx0 / k; cx <= sx1 / k; ++cx) {
-        const int i1 = b.seg[row + min(sx1, k * cx + k - 1)];
-        if (i1 > i0) {
-          const int c[3] = {cx, sy / k, sz / k};
-          f(c, i0, i1);
-        }
-        i0 = i1;
-      }
-    }
+// ------------------------------------------- deterministic P2G scatter
+// Particle -> node transfers of linear, GIMP and B-spline scenes are
+// particle-centric: each particle adds its FP32 contributions to the nodes it
+// influences. Contributions are quantised to 64-bit fixed point with a
+// per-scene, per-quantity power-of-two scale and summed with integer adds, so
+// a node's sum is exact and independent of the order of the adds (and of
+// which other scenes share the batch). The scale comes from a per-step bound
+// B on any single contribution's magnitude (a max over the scene's particles,
+// also order-independent): a node sums at most np contributions, np * B <
+// 2^E, and contributions are scaled by 2^(61 - E), so no sum can reach 2^62.
+// The rounding of a contribution to the fixed-point grid (np * B * 2^-61)
+// is far below its FP32 rounding.
+//
+// A block adds the contributions of its 256 consecutive (cell-sorted)
+// particles into a shared-memory hash tile keyed by node, then adds each
+// tile entry to the global accumulator with one atomic per channel.
+
+// per-scene bound slots (SceneState::qmax, float bits, reset every step)
+enum QSlot { Q_MASS = 0, Q_MOM = 1, Q_FORCE = 2, Q_MOM_MUSL = 3 };
+
+// warp-aggregated max of non-negative v into sst[s].qmax[slot]; every lane of
+// the warp must call it (s < 0: no value)
+__device__ __forceinline__ void scene_max(BState& b, int s, int slot, float v) {
+  const unsigned bits = __float_as_uint(v);
+  const unsigned grp = __match_any_sync(0xffffffffu, s);
+  const unsigned mx = __reduce_max_sync(grp, bits);
+  if (s >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&b.sst[s].qmax[slot], mx);
 }
 
-// P2G of mass and momentum for linear / GIMP / B-spline scenes
-// (GridMomentumInitial); SGMP scenes take their values from the centre grid.
+// Fixed-point shift sh of a scene's channel: contributions are rounded to
+// integers after scaling by 2^sh, sh = 62 - E with np * bound < 2^E (clamped
+// to the FP32 exponent range; 0 when the bound is 0 and every contribution
+// is 0). Quantisation is one FP32 multiply by 2^sh (exact) and a conversion
+// to int64 -- no FP64 arithmetic on the particle side.
+__device__ __forceinline__ int q_shift(const Scene& sc, unsigned bound_bits) {
+  const float bound = __uint_as_float(bound_bits);
+  if (!(bound > 0.f)) return 0;
+  int E;
+  frexpf((float)sc.np * bound, &E);  // np < 2^31: the product is exact up to one rounding, covered by E + 1
+  return max(-126, min(127, 61 - E));
+}
+__device__ __forceinline__ float q_scale(int sh) { return __int_as_float((sh + 127) << 23); }
+__device__ __forceinline__ long long quant(float c, float scale) { return __float2ll_rn(c * scale); }
+__device__ __forceinline__ double q_unit(int sh) { return ldexp(1.0, -sh); }
+
+// influence nodes of a particle along one direction: node = cell + t[k],
+// weight w[k] and derivative d[k] (per cell) -- NShape / the cpGIMP quarter
+// rule of FindInflNode with NShape_GIMP / NShape_Bspline
+__device__ __forceinline__ int dim_nodes(int shape, float off, int t[4], float w[4], float d[4]) {
+  if (shape == 0) {
+    t[0] = 0;
+    t[1] = 1;
+    lin1(0, off, w[0], d[0]);
+    lin1(1, off, w[1], d[1]);
+    return 2;
+  }
+  if (shape == 2) {
+    for (int k = 0; k < 3; ++k) {
+      t[k] = k - 1;
+      bsp1(k - 1, off, w[k], d[k]);
+    }
+    return 3;
+  }
+  int n = 0;
+  if (off < 0.25f) t[n++] = -1;
+  t[n++] = 0;
+  t[n++] = 1;
+  if (off > 0.75f) t[n++] = 2;
+  for (int k = 0; k < n; ++k) gimp1((float)(-t[k]) + off, w[k], d[k]);
+  return n;
+}
+
+constexpr int kTileBits = 10;
+constexpr int kTile = 1 << kTileBits;  // hash slots per block
+constexpr int kScatterBlock = 256;
+
+template <int NV>
+struct Tile {
+  int key[kTile];                      // global node index, -1 = empty
+  unsigned long long val[NV][kTile];   // fixed-point sums (two's complement)
+};
+
+template <int NV>
+__device__ __forceinline__ void tile_init(Tile<NV>& t) {
+  for (int e = threadIdx.x; e < kTile; e += blockDim.x) {
+    t.key[e] = -1;
+    for (int v = 0; v < NV; ++v) t.val[v][e] = 0ull;
+  }
+  __syncthreads();
+}
+
+// add q[NV] to node n: into the tile (linear probing), or straight into the
+// global accumulator if the tile has no room within the probe limit
+template <int NV>
+__device__ __forceinline__ void tile_add(Tile<NV>& t, int n, const long long q[NV], unsigned long long* acc,
+                                         long long stride) {
+  unsigned h = ((unsigned)n * 2654435761u) >> (32 - kTileBits);
+  volatile int* key = t.key;
+  for (int probe = 0; probe < 64; ++probe) {
+    int k = key[h];
+    if (k == -1) {
+      k = atomicCAS(&t.key[h], -1, n);
+      if (k == -1) k = n;
+    }
+    if (k == n) {
+      for (int v = 0; v < NV; ++v)
+        if (q[v]) atomicAdd(&t.val[v][h], (unsigned long long)q[v]);
+      return;
+    }
+    h = (h + 1) & (kTile - 1);
+  }
+  for (int v = 0; v < NV; ++v)
+    if (q[v]) atomicAdd(&acc[v * stride + n], (unsigned long long)q[v]);
+}
+
+template <int NV>
+__device__ __forceinline__ void tile_flush(Tile<NV>& t, unsigned long long* acc, long long stride) {
+  __syncthreads();
+  for (int e = threadIdx.x; e < kTile; e += blockDim.x) {
+    const int n = t.key[e];
+    if (n < 0) continue;
+    for (int v = 0; v < NV; ++v) {
+      const unsigned long long x = t.val[v][e];
+      if (x) atomicAdd(&acc[v * stride + n], x);
+    }
+  }
+}
+
+// per-step contribution bounds of the scatter transfers:
+// mode 0: mass and momentum at the start of the step (GridMomentumInitial),
+// mode 1: force (sigma * vol * grad N + fext * N, from the staged inputs),
+// mode 2: momentum with the updated velocities (GridMomentumMUSL)
+__global__ void kb_bounds(BState b, int mode) {
+  const long long i = btid();
+  int s = -1;
+  float v0 = 0.f, v1 = 0.f;
+  if (i < b.NP) {
+    s = b.scene[i];
+    const Scene& sc = b.scenes[s];
+    if (!scene_live(b, s) || sc.shape == 3) {
+      s = -1;
+    } else {
+      const long long NP = b.NP;
+      if (mode == 1) {
+        const float* f = b.fs;
+        float sig = fabsf(f[i]) + fabsf(f[NP + i]) + fabsf(f[2 * NP + i]) +
+                    2.f * (fabsf(f[3 * NP + i]) + fabsf(f[4 * NP + i]) + fabsf(f[5 * NP + i]));
+        v0 = sig * (float)sc.idcell + fabsf(f[6 * NP + i]) + fabsf(f[7 * NP + i]) + fabsf(f[8 * NP + i]);
+        v0 *= 1.0001f;  // covers the FP32 rounding of the products
+      } else {
+        const float m = (float)b.mass[i];
+        const float vm = fmaxf(fabsf((float)b.v[i]), fmaxf(fabsf((float)b.v[NP + i]), fabsf((float)b.v[2 * NP + i])));
+        v0 = m;
+        v1 = m * vm * 1.0001f;
+      }
+    }
+  }
+  if (mode == 0) {
+    scene_max(b, s, Q_MASS, v0);
+    scene_max(b, s, Q_MOM, v1);
+  } else if (mode == 1) {
+    scene_max(b, s, Q_FORCE, v0);
+  } else {
+    scene_max(b, s, Q_MOM_MUSL, v1);
+  }
+}
+
+// particle of a live scatter scene: its cell (x, y, z) and offsets, or false
+__device__ __forceinline__ bool scatter_particle(const BState& b, long long i, int& s, int c[3], float off[3]) {
+  if (i >= b.NP) return false;
+  s = b.scene[i];
+  const Scene& sc = b.scenes[s];
+  if (!scene_live(b, s) || sc.shape == 3) return false;
+  const int cl = b.cell[i];
+  if (cl < 0) return false;
+  c[2] = cl / sc.NCxy;
+  const int rem = cl - c[2] * sc.NCxy;
+  c[1] = rem / sc.NCx;
+  c[0] = rem - c[1] * sc.NCx;
+  const long long NP = b.NP;
+  off[0] = b.off[i];
+  off[1] = b.off[NP + i];
+  off[2] = b.off[2 * NP + i];
+  return true;
+}
+
+// GridMomentumInitial (update_step.f90:288-406) of linear / GIMP / B-spline
+// scenes, particle side: mass and momentum (musl = 0), or GridMomentumMUSL
+// (update_step.f90:1668-1793): momentum with the updated velocities (musl = 1)
+template <int MUSL>
+__global__ void __launch_bounds__(kScatterBlock) kb_scatter_momentum(BState b) {
+  constexpr int NV = MUSL ? 3 : 4;
+  __shared__ Tile<NV> tile;
+  tile_init(tile);
+  const long long i = btid();
+  int s, c[3];
+  float off[3];
+  if (scatter_particle(b, i, s, c, off)) {
+    const Scene& sc = b.scenes[s];
+    const SceneState& st = b.sst[s];
+    if (!MUSL || sc.musl) {
+      const long long NP = b.NP;
+      const float sm = q_scale(q_shift(sc, st.qmax[Q_MASS]));
+      const float sp = q_scale(q_shift(sc, st.qmax[MUSL ? Q_MOM_MUSL : Q_MOM]));
+      int t[3][4], nt[3];
+      float w[3][4], d[3][4];
+      for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], w[a], d[a]);
+      const float m = (float)b.mass[i];
+      const float v0 = (float)b.v[i], v1 = (float)b.v[NP + i], v2 = (float)b.v[2 * NP + i];
+      for (int az = 0; az < nt[2]; ++az) {
+        const int jz = c[2] + t[2][az];
+        if (jz < 0 || jz >= sc.NGz) continue;
+        for (int ay = 0; ay < nt[1]; ++ay) {
+          const int jy = c[1] + t[1][ay];
+          if (jy < 0 || jy >= sc.NGy) continue;
+          const float wyz = w[1][ay] * w[2][az];
+          for (int ax = 0; ax < nt[0]; ++ax) {
+            const int jx = c[0] + t[0][ax];
+            if (jx < 0 || jx >= sc.NGx) continue;
+            const float wm = w[0][ax] * wyz * m;
+            long long q[NV];
+            if (MUSL) {
+              q[0] = quant(wm * v0, sp);
+              q[1] = quant(wm * v1, sp);
+              q[2] = quant(wm * v2, sp);
+            } else {
+              q[0] = quant(wm, sm);
+              q[1] = quant(wm * v0, sp);
+              q[2] = quant(wm * v1, sp);
+              q[3] = quant(wm * v2, sp);
+            }
+            const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
+            tile_add<NV>(tile, (int)n, q, b.acc, b.NN);
+          }
+        }
+      }
+    }
+  }
+  tile_flush(tile, b.acc, b.NN);
+}
+
+// GridMomentumUpdate (update_step.f90:831-1013), particle side: internal
+// force -sigma vol grad N plus the staged external force times N
+__global__ void __launch_bounds__(kScatterBlock) kb_scatter_force(BState b) {
+  __shared__ Tile<3> tile;
+  tile_init(tile);
+  const long long i = btid();
+  int s, c[3];
+  float off[3];
+  if (scatter_particle(b, i, s, c, off)) {
+    const Scene& sc = b.scenes[s];
+    const long long NP = b.NP;
+    const float sf = q_scale(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
+    int t[3][4], nt[3];
+    float w[3][4], d[3][4];
+    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], w[a], d[a]);
+    const float idc = (float)sc.idcell;
+    const float sxx = b.fs[i], syy = b.fs[NP + i], szz = b.fs[2 * NP + i];
+    const float sxy = b.fs[3 * NP + i], syz = b.fs[4 * NP + i], sxz = b.fs[5 * NP + i];
+    const float e0 = b.fs[6 * NP + i], e1 = b.fs[7 * NP + i], e2 = b.fs[8 * NP + i];
+    for (int az = 0; az < nt[2]; ++az) {
+      const int jz = c[2] + t[2][az];
+      if (jz < 0 || jz >= sc.NGz) continue;
+      for (int ay = 0; ay < nt[1]; ++ay) {
+        const int jy = c[1] + t[1][ay];
+        if (jy < 0 || jy >= sc.NGy) continue;
+        for (int ax = 0; ax < nt[0]; ++ax) {
+          const int jx = c[0] + t[0][ax];
+          if (jx < 0 || jx >= sc.NGx) continue;
+          const float wv = w[0][ax] * w[1][ay] * w[2][az];
+          const float dx = d[0][ax] * w[1][ay] * w[2][az] * idc;
+          const float dy = w[0][ax] * d[1][ay] * w[2][az] * idc;
+          const float dz = w[0][ax] * w[1][ay] * d[2][az] * idc;
+          long long q[3];
+          q[0] = quant(-(sxx * dx + sxy * dy + sxz * dz) + e0 * wv, sf);
+          q[1] = quant(-(sxy * dx + syy * dy + syz * dz) + e1 * wv, sf);
+          q[2] = quant(-(sxz * dx + syz * dy + szz * dz) + e2 * wv, sf);
+          const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
+          tile_add<3>(tile, (int)n, q, b.acc, b.NN);
+        }
+      }
+    }
+  }
+  tile_flush(tile, b.acc, b.NN);
+}
+
+// accumulated channel v of node n in FP64 (and the accumulator cleared for
+// the next transfer)
+__device__ __forceinline__ double take_acc(BState& b, long long n, int v, double unit) {
+  const long long x = (long long)b.acc[v * b.NN + n];
+  b.acc[v * b.NN + n] = 0ull;
+  return (double)x * unit;
+}
+
 __device__ __forceinline__ void node_finish(BState& b, const Scene& sc, long long n, int bc, int vel) {
   const long long NN = b.NN;
   if (bc) {
@@ -282,9 +487,17 @@ __device__ __forceinline__ void node_finish(BState& b, const Scene& sc, long lon
       }
   }
   if (vel) {
-    double m = b.mg[n];
-    if (m > sc.cutoff)
-      for (int a = 0; a < 3; ++a) b.vg[a * NN + n] = b.px[a * NN + n] / m;
+    // node velocity for the FP32 particle gathers; nodes at or below the
+    // cut-off mass contribute nothing, so they hold zero
+    const double m = b.mg[n];
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (m > sc.cutoff) {
+      const float m32 = (float)m;
+      v.x = (float)b.px[n] / m32;
+      v.y = (float)b.px[NN + n] / m32;
+      v.z = (float)b.px[2 * NN + n] / m32;
+    }
+    b.nvel[n] = v;
   }
 }
 
@@ -320,37 +533,12 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
           }
         }
       } else {
-        auto gather = [&](const int c[3], int i0, int i1) {
-          float m = 0, p0 = 0, p1 = 0, p2 = 0;
-          for (int i = i0; i < i1; ++i) {
-            float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-            float w, g[3];
-            if (!weight3(sc.shape, c, j, off, w, g)) continue;
-            float wm = w * (float)b.mass[i];
-            m += wm;
-            p0 += wm * (float)b.v[i];
-            p1 += wm * (float)b.v[NP + i];
-            p2 += wm * (float)b.v[2 * NP + i];
-          }
-          M += m;
-          P0 += p0;
-          P1 += p1;
-          P2 += p2;
-        };
-        if (sc.kdiv > 1) {
-          gimp_sources(b, sc, j, gather);
-        } else {
-          int lo, hi;
-          cell_window(sc.shape, lo, hi);
-          for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
-            for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
-              for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
-                int i0, i1;
-                key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
-                const int c[3] = {cx, cy, cz};
-                if (i0 < i1) gather(c, i0, i1);
-              }
-        }
+        const SceneState& st = b.sst[s];
+        const double um = q_unit(q_shift(sc, st.qmax[Q_MASS])), up = q_unit(q_shift(sc, st.qmax[Q_MOM]));
+        M = take_acc(b, n, 0, um);
+        P0 = take_acc(b, n, 1, up);
+        P1 = take_acc(b, n, 2, up);
+        P2 = take_acc(b, n, 3, up);
       }
       b.mg[n] = M;
       b.px[n] = P0;
@@ -474,7 +662,8 @@ __global__ void kb_stress(BState b, int usf_pass) {
     c[0] = rem - c[1] * sc.NCx;
     float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
     int t[3][4], nt[3];
-    for (int a = 0; a < 3; ++a) nt[a] = node_offsets(sc.shape, off[a], t[a]);
+    float wd[3][4], dd[3][4];
+    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], wd[a], dd[a]);
     const float idc = (float)sc.idcell;
     for (int az = 0; az < nt[2]; ++az)
       for (int ay = 0; ay < nt[1]; ++ay)
@@ -482,11 +671,11 @@ __global__ void kb_stress(BState b, int usf_pass) {
           int j[3] = {c[0] + t[0][ax], c[1] + t[1][ay], c[2] + t[2][az]};
           if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
           long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
-          if (!(b.mg[n] > sc.cutoff)) continue;
-          float w, g[3];
-          if (!weight3(sc.shape, c, j, off, w, g)) continue;
-          float dx = g[0] * idc, dy = g[1] * idc, dz = g[2] * idc;
-          float v[3] = {(float)b.vg[n], (float)b.vg[NN + n], (float)b.vg[2 * NN + n]};
+          const float4 v4 = b.nvel[n];  // zero below the cut-off mass
+          float dx = dd[0][ax] * wd[1][ay] * wd[2][az] * idc;
+          float dy = wd[0][ax] * dd[1][ay] * wd[2][az] * idc;
+          float dz = wd[0][ax] * wd[1][ay] * dd[2][az] * idc;
+          float v[3] = {v4.x, v4.y, v4.z};
           de[0] += dx * v[0];
           de[1] += dy * v[1];
           de[2] += dz * v[2];
@@ -684,9 +873,15 @@ __device__ __forceinline__ void node_integrate(BState& b, const Scene& sc, long 
     b.px[a * NN + n] = p;
   }
   node_finish(b, sc, n, 1, 1);
-  double m = b.mg[n];
-  if (m > sc.cutoff)
-    for (int a = 0; a < 3; ++a) b.ag[a * NN + n] = b.fx[a * NN + n] / m;
+  const double m = b.mg[n];
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (m > sc.cutoff) {
+    const float m32 = (float)m;
+    acc.x = (float)b.fx[n] / m32;
+    acc.y = (float)b.fx[NN + n] / m32;
+    acc.z = (float)b.fx[2 * NN + n] / m32;
+  }
+  b.nacc[n] = acc;
 }
 
 __global__ void kb_p2g_force(BState b) {
@@ -701,7 +896,6 @@ __global__ void kb_p2g_force(BState b) {
   double F[3] = {0, 0, 0};
   if (sc.shape == 3) {
     const long long NC = b.NC;
-    const float j4 = (float)sc.iJacobi4;
     for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
       if (cz < 0 || cz >= sc.NCz) continue;
       for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
@@ -718,43 +912,12 @@ __global__ void kb_p2g_force(BState b) {
           F[0] += 0.125 * b.cfext[c] - (c0 * dx + c3 * dy + c5 * dz);
           F[1] += 0.125 * b.cfext[NC + c] - (c3 * dx + c1 * dy + c4 * dz);
           F[2] += 0.125 * b.cfext[2 * NC + c] - (c5 * dx + c4 * dy + c2 * dz);
-          (void)j4;
         }
       }
     }
   } else {
-    const float idc = (float)sc.idcell;
-    auto gather = [&](const int c[3], int i0, int i1) {
-      float f0 = 0, f1 = 0, f2 = 0;
-      for (int i = i0; i < i1; ++i) {
-        float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-        float w, g[3];
-        if (!weight3(sc.shape, c, j, off, w, g)) continue;
-        float dx = g[0] * idc, dy = g[1] * idc, dz = g[2] * idc;
-        float sxx = b.fs[i], syy = b.fs[NP + i], szz = b.fs[2 * NP + i];
-        float sxy = b.fs[3 * NP + i], syz = b.fs[4 * NP + i], sxz = b.fs[5 * NP + i];
-        f0 += -(sxx * dx + sxy * dy + sxz * dz) + b.fs[6 * NP + i] * w;
-        f1 += -(sxy * dx + syy * dy + syz * dz) + b.fs[7 * NP + i] * w;
-        f2 += -(sxz * dx + syz * dy + szz * dz) + b.fs[8 * NP + i] * w;
-      }
-      F[0] += f0;
-      F[1] += f1;
-      F[2] += f2;
-    };
-    if (sc.kdiv > 1) {
-      gimp_sources(b, sc, j, gather);
-    } else {
-      int lo, hi;
-      cell_window(sc.shape, lo, hi);
-      for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
-        for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
-          for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
-            int i0, i1;
-            key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
-            const int c[3] = {cx, cy, cz};
-            if (i0 < i1) gather(c, i0, i1);
-          }
-    }
+    const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
+    for (int a = 0; a < 3; ++a) F[a] = take_acc(b, n, a, u);
   }
   node_integrate(b, sc, n, F);
 }
@@ -799,20 +962,21 @@ __global__ void kb_sg_centre_gradient(BState b, int usf_pass) {
   if (!scene_live(b, s)) return;
   const Scene& sc = b.scenes[s];
   if (sc.usf != usf_pass) return;
-  const long long NN = b.NN, NC = b.NC;
+  const long long NC = b.NC;
   long long lc = c - sc.c0;
   int q[3];
   q[2] = (int)(lc / sc.NCxy);
   int rem = (int)(lc - (long long)q[2] * sc.NCxy);
   q[1] = rem / sc.NCx;
   q[0] = rem - q[1] * sc.NCx;
-  double co[6] = {0, 0, 0, 0, 0, 0}, cw[3] = {0, 0, 0}, cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float co[6] = {0, 0, 0, 0, 0, 0}, cw[3] = {0, 0, 0}, cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const float j4 = (float)sc.iJacobi4;
   for (int k = 0; k < 8; ++k) {
     long long n = sc.n0 + ((long long)(q[2] + kCorner[k][2]) * sc.NGy + q[1] + kCorner[k][1]) * sc.NGx + q[0] +
                   kCorner[k][0];
-    if (!(b.mg[n] > sc.cutoff)) continue;
-    double v[3] = {b.vg[n], b.vg[NN + n], b.vg[2 * NN + n]};
-    double dx = kSN[0][k] * sc.iJacobi4, dy = kSN[1][k] * sc.iJacobi4, dz = kSN[2][k] * sc.iJacobi4;
+    const float4 v4 = b.nvel[n];  // zero below the cut-off mass
+    const float v[3] = {v4.x, v4.y, v4.z};
+    const float dx = kSN[0][k] * j4, dy = kSN[1][k] * j4, dz = kSN[2][k] * j4;
     co[0] += dx * v[0];
     co[1] += dy * v[1];
     co[2] += dz * v[2];
@@ -841,7 +1005,6 @@ __global__ void kb_sg_centre_velocity(BState b) {
   int s = b.cscene[c];
   if (!scene_live(b, s)) return;
   const Scene& sc = b.scenes[s];
-  const long long NN = b.NN, NC = b.NC;
   long long lc = c - sc.c0;
   int q[3];
   q[2] = (int)(lc / sc.NCxy);
@@ -849,6 +1012,7 @@ __global__ void kb_sg_centre_velocity(BState b) {
   q[1] = rem / sc.NCx;
   q[0] = rem - q[1] * sc.NCx;
   const int NCd[3] = {sc.NCx, sc.NCy, sc.NCz};
+  const long long NC = b.NC;
   bool boundary = false;
   for (int a = 0; a < 3; ++a)
     if (NCd[a] > 1 && ((q[a] == 0 && sc.fixs[2 * a] != 0) || (q[a] == NCd[a] - 1 && sc.fixs[2 * a + 1] != 0)))
@@ -857,18 +1021,21 @@ __global__ void kb_sg_centre_velocity(BState b) {
   if (boundary)
     for (int a = 0; a < 3; ++a)
       if (NCd[a] > 1) cxx[a] = q[a] == NCd[a] - 1 ? -1.0 : (q[a] == 0 ? 1.0 : 0.0);
-  double v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
+  float v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
   for (int k = 0; k < 8; ++k) {
     long long n = sc.n0 + ((long long)(q[2] + kCorner[k][2]) * sc.NGy + q[1] + kCorner[k][1]) * sc.NGx + q[0] +
                   kCorner[k][0];
-    double m = b.mg[n];
-    if (!(m > sc.cutoff)) continue;
-    double w = 0.125;
-    if (boundary) w = (kSN[0][k] * cxx[0] + 1.0) * (kSN[1][k] * cxx[1] + 1.0) * (kSN[2][k] * cxx[2] + 1.0) * 0.125;
-    for (int a = 0; a < 3; ++a) {
-      v[a] += w * b.px[a * NN + n] / m;
-      acc[a] += w * b.fx[a * NN + n] / m;
-    }
+    float w = 0.125f;
+    if (boundary)
+      w = ((float)kSN[0][k] * (float)cxx[0] + 1.f) * ((float)kSN[1][k] * (float)cxx[1] + 1.f) *
+          ((float)kSN[2][k] * (float)cxx[2] + 1.f) * 0.125f;
+    const float4 vn = b.nvel[n], an = b.nacc[n];  // zero below the cut-off mass
+    v[0] += w * vn.x;
+    v[1] += w * vn.y;
+    v[2] += w * vn.z;
+    acc[0] += w * an.x;
+    acc[1] += w * an.y;
+    acc[2] += w * an.z;
   }
   for (int a = 0; a < 3; ++a) {
     b.cvx[a * NC + c] = v[a];
@@ -924,21 +1091,22 @@ __global__ void kb_position(BState b) {
     c[0] = rem - c[1] * sc.NCx;
     float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
     int t[3][4], nt[3];
-    for (int a = 0; a < 3; ++a) nt[a] = node_offsets(sc.shape, off[a], t[a]);
+    float wd[3][4], dd[3][4];
+    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], wd[a], dd[a]);
     for (int az = 0; az < nt[2]; ++az)
       for (int ay = 0; ay < nt[1]; ++ay)
         for (int ax = 0; ax < nt[0]; ++ax) {
           int j[3] = {c[0] + t[0][ax], c[1] + t[1][ay], c[2] + t[2][az]};
           if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
           long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
-          double m = b.mg[n];
-          if (!(m > sc.cutoff)) continue;
-          float w, g[3];
-          if (!weight3(sc.shape, c, j, off, w, g)) continue;
-          for (int a = 0; a < 3; ++a) {
-            v[a] += w * (float)b.vg[a * NN + n];
-            acc[a] += w * (float)b.ag[a * NN + n];
-          }
+          const float w = wd[0][ax] * wd[1][ay] * wd[2][az];
+          const float4 vn = b.nvel[n], an = b.nacc[n];  // zero below the cut-off mass
+          v[0] += w * vn.x;
+          v[1] += w * vn.y;
+          v[2] += w * vn.z;
+          acc[0] += w * an.x;
+          acc[1] += w * an.y;
+          acc[2] += w * an.z;
         }
   }
   const double dt = st.dt;
@@ -980,35 +1148,10 @@ __global__ void kb_p2g_momentum(BState b) {
       }
     }
   } else {
-    auto gather = [&](const int c[3], int i0, int i1) {
-      float p0 = 0, p1 = 0, p2 = 0;
-      for (int i = i0; i < i1; ++i) {
-        float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-        float w, g[3];
-        if (!weight3(sc.shape, c, j, off, w, g)) continue;
-        float wm = w * (float)b.mass[i];
-        p0 += wm * (float)b.v[i];
-        p1 += wm * (float)b.v[NP + i];
-        p2 += wm * (float)b.v[2 * NP + i];
-      }
-      P0 += p0;
-      P1 += p1;
-      P2 += p2;
-    };
-    if (sc.kdiv > 1) {
-      gimp_sources(b, sc, j, gather);
-    } else {
-      int lo, hi;
-      cell_window(sc.shape, lo, hi);
-      for (int cz = max(0, j[2] + lo); cz <= min(sc.NCz - 1, j[2] + hi); ++cz)
-        for (int cy = max(0, j[1] + lo); cy <= min(sc.NCy - 1, j[1] + hi); ++cy)
-          for (int cx = max(0, j[0] + lo); cx <= min(sc.NCx - 1, j[0] + hi); ++cx) {
-            int i0, i1;
-            key_range(b, sc.k0 + (cz * sc.NCy + cy) * sc.NCx + cx, i0, i1);
-            const int c[3] = {cx, cy, cz};
-            if (i0 < i1) gather(c, i0, i1);
-          }
-    }
+    const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]));
+    P0 = take_acc(b, n, 0, u);
+    P1 = take_acc(b, n, 1, u);
+    P2 = take_acc(b, n, 2, u);
   }
   b.px[n] = P0;
   b.px[NN + n] = P1;

@@ -351,7 +351,7 @@ class MpmStep:
         return int(library().mpm_device_bytes(self._h))
 
 
-BATCH_OPTIONS = {"particle_block": 1, "node_block": 2, "gimp_split": 3}
+BATCH_OPTIONS = {"particle_block": 1, "node_block": 2}
 
 
 class Batch:
