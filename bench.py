@@ -278,11 +278,57 @@ def run_ours(args) -> dict:
         "gpu_launches": sum(k["launches"] for k in mixed["kernels"]),
         "clocks": mixed["clocks"],
     }
+    if world == 1 and args.serve_scenes > 0:
+        line["serving"] = run_serving(args, local)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(text, args.cpu_steps, npart)
     if dist:
         dist.destroy_process_group()
     return line if rank == 0 else None
+
+
+def run_serving(args, device: int) -> dict:
+    """Serving workload: scenes (Cook membrane panels and cantilever soft
+    beams, SGMP, MUSL, neo-Hookean; particle counts log-uniform in 2k..400k;
+    E log-uniform in 1..100 MPa, nu uniform in 0.3..0.49) arriving as a
+    Poisson process, each run for a fixed step count through the serving
+    runtime (HBM-budget admission, batched chunks, CUDA graphs, launch-shape
+    autotuning). Reports scene latency (submit to retirement) percentiles and
+    the aggregate particle-step rate over the run."""
+    import numpy as np
+    import mpm3d_gb300 as m
+    from mpm3d_gb300 import decks
+
+    rng = np.random.default_rng(0x5E4E)
+    gen = [decks.serving_scene(rng) for _ in range(args.serve_scenes)]
+    dks = [m.Deck.parse(t) for t, _, _ in gen]
+    nps = np.array([n for _, n, _ in gen], dtype=np.float64)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=len(dks)))
+    with m.Server(device=device, chunk_steps=25, autotune=True) as srv:
+        tickets = []
+        t0 = time.perf_counter()
+        for k, d in enumerate(dks):
+            wait = arrivals[k] - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            tickets.append(srv.submit(d, args.serve_steps))
+        for t in tickets:
+            srv.wait(t)
+        wall = time.perf_counter() - t0
+        res = [srv.result(t) for t in tickets]
+        st = srv.stats()
+    lat = np.array([r["latency_ms"] for r in res])
+    queue = np.array([r["queue_ms"] for r in res])
+    return {
+        "scenes": len(dks), "steps_per_scene": args.serve_steps, "arrival_rate_per_s": args.serve_rate,
+        "particles_min_max_mean": [int(nps.min()), int(nps.max()), float(nps.mean())],
+        "p50_latency_ms": float(np.percentile(lat, 50)), "p99_latency_ms": float(np.percentile(lat, 99)),
+        "mean_queue_ms": float(queue.mean()), "makespan_s": wall,
+        "particle_steps_per_s": float(nps.sum() * args.serve_steps / wall),
+        "gpu_busy_frac": st["busy_ms"] / 1e3 / wall, "chunks": int(st["chunks"]),
+        "autotuned_blocks": [int(st["particle_block"]), int(st["node_block"])],
+        "peak_resident_bytes": int(st["peak_resident_bytes"]),
+    }
 
 
 def cpu_baseline(text: str, steps: int, npart: int, cores: int = 1) -> dict:
@@ -357,6 +403,9 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=2)
     ap.add_argument("--ref-warmup", type=int, default=1)
     ap.add_argument("--ref-cores", type=int, default=0)
+    ap.add_argument("--serve-scenes", type=int, default=256, help="serving workload scenes (0 = skip)")
+    ap.add_argument("--serve-steps", type=int, default=500)
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (scenes/s)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

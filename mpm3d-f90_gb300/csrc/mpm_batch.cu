@@ -265,7 +265,7 @@ int enqueue_step(mpm_batch* b) {
   kb_begin<<<gridn(a.nscene, 128), 128, 0, st>>>(a, b->d_target);
   prof_end(K_BEGIN, st);
   prof_begin(K_LOCATE, st);
-  if (b->any_sgmp) cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
+  cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
   kb_keys<<<gridn(a.NP, pb), pb, 0, st>>>(a);
   prof_end(K_LOCATE, st);
   prof_begin(K_SORT, st);
@@ -273,11 +273,9 @@ int enqueue_step(mpm_batch* b) {
   cudaError_t e = cub::DeviceRadixSort::SortPairs(b->cub_tmp, tmp, a.key, a.key_sorted, a.val, a.perm, (int)a.NP, 0,
                                                   b->key_bits, st);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "sort: %s", cudaGetErrorString(e));
-  if (b->any_sgmp) {
-    tmp = b->cub_bytes;
-    e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
-    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
-  }
+  tmp = b->cub_bytes;
+  e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
   prof_end(K_SORT, st);
   prof_begin(K_PERMUTE, st);
   kb_permute<<<gridn(a.NP, pb), pb, 0, st>>>(a, b->B);
@@ -289,8 +287,7 @@ int enqueue_step(mpm_batch* b) {
   prof_begin(K_P2G_MASS, st);
   if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
   if (scatter) {
-    kb_bounds<<<gridn(s.NP, pb), pb, 0, st>>>(s, 0);
-    kb_scatter_momentum<0><<<gridn(s.NP, kScatterBlock), kScatterBlock, 0, st>>>(s);
+    kb_cell_scatter<0><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
   }
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
   prof_end(K_P2G_MASS, st);
@@ -318,8 +315,7 @@ int enqueue_step(mpm_batch* b) {
   prof_begin(K_P2G_FORCE, st);
   if (b->any_sgmp) kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
   if (scatter) {
-    kb_bounds<<<gridn(s.NP, pb), pb, 0, st>>>(s, 1);
-    kb_scatter_force<<<gridn(s.NP, kScatterBlock), kScatterBlock, 0, st>>>(s);
+    kb_cell_scatter<2><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
   }
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
   prof_end(K_P2G_FORCE, st);
@@ -331,8 +327,7 @@ int enqueue_step(mpm_batch* b) {
     prof_begin(K_P2G_MOM, st);
     if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
     if (scatter) {
-      kb_bounds<<<gridn(s.NP, pb), pb, 0, st>>>(s, 2);
-      kb_scatter_momentum<1><<<gridn(s.NP, kScatterBlock), kScatterBlock, 0, st>>>(s);
+      kb_cell_scatter<1><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
     }
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
     prof_end(K_P2G_MOM, st);
@@ -484,11 +479,11 @@ int commit(mpm_batch* b) {
   shared.cpx = al.get<double>(3 * NC);
   shared.cfext = al.get<double>(3 * NC);
   shared.cfint = al.get<double>(6 * NC);
-  shared.co = al.get<double>(6 * NC);
-  shared.cw = al.get<double>(3 * NC);
-  shared.cdefp = al.get<double>(9 * NC);
-  shared.cvx = al.get<double>(3 * NC);
-  shared.cax = al.get<double>(3 * NC);
+  shared.co = al.get<float>(6 * NC);
+  shared.cw = al.get<float>(3 * NC);
+  shared.cdefp = al.get<float>(9 * NC);
+  shared.cvx = al.get<float>(3 * NC);
+  shared.cax = al.get<float>(3 * NC);
   shared.cscene = al.get<uint16_t>(NC);
   if (b->any_jc) {
     shared.setter = al.get<int>(NP);

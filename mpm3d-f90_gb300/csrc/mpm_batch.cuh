@@ -13,7 +13,7 @@
 //   grid nodes concatenated: FP64 mg, px[3], fx[3]; FP32 float4 velocity and
 //     acceleration (for the particle gathers); fix, bd, node scene
 //   SGMP centre nodes (one per cell) concatenated: FP64 cmg, cpx[3], cfext[3],
-//     cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3]
+//     cfint[6]; FP32 co[6], cw[3], cdefp[9], cvx[3], cax[3]
 //   sort keys: scene s owns keys [k0, k0 + nk), the last one collects the
 //     particles outside its grid; seg[k] = end of key k's particle range
 //     (kept for SGMP scenes). Linear / GIMP / B-spline: one key per cell;
@@ -86,7 +86,8 @@ struct BState {
   uint8_t *fix, *bd;
   uint16_t* node_scene;
   // SGMP centre grid
-  double *cmg, *cpx, *cfext, *cfint, *co, *cw, *cdefp, *cvx, *cax;
+  double *cmg, *cpx, *cfext, *cfint;   // accumulated (FP64)
+  float *co, *cw, *cdefp, *cvx, *cax;  // derived from node velocities / accelerations (FP32)
   uint16_t* cscene;
   // Johnson-Cook depeff carry (indexed by scene particle range + orig)
   int *setter, *setter_scan;

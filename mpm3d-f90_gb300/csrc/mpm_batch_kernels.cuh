@@ -117,16 +117,14 @@ __global__ void kb_keys(BState b) {
   long long key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
   b.key[i] = (unsigned)key;
   b.val[i] = (int)i;
-  if (b.any_sgmp) atomicAdd(&b.seg[key], 1);  // per-key counts for the SGMP centre gathers
+  atomicAdd(&b.seg[key], 1);
 }
 
 // ---------------------------------------------------- permutation + derived
 // dst[i] = src[perm[i]] for every persistent particle field, then the per-step
 // derived data of the particle at its new position (ParticleInitial,
 // update_step.f90:408-453, in FP32 form).
-__global__ void kb_permute(BState src, BState dst) {
-  long long i = btid();
-  if (i >= src.NP) return;
+__device__ __forceinline__ void permute_one(const BState& src, BState& dst, long long i) {
   const long long NP = src.NP;
   const long long j = src.perm[i];
   for (int a = 0; a < 3; ++a) {
@@ -194,21 +192,41 @@ __global__ void kb_permute(BState src, BState dst) {
 // 2^E, and contributions are scaled by 2^(61 - E), so no sum can reach 2^62.
 // The rounding of a contribution to the fixed-point grid (np * B * 2^-61)
 // is far below its FP32 rounding.
-//
-// A block adds the contributions of its 256 consecutive (cell-sorted)
-// particles into a shared-memory hash tile keyed by node, then adds each
-// tile entry to the global accumulator with one atomic per channel.
+// The bounds are taken by the kernels that run before each transfer
+// (permutation, force staging, position update).
 
 // per-scene bound slots (SceneState::qmax, float bits, reset every step)
 enum QSlot { Q_MASS = 0, Q_MOM = 1, Q_FORCE = 2, Q_MOM_MUSL = 3 };
 
-// warp-aggregated max of non-negative v into sst[s].qmax[slot]; every lane of
-// the warp must call it (s < 0: no value)
-__device__ __forceinline__ void scene_max(BState& b, int s, int slot, float v) {
-  const unsigned bits = __float_as_uint(v);
+// Max of non-negative values v[k] over the block into sst[s].qmax[slot[k]],
+// per scene s (s < 0: no value). Every thread of the block must call it.
+// Warps whose lanes all belong to one scene combine through shared memory,
+// so a block usually issues one atomic per slot: a per-warp atomic on the
+// same address from every warp of a large scene would serialise in L2.
+template <int NS>
+__device__ __forceinline__ void block_scene_max(BState& b, int s, const int (&slot)[NS], const float (&v)[NS]) {
+  __shared__ int ws[32];
+  __shared__ unsigned wv[32][NS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   const unsigned grp = __match_any_sync(0xffffffffu, s);
-  const unsigned mx = __reduce_max_sync(grp, bits);
-  if (s >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&b.sst[s].qmax[slot], mx);
+  unsigned mx[NS];
+  for (int k = 0; k < NS; ++k) mx[k] = __reduce_max_sync(grp, __float_as_uint(v[k]));
+  const bool uniform = grp == 0xffffffffu;
+  if (!uniform && s >= 0 && lane == __ffs(grp) - 1)
+    for (int k = 0; k < NS; ++k) atomicMax(&b.sst[s].qmax[slot[k]], mx[k]);
+  if (lane == 0) {
+    ws[warp] = uniform ? s : -1;
+    for (int k = 0; k < NS; ++k) wv[warp][k] = mx[k];
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int s2 = lane < nw ? ws[lane] : -1;
+    const unsigned g2 = __match_any_sync(0xffffffffu, s2);
+    for (int k = 0; k < NS; ++k) {
+      const unsigned m2 = __reduce_max_sync(g2, lane < nw ? wv[lane][k] : 0u);
+      if (s2 >= 0 && lane == __ffs(g2) - 1) atomicMax(&b.sst[s2].qmax[slot[k]], m2);
+    }
+  }
 }
 
 // Fixed-point shift sh of a scene's channel: contributions are rounded to
@@ -254,218 +272,158 @@ __device__ __forceinline__ int dim_nodes(int shape, float off, int t[4], float w
   return n;
 }
 
-constexpr int kTileBits = 10;
-constexpr int kTile = 1 << kTileBits;  // hash slots per block
-constexpr int kScatterBlock = 256;
-
-template <int NV>
-struct Tile {
-  int key[kTile];                      // global node index, -1 = empty
-  unsigned long long val[NV][kTile];   // fixed-point sums (two's complement)
-};
-
-template <int NV>
-__device__ __forceinline__ void tile_init(Tile<NV>& t) {
-  for (int e = threadIdx.x; e < kTile; e += blockDim.x) {
-    t.key[e] = -1;
-    for (int v = 0; v < NV; ++v) t.val[v][e] = 0ull;
-  }
-  __syncthreads();
-}
-
-// add q[NV] to node n: into the tile (linear probing), or straight into the
-// global accumulator if the tile has no room within the probe limit
-template <int NV>
-__device__ __forceinline__ void tile_add(Tile<NV>& t, int n, const long long q[NV], unsigned long long* acc,
-                                         long long stride) {
-  unsigned h = ((unsigned)n * 2654435761u) >> (32 - kTileBits);
-  volatile int* key = t.key;
-  for (int probe = 0; probe < 64; ++probe) {
-    int k = key[h];
-    if (k == -1) {
-      k = atomicCAS(&t.key[h], -1, n);
-      if (k == -1) k = n;
-    }
-    if (k == n) {
-      for (int v = 0; v < NV; ++v)
-        if (q[v]) atomicAdd(&t.val[v][h], (unsigned long long)q[v]);
-      return;
-    }
-    h = (h + 1) & (kTile - 1);
-  }
-  for (int v = 0; v < NV; ++v)
-    if (q[v]) atomicAdd(&acc[v * stride + n], (unsigned long long)q[v]);
-}
-
-template <int NV>
-__device__ __forceinline__ void tile_flush(Tile<NV>& t, unsigned long long* acc, long long stride) {
-  __syncthreads();
-  for (int e = threadIdx.x; e < kTile; e += blockDim.x) {
-    const int n = t.key[e];
-    if (n < 0) continue;
-    for (int v = 0; v < NV; ++v) {
-      const unsigned long long x = t.val[v][e];
-      if (x) atomicAdd(&acc[v * stride + n], x);
-    }
-  }
-}
-
-// per-step contribution bounds of the scatter transfers:
-// mode 0: mass and momentum at the start of the step (GridMomentumInitial),
-// mode 1: force (sigma * vol * grad N + fext * N, from the staged inputs),
-// mode 2: momentum with the updated velocities (GridMomentumMUSL)
-__global__ void kb_bounds(BState b, int mode) {
+// permutation kernel; it also takes the mass and momentum bounds of the
+// step's first particle -> node transfer
+__global__ void kb_permute(BState src, BState dst) {
   const long long i = btid();
   int s = -1;
-  float v0 = 0.f, v1 = 0.f;
-  if (i < b.NP) {
-    s = b.scene[i];
-    const Scene& sc = b.scenes[s];
-    if (!scene_live(b, s) || sc.shape == 3) {
-      s = -1;
+  float bm = 0.f, bv = 0.f;
+  if (i < src.NP) {
+    permute_one(src, dst, i);
+    s = dst.scene[i];
+    if (scene_live(dst, s)) {
+      const long long NP = dst.NP;
+      bm = (float)dst.mass[i];
+      bv = bm * fmaxf(fabsf((float)dst.v[i]), fmaxf(fabsf((float)dst.v[NP + i]), fabsf((float)dst.v[2 * NP + i]))) *
+           1.0001f;
     } else {
-      const long long NP = b.NP;
-      if (mode == 1) {
-        const float* f = b.fs;
-        float sig = fabsf(f[i]) + fabsf(f[NP + i]) + fabsf(f[2 * NP + i]) +
-                    2.f * (fabsf(f[3 * NP + i]) + fabsf(f[4 * NP + i]) + fabsf(f[5 * NP + i]));
-        v0 = sig * (float)sc.idcell + fabsf(f[6 * NP + i]) + fabsf(f[7 * NP + i]) + fabsf(f[8 * NP + i]);
-        v0 *= 1.0001f;  // covers the FP32 rounding of the products
-      } else {
-        const float m = (float)b.mass[i];
-        const float vm = fmaxf(fabsf((float)b.v[i]), fmaxf(fabsf((float)b.v[NP + i]), fabsf((float)b.v[2 * NP + i])));
-        v0 = m;
-        v1 = m * vm * 1.0001f;
-      }
+      s = -1;
     }
   }
-  if (mode == 0) {
-    scene_max(b, s, Q_MASS, v0);
-    scene_max(b, s, Q_MOM, v1);
-  } else if (mode == 1) {
-    scene_max(b, s, Q_FORCE, v0);
-  } else {
-    scene_max(b, s, Q_MOM_MUSL, v1);
-  }
+  block_scene_max<2>(dst, s, {Q_MASS, Q_MOM}, {bm, bv});
 }
 
-// particle of a live scatter scene: its cell (x, y, z) and offsets, or false
-__device__ __forceinline__ bool scatter_particle(const BState& b, long long i, int& s, int c[3], float off[3]) {
-  if (i >= b.NP) return false;
-  s = b.scene[i];
+// Cell-centric form of the scatter: one warp per sort key (cell). The cell's
+// particles are staged 32 at a time in shared memory with their per-direction
+// weight (and derivative) tables for the node offsets t = -1..2 of the cell
+// (zero where the shape function has no support; linear shapes use t = 0..1,
+// B-splines t = -1..1); lane l then sums node slots l and l + 32 -- slot =
+// (tz + 1) * 16 + (ty + 1) * 4 + (tx + 1) -- over the cell's particles in
+// storage order (FP32), and adds each nonzero slot sum, quantised, to the
+// node's fixed-point accumulator. A cell's sums depend only on its own
+// particle list, so they are the same alone or in a batch.
+// mode 0: mass + momentum (GridMomentumInitial), 1: momentum with the updated
+// velocities (GridMomentumMUSL), 2: force (GridMomentumUpdate).
+constexpr int kCellWarps = 8;  // warps (cells) per block
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b) {
+  constexpr int NV = MODE == 0 ? 4 : 3;       // channels
+  constexpr int NQ = MODE == 2 ? 9 : 4;       // per-particle quantities staged
+  constexpr int NT = MODE == 2 ? 24 : 12;     // per-particle table entries (w, and d for the force)
+  __shared__ float sq[kCellWarps][32][NQ + NT + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long key = (long long)blockIdx.x * kCellWarps + warp;
+  if (key >= b.NK) return;
+  int i0, i1;
+  key_range(b, key, i0, i1);
+  if (i0 >= i1) return;
+  const int s = b.scene[i0];
   const Scene& sc = b.scenes[s];
-  if (!scene_live(b, s) || sc.shape == 3) return false;
-  const int cl = b.cell[i];
-  if (cl < 0) return false;
+  if (!scene_live(b, s) || sc.shape == 3 || (MODE == 1 && !sc.musl)) return;
+  const int cl = b.cell[i0];
+  if (cl < 0) return;  // the scene's off-grid bucket
+  int c[3];
   c[2] = cl / sc.NCxy;
-  const int rem = cl - c[2] * sc.NCxy;
-  c[1] = rem / sc.NCx;
-  c[0] = rem - c[1] * sc.NCx;
+  {
+    const int rem = cl - c[2] * sc.NCxy;
+    c[1] = rem / sc.NCx;
+    c[0] = rem - c[1] * sc.NCx;
+  }
   const long long NP = b.NP;
-  off[0] = b.off[i];
-  off[1] = b.off[NP + i];
-  off[2] = b.off[2 * NP + i];
-  return true;
-}
-
-// GridMomentumInitial (update_step.f90:288-406) of linear / GIMP / B-spline
-// scenes, particle side: mass and momentum (musl = 0), or GridMomentumMUSL
-// (update_step.f90:1668-1793): momentum with the updated velocities (musl = 1)
-template <int MUSL>
-__global__ void __launch_bounds__(kScatterBlock) kb_scatter_momentum(BState b) {
-  constexpr int NV = MUSL ? 3 : 4;
-  __shared__ Tile<NV> tile;
-  tile_init(tile);
-  const long long i = btid();
-  int s, c[3];
-  float off[3];
-  if (scatter_particle(b, i, s, c, off)) {
-    const Scene& sc = b.scenes[s];
-    const SceneState& st = b.sst[s];
-    if (!MUSL || sc.musl) {
-      const long long NP = b.NP;
-      const float sm = q_scale(q_shift(sc, st.qmax[Q_MASS]));
-      const float sp = q_scale(q_shift(sc, st.qmax[MUSL ? Q_MOM_MUSL : Q_MOM]));
-      int t[3][4], nt[3];
-      float w[3][4], d[3][4];
-      for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], w[a], d[a]);
-      const float m = (float)b.mass[i];
-      const float v0 = (float)b.v[i], v1 = (float)b.v[NP + i], v2 = (float)b.v[2 * NP + i];
-      for (int az = 0; az < nt[2]; ++az) {
-        const int jz = c[2] + t[2][az];
-        if (jz < 0 || jz >= sc.NGz) continue;
-        for (int ay = 0; ay < nt[1]; ++ay) {
-          const int jy = c[1] + t[1][ay];
-          if (jy < 0 || jy >= sc.NGy) continue;
-          const float wyz = w[1][ay] * w[2][az];
-          for (int ax = 0; ax < nt[0]; ++ax) {
-            const int jx = c[0] + t[0][ax];
-            if (jx < 0 || jx >= sc.NGx) continue;
-            const float wm = w[0][ax] * wyz * m;
-            long long q[NV];
-            if (MUSL) {
-              q[0] = quant(wm * v0, sp);
-              q[1] = quant(wm * v1, sp);
-              q[2] = quant(wm * v2, sp);
-            } else {
-              q[0] = quant(wm, sm);
-              q[1] = quant(wm * v0, sp);
-              q[2] = quant(wm * v1, sp);
-              q[3] = quant(wm * v2, sp);
-            }
-            const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
-            tile_add<NV>(tile, (int)n, q, b.acc, b.NN);
+  const SceneState& st = b.sst[s];
+  float scale[NV];
+  if (MODE == 0) {
+    scale[0] = q_scale(q_shift(sc, st.qmax[Q_MASS]));
+    scale[1] = scale[2] = scale[3] = q_scale(q_shift(sc, st.qmax[Q_MOM]));
+  } else {
+    const float sv = q_scale(q_shift(sc, st.qmax[MODE == 1 ? Q_MOM_MUSL : Q_FORCE]));
+    for (int v = 0; v < NV; ++v) scale[v] = sv;
+  }
+  // node offsets of this lane's two slots (-1..2 per direction)
+  int to[2][3];
+  bool use[2];
+  const int tlo = sc.shape == 0 ? 0 : -1, thi = sc.shape == 1 ? 2 : 1;
+  for (int k = 0; k < 2; ++k) {
+    const int slot = lane + 32 * k;
+    to[k][0] = (slot & 3) - 1;
+    to[k][1] = ((slot >> 2) & 3) - 1;
+    to[k][2] = (slot >> 4) - 1;
+    use[k] = true;
+    for (int a = 0; a < 3; ++a) use[k] = use[k] && to[k][a] >= tlo && to[k][a] <= thi;
+  }
+  const float idc = (float)sc.idcell;
+  float acc[2][NV];
+  for (int k = 0; k < 2; ++k)
+    for (int v = 0; v < NV; ++v) acc[k][v] = 0.f;
+  float* row = sq[warp][lane];
+  for (int base = i0; base < i1; base += 32) {
+    const int cnt = min(32, i1 - base);
+    if (lane < cnt) {
+      const long long i = base + lane;
+      float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+      if (MODE == 2) {
+        for (int q = 0; q < 9; ++q) row[q] = b.fs[q * NP + i];
+      } else {
+        const float m = (float)b.mass[i];
+        row[0] = m;
+        row[1] = (float)b.v[i];
+        row[2] = (float)b.v[NP + i];
+        row[3] = (float)b.v[2 * NP + i];
+      }
+      for (int a = 0; a < 3; ++a)
+        for (int t = -1; t <= 2; ++t) {
+          float w = 0.f, d = 0.f;
+          if (t >= tlo && t <= thi) {
+            if (sc.shape == 0) lin1(t, off[a], w, d);
+            else if (sc.shape == 2) bsp1(t, off[a], w, d);
+            else gimp1((float)(-t) + off[a], w, d);
+          }
+          row[NQ + a * 4 + t + 1] = w;
+          if (MODE == 2) row[NQ + 12 + a * 4 + t + 1] = d;
+        }
+    }
+    __syncwarp();
+    for (int p = 0; p < cnt; ++p) {
+      const float* r = sq[warp][p];
+      for (int k = 0; k < 2; ++k) {
+        if (!use[k]) continue;
+        const float wx = r[NQ + 0 + to[k][0] + 1], wy = r[NQ + 4 + to[k][1] + 1], wz = r[NQ + 8 + to[k][2] + 1];
+        if (MODE == 2) {
+          const float dx = r[NQ + 12 + to[k][0] + 1] * wy * wz * idc;
+          const float dy = wx * r[NQ + 16 + to[k][1] + 1] * wz * idc;
+          const float dz = wx * wy * r[NQ + 20 + to[k][2] + 1] * idc;
+          const float wv = wx * wy * wz;
+          acc[k][0] += -(r[0] * dx + r[3] * dy + r[5] * dz) + r[6] * wv;
+          acc[k][1] += -(r[3] * dx + r[1] * dy + r[4] * dz) + r[7] * wv;
+          acc[k][2] += -(r[5] * dx + r[4] * dy + r[2] * dz) + r[8] * wv;
+        } else {
+          const float wm = wx * wy * wz * r[0];
+          if (MODE == 0) {
+            acc[k][0] += wm;
+            acc[k][1] += wm * r[1];
+            acc[k][2] += wm * r[2];
+            acc[k][3] += wm * r[3];
+          } else {
+            acc[k][0] += wm * r[1];
+            acc[k][1] += wm * r[2];
+            acc[k][2] += wm * r[3];
           }
         }
       }
     }
+    __syncwarp();
   }
-  tile_flush(tile, b.acc, b.NN);
-}
-
-// GridMomentumUpdate (update_step.f90:831-1013), particle side: internal
-// force -sigma vol grad N plus the staged external force times N
-__global__ void __launch_bounds__(kScatterBlock) kb_scatter_force(BState b) {
-  __shared__ Tile<3> tile;
-  tile_init(tile);
-  const long long i = btid();
-  int s, c[3];
-  float off[3];
-  if (scatter_particle(b, i, s, c, off)) {
-    const Scene& sc = b.scenes[s];
-    const long long NP = b.NP;
-    const float sf = q_scale(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
-    int t[3][4], nt[3];
-    float w[3][4], d[3][4];
-    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], w[a], d[a]);
-    const float idc = (float)sc.idcell;
-    const float sxx = b.fs[i], syy = b.fs[NP + i], szz = b.fs[2 * NP + i];
-    const float sxy = b.fs[3 * NP + i], syz = b.fs[4 * NP + i], sxz = b.fs[5 * NP + i];
-    const float e0 = b.fs[6 * NP + i], e1 = b.fs[7 * NP + i], e2 = b.fs[8 * NP + i];
-    for (int az = 0; az < nt[2]; ++az) {
-      const int jz = c[2] + t[2][az];
-      if (jz < 0 || jz >= sc.NGz) continue;
-      for (int ay = 0; ay < nt[1]; ++ay) {
-        const int jy = c[1] + t[1][ay];
-        if (jy < 0 || jy >= sc.NGy) continue;
-        for (int ax = 0; ax < nt[0]; ++ax) {
-          const int jx = c[0] + t[0][ax];
-          if (jx < 0 || jx >= sc.NGx) continue;
-          const float wv = w[0][ax] * w[1][ay] * w[2][az];
-          const float dx = d[0][ax] * w[1][ay] * w[2][az] * idc;
-          const float dy = w[0][ax] * d[1][ay] * w[2][az] * idc;
-          const float dz = w[0][ax] * w[1][ay] * d[2][az] * idc;
-          long long q[3];
-          q[0] = quant(-(sxx * dx + sxy * dy + sxz * dz) + e0 * wv, sf);
-          q[1] = quant(-(sxy * dx + syy * dy + syz * dz) + e1 * wv, sf);
-          q[2] = quant(-(sxz * dx + syz * dy + szz * dz) + e2 * wv, sf);
-          const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
-          tile_add<3>(tile, (int)n, q, b.acc, b.NN);
-        }
-      }
+  for (int k = 0; k < 2; ++k) {
+    if (!use[k]) continue;
+    const int jx = c[0] + to[k][0], jy = c[1] + to[k][1], jz = c[2] + to[k][2];
+    if (jx < 0 || jx >= sc.NGx || jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
+    const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
+    for (int v = 0; v < NV; ++v) {
+      const long long q = quant(acc[k][v], scale[v]);
+      if (q) atomicAdd(&b.acc[v * b.NN + n], (unsigned long long)q);
     }
   }
-  tile_flush(tile, b.acc, b.NN);
 }
 
 // accumulated channel v of node n in FP64 (and the accumulator cleared for
@@ -594,7 +552,12 @@ __global__ void kb_sg_centre_mass(BState b, int momentum_only) {
   int rem = (int)(lc - (long long)q[2] * sc.NCxy);
   q[1] = rem / sc.NCx;
   q[0] = rem - q[1] * sc.NCx;
-  double M = 0, P0 = 0, P1 = 0, P2 = 0;
+  // FP32 sums per dual cell, added in 64-bit fixed point (exact), as the
+  // particle -> node scatter does
+  const SceneState& st = b.sst[s];
+  const int shm = q_shift(sc, st.qmax[Q_MASS]), shp = q_shift(sc, st.qmax[momentum_only ? Q_MOM_MUSL : Q_MOM]);
+  const float sm = q_scale(shm), sp = q_scale(shp);
+  long long QM = 0, Q0 = 0, Q1 = 0, Q2 = 0;
   for (int k = 0; k < 8; ++k) {
     int i0, i1;
     if (!sg_dual_range(b, sc, q, k, i0, i1)) continue;
@@ -606,15 +569,16 @@ __global__ void kb_sg_centre_mass(BState b, int momentum_only) {
       p1 += wm * (float)b.v[NP + i];
       p2 += wm * (float)b.v[2 * NP + i];
     }
-    M += m;
-    P0 += p0;
-    P1 += p1;
-    P2 += p2;
+    QM += quant(m, sm);
+    Q0 += quant(p0, sp);
+    Q1 += quant(p1, sp);
+    Q2 += quant(p2, sp);
   }
-  if (!momentum_only) b.cmg[c] = M;
-  b.cpx[c] = P0;
-  b.cpx[NC + c] = P1;
-  b.cpx[2 * NC + c] = P2;
+  const double um = q_unit(shm), up = q_unit(shp);
+  if (!momentum_only) b.cmg[c] = (double)QM * um;
+  b.cpx[c] = (double)Q0 * up;
+  b.cpx[NC + c] = (double)Q1 * up;
+  b.cpx[2 * NC + c] = (double)Q2 * up;
 }
 
 // -------------------------------------------------------------- stress
@@ -648,9 +612,9 @@ __global__ void kb_stress(BState b, int usf_pass) {
       float w = 0.125f;
       for (int a = 0; a < 3; ++a) w *= oc[a] ? 1.f + xx[a] : 1.f - xx[a];
       const long long NC = b.NC;
-      for (int a = 0; a < 6; ++a) de[a] += (R)b.co[a * NC + c] * w;
-      for (int a = 0; a < 3; ++a) vort[a] += (R)b.cw[a * NC + c] * w;
-      for (int a = 0; a < 9; ++a) deFp[a / 3][a % 3] += w * (R)b.cdefp[a * NC + c];
+      for (int a = 0; a < 6; ++a) de[a] += b.co[a * NC + c] * w;
+      for (int a = 0; a < 3; ++a) vort[a] += b.cw[a * NC + c] * w;
+      for (int a = 0; a < 9; ++a) deFp[a / 3][a % 3] += w * b.cdefp[a * NC + c];
     }
   } else {
     const int cl = b.cell[i];
@@ -830,25 +794,23 @@ __global__ void kb_depeff_carry(BState b, int usf_pass) {
 // ------------------------------------------------------------ force input
 // external force (QuLo ramp, Damp, gravity; update_step.f90:889-903) and
 // sigma * vol, staged per particle in FP32 for the force gather
-__global__ void kb_force_prep(BState b) {
-  long long i = btid();
-  if (i >= b.NP) return;
+__device__ __forceinline__ float force_prep_one(BState& b, long long i) {
   const int s = b.scene[i];
-  if (!scene_live(b, s)) return;
+  if (!scene_live(b, s)) return -1.f;
   const Scene& sc = b.scenes[s];
   const SceneState& st = b.sst[s];
   const long long NP = b.NP;
-  double f[3];
-  for (int a = 0; a < 3; ++a) {
-    double fa = b.fxp[a * NP + i];
-    if (sc.qload && !(st.time >= sc.qload_time)) fa = fa / sc.qload_time * st.time;
-    f[a] = fa;
-  }
+  // external force in FP32 (the staged force is FP32): load ramp, mass
+  // damping, gravity
+  float f[3];
+  const float m = (float)b.mass[i];
+  const float ramp = (sc.qload && !(st.time >= sc.qload_time)) ? (float)(st.time / sc.qload_time) : 1.f;
+  for (int a = 0; a < 3; ++a) f[a] = (float)b.fxp[a * NP + i] * ramp;
   if (sc.qdamp)
-    for (int a = 0; a < 3; ++a) f[a] = f[a] - sc.damp_factor * b.mass[i] * b.v[a * NP + i];
+    for (int a = 0; a < 3; ++a) f[a] = f[a] - (float)sc.damp_factor * m * (float)b.v[a * NP + i];
   if (sc.gravity) {
     const DevBody& bd = b.bodies[b.body[i]];
-    for (int a = 0; a < 3; ++a) f[a] = f[a] + b.mass[i] * bd.gravp[a];
+    for (int a = 0; a < 3; ++a) f[a] = f[a] + m * (float)bd.gravp[a];
   }
   float vol = b.vol[i];
   float smq = b.sm[i] - b.q[i];
@@ -858,7 +820,21 @@ __global__ void kb_force_prep(BState b) {
   b.fs[3 * NP + i] = b.sd[3 * NP + i] * vol;
   b.fs[4 * NP + i] = b.sd[4 * NP + i] * vol;
   b.fs[5 * NP + i] = b.sd[5 * NP + i] * vol;
-  for (int a = 0; a < 3; ++a) b.fs[(6 + a) * NP + i] = (float)f[a];
+  for (int a = 0; a < 3; ++a) b.fs[(6 + a) * NP + i] = f[a];
+  // bound of one contribution: node force (|grad N| <= 1 / h per component,
+  // N <= 1), or for SGMP one centre-node channel (N times a staged value)
+  const float* fs = b.fs;
+  const float sig = fabsf(fs[i]) + fabsf(fs[NP + i]) + fabsf(fs[2 * NP + i]) +
+                    2.f * (fabsf(fs[3 * NP + i]) + fabsf(fs[4 * NP + i]) + fabsf(fs[5 * NP + i]));
+  const float gscale = sc.shape == 3 ? 1.f : (float)sc.idcell;
+  return (sig * gscale + fabsf(f[0]) + fabsf(f[1]) + fabsf(f[2])) * 1.0001f;
+}
+
+__global__ void kb_force_prep(BState b) {
+  const long long i = btid();
+  float bound = -1.f;
+  if (i < b.NP) bound = force_prep_one(b, i);
+  block_scene_max<1>(b, bound >= 0.f ? (int)b.scene[i] : -1, {Q_FORCE}, {fmaxf(bound, 0.f)});
 }
 
 // GridMomentumUpdate + IntegrateMomentum for one node
@@ -903,15 +879,17 @@ __global__ void kb_p2g_force(BState b) {
         for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
           if (cx < 0 || cx >= sc.NCx) continue;
           long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
-          int ox = j[0] - cx, oy = j[1] - cy, oz = j[2] - cz;
-          double dx = (ox ? 1.0 : -1.0) * sc.iJacobi4, dy = (oy ? 1.0 : -1.0) * sc.iJacobi4,
-                 dz = (oz ? 1.0 : -1.0) * sc.iJacobi4;
+          // the cell's contribution in FP32 (CNShape derivatives at the
+          // centre, +-1/(4 Jacobi)), accumulated in FP64
+          const int ox = j[0] - cx, oy = j[1] - cy, oz = j[2] - cz;
+          const float j4 = (float)sc.iJacobi4;
+          const float dx = ox ? j4 : -j4, dy = oy ? j4 : -j4, dz = oz ? j4 : -j4;
           const double* ci = b.cfint;
-          double c0 = ci[c], c1 = ci[NC + c], c2 = ci[2 * NC + c], c3 = ci[3 * NC + c], c4 = ci[4 * NC + c],
-                 c5 = ci[5 * NC + c];
-          F[0] += 0.125 * b.cfext[c] - (c0 * dx + c3 * dy + c5 * dz);
-          F[1] += 0.125 * b.cfext[NC + c] - (c3 * dx + c1 * dy + c4 * dz);
-          F[2] += 0.125 * b.cfext[2 * NC + c] - (c5 * dx + c4 * dy + c2 * dz);
+          const float c0 = (float)ci[c], c1 = (float)ci[NC + c], c2 = (float)ci[2 * NC + c],
+                      c3 = (float)ci[3 * NC + c], c4 = (float)ci[4 * NC + c], c5 = (float)ci[5 * NC + c];
+          F[0] += (double)(0.125f * (float)b.cfext[c] - (c0 * dx + c3 * dy + c5 * dz));
+          F[1] += (double)(0.125f * (float)b.cfext[NC + c] - (c3 * dx + c1 * dy + c4 * dz));
+          F[2] += (double)(0.125f * (float)b.cfext[2 * NC + c] - (c5 * dx + c4 * dy + c2 * dz));
         }
       }
     }
@@ -936,7 +914,9 @@ __global__ void kb_sg_centre_force(BState b) {
   int rem = (int)(lc - (long long)q[2] * sc.NCxy);
   q[1] = rem / sc.NCx;
   q[0] = rem - q[1] * sc.NCx;
-  double E[3] = {0, 0, 0}, I[6] = {0, 0, 0, 0, 0, 0};
+  const int sh = q_shift(sc, b.sst[s].qmax[Q_FORCE]);
+  const float sf = q_scale(sh);
+  long long E[3] = {0, 0, 0}, I[6] = {0, 0, 0, 0, 0, 0};
   for (int k = 0; k < 8; ++k) {
     int i0, i1;
     if (!sg_dual_range(b, sc, q, k, i0, i1)) continue;
@@ -946,12 +926,13 @@ __global__ void kb_sg_centre_force(BState b) {
       for (int a = 0; a < 3; ++a) e[a] += b.fs[(6 + a) * NP + i] * w;
       for (int a = 0; a < 6; ++a) t[a] += w * b.fs[a * NP + i];
     }
-    for (int a = 0; a < 3; ++a) E[a] += e[a];
-    for (int a = 0; a < 6; ++a) I[a] += t[a];
+    for (int a = 0; a < 3; ++a) E[a] += quant(e[a], sf);
+    for (int a = 0; a < 6; ++a) I[a] += quant(t[a], sf);
   }
-  for (int a = 0; a < 3; ++a) b.cfext[a * NC + c] = E[a];
+  const double u = q_unit(sh);
+  for (int a = 0; a < 3; ++a) b.cfext[a * NC + c] = (double)E[a] * u;
   // Cfint order of the reference: xx, yy, zz, xy, yz, xz
-  for (int a = 0; a < 6; ++a) b.cfint[a * NC + c] = I[a];
+  for (int a = 0; a < 6; ++a) b.cfint[a * NC + c] = (double)I[a] * u;
 }
 
 // SGMP: strain rate / spin at the centre nodes from the 8 cell nodes
@@ -1044,18 +1025,16 @@ __global__ void kb_sg_centre_velocity(BState b) {
 }
 
 // ---------------------------------------------------------- G2P position
-__global__ void kb_position(BState b) {
-  long long i = btid();
-  if (i >= b.NP) return;
+__device__ __forceinline__ float position_one(BState& b, long long i) {
   const int s = b.scene[i];
-  if (!scene_live(b, s)) return;
+  if (!scene_live(b, s)) return -1.f;
   const Scene& sc = b.scenes[s];
   const SceneState& st = b.sst[s];
   const long long NP = b.NP, NN = b.NN;
   float v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
   if (sc.shape == 3) {
     int d = b.dual[i];
-    if (d < 0) return;
+    if (d < 0) return -1.f;
     int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
     int ln = b.inode[i];
     int bd = ln >= 0 ? b.bd[sc.n0 + ln] : 0;
@@ -1077,13 +1056,13 @@ __global__ void kb_position(BState b) {
       float w = 0.125f;
       for (int a = 0; a < 3; ++a) w *= oc[a] ? 1.f + xx[a] : 1.f - xx[a];
       for (int a = 0; a < 3; ++a) {
-        v[a] += w * (float)b.cvx[a * NC + c];
-        acc[a] += w * (float)b.cax[a * NC + c];
+        v[a] += w * b.cvx[a * NC + c];
+        acc[a] += w * b.cax[a * NC + c];
       }
     }
   } else {
     const int cl = b.cell[i];
-    if (cl < 0) return;
+    if (cl < 0) return -1.f;
     int c[3];
     c[2] = cl / sc.NCxy;
     int rem = cl - c[2] * sc.NCxy;
@@ -1118,6 +1097,17 @@ __global__ void kb_position(BState b) {
     b.v[a * NP + i] = vv;
     if (sc.usf) b.x[a * NP + i] = xx;
   }
+  if (!sc.musl) return -1.f;
+  // bound of GridMomentumMUSL's contributions with the updated velocity
+  const float m = (float)b.mass[i];
+  return m * fmaxf(fabsf((float)b.v[i]), fmaxf(fabsf((float)b.v[NP + i]), fabsf((float)b.v[2 * NP + i]))) * 1.0001f;
+}
+
+__global__ void kb_position(BState b) {
+  const long long i = btid();
+  float bound = -1.f;
+  if (i < b.NP) bound = position_one(b, i);
+  block_scene_max<1>(b, bound >= 0.f ? (int)b.scene[i] : -1, {Q_MOM_MUSL}, {fmaxf(bound, 0.f)});
 }
 
 // GridMomentumMUSL: momentum re-map with the new particle velocities
