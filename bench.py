@@ -304,7 +304,17 @@ def run_serving(args, device: int) -> dict:
     dks = [m.Deck.parse(t) for t, _, _ in gen]
     nps = np.array([n for _, n, _ in gen], dtype=np.float64)
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=len(dks)))
-    with m.Server(device=device, chunk_steps=25, autotune=True) as srv:
+    out = {"fifo": serve_scenes(args, device, dks, nps, arrivals, "fifo", 0)}
+    if args.serve_cap > 0:
+        out["shortest_capped"] = serve_scenes(args, device, dks, nps, arrivals, "shortest", args.serve_cap)
+    return out
+
+
+def serve_scenes(args, device: int, dks, nps, arrivals, policy: str, cap: int) -> dict:
+    import numpy as np
+    import mpm3d_gb300 as m
+
+    with m.Server(device=device, chunk_steps=25, autotune=True, policy=policy, max_resident_particles=cap) as srv:
         tickets = []
         t0 = time.perf_counter()
         for k, d in enumerate(dks):
@@ -321,6 +331,7 @@ def run_serving(args, device: int) -> dict:
     queue = np.array([r["queue_ms"] for r in res])
     return {
         "scenes": len(dks), "steps_per_scene": args.serve_steps, "arrival_rate_per_s": args.serve_rate,
+        "policy": policy, "max_resident_particles": cap,
         "particles_min_max_mean": [int(nps.min()), int(nps.max()), float(nps.mean())],
         "p50_latency_ms": float(np.percentile(lat, 50)), "p99_latency_ms": float(np.percentile(lat, 99)),
         "mean_queue_ms": float(queue.mean()), "makespan_s": wall,
@@ -406,6 +417,8 @@ def main():
     ap.add_argument("--serve-scenes", type=int, default=256, help="serving workload scenes (0 = skip)")
     ap.add_argument("--serve-steps", type=int, default=500)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (scenes/s)")
+    ap.add_argument("--serve-cap", type=int, default=2_000_000,
+                    help="resident particle cap of the shortest-work-first serving run (0 = FIFO run only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -201,10 +201,18 @@ typedef struct mpm_server mpm_server;
 typedef struct mpm_serve_config {
   int device;               /* CUDA device, -1 = current                        */
   int chunk_steps;          /* steps between admission points (0 = 25)          */
-  int64_t hbm_budget_bytes; /* device bytes for resident scenes (0 = 80% of free) */
+  int64_t hbm_budget_bytes; /* sum of the resident scenes' mpm_scene_device_bytes
+                               (0 = 35% of free memory: a batch keeps two arenas) */
   int max_scenes;           /* resident scene cap (0 = 4096)                     */
   int autotune;             /* 1 = pick the batch launch shape on the first chunks */
+  int policy;               /* admission order: MPM_SERVE_FIFO or MPM_SERVE_SHORTEST */
+  int64_t max_resident_particles; /* admit while the resident particles stay below
+                                     this (0 = no cap; a lone scene is always admitted) */
 } mpm_serve_config;
+/* FIFO admits in submission order; SHORTEST admits the queued scene with the
+ * least work (particles x steps) first, which lowers the median latency when
+ * the offered load exceeds the device's rate. */
+enum mpm_serve_policy { MPM_SERVE_FIFO = 0, MPM_SERVE_SHORTEST = 1 };
 /* bit (1u << field) of field_mask snapshots particle field `field` (mpm_field
  * ids 1..25) when the scene finishes */
 #define MPM_SERVE_FIELD(f) (1u << (f))

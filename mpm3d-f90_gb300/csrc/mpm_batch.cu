@@ -100,7 +100,13 @@ struct mpm_batch {
   bool dirty = false;
   // current layout
   BState A{}, B{};
-  std::vector<void*> allocs;
+  // device arenas: the current layout's, and a spare one kept for the next
+  // re-layout (the relocation copies from one to the other), so that a new
+  // composition does not allocate when its layout fits the spare
+  char* arena = nullptr;
+  size_t arena_cap = 0;
+  char* spare = nullptr;
+  size_t spare_cap = 0;
   long long bytes = 0;
   int* d_target = nullptr;
   void* cub_tmp = nullptr;
@@ -132,26 +138,18 @@ int berr(mpm_batch* b, int code, const char* fmt, ...) {
     if (e__ != cudaSuccess) return berr(b, MPM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e__)); \
   } while (0)
 
+// Carves the arrays of one layout out of one device arena (256-byte aligned);
+// with a null base it only measures the arena size.
 struct Alloc {
-  std::vector<void*> ptrs;
-  long long bytes = 0;
-  bool fail = false;
+  char* base = nullptr;
+  size_t off = 0;
   template <class T>
   T* get(long long n) {
     if (n <= 0) n = 1;
-    void* p = nullptr;
-    if (cudaMalloc(&p, (size_t)n * sizeof(T)) != cudaSuccess) {
-      fail = true;
-      return nullptr;
-    }
-    ptrs.push_back(p);
-    bytes += n * (long long)sizeof(T);
-    return (T*)p;
-  }
-  void release() {
-    for (void* p : ptrs) cudaFree(p);
-    ptrs.clear();
-    bytes = 0;
+    off = (off + 255) & ~(size_t)255;
+    T* p = base ? (T*)(base + off) : nullptr;
+    off += (size_t)n * sizeof(T);
+    return p;
   }
 };
 
@@ -386,8 +384,10 @@ int commit(mpm_batch* b) {
   cudaStream_t st = b->stream;
   if (b->order.empty()) {
     drop_graph(b);
-    for (void* p : b->allocs) cudaFree(p);
-    b->allocs.clear();
+    if (b->arena) cudaFree(b->arena);
+    if (b->spare) cudaFree(b->spare);
+    b->arena = b->spare = nullptr;
+    b->arena_cap = b->spare_cap = 0;
     b->bytes = 0;
     b->A = BState{};
     b->B = BState{};
@@ -440,8 +440,24 @@ int commit(mpm_batch* b) {
   if (NP >= (1LL << 31) || NK >= (1LL << 31) || NN >= (1LL << 31))
     return berr(b, MPM_ERR_UNSUPPORTED, "batch too large for 32-bit indices");
   layout_flags(b);
-  Alloc al;
-  BState A{}, B{};
+  // CUB scratch sizes for this layout (size queries only)
+  size_t t1 = 0, t2 = 0, t3 = 0;
+  int bits = 1;
+  while ((1LL << bits) <= NK) ++bits;
+  cub::DeviceRadixSort::SortPairs(nullptr, t1, (unsigned*)nullptr, (unsigned*)nullptr, (int*)nullptr, (int*)nullptr,
+                                  (int)NP, 0, bits, st);
+  cub::DeviceScan::InclusiveSum(nullptr, t2, (int*)nullptr, (int*)nullptr, (int)NK, st);
+  if (b->any_jc) cub::DeviceScan::InclusiveScan(nullptr, t3, (int*)nullptr, (int*)nullptr, MaxOpB(), (int)NP, st);
+  const size_t tb = std::max(t1, std::max(t2, t3));
+  BState A{}, B{}, shared{};
+  int* d_target = nullptr;
+  int* d_map = nullptr;
+  uint16_t *d_smap = nullptr, *d_bmap = nullptr;
+  void* tmp = nullptr;
+  auto carve = [&](Alloc& al) {
+  A = BState{};
+  B = BState{};
+  shared = BState{};
   A.NP = B.NP = NP;
   A.NN = B.NN = NN;
   A.NK = B.NK = NK;
@@ -453,7 +469,6 @@ int commit(mpm_batch* b) {
   A.any_jc = B.any_jc = b->any_jc;
   alloc_particles(al, A, NP, b->any_uvfp);
   alloc_particles(al, B, NP, b->any_uvfp);
-  BState shared{};
   shared.cell = al.get<int>(NP);
   shared.dual = al.get<int>(NP);
   shared.inode = al.get<int>(NP);
@@ -498,14 +513,34 @@ int commit(mpm_batch* b) {
   shared.sst = al.get<SceneState>((long long)b->order.size());
   shared.mats = al.get<DevMaterial>(nmat);
   shared.bodies = al.get<DevBody>(nbody);
-  int* d_target = al.get<int>((long long)b->order.size());
-  int* d_map = al.get<int>(NP);
-  uint16_t* d_smap = al.get<uint16_t>(b->A.nscene + 1);
-  uint16_t* d_bmap = al.get<uint16_t>(65536);
-  if (al.fail) {
-    al.release();
-    return berr(b, MPM_ERR_OOM, "device memory for a batch of %lld particles", NP);
+  d_target = al.get<int>((long long)b->order.size());
+  d_map = al.get<int>(NP);
+  d_smap = al.get<uint16_t>(b->A.nscene + 1);
+  d_bmap = al.get<uint16_t>(65536);
+  tmp = al.get<char>((long long)tb);
+  };
+  Alloc measure;
+  carve(measure);
+  const size_t need = measure.off + 256;
+  // reuse the spare arena when the layout fits it (and it is not far larger)
+  if (b->spare && (b->spare_cap < need || b->spare_cap > 3 * need)) {
+    cudaFree(b->spare);
+    b->spare = nullptr;
+    b->spare_cap = 0;
   }
+  if (!b->spare) {
+    const size_t cap = need + need / 4;
+    void* p = nullptr;
+    if (cudaMalloc(&p, cap) != cudaSuccess) {
+      cudaGetLastError();
+      return berr(b, MPM_ERR_OOM, "device memory for a batch of %lld particles (%zu bytes)", NP, cap);
+    }
+    b->spare = (char*)p;
+    b->spare_cap = cap;
+  }
+  Alloc al;
+  al.base = b->spare;
+  carve(al);
   auto share = [&](BState& s) {
     s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
     s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
@@ -614,34 +649,18 @@ int commit(mpm_batch* b) {
   for (HostScene* h : b->order)
     if (!h->resident) {
       int r = upload_scene_particles(b, h, A);
-      if (r) {
-        al.release();
-        return r;
-      }
+      if (r) return r;
     }
-  // CUB scratch for this layout
-  size_t t1 = 0, t2 = 0, t3 = 0;
-  int bits = 1;
-  while ((1LL << bits) <= NK) ++bits;
-  cub::DeviceRadixSort::SortPairs(nullptr, t1, A.key, A.key_sorted, A.val, A.perm, (int)NP, 0, bits, st);
-  cub::DeviceScan::InclusiveSum(nullptr, t2, A.seg, A.seg, (int)NK, st);
-  if (b->any_jc) cub::DeviceScan::InclusiveScan(nullptr, t3, A.setter, A.setter_scan, MaxOpB(), (int)NP, st);
-  size_t tb = std::max(t1, std::max(t2, t3));
-  void* tmp = al.get<char>((long long)tb);
-  if (al.fail) {
-    al.release();
-    return berr(b, MPM_ERR_OOM, "device memory for the sort scratch");
-  }
   // calcEnergy of the new scenes (MPM3D.f90:42)
   kb_reduce_chunks<<<(unsigned)NR, 256, 0, st>>>(A);
   kb_reduce_scenes<<<(unsigned)A.nscene, 256, 0, st>>>(A, 1);
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(st));
-  // swap in the new layout
+  // swap in the new layout: its arena becomes current, the old one spare
   drop_graph(b);
-  for (void* p : b->allocs) cudaFree(p);
-  b->allocs = al.ptrs;
-  b->bytes = al.bytes;
+  std::swap(b->arena, b->spare);
+  std::swap(b->arena_cap, b->spare_cap);
+  b->bytes = (long long)(b->arena_cap + b->spare_cap);
   b->A = A;
   b->B = B;
   b->set0_x = A.x;
@@ -690,7 +709,8 @@ void mpm_batch_destroy(mpm_batch* b) {
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  for (void* p : b->allocs) cudaFree(p);
+  if (b->arena) cudaFree(b->arena);
+  if (b->spare) cudaFree(b->spare);
   for (auto& kv : b->by_id) delete kv.second;
   prof_free(&b->prof);
   cudaStreamDestroy(b->stream);

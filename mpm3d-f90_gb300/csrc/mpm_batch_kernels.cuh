@@ -527,15 +527,30 @@ __device__ __forceinline__ float sg_corner_weight(const BState& b, long long i, 
 }
 
 // particle key range of the dual cell q - kCorner[k] (empty if it does not exist)
-__device__ __forceinline__ bool sg_dual_range(const BState& b, const Scene& sc, const int q[3], int k, int& i0,
+// Corner k of the dual cell (dx, dy, dz) as a scene cell, with the
+// reference's flat arithmetic (CenterCellNode, Grid.f90:380-418: first corner
+// plus the corner's flat offset; corners at or past the last cell are
+// dropped, and a direction with a single cell -- one dual cell -- spills into
+// the next row); -1 if dropped.
+__device__ __forceinline__ long long sg_corner_cell(const Scene& sc, int dx, int dy, int dz, int k) {
+  const long long c1 = ((long long)dz * sc.NCy + dy) * sc.NCx + dx;
+  const long long cid = c1 + kCorner[k][0] + (long long)kCorner[k][1] * sc.NCx + (long long)kCorner[k][2] * sc.NCxy;
+  return cid < (long long)sc.NCxy * sc.NCz ? cid : -1;
+}
+
+// particle range of the dual cell whose corner k is the centre node (cell)
+// cq, inverting sg_corner_cell: first corner t = cq - corner offset, which
+// must be a dual cell's first corner (t's per-direction indices within the
+// dual grid); false if there is none or it holds no particle
+__device__ __forceinline__ bool sg_dual_range(const BState& b, const Scene& sc, long long cq, int k, int& i0,
                                               int& i1) {
-  int d[3];
-  const int CN[3] = {sc.CNCx, sc.CNCy, sc.CNCz};
-  for (int a = 0; a < 3; ++a) {
-    d[a] = q[a] - kCorner[k][a];
-    if (d[a] < 0 || d[a] >= CN[a]) return false;
-  }
-  key_range(b, sc.k0 + ((long long)d[2] * sc.CNCy + d[1]) * sc.CNCx + d[0], i0, i1);
+  const long long t = cq - kCorner[k][0] - (long long)kCorner[k][1] * sc.NCx - (long long)kCorner[k][2] * sc.NCxy;
+  if (t < 0) return false;
+  const int tz = (int)(t / sc.NCxy);
+  const int rem = (int)(t - (long long)tz * sc.NCxy);
+  const int ty = rem / sc.NCx, tx = rem - ty * sc.NCx;
+  if (tx >= sc.CNCx || ty >= sc.CNCy || tz >= sc.CNCz) return false;
+  key_range(b, sc.k0 + ((long long)tz * sc.CNCy + ty) * sc.CNCx + tx, i0, i1);
   return i0 < i1;
 }
 
@@ -560,7 +575,7 @@ __global__ void kb_sg_centre_mass(BState b, int momentum_only) {
   long long QM = 0, Q0 = 0, Q1 = 0, Q2 = 0;
   for (int k = 0; k < 8; ++k) {
     int i0, i1;
-    if (!sg_dual_range(b, sc, q, k, i0, i1)) continue;
+    if (!sg_dual_range(b, sc, lc, k, i0, i1)) continue;
     float m = 0, p0 = 0, p1 = 0, p2 = 0;
     for (int i = i0; i < i1; ++i) {
       float wm = sg_corner_weight(b, i, k) * (float)b.mass[i];
@@ -608,7 +623,9 @@ __global__ void kb_stress(BState b, int usf_pass) {
     float xx[3] = {b.xxn[i], b.xxn[NP + i], b.xxn[2 * NP + i]};
     for (int k = 0; k < 8; ++k) {
       int oc[3] = {kCorner[k][0], kCorner[k][1], kCorner[k][2]};
-      long long c = sc.c0 + ((dz + oc[2]) * sc.NCy + (dy + oc[1])) * sc.NCx + (dx + oc[0]);
+      const long long cid = sg_corner_cell(sc, dx, dy, dz, k);
+      if (cid < 0) continue;
+      const long long c = sc.c0 + cid;
       float w = 0.125f;
       for (int a = 0; a < 3; ++a) w *= oc[a] ? 1.f + xx[a] : 1.f - xx[a];
       const long long NC = b.NC;
@@ -919,7 +936,7 @@ __global__ void kb_sg_centre_force(BState b) {
   long long E[3] = {0, 0, 0}, I[6] = {0, 0, 0, 0, 0, 0};
   for (int k = 0; k < 8; ++k) {
     int i0, i1;
-    if (!sg_dual_range(b, sc, q, k, i0, i1)) continue;
+    if (!sg_dual_range(b, sc, lc, k, i0, i1)) continue;
     float e[3] = {0, 0, 0}, t[6] = {0, 0, 0, 0, 0, 0};
     for (int i = i0; i < i1; ++i) {
       float w = sg_corner_weight(b, i, k);
@@ -1052,7 +1069,9 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
     const long long NC = b.NC;
     for (int k = 0; k < 8; ++k) {
       int oc[3] = {kCorner[k][0], kCorner[k][1], kCorner[k][2]};
-      long long c = sc.c0 + ((dz + oc[2]) * sc.NCy + (dy + oc[1])) * sc.NCx + (dx + oc[0]);
+      const long long cid = sg_corner_cell(sc, dx, dy, dz, k);
+      if (cid < 0) continue;
+      const long long c = sc.c0 + cid;
       float w = 0.125f;
       for (int a = 0; a < 3; ++a) w *= oc[a] ? 1.f + xx[a] : 1.f - xx[a];
       for (int a = 0; a < 3; ++a) {

@@ -6,8 +6,9 @@
 // scene (deck -> host set-up and input copy) runs on the client thread.
 //
 // Server loop:
-//   1. admit queued scenes first-come first-served while the estimated device
-//      bytes of the resident scenes stay within the budget;
+//   1. admit queued scenes -- in submission order, or least work first --
+//      while the estimated device bytes of the resident scenes stay within the
+//      budget (and their particles within the optional cap);
 //   2. run min(chunk_steps, steps until the next scene finishes) steps of the
 //      batch (graph replays; the batch recaptures after a composition change);
 //   3. read every resident scene's progress in one copy, snapshot the fields
@@ -79,7 +80,7 @@ struct mpm_server {
   std::map<int64_t, Ticket*> tickets;
   std::map<int, int64_t> by_scene;  // resident scene id -> ticket
   int64_t next_ticket = 1;
-  long long resident_bytes = 0, peak_bytes = 0;
+  long long resident_bytes = 0, peak_bytes = 0, resident_particles = 0;
   // statistics
   long long submitted = 0, finished = 0, chunks = 0;
   double particle_steps = 0, busy_ms = 0;
@@ -116,6 +117,7 @@ void fail_resident(mpm_server* s, int code, const std::string& msg) {
   }
   s->by_scene.clear();
   s->resident_bytes = 0;
+  s->resident_particles = 0;
 }
 
 void serve_loop(mpm_server* s) {
@@ -129,8 +131,19 @@ void serve_loop(mpm_server* s) {
       for (;;) {
         if (s->stop) return;
         while (!s->queue.empty()) {
-          Ticket* t = s->tickets[s->queue.front()];
+          // next candidate: the oldest, or the one with the least work
+          auto pick = s->queue.begin();
+          if (s->cfg.policy == MPM_SERVE_SHORTEST)
+            for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+              const Ticket* a = s->tickets[*it];
+              const Ticket* bst = s->tickets[*pick];
+              if ((double)a->np * a->steps < (double)bst->np * bst->steps) pick = it;
+            }
+          Ticket* t = s->tickets[*pick];
           if ((int)s->by_scene.size() >= s->cfg.max_scenes) break;
+          if (s->cfg.max_resident_particles > 0 && !s->by_scene.empty() &&
+              s->resident_particles + t->np > s->cfg.max_resident_particles)
+            break;
           if (s->resident_bytes + t->bytes > s->cfg.hbm_budget_bytes) {
             if (s->by_scene.empty()) {  // can never fit: fail it rather than block the queue
               t->state = T_FAILED;
@@ -139,7 +152,7 @@ void serve_loop(mpm_server* s) {
               t->t_done = Clock::now();
               delete t->scene;
               t->scene = nullptr;
-              s->queue.pop_front();
+              s->queue.erase(pick);
               s->cv_done.notify_all();
               continue;
             }
@@ -153,8 +166,9 @@ void serve_loop(mpm_server* s) {
           t->t_admit = Clock::now();
           s->by_scene[id] = t->id;
           s->resident_bytes += t->bytes;
+          s->resident_particles += t->np;
           s->peak_bytes = std::max(s->peak_bytes, s->resident_bytes);
-          s->queue.pop_front();
+          s->queue.erase(pick);
         }
         if (!s->by_scene.empty()) break;
         s->cv_work.wait(lk);
@@ -233,6 +247,7 @@ void serve_loop(mpm_server* s) {
           t->t_done = now;
           s->by_scene.erase(t->scene_id);
           s->resident_bytes -= t->bytes;
+          s->resident_particles -= t->np;
           s->finished++;
         }
       } else {
@@ -274,7 +289,9 @@ int mpm_serve_create(const mpm_serve_config* cfg, mpm_server** out) {
     size_t fr = 0, tot = 0;
     cudaSetDevice(s->cfg.device);
     cudaMemGetInfo(&fr, &tot);
-    s->cfg.hbm_budget_bytes = (int64_t)(0.8 * (double)fr);
+    // resident scenes' estimates; the batch holds two arenas of the layout
+    // (current and spare, with headroom), so about 2.5x this is in use
+    s->cfg.hbm_budget_bytes = (int64_t)(0.35 * (double)fr);
   }
   if (s->cfg.autotune) {
     const int cand[3] = {128, 256, 512};

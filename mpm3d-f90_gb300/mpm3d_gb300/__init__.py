@@ -472,7 +472,11 @@ class Batch:
 
 class _ServeConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("chunk_steps", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_int64),
-                ("max_scenes", ctypes.c_int), ("autotune", ctypes.c_int)]
+                ("max_scenes", ctypes.c_int), ("autotune", ctypes.c_int), ("policy", ctypes.c_int),
+                ("max_resident_particles", ctypes.c_int64)]
+
+
+SERVE_POLICY = {"fifo": 0, "shortest": 1}
 
 
 SERVE_STATS = ("submitted", "finished", "queued", "resident", "chunks", "particle_steps", "busy_ms",
@@ -485,9 +489,11 @@ class Server:
     chunks of steps and retired when they reach their step count."""
 
     def __init__(self, device: int = -1, chunk_steps: int = 25, hbm_budget_bytes: int = 0,
-                 max_scenes: int = 0, autotune: bool = False):
+                 max_scenes: int = 0, autotune: bool = False, policy: str = "fifo",
+                 max_resident_particles: int = 0):
         lib = library()
-        cfg = _ServeConfig(device, chunk_steps, hbm_budget_bytes, max_scenes, int(bool(autotune)))
+        cfg = _ServeConfig(device, chunk_steps, hbm_budget_bytes, max_scenes, int(bool(autotune)),
+                           SERVE_POLICY[policy], max_resident_particles)
         h = ctypes.c_void_p()
         st = lib.mpm_serve_create(ctypes.byref(cfg), ctypes.byref(h))
         if st:

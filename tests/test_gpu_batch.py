@@ -173,3 +173,22 @@ def test_serving_budget_admission(built):
         for t in ts:
             assert srv.wait(t, 60000)
         assert srv.stats()["peak_resident_bytes"] <= budget
+
+
+def test_serving_shortest_first(built):
+    """With one scene resident at a time, the shortest-work-first policy runs
+    the small queued scenes before a larger one submitted earlier."""
+    from mpm3d_gb300 import Deck, Server, decks
+    rng = np.random.default_rng(9)
+    first = Deck.parse(decks.serving_scene(rng, 20000, 20001, kind="beam")[0])
+    big = Deck.parse(decks.serving_scene(rng, 30000, 30001, kind="beam")[0])
+    small = [Deck.parse(decks.serving_scene(rng, 2000, 2001, kind="beam")[0]) for _ in range(2)]
+    with Server(chunk_steps=10, policy="shortest", max_resident_particles=1) as srv:
+        t0 = srv.submit(first, 300)
+        tb = srv.submit(big, 20)
+        ts = [srv.submit(d, 20) for d in small]
+        for t in [t0, tb] + ts:
+            assert srv.wait(t, 120000)
+        done_big = srv.result(tb)["latency_ms"]
+        for t in ts:
+            assert srv.result(t)["latency_ms"] < done_big
