@@ -142,23 +142,44 @@ def kernel_bytes(kernel: str, np_: int, nn_active: float, usf: bool = True) -> f
     once, at their stored widths (FP64 position, velocity, mass, energy, grid;
     FP32 stress state). Sort keys, permutation and per-step scratch are
     implementation overhead and are not counted."""
+    if kernel == "p2g_mass_scatter":
+        # read x, mass, v; add node mass + momentum
+        return np_ * (24 + 8 + 24) + nn_active * 32
+    if kernel == "p2g_force_scatter":
+        # read x, sigma * vol (6), external force (3); add node force
+        return np_ * (24 + 36) + nn_active * 24
     if kernel == "p2g_mass":
-        # read x, mass, v; write node mass + momentum (+ velocity under USF)
-        return np_ * (24 + 8 + 24) + nn_active * (32 + (24 if usf else 0))
+        # node finalize: node mass + momentum written (+ velocity under USF)
+        return nn_active * (32 + (12 if usf else 0))
     if kernel == "p2g_force_integrate":
-        # read sigma (SM, SD), vol, q, FXp, mass; node: read mass + momentum,
-        # write force, momentum, velocity, acceleration
-        return np_ * (4 * 7 + 4 + 4 + 24 + 8) + nn_active * (32 + 96)
+        # node finalize: read mass + momentum, write force, momentum, velocity, acceleration
+        return nn_active * (32 + 24 + 24 + 24)
     if kernel == "stress_update":
         # read x, vol, SM, SD, q, ie, cp, epeff, sig_y; write vol, SM, SD, q,
-        # ie, seqv, epeff; node velocity + mass read once
-        return np_ * (24 + 4 * 13 + 8) + np_ * (4 * 11 + 8) + nn_active * 32
+        # ie, seqv, epeff; node velocity read once
+        return np_ * (24 + 4 * 13 + 8) + np_ * (4 * 11 + 8) + nn_active * 12
     if kernel == "g2p_position":
-        # read x, v; write x, v; node mass, velocity, acceleration read once
-        return np_ * 96 + nn_active * 56
+        # read x, v; write x, v; node velocity and acceleration read once
+        return np_ * 96 + nn_active * 24
     if kernel == "permute":
         return np_ * 2 * (6 * 8 + 6 * 8 + 16 * 4 + 1 + 2 + 2 + 4)
     return np_ * 100.0
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch (dram__bytes_read + write) of a step category,
+    as recorded from one ncu capture in profiles/ ('traffic_bytes: <name> <bytes>'
+    lines); None if not recorded."""
+    import glob
+    import re
+
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for line in f:
+                m = re.match(r"traffic_bytes:\s+(\S+)\s+([0-9.eE+]+)", line.strip())
+                if m and m.group(1) == kernel:
+                    return float(m.group(2))
+    return None
 
 
 def run_ours(args) -> dict:
@@ -271,7 +292,8 @@ def run_ours(args) -> dict:
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                     "traffic": None, "avg_launch_ms": dom["avg_ms"]},
+                     "traffic": profiled_traffic(dom["kernel"]), "algorithmic_bytes": kb,
+                     "avg_launch_ms": dom["avg_ms"]},
         "step_alg_gbs": mixed["alg_bytes_step"] / (mixed["ms"] / args.steps / 1e3) / 1e9,
         "kernels_mixed": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in mixed["kernels"] if k["launches"]},
         "kernels_fp64": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in fp64["kernels"] if k["launches"]},

@@ -236,6 +236,16 @@ int mpm_serve_release(mpm_server* s, int64_t ticket);
 int mpm_serve_stats(mpm_server* s, double* out10);
 /* block until no scene is queued or resident (or timeout_ms passes) */
 int mpm_serve_drain(mpm_server* s, int timeout_ms);
+/* The server's admission decision as a pure host function (no device needed;
+ * also a capacity-planning aid). Queued scenes in submission order: particle
+ * counts np, step counts, device-byte estimates (mpm_scene_device_bytes);
+ * resident totals. Writes the queue positions admitted now, in admission
+ * order, into admit and returns their count; writes into reject (count in
+ * *nreject) the scenes that can never run (over the byte budget with nothing
+ * resident). A budget of 0 is unlimited here. Negative return: -mpm_status. */
+int mpm_serve_plan(const mpm_serve_config* cfg, int nqueued, const int64_t* np, const int* steps,
+                   const int64_t* bytes, int resident_scenes, int64_t resident_particles, int64_t resident_bytes,
+                   int* admit, int* reject, int* nreject);
 
 /* ------------------------------------------------ allocation-free call */
 /* No counterpart in the reference: an extra entry point for hosts that may not

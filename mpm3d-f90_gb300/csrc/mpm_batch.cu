@@ -282,11 +282,13 @@ int enqueue_step(mpm_batch* b) {
   std::swap(b->A, b->B);
   BState& s = b->A;
   const bool scatter = b->any_nonsgmp;
+  if (scatter) {
+    prof_begin(K_SCATTER_MASS, st);
+    kb_cell_scatter<0><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
+    prof_end(K_SCATTER_MASS, st);
+  }
   prof_begin(K_P2G_MASS, st);
   if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
-  if (scatter) {
-    kb_cell_scatter<0><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
-  }
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
   prof_end(K_P2G_MASS, st);
   auto stress = [&](int usf_pass) -> int {
@@ -310,11 +312,13 @@ int enqueue_step(mpm_batch* b) {
   prof_begin(K_FORCE_PREP, st);
   kb_force_prep<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_FORCE_PREP, st);
+  if (scatter) {
+    prof_begin(K_SCATTER_FORCE, st);
+    kb_cell_scatter<2><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
+    prof_end(K_SCATTER_FORCE, st);
+  }
   prof_begin(K_P2G_FORCE, st);
   if (b->any_sgmp) kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
-  if (scatter) {
-    kb_cell_scatter<2><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
-  }
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
   prof_end(K_P2G_FORCE, st);
   prof_begin(K_POSITION, st);
@@ -322,11 +326,13 @@ int enqueue_step(mpm_batch* b) {
   kb_position<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_POSITION, st);
   if (b->any_musl) {
+    if (scatter) {
+      prof_begin(K_SCATTER_MOM, st);
+      kb_cell_scatter<1><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
+      prof_end(K_SCATTER_MOM, st);
+    }
     prof_begin(K_P2G_MOM, st);
     if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
-    if (scatter) {
-      kb_cell_scatter<1><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
-    }
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
     prof_end(K_P2G_MOM, st);
   }

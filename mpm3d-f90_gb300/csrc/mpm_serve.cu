@@ -120,6 +120,47 @@ void fail_resident(mpm_server* s, int code, const std::string& msg) {
   s->resident_particles = 0;
 }
 
+// The admission decision (see mpm_serve_plan). Candidates are taken in
+// submission order (FIFO) or least work (particles x steps, ties by
+// submission order) first; admission stops at the first candidate that does
+// not fit the scene cap, the particle cap (a lone scene is always admitted)
+// or the byte budget. With nothing resident, a candidate over the byte budget
+// can never run: it is rejected and the next one is tried.
+int serve_plan(const mpm_serve_config& cfg, int n, const int64_t* np, const int* steps, const int64_t* bytes,
+               int rs, int64_t rp, int64_t rb, int* admit, int* reject, int* nreject) {
+  std::vector<char> taken((size_t)n, 0);
+  int na = 0, nr = 0;
+  const int max_scenes = cfg.max_scenes > 0 ? cfg.max_scenes : 4096;
+  for (;;) {
+    int pick = -1;
+    for (int k = 0; k < n; ++k) {
+      if (taken[k]) continue;
+      if (pick < 0) {
+        pick = k;
+        if (cfg.policy != MPM_SERVE_SHORTEST) break;
+        continue;
+      }
+      if ((double)np[k] * steps[k] < (double)np[pick] * steps[pick]) pick = k;
+    }
+    if (pick < 0) break;
+    if (rs >= max_scenes) break;
+    if (cfg.max_resident_particles > 0 && rs > 0 && rp + np[pick] > cfg.max_resident_particles) break;
+    if (cfg.hbm_budget_bytes > 0 && rb + bytes[pick] > cfg.hbm_budget_bytes) {
+      if (rs > 0) break;
+      taken[pick] = 1;
+      reject[nr++] = pick;
+      continue;
+    }
+    taken[pick] = 1;
+    admit[na++] = pick;
+    rs += 1;
+    rp += np[pick];
+    rb += bytes[pick];
+  }
+  *nreject = nr;
+  return na;
+}
+
 void serve_loop(mpm_server* s) {
   cudaSetDevice(s->cfg.device);
   std::vector<BatchProgress> prog;
@@ -130,45 +171,51 @@ void serve_loop(mpm_server* s) {
       std::unique_lock<std::mutex> lk(s->mu);
       for (;;) {
         if (s->stop) return;
-        while (!s->queue.empty()) {
-          // next candidate: the oldest, or the one with the least work
-          auto pick = s->queue.begin();
-          if (s->cfg.policy == MPM_SERVE_SHORTEST)
-            for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
-              const Ticket* a = s->tickets[*it];
-              const Ticket* bst = s->tickets[*pick];
-              if ((double)a->np * a->steps < (double)bst->np * bst->steps) pick = it;
-            }
-          Ticket* t = s->tickets[*pick];
-          if ((int)s->by_scene.size() >= s->cfg.max_scenes) break;
-          if (s->cfg.max_resident_particles > 0 && !s->by_scene.empty() &&
-              s->resident_particles + t->np > s->cfg.max_resident_particles)
-            break;
-          if (s->resident_bytes + t->bytes > s->cfg.hbm_budget_bytes) {
-            if (s->by_scene.empty()) {  // can never fit: fail it rather than block the queue
-              t->state = T_FAILED;
-              t->code = MPM_ERR_OOM;
-              t->err = "scene needs more device memory than the serving budget";
-              t->t_done = Clock::now();
-              delete t->scene;
-              t->scene = nullptr;
-              s->queue.erase(pick);
-              s->cv_done.notify_all();
-              continue;
-            }
-            break;
+        if (!s->queue.empty()) {
+          const int nq = (int)s->queue.size();
+          std::vector<int64_t> qnp(nq), qbytes(nq);
+          std::vector<int> qsteps(nq), admit(nq), reject(nq);
+          std::vector<int64_t> ids(s->queue.begin(), s->queue.end());
+          for (int k = 0; k < nq; ++k) {
+            const Ticket* t = s->tickets[ids[k]];
+            qnp[k] = t->np;
+            qsteps[k] = t->steps;
+            qbytes[k] = t->bytes;
           }
-          int id = -1;
-          mpm::batch_insert(s->batch, t->scene, &id);
-          t->scene = nullptr;  // the batch owns it now
-          t->scene_id = id;
-          t->state = T_RESIDENT;
-          t->t_admit = Clock::now();
-          s->by_scene[id] = t->id;
-          s->resident_bytes += t->bytes;
-          s->resident_particles += t->np;
-          s->peak_bytes = std::max(s->peak_bytes, s->resident_bytes);
-          s->queue.erase(pick);
+          int nrej = 0;
+          const int nadm = serve_plan(s->cfg, nq, qnp.data(), qsteps.data(), qbytes.data(), (int)s->by_scene.size(),
+                                      s->resident_particles, s->resident_bytes, admit.data(), reject.data(), &nrej);
+          for (int k = 0; k < nrej; ++k) {  // can never fit: fail them rather than block the queue
+            Ticket* t = s->tickets[ids[reject[k]]];
+            t->state = T_FAILED;
+            t->code = MPM_ERR_OOM;
+            t->err = "scene needs more device memory than the serving budget";
+            t->t_done = Clock::now();
+            delete t->scene;
+            t->scene = nullptr;
+          }
+          for (int k = 0; k < nadm; ++k) {
+            Ticket* t = s->tickets[ids[admit[k]]];
+            int id = -1;
+            mpm::batch_insert(s->batch, t->scene, &id);
+            t->scene = nullptr;  // the batch owns it now
+            t->scene_id = id;
+            t->state = T_RESIDENT;
+            t->t_admit = Clock::now();
+            s->by_scene[id] = t->id;
+            s->resident_bytes += t->bytes;
+            s->resident_particles += t->np;
+            s->peak_bytes = std::max(s->peak_bytes, s->resident_bytes);
+          }
+          if (nadm || nrej) {
+            std::vector<char> gone(nq, 0);
+            for (int k = 0; k < nadm; ++k) gone[admit[k]] = 1;
+            for (int k = 0; k < nrej; ++k) gone[reject[k]] = 1;
+            s->queue.clear();
+            for (int k = 0; k < nq; ++k)
+              if (!gone[k]) s->queue.push_back(ids[k]);
+            if (nrej) s->cv_done.notify_all();
+          }
         }
         if (!s->by_scene.empty()) break;
         s->cv_work.wait(lk);
@@ -426,6 +473,15 @@ int mpm_serve_stats(mpm_server* s, double* o) {
   o[8] = s->nb;
   o[9] = (double)s->peak_bytes;
   return MPM_OK;
+}
+
+int mpm_serve_plan(const mpm_serve_config* cfg, int nqueued, const int64_t* np, const int* steps,
+                   const int64_t* bytes, int resident_scenes, int64_t resident_particles, int64_t resident_bytes,
+                   int* admit, int* reject, int* nreject) {
+  if (!cfg || nqueued < 0 || (nqueued > 0 && (!np || !steps || !bytes || !admit || !reject)) || !nreject)
+    return -MPM_ERR_ARG;
+  return serve_plan(*cfg, nqueued, np, steps, bytes, resident_scenes, resident_particles, resident_bytes, admit,
+                    reject, nreject);
 }
 
 int mpm_serve_drain(mpm_server* s, int timeout_ms) {

@@ -136,6 +136,7 @@ def library() -> ctypes.CDLL:
         "mpm_serve_release": (i, [vp, i64]),
         "mpm_serve_stats": (i, [vp, P(d)]),
         "mpm_serve_drain": (i, [vp, i]),
+        "mpm_serve_plan": (i, [vp, i, P(i64), P(i), P(i64), i, i64, i64, P(i), P(i), P(i)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -483,6 +484,25 @@ SERVE_STATS = ("submitted", "finished", "queued", "resident", "chunks", "particl
                "particle_block", "node_block", "peak_resident_bytes")
 
 
+def serve_plan(np_, steps, bytes_, policy: str = "fifo", budget: int = 0, max_resident_particles: int = 0,
+               max_scenes: int = 0, resident=(0, 0, 0)):
+    """The serving runtime's admission decision for a queue (host only): returns
+    (admitted queue positions in admission order, rejected positions)."""
+    n = len(np_)
+    cfg = _ServeConfig(-1, 0, int(budget), int(max_scenes), 0, SERVE_POLICY[policy], int(max_resident_particles))
+    a_np = (ctypes.c_int64 * max(1, n))(*[int(x) for x in np_])
+    a_st = (ctypes.c_int * max(1, n))(*[int(x) for x in steps])
+    a_by = (ctypes.c_int64 * max(1, n))(*[int(x) for x in bytes_])
+    adm = (ctypes.c_int * max(1, n))()
+    rej = (ctypes.c_int * max(1, n))()
+    nrej = ctypes.c_int()
+    na = library().mpm_serve_plan(ctypes.byref(cfg), n, a_np, a_st, a_by, int(resident[0]), int(resident[1]),
+                                  int(resident[2]), adm, rej, ctypes.byref(nrej))
+    if na < 0:
+        raise MpmError(-na, "mpm_serve_plan")
+    return list(adm[:na]), list(rej[:nrej.value])
+
+
 class Server:
     """Serving runtime: scenes submitted from any thread are admitted into one
     device-resident batch while they fit the device-memory budget, advanced in
@@ -571,5 +591,5 @@ class Server:
         return True
 
 
-__all__ = ["Deck", "MpmStep", "Batch", "Server", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
+__all__ = ["Deck", "MpmStep", "Batch", "Server", "serve_plan", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
            "LIB_PATH"]
