@@ -46,6 +46,8 @@ WORKLOADS = {
     "soil_slope": ("soil slope 20 m 45 deg, 0.1 m spacing, GIMP, Drucker-Prager, USF",),
     "taylor_bar": ("Taylor bar R 3.2 mm L 32.4 mm, 0.4 mm spacing, linear, Johnson-Cook + EOS, USF",),
     "dam_break": ("dam break 4x2x2 m in 10x2x4 m tank, 1 cm spacing, B-spline, null + EOS 4, MUSL",),
+    "granular_column": ("granular column r 0.5 m H 1 m, 2.307 mm spacing, 512x512x256 grid of 4 mm, GIMP, "
+                        "Drucker-Prager phi 30 c 0, MUSL",),
 }
 
 
@@ -58,6 +60,8 @@ def make_deck(workload: str, scale: float = 1.0) -> str:
         return decks.taylor_bar(dp=4e-4 * scale)
     if workload == "dam_break":
         return decks.dam_break(dp=0.01 * scale, h=0.02 * scale)
+    if workload == "granular_column":
+        return decks.granular_column(scale)[0]
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -217,7 +221,7 @@ def run_ours(args) -> dict:
 
     results = {}
     states = {}
-    for form in ("fp64", "mixed"):
+    for form in (("mixed",) if args.no_fp64 else ("fp64", "mixed")):
         s = m.MpmStep(deck, precision=form, device=local)
         s.run(args.warmup, graph=True)
         s.sync()
@@ -239,10 +243,12 @@ def run_ours(args) -> dict:
         results[form]["kernels"] = s.kernel_stats()
         s.profile(False)
         s.close()
-    err = {"nodal_momentum_rel": rel_err(states["mixed"]["PXg"], states["fp64"]["PXg"]),
-           "particle_stress_rel": max(rel_err(states["mixed"]["SM"], states["fp64"]["SM"]),
-                                      rel_err(states["mixed"]["SD"], states["fp64"]["SD"])),
-           "position_rel": rel_err(states["mixed"]["Xp"], states["fp64"]["Xp"])}
+    err = None
+    if "fp64" in states:
+        err = {"nodal_momentum_rel": rel_err(states["mixed"]["PXg"], states["fp64"]["PXg"]),
+               "particle_stress_rel": max(rel_err(states["mixed"]["SM"], states["fp64"]["SM"]),
+                                          rel_err(states["mixed"]["SD"], states["fp64"]["SD"])),
+               "position_rel": rel_err(states["mixed"]["Xp"], states["fp64"]["Xp"])}
 
     # end to end through the C ABI from host buffers
     if args.no_e2e:
@@ -260,9 +266,9 @@ def run_ours(args) -> dict:
         e2.close()
         t_e2e = max_over_ranks(t_e2e)
 
-    mixed, fp64 = results["mixed"], results["fp64"]
+    mixed, fp64 = results["mixed"], results.get("fp64")
     value = npart * world * args.steps / (mixed["ms"] / 1e3)
-    fp64_value = npart * world * args.steps / (fp64["ms"] / 1e3)
+    fp64_value = npart * world * args.steps / (fp64["ms"] / 1e3) if fp64 else None
     peaks = measured_peaks()
     dom = dominant_kernel(mixed["kernels"], args.steps)
     nn_active = mixed["scalars"]["active_nodes"]
@@ -284,9 +290,9 @@ def run_ours(args) -> dict:
         "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
                    "grid_nodes": int(mixed["scalars"]["nb_gridnode"]), "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (no flush)", "graph": True},
-        "fp64": {"value": fp64_value, "ms_per_step": fp64["ms"] / args.steps, "dtype": "f64",
-                 "parity": "bit-identical to the CPU oracle (tests/test_gpu_parity.py)",
-                 "speedup_mixed_over_fp64": value / fp64_value},
+        "fp64": ({"value": fp64_value, "ms_per_step": fp64["ms"] / args.steps, "dtype": "f64",
+                  "parity": "bit-identical to the CPU oracle (tests/test_gpu_parity.py)",
+                  "speedup_mixed_over_fp64": value / fp64_value} if fp64 else None),
         "error_vs_fp64": err,
         "e2e": {"value": npart * world * args.steps / t_e2e, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
@@ -296,7 +302,8 @@ def run_ours(args) -> dict:
                      "avg_launch_ms": dom["avg_ms"]},
         "step_alg_gbs": mixed["alg_bytes_step"] / (mixed["ms"] / args.steps / 1e3) / 1e9,
         "kernels_mixed": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in mixed["kernels"] if k["launches"]},
-        "kernels_fp64": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in fp64["kernels"] if k["launches"]},
+        "kernels_fp64": ({k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in fp64["kernels"] if k["launches"]}
+                         if fp64 else None),
         "gpu_launches": sum(k["launches"] for k in mixed["kernels"]),
         "clocks": mixed["clocks"],
     }
@@ -433,6 +440,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 form (large workloads)")
     ap.add_argument("--ref-steps", type=int, default=2)
     ap.add_argument("--ref-warmup", type=int, default=1)
     ap.add_argument("--ref-cores", type=int, default=0)

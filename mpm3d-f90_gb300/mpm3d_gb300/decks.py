@@ -403,3 +403,45 @@ def serving_scene(rng: np.random.Generator, np_min: int = 2000, np_max: int = 40
     loads = ["load"] + ["part %d 0 %s 0" % (i + 1, f32s(per)) for i in right] + ["endl"]
     w.tail += loads
     return w.text(), n, kind
+
+
+def granular_column(scale: float = 1.0, radius: float = 0.5, height: float = 1.0, dtscale: float = 0.5,
+                    rho: float = 2650.0, young: float = 1e7, nu: float = 0.3, phi: float = 30.0,
+                    cohesion: float = 0.0) -> tuple[str, int]:
+    """Granular column collapse: a cylinder (radius 0.5 m, height 1 m) of
+    Drucker-Prager sand (phi 30 deg, c 0) on a rough floor, GIMP, MUSL,
+    gravity. At scale 1 the particle spacing is 2.307 mm (about 64 M
+    particles; 5.2 particles per cell) on a 512 x 512 x 256 grid of 4 mm cells;
+    `scale` multiplies spacing and cell size. The cylinder is a stack of
+    one-layer discs (the 'cicl' generator, DataIn.f90:792-838), one body per
+    layer, so the deck stays a few kB at any particle count. Returns (deck
+    text, particle count)."""
+    dp = float(np.float32(2.307e-3 * scale))
+    h = 4e-3 * scale
+    nr = int(round(radius / dp))
+    nl = int(round(height / dp))
+    # particles per layer, with the reader's arithmetic (DataIn.f90:810-817)
+    ix = np.arange(1 - nr, nr + 1, dtype=np.float64)
+    t = (ix - 1) * dp + 0.0 + 0.5 * dp
+    A, B = np.meshgrid(t, t)
+    r2 = float(nr) * dp
+    per_layer = int(np.count_nonzero(A * A + B * B < r2 * r2))
+    n = per_layer * nl
+    half = 1.024  # 2.048 x 2.048 x 1.024 m domain (512 x 512 x 256 cells of 4 mm at scale 1)
+    q, k, qpsi, tens = dp_parameters(cohesion, phi)
+    w = DeckWriter("granular column collapse, Drucker-Prager, GIMP, MUSL")
+    w.nbmp = n
+    w.nbbo = nl
+    w.kw("nmat 1")
+    w.head += _grid_lines(((-half, half), (-half, half), (0.0, half)), h)
+    w.kw(f"dtsc {f32s(dtscale)}")
+    w.kw("endt 100.0")
+    w.kw("musl on")
+    w.kw("gimp")
+    w.kw("fixe 0 0 0 0 1 0")
+    w.kw("mate")
+    w.kw(f"1 dpm {f32s(rho)} {f32s(young)} {f32s(nu)} {f32s(q)} {f32s(k)} {f32s(qpsi)} {f32s(tens)}")
+    for layer in range(nl):
+        w.bodies.append(f"part cicl 1 1 {f32s(rho)} {f32s(dp)} 0 0 {f32s(layer * dp)} {nr}")
+    w.tail += ["load"] + [f"grav {b + 1} 0 0 -9.81" for b in range(nl)] + ["endl"]
+    return w.text(), n
