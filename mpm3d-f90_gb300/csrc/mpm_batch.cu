@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_run_length_encode.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -116,6 +117,7 @@ struct mpm_batch {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
+  int scatter_blocks = 9728;  // scatter grid cap (64 blocks per SM; warps stride over the occupied cells)
   Profiler prof;
   std::string err;
 };
@@ -274,6 +276,12 @@ int enqueue_step(mpm_batch* b) {
   tmp = b->cub_bytes;
   e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
+  if (b->any_nonsgmp) {  // occupied cells for the persistent scatters
+    tmp = b->cub_bytes;
+    e = cub::DeviceRunLengthEncode::Encode(b->cub_tmp, tmp, a.key_sorted, a.runs, a.run_counts, a.nruns, (int)a.NP,
+                                           st);
+    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "run-length encode: %s", cudaGetErrorString(e));
+  }
   prof_end(K_SORT, st);
   prof_begin(K_PERMUTE, st);
   kb_permute<<<gridn(a.NP, pb), pb, 0, st>>>(a, b->B);
@@ -282,9 +290,10 @@ int enqueue_step(mpm_batch* b) {
   std::swap(b->A, b->B);
   BState& s = b->A;
   const bool scatter = b->any_nonsgmp;
+  const unsigned sgrid = (unsigned)std::min<long long>(b->scatter_blocks, (s.NK + kCellWarps - 1) / kCellWarps);
   if (scatter) {
     prof_begin(K_SCATTER_MASS, st);
-    kb_cell_scatter<0><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
+    kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
     prof_end(K_SCATTER_MASS, st);
   }
   prof_begin(K_P2G_MASS, st);
@@ -314,7 +323,7 @@ int enqueue_step(mpm_batch* b) {
   prof_end(K_FORCE_PREP, st);
   if (scatter) {
     prof_begin(K_SCATTER_FORCE, st);
-    kb_cell_scatter<2><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
+    kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
     prof_end(K_SCATTER_FORCE, st);
   }
   prof_begin(K_P2G_FORCE, st);
@@ -328,7 +337,7 @@ int enqueue_step(mpm_batch* b) {
   if (b->any_musl) {
     if (scatter) {
       prof_begin(K_SCATTER_MOM, st);
-      kb_cell_scatter<1><<<gridn(s.NK, kCellWarps), 32 * kCellWarps, 0, st>>>(s);
+      kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
       prof_end(K_SCATTER_MOM, st);
     }
     prof_begin(K_P2G_MOM, st);
@@ -454,7 +463,10 @@ int commit(mpm_batch* b) {
                                   (int)NP, 0, bits, st);
   cub::DeviceScan::InclusiveSum(nullptr, t2, (int*)nullptr, (int*)nullptr, (int)NK, st);
   if (b->any_jc) cub::DeviceScan::InclusiveScan(nullptr, t3, (int*)nullptr, (int*)nullptr, MaxOpB(), (int)NP, st);
-  const size_t tb = std::max(t1, std::max(t2, t3));
+  size_t t4 = 0;
+  cub::DeviceRunLengthEncode::Encode(nullptr, t4, (unsigned*)nullptr, (unsigned*)nullptr, (int*)nullptr, (int*)nullptr,
+                                     (int)NP, st);
+  const size_t tb = std::max(std::max(t1, t4), std::max(t2, t3));
   BState A{}, B{}, shared{};
   int* d_target = nullptr;
   int* d_map = nullptr;
@@ -487,6 +499,9 @@ int commit(mpm_batch* b) {
   shared.val = al.get<int>(NP);
   shared.perm = al.get<int>(NP);
   shared.seg = al.get<int>(NK + 1);
+  shared.runs = al.get<unsigned>(NP);
+  shared.run_counts = al.get<int>(NP);
+  shared.nruns = al.get<int>(1);
   shared.mg = al.get<double>(NN);
   shared.px = al.get<double>(3 * NN);
   shared.fx = al.get<double>(3 * NN);
@@ -550,7 +565,7 @@ int commit(mpm_batch* b) {
   auto share = [&](BState& s) {
     s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
     s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
-    s.perm = shared.perm; s.seg = shared.seg; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
+    s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.run_counts = shared.run_counts; s.nruns = shared.nruns; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
     s.nvel = shared.nvel; s.nacc = shared.nacc; s.acc = shared.acc; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
     s.cmg = shared.cmg; s.cpx = shared.cpx; s.cfext = shared.cfext; s.cfint = shared.cfint; s.co = shared.co;
     s.cw = shared.cw; s.cdefp = shared.cdefp; s.cvx = shared.cvx; s.cax = shared.cax; s.cscene = shared.cscene;
@@ -702,6 +717,9 @@ int mpm_batch_create(int device, mpm_batch** out) {
   if (device >= 0) cudaSetDevice(device);
   mpm_batch* b = new mpm_batch();
   cudaGetDevice(&b->device);
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) == cudaSuccess && sms > 0)
+    b->scatter_blocks = 64 * sms;
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete b;
     return MPM_ERR_CUDA;

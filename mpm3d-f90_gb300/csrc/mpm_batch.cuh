@@ -79,6 +79,8 @@ struct BState {
   // sort
   unsigned *key, *key_sorted;
   int *val, *perm, *seg;
+  unsigned* runs;    // occupied sort keys of the step (run-length encoding of key_sorted)
+  int *run_counts, *nruns;
   // grid
   double *mg, *px, *fx;
   float4 *nvel, *nacc;             // FP32 px / mg and fx / mg for the gathers (zero at or below the cut-off)

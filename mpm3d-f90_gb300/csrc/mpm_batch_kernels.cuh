@@ -307,14 +307,18 @@ __global__ void kb_permute(BState src, BState dst) {
 constexpr int kCellWarps = 8;  // warps (cells) per block
 
 template <int MODE>
-__global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b) {
-  constexpr int NV = MODE == 0 ? 4 : 3;       // channels
-  constexpr int NQ = MODE == 2 ? 9 : 4;       // per-particle quantities staged
-  constexpr int NT = MODE == 2 ? 24 : 12;     // per-particle table entries (w, and d for the force)
-  __shared__ float sq[kCellWarps][32][NQ + NT + 1];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long key = (long long)blockIdx.x * kCellWarps + warp;
-  if (key >= b.NK) return;
+struct ScatterShape {
+  static constexpr int NV = MODE == 0 ? 4 : 3;    // channels
+  static constexpr int NQ = MODE == 2 ? 9 : 4;    // per-particle quantities staged
+  static constexpr int NT = MODE == 2 ? 24 : 12;  // per-particle table entries (w, and d for the force)
+  static constexpr int ROW = NQ + NT + 1;         // staged floats per particle (odd: no bank conflicts)
+};
+
+// the scatter of one sort key (cell) by one warp; sq = the warp's staging rows
+template <int MODE>
+__device__ __forceinline__ void scatter_cell(BState& b, long long key, float (*sq)[ScatterShape<MODE>::ROW]) {
+  constexpr int NV = ScatterShape<MODE>::NV, NQ = ScatterShape<MODE>::NQ;
+  const int lane = threadIdx.x & 31;
   int i0, i1;
   key_range(b, key, i0, i1);
   if (i0 >= i1) return;
@@ -356,7 +360,7 @@ __global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b) {
   float acc[2][NV];
   for (int k = 0; k < 2; ++k)
     for (int v = 0; v < NV; ++v) acc[k][v] = 0.f;
-  float* row = sq[warp][lane];
+  float* row = sq[lane];
   for (int base = i0; base < i1; base += 32) {
     const int cnt = min(32, i1 - base);
     if (lane < cnt) {
@@ -385,7 +389,7 @@ __global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b) {
     }
     __syncwarp();
     for (int p = 0; p < cnt; ++p) {
-      const float* r = sq[warp][p];
+      const float* r = sq[p];
       for (int k = 0; k < 2; ++k) {
         if (!use[k]) continue;
         const float wx = r[NQ + 0 + to[k][0] + 1], wy = r[NQ + 4 + to[k][1] + 1], wz = r[NQ + 8 + to[k][2] + 1];
@@ -424,6 +428,19 @@ __global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b) {
       if (q) atomicAdd(&b.acc[v * b.NN + n], (unsigned long long)q);
     }
   }
+}
+
+// Persistent scatter over the occupied sort keys (the run-length encoding of
+// the sorted keys, count on the device): a fixed grid, each warp taking keys
+// r, r + total warps, ... Empty cells cost nothing, which matters on sparse
+// grids (a granular column fills a fifth of its grid).
+template <int MODE>
+__global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b, const unsigned* runs, const int* nruns) {
+  __shared__ float sq[kCellWarps][32][ScatterShape<MODE>::ROW];
+  const int warp = threadIdx.x >> 5;
+  const long long n = *nruns;
+  for (long long r = (long long)blockIdx.x * kCellWarps + warp; r < n; r += (long long)gridDim.x * kCellWarps)
+    scatter_cell<MODE>(b, runs[r], sq[warp]);
 }
 
 // accumulated channel v of node n in FP64 (and the accumulator cleared for
@@ -506,11 +523,27 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
       node_finish(b, sc, n, bc_usf && sc.usf, vel_usf && sc.usf);
     }
   }
-  // per-scene active-node count: one atomic per (warp, scene) group
-  unsigned grp = __match_any_sync(0xffffffffu, s);
-  unsigned actg = __ballot_sync(0xffffffffu, act) & grp;
-  int lane = threadIdx.x & 31;
-  if (s >= 0 && actg && lane == __ffs(grp) - 1) atomicAdd(&b.sst[s].active_nodes, (unsigned long long)__popc(actg));
+  // per-scene active-node count, combined per block (one atomic per scene
+  // and block in the common case)
+  __shared__ int ws[32];
+  __shared__ unsigned wc[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const unsigned grp = __match_any_sync(0xffffffffu, s);
+  const unsigned actg = __ballot_sync(0xffffffffu, act) & grp;
+  const bool uniform = grp == 0xffffffffu;
+  if (!uniform && s >= 0 && actg && lane == __ffs(grp) - 1)
+    atomicAdd(&b.sst[s].active_nodes, (unsigned long long)__popc(actg));
+  if (lane == 0) {
+    ws[warp] = uniform ? s : -1;
+    wc[warp] = uniform ? (unsigned)__popc(actg) : 0u;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int s2 = lane < nw ? ws[lane] : -1;
+    const unsigned g2 = __match_any_sync(0xffffffffu, s2);
+    const unsigned c2 = __reduce_add_sync(g2, lane < nw ? wc[lane] : 0u);
+    if (s2 >= 0 && c2 && lane == __ffs(g2) - 1) atomicAdd(&b.sst[s2].active_nodes, (unsigned long long)c2);
+  }
 }
 
 // SGMP: particles -> centre nodes. The centre node of cell q is corner k of
