@@ -443,12 +443,25 @@ __global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b, con
     scatter_cell<MODE>(b, runs[r], sq[warp]);
 }
 
-// accumulated channel v of node n in FP64 (and the accumulator cleared for
-// the next transfer)
-__device__ __forceinline__ double take_acc(BState& b, long long n, int v, double unit) {
-  const long long x = (long long)b.acc[v * b.NN + n];
-  b.acc[v * b.NN + n] = 0ull;
-  return (double)x * unit;
+// Accumulated channels 0..nv-1 of node n in FP64 (the accumulators cleared
+// for the next transfer). Returns false for an idle node: nothing
+// accumulated and no mass at the node already, so every node field is still
+// zero from the last time the node was written and nothing needs writing --
+// on sparse grids most nodes are idle. (A node that no particle reaches is
+// never read by a particle, and one whose mass drops to zero is written once.)
+__device__ __forceinline__ bool take_acc(BState& b, long long n, int nv, const double* unit, double* out) {
+  unsigned long long q[4];
+  unsigned long long any = 0ull;
+  for (int v = 0; v < nv; ++v) {
+    q[v] = b.acc[v * b.NN + n];
+    any |= q[v];
+  }
+  if (any == 0ull && b.mg[n] == 0.0) return false;
+  for (int v = 0; v < nv; ++v) {
+    out[v] = (double)(long long)q[v] * unit[v];
+    if (q[v]) b.acc[v * b.NN + n] = 0ull;
+  }
+  return true;
 }
 
 __device__ __forceinline__ void node_finish(BState& b, const Scene& sc, long long n, int bc, int vel) {
@@ -484,8 +497,9 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
     s = b.node_scene[n];
     if (scene_live(b, s)) {
       const Scene& sc = b.scenes[s];
-      const long long NN = b.NN, NP = b.NP;
+      const long long NN = b.NN;
       double M = 0, P0 = 0, P1 = 0, P2 = 0;
+      bool live = true;
       int j[3];
       node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
       if (sc.shape == 3) {
@@ -509,18 +523,30 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
         }
       } else {
         const SceneState& st = b.sst[s];
-        const double um = q_unit(q_shift(sc, st.qmax[Q_MASS])), up = q_unit(q_shift(sc, st.qmax[Q_MOM]));
-        M = take_acc(b, n, 0, um);
-        P0 = take_acc(b, n, 1, up);
-        P1 = take_acc(b, n, 2, up);
-        P2 = take_acc(b, n, 3, up);
+        const double up = q_unit(q_shift(sc, st.qmax[Q_MOM]));
+        const double unit[4] = {q_unit(q_shift(sc, st.qmax[Q_MASS])), up, up, up};
+        double o[4];
+        live = take_acc(b, n, 4, unit, o);
+        M = o[0];
+        P0 = o[1];
+        P1 = o[2];
+        P2 = o[3];
       }
-      b.mg[n] = M;
-      b.px[n] = P0;
-      b.px[NN + n] = P1;
-      b.px[2 * NN + n] = P2;
-      act = M > 0.0;
-      node_finish(b, sc, n, bc_usf && sc.usf, vel_usf && sc.usf);
+      if (live) {
+        b.mg[n] = M;
+        b.px[n] = P0;
+        b.px[NN + n] = P1;
+        b.px[2 * NN + n] = P2;
+        act = M > 0.0;
+        node_finish(b, sc, n, bc_usf && sc.usf, vel_usf && sc.usf);
+        if (!(M != 0.0) && sc.shape != 3) {
+          // the node goes idle: clear the rest of its fields once (the idle
+          // test of the later transfers skips it from now on)
+          for (int a = 0; a < 3; ++a) b.fx[a * NN + n] = 0.0;
+          b.nvel[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+          b.nacc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
     }
   }
   // per-scene active-node count, combined per block (one atomic per scene
@@ -916,7 +942,6 @@ __global__ void kb_p2g_force(BState b) {
   const int s = b.node_scene[n];
   if (!scene_live(b, s)) return;
   const Scene& sc = b.scenes[s];
-  const long long NP = b.NP;
   int j[3];
   node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
   double F[3] = {0, 0, 0};
@@ -945,7 +970,8 @@ __global__ void kb_p2g_force(BState b) {
     }
   } else {
     const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
-    for (int a = 0; a < 3; ++a) F[a] = take_acc(b, n, a, u);
+    const double unit[3] = {u, u, u};
+    if (!take_acc(b, n, 3, unit, F)) return;  // idle node
   }
   node_integrate(b, sc, n, F);
 }
@@ -1170,7 +1196,7 @@ __global__ void kb_p2g_momentum(BState b) {
   if (!scene_live(b, s)) return;
   const Scene& sc = b.scenes[s];
   if (!sc.musl) return;
-  const long long NN = b.NN, NP = b.NP;
+  const long long NN = b.NN;
   int j[3];
   node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
   double P0 = 0, P1 = 0, P2 = 0;
@@ -1191,9 +1217,12 @@ __global__ void kb_p2g_momentum(BState b) {
     }
   } else {
     const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]));
-    P0 = take_acc(b, n, 0, u);
-    P1 = take_acc(b, n, 1, u);
-    P2 = take_acc(b, n, 2, u);
+    const double unit[3] = {u, u, u};
+    double o[3];
+    if (!take_acc(b, n, 3, unit, o)) return;  // idle node
+    P0 = o[0];
+    P1 = o[1];
+    P2 = o[2];
   }
   b.px[n] = P0;
   b.px[NN + n] = P1;
