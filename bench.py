@@ -186,18 +186,53 @@ def profiled_traffic(kernel: str):
     return None
 
 
+class Replicas:
+    """Multi-GPU runs are replicas: one process per GPU (torchrun), each
+    advancing its own copy of the workload; the only cross-rank traffic is a
+    barrier around the timed region and the max of the timings (gloo, host
+    side; no collective on the data path)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo", init_method="env://")
+            self.dist = dist
+
+    def barrier(self) -> None:
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.dist:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def aggregate_rate(units_per_rank: float, world: int, steps: int, ms_max: float) -> float:
+    """Whole-job rate: the units all ranks processed over the slowest rank's time."""
+    return units_per_rank * world * steps / (ms_max / 1e3)
+
+
 def run_ours(args) -> dict:
     import numpy as np
     import mpm3d_gb300 as m
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist  # replicas only: barrier + max of times
-
-        dist.init_process_group("gloo", init_method="env://")
+    rep = Replicas()
+    world, rank, local = rep.world, rep.rank, rep.local
     text = make_deck(args.workload, args.scale)
     with tempfile.NamedTemporaryFile("w", suffix=".mpm", delete=False) as f:
         f.write(text)
@@ -206,18 +241,8 @@ def run_ours(args) -> dict:
     os.unlink(deck_path)
     npart = deck.nb_particle
 
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if not dist:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier = rep.barrier
+    max_over_ranks = rep.max
 
     results = {}
     states = {}
@@ -267,8 +292,8 @@ def run_ours(args) -> dict:
         t_e2e = max_over_ranks(t_e2e)
 
     mixed, fp64 = results["mixed"], results.get("fp64")
-    value = npart * world * args.steps / (mixed["ms"] / 1e3)
-    fp64_value = npart * world * args.steps / (fp64["ms"] / 1e3) if fp64 else None
+    value = aggregate_rate(npart, world, args.steps, mixed["ms"])
+    fp64_value = aggregate_rate(npart, world, args.steps, fp64["ms"]) if fp64 else None
     peaks = measured_peaks()
     dom = dominant_kernel(mixed["kernels"], args.steps)
     nn_active = mixed["scalars"]["active_nodes"]
@@ -311,8 +336,7 @@ def run_ours(args) -> dict:
         line["serving"] = run_serving(args, local)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(text, args.cpu_steps, npart)
-    if dist:
-        dist.destroy_process_group()
+    rep.close()
     return line if rank == 0 else None
 
 
