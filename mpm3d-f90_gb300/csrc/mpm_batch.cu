@@ -72,6 +72,7 @@ __global__ void kb_relocate(BState src, BState dst, const int* map, const uint16
   dst.mass[i] = src.mass[j];
   dst.ie[i] = src.ie[j];
   dst.vol[i] = src.vol[j];
+  dst.evol[i] = src.evol[j];
   dst.sig_y[i] = src.sig_y[j];
   dst.sm[i] = src.sm[j];
   dst.seqv[i] = src.seqv[j];
@@ -163,6 +164,7 @@ void alloc_particles(Alloc& al, BState& s, long long NP, bool uvfp) {
   s.mass = al.get<double>(NP);
   s.ie = al.get<double>(NP);
   s.vol = al.get<float>(NP);
+  s.evol = al.get<float>(NP);
   s.sig_y = al.get<float>(NP);
   s.sm = al.get<float>(NP);
   s.seqv = al.get<float>(NP);
@@ -181,7 +183,7 @@ void alloc_particles(Alloc& al, BState& s, long long NP, bool uvfp) {
 }
 
 long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bool uvfp, bool jc) {
-  long long per_p = 2 * (16 * 8 + 16 * 4 + (uvfp ? 36 : 0) + 1 + 2 + 2 + 4);  // two particle buffer sets
+  long long per_p = 2 * (16 * 8 + 17 * 4 + (uvfp ? 36 : 0) + 1 + 2 + 2 + 4);  // two particle buffer sets
   per_p += 4 * 3 + 4 * 9 + 4 * 6 + 4 * 9;                                  // derived + force staging
   per_p += 4 * 4;                                                         // sort keys / values
   if (jc) per_p += 4 * 2 + 8 * 6 + 1;
@@ -231,6 +233,7 @@ int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
   std::vector<double> t293((size_t)np, (double)293.0f);
   BCK(upf(s.celsius + p0, t293));
   BCK(cudaMemsetAsync(s.sm + p0, 0, sizeof(float) * np, b->stream));
+  BCK(cudaMemsetAsync(s.evol + p0, 0, sizeof(float) * np, b->stream));
   BCK(cudaMemsetAsync(s.seqv + p0, 0, sizeof(float) * np, b->stream));
   for (int a = 0; a < 6; ++a) BCK(cudaMemsetAsync(s.sd + a * NP + p0, 0, sizeof(float) * np, b->stream));
   if (s.any_uvfp)

@@ -6,7 +6,8 @@
 //   step (stable sort of the previous order, then a permutation of every
 //   field), component-major over the total particle count NP:
 //     FP64: x[3], xx[3], v[3], fxp[3], mass, ie
-//     FP32: vol, sig_y, sm, seqv, sd[6], fp[9], epeff, celsius, dmg, lt, cp, q
+//     FP32: vol, evol (V / V0 - 1), sig_y, sm, seqv, sd[6], fp[9], epeff, celsius,
+//     dmg, lt, cp, q
 //     per step (written by the permutation): cell (scene-local cell, -1
 //     outside), off[3] (offset in the cell, in cells), SGMP dual cell, nearest
 //     node, xxn[3], xn[3]; body, scene, orig (scene-local input index)
@@ -68,7 +69,7 @@ struct BState {
   int any_uvfp, any_sgmp, any_jc;
   // particles (A = current, B = permutation target)
   double *x, *xx, *v, *fxp, *mass, *ie;
-  float *vol, *sig_y, *sm, *seqv, *sd, *fp, *epeff, *celsius, *dmg, *lt, *cp, *q;
+  float *vol, *evol, *sig_y, *sm, *seqv, *sd, *fp, *epeff, *celsius, *dmg, *lt, *cp, *q;
   uint8_t* failure;
   uint16_t *body, *scene;
   int* orig;

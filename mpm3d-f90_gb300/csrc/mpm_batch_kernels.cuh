@@ -135,6 +135,7 @@ __device__ __forceinline__ void permute_one(const BState& src, BState& dst, long
   dst.mass[i] = src.mass[j];
   dst.ie[i] = src.ie[j];
   dst.vol[i] = src.vol[j];
+  dst.evol[i] = src.evol[j];
   dst.sig_y[i] = src.sig_y[j];
   dst.sm[i] = src.sm[j];
   dst.seqv[i] = src.seqv[j];
@@ -763,6 +764,7 @@ __global__ void kb_stress(BState b, int usf_pass) {
   ps.q = b.q[i];
   for (int a = 0; a < 6; ++a) ps.sd[a] = b.sd[a * NP + i];
   ps.failure = b.failure[i] != 0;
+  ps.evol = b.evol[i];
   const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
   CResult<R> res;
   constitution<P>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2, res);
@@ -783,6 +785,7 @@ __global__ void kb_stress(BState b, int usf_pass) {
     }
   }
   b.vol[i] = ps.vol;
+  b.evol[i] = ps.evol;
   b.sm[i] = ps.sm;
   b.seqv[i] = ps.seqv;
   for (int a = 0; a < 6; ++a) b.sd[a * NP + i] = ps.sd[a];

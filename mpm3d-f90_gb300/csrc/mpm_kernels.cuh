@@ -358,6 +358,7 @@ template <class R>
 struct PState {
   R vol, epeff, sig_y, seqv, lt, celsius, ie, mass, dmg, cp, sm, q;
   R sd[6];
+  R evol;  // mixed form only: volumetric strain V / V0 - 1, carried per particle
   bool failure;
 };
 
@@ -388,6 +389,7 @@ __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const De
   m.bfac = (R)0;
   for (int i = 0; i < 6; ++i) m.dinc[i] = de[i];
   m.vold = ps.vol;
+  R dJ = (R)0;  // mixed form: volume ratio of the step minus one, without cancellation
   if (uvfp) {
     R dF[3][3];
     for (int i = 0; i < 3; ++i)
@@ -401,8 +403,16 @@ __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const De
       m.Fp[i][i] = m.Fp[i][i] + (R)1.0;
     }
     m.vol_ = m.vold * det3(dF);
+    if constexpr (!P::kExact) {
+      const R(*A)[3] = deFp;  // det(I + A) - 1 = tr A + I2(A) + det A
+      dJ = (A[0][0] + A[1][1] + A[2][2]) +
+           (A[0][0] * A[1][1] + A[1][1] * A[2][2] + A[0][0] * A[2][2] - A[0][1] * A[1][0] - A[1][2] * A[2][1] -
+            A[0][2] * A[2][0]) +
+           det3(A);
+    }
   } else {
     m.vol_ = m.vold * ((R)1 + de[0] + de[1] + de[2]);
+    dJ = de[0] + de[1] + de[2];
     // without UpdateVbyFp the reference's module variable Fp is never set
     // (zero from program start)
     for (int i = 0; i < 3; ++i)
@@ -433,6 +443,24 @@ __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const De
   m.den_ = mp_ / m.vol_;
   m.mu = m.den_ / m.den0_ - (R)1;
   m.rv = m.vol_ / m.vol0_;
+  m.dden = m.den_ - m.den0_;
+  if constexpr (!P::kExact) {
+    // FP32 volumes cannot resolve V / V0 - 1 of nearly incompressible
+    // states (1e-6 and below): carry the volumetric strain e = V / V0 - 1
+    // itself and derive the volume, its increment, mu and the density
+    // change from it
+    const R e0 = ps.evol;
+    const R e1 = e0 + ((R)1 + e0) * dJ;
+    ps.evol = e1;
+    m.vol_ = m.vol0_ * ((R)1 + e1);
+    vol_store = m.vol_;
+    res.negative_volume = m.vol_ < (R)0;
+    m.dvol = (R)0.5 * m.vol0_ * (e1 - e0);
+    m.den_ = mp_ / m.vol_;
+    m.mu = -e1 / ((R)1 + e1);
+    m.rv = (R)1 + e1;
+    m.dden = m.den0_ * m.mu;
+  }
   m.specen = m.iener / m.vol0_;
   m.DMG = ps.dmg;
   m.oldDMG = m.DMG;
@@ -700,6 +728,7 @@ __global__ void k_stress(St<P> s, Geometry g) {
   ps.q = (R)s.q[p];
   for (int i = 0; i < 6; ++i) ps.sd[i] = (R)s.sd[i * np + p];
   ps.failure = s.failure[p] != 0;
+  ps.evol = (R)0;
   const DevMaterial& mt = s.mats[s.bodies[s.body[p]].mat];
   CResult<R> res;
   constitution<P>(ps, mt, de, vort, deFp, Fpn, g.uvfp != 0, DT, s.sc->time, (R)g.dcell, (R)g.bq1, (R)g.bq2, res);

@@ -164,6 +164,7 @@ __device__ __forceinline__ int cell_node1(const Geometry& g, int icell) {
 template <class R>
 struct Mm {
   R vold, vol_, vol0_, dvol, den0_, den_, mu, rv, specen, iener, ieinc;
+  R dden;  // den_ - den0_
   R dinc[6], sig[6], sd[6], sold[6], sm, smold, bqf, seqv, epeff_, sig_y_, depeff, ratio;
   R G2, K3, PlaMod, lamda, miu2, young_, poisson_, yield0_, tmprt, cp, DMG, oldDMG, bfac;
   R Fp[3][3];
@@ -531,7 +532,7 @@ __device__ __forceinline__ bool seleos(Mm<typename P::R>& m, const DevMaterial& 
       R c0 = (R)mt.cEos[0];
       if (m.sm < (R)0) bulkq(m, DT, dcell, bq1, bq2);
       hieupd(m, failure);
-      R pnew = c0 * c0 * (m.den_ - m.den0_);
+      R pnew = c0 * c0 * m.dden;
       if (failure && pnew < (R)0) pnew = (R)0.0;
       m.iener = m.iener - m.dvol * pnew;
       m.sm = -pnew;

@@ -15,11 +15,14 @@ pytestmark = pytest.mark.gpu
 # Prager, J2-plastic and fluid cases stay near FP32 rounding (< 1e-4; most
 # are ~1e-6). Johnson-Cook cases amplify rounding through the plastic return
 # map and the rate term (the FP64 form itself moves by ~1e-2 in SD over 1000
-# Taylor steps when only the libm changes), so they get a looser bound.
+# Taylor steps when only the libm changes), so they get a looser bound; with
+# failure ('sjcf') a particle's failure flag flips on a threshold, so
+# rounding-level differences switch individual particles between failed and
+# intact and the fields differ locally by O(1) of those particles' share.
 MIXED_TOL = {
     "taylor_small_usf_jcf_linear": 0.1,
     "block_musl_sjc_gruneisen": 2e-2,
-    "block_usf_sjcf_gruneisen": 2e-2,
+    "block_usf_sjcf_gruneisen": 5e-2,
 }
 DEFAULT_TOL = 1e-4
 FIELDS = ["PXg", "Mg", "SM", "SD", "Xp", "VXp"]
