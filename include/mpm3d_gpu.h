@@ -177,6 +177,11 @@ int mpm_batch_sync(mpm_batch* b);
 int mpm_batch_time_steps(mpm_batch* b, int nsteps, int use_graph, double* ms);
 int mpm_batch_scene_scalars(mpm_batch* b, int scene_id, double* out16);
 int mpm_batch_scene_download(mpm_batch* b, int scene_id, int field, double* out);
+/* mpm_gather_async / mpm_gather_wait for one scene of a batch (particles in
+ * the scene's deck order) */
+int mpm_batch_scene_gather_async(mpm_batch* b, int scene_id, int n, const int64_t* particle, const int* field,
+                                 const int* component);
+int mpm_batch_scene_gather_wait(mpm_batch* b, double* out);
 const char* mpm_batch_last_error(const mpm_batch* b);
 /* Launch shape of the batch kernels (threads per block for particle and node
  * kernels; 0 keeps the current value). */
@@ -187,6 +192,18 @@ int mpm_batch_set_option(mpm_batch* b, int option, int value);
 int mpm_batch_get_option(const mpm_batch* b, int option);
 int mpm_batch_profile_enable(mpm_batch* b, int on);
 int mpm_batch_kernel_stats(mpm_batch* b, int k, char* name, int namelen, int64_t* launches, double* total_ms);
+
+/* ------------------------------------------------- particle value gather */
+/* Values of a few particles (curve output, OutCurve): n (particle, field,
+ * component) triples, particles 0-based in deck order, fields particle fields
+ * of mpm_field. mpm_gather_async enqueues the gather behind the work already
+ * on the context's stream and copies the values into pinned host memory;
+ * mpm_gather_wait blocks until they have arrived and copies them to out
+ * (n doubles); mpm_gather does both. At most MPM_GATHER_MAX items per call. */
+#define MPM_GATHER_MAX 1024
+int mpm_gather_async(mpm_ctx* ctx, int n, const int64_t* particle, const int* field, const int* component);
+int mpm_gather_wait(mpm_ctx* ctx, double* out);
+int mpm_gather(mpm_ctx* ctx, int n, const int64_t* particle, const int* field, const int* component, double* out);
 
 /* ------------------------------------------------------ serving runtime */
 /* No counterpart in the reference (a serial one-scene program): a server owns

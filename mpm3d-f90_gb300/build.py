@@ -83,11 +83,12 @@ def build_library(force: bool = False) -> str:
         objs.append(o)
         if force or _newer(o, [s] + hdr):
             jobs.append([nvcc] + NVCC_COMMON + extra + ["-c", s, "-o", o])
-    deck_c = os.path.join(CSRC, "mpm_deck.c")
-    deck_o = os.path.join(BUILD, "mpm_deck.o")
-    objs.append(deck_o)
-    if force or _newer(deck_o, [deck_c] + hdr):
-        jobs.append(["gcc"] + CC_COMMON + ["-c", deck_c, "-o", deck_o])
+    for csrc in ("mpm_deck.c", "mpm_output.c"):
+        c_src = os.path.join(CSRC, csrc)
+        c_obj = os.path.join(BUILD, csrc.replace(".c", ".o"))
+        objs.append(c_obj)
+        if force or _newer(c_obj, [c_src] + hdr):
+            jobs.append(["gcc"] + CC_COMMON + ["-c", c_src, "-o", c_obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()

@@ -51,6 +51,12 @@ struct HostScene {
 
 namespace {
 
+__global__ void kb_inverse(BState s) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.NP) return;
+  s.inv[s.scenes[s.scene[i]].p0 + s.orig[i]] = (int)i;
+}
+
 struct MaxOpB {
   __host__ __device__ int operator()(int a, int b) const { return a > b ? a : b; }
 };
@@ -120,6 +126,11 @@ struct mpm_batch {
   int pblock = 256, nblock = 256;
   int scatter_blocks = 9728;  // scatter grid cap (64 blocks per SM; warps stride over the occupied cells)
   Profiler prof;
+  // particle value gather (curve output)
+  GatherItem *g_items_h = nullptr, *g_items_d = nullptr;
+  double *g_out_h = nullptr, *g_out_d = nullptr;
+  cudaEvent_t g_done = nullptr;
+  int g_n = 0;
   std::string err;
 };
 
@@ -503,6 +514,7 @@ int commit(mpm_batch* b) {
   shared.perm = al.get<int>(NP);
   shared.seg = al.get<int>(NK + 1);
   shared.runs = al.get<unsigned>(NP);
+  shared.inv = al.get<int>(NP);
   shared.run_counts = al.get<int>(NP);
   shared.nruns = al.get<int>(1);
   shared.mg = al.get<double>(NN);
@@ -568,7 +580,7 @@ int commit(mpm_batch* b) {
   auto share = [&](BState& s) {
     s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
     s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
-    s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.run_counts = shared.run_counts; s.nruns = shared.nruns; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
+    s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.inv = shared.inv; s.run_counts = shared.run_counts; s.nruns = shared.nruns; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
     s.nvel = shared.nvel; s.nacc = shared.nacc; s.acc = shared.acc; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
     s.cmg = shared.cmg; s.cpx = shared.cpx; s.cfext = shared.cfext; s.cfint = shared.cfint; s.co = shared.co;
     s.cw = shared.cw; s.cdefp = shared.cdefp; s.cvx = shared.cvx; s.cax = shared.cax; s.cscene = shared.cscene;
@@ -675,6 +687,9 @@ int commit(mpm_batch* b) {
       int r = upload_scene_particles(b, h, A);
       if (r) return r;
     }
+  // inverse permutation of the new layout (the permutation kernel keeps it
+  // up to date from the first step on)
+  kb_inverse<<<gridn(NP, 256), 256, 0, st>>>(A);
   // calcEnergy of the new scenes (MPM3D.f90:42)
   kb_reduce_chunks<<<(unsigned)NR, 256, 0, st>>>(A);
   kb_reduce_scenes<<<(unsigned)A.nscene, 256, 0, st>>>(A, 1);
@@ -738,6 +753,11 @@ void mpm_batch_destroy(mpm_batch* b) {
   drop_graph(b);
   if (b->arena) cudaFree(b->arena);
   if (b->spare) cudaFree(b->spare);
+  if (b->g_items_h) cudaFreeHost(b->g_items_h);
+  if (b->g_out_h) cudaFreeHost(b->g_out_h);
+  if (b->g_items_d) cudaFree(b->g_items_d);
+  if (b->g_out_d) cudaFree(b->g_out_d);
+  if (b->g_done) cudaEventDestroy(b->g_done);
   for (auto& kv : b->by_id) delete kv.second;
   prof_free(&b->prof);
   cudaStreamDestroy(b->stream);
@@ -952,6 +972,50 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
     }
     if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "download: %s", cudaGetErrorString(e));
   }
+  return MPM_OK;
+}
+
+int mpm_batch_scene_gather_async(mpm_batch* b, int id, int n, const int64_t* particle, const int* field,
+                                 const int* component) {
+  if (!b || n < 0 || n > MPM_GATHER_MAX || (n > 0 && (!particle || !field || !component))) return MPM_ERR_ARG;
+  int r = ensure_committed(b);
+  if (r) return r;
+  HostScene* h = find(b, id);
+  if (!h) return berr(b, MPM_ERR_ARG, "no scene %d", id);
+  for (int k = 0; k < n; ++k) {
+    const int f = field[k], nc = mpm_field_components(f);
+    const bool ok = f >= MPM_P_XP && f <= MPM_P_FAILURE && f != MPM_P_XN && f != MPM_P_XXN && f != MPM_P_VOL0 &&
+                    nc > 0 && component[k] >= 0 && component[k] < nc && particle[k] >= 0 && particle[k] < h->np &&
+                    (f != MPM_P_FP || b->any_uvfp);
+    if (!ok)
+      return berr(b, MPM_ERR_ARG, "gather item %d: particle %lld field %d component %d", k, (long long)particle[k], f,
+                  component[k]);
+  }
+  if (!b->g_items_h) {
+    BCK(cudaMallocHost((void**)&b->g_items_h, sizeof(GatherItem) * MPM_GATHER_MAX));
+    BCK(cudaMallocHost((void**)&b->g_out_h, sizeof(double) * MPM_GATHER_MAX));
+    BCK(cudaMalloc((void**)&b->g_items_d, sizeof(GatherItem) * MPM_GATHER_MAX));
+    BCK(cudaMalloc((void**)&b->g_out_d, sizeof(double) * MPM_GATHER_MAX));
+    BCK(cudaEventCreateWithFlags(&b->g_done, cudaEventDisableTiming));
+  }
+  BCK(cudaEventSynchronize(b->g_done));
+  for (int k = 0; k < n; ++k) b->g_items_h[k] = GatherItem{(long long)particle[k], field[k], component[k]};
+  b->g_n = n;
+  if (n > 0) {
+    BCK(cudaMemcpyAsync(b->g_items_d, b->g_items_h, sizeof(GatherItem) * n, cudaMemcpyHostToDevice, b->stream));
+    kb_gather<<<(n + 127) / 128, 128, 0, b->stream>>>(b->A, h->index, b->g_items_d, n, b->g_out_d);
+    BCK(cudaGetLastError());
+    BCK(cudaMemcpyAsync(b->g_out_h, b->g_out_d, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));
+  }
+  BCK(cudaEventRecord(b->g_done, b->stream));
+  return MPM_OK;
+}
+
+int mpm_batch_scene_gather_wait(mpm_batch* b, double* out) {
+  if (!b || !out) return MPM_ERR_ARG;
+  if (!b->g_done) return berr(b, MPM_ERR_STATE, "no gather in flight");
+  BCK(cudaEventSynchronize(b->g_done));
+  memcpy(out, b->g_out_h, sizeof(double) * (size_t)b->g_n);
   return MPM_OK;
 }
 

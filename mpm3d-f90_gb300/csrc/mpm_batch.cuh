@@ -73,6 +73,7 @@ struct BState {
   uint8_t* failure;
   uint16_t *body, *scene;
   int* orig;
+  int* inv;  // position of a particle by scene p0 + deck index (written by the permutation)
   // per-step derived (written by the permutation)
   int *cell, *dual, *inode;
   float *off, *xxn, *xn;

@@ -153,6 +153,7 @@ __device__ __forceinline__ void permute_one(const BState& src, BState& dst, long
   const int s = src.scene[j];
   dst.scene[i] = (uint16_t)s;
   dst.orig[i] = src.orig[j];
+  dst.inv[src.scenes[s].p0 + src.orig[j]] = (int)i;
   // derived
   const Scene& sc = src.scenes[s];
   double x[3] = {dst.x[i], dst.x[NP + i], dst.x[2 * NP + i]};
@@ -1338,6 +1339,43 @@ __global__ void kb_dr_finish(BState b) {
   if (!b.scenes[s].drdamp || !scene_live(b, s)) return;
   SceneState& st = b.sst[s];
   if (st.ke - st.ke_prev <= 0.0) st.ke = 0;
+}
+
+// values of a few particles of one scene (by deck index) for the curve output
+struct GatherItem {
+  long long p;
+  int field, comp;
+};
+
+__global__ void kb_gather(BState b, int scene, const GatherItem* it, int n, double* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const Scene& sc = b.scenes[scene];
+  const long long NP = b.NP, i = b.inv[sc.p0 + it[k].p], c = it[k].comp;
+  double v = 0.0;
+  switch (it[k].field) {
+    case MPM_P_XP: v = b.x[c * NP + i]; break;
+    case MPM_P_XX: v = b.xx[c * NP + i]; break;
+    case MPM_P_VXP: v = b.v[c * NP + i]; break;
+    case MPM_P_FXP: v = b.fxp[c * NP + i]; break;
+    case MPM_P_VOL: v = b.vol[i]; break;
+    case MPM_P_SIG_Y: v = b.sig_y[i]; break;
+    case MPM_P_SM: v = b.sm[i]; break;
+    case MPM_P_SEQV: v = b.seqv[i]; break;
+    case MPM_P_SD: v = b.sd[c * NP + i]; break;
+    case MPM_P_FP: v = b.fp[c * NP + i]; break;
+    case MPM_P_EPEFF: v = b.epeff[i]; break;
+    case MPM_P_CELSIUS: v = b.celsius[i]; break;
+    case MPM_P_DMG: v = b.dmg[i]; break;
+    case MPM_P_LT: v = b.lt[i]; break;
+    case MPM_P_IE: v = b.ie[i]; break;
+    case MPM_P_MASS: v = b.mass[i]; break;
+    case MPM_P_CP: v = b.cp[i]; break;
+    case MPM_P_Q: v = b.q[i]; break;
+    case MPM_P_FAILURE: v = b.failure[i] ? 1.0 : 0.0; break;
+    default: v = 0.0; break;
+  }
+  out[k] = v;
 }
 
 }  // namespace bm

@@ -36,6 +36,11 @@ struct MaxOp {
 
 }  // namespace
 
+struct GatherItem {
+  long long p;
+  int field, comp;
+};
+
 struct mpm_ctx {
   int precision = 0;
   const StepOps* ops = nullptr;
@@ -61,6 +66,11 @@ struct mpm_ctx {
   Profiler prof;
   mpm_batch* batch = nullptr;  // the mixed form runs as a batch of one scene
   int batch_scene = -1;
+  // particle value gather (curve output): pinned host and device item / value buffers
+  GatherItem *g_items_h = nullptr, *g_items_d = nullptr;
+  double *g_out_h = nullptr, *g_out_d = nullptr;
+  cudaEvent_t g_done = nullptr;
+  int g_n = 0;
   std::string err;
 };
 
@@ -202,6 +212,43 @@ int batch_status(mpm_ctx* c, int r) {
   return r;
 }
 
+// particle values of a gather request (fields of the FP64 forms: double
+// arrays; failure bytes; cell / node ids as integers)
+__global__ void k_gather(DevState<double, double> s, long long np, const GatherItem* it, int n, double* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long long p = it[k].p, c = it[k].comp;
+  double v = 0.0;
+  switch (it[k].field) {
+    case MPM_P_XP: v = s.xp[c * np + p]; break;
+    case MPM_P_XX: v = s.xx[c * np + p]; break;
+    case MPM_P_VXP: v = s.vxp[c * np + p]; break;
+    case MPM_P_FXP: v = s.fxp[c * np + p]; break;
+    case MPM_P_XN: v = s.xn[c * np + p]; break;
+    case MPM_P_XXN: v = s.xxn[c * np + p]; break;
+    case MPM_P_VOL: v = s.vol[p]; break;
+    case MPM_P_SIG_Y: v = s.sig_y[p]; break;
+    case MPM_P_SM: v = s.sm[p]; break;
+    case MPM_P_SEQV: v = s.seqv[p]; break;
+    case MPM_P_SD: v = s.sd[c * np + p]; break;
+    case MPM_P_FP: v = s.fp[c * np + p]; break;
+    case MPM_P_EPEFF: v = s.epeff[p]; break;
+    case MPM_P_CELSIUS: v = s.celsius[p]; break;
+    case MPM_P_DMG: v = s.dmg[p]; break;
+    case MPM_P_LT: v = s.lt[p]; break;
+    case MPM_P_IE: v = s.ie[p]; break;
+    case MPM_P_MASS: v = s.mass[p]; break;
+    case MPM_P_CP: v = s.cp[p]; break;
+    case MPM_P_Q: v = s.q[p]; break;
+    case MPM_P_FAILURE: v = s.failure[p] ? 1.0 : 0.0; break;
+    case MPM_P_ICELL: v = s.icell[p]; break;
+    case MPM_P_CENTERICELL: v = s.centericell[p]; break;
+    case MPM_P_INODE: v = s.inode[p]; break;
+    default: v = 0.0; break;
+  }
+  out[k] = v;
+}
+
 // ------------------------------------------------------------- set-up
 
 int derive_setup(mpm_ctx* c, const mpm_deck* d, std::vector<double>& host_vol, std::vector<double>& sig_y,
@@ -302,6 +349,11 @@ int enqueue_step(mpm_ctx* c) {
 
 void free_ctx(mpm_ctx* c) {
   if (!c) return;
+  if (c->g_items_h) cudaFreeHost(c->g_items_h);
+  if (c->g_out_h) cudaFreeHost(c->g_out_h);
+  if (c->g_items_d) cudaFree(c->g_items_d);
+  if (c->g_out_d) cudaFree(c->g_out_d);
+  if (c->g_done) cudaEventDestroy(c->g_done);
   if (c->batch) mpm_batch_destroy(c->batch);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   for (void* p : c->allocs) cudaFree(p);
@@ -804,6 +856,53 @@ int mpm_kernel_stats(mpm_ctx* c, int k, char* name, int namelen, int64_t* launch
   if (launches) *launches = c->prof.n[k];
   if (total_ms) *total_ms = c->prof.ms[k];
   return MPM_OK;
+}
+
+int mpm_gather_async(mpm_ctx* c, int n, const int64_t* particle, const int* field, const int* component) {
+  if (!c || n < 0 || n > MPM_GATHER_MAX || (n > 0 && (!particle || !field || !component)))
+    return set_err(c, MPM_ERR_ARG, "bad gather request");
+  if (c->batch) return batch_status(c, mpm_batch_scene_gather_async(c->batch, c->batch_scene, n, particle, field, component));
+  for (int k = 0; k < n; ++k) {
+    const int nc = mpm_field_components(field[k]);
+    if (field[k] < MPM_P_XP || field[k] > MPM_P_INODE || nc == 0 || component[k] < 0 || component[k] >= nc ||
+        particle[k] < 0 || particle[k] >= c->g.np)
+      return set_err(c, MPM_ERR_ARG, "gather item %d: particle %lld field %d component %d", k,
+                     (long long)particle[k], field[k], component[k]);
+    if (field[k] == MPM_P_FP && !c->g.uvfp) return set_err(c, MPM_ERR_ARG, "deformation gradient is not tracked");
+    if (field[k] == MPM_P_VOL0) return set_err(c, MPM_ERR_ARG, "field %d is not available", field[k]);
+  }
+  if (!c->g_items_h) {
+    CK(cudaMallocHost((void**)&c->g_items_h, sizeof(GatherItem) * MPM_GATHER_MAX));
+    CK(cudaMallocHost((void**)&c->g_out_h, sizeof(double) * MPM_GATHER_MAX));
+    CK(cudaMalloc((void**)&c->g_items_d, sizeof(GatherItem) * MPM_GATHER_MAX));
+    CK(cudaMalloc((void**)&c->g_out_d, sizeof(double) * MPM_GATHER_MAX));
+    CK(cudaEventCreateWithFlags(&c->g_done, cudaEventDisableTiming));
+  }
+  CK(cudaEventSynchronize(c->g_done));  // the previous gather has released the staging buffers
+  for (int k = 0; k < n; ++k) c->g_items_h[k] = GatherItem{(long long)particle[k], field[k], component[k]};
+  c->g_n = n;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(c->g_items_d, c->g_items_h, sizeof(GatherItem) * n, cudaMemcpyHostToDevice, c->stream));
+    k_gather<<<(n + 127) / 128, 128, 0, c->stream>>>(c->st, c->g.np, c->g_items_d, n, c->g_out_d);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->g_out_h, c->g_out_d, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaEventRecord(c->g_done, c->stream));
+  return MPM_OK;
+}
+
+int mpm_gather_wait(mpm_ctx* c, double* out) {
+  if (!c || !out) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return batch_status(c, mpm_batch_scene_gather_wait(c->batch, out));
+  if (!c->g_done) return set_err(c, MPM_ERR_STATE, "no gather in flight");
+  CK(cudaEventSynchronize(c->g_done));
+  memcpy(out, c->g_out_h, sizeof(double) * (size_t)c->g_n);
+  return MPM_OK;
+}
+
+int mpm_gather(mpm_ctx* c, int n, const int64_t* particle, const int* field, const int* component, double* out) {
+  int r = mpm_gather_async(c, n, particle, field, component);
+  return r ? r : mpm_gather_wait(c, out);
 }
 
 int mpm_algorithmic_bytes(mpm_ctx* c, double* bytes) {

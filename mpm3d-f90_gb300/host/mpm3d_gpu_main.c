@@ -2,7 +2,14 @@
  * mpm3d_gpu_main.c -- command-line driver: the MPM3D.f90 time loop
  * (MPM3D.f90:62-160) over the C ABI of libmpm3d_gpu.
  *
- *   mpm3d_gpu deck.mpm [--precision fp64|native|mixed] [--steps N] [--report K]
+ *   mpm3d_gpu deck.mpm [--precision fp64|native|mixed] [--steps N] [--report K] [--no-output]
+ *
+ * It writes the reference's result files next to the deck (job = the deck
+ * path without its extension): <job>_curv.dat, EnergyPlot.dat and
+ * MomentumPlot.dat every step (OutCurve, fed by a gather of the curve
+ * particles' values behind each step), and with 'tecp' / 'para' the
+ * animation frames at t = 0 and every OutTime (OutAnim / OutAnimPV, from full
+ * field downloads).
  *
  * Without --steps it runs until the reference's exit test is met (CurrentTime >
  * EndTime, or for quasi-static decks CurrentTime > EndTime, KE/(KE+IE) < 0.005
@@ -16,11 +23,37 @@
 #include <time.h>
 
 #include "mpm3d_gpu.h"
+#include "mpm_output.h"
 
 static double now_s(void) {
   struct timespec ts;
   clock_gettime(CLOCK_MONOTONIC, &ts);
   return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* OutAnim / OutAnimPV frame from the device state (only with 'tecp' / 'para') */
+static int anim_frame(mpm_ctx* c, const mpm_deck* d, mpm_output* out, const double* s) {
+  if (!(d->flags & (MPM_F_TECPLOT | MPM_F_PARAVIEW))) return 0;
+  const int64_t np = d->nb_particle;
+  static const struct {
+    int field, ncomp;
+  } want[] = {{MPM_P_XP, 3},   {MPM_P_VXP, 3},  {MPM_P_FXP, 3},     {MPM_P_MASS, 1}, {MPM_P_SEQV, 1},
+              {MPM_P_EPEFF, 1}, {MPM_P_SM, 1},   {MPM_P_VOL, 1},     {MPM_P_IE, 1},   {MPM_P_CELSIUS, 1},
+              {MPM_P_CP, 1},    {MPM_P_DMG, 1},  {MPM_P_SD, 6},      {MPM_P_FAILURE, 1}, {MPM_P_ICELL, 1}};
+  enum { NW = sizeof want / sizeof want[0] };
+  double* a[NW];
+  for (int k = 0; k < NW; ++k) {
+    a[k] = (double*)malloc(sizeof(double) * (size_t)(want[k].ncomp * np));
+    if (!a[k] || mpm_download(c, want[k].field, a[k])) { /* a form without this field */
+      free(a[k]);
+      a[k] = NULL;
+    }
+  }
+  mpm_particle_view v = {a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10], a[11], a[12], a[13], a[14]};
+  int st = mpm_output_anim(out, s, &v);
+  for (int k = 0; k < NW; ++k) free(a[k]);
+  if (st) fprintf(stderr, "animation output error %d\n", st);
+  return st;
 }
 
 int main(int argc, char** argv) {
@@ -30,6 +63,7 @@ int main(int argc, char** argv) {
   }
   int precision = MPM_FP64_STRICT;
   long steps = -1, report = 100;
+  int write_output = 1;
   for (int i = 2; i < argc; ++i) {
     if (!strcmp(argv[i], "--precision") && i + 1 < argc) {
       ++i;
@@ -38,6 +72,8 @@ int main(int argc, char** argv) {
       steps = atol(argv[++i]);
     } else if (!strcmp(argv[i], "--report") && i + 1 < argc) {
       report = atol(argv[++i]);
+    } else if (!strcmp(argv[i], "--no-output")) {
+      write_output = 0;
     }
   }
   char err[256] = {0};
@@ -55,6 +91,28 @@ int main(int argc, char** argv) {
   }
   double s[MPM_NSCALARS];
   mpm_get_scalars(c, s);
+  /* result files (InputPara / OutCurve / OutAnim) */
+  mpm_output* out = NULL;
+  int ncur = 0;
+  int64_t cp_[64];
+  int cf_[64], cc_[64];
+  double cv_[64];
+  char job[1024];
+  snprintf(job, sizeof job, "%s", argv[1]);
+  {
+    char* base = strrchr(job, '/');
+    char* dot = strchr(base ? base + 1 : job, '.');
+    if (dot) *dot = 0;
+  }
+  if (write_output) {
+    if ((st = mpm_output_open(d, job, NULL, &out))) {
+      fprintf(stderr, "cannot open the result files of %s\n", job);
+      return 1;
+    }
+    ncur = mpm_output_curve_items(out, cp_, cf_, cc_, 64);
+    if (anim_frame(c, d, out, s)) return 1;
+  }
+  float plt = (float)d->outtime; /* plt is a default REAL (MPM3D.f90:34, 45) */
   printf("particles %lld  grid nodes %lld  DT = %10.3e\nsolving...\n", (long long)mpm_nb_particle(c),
          (long long)mpm_nb_gridnode(c), s[2]);
   const int quasi = (d->flags & MPM_F_QUASILOAD) != 0;
@@ -64,7 +122,16 @@ int main(int argc, char** argv) {
     if (steps >= 0 && n >= steps) break;
     if ((st = mpm_step(c))) break;
     ++n;
+    if (out && ncur > 0 && (st = mpm_gather_async(c, ncur, cp_, cf_, cc_))) break;
     if ((st = mpm_get_scalars(c, s))) break; /* exit test needs CurrentTime */
+    if (out) {
+      if (ncur > 0 && (st = mpm_gather_wait(c, cv_))) break;
+      if ((st = mpm_output_curve(out, s, cv_))) break;
+      if (s[1] >= (double)plt) {
+        plt = plt + (float)d->outtime;
+        if ((st = anim_frame(c, d, out, s))) break;
+      }
+    }
     if (report > 0 && n % report == 0)
       printf(" Step=%6ld   T=%10.3e   DT=%10.3e   K.E.=%10.3e  T.E.=%10.3e\n", n, s[1], s[2], s[3], s[3] + s[4]);
     if (steps < 0) {
@@ -84,6 +151,7 @@ int main(int argc, char** argv) {
   const double np = (double)mpm_nb_particle(c);
   printf("** steps %ld  elapsed %.4f s\n** Time per particle cycle: %12.4f nanoseconds\n", n, t,
          1e9 * t / np / (double)(n > 0 ? n : 1));
+  mpm_output_close(out);
   mpm_destroy(c);
   mpm_deck_free(d);
   return 0;

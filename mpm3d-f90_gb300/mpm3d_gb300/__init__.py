@@ -126,6 +126,18 @@ def library() -> ctypes.CDLL:
         "mpm_batch_get_option": (i, [vp, i]),
         "mpm_batch_profile_enable": (i, [vp, i]),
         "mpm_batch_kernel_stats": (i, [vp, i, c, i, P(i64), P(d)]),
+        "mpm_gather_async": (i, [vp, i, P(i64), P(i), P(i)]),
+        "mpm_gather_wait": (i, [vp, P(d)]),
+        "mpm_gather": (i, [vp, i, P(i64), P(i), P(i), P(d)]),
+        "mpm_batch_scene_gather_async": (i, [vp, i, i, P(i64), P(i), P(i)]),
+        "mpm_batch_scene_gather_wait": (i, [vp, P(d)]),
+        "mpm_output_open": (i, [vp, c, c, P(vp)]),
+        "mpm_output_close": (None, [vp]),
+        "mpm_output_curve_count": (i, [vp]),
+        "mpm_output_curve_items": (i, [vp, P(i64), P(i), P(i), i]),
+        "mpm_output_curve": (i, [vp, P(d), P(d)]),
+        "mpm_output_anim": (i, [vp, P(d), vp]),
+        "mpm_format_e": (i, [c, i, i, i, d]),
         "mpm_serve_create": (i, [vp, P(vp)]),
         "mpm_serve_destroy": (None, [vp]),
         "mpm_serve_last_error": (c, [vp]),
@@ -348,6 +360,31 @@ class MpmStep:
         self._check(library().mpm_algorithmic_bytes(self._h, ctypes.byref(b)))
         return b.value
 
+    # -- a few particles' values (curve output)
+    @staticmethod
+    def _items(items):
+        n = len(items)
+        p = (ctypes.c_int64 * max(1, n))(*[int(x[0]) for x in items])
+        f = (ctypes.c_int * max(1, n))(*[FIELDS[x[1]] if isinstance(x[1], str) else int(x[1]) for x in items])
+        c = (ctypes.c_int * max(1, n))(*[int(x[2]) if len(x) > 2 else 0 for x in items])
+        return n, p, f, c
+
+    def gather_async(self, items) -> None:
+        """Enqueue a gather of (particle, field[, component]) values behind the
+        work on the context's stream."""
+        n, p, f, c = self._items(items)
+        self._n_gather = n
+        self._check(library().mpm_gather_async(self._h, n, p, f, c))
+
+    def gather_wait(self) -> np.ndarray:
+        out = np.zeros(max(1, self._n_gather))
+        self._check(library().mpm_gather_wait(self._h, _dptr(out)))
+        return out[: self._n_gather]
+
+    def gather(self, items) -> np.ndarray:
+        self.gather_async(items)
+        return self.gather_wait()
+
     def device_bytes(self) -> int:
         return int(library().mpm_device_bytes(self._h))
 
@@ -471,6 +508,77 @@ class Batch:
         return int(library().mpm_batch_scene_count(self._h))
 
 
+class _ParticleView(ctypes.Structure):
+    _fields_ = [(n, ctypes.POINTER(ctypes.c_double)) for n in
+                ("xp", "vxp", "fxp", "mass", "seqv", "epeff", "sm", "vol", "ie", "celsius", "cp", "dmg", "sd",
+                 "failure", "icell")]
+
+
+def format_e(w: int, d: int, x: float) -> str:
+    """Fortran Ew.d as gfortran writes it."""
+    b = ctypes.create_string_buffer(64)
+    library().mpm_format_e(b, 64, int(w), int(d), float(x))
+    return b.value.decode()
+
+
+class Output:
+    """The reference's result files (curves, energy / momentum plots,
+    Tecplot or ParaView animation) for a deck, written from host arrays."""
+
+    VIEW_FIELDS = {"xp": "Xp", "vxp": "VXp", "fxp": "FXp", "mass": "mass", "seqv": "Seqv", "epeff": "epeff",
+                   "sm": "SM", "vol": "VOL", "ie": "ie", "celsius": "celsius_t", "cp": "cp", "dmg": "DMG",
+                   "sd": "SD", "failure": "failure", "icell": "icell"}
+
+    def __init__(self, deck: Deck, job: str, plot_dir: Optional[str] = None):
+        h = ctypes.c_void_p()
+        st = library().mpm_output_open(deck.handle, job.encode(), plot_dir.encode() if plot_dir else None,
+                                       ctypes.byref(h))
+        if st:
+            raise MpmError(st, f"cannot open the result files of {job}")
+        self._h = h
+        self._deck = deck
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            library().mpm_output_close(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def curve_items(self) -> list:
+        n = library().mpm_output_curve_items(self._h, None, None, None, 0)
+        p = (ctypes.c_int64 * max(1, n))()
+        f = (ctypes.c_int * max(1, n))()
+        c = (ctypes.c_int * max(1, n))()
+        library().mpm_output_curve_items(self._h, p, f, c, n)
+        return [(p[k], f[k], c[k]) for k in range(n)]
+
+    def curve(self, scalars, values) -> None:
+        s = np.ascontiguousarray(scalars, dtype=np.float64)
+        v = np.ascontiguousarray(values if len(values) else [0.0], dtype=np.float64)
+        st = library().mpm_output_curve(self._h, _dptr(s), _dptr(v))
+        if st:
+            raise MpmError(st, "curve output")
+
+    def anim(self, scalars, fields: dict) -> None:
+        """fields: name (as in the view: xp, vxp, ..., icell) -> array in deck order."""
+        keep = {}
+        view = _ParticleView()
+        for k in self.VIEW_FIELDS:
+            a = fields.get(k)
+            if a is not None:
+                keep[k] = np.ascontiguousarray(a, dtype=np.float64).ravel()
+                setattr(view, k, _dptr(keep[k]))
+        s = np.ascontiguousarray(scalars, dtype=np.float64)
+        st = library().mpm_output_anim(self._h, _dptr(s), ctypes.byref(view))
+        if st:
+            raise MpmError(st, "animation output")
+
+
 class _ServeConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("chunk_steps", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_int64),
                 ("max_scenes", ctypes.c_int), ("autotune", ctypes.c_int), ("policy", ctypes.c_int),
@@ -591,5 +699,5 @@ class Server:
         return True
 
 
-__all__ = ["Deck", "MpmStep", "Batch", "Server", "serve_plan", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
+__all__ = ["Deck", "MpmStep", "Batch", "Server", "Output", "format_e", "serve_plan", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
            "LIB_PATH"]

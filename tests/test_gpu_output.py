@@ -1,0 +1,80 @@
+"""Curve output fed by the device gather: the gathered values equal full
+downloads (FP64 and mixed forms), and the curve / energy / momentum files of
+the FP64 strict form equal those written from the CPU oracle's state."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+EXTRA = ["curv seqv 3", "curv disz 40", "curv stsx 7", "curv velz 12", "curv pres 100", "curv fail 5",
+         "curv damg 9", "curv cels 2", "outr seqv", "outr pres"]
+
+
+def _text():
+    from mpm3d_gb300 import decks
+    return decks.generic_block(
+        "1 john 8930 1.17e11 0.35 9e7 2.92e8 0.31 0.025 1.09 293 1356 383 1", dp=4e-4,
+        velocity=(0.0, 0.0, -150.0), rho=8930.0, dtscale=0.2, gravity=None, extra=EXTRA)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gather_equals_download(built, precision):
+    from mpm3d_gb300 import Deck, MpmStep
+    d = Deck.parse(_text())
+    s = MpmStep(d, precision)
+    s.run(25)
+    items = [(0, "Xp", 2), (17, "VXp", 1), (5, "SD", 2), (9, "SM"), (33, "Seqv"), (2, "ie"), (40, "epeff"),
+             (11, "failure"), (3, "VOL"), (63, "celsius_t")]
+    got = s.gather(items)
+    for (p, f, *c), v in zip(items, got):
+        full = s.download(f)
+        ref = full[c[0] if c else 0][p] if full.ndim == 2 else full[p]
+        assert v == ref, (f, p)
+    # asynchronous form: enqueued behind further steps
+    s.step()
+    s.gather_async(items[:3])
+    later = s.gather_wait()
+    assert later[0] == s.download("Xp")[2][0]
+
+
+def test_curve_files_match_oracle(gpu_mod, oracle_mod, tmp_path):
+    from mpm3d_gb300 import Deck, MpmStep, Output
+    text = _text()
+    d = Deck.parse(text)
+    g = MpmStep(d, "fp64")
+    o = oracle_mod.Oracle(deck_text=text, libm="project")
+    (tmp_path / "gpu").mkdir()
+    (tmp_path / "cpu").mkdir()
+    og = Output(d, str(tmp_path / "gpu" / "run"))
+    oc = Output(d, str(tmp_path / "cpu" / "run"))
+    items = og.curve_items()
+    assert len(items) == 9  # eight curves with a particle value; stsx takes two
+    for _ in range(40):
+        g.step()
+        o.step()
+        sg = np.array(list(g.scalars().values()))
+        so = np.array(list(o.scalars().values()))
+        og.curve(sg, g.gather(items))
+        vals = []
+        for p, f, c in items:
+            name = [k for k, v in gpu_mod.FIELDS.items() if v == f][0]
+            a = o.download(name)
+            vals.append(a[c][p] if a.ndim == 2 else a[p])
+        oc.curve(so, vals)
+    og.close()
+    oc.close()
+    for f in ["run_curv.dat", "EnergyPlot.dat", "MomentumPlot.dat"]:
+        a = (tmp_path / "gpu" / f).read_text()
+        b = (tmp_path / "cpu" / f).read_text()
+        assert len(a.splitlines()) == (41 if f == "run_curv.dat" else 40)
+        if f != "MomentumPlot.dat":
+            assert a == b, f
+            continue
+        # energies and momentum are sums over particles; the GPU's fixed
+        # reduction tree and the oracle's sequential loop round differently,
+        # which shows only in components that are zero up to rounding
+        ra = np.array([[float(x) for x in ln.split()] for ln in a.splitlines()])
+        rb = np.array([[float(x) for x in ln.split()] for ln in b.splitlines()])
+        scale = np.abs(rb[:, 1:]).max()
+        assert np.all(ra[:, 0] == rb[:, 0])
+        assert np.abs(ra[:, 1:] - rb[:, 1:]).max() <= 1e-12 * scale
