@@ -858,6 +858,135 @@ int mpm_kernel_stats(mpm_ctx* c, int k, char* name, int namelen, int64_t* launch
   return MPM_OK;
 }
 
+// persistent particle fields of a snapshot (the grid and per-step data are
+// recomputed by every step)
+static const int kSnapFields[] = {MPM_P_XP,  MPM_P_XX,      MPM_P_VXP, MPM_P_FXP, MPM_P_XN,    MPM_P_XXN,
+                                  MPM_P_VOL, MPM_P_SIG_Y,   MPM_P_SM,  MPM_P_SEQV, MPM_P_SD,   MPM_P_FP,
+                                  MPM_P_EPEFF, MPM_P_CELSIUS, MPM_P_DMG, MPM_P_LT, MPM_P_IE,   MPM_P_MASS,
+                                  MPM_P_CP,  MPM_P_Q,       MPM_P_FAILURE};
+static const char kSnapMagic[8] = {'M', 'P', 'M', '3', 'D', 'S', 'N', '1'};
+
+struct SnapHeader {
+  char magic[8];
+  int32_t precision, nfields;
+  int64_t np, nn, ncell;
+  int32_t scalars_bytes, uvfp;
+  uint64_t deck_hash;  // geometry, materials and particle masses of the context's deck
+};
+
+// FNV-1a over the set-up a snapshot belongs to
+static uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+static int deck_hash(mpm_ctx* c, uint64_t* out) {
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(h, &c->g, sizeof c->g);
+  h = fnv1a(h, c->mats.data(), sizeof(DevMaterial) * c->mats.size());
+  std::vector<double> m((size_t)c->g.np);
+  CK(cudaMemcpy(m.data(), c->st.mass, sizeof(double) * m.size(), cudaMemcpyDeviceToHost));
+  *out = fnv1a(h, m.data(), sizeof(double) * m.size());
+  return MPM_OK;
+}
+
+int mpm_snapshot_save(mpm_ctx* c, const char* path) {
+  if (!c || !path) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "snapshots cover the FP64 forms");
+  CK(cudaStreamSynchronize(c->stream));
+  FILE* f = fopen(path, "wb");
+  if (!f) return set_err(c, MPM_ERR_IO, "cannot write %s", path);
+  SnapHeader h;
+  memset(&h, 0, sizeof h);
+  memcpy(h.magic, kSnapMagic, 8);
+  h.precision = c->precision;
+  h.nfields = (int)(sizeof kSnapFields / sizeof kSnapFields[0]);
+  h.np = c->g.np;
+  h.nn = c->g.nn;
+  h.ncell = c->g.ncell;
+  h.scalars_bytes = (int)sizeof(DevScalars);
+  h.uvfp = c->g.uvfp;
+  if (int r = deck_hash(c, &h.deck_hash)) {
+    fclose(f);
+    return r;
+  }
+  bool ok = fwrite(&h, sizeof h, 1, f) == 1;
+  DevScalars sc;
+  cudaError_t e = cudaMemcpy(&sc, c->st.sc, sizeof sc, cudaMemcpyDeviceToHost);
+  ok = ok && e == cudaSuccess && fwrite(&sc, sizeof sc, 1, f) == 1;
+  std::vector<unsigned char> buf;
+  for (int k = 0; ok && k < h.nfields; ++k) {
+    const int fld = kSnapFields[k];
+    if (fld == MPM_P_FP && !c->g.uvfp) continue;
+    void* p = nullptr;
+    size_t elem = 0;
+    long long n = 0;
+    if (field_ptr(c, fld, &p, &elem, &n)) {
+      ok = false;
+      break;
+    }
+    buf.resize((size_t)n * elem);
+    e = cudaMemcpy(buf.data(), p, buf.size(), cudaMemcpyDeviceToHost);
+    int32_t tag[2] = {fld, (int32_t)elem};
+    ok = e == cudaSuccess && fwrite(tag, sizeof tag, 1, f) == 1 && fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+  }
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return set_err(c, MPM_ERR_IO, "writing %s failed", path);
+  return MPM_OK;
+}
+
+int mpm_snapshot_load(mpm_ctx* c, const char* path) {
+  if (!c || !path) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "snapshots cover the FP64 forms");
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_err(c, MPM_ERR_IO, "cannot read %s", path);
+  SnapHeader h;
+  DevScalars sc;
+  uint64_t mine = 0;
+  int r = deck_hash(c, &mine);
+  if (r) {
+    fclose(f);
+    return r;
+  }
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, kSnapMagic, 8) != 0) {
+    r = set_err(c, MPM_ERR_IO, "%s is not a snapshot", path);
+  } else if (h.precision != c->precision || h.np != c->g.np || h.nn != c->g.nn || h.ncell != c->g.ncell ||
+             h.scalars_bytes != (int)sizeof(DevScalars) || h.uvfp != c->g.uvfp || h.deck_hash != mine) {
+    r = set_err(c, MPM_ERR_STATE, "snapshot of another deck or precision");
+  } else if (fread(&sc, sizeof sc, 1, f) != 1) {
+    r = set_err(c, MPM_ERR_IO, "truncated snapshot");
+  }
+  std::vector<unsigned char> buf;
+  for (int k = 0; r == MPM_OK && k < h.nfields; ++k) {
+    const int fld = kSnapFields[k];
+    if (fld == MPM_P_FP && !c->g.uvfp) continue;
+    void* p = nullptr;
+    size_t elem = 0;
+    long long n = 0;
+    int32_t tag[2];
+    if (field_ptr(c, fld, &p, &elem, &n) || fread(tag, sizeof tag, 1, f) != 1 || tag[0] != fld ||
+        tag[1] != (int32_t)elem) {
+      r = set_err(c, MPM_ERR_STATE, "snapshot field %d does not match this context", fld);
+      break;
+    }
+    buf.resize((size_t)n * elem);
+    if (fread(buf.data(), 1, buf.size(), f) != buf.size()) {
+      r = set_err(c, MPM_ERR_IO, "truncated snapshot");
+      break;
+    }
+    cudaError_t e = cudaMemcpy(p, buf.data(), buf.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) r = cuda_err(c, e, "snapshot upload");
+  }
+  fclose(f);
+  if (r) return r;
+  CK(cudaMemcpy(c->st.sc, &sc, sizeof sc, cudaMemcpyHostToDevice));
+  return MPM_OK;
+}
+
 int mpm_gather_async(mpm_ctx* c, int n, const int64_t* particle, const int* field, const int* component) {
   if (!c || n < 0 || n > MPM_GATHER_MAX || (n > 0 && (!particle || !field || !component)))
     return set_err(c, MPM_ERR_ARG, "bad gather request");

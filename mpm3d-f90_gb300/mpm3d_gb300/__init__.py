@@ -126,6 +126,8 @@ def library() -> ctypes.CDLL:
         "mpm_batch_get_option": (i, [vp, i]),
         "mpm_batch_profile_enable": (i, [vp, i]),
         "mpm_batch_kernel_stats": (i, [vp, i, c, i, P(i64), P(d)]),
+        "mpm_snapshot_save": (i, [vp, c]),
+        "mpm_snapshot_load": (i, [vp, c]),
         "mpm_gather_async": (i, [vp, i, P(i64), P(i), P(i)]),
         "mpm_gather_wait": (i, [vp, P(d)]),
         "mpm_gather": (i, [vp, i, P(i64), P(i), P(i), P(d)]),
@@ -359,6 +361,13 @@ class MpmStep:
         b = ctypes.c_double()
         self._check(library().mpm_algorithmic_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+    # -- restart snapshot (FP64 forms)
+    def save(self, path: str) -> None:
+        self._check(library().mpm_snapshot_save(self._h, path.encode()))
+
+    def load(self, path: str) -> None:
+        self._check(library().mpm_snapshot_load(self._h, path.encode()))
 
     # -- a few particles' values (curve output)
     @staticmethod
