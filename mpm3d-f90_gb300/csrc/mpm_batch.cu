@@ -39,7 +39,28 @@ struct HostScene {
   SceneSetup su;
   long long np = 0, nn = 0, ncell = 0;
   std::vector<double> mass, x, v, fxp;  // input state, component-major, input order
+  // borrowed input state (the deck's arrays) when the scene is committed
+  // before its deck may be freed; otherwise null and the copies above are used
+  const double *bmass = nullptr, *bx = nullptr, *bv = nullptr, *bfxp = nullptr;
   std::vector<uint16_t> body_local;     // body index per particle
+  const double* in_mass() const { return bmass ? bmass : mass.data(); }
+  const double* in_x() const { return bx ? bx : x.data(); }
+  const double* in_v() const { return bv ? bv : v.data(); }
+  const double* in_fxp() const { return bfxp ? bfxp : fxp.data(); }
+  // the input state is on the device: drop the host copies
+  void release_inputs() {
+    std::vector<double>().swap(mass);
+    std::vector<double>().swap(x);
+    std::vector<double>().swap(v);
+    std::vector<double>().swap(fxp);
+    std::vector<uint16_t>().swap(body_local);
+    std::vector<double>().swap(su.vol);
+    std::vector<double>().swap(su.sig_y);
+    std::vector<double>().swap(su.ie);
+    std::vector<double>().swap(su.cp);
+    std::vector<double>().swap(su.lt);
+    bmass = bx = bv = bfxp = nullptr;
+  }
   bool resident = false;
   long long p0 = 0, n0 = 0, k0 = 0, c0 = 0, r0 = 0, nr = 0;
   int mat0 = 0, body0 = 0, index = 0;
@@ -50,6 +71,34 @@ struct HostScene {
 }  // namespace mpm
 
 namespace {
+
+// particle state of a newly admitted scene from its uploaded inputs:
+// scr = vol, sig_y, cp, lt (FP64, np each); the rest of the state starts at
+// zero, the temperature at 293 (Particle.f90:131)
+__global__ void kb_init_scene(BState s, int scene, int body0, const double* scr) {
+  const Scene& sc = s.scenes[scene];
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sc.np) return;
+  const long long NP = s.NP, np = sc.np, i = sc.p0 + k;
+  s.vol[i] = (float)scr[k];
+  s.sig_y[i] = (float)scr[np + k];
+  s.cp[i] = (float)scr[2 * np + k];
+  s.lt[i] = (float)scr[3 * np + k];
+  s.celsius[i] = 293.0f;
+  s.sm[i] = 0.f;
+  s.evol[i] = 0.f;
+  s.seqv[i] = 0.f;
+  s.epeff[i] = 0.f;
+  s.dmg[i] = 0.f;
+  s.q[i] = 0.f;
+  for (int a = 0; a < 6; ++a) s.sd[a * NP + i] = 0.f;
+  if (s.any_uvfp)
+    for (int a = 0; a < 9; ++a) s.fp[a * NP + i] = 0.f;
+  s.failure[i] = 0;
+  s.body[i] = (uint16_t)(body0 + s.body[i]);
+  s.scene[i] = (uint16_t)scene;
+  s.orig[i] = (int)k;
+}
 
 __global__ void kb_inverse(BState s) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,48 +268,31 @@ void layout_flags(mpm_batch* b) {
 
 int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
   const long long NP = s.NP, np = h->np, p0 = h->p0;
-  std::vector<float> f((size_t)np);
+  cudaStream_t st = b->stream;
   auto upd = [&](double* dst, const double* src, long long n) {
-    return cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, b->stream);
+    return cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, st);
   };
+  const double *x = h->in_x(), *v = h->in_v(), *fxp = h->in_fxp();
   for (int a = 0; a < 3; ++a) {
-    BCK(upd(s.x + a * NP + p0, h->x.data() + a * np, np));
-    BCK(upd(s.xx + a * NP + p0, h->x.data() + a * np, np));
-    BCK(upd(s.v + a * NP + p0, h->v.data() + a * np, np));
-    BCK(upd(s.fxp + a * NP + p0, h->fxp.data() + a * np, np));
+    BCK(upd(s.x + a * NP + p0, x + a * np, np));
+    BCK(cudaMemcpyAsync(s.xx + a * NP + p0, s.x + a * NP + p0, sizeof(double) * np, cudaMemcpyDeviceToDevice, st));
+    BCK(upd(s.v + a * NP + p0, v + a * np, np));
+    BCK(upd(s.fxp + a * NP + p0, fxp + a * np, np));
   }
-  BCK(upd(s.mass + p0, h->mass.data(), np));
+  BCK(upd(s.mass + p0, h->in_mass(), np));
   BCK(upd(s.ie + p0, h->su.ie.data(), np));
-  auto upf = [&](float* dst, const std::vector<double>& src) {
-    for (long long i = 0; i < np; ++i) f[i] = (float)src[i];
-    cudaError_t e = cudaMemcpyAsync(dst, f.data(), sizeof(float) * np, cudaMemcpyHostToDevice, b->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-    return e;
-  };
-  BCK(upf(s.vol + p0, h->su.vol));
-  BCK(upf(s.sig_y + p0, h->su.sig_y));
-  BCK(upf(s.cp + p0, h->su.cp));
-  BCK(upf(s.lt + p0, h->su.lt));
-  std::vector<double> t293((size_t)np, (double)293.0f);
-  BCK(upf(s.celsius + p0, t293));
-  BCK(cudaMemsetAsync(s.sm + p0, 0, sizeof(float) * np, b->stream));
-  BCK(cudaMemsetAsync(s.evol + p0, 0, sizeof(float) * np, b->stream));
-  BCK(cudaMemsetAsync(s.seqv + p0, 0, sizeof(float) * np, b->stream));
-  for (int a = 0; a < 6; ++a) BCK(cudaMemsetAsync(s.sd + a * NP + p0, 0, sizeof(float) * np, b->stream));
-  if (s.any_uvfp)
-    for (int a = 0; a < 9; ++a) BCK(cudaMemsetAsync(s.fp + a * NP + p0, 0, sizeof(float) * np, b->stream));
-  BCK(cudaMemsetAsync(s.epeff + p0, 0, sizeof(float) * np, b->stream));
-  BCK(cudaMemsetAsync(s.dmg + p0, 0, sizeof(float) * np, b->stream));
-  BCK(cudaMemsetAsync(s.q + p0, 0, sizeof(float) * np, b->stream));
-  BCK(cudaMemsetAsync(s.failure + p0, 0, np, b->stream));
-  std::vector<uint16_t> body((size_t)np), scene((size_t)np, (uint16_t)h->index);
-  for (long long i = 0; i < np; ++i) body[i] = (uint16_t)(h->body0 + h->body_local[i]);
-  std::vector<int> orig((size_t)np);
-  for (long long i = 0; i < np; ++i) orig[i] = (int)i;
-  BCK(cudaMemcpyAsync(s.body + p0, body.data(), 2 * np, cudaMemcpyHostToDevice, b->stream));
-  BCK(cudaMemcpyAsync(s.scene + p0, scene.data(), 2 * np, cudaMemcpyHostToDevice, b->stream));
-  BCK(cudaMemcpyAsync(s.orig + p0, orig.data(), 4 * np, cudaMemcpyHostToDevice, b->stream));
-  BCK(cudaStreamSynchronize(b->stream));
+  // FP64 set-up values through the force staging scratch (idle outside a
+  // step; 9 floats per particle hold 4 doubles), converted and completed by
+  // one kernel
+  double* scr = reinterpret_cast<double*>(s.fs);
+  BCK(upd(scr, h->su.vol.data(), np));
+  BCK(upd(scr + np, h->su.sig_y.data(), np));
+  BCK(upd(scr + 2 * np, h->su.cp.data(), np));
+  BCK(upd(scr + 3 * np, h->su.lt.data(), np));
+  BCK(cudaMemcpyAsync(s.body + p0, h->body_local.data(), sizeof(uint16_t) * np, cudaMemcpyHostToDevice, st));
+  kb_init_scene<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(s, h->index, h->body0, scr);
+  BCK(cudaGetLastError());
+  BCK(cudaStreamSynchronize(st));  // the host arrays may go away after this
   return MPM_OK;
 }
 
@@ -707,7 +739,10 @@ int commit(mpm_batch* b) {
   b->cub_tmp = tmp;
   b->cub_bytes = tb;
   b->key_bits = bits;
-  for (HostScene* h : b->order) h->resident = true;
+  for (HostScene* h : b->order) {
+    if (!h->resident) h->release_inputs();  // the scene's inputs are on the device now
+    h->resident = true;
+  }
   b->dirty = false;
   return MPM_OK;
 }
@@ -923,54 +958,19 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
       BCK(cudaMemcpy(out + a * h->ncell, src + a * s.NC + h->c0, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost));
     return MPM_OK;
   }
-  std::vector<int> orig((size_t)np);
-  BCK(cudaMemcpy(orig.data(), s.orig + p0, sizeof(int) * np, cudaMemcpyDeviceToHost));
-  std::vector<double> dbuf((size_t)np);
-  std::vector<float> fbuf((size_t)np);
-  auto fetch_d = [&](const double* base, int a) -> cudaError_t {
-    cudaError_t e = cudaMemcpy(dbuf.data(), base + a * NP + p0, sizeof(double) * np, cudaMemcpyDeviceToHost);
-    for (long long i = 0; i < np; ++i) out[a * np + orig[i]] = dbuf[i];
-    return e;
-  };
-  auto fetch_f = [&](const float* base, int a) -> cudaError_t {
-    cudaError_t e = cudaMemcpy(fbuf.data(), base + a * NP + p0, sizeof(float) * np, cudaMemcpyDeviceToHost);
-    for (long long i = 0; i < np; ++i) out[a * np + orig[i]] = fbuf[i];
-    return e;
-  };
+  // particle fields: un-permuted on the device into a per-step scratch (the
+  // force staging array, idle between steps), one copy per component
+  const bool ok = field >= MPM_P_XP && field <= MPM_P_FAILURE && field != MPM_P_XN && field != MPM_P_XXN &&
+                  field != MPM_P_VOL0 && nc > 0 && (field != MPM_P_FP || b->any_uvfp);
+  if (!ok) return berr(b, MPM_ERR_ARG, "field %d is not available for batched scenes", field);
+  double* scratch = reinterpret_cast<double*>(s.fs);  // 9 floats per particle >= one double per particle
+  (void)NP;
+  (void)p0;
   for (int a = 0; a < nc; ++a) {
-    cudaError_t e = cudaSuccess;
-    switch (field) {
-      case MPM_P_XP: e = fetch_d(s.x, a); break;
-      case MPM_P_XX: e = fetch_d(s.xx, a); break;
-      case MPM_P_VXP: e = fetch_d(s.v, a); break;
-      case MPM_P_FXP: e = fetch_d(s.fxp, a); break;
-      case MPM_P_MASS: e = fetch_d(s.mass, a); break;
-      case MPM_P_IE: e = fetch_d(s.ie, a); break;
-      case MPM_P_VOL: e = fetch_f(s.vol, a); break;
-      case MPM_P_SIG_Y: e = fetch_f(s.sig_y, a); break;
-      case MPM_P_SM: e = fetch_f(s.sm, a); break;
-      case MPM_P_SEQV: e = fetch_f(s.seqv, a); break;
-      case MPM_P_SD: e = fetch_f(s.sd, a); break;
-      case MPM_P_FP:
-        if (!b->any_uvfp) return berr(b, MPM_ERR_ARG, "deformation gradient is not tracked");
-        e = fetch_f(s.fp, a);
-        break;
-      case MPM_P_EPEFF: e = fetch_f(s.epeff, a); break;
-      case MPM_P_CELSIUS: e = fetch_f(s.celsius, a); break;
-      case MPM_P_DMG: e = fetch_f(s.dmg, a); break;
-      case MPM_P_LT: e = fetch_f(s.lt, a); break;
-      case MPM_P_CP: e = fetch_f(s.cp, a); break;
-      case MPM_P_Q: e = fetch_f(s.q, a); break;
-      case MPM_P_FAILURE: {
-        std::vector<uint8_t> u((size_t)np);
-        e = cudaMemcpy(u.data(), s.failure + p0, np, cudaMemcpyDeviceToHost);
-        for (long long i = 0; i < np; ++i) out[orig[i]] = u[i];
-        break;
-      }
-      default:
-        return berr(b, MPM_ERR_ARG, "field %d is not available for batched scenes", field);
-    }
-    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "download: %s", cudaGetErrorString(e));
+    kb_unpermute<<<gridn(np, 256), 256, 0, b->stream>>>(s, h->index, field, a, scratch);
+    BCK(cudaGetLastError());
+    BCK(cudaMemcpyAsync(out + a * np, scratch, sizeof(double) * np, cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
   }
   return MPM_OK;
 }
@@ -1069,7 +1069,7 @@ int mpm_batch_kernel_stats(mpm_batch* b, int k, char* name, int namelen, int64_t
 
 namespace mpm {
 
-HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code) {
+HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code, bool borrow) {
   *code = MPM_OK;
   if (!d) {
     *code = MPM_ERR_ARG;
@@ -1099,10 +1099,17 @@ HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code
   h->nn = h->su.g.nn;
   h->ncell = h->su.g.ncell;
   h->drdamp = !!(d->flags & MPM_F_DRDAMP);
-  h->mass.assign(d->mass, d->mass + h->np);
-  h->x.assign(d->xp, d->xp + 3 * h->np);
-  h->v.assign(d->vxp, d->vxp + 3 * h->np);
-  h->fxp.assign(d->fxp, d->fxp + 3 * h->np);
+  if (borrow) {
+    h->bmass = d->mass;
+    h->bx = d->xp;
+    h->bv = d->vxp;
+    h->bfxp = d->fxp;
+  } else {
+    h->mass.assign(d->mass, d->mass + h->np);
+    h->x.assign(d->xp, d->xp + 3 * h->np);
+    h->v.assign(d->vxp, d->vxp + 3 * h->np);
+    h->fxp.assign(d->fxp, d->fxp + 3 * h->np);
+  }
   h->body_local.assign((size_t)h->np, 0);
   for (int bo = 0; bo < d->nb_body; ++bo)
     for (long long p = d->bodies[bo].par_begin; p < d->bodies[bo].par_end; ++p) h->body_local[p] = (uint16_t)bo;
@@ -1110,6 +1117,8 @@ HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code
 }
 
 void scene_free(HostScene* h) { delete h; }
+
+const SceneSetup& scene_setup_of(const HostScene* h) { return h->su; }
 
 long long scene_np(const HostScene* h) { return h->np; }
 

@@ -6,12 +6,18 @@
 #include <vector>
 
 #include "mpm3d_gpu.h"
+#include "mpm_setup.h"
 
 namespace mpm {
 
 struct HostScene;
-// stage a scene from a deck on any thread (nullptr + code/err on failure)
-HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code);
+// stage a scene from a deck on any thread (nullptr + code/err on failure);
+// with borrow the deck's particle arrays are used in place, so the scene must
+// be committed before the deck may be freed
+HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code, bool borrow = false);
+// the scene's set-up (geometry, materials; per-particle inputs are released
+// once the scene is resident)
+const SceneSetup& scene_setup_of(const HostScene* h);
 void scene_free(HostScene* h);
 long long scene_np(const HostScene* h);
 long long scene_device_bytes(const HostScene* h);

@@ -1347,13 +1347,11 @@ struct GatherItem {
   int field, comp;
 };
 
-__global__ void kb_gather(BState b, int scene, const GatherItem* it, int n, double* out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const Scene& sc = b.scenes[scene];
-  const long long NP = b.NP, i = b.inv[sc.p0 + it[k].p], c = it[k].comp;
+// value of particle field `field` (component c) at storage position i
+__device__ __forceinline__ double field_value(const BState& b, int field, long long c, long long i) {
+  const long long NP = b.NP;
   double v = 0.0;
-  switch (it[k].field) {
+  switch (field) {
     case MPM_P_XP: v = b.x[c * NP + i]; break;
     case MPM_P_XX: v = b.xx[c * NP + i]; break;
     case MPM_P_VXP: v = b.v[c * NP + i]; break;
@@ -1375,7 +1373,22 @@ __global__ void kb_gather(BState b, int scene, const GatherItem* it, int n, doub
     case MPM_P_FAILURE: v = b.failure[i] ? 1.0 : 0.0; break;
     default: v = 0.0; break;
   }
-  out[k] = v;
+  return v;
+}
+
+__global__ void kb_gather(BState b, int scene, const GatherItem* it, int n, double* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const Scene& sc = b.scenes[scene];
+  out[k] = field_value(b, it[k].field, it[k].comp, b.inv[sc.p0 + it[k].p]);
+}
+
+// one component of a particle field of a scene in deck order (downloads)
+__global__ void kb_unpermute(BState b, int scene, int field, int comp, double* dst) {
+  const Scene& sc = b.scenes[scene];
+  const long long k = btid();
+  if (k >= sc.np) return;
+  dst[k] = field_value(b, field, comp, b.inv[sc.p0 + k]);
 }
 
 }  // namespace bm

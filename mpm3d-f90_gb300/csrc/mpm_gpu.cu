@@ -22,6 +22,7 @@
 
 #include "mpm3d_gpu.h"
 #include "mpm_gpu_internal.cuh"
+#include "mpm_batch_host.h"
 #include "mpm_setup.h"
 
 using namespace mpm;
@@ -429,24 +430,26 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
   }
   c->flags = d->flags;
   c->drdamp = !!(d->flags & MPM_F_DRDAMP);
-  std::vector<double> vol, sig_y, ie, cp, lt;
-  std::vector<uint8_t> fix, bd;
-  int r = derive_setup(c, d, vol, sig_y, ie, cp, lt, fix, bd);
-  if (r) {
-    g_lib_error = c->err;
-    free_ctx(c);
-    return r;
-  }
   if (precision == MPM_MIXED) {
-    // the mixed form is the batched engine running a batch of one scene
-    if ((r = mpm_batch_create(c->device, &c->batch))) {
-      set_err(c, r, "batch create failed");
-      g_lib_error = c->err;
-      free_ctx(c);
-      return r;
+    // the mixed form is the batched engine running a batch of one scene; the
+    // deck's arrays are uploaded in place (committed before returning)
+    int r = mpm_batch_create(c->device, &c->batch);
+    std::string err;
+    int code = MPM_OK;
+    mpm::HostScene* h = r ? nullptr : mpm::scene_stage(d, 0, err, &code, true);
+    if (!r && !h) r = code;
+    if (!r) {
+      mpm::batch_insert(c->batch, h, &c->batch_scene);
+      c->g = mpm::scene_setup_of(h).g;
+      c->mats = mpm::scene_setup_of(h).mats;
+      c->bodies = mpm::scene_setup_of(h).bodies;
+      r = mpm_batch_commit(c->batch);
+      if (r) err = mpm_batch_last_error(c->batch);
+    } else if (err.empty() && c->batch) {
+      err = "batch create failed";
     }
-    if ((r = mpm_batch_add(c->batch, d, 0, &c->batch_scene)) || (r = mpm_batch_commit(c->batch))) {
-      set_err(c, r, "%s", mpm_batch_last_error(c->batch));
+    if (r) {
+      set_err(c, r, "%s", err.c_str());
       g_lib_error = c->err;
       free_ctx(c);
       return r;
@@ -454,6 +457,14 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     c->bytes = mpm_batch_device_bytes(c->batch);
     *out = c;
     return MPM_OK;
+  }
+  std::vector<double> vol, sig_y, ie, cp, lt;
+  std::vector<uint8_t> fix, bd;
+  int r = derive_setup(c, d, vol, sig_y, ie, cp, lt, fix, bd);
+  if (r) {
+    g_lib_error = c->err;
+    free_ctx(c);
+    return r;
   }
   Geometry& g = c->g;
   const long long np = g.np, nn = g.nn, nc = g.ncell;
@@ -630,9 +641,9 @@ int mpm_step_phase(mpm_ctx* c, int phase) {
 
 int mpm_step(mpm_ctx* c) {
   if (!c) return set_err(nullptr, MPM_ERR_ARG, "ctx is NULL");
-  if (c->batch) return batch_status(c, mpm_batch_run(c->batch, 1, 0));
-  ProfScope ps(c);
-  return enqueue_step(c);
+  // one step replayed from the context's one-step CUDA graph
+  if (c->batch) return batch_status(c, mpm_batch_run(c->batch, 1, 1));
+  return mpm_run(c, 1, 1);
 }
 
 static int ensure_graph(mpm_ctx* c, int nsteps) {
