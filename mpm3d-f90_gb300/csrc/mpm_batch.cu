@@ -170,6 +170,7 @@ struct mpm_batch {
   size_t cub_bytes = 0;
   int key_bits = 1;
   int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
+  int stress_type = 0;  // material type shared by every material of the batch (0: several)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
@@ -264,6 +265,13 @@ void layout_flags(mpm_batch* b) {
     if (g.uvfp) b->any_uvfp = 1;
     if (h->drdamp) b->any_dr = 1;
   }
+  b->stress_type = -1;
+  for (HostScene* h : b->order)
+    for (const DevMaterial& m : h->su.mats) {
+      if (b->stress_type == -1) b->stress_type = m.mat_type;
+      else if (b->stress_type != m.mat_type) b->stress_type = 0;
+    }
+  if (b->stress_type < 0) b->stress_type = 0;
 }
 
 int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
@@ -349,7 +357,13 @@ int enqueue_step(mpm_batch* b) {
   auto stress = [&](int usf_pass) -> int {
     prof_begin(K_STRESS, st);
     if (b->any_sgmp) kb_sg_centre_gradient<<<gridn(s.NC, nb), nb, 0, st>>>(s, usf_pass);
-    kb_stress<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass);
+    switch (b->stress_type) {  // the one material type of the batch, if any
+      case 1: kb_stress<1><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
+      case 9: kb_stress<9><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
+      case 10: kb_stress<10><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
+      case 11: kb_stress<11><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
+      default: kb_stress<0><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
+    }
     prof_end(K_STRESS, st);
     if (b->any_jc) {
       prof_begin(K_DEPEFF, st);

@@ -661,6 +661,8 @@ __global__ void kb_sg_centre_mass(BState b, int momentum_only) {
 // ParticleStressUpdate + Constitution for one particle (FP32). The stress pass
 // runs twice per step: before the force transfer for USF scenes (usf_pass 1)
 // and after the position update for USL / MUSL scenes (usf_pass 0).
+// MT != 0: a batch whose materials are all of type MT (fewer registers)
+template <int MT>
 __global__ void kb_stress(BState b, int usf_pass) {
   using P = PMixed;
   using R = float;
@@ -768,7 +770,8 @@ __global__ void kb_stress(BState b, int usf_pass) {
   ps.evol = b.evol[i];
   const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
   CResult<R> res;
-  constitution<P>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2, res);
+  constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2,
+                      res);
   if (res.negative_volume) atomicOr(&b.sst[s].status, (unsigned)ST_NEGATIVE_VOLUME);
   if (!res.eos_ok) atomicOr(&b.sst[s].status, (unsigned)ST_BAD_EOS);
   if (sc.has_jc) {

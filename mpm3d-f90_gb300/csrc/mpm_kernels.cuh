@@ -374,8 +374,9 @@ struct CResult {
 
 // Constitution (Constitution.f90:79-368) for one particle: volume update,
 // material constants, the material model of the particle's material and the
-// write-back of Constitution.f90:351-366.
-template <class P>
+// write-back of Constitution.f90:351-366. MT != 0 compiles the model of
+// material type MT only (the caller guarantees mt.mat_type == MT).
+template <class P, int MT = 0>
 __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const DevMaterial& mt,
                                              const typename P::R de[6], const typename P::R vort[3],
                                              const typename P::R deFp[3][3], const typename P::R Fpn[3][3],
@@ -493,7 +494,7 @@ __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const De
   bool eos_ok = true;
   bool defer = false;  // Johnson-Cook tail needs the carried depeff
   int tail = 0;        // 4: celsius update only, 7: failure + damage tail
-  switch (mt.mat_type) {
+  switch (MT ? MT : mt.mat_type) {
     case 1:
       sigrot(m, vort);
       m.ieinc = sig_work(m);
