@@ -350,13 +350,21 @@ int enqueue_step(mpm_batch* b) {
     kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
     prof_end(K_SCATTER_MASS, st);
   }
+  if (b->any_sgmp) {
+    prof_begin(K_SG_MASS, st);
+    kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
+    prof_end(K_SG_MASS, st);
+  }
   prof_begin(K_P2G_MASS, st);
-  if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
   prof_end(K_P2G_MASS, st);
   auto stress = [&](int usf_pass) -> int {
+    if (b->any_sgmp) {
+      prof_begin(K_SG_GRADIENT, st);
+      kb_sg_centre_gradient<<<gridn(s.NC, nb), nb, 0, st>>>(s, usf_pass);
+      prof_end(K_SG_GRADIENT, st);
+    }
     prof_begin(K_STRESS, st);
-    if (b->any_sgmp) kb_sg_centre_gradient<<<gridn(s.NC, nb), nb, 0, st>>>(s, usf_pass);
     switch (b->stress_type) {  // the one material type of the batch, if any
       case 1: kb_stress<1><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
       case 9: kb_stress<9><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
@@ -386,12 +394,20 @@ int enqueue_step(mpm_batch* b) {
     kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
     prof_end(K_SCATTER_FORCE, st);
   }
+  if (b->any_sgmp) {
+    prof_begin(K_SG_FORCE, st);
+    kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
+    prof_end(K_SG_FORCE, st);
+  }
   prof_begin(K_P2G_FORCE, st);
-  if (b->any_sgmp) kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
   prof_end(K_P2G_FORCE, st);
+  if (b->any_sgmp) {
+    prof_begin(K_SG_VELOCITY, st);
+    kb_sg_centre_velocity<<<gridn(s.NC, nb), nb, 0, st>>>(s);
+    prof_end(K_SG_VELOCITY, st);
+  }
   prof_begin(K_POSITION, st);
-  if (b->any_sgmp) kb_sg_centre_velocity<<<gridn(s.NC, nb), nb, 0, st>>>(s);
   kb_position<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_POSITION, st);
   if (b->any_musl) {
@@ -400,8 +416,12 @@ int enqueue_step(mpm_batch* b) {
       kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
       prof_end(K_SCATTER_MOM, st);
     }
+    if (b->any_sgmp) {
+      prof_begin(K_SG_MASS, st);
+      kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
+      prof_end(K_SG_MASS, st);
+    }
     prof_begin(K_P2G_MOM, st);
-    if (b->any_sgmp) kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
     prof_end(K_P2G_MOM, st);
   }
