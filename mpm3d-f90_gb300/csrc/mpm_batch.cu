@@ -330,7 +330,7 @@ int enqueue_step(mpm_batch* b) {
   tmp = b->cub_bytes;
   e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
-  if (b->any_nonsgmp) {  // occupied cells for the persistent scatters
+  {  // occupied cells (dual cells for SGMP) for the persistent scatters
     tmp = b->cub_bytes;
     e = cub::DeviceRunLengthEncode::Encode(b->cub_tmp, tmp, a.key_sorted, a.runs, a.run_counts, a.nruns, (int)a.NP,
                                            st);
@@ -343,18 +343,15 @@ int enqueue_step(mpm_batch* b) {
   // swap the particle buffer sets (node and scene arrays are shared)
   std::swap(b->A, b->B);
   BState& s = b->A;
-  const bool scatter = b->any_nonsgmp;
   const unsigned sgrid = (unsigned)std::min<long long>(b->scatter_blocks, (s.NK + kCellWarps - 1) / kCellWarps);
-  if (scatter) {
-    prof_begin(K_SCATTER_MASS, st);
-    kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
-    prof_end(K_SCATTER_MASS, st);
-  }
   if (b->any_sgmp) {
-    prof_begin(K_SG_MASS, st);
-    kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 0);
-    prof_end(K_SG_MASS, st);
+    prof_begin(K_SG_CLEAR, st);
+    kb_sg_clear<<<gridn(s.NC, nb), nb, 0, st>>>(s);
+    prof_end(K_SG_CLEAR, st);
   }
+  prof_begin(K_SCATTER_MASS, st);
+  kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
+  prof_end(K_SCATTER_MASS, st);
   prof_begin(K_P2G_MASS, st);
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
   prof_end(K_P2G_MASS, st);
@@ -389,16 +386,9 @@ int enqueue_step(mpm_batch* b) {
   prof_begin(K_FORCE_PREP, st);
   kb_force_prep<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_FORCE_PREP, st);
-  if (scatter) {
-    prof_begin(K_SCATTER_FORCE, st);
-    kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
-    prof_end(K_SCATTER_FORCE, st);
-  }
-  if (b->any_sgmp) {
-    prof_begin(K_SG_FORCE, st);
-    kb_sg_centre_force<<<gridn(s.NC, nb), nb, 0, st>>>(s);
-    prof_end(K_SG_FORCE, st);
-  }
+  prof_begin(K_SCATTER_FORCE, st);
+  kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
+  prof_end(K_SCATTER_FORCE, st);
   prof_begin(K_P2G_FORCE, st);
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
   prof_end(K_P2G_FORCE, st);
@@ -411,16 +401,9 @@ int enqueue_step(mpm_batch* b) {
   kb_position<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_POSITION, st);
   if (b->any_musl) {
-    if (scatter) {
-      prof_begin(K_SCATTER_MOM, st);
-      kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
-      prof_end(K_SCATTER_MOM, st);
-    }
-    if (b->any_sgmp) {
-      prof_begin(K_SG_MASS, st);
-      kb_sg_centre_mass<<<gridn(s.NC, nb), nb, 0, st>>>(s, 1);
-      prof_end(K_SG_MASS, st);
-    }
+    prof_begin(K_SCATTER_MOM, st);
+    kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
+    prof_end(K_SCATTER_MOM, st);
     prof_begin(K_P2G_MOM, st);
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
     prof_end(K_P2G_MOM, st);
@@ -592,10 +575,7 @@ int commit(mpm_batch* b) {
   shared.fix = al.get<uint8_t>(NN);
   shared.bd = al.get<uint8_t>(NN);
   shared.node_scene = al.get<uint16_t>(NN);
-  shared.cmg = al.get<double>(NC);
-  shared.cpx = al.get<double>(3 * NC);
-  shared.cfext = al.get<double>(3 * NC);
-  shared.cfint = al.get<double>(6 * NC);
+  shared.cacc = al.get<unsigned long long>(CQ_N * NC);
   shared.co = al.get<float>(6 * NC);
   shared.cw = al.get<float>(3 * NC);
   shared.cdefp = al.get<float>(9 * NC);
@@ -648,7 +628,7 @@ int commit(mpm_batch* b) {
     s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
     s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.inv = shared.inv; s.run_counts = shared.run_counts; s.nruns = shared.nruns; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
     s.nvel = shared.nvel; s.nacc = shared.nacc; s.acc = shared.acc; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
-    s.cmg = shared.cmg; s.cpx = shared.cpx; s.cfext = shared.cfext; s.cfint = shared.cfint; s.co = shared.co;
+    s.cacc = shared.cacc; s.co = shared.co;
     s.cw = shared.cw; s.cdefp = shared.cdefp; s.cvx = shared.cvx; s.cax = shared.cax; s.cscene = shared.cscene;
     s.setter = shared.setter; s.setter_scan = shared.setter_scan; s.dep = shared.dep; s.jc_aux = shared.jc_aux;
     s.deferred = shared.deferred; s.red_part = shared.red_part; s.rscene = shared.rscene; s.scenes = shared.scenes;
@@ -742,6 +722,7 @@ int commit(mpm_batch* b) {
   BCK(cudaMemsetAsync(shared.nvel, 0, sizeof(float4) * NN, st));
   BCK(cudaMemsetAsync(shared.nacc, 0, sizeof(float4) * NN, st));
   BCK(cudaMemsetAsync(shared.acc, 0, sizeof(unsigned long long) * 4 * NN, st));
+  if (NC) BCK(cudaMemsetAsync(shared.cacc, 0, sizeof(unsigned long long) * CQ_N * NC, st));
   // every depeff setter entry is -1 or its own index (the max-scan relies on
   // it); only Johnson-Cook scenes rewrite theirs each step
   if (b->any_jc) {
@@ -987,9 +968,19 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
   }
   if (field == MPM_C_MG || field == MPM_C_PX) {
     if (h->su.g.shape != 3) return berr(b, MPM_ERR_ARG, "no auxiliary grid (not SGMP)");
-    const double* src = field == MPM_C_MG ? s.cmg : s.cpx;
-    for (int a = 0; a < nc; ++a)
-      BCK(cudaMemcpy(out + a * h->ncell, src + a * s.NC + h->c0, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost));
+    // decoded from the fixed-point sums, one component at a time
+    double* tmp = nullptr;
+    BCK(cudaMalloc(&tmp, sizeof(double) * (size_t)std::max<long long>(h->ncell, 1)));
+    cudaError_t e = cudaSuccess;
+    for (int a = 0; a < nc && e == cudaSuccess; ++a) {
+      kb_centre_field<<<gridn(h->ncell, 256), 256, 0, b->stream>>>(s, h->index, field == MPM_C_MG ? -1 : a, tmp);
+      e = cudaGetLastError();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out + a * h->ncell, tmp, sizeof(double) * h->ncell, cudaMemcpyDeviceToHost, b->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    }
+    cudaFree(tmp);
+    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "centre field: %s", cudaGetErrorString(e));
     return MPM_OK;
   }
   // particle fields: un-permuted on the device into a per-step scratch (the

@@ -13,20 +13,20 @@
 //     node, xxn[3], xn[3]; body, scene, orig (scene-local input index)
 //   grid nodes concatenated: FP64 mg, px[3], fx[3]; FP32 float4 velocity and
 //     acceleration (for the particle gathers); fix, bd, node scene
-//   SGMP centre nodes (one per cell) concatenated: FP64 cmg, cpx[3], cfext[3],
-//     cfint[6]; FP32 co[6], cw[3], cdefp[9], cvx[3], cax[3]
+//   SGMP centre nodes (one per cell) concatenated: 64-bit fixed-point
+//     accumulators cacc[13] (mass, momentum[3], external force[3], internal
+//     force[6]); FP32 co[6], cw[3], cdefp[9], cvx[3], cax[3]
 //   sort keys: scene s owns keys [k0, k0 + nk), the last one collects the
 //     particles outside its grid; seg[k] = end of key k's particle range
 //     (kept for SGMP scenes). Linear / GIMP / B-spline: one key per cell;
 //     SGMP: one key per dual cell.
 //   P2G accumulators: acc[4][NN] 64-bit fixed point (see the scatter kernels).
 //
-// Transfers particle -> grid of linear / GIMP / B-spline scenes are
-// particle-centric scatters of FP32 contributions summed exactly in 64-bit
-// fixed point; SGMP particle -> centre-node transfers are node-centric
-// gathers over the dual cells' particle ranges with FP32 partial sums per
-// dual cell accumulated in FP64. Both are deterministic and give a scene the
-// same results alone or in a batch.
+// Transfers particle -> grid are scatters of FP32 per-cell partial sums
+// (one warp per occupied cell, or dual cell for SGMP), summed exactly in
+// 64-bit fixed point into the nodes (SGMP: the centre nodes, whose integer
+// sums the node kernels add up exactly). They are deterministic and give a
+// scene the same results alone or in a batch.
 // Transfers grid -> particle are particle-centric with shape functions
 // evaluated on the fly in FP32.
 #pragma once
@@ -90,7 +90,7 @@ struct BState {
   uint8_t *fix, *bd;
   uint16_t* node_scene;
   // SGMP centre grid
-  double *cmg, *cpx, *cfext, *cfint;   // accumulated (FP64)
+  unsigned long long* cacc;            // [CQ_N][NC] fixed-point particle -> centre sums (channels below)
   float *co, *cw, *cdefp, *cvx, *cax;  // derived from node velocities / accelerations (FP32)
   uint16_t* cscene;
   // Johnson-Cook depeff carry (indexed by scene particle range + orig)
@@ -107,6 +107,12 @@ struct BState {
 };
 
 constexpr int kChunk = 2048;  // particles per reduction chunk
+
+// SGMP centre accumulator channels (cacc[channel * NC + cell]): mass and
+// momentum (CenterNode Mg / PXg, the MUSL momentum reuses the momentum
+// channels), external force, internal force in the reference's Cfint order
+// xx, yy, zz, xy, yz, xz
+enum : int { CQ_M = 0, CQ_P = 1, CQ_FE = 4, CQ_FI = 7, CQ_N = 13 };
 
 }  // namespace bm
 }  // namespace mpm

@@ -181,11 +181,11 @@ __device__ __forceinline__ void permute_one(const BState& src, BState& dst, long
   }
 }
 
-// ------------------------------------------------- node-centric gathers
 // ------------------------------------------- deterministic P2G scatter
-// Particle -> node transfers of linear, GIMP and B-spline scenes are
-// particle-centric: each particle adds its FP32 contributions to the nodes it
-// influences. Contributions are quantised to 64-bit fixed point with a
+// Particle -> node transfers of linear, GIMP and B-spline scenes, and the
+// particle -> centre-node transfers of SGMP scenes, are scatters: each cell's
+// (dual cell's) particles add their FP32 contributions to the nodes they
+// influence. Contributions are quantised to 64-bit fixed point with a
 // per-scene, per-quantity power-of-two scale and summed with integer adds, so
 // a node's sum is exact and independent of the order of the adds (and of
 // which other scenes share the batch). The scale comes from a per-step bound
@@ -245,7 +245,7 @@ __device__ __forceinline__ int q_shift(const Scene& sc, unsigned bound_bits) {
 }
 __device__ __forceinline__ float q_scale(int sh) { return __int_as_float((sh + 127) << 23); }
 __device__ __forceinline__ long long quant(float c, float scale) { return __float2ll_rn(c * scale); }
-__device__ __forceinline__ double q_unit(int sh) { return ldexp(1.0, -sh); }
+__device__ __forceinline__ double q_unit(int sh) { return __longlong_as_double((long long)(1023 - sh) << 52); }  // 2^-sh
 
 // influence nodes of a particle along one direction: node = cell + t[k],
 // weight w[k] and derivative d[k] (per cell) -- NShape / the cpGIMP quarter
@@ -295,40 +295,141 @@ __global__ void kb_permute(BState src, BState dst) {
   block_scene_max<2>(dst, s, {Q_MASS, Q_MOM}, {bm, bv});
 }
 
-// Cell-centric form of the scatter: one warp per sort key (cell). The cell's
-// particles are staged 32 at a time in shared memory with their per-direction
-// weight (and derivative) tables for the node offsets t = -1..2 of the cell
-// (zero where the shape function has no support; linear shapes use t = 0..1,
-// B-splines t = -1..1); lane l then sums node slots l and l + 32 -- slot =
-// (tz + 1) * 16 + (ty + 1) * 4 + (tx + 1) -- over the cell's particles in
-// storage order (FP32), and adds each nonzero slot sum, quantised, to the
-// node's fixed-point accumulator. A cell's sums depend only on its own
-// particle list, so they are the same alone or in a batch.
+// Cell-centric form of the scatter: one warp per sort key (cell), over the
+// box of node offsets t = tlo .. tlo + nt - 1 per direction that the shape
+// reaches from a cell (linear 0..1, B-spline -1..1, GIMP -1..2). Lane l owns
+// box slots l and l + 32 and sums their contributions over the cell's
+// particles in storage order (FP32); each nonzero slot sum is quantised and
+// added to the node's fixed-point accumulator. A cell's sums depend only on
+// its own particle list, so they are the same alone or in a batch.
+// The shape functions are tensor products, N = Wx Wy Wz, so the work is
+// split by direction: the particles' 1-D tables (w, dw/dx) per offset, then
+// per particle and (ty, tz) the y-z factors of every channel, e.g. for the
+// force  f_x = Dx * (-s_xx Wy Wz) + Wx * (b_x Wy Wz - s_xy Dy Wz - s_xz Wy Dz),
+// shared by the nt slots that differ in tx; a slot then costs 2 multiply-adds
+// per channel and particle. Particles go 8 at a time through the warp's
+// shared workspace.
 // mode 0: mass + momentum (GridMomentumInitial), 1: momentum with the updated
 // velocities (GridMomentumMUSL), 2: force (GridMomentumUpdate).
 constexpr int kCellWarps = 8;  // warps (cells) per block
 
 template <int MODE>
 struct ScatterShape {
-  static constexpr int NV = MODE == 0 ? 4 : 3;    // channels
-  static constexpr int NQ = MODE == 2 ? 9 : 4;    // per-particle quantities staged
-  static constexpr int NT = MODE == 2 ? 24 : 12;  // per-particle table entries (w, and d for the force)
-  static constexpr int ROW = NQ + NT + 1;         // staged floats per particle (odd: no bank conflicts)
+  static constexpr int NV = MODE == 0 ? 4 : 3;   // channels
+  static constexpr int NQ = MODE == 2 ? 9 : 4;   // per-particle quantities staged
+  static constexpr int PC = 8;                   // particles per staging round (box shapes)
+  static constexpr int NPQ = MODE == 2 ? 6 : 4;  // y-z factors per (particle, ty, tz)
+  static constexpr int PQ = PC * 16 * NPQ;       // floats: y-z factors [PC][tz * 4 + ty][NPQ]
+  static constexpr int TAB = PC * 3 * 4 * 2;     // floats: (w, dw/dx) [PC][direction][t - tlo]
+  static constexpr int VAL = NQ * PC;            // floats: particle values [NQ][PC]
+  static constexpr int SROW = MODE == 2 ? 19 : 13;  // SGMP staging row: NQ values, 8 weights, 1 (odd length)
+  static constexpr int BOX = PQ + TAB + VAL;
+  static constexpr int WS = ((BOX > 32 * SROW ? BOX : 32 * SROW) + 3) / 4 * 4;  // floats per warp
 };
 
-// the scatter of one sort key (cell) by one warp; sq = the warp's staging rows
+// Corner k of the dual cell (dx, dy, dz) as a scene cell (its centre node),
+// with the reference's flat arithmetic (CenterCellNode, Grid.f90:380-418:
+// first corner plus the corner's flat offset; corners at or past the last
+// cell are dropped, and a direction with a single cell -- one dual cell --
+// spills into the next row); -1 if dropped.
+__device__ __forceinline__ long long sg_corner_cell(const Scene& sc, int dx, int dy, int dz, int k) {
+  const long long c1 = ((long long)dz * sc.NCy + dy) * sc.NCx + dx;
+  const long long cid = c1 + kCorner[k][0] + (long long)kCorner[k][1] * sc.NCx + (long long)kCorner[k][2] * sc.NCxy;
+  return cid < (long long)sc.NCxy * sc.NCz ? cid : -1;
+}
+
+// SGMP form of the scatter: the sort key is a dual cell, whose particles
+// reach the centre nodes of its 8 corners with the SGNShape weights
+// 0.125 (1 +- xi)(1 +- eta)(1 +- zeta). Lane l sums slots l, l + 32, l + 64
+// (slot = corner * channels + channel) over the dual cell's particles in
+// storage order (FP32) and adds each nonzero sum, quantised, to the centre
+// node's fixed-point accumulator (cacc). Channels: mode 0 mass and momentum
+// (CenterNode Mg, PXg), 1 momentum with the updated velocities, 2 external
+// force then internal force (Cfext, Cfint).
 template <int MODE>
-__device__ __forceinline__ void scatter_cell(BState& b, long long key, float (*sq)[ScatterShape<MODE>::ROW]) {
-  constexpr int NV = ScatterShape<MODE>::NV, NQ = ScatterShape<MODE>::NQ;
+__device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int s, int i0, int i1, int d, float* ws) {
+  constexpr int NQ = ScatterShape<MODE>::NQ;      // staged quantities, then 8 corner weights, then 1
+  constexpr int SROW = ScatterShape<MODE>::SROW;
+  constexpr int NV = MODE == 0 ? 4 : (MODE == 1 ? 3 : 9);  // channels
+  constexpr int NS = 8 * NV, KS = (NS + 31) / 32;           // slots, slots per lane
+  constexpr int CH0 = MODE == 2 ? CQ_FE : (MODE == 1 ? CQ_P : CQ_M);  // first accumulator channel
+  static_assert(NQ + 9 <= SROW, "staging row");
   const int lane = threadIdx.x & 31;
-  int i0, i1;
-  key_range(b, key, i0, i1);
-  if (i0 >= i1) return;
-  const int s = b.scene[i0];
-  const Scene& sc = b.scenes[s];
-  if (!scene_live(b, s) || sc.shape == 3 || (MODE == 1 && !sc.musl)) return;
-  const int cl = b.cell[i0];
-  if (cl < 0) return;  // the scene's off-grid bucket
+  if (d < 0) return;  // the scene's off-grid bucket
+  const int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+  const SceneState& st = b.sst[s];
+  const long long NP = b.NP, NC = b.NC;
+  // per slot: corner weight index, the staged factors (mass / force value,
+  // velocity or the 1 at the end of the row), scale, target cell
+  int wi[KS], f0[KS], f1[KS], ch[KS];
+  long long cell[KS];
+  float scale[KS], acc[KS];
+#pragma unroll
+  for (int k = 0; k < KS; ++k) {
+    const int slot = lane + 32 * k;
+    const int corner = slot / NV;
+    ch[k] = slot - corner * NV;
+    wi[k] = NQ + (corner & 7);
+    cell[k] = slot < NS ? sg_corner_cell(sc, dx, dy, dz, corner) : -1;
+    if (MODE == 2) {
+      f0[k] = ch[k] < 3 ? 6 + ch[k] : ch[k] - 3;  // fs: sigma*vol xx..xz (0..5), external force (6..8)
+      f1[k] = NQ + 8;
+      scale[k] = q_scale(q_shift(sc, st.qmax[Q_FORCE]));
+    } else {
+      f0[k] = 0;  // mass
+      f1[k] = MODE == 0 ? (ch[k] == 0 ? NQ + 8 : ch[k]) : ch[k] + 1;
+      scale[k] = q_scale(q_shift(sc, st.qmax[MODE == 1 ? Q_MOM_MUSL : (ch[k] == 0 ? Q_MASS : Q_MOM)]));
+    }
+    acc[k] = 0.f;
+  }
+  float* row = ws + lane * SROW;
+  for (int base = i0; base < i1; base += 32) {
+    const int cnt = min(32, i1 - base);
+    if (lane < cnt) {
+      const long long i = base + lane;
+      const float xx[3] = {b.xxn[i], b.xxn[NP + i], b.xxn[2 * NP + i]};
+      if (MODE == 2) {
+        for (int q = 0; q < 9; ++q) row[q] = b.fs[q * NP + i];
+      } else {
+        row[0] = (float)b.mass[i];
+        row[1] = (float)b.v[i];
+        row[2] = (float)b.v[NP + i];
+        row[3] = (float)b.v[2 * NP + i];
+      }
+      for (int k = 0; k < 8; ++k) {
+        float w = 0.125f;
+        for (int a = 0; a < 3; ++a) w *= kCorner[k][a] ? 1.f + xx[a] : 1.f - xx[a];
+        row[NQ + k] = w;
+      }
+      row[NQ + 8] = 1.f;
+    }
+    __syncwarp();
+    for (int p = 0; p < cnt; ++p) {
+      const float* r = ws + p * SROW;
+#pragma unroll
+      for (int k = 0; k < KS; ++k)
+        if (cell[k] >= 0) acc[k] += MODE == 2 ? r[wi[k]] * r[f0[k]] : (r[wi[k]] * r[f0[k]]) * r[f1[k]];
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int k = 0; k < KS; ++k) {
+    if (cell[k] < 0) continue;
+    const long long q = quant(acc[k], scale[k]);
+    if (q) atomicAdd(&b.cacc[(long long)(CH0 + ch[k]) * NC + sc.c0 + cell[k]], (unsigned long long)q);
+  }
+}
+
+// the scatter of one cell's particles [i0, i1) of a linear / GIMP /
+// B-spline scene by one warp; ws = the warp's shared workspace
+template <int MODE>
+__device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int s, int i0, int i1, int cl, float* ws) {
+  using SS = ScatterShape<MODE>;
+  constexpr int NV = SS::NV, NQ = SS::NQ, PC = SS::PC, NPQ = SS::NPQ;
+  float* pq = ws;                                   // [PC][16][NPQ], 16-byte aligned
+  float2* tab = reinterpret_cast<float2*>(ws + SS::PQ);  // [PC][3][4]
+  float* val = ws + SS::PQ + SS::TAB;               // [NQ][PC]
+  const int lane = threadIdx.x & 31;
   int c[3];
   c[2] = cl / sc.NCxy;
   {
@@ -346,75 +447,96 @@ __device__ __forceinline__ void scatter_cell(BState& b, long long key, float (*s
     const float sv = q_scale(q_shift(sc, st.qmax[MODE == 1 ? Q_MOM_MUSL : Q_FORCE]));
     for (int v = 0; v < NV; ++v) scale[v] = sv;
   }
-  // node offsets of this lane's two slots (-1..2 per direction)
-  int to[2][3];
+  const int shape = sc.shape;
+  const int tlo = shape == 0 ? 0 : -1, nt = shape == 1 ? 4 : (shape == 2 ? 3 : 2);
+  const int ns = nt * nt * nt;
+  // this lane's slots (box offsets sx, sy, sz)
+  int sx[2], syz[2], sy[2], sz[2];
   bool use[2];
-  const int tlo = sc.shape == 0 ? 0 : -1, thi = sc.shape == 1 ? 2 : 1;
   for (int k = 0; k < 2; ++k) {
     const int slot = lane + 32 * k;
-    to[k][0] = (slot & 3) - 1;
-    to[k][1] = ((slot >> 2) & 3) - 1;
-    to[k][2] = (slot >> 4) - 1;
-    use[k] = true;
-    for (int a = 0; a < 3; ++a) use[k] = use[k] && to[k][a] >= tlo && to[k][a] <= thi;
+    use[k] = slot < ns;
+    sz[k] = slot / (nt * nt);
+    const int r2 = slot - sz[k] * nt * nt;
+    sy[k] = r2 / nt;
+    sx[k] = r2 - sy[k] * nt;
+    syz[k] = sz[k] * 4 + sy[k];
   }
   const float idc = (float)sc.idcell;
   float acc[2][NV];
   for (int k = 0; k < 2; ++k)
     for (int v = 0; v < NV; ++v) acc[k][v] = 0.f;
-  float* row = sq[lane];
-  for (int base = i0; base < i1; base += 32) {
-    const int cnt = min(32, i1 - base);
-    if (lane < cnt) {
-      const long long i = base + lane;
-      float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
+  for (int base = i0; base < i1; base += PC) {
+    const int cnt = min(PC, i1 - base);
+    // particle values, component-major
+    for (int e = lane; e < NQ * PC; e += 32) {
+      const int q = e / PC, p = e % PC;
+      if (p >= cnt) continue;
+      const long long i = base + p;
+      if (MODE == 2) val[e] = b.fs[q * NP + i];
+      else val[e] = q == 0 ? (float)b.mass[i] : (float)b.v[(q - 1) * NP + i];
+    }
+    // 1-D weights and derivatives (per unit length) at offsets tlo + t
+    for (int e = lane; e < 12 * PC; e += 32) {
+      const int p = e % PC, r = e / PC, a = r >> 2, t = r & 3;
+      if (p >= cnt || t >= nt) continue;
+      const float off = b.off[a * NP + base + p];
+      float w, d;
+      if (shape == 0) lin1(tlo + t, off, w, d);
+      else if (shape == 2) bsp1(tlo + t, off, w, d);
+      else gimp1((float)(-(tlo + t)) + off, w, d);
+      tab[(p * 3 + a) * 4 + t] = make_float2(w, d * idc);
+    }
+    __syncwarp();
+    // y-z factors per particle and (ty, tz)
+    for (int e = lane; e < 16 * PC; e += 32) {
+      const int p = e >> 4, yz = e & 15, ty = yz & 3, tz = yz >> 2;
+      if (p >= cnt || ty >= nt || tz >= nt) continue;
+      const float2 y = tab[(p * 3 + 1) * 4 + ty], z = tab[(p * 3 + 2) * 4 + tz];
+      const float A = y.x * z.x;
+      float* o = pq + (p * 16 + yz) * NPQ;
       if (MODE == 2) {
-        for (int q = 0; q < 9; ++q) row[q] = b.fs[q * NP + i];
+        const float B = y.y * z.x, C = y.x * z.y;
+        const float sxx = val[0 * PC + p], syy = val[1 * PC + p], szz = val[2 * PC + p];
+        const float sxy = val[3 * PC + p], syz_ = val[4 * PC + p], sxz = val[5 * PC + p];
+        o[0] = -sxx * A;
+        o[1] = val[6 * PC + p] * A - sxy * B - sxz * C;
+        o[2] = -sxy * A;
+        o[3] = val[7 * PC + p] * A - syy * B - syz_ * C;
+        o[4] = -sxz * A;
+        o[5] = val[8 * PC + p] * A - syz_ * B - szz * C;
       } else {
-        const float m = (float)b.mass[i];
-        row[0] = m;
-        row[1] = (float)b.v[i];
-        row[2] = (float)b.v[NP + i];
-        row[3] = (float)b.v[2 * NP + i];
-      }
-      for (int a = 0; a < 3; ++a)
-        for (int t = -1; t <= 2; ++t) {
-          float w = 0.f, d = 0.f;
-          if (t >= tlo && t <= thi) {
-            if (sc.shape == 0) lin1(t, off[a], w, d);
-            else if (sc.shape == 2) bsp1(t, off[a], w, d);
-            else gimp1((float)(-t) + off[a], w, d);
-          }
-          row[NQ + a * 4 + t + 1] = w;
-          if (MODE == 2) row[NQ + 12 + a * 4 + t + 1] = d;
+        const float M = val[p] * A;
+        if (MODE == 0) {
+          o[0] = M;
+          o[1] = M * val[PC + p];
+          o[2] = M * val[2 * PC + p];
+          o[3] = M * val[3 * PC + p];
+        } else {
+          o[0] = M * val[PC + p];
+          o[1] = M * val[2 * PC + p];
+          o[2] = M * val[3 * PC + p];
         }
+      }
     }
     __syncwarp();
     for (int p = 0; p < cnt; ++p) {
-      const float* r = sq[p];
       for (int k = 0; k < 2; ++k) {
         if (!use[k]) continue;
-        const float wx = r[NQ + 0 + to[k][0] + 1], wy = r[NQ + 4 + to[k][1] + 1], wz = r[NQ + 8 + to[k][2] + 1];
+        const float2 x = tab[p * 12 + sx[k]];
+        const float* o = pq + (p * 16 + syz[k]) * NPQ;
         if (MODE == 2) {
-          const float dx = r[NQ + 12 + to[k][0] + 1] * wy * wz * idc;
-          const float dy = wx * r[NQ + 16 + to[k][1] + 1] * wz * idc;
-          const float dz = wx * wy * r[NQ + 20 + to[k][2] + 1] * idc;
-          const float wv = wx * wy * wz;
-          acc[k][0] += -(r[0] * dx + r[3] * dy + r[5] * dz) + r[6] * wv;
-          acc[k][1] += -(r[3] * dx + r[1] * dy + r[4] * dz) + r[7] * wv;
-          acc[k][2] += -(r[5] * dx + r[4] * dy + r[2] * dz) + r[8] * wv;
+          const float2 o01 = *reinterpret_cast<const float2*>(o), o23 = *reinterpret_cast<const float2*>(o + 2),
+                       o45 = *reinterpret_cast<const float2*>(o + 4);
+          acc[k][0] += x.y * o01.x + x.x * o01.y;
+          acc[k][1] += x.y * o23.x + x.x * o23.y;
+          acc[k][2] += x.y * o45.x + x.x * o45.y;
         } else {
-          const float wm = wx * wy * wz * r[0];
-          if (MODE == 0) {
-            acc[k][0] += wm;
-            acc[k][1] += wm * r[1];
-            acc[k][2] += wm * r[2];
-            acc[k][3] += wm * r[3];
-          } else {
-            acc[k][0] += wm * r[1];
-            acc[k][1] += wm * r[2];
-            acc[k][2] += wm * r[3];
-          }
+          const float4 m4 = *reinterpret_cast<const float4*>(o);
+          acc[k][0] += x.x * m4.x;
+          acc[k][1] += x.x * m4.y;
+          acc[k][2] += x.x * m4.z;
+          if (MODE == 0) acc[k][3] += x.x * m4.w;
         }
       }
     }
@@ -422,7 +544,7 @@ __device__ __forceinline__ void scatter_cell(BState& b, long long key, float (*s
   }
   for (int k = 0; k < 2; ++k) {
     if (!use[k]) continue;
-    const int jx = c[0] + to[k][0], jy = c[1] + to[k][1], jz = c[2] + to[k][2];
+    const int jx = c[0] + tlo + sx[k], jy = c[1] + tlo + sy[k], jz = c[2] + tlo + sz[k];
     if (jx < 0 || jx >= sc.NGx || jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
     const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
     for (int v = 0; v < NV; ++v) {
@@ -432,17 +554,49 @@ __device__ __forceinline__ void scatter_cell(BState& b, long long key, float (*s
   }
 }
 
-// Persistent scatter over the occupied sort keys (the run-length encoding of
-// the sorted keys, count on the device): a fixed grid, each warp taking keys
-// r, r + total warps, ... Empty cells cost nothing, which matters on sparse
-// grids (a granular column fills a fifth of its grid).
+// the scatter of one sort key by one warp: particles [i0, i1) of scene s in
+// cell cl (dual cell d for SGMP)
 template <int MODE>
-__global__ void __launch_bounds__(32 * kCellWarps) kb_cell_scatter(BState b, const unsigned* runs, const int* nruns) {
-  __shared__ float sq[kCellWarps][32][ScatterShape<MODE>::ROW];
-  const int warp = threadIdx.x >> 5;
+__device__ __forceinline__ void scatter_cell(BState& b, int i0, int i1, int s, int cl, int d, float* ws) {
+  const Scene& sc = b.scenes[s];
+  if (!scene_live(b, s) || (MODE == 1 && !sc.musl)) return;
+  if (sc.shape == 3) sg_scatter_cell<MODE>(b, sc, s, i0, i1, d, ws);
+  else if (cl >= 0) box_scatter_cell<MODE>(b, sc, s, i0, i1, cl, ws);  // cl < 0: the off-grid bucket
+}
+
+// Persistent scatter over the occupied sort keys (the run-length encoding of
+// the sorted keys, count on the device): a fixed grid, each warp taking
+// chunks of up to 32 consecutive keys (fewer when there are few keys, so
+// that every warp has work). The lanes first load one key's particle range,
+// scene and cell each -- one round of dependent loads for the whole chunk
+// instead of one per key -- then the warp scatters the keys in turn. Empty
+// cells cost nothing, which matters on sparse grids (a granular column fills
+// a fifth of its grid).
+template <int MODE>
+__global__ void __launch_bounds__(32 * kCellWarps, 4) kb_cell_scatter(BState b, const unsigned* runs, const int* nruns) {
+  __shared__ float4 wsp[kCellWarps][ScatterShape<MODE>::WS / 4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long n = *nruns;
-  for (long long r = (long long)blockIdx.x * kCellWarps + warp; r < n; r += (long long)gridDim.x * kCellWarps)
-    scatter_cell<MODE>(b, runs[r], sq[warp]);
+  const long long nw = (long long)gridDim.x * kCellWarps;
+  const int chunk = (int)max(1LL, min(32LL, (n + nw - 1) / nw));
+  for (long long r0 = ((long long)blockIdx.x * kCellWarps + warp) * chunk; r0 < n; r0 += nw * chunk) {
+    int i0 = 0, i1 = 0, s = -1, cl = -1, d = -1;
+    if (lane < chunk && r0 + lane < n) {
+      key_range(b, runs[r0 + lane], i0, i1);
+      if (i0 < i1) {
+        s = b.scene[i0];
+        cl = b.cell[i0];
+        d = b.dual[i0];
+      }
+    }
+    const int m = (int)min((long long)chunk, n - r0);
+    for (int j = 0; j < m; ++j) {
+      const int sj = __shfl_sync(0xffffffffu, s, j);
+      const int a = __shfl_sync(0xffffffffu, i0, j), e = __shfl_sync(0xffffffffu, i1, j);
+      const int cj = __shfl_sync(0xffffffffu, cl, j), dj = __shfl_sync(0xffffffffu, d, j);
+      if (sj >= 0) scatter_cell<MODE>(b, a, e, sj, cj, dj, reinterpret_cast<float*>(wsp[warp]));
+    }
+  }
 }
 
 // Accumulated channels 0..nv-1 of node n in FP64 (the accumulators cleared
@@ -505,24 +659,38 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
       int j[3];
       node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
       if (sc.shape == 3) {
-        // centre nodes -> node: adjacent cells in ascending order, cut-off on the cell mass
-        const long long nc0 = sc.c0;
+        // centre nodes -> node (GridMomentumInitial of SGMP): 1/8 of the
+        // adjacent cells' mass and momentum, cells at or below the cut-off
+        // mass left out; the cells' fixed-point sums are added exactly
+        const SceneState& st = b.sst[s];
+        const int shm = q_shift(sc, st.qmax[Q_MASS]);
+        const double um = q_unit(shm), up = q_unit(q_shift(sc, st.qmax[Q_MOM]));
+        // cm = q * um > cutoff  <=>  q > floor(cutoff / um) (um a power of two)
+        const double thr = ldexp(sc.cutoff, shm);
+        const long long qcut = thr >= 9.0e18 ? LLONG_MAX : (long long)floor(thr);
+        const unsigned long long* ca = b.cacc;
+        const long long NC = b.NC;
+        long long QM = 0, Q0 = 0, Q1 = 0, Q2 = 0;
         for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
           if (cz < 0 || cz >= sc.NCz) continue;
           for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
             if (cy < 0 || cy >= sc.NCy) continue;
             for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
               if (cx < 0 || cx >= sc.NCx) continue;
-              long long c = nc0 + (cz * sc.NCy + cy) * sc.NCx + cx;
-              double cm = b.cmg[c];
-              if (!(cm > sc.cutoff)) continue;
-              M += 0.125 * cm;
-              P0 += 0.125 * b.cpx[c];
-              P1 += 0.125 * b.cpx[b.NC + c];
-              P2 += 0.125 * b.cpx[2 * b.NC + c];
+              const long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
+              const long long qm = (long long)ca[CQ_M * NC + c];
+              if (qm <= qcut) continue;
+              QM += qm;
+              Q0 += (long long)ca[CQ_P * NC + c];
+              Q1 += (long long)ca[(CQ_P + 1) * NC + c];
+              Q2 += (long long)ca[(CQ_P + 2) * NC + c];
             }
           }
         }
+        M = 0.125 * ((double)QM * um);
+        P0 = 0.125 * ((double)Q0 * up);
+        P1 = 0.125 * ((double)Q1 * up);
+        P2 = 0.125 * ((double)Q2 * up);
       } else {
         const SceneState& st = b.sst[s];
         const double up = q_unit(q_shift(sc, st.qmax[Q_MOM]));
@@ -572,89 +740,6 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
     const unsigned c2 = __reduce_add_sync(g2, lane < nw ? wc[lane] : 0u);
     if (s2 >= 0 && c2 && lane == __ffs(g2) - 1) atomicAdd(&b.sst[s2].active_nodes, (unsigned long long)c2);
   }
-}
-
-// SGMP: particles -> centre nodes. The centre node of cell q is corner k of
-// the dual cells q - kCorner[k]; a particle of such a dual cell contributes
-// with the SGNShape weight of that corner.
-__device__ __forceinline__ float sg_corner_weight(const BState& b, long long i, int k) {
-  const long long NP = b.NP;
-  float w = 0.125f;
-  for (int a = 0; a < 3; ++a) {
-    float xx = b.xxn[a * NP + i];
-    w *= kCorner[k][a] ? 1.f + xx : 1.f - xx;
-  }
-  return w;
-}
-
-// particle key range of the dual cell q - kCorner[k] (empty if it does not exist)
-// Corner k of the dual cell (dx, dy, dz) as a scene cell, with the
-// reference's flat arithmetic (CenterCellNode, Grid.f90:380-418: first corner
-// plus the corner's flat offset; corners at or past the last cell are
-// dropped, and a direction with a single cell -- one dual cell -- spills into
-// the next row); -1 if dropped.
-__device__ __forceinline__ long long sg_corner_cell(const Scene& sc, int dx, int dy, int dz, int k) {
-  const long long c1 = ((long long)dz * sc.NCy + dy) * sc.NCx + dx;
-  const long long cid = c1 + kCorner[k][0] + (long long)kCorner[k][1] * sc.NCx + (long long)kCorner[k][2] * sc.NCxy;
-  return cid < (long long)sc.NCxy * sc.NCz ? cid : -1;
-}
-
-// particle range of the dual cell whose corner k is the centre node (cell)
-// cq, inverting sg_corner_cell: first corner t = cq - corner offset, which
-// must be a dual cell's first corner (t's per-direction indices within the
-// dual grid); false if there is none or it holds no particle
-__device__ __forceinline__ bool sg_dual_range(const BState& b, const Scene& sc, long long cq, int k, int& i0,
-                                              int& i1) {
-  const long long t = cq - kCorner[k][0] - (long long)kCorner[k][1] * sc.NCx - (long long)kCorner[k][2] * sc.NCxy;
-  if (t < 0) return false;
-  const int tz = (int)(t / sc.NCxy);
-  const int rem = (int)(t - (long long)tz * sc.NCxy);
-  const int ty = rem / sc.NCx, tx = rem - ty * sc.NCx;
-  if (tx >= sc.CNCx || ty >= sc.CNCy || tz >= sc.CNCz) return false;
-  key_range(b, sc.k0 + ((long long)tz * sc.CNCy + ty) * sc.CNCx + tx, i0, i1);
-  return i0 < i1;
-}
-
-__global__ void kb_sg_centre_mass(BState b, int momentum_only) {
-  long long c = btid();
-  if (c >= b.NC) return;
-  int s = b.cscene[c];
-  if (!scene_live(b, s)) return;
-  const Scene& sc = b.scenes[s];
-  const long long NP = b.NP, NC = b.NC;
-  long long lc = c - sc.c0;
-  int q[3];
-  q[2] = (int)(lc / sc.NCxy);
-  int rem = (int)(lc - (long long)q[2] * sc.NCxy);
-  q[1] = rem / sc.NCx;
-  q[0] = rem - q[1] * sc.NCx;
-  // FP32 sums per dual cell, added in 64-bit fixed point (exact), as the
-  // particle -> node scatter does
-  const SceneState& st = b.sst[s];
-  const int shm = q_shift(sc, st.qmax[Q_MASS]), shp = q_shift(sc, st.qmax[momentum_only ? Q_MOM_MUSL : Q_MOM]);
-  const float sm = q_scale(shm), sp = q_scale(shp);
-  long long QM = 0, Q0 = 0, Q1 = 0, Q2 = 0;
-  for (int k = 0; k < 8; ++k) {
-    int i0, i1;
-    if (!sg_dual_range(b, sc, lc, k, i0, i1)) continue;
-    float m = 0, p0 = 0, p1 = 0, p2 = 0;
-    for (int i = i0; i < i1; ++i) {
-      float wm = sg_corner_weight(b, i, k) * (float)b.mass[i];
-      m += wm;
-      p0 += wm * (float)b.v[i];
-      p1 += wm * (float)b.v[NP + i];
-      p2 += wm * (float)b.v[2 * NP + i];
-    }
-    QM += quant(m, sm);
-    Q0 += quant(p0, sp);
-    Q1 += quant(p1, sp);
-    Q2 += quant(p2, sp);
-  }
-  const double um = q_unit(shm), up = q_unit(shp);
-  if (!momentum_only) b.cmg[c] = (double)QM * um;
-  b.cpx[c] = (double)Q0 * up;
-  b.cpx[NC + c] = (double)Q1 * up;
-  b.cpx[2 * NC + c] = (double)Q2 * up;
 }
 
 // -------------------------------------------------------------- stress
@@ -953,69 +1038,42 @@ __global__ void kb_p2g_force(BState b) {
   node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
   double F[3] = {0, 0, 0};
   if (sc.shape == 3) {
+    // centre nodes -> node (GridMomentumUpdate of SGMP): 1/8 of the cells'
+    // external force minus Cfint . dN, dN = +-1 / (4 Jacobi) per direction
+    // by the node's side of the cell; the cells' fixed-point sums are
+    // combined exactly, then scaled once
     const long long NC = b.NC;
+    const unsigned long long* ca = b.cacc;
+    long long E[3] = {0, 0, 0}, T[3] = {0, 0, 0};
     for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
       if (cz < 0 || cz >= sc.NCz) continue;
       for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
         if (cy < 0 || cy >= sc.NCy) continue;
         for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
           if (cx < 0 || cx >= sc.NCx) continue;
-          long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
-          // the cell's contribution in FP32 (CNShape derivatives at the
-          // centre, +-1/(4 Jacobi)), accumulated in FP64
-          const int ox = j[0] - cx, oy = j[1] - cy, oz = j[2] - cz;
-          const float j4 = (float)sc.iJacobi4;
-          const float dx = ox ? j4 : -j4, dy = oy ? j4 : -j4, dz = oz ? j4 : -j4;
-          const double* ci = b.cfint;
-          const float c0 = (float)ci[c], c1 = (float)ci[NC + c], c2 = (float)ci[2 * NC + c],
-                      c3 = (float)ci[3 * NC + c], c4 = (float)ci[4 * NC + c], c5 = (float)ci[5 * NC + c];
-          F[0] += (double)(0.125f * (float)b.cfext[c] - (c0 * dx + c3 * dy + c5 * dz));
-          F[1] += (double)(0.125f * (float)b.cfext[NC + c] - (c3 * dx + c1 * dy + c4 * dz));
-          F[2] += (double)(0.125f * (float)b.cfext[2 * NC + c] - (c5 * dx + c4 * dy + c2 * dz));
+          const long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
+          long long I[6];
+          for (int a = 0; a < 3; ++a) E[a] += (long long)ca[(CQ_FE + a) * NC + c];
+          for (int a = 0; a < 6; ++a) I[a] = (long long)ca[(CQ_FI + a) * NC + c];
+          // signed by the node's side: +dN at the upper corner of the cell
+          const bool ux = j[0] != cx, uy = j[1] != cy, uz = j[2] != cz;
+          const long long xx = ux ? I[0] : -I[0], xy_x = ux ? I[3] : -I[3], xz_x = ux ? I[5] : -I[5];
+          const long long xy_y = uy ? I[3] : -I[3], yy = uy ? I[1] : -I[1], yz_y = uy ? I[4] : -I[4];
+          const long long xz_z = uz ? I[5] : -I[5], yz_z = uz ? I[4] : -I[4], zz = uz ? I[2] : -I[2];
+          T[0] += xx + xy_y + xz_z;
+          T[1] += xy_x + yy + yz_z;
+          T[2] += xz_x + yz_y + zz;
         }
       }
     }
+    const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
+    for (int a = 0; a < 3; ++a) F[a] = (0.125 * (double)E[a] - sc.iJacobi4 * (double)T[a]) * u;
   } else {
     const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
     const double unit[3] = {u, u, u};
     if (!take_acc(b, n, 3, unit, F)) return;  // idle node
   }
   node_integrate(b, sc, n, F);
-}
-
-// SGMP: particles -> centre nodes, force terms
-__global__ void kb_sg_centre_force(BState b) {
-  long long c = btid();
-  if (c >= b.NC) return;
-  int s = b.cscene[c];
-  if (!scene_live(b, s)) return;
-  const Scene& sc = b.scenes[s];
-  const long long NP = b.NP, NC = b.NC;
-  long long lc = c - sc.c0;
-  int q[3];
-  q[2] = (int)(lc / sc.NCxy);
-  int rem = (int)(lc - (long long)q[2] * sc.NCxy);
-  q[1] = rem / sc.NCx;
-  q[0] = rem - q[1] * sc.NCx;
-  const int sh = q_shift(sc, b.sst[s].qmax[Q_FORCE]);
-  const float sf = q_scale(sh);
-  long long E[3] = {0, 0, 0}, I[6] = {0, 0, 0, 0, 0, 0};
-  for (int k = 0; k < 8; ++k) {
-    int i0, i1;
-    if (!sg_dual_range(b, sc, lc, k, i0, i1)) continue;
-    float e[3] = {0, 0, 0}, t[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = i0; i < i1; ++i) {
-      float w = sg_corner_weight(b, i, k);
-      for (int a = 0; a < 3; ++a) e[a] += b.fs[(6 + a) * NP + i] * w;
-      for (int a = 0; a < 6; ++a) t[a] += w * b.fs[a * NP + i];
-    }
-    for (int a = 0; a < 3; ++a) E[a] += quant(e[a], sf);
-    for (int a = 0; a < 6; ++a) I[a] += quant(t[a], sf);
-  }
-  const double u = q_unit(sh);
-  for (int a = 0; a < 3; ++a) b.cfext[a * NC + c] = (double)E[a] * u;
-  // Cfint order of the reference: xx, yy, zz, xy, yz, xz
-  for (int a = 0; a < 6; ++a) b.cfint[a * NC + c] = (double)I[a] * u;
 }
 
 // SGMP: strain rate / spin at the centre nodes from the 8 cell nodes
@@ -1105,6 +1163,18 @@ __global__ void kb_sg_centre_velocity(BState b) {
     b.cvx[a * NC + c] = v[a];
     b.cax[a * NC + c] = acc[a];
   }
+  // the force sums are consumed (and so are the momentum sums when the
+  // MUSL transfer refills them): cleared for the next scatter
+  for (int a = sc.musl ? CQ_P : CQ_FE; a < CQ_N; ++a) b.cacc[a * NC + c] = 0ull;
+}
+
+// SGMP: clears the mass and momentum sums of the live scenes' centre nodes
+// before the step's first transfer (they stay readable between steps)
+__global__ void kb_sg_clear(BState b) {
+  const long long c = btid();
+  if (c >= b.NC) return;
+  if (!scene_live(b, b.cscene[c])) return;
+  for (int a = CQ_M; a < CQ_FE; ++a) b.cacc[a * b.NC + c] = 0ull;
 }
 
 // ---------------------------------------------------------- G2P position
@@ -1208,20 +1278,26 @@ __global__ void kb_p2g_momentum(BState b) {
   node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
   double P0 = 0, P1 = 0, P2 = 0;
   if (sc.shape == 3) {
+    // centre nodes -> node (GridMomentumMUSL of SGMP), exact sums of the
+    // cells' fixed-point momenta
     const long long NC = b.NC;
+    const unsigned long long* ca = b.cacc;
+    long long Q[3] = {0, 0, 0};
     for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
       if (cz < 0 || cz >= sc.NCz) continue;
       for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
         if (cy < 0 || cy >= sc.NCy) continue;
         for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
           if (cx < 0 || cx >= sc.NCx) continue;
-          long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
-          P0 += 0.125 * b.cpx[c];
-          P1 += 0.125 * b.cpx[NC + c];
-          P2 += 0.125 * b.cpx[2 * NC + c];
+          const long long c = sc.c0 + (cz * sc.NCy + cy) * sc.NCx + cx;
+          for (int a = 0; a < 3; ++a) Q[a] += (long long)ca[(CQ_P + a) * NC + c];
         }
       }
     }
+    const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]));
+    P0 = 0.125 * ((double)Q[0] * u);
+    P1 = 0.125 * ((double)Q[1] * u);
+    P2 = 0.125 * ((double)Q[2] * u);
   } else {
     const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]));
     const double unit[3] = {u, u, u};
@@ -1392,6 +1468,19 @@ __global__ void kb_unpermute(BState b, int scene, int field, int comp, double* d
   const long long k = btid();
   if (k >= sc.np) return;
   dst[k] = field_value(b, field, comp, b.inv[sc.p0 + k]);
+}
+
+// SGMP centre-node mass (comp -1) or momentum component of a scene from
+// its fixed-point sums (downloads; the momentum of the last transfer, MUSL
+// or not)
+__global__ void kb_centre_field(BState b, int scene, int comp, double* dst) {
+  const Scene& sc = b.scenes[scene];
+  const long long k = btid();
+  if (k >= sc.nc) return;
+  const SceneState& st = b.sst[scene];
+  const int q = comp < 0 ? Q_MASS : (sc.musl ? Q_MOM_MUSL : Q_MOM);
+  const int ch = comp < 0 ? CQ_M : CQ_P + comp;
+  dst[k] = (double)(long long)b.cacc[(long long)ch * b.NC + sc.c0 + k] * q_unit(q_shift(sc, st.qmax[q]));
 }
 
 }  // namespace bm

@@ -119,7 +119,7 @@ const char* const kKernelNames[K_COUNT] = {
     "begin_step", "locate", "pair_sort", "segments", "p2g_mass", "node_velocity", "apply_bc",
     "stress_update", "depeff_tail", "force_prep", "p2g_force_integrate", "integrate", "g2p_position",
     "p2g_musl", "reduce_energy_dt", "dr_damping", "permute",
-    "p2g_mass_scatter", "p2g_force_scatter", "p2g_musl_scatter", "sgmp_centre_mass", "sgmp_centre_force",
+    "p2g_mass_scatter", "p2g_force_scatter", "p2g_musl_scatter", "sgmp_centre_clear",
     "sgmp_centre_gradient", "sgmp_centre_velocity"};
 
 static thread_local Profiler* t_prof = nullptr;

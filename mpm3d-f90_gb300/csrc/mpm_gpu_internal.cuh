@@ -157,7 +157,7 @@ void prof_end(int kernel_id, cudaStream_t s);
 enum KernelId {
   K_BEGIN = 0, K_LOCATE, K_SORT, K_SEG, K_P2G_MASS, K_NODE_VEL, K_BC, K_STRESS, K_DEPEFF,
   K_FORCE_PREP, K_P2G_FORCE, K_INTEGRATE, K_POSITION, K_P2G_MOM, K_REDUCE, K_DR, K_PERMUTE,
-  K_SCATTER_MASS, K_SCATTER_FORCE, K_SCATTER_MOM, K_SG_MASS, K_SG_FORCE, K_SG_GRADIENT, K_SG_VELOCITY,
+  K_SCATTER_MASS, K_SCATTER_FORCE, K_SCATTER_MOM, K_SG_CLEAR, K_SG_GRADIENT, K_SG_VELOCITY,
   K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
