@@ -51,7 +51,8 @@ enum mpm_phase {
   MPM_PHASE_CALC_ENERGY = 8,              /* Particle.f90:204     calcEnergy              */
   MPM_PHASE_UPDATE_DT = 9,                /* update_step.f90:1833 UpdateDT                */
   MPM_PHASE_DR_DAMPING = 10,              /* Particle.f90:172     dynamicRelaxationDamping*/
-  MPM_PHASE_BEGIN_STEP = 11               /* MPM3D.f90:72-74: istep+1, time += DT         */
+  MPM_PHASE_BEGIN_STEP = 11,              /* MPM3D.f90:72-74: istep+1, time += DT         */
+  MPM_PHASE_SMOOTH_STRESS = 12            /* update_step.f90:1876 SmoothStressbyGrid      */
 };
 
 /* Field identifiers for mpm_download / oracle accessors. Particle fields are
@@ -84,6 +85,7 @@ enum mpm_field {
   MPM_P_ICELL = 23,   /* 1-based cell id, -1 outside */
   MPM_P_CENTERICELL = 24,
   MPM_P_INODE = 25,
+  MPM_P_SPRE = 26,   /* smoothed pressure (SmoothStressbyGrid; 0 without 'smoo') */
   MPM_G_MG = 40,
   MPM_G_PX = 41,     /* 3 */
   MPM_G_FX = 42,     /* 3 */

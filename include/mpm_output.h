@@ -8,8 +8,7 @@
  * The writer takes plain host arrays, so the same calls serve the GPU
  * library (curve values gathered from the device, mpm_gather*) and any other
  * producer of the step's state. Not written: the contact-force plot (contact
- * is outside the explicit-step path) and smoothed pressures (written as 0, as
- * the reference does without stress smoothing).
+ * is outside the explicit-step path).
  */
 #ifndef MPM_OUTPUT_H
 #define MPM_OUTPUT_H
@@ -28,12 +27,14 @@ typedef struct mpm_output mpm_output;
  * arrays of nb_particle doubles each; sd = SDxx, SDyy, SDzz, SDxy, SDyz,
  * SDxz). Fields the deck's animation options do not need may be NULL; icell
  * (1-based cell, <= 0 outside the grid) may be NULL when every particle is
- * inside the grid. */
+ * inside the grid; spre (smoothed pressure, mpm_download MPM_P_SPRE) NULL
+ * reads as 0, its value without stress smoothing. */
 typedef struct mpm_particle_view {
   const double *xp, *vxp, *fxp, *mass;
   const double *seqv, *epeff, *sm, *vol, *ie, *celsius, *cp, *dmg, *sd;
   const double* failure; /* 0 / 1 */
   const double* icell;
+  const double* spre;
 } mpm_particle_view;
 
 /* Opens the files of job `job` (a path prefix; the reference derives it

@@ -66,6 +66,7 @@ struct HostScene {
   int mat0 = 0, body0 = 0, index = 0;
   SceneState st{};
   int drdamp = 0;
+  int smooth = 0;  // 'smoo': Spre is computed when read
 };
 
 }  // namespace mpm
@@ -170,7 +171,7 @@ struct mpm_batch {
   size_t cub_bytes = 0;
   int key_bits = 1;
   int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
-  int stress_type = 0;  // material type shared by every material of the batch (0: several)
+  unsigned stress_types = 0;  // stress instantiations to launch: bit MT per specialised type, bit 0 for the rest
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
@@ -265,13 +266,9 @@ void layout_flags(mpm_batch* b) {
     if (g.uvfp) b->any_uvfp = 1;
     if (h->drdamp) b->any_dr = 1;
   }
-  b->stress_type = -1;
+  b->stress_types = 0;
   for (HostScene* h : b->order)
-    for (const DevMaterial& m : h->su.mats) {
-      if (b->stress_type == -1) b->stress_type = m.mat_type;
-      else if (b->stress_type != m.mat_type) b->stress_type = 0;
-    }
-  if (b->stress_type < 0) b->stress_type = 0;
+    for (const DevMaterial& m : h->su.mats) b->stress_types |= 1u << (stress_specialised(m.mat_type) ? m.mat_type : 0);
 }
 
 int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
@@ -362,13 +359,15 @@ int enqueue_step(mpm_batch* b) {
       prof_end(K_SG_GRADIENT, st);
     }
     prof_begin(K_STRESS, st);
-    switch (b->stress_type) {  // the one material type of the batch, if any
-      case 1: kb_stress<1><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
-      case 9: kb_stress<9><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
-      case 10: kb_stress<10><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
-      case 11: kb_stress<11><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
-      default: kb_stress<0><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass); break;
-    }
+    // one launch per material instantiation present (each takes its own
+    // particles); usually a single one
+    const unsigned ty = b->stress_types;
+    const int f = __builtin_popcount(ty) > 1;
+    if (ty & (1u << 1)) kb_stress<1><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
+    if (ty & (1u << 9)) kb_stress<9><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
+    if (ty & (1u << 10)) kb_stress<10><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
+    if (ty & (1u << 11)) kb_stress<11><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
+    if (ty & 1u) kb_stress<0><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
     prof_end(K_STRESS, st);
     if (b->any_jc) {
       prof_begin(K_DEPEFF, st);
@@ -950,6 +949,41 @@ int mpm_batch_scene_scalars(mpm_batch* b, int id, double* o) {
   return MPM_OK;
 }
 
+// Spre of a scene (SmoothStressbyGrid on its state after the last step;
+// zero without 'smoo', as in the reference), in its input order
+static int scene_spre(mpm_batch* b, HostScene* h, double* out) {
+  if (!h->smooth) {
+    std::fill(out, out + h->np, 0.0);
+    return MPM_OK;
+  }
+  const BState& s = b->A;
+  const long long nodes = h->su.g.shape == 3 ? h->ncell : h->nn;
+  const size_t bytes = sizeof(unsigned) * 2 + sizeof(unsigned long long) * 2 * (size_t)nodes +
+                       sizeof(double) * ((size_t)h->nn + (size_t)h->ncell + (size_t)h->np);
+  char* tmp = nullptr;
+  BCK(cudaMalloc(&tmp, bytes));
+  unsigned* bnd = reinterpret_cast<unsigned*>(tmp);
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(tmp + 8);
+  double* gpre = reinterpret_cast<double*>(acc + 2 * nodes);
+  double* cgpre = gpre + h->nn;
+  double* spre = cgpre + h->ncell;
+  cudaStream_t st = b->stream;
+  cudaError_t e = cudaMemsetAsync(tmp, 0, 8 + sizeof(unsigned long long) * 2 * (size_t)nodes, st);
+  if (e == cudaSuccess) {
+    kb_smooth_bound<<<gridn(h->np, 256), 256, 0, st>>>(s, h->index, bnd);
+    kb_smooth_p2g<<<gridn(h->np, 256), 256, 0, st>>>(s, h->index, bnd, acc);
+    kb_smooth_node<<<gridn(h->nn, 256), 256, 0, st>>>(s, h->index, bnd, acc, gpre);
+    if (h->su.g.shape == 3) kb_smooth_back<<<gridn(h->ncell, 256), 256, 0, st>>>(s, h->index, gpre, cgpre);
+    kb_smooth_g2p<<<gridn(h->np, 256), 256, 0, st>>>(s, h->index, gpre, cgpre, spre);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, spre, sizeof(double) * (size_t)h->np, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "stress smoothing: %s", cudaGetErrorString(e));
+  return MPM_OK;
+}
+
 int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
   if (!b || !out) return MPM_ERR_ARG;
   int r = ensure_committed(b);
@@ -966,6 +1000,7 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
       BCK(cudaMemcpy(out + a * h->nn, src + a * s.NN + h->n0, sizeof(double) * h->nn, cudaMemcpyDeviceToHost));
     return MPM_OK;
   }
+  if (field == MPM_P_SPRE) return scene_spre(b, h, out);
   if (field == MPM_C_MG || field == MPM_C_PX) {
     if (h->su.g.shape != 3) return berr(b, MPM_ERR_ARG, "no auxiliary grid (not SGMP)");
     // decoded from the fixed-point sums, one component at a time
@@ -1124,6 +1159,7 @@ HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code
   h->nn = h->su.g.nn;
   h->ncell = h->su.g.ncell;
   h->drdamp = !!(d->flags & MPM_F_DRDAMP);
+  h->smooth = !!(d->flags & MPM_F_SMOOTH);
   if (borrow) {
     h->bmass = d->mass;
     h->bx = d->xp;

@@ -746,9 +746,14 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
 // ParticleStressUpdate + Constitution for one particle (FP32). The stress pass
 // runs twice per step: before the force transfer for USF scenes (usf_pass 1)
 // and after the position update for USL / MUSL scenes (usf_pass 0).
-// MT != 0: a batch whose materials are all of type MT (fewer registers)
+// MT != 0: the particles of material type MT (an instantiation for each of
+// the common types, fewer registers); MT = 0: every other type
+__host__ __device__ constexpr bool stress_specialised(int mat_type) {
+  return mat_type == 1 || mat_type == 9 || mat_type == 10 || mat_type == 11;
+}
+
 template <int MT>
-__global__ void kb_stress(BState b, int usf_pass) {
+__global__ void kb_stress(BState b, int usf_pass, int filter) {
   using P = PMixed;
   using R = float;
   long long i = btid();
@@ -757,7 +762,13 @@ __global__ void kb_stress(BState b, int usf_pass) {
   if (!scene_live(b, s)) return;
   const Scene& sc = b.scenes[s];
   if (sc.usf != usf_pass) return;
-  const long long NP = b.NP, NN = b.NN;
+  const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
+  // every particle goes through the instantiation of its own material type
+  // (or the general one), whatever else shares the batch: the compiled FP32
+  // arithmetic, and so the result, is the same alone or in a batch (filter
+  // 0: the batch needs this instantiation only)
+  if (filter && (MT ? mt.mat_type != MT : stress_specialised(mt.mat_type))) return;
+  const long long NP = b.NP;
   const long long o = sc.p0 + b.orig[i];  // position in the reference processing order
   if (sc.has_jc) {
     b.setter[o] = -1;
@@ -853,7 +864,6 @@ __global__ void kb_stress(BState b, int usf_pass) {
   for (int a = 0; a < 6; ++a) ps.sd[a] = b.sd[a * NP + i];
   ps.failure = b.failure[i] != 0;
   ps.evol = b.evol[i];
-  const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
   CResult<R> res;
   constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2,
                       res);
@@ -1468,6 +1478,179 @@ __global__ void kb_unpermute(BState b, int scene, int field, int comp, double* d
   const long long k = btid();
   if (k >= sc.np) return;
   dst[k] = field_value(b, field, comp, b.inv[sc.p0 + k]);
+}
+
+// ----------------------------------------------------- stress smoothing
+// SmoothStressbyGrid (update_step.f90:1876-2055) for one scene, computed
+// from the state after its last step when Spre is read (it feeds only the
+// output): -SM * VOL and VOL mapped to the grid, Gpre = their ratio on the
+// mapped nodes, Spre interpolated back. Shapes as in the reference: GIMP and
+// B-spline at the current position against the step's cell, linear ones at
+// the step's offsets, SGMP ones at the step's XXN through the centre nodes
+// (nodes above the cut-off mass on the way back). Contributions are FP32,
+// quantised per particle and node and summed exactly (64-bit fixed point,
+// scales from the scene's largest |SM * VOL| and VOL), so Spre does not
+// depend on the other scenes of the batch.
+
+// bounds: bnd[0] = max |SM * VOL|, bnd[1] = max VOL (float bits)
+__global__ void kb_smooth_bound(BState b, int scene, unsigned* bnd) {
+  const Scene& sc = b.scenes[scene];
+  const long long k = btid();
+  if (k >= sc.np) return;
+  const long long i = sc.p0 + k;
+  atomicMax(&bnd[0], __float_as_uint(fabsf(b.sm[i] * b.vol[i]) * 1.0001f));
+  atomicMax(&bnd[1], __float_as_uint(fabsf(b.vol[i]) * 1.0001f));
+}
+
+// particles -> nodes (SGMP: centre nodes); acc = [2][nodes or cells of the scene]
+__global__ void kb_smooth_p2g(BState b, int scene, const unsigned* bnd, unsigned long long* acc) {
+  const Scene& sc = b.scenes[scene];
+  const long long k = btid();
+  if (k >= sc.np) return;
+  const long long i = sc.p0 + k, NP = b.NP;
+  const float sp = q_scale(q_shift(sc, bnd[0])), sv = q_scale(q_shift(sc, bnd[1]));
+  const float pv = -b.sm[i] * b.vol[i], v = b.vol[i];
+  if (sc.shape == 3) {
+    const int d = b.dual[i];
+    if (d < 0) return;
+    const int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+    const long long nc = sc.nc;
+    for (int c = 0; c < 8; ++c) {
+      const long long cid = sg_corner_cell(sc, dx, dy, dz, c);
+      if (cid < 0) continue;
+      float w = 0.125f;
+      for (int a = 0; a < 3; ++a) w *= kCorner[c][a] ? 1.f + b.xxn[a * NP + i] : 1.f - b.xxn[a * NP + i];
+      const long long qp = quant(w * pv, sp), qv = quant(w * v, sv);
+      if (qp) atomicAdd(&acc[cid], (unsigned long long)qp);
+      if (qv) atomicAdd(&acc[nc + cid], (unsigned long long)qv);
+    }
+    return;
+  }
+  const int cl = b.cell[i];
+  if (cl < 0) return;
+  int c[3];
+  c[2] = cl / sc.NCxy;
+  c[1] = (cl - c[2] * sc.NCxy) / sc.NCx;
+  c[0] = cl - c[2] * sc.NCxy - c[1] * sc.NCx;
+  float off[3];
+  for (int a = 0; a < 3; ++a)
+    off[a] = sc.shape == 0 ? b.off[a * NP + i] : (float)((b.x[a * NP + i] - sc.span0[a]) * sc.idcell - (double)c[a]);
+  const int tlo = sc.shape == 0 ? 0 : -1, thi = sc.shape == 1 ? 2 : 1;
+  float w1[3][4];
+  for (int a = 0; a < 3; ++a)
+    for (int t = tlo; t <= thi; ++t) {
+      float w, dd;
+      if (sc.shape == 0) lin1(t, off[a], w, dd);
+      else if (sc.shape == 2) bsp1(t, off[a], w, dd);
+      else gimp1((float)(-t) + off[a], w, dd);
+      w1[a][t + 1] = w;
+    }
+  for (int tz = tlo; tz <= thi; ++tz)
+    for (int ty = tlo; ty <= thi; ++ty)
+      for (int tx = tlo; tx <= thi; ++tx) {
+        const float w = w1[0][tx + 1] * w1[1][ty + 1] * w1[2][tz + 1];
+        const int jx = c[0] + tx, jy = c[1] + ty, jz = c[2] + tz;
+        if (w == 0.f || jx < 0 || jx >= sc.NGx || jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
+        const long long n = ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
+        const long long qp = quant(w * pv, sp), qv = quant(w * v, sv);
+        if (qp) atomicAdd(&acc[n], (unsigned long long)qp);
+        if (qv) atomicAdd(&acc[sc.nn + n], (unsigned long long)qv);
+      }
+}
+
+// Gpre per node of the scene: the ratio of the sums where volume arrived
+// (SGMP: of 1/8 of every adjacent cell's sums; every node counts as mapped,
+// 0/0 where none arrived)
+__global__ void kb_smooth_node(BState b, int scene, const unsigned* bnd, const unsigned long long* acc, double* gpre) {
+  const Scene& sc = b.scenes[scene];
+  const long long ln = btid();
+  if (ln >= sc.nn) return;
+  const double up = q_unit(q_shift(sc, bnd[0])), uv = q_unit(q_shift(sc, bnd[1]));
+  if (sc.shape == 3) {
+    int j[3];
+    node_xyz(sc, ln, j[0], j[1], j[2]);
+    long long qp = 0, qv = 0;
+    for (int cz = j[2] - 1; cz <= j[2]; ++cz) {
+      if (cz < 0 || cz >= sc.NCz) continue;
+      for (int cy = j[1] - 1; cy <= j[1]; ++cy) {
+        if (cy < 0 || cy >= sc.NCy) continue;
+        for (int cx = j[0] - 1; cx <= j[0]; ++cx) {
+          if (cx < 0 || cx >= sc.NCx) continue;
+          const long long c = ((long long)cz * sc.NCy + cy) * sc.NCx + cx;
+          qp += (long long)acc[c];
+          qv += (long long)acc[sc.nc + c];
+        }
+      }
+    }
+    gpre[ln] = (0.125 * ((double)qp * up)) / (0.125 * ((double)qv * uv));
+    return;
+  }
+  const long long qv = (long long)acc[sc.nn + ln];
+  gpre[ln] = qv != 0 ? ((double)(long long)acc[ln] * up) / ((double)qv * uv) : 0.0;
+}
+
+// SGMP: nodes above the cut-off mass -> centre nodes
+__global__ void kb_smooth_back(BState b, int scene, const double* gpre, double* cgpre) {
+  const Scene& sc = b.scenes[scene];
+  const long long c = btid();
+  if (c >= sc.nc) return;
+  const int cz = (int)(c / sc.NCxy), rem = (int)(c - (long long)cz * sc.NCxy), cy = rem / sc.NCx, cx = rem - cy * sc.NCx;
+  double g = 0.0;
+  for (int k = 0; k < 8; ++k) {
+    const long long ln = ((long long)(cz + kCorner[k][2]) * sc.NGy + cy + kCorner[k][1]) * sc.NGx + cx + kCorner[k][0];
+    if (b.mg[sc.n0 + ln] > sc.cutoff) g = g + 0.125 * gpre[ln];
+  }
+  cgpre[c] = g;
+}
+
+// (centre) nodes -> particles: Spre in the scene's input order
+__global__ void kb_smooth_g2p(BState b, int scene, const double* gpre, const double* cgpre, double* spre) {
+  const Scene& sc = b.scenes[scene];
+  const long long k = btid();
+  if (k >= sc.np) return;
+  const long long i = sc.p0 + k, NP = b.NP;
+  double s = 0.0;
+  if (sc.shape == 3) {
+    const int d = b.dual[i];
+    if (d >= 0) {
+      const int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+      for (int c = 0; c < 8; ++c) {
+        const long long cid = sg_corner_cell(sc, dx, dy, dz, c);
+        if (cid < 0) continue;
+        float w = 0.125f;
+        for (int a = 0; a < 3; ++a) w *= kCorner[c][a] ? 1.f + b.xxn[a * NP + i] : 1.f - b.xxn[a * NP + i];
+        s = s + (double)w * cgpre[cid];
+      }
+    }
+  } else if (b.cell[i] >= 0) {
+    const int cl = b.cell[i];
+    int c[3];
+    c[2] = cl / sc.NCxy;
+    c[1] = (cl - c[2] * sc.NCxy) / sc.NCx;
+    c[0] = cl - c[2] * sc.NCxy - c[1] * sc.NCx;
+    float off[3];
+    for (int a = 0; a < 3; ++a)
+      off[a] = sc.shape == 0 ? b.off[a * NP + i] : (float)((b.x[a * NP + i] - sc.span0[a]) * sc.idcell - (double)c[a]);
+    const int tlo = sc.shape == 0 ? 0 : -1, thi = sc.shape == 1 ? 2 : 1;
+    float w1[3][4];
+    for (int a = 0; a < 3; ++a)
+      for (int t = tlo; t <= thi; ++t) {
+        float w, dd;
+        if (sc.shape == 0) lin1(t, off[a], w, dd);
+        else if (sc.shape == 2) bsp1(t, off[a], w, dd);
+        else gimp1((float)(-t) + off[a], w, dd);
+        w1[a][t + 1] = w;
+      }
+    for (int tz = tlo; tz <= thi; ++tz)
+      for (int ty = tlo; ty <= thi; ++ty)
+        for (int tx = tlo; tx <= thi; ++tx) {
+          const float w = w1[0][tx + 1] * w1[1][ty + 1] * w1[2][tz + 1];
+          const int jx = c[0] + tx, jy = c[1] + ty, jz = c[2] + tz;
+          if (w == 0.f || jx < 0 || jx >= sc.NGx || jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
+          s = s + (double)w * gpre[((long long)jz * sc.NGy + jy) * sc.NGx + jx];
+        }
+  }
+  spre[b.orig[i]] = s;
 }
 
 // SGMP centre-node mass (comp -1) or momentum component of a scene from

@@ -49,6 +49,7 @@ struct mpm_ctx {
   int device = 0;
   int flags = 0;
   int drdamp = 0;
+  int smooth = 0;  // SmoothStressbyGrid after every step ('smoo')
   cudaStream_t stream = nullptr;
   DevState<double, double> st{};  // pointer layout is the same for every form
   std::vector<void*> allocs;
@@ -120,7 +121,7 @@ const char* const kKernelNames[K_COUNT] = {
     "stress_update", "depeff_tail", "force_prep", "p2g_force_integrate", "integrate", "g2p_position",
     "p2g_musl", "reduce_energy_dt", "dr_damping", "permute",
     "p2g_mass_scatter", "p2g_force_scatter", "p2g_musl_scatter", "sgmp_centre_clear",
-    "sgmp_centre_gradient", "sgmp_centre_velocity"};
+    "sgmp_centre_gradient", "sgmp_centre_velocity", "stress_smoothing"};
 
 static thread_local Profiler* t_prof = nullptr;
 void prof_set_current(Profiler* p) { t_prof = p; }
@@ -246,6 +247,7 @@ __global__ void k_gather(DevState<double, double> s, long long np, const GatherI
     case MPM_P_ICELL: v = s.icell[p]; break;
     case MPM_P_CENTERICELL: v = s.centericell[p]; break;
     case MPM_P_INODE: v = s.inode[p]; break;
+    case MPM_P_SPRE: v = s.spre ? s.spre[p] : 0.0; break;
     default: v = 0.0; break;
   }
   out[k] = v;
@@ -319,6 +321,18 @@ int build_pairs(mpm_ctx* c) {
   return sort_pairs(c);
 }
 
+// SmoothStressbyGrid: shapes and pairs of the step's cells, then the maps
+int smooth_pass(mpm_ctx* c) {
+  if (!c->st.spre) return set_err(c, MPM_ERR_ARG, "stress smoothing is off for this deck (no 'smoo')");
+  cudaError_t e = cudaMemsetAsync(c->st.seg, 0, sizeof(int) * ((size_t)c->nkeys + 1), c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "memset seg");
+  c->ops->smooth_locate(&c->st, c->g, c->stream);
+  int r = sort_pairs(c);
+  if (r) return r;
+  c->ops->smooth(&c->st, c->g, c->stream);
+  return MPM_OK;
+}
+
 int stress_pass(mpm_ctx* c) {
   c->ops->stress(&c->st, c->g, c->stream);
   return depeff_pass(c);
@@ -343,6 +357,8 @@ int enqueue_step(mpm_ctx* c) {
   if (!g.usf)
     if ((r = stress_pass(c))) return r;
   o->reduce(st, g, 3, c->red_blocks, s);
+  if (c->smooth)
+    if ((r = smooth_pass(c))) return r;
   if (c->drdamp) o->dr_damping(st, g, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_err(c, e, "kernel launch");
@@ -381,7 +397,7 @@ int mpm_field_components(int f) {
     case MPM_P_FP: return 9;
     case MPM_P_VOL: case MPM_P_VOL0: case MPM_P_SIG_Y: case MPM_P_SM: case MPM_P_SEQV: case MPM_P_EPEFF:
     case MPM_P_CELSIUS: case MPM_P_DMG: case MPM_P_LT: case MPM_P_IE: case MPM_P_MASS: case MPM_P_CP:
-    case MPM_P_Q: case MPM_P_FAILURE: case MPM_P_ICELL: case MPM_P_CENTERICELL: case MPM_P_INODE:
+    case MPM_P_Q: case MPM_P_FAILURE: case MPM_P_ICELL: case MPM_P_CENTERICELL: case MPM_P_INODE: case MPM_P_SPRE:
     case MPM_G_MG: case MPM_C_MG:
       return 1;
     default: return 0;
@@ -431,6 +447,7 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
   }
   c->flags = d->flags;
   c->drdamp = !!(d->flags & MPM_F_DRDAMP);
+  c->smooth = !!(d->flags & MPM_F_SMOOTH);
   if (precision == MPM_MIXED) {
     // the mixed form is the batched engine running a batch of one scene; the
     // deck's arrays are uploaded in place (committed before returning)
@@ -510,6 +527,10 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
       AL(s.setter, int, np); AL(s.setter_scan, int, np); AL(s.dep, double, np);
       AL(s.jc_aux, double, 5 * np); AL(s.deferred, uint8_t, np);
     }
+    if (c->smooth) {
+      AL(s.spre, double, np); AL(s.gpre, double, nn);
+      if (g.shape == 3) { AL(s.cgpre, double, nc); AL(s.cgvall, double, nc); }
+    }
     AL(s.red_part, double, (long long)kRedVals * c->red_blocks); AL(s.red_count, unsigned, 1);
     AL(s.mats, DevMaterial, (long long)c->mats.size()); AL(s.bodies, DevBody, (long long)c->bodies.size());
     AL(s.sc, DevScalars, 1);
@@ -570,6 +591,7 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     CKF(cudaMemsetAsync(s.fx, 0, sizeof(double) * 3 * nn, c->stream));
     CKF(cudaMemsetAsync(s.vg, 0, sizeof(double) * 3 * nn, c->stream));
     CKF(cudaMemsetAsync(s.red_count, 0, sizeof(unsigned), c->stream));
+    if (s.spre) CKF(cudaMemsetAsync(s.spre, 0, sizeof(double) * np, c->stream));
     DevScalars sc0;
     memset(&sc0, 0, sizeof sc0);
     sc0.dt = set_dt(c->mats, g.dcell, g.dtscale);
@@ -633,6 +655,9 @@ int mpm_step_phase(mpm_ctx* c, int phase) {
     case MPM_PHASE_CALC_ENERGY: o->reduce(st, g, 1, c->red_blocks, s); break;
     case MPM_PHASE_UPDATE_DT: o->reduce(st, g, 2, c->red_blocks, s); break;
     case MPM_PHASE_DR_DAMPING: o->dr_damping(st, g, s); break;
+    case MPM_PHASE_SMOOTH_STRESS:
+      if ((r = smooth_pass(c))) return r;
+      break;
     default: return set_err(c, MPM_ERR_ARG, "unknown phase %d", phase);
   }
   cudaError_t e = cudaGetLastError();
@@ -762,6 +787,7 @@ static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long*
     case MPM_P_ICELL: *ptr = s.icell; *elem = 4; break;
     case MPM_P_CENTERICELL: *ptr = s.centericell; *elem = 4; break;
     case MPM_P_INODE: *ptr = s.inode; *elem = 4; break;
+    case MPM_P_SPRE: *ptr = s.spre; break;  // null without 'smoo': reads as zeros
     case MPM_G_MG: *ptr = s.mg; *count = nn; break;
     case MPM_G_PX: *ptr = s.px; *count = 3 * nn; break;
     case MPM_G_FX: *ptr = s.fx; *count = 3 * nn; break;
@@ -785,6 +811,10 @@ int mpm_download(mpm_ctx* c, int field, double* out) {
   int r = field_ptr(c, field, &p, &elem, &n);
   if (r) return r;
   CK(cudaStreamSynchronize(c->stream));
+  if (!p) {  // a field the deck does not switch on (Spre without 'smoo'): zero, as in the reference
+    memset(out, 0, sizeof(double) * (size_t)n);
+    return MPM_OK;
+  }
   if (elem == 8) {
     CK(cudaMemcpy(out, p, (size_t)n * 8, cudaMemcpyDeviceToHost));
     return MPM_OK;
@@ -806,7 +836,7 @@ int mpm_upload(mpm_ctx* c, int field, const double* in) {
   if (!c || !in) return set_err(c, MPM_ERR_ARG, "bad argument");
   if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "the mixed form takes its state from the deck only");
   if (field >= MPM_G_MG || field == MPM_P_ICELL || field == MPM_P_CENTERICELL || field == MPM_P_INODE ||
-      field == MPM_P_FAILURE)
+      field == MPM_P_FAILURE || field == MPM_P_SPRE)
     return set_err(c, MPM_ERR_ARG, "field %d cannot be uploaded", field);
   void* p = nullptr;
   size_t elem = 0;

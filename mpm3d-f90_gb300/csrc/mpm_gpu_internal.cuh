@@ -20,6 +20,8 @@
 //     vg[3][Nn] (= px/mg), uint8 fix[Nn] (bit c = DOF c fixed), uint8 bd[Nn]
 //   SGMP auxiliary grid (one centre node per cell), FP64: cmg, cpx[3],
 //     cfext[3], cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3].
+//   stress smoothing (decks with 'smoo'), FP64: spre[Np], gpre[Nn],
+//     cgpre[Nc], cgvall[Nc].
 #pragma once
 
 #include <cuda_runtime.h>
@@ -109,6 +111,9 @@ struct DevState {
   uint8_t *fix, *bd;
   // SGMP centre grid
   double *cmg, *cpx, *cfext, *cfint, *co, *cw, *cdefp, *cvx, *cax;
+  // stress smoothing (decks with 'smoo'): Spre per particle, Gpre per node,
+  // CGpre / CGV_all per centre node
+  double *spre, *gpre, *cgpre, *cgvall;
   // Johnson-Cook depeff carry
   int *setter, *setter_scan;
   double *dep;
@@ -145,6 +150,10 @@ struct StepOps {
   // mode bit 0: energies and momentum (calcEnergy), bit 1: next DT (UpdateDT)
   void (*reduce)(void* st, const Geometry& g, int mode, int nblocks, cudaStream_t s);
   void (*dr_damping)(void* st, const Geometry& g, cudaStream_t s);
+  // SmoothStressbyGrid: shapes + pair keys, then (after the pair sort) the
+  // maps to the grid and back
+  void (*smooth_locate)(void* st, const Geometry& g, cudaStream_t s);
+  void (*smooth)(void* st, const Geometry& g, cudaStream_t s);
 };
 
 extern const StepOps kOpsStrict;   // MPM_FP64_STRICT
@@ -157,7 +166,7 @@ void prof_end(int kernel_id, cudaStream_t s);
 enum KernelId {
   K_BEGIN = 0, K_LOCATE, K_SORT, K_SEG, K_P2G_MASS, K_NODE_VEL, K_BC, K_STRESS, K_DEPEFF,
   K_FORCE_PREP, K_P2G_FORCE, K_INTEGRATE, K_POSITION, K_P2G_MOM, K_REDUCE, K_DR, K_PERMUTE,
-  K_SCATTER_MASS, K_SCATTER_FORCE, K_SCATTER_MOM, K_SG_CLEAR, K_SG_GRADIENT, K_SG_VELOCITY,
+  K_SCATTER_MASS, K_SCATTER_FORCE, K_SCATTER_MOM, K_SG_CLEAR, K_SG_GRADIENT, K_SG_VELOCITY, K_SMOOTH,
   K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];

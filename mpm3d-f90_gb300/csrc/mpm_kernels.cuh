@@ -52,60 +52,20 @@ __device__ __forceinline__ void gimp_1d(R rr, R& sh, R& dn) {
   }
 }
 
-// ----------------------------------------------------------------- locate
-// ParticleInitial (update_step.f90:408-453) plus the shape functions of the
-// step (NShape / FindInflNode+NShape_GIMP / BFindInflNode+NShape_Bspline /
-// SGNShape), cached per (slot, particle), and the pair keys of the
-// node-sorted list. Pair j = p*K + k keeps (particle, slot) order for the
-// stable sort; invalid slots get the sentinel key nkeys.
+// Influence slots of particle p (node or, for SGMP, centre-node index per
+// slot, -1 when invalid) and their shape functions, written to the shape
+// cache; returns the number of slots used. x = the position the GIMP and
+// B-spline weights are taken at, icell / xn = the particle's cell and its
+// natural coordinates (linear), cc / xxn = its dual cell and coordinates
+// (SGMP). ParticleInitial passes the state at the start of the step;
+// SmoothStressbyGrid passes the current position with the step's cells.
 template <class P>
-__global__ void k_locate(St<P> s, Geometry g, int nkeys) {
+__device__ __forceinline__ int slot_shapes(St<P>& s, const Geometry& g, long long p, const double x[3], int icell,
+                                           const double xn[3], int cc, const double xxn[3], int slot_node[27]) {
   using R = typename P::R;
-  using B = typename P::B;
-  const long long p = gtid();
-  if (p >= g.np) return;
   const long long np = g.np;
-  const int K = g.K;
-  double x[3] = {s.xp[p], s.xp[np + p], s.xp[2 * np + p]};
-  int icell = in_which_cell(g, x);
-  s.icell[p] = icell;
-  double xn[3] = {0, 0, 0};
-  if (icell > 0) {
-    int n1 = cell_node1(g, icell);
-    for (int d = 0; d < 3; ++d) {
-      double cxg = node_coord(g, n1, d) + g.dcell / 2.0;  // Cxg, Grid.f90:380
-      xn[d] = (x[d] - cxg) * g.iJacobi;
-      s.xn[d * np + p] = (B)xn[d];
-    }
-  } else {
-    atomicOr(&s.sc->status, (unsigned)ST_OUT_OF_GRID);
-  }
   int nvalid = 0;
-  int slot_node[27];
-  if (g.shape == 3) {  // SGMP: the dual (cell-centre) grid
-    int cc = center_in_which_cell(g, x);
-    s.centericell[p] = cc;
-    int ix = (int)((x[0] - g.span0[0]) / g.dcell + 0.5) + 1;
-    int iy = (int)((x[1] - g.span0[1]) / g.dcell + 0.5) + 1;
-    int iz = (int)((x[2] - g.span0[2]) / g.dcell + 0.5) + 1;
-    long long inode = (long long)(iz - 1) * g.NGxy + (long long)(iy - 1) * g.NGx + ix;
-    s.inode[p] = (int)inode;
-    double xxn[3] = {0, 0, 0};
-    if (inode >= 1 && inode <= g.nn) {
-      int bd = s.bd[inode - 1];
-      for (int d = 0; d < 3; ++d) {
-        double xg = node_coord(g, (int)inode - 1, d);
-        xxn[d] = (x[d] - xg) * g.iJacobi;
-        int bt = (bd >> (2 * d)) & 3;
-        if (bt != 0) {
-          if (xxn[d] > 0) xxn[d] = 1;
-          else if (xxn[d] < 0) xxn[d] = -1;
-        }
-        s.xxn[d * np + p] = (B)xxn[d];
-      }
-    } else {
-      for (int d = 0; d < 3; ++d) xxn[d] = (double)s.xxn[d * np + p];
-    }
+  if (g.shape == 3) {
     if (cc > 0) {
       int c = cc - 1;
       int cz = c / g.CNCxy, rem = c - cz * g.CNCxy, cy = rem / g.CNCx, cx = rem - cy * g.CNCx;
@@ -232,6 +192,17 @@ __global__ void k_locate(St<P> s, Geometry g, int nkeys) {
       nvalid = 27;
     }
   }
+  return nvalid;
+}
+
+// pair keys of particle p's slots (node-sorted list; pair j = p*K + k keeps
+// (particle, slot) order for the stable sort; invalid slots get the
+// sentinel key nkeys) and the per-node pair counts
+template <class P>
+__device__ __forceinline__ void write_pairs(St<P>& s, const Geometry& g, long long p, int nvalid,
+                                            const int slot_node[27], int nkeys) {
+  const long long np = g.np;
+  const int K = g.K;
   for (int k = 0; k < K; ++k) {
     int nd = k < nvalid ? slot_node[k] : -1;
     s.snode[k * np + p] = nd;
@@ -240,6 +211,63 @@ __global__ void k_locate(St<P> s, Geometry g, int nkeys) {
     s.val[j] = ((unsigned)p << 5) | (unsigned)k;
     if (nd >= 0) atomicAdd(&s.seg[nd], 1);  // per-node pair count (integer, deterministic)
   }
+}
+
+// ----------------------------------------------------------------- locate
+// ParticleInitial (update_step.f90:408-453) plus the shape functions of the
+// step (NShape / FindInflNode+NShape_GIMP / BFindInflNode+NShape_Bspline /
+// SGNShape), cached per (slot, particle), and the pair keys of the
+// node-sorted list. Pair j = p*K + k keeps (particle, slot) order for the
+// stable sort; invalid slots get the sentinel key nkeys.
+template <class P>
+__global__ void k_locate(St<P> s, Geometry g, int nkeys) {
+  using B = typename P::B;
+  const long long p = gtid();
+  if (p >= g.np) return;
+  const long long np = g.np;
+  double x[3] = {s.xp[p], s.xp[np + p], s.xp[2 * np + p]};
+  int icell = in_which_cell(g, x);
+  s.icell[p] = icell;
+  double xn[3] = {0, 0, 0};
+  if (icell > 0) {
+    int n1 = cell_node1(g, icell);
+    for (int d = 0; d < 3; ++d) {
+      double cxg = node_coord(g, n1, d) + g.dcell / 2.0;  // Cxg, Grid.f90:380
+      xn[d] = (x[d] - cxg) * g.iJacobi;
+      s.xn[d * np + p] = (B)xn[d];
+    }
+  } else {
+    atomicOr(&s.sc->status, (unsigned)ST_OUT_OF_GRID);
+  }
+  int cc = 0;
+  double xxn[3] = {0, 0, 0};
+  if (g.shape == 3) {  // SGMP: the dual (cell-centre) grid
+    cc = center_in_which_cell(g, x);
+    s.centericell[p] = cc;
+    int ix = (int)((x[0] - g.span0[0]) / g.dcell + 0.5) + 1;
+    int iy = (int)((x[1] - g.span0[1]) / g.dcell + 0.5) + 1;
+    int iz = (int)((x[2] - g.span0[2]) / g.dcell + 0.5) + 1;
+    long long inode = (long long)(iz - 1) * g.NGxy + (long long)(iy - 1) * g.NGx + ix;
+    s.inode[p] = (int)inode;
+    if (inode >= 1 && inode <= g.nn) {
+      int bd = s.bd[inode - 1];
+      for (int d = 0; d < 3; ++d) {
+        double xg = node_coord(g, (int)inode - 1, d);
+        xxn[d] = (x[d] - xg) * g.iJacobi;
+        int bt = (bd >> (2 * d)) & 3;
+        if (bt != 0) {
+          if (xxn[d] > 0) xxn[d] = 1;
+          else if (xxn[d] < 0) xxn[d] = -1;
+        }
+        s.xxn[d * np + p] = (B)xxn[d];
+      }
+    } else {
+      for (int d = 0; d < 3; ++d) xxn[d] = (double)s.xxn[d * np + p];
+    }
+  }
+  int slot_node[27];
+  const int nvalid = slot_shapes<P>(s, g, p, x, icell, xn, cc, xxn, slot_node);
+  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys);
 }
 
 __device__ __forceinline__ void decode_pair(unsigned v, long long np, long long* p, long long* idx) {
@@ -1309,6 +1337,117 @@ __global__ void k_sg_node_momentum(St<P> s, Geometry g, int vel) {
   s.px[2LL * nn + n] = pz;
   node_bc(s.fix[n], s.px, s.fx, (int)n, nn);
   if (vel) node_vel(s.mg, s.px, s.vg, (int)n, nn, g.cutoff);
+}
+
+// ====================================================== stress smoothing
+// SmoothStressbyGrid (update_step.f90:1876-2055): the particles' pressure
+// -SM mapped to the grid with volume weights, normalised by the mapped
+// volume, and interpolated back into Spre. Runs after UpdateDT with the
+// shapes of the step's cells: GIMP and B-spline weights at the current Xp
+// against the cell found at the start of the step, linear ones at XN, SGMP
+// ones at XXN (the reference recomputes them from those fields). The pair
+// list is rebuilt for these shapes and every sum runs in the reference's
+// order (ascending particle per node or centre node; ascending cell per node;
+// slot order per particle).
+
+// the smoothing shapes and pair keys of every particle
+template <class P>
+__global__ void k_smooth_locate(St<P> s, Geometry g, int nkeys) {
+  const long long p = gtid();
+  if (p >= g.np) return;
+  const long long np = g.np;
+  const double x[3] = {s.xp[p], s.xp[np + p], s.xp[2 * np + p]};
+  const int icell = s.icell[p];
+  double xn[3] = {0, 0, 0}, xxn[3] = {0, 0, 0};
+  for (int d = 0; d < 3; ++d) {
+    xn[d] = (double)s.xn[d * np + p];
+    if (g.shape == 3) xxn[d] = (double)s.xxn[d * np + p];
+  }
+  const int cc = g.shape == 3 ? s.centericell[p] : 0;
+  int slot_node[27];
+  const int nvalid = slot_shapes<P>(s, g, p, x, g.shape == 3 ? 0 : icell, xn, cc, xxn, slot_node);
+  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys);
+}
+
+// pressure * volume and volume of one (node or centre node) slice of pairs,
+// in particle order; returns false for an empty slice
+template <class P>
+__device__ __forceinline__ bool smooth_sums(const St<P>& s, long long np, int j0, int j1, double& gp, double& gv) {
+  gp = 0.0;
+  gv = 0.0;
+  for (int j = j0; j < j1; ++j) {
+    long long p, idx;
+    decode_pair(s.val_sorted[j], np, &p, &idx);
+    const double shp = (double)s.shp[idx], sm = (double)s.sm[p], vol = (double)s.vol[p];
+    gp = gp + shp * (-1 * sm) * vol;
+    gv = gv + shp * vol;
+  }
+  return j1 > j0;
+}
+
+// particles -> nodes, Gpre / GV_all on the mapped nodes
+template <class P>
+__global__ void k_smooth_node(St<P> s, Geometry g) {
+  const long long n = gtid();
+  if (n >= g.nn) return;
+  double gp, gv;
+  const bool mapped = smooth_sums<P>(s, g.np, n == 0 ? 0 : s.seg[n - 1], s.seg[n], gp, gv);
+  s.gpre[n] = mapped ? gp / gv : gp;
+}
+
+// SGMP: particles -> centre nodes
+template <class P>
+__global__ void k_smooth_cell(St<P> s, Geometry g) {
+  const long long c = gtid();
+  if (c >= g.ncell) return;
+  double gp, gv;
+  smooth_sums<P>(s, g.np, c == 0 ? 0 : s.seg[c - 1], s.seg[c], gp, gv);
+  s.cgpre[c] = gp;
+  s.cgvall[c] = gv;
+}
+
+// SGMP: centre nodes -> nodes (1/8 of every adjacent cell; every node is
+// mapped, 0/0 where no volume reached it)
+template <class P>
+__global__ void k_smooth_sg_node(St<P> s, Geometry g) {
+  const long long n = gtid();
+  if (n >= g.nn) return;
+  double gp = 0.0, gv = 0.0;
+  for_adjacent_cells(g, n, [&](int c, int) {
+    gp = gp + 0.125 * s.cgpre[c];
+    gv = gv + 0.125 * s.cgvall[c];
+  });
+  s.gpre[n] = gp / gv;
+}
+
+// SGMP: nodes above the cut-off mass -> centre nodes
+template <class P>
+__global__ void k_smooth_sg_back(St<P> s, Geometry g) {
+  const long long c = gtid();
+  if (c >= g.ncell) return;
+  const int n1 = cell_node1(g, (int)c + 1);
+  double cp = 0.0;
+  for (int j = 0; j < 8; ++j) {
+    const int n = n1 + kCorner[j][0] + kCorner[j][1] * g.NGx + kCorner[j][2] * g.NGxy;
+    if (s.mg[n] > g.cutoff) cp = cp + 0.125 * s.gpre[n];
+  }
+  s.cgpre[c] = cp;
+}
+
+// (centre) nodes -> particles: Spre
+template <class P>
+__global__ void k_smooth_g2p(St<P> s, Geometry g) {
+  const long long p = gtid();
+  if (p >= g.np) return;
+  const long long np = g.np;
+  const double* src = g.shape == 3 ? s.cgpre : s.gpre;
+  double sp = 0.0;
+  for (int k = 0; k < g.K; ++k) {
+    const int nd = s.snode[k * np + p];
+    if (nd < 0) continue;
+    sp = sp + (double)s.shp[k * np + p] * src[nd];
+  }
+  s.spre[p] = sp;
 }
 
 // ============================================================ reductions

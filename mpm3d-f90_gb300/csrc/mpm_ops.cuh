@@ -103,6 +103,24 @@ struct Ops {
     prof_end(K_DR, s);
   }
 
+  static void smooth_locate(void* st, const Geometry& g, cudaStream_t s) {
+    prof_begin(K_SMOOTH, s);
+    k_smooth_locate<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g, g.shape == 3 ? g.ncell : g.nn);
+    prof_end(K_SMOOTH, s);
+  }
+  static void smooth(void* st, const Geometry& g, cudaStream_t s) {
+    prof_begin(K_SMOOTH, s);
+    if (g.shape == 3) {
+      k_smooth_cell<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
+      k_smooth_sg_node<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g);
+      k_smooth_sg_back<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
+    } else {
+      k_smooth_node<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g);
+    }
+    k_smooth_g2p<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g);
+    prof_end(K_SMOOTH, s);
+  }
+
   static StepOps table(const char* name) {
     StepOps o;
     o.name = name;
@@ -123,6 +141,8 @@ struct Ops {
     o.p2g_momentum = p2g_momentum;
     o.reduce = reduce;
     o.dr_damping = dr_damping;
+    o.smooth_locate = smooth_locate;
+    o.smooth = smooth;
     return o;
   }
 };

@@ -364,9 +364,9 @@ static int paraview_frame(mpm_output* o, const double* s, const mpm_particle_vie
   pv_array(f, "seqv", np, v->seqv, 1.0, NULL);
   pv_array(f, "epeff", np, v->epeff, 1.0, NULL);
   pv_array(f, "pressure", np, v->sm, -1.0, NULL);
-  pv_array(f, "Smoothpressure", np, NULL, 1.0, NULL);
+  pv_array(f, "Smoothpressure", np, v->spre, 1.0, NULL);
   pv_array(f, "MeanNormalStress", np, v->sm, 1.0, NULL);
-  pv_array(f, "SmoothMeanNormalStress", np, NULL, -1.0, NULL);
+  pv_array(f, "SmoothMeanNormalStress", np, v->spre, -1.0, NULL);
   pv_array(f, "vx", np, v->vxp, 1.0, NULL);
   pv_array(f, "vy", np, v->vxp + np, 1.0, NULL);
   pv_array(f, "vz", np, v->vxp + 2 * np, 1.0, NULL);

@@ -39,7 +39,8 @@ static int anim_frame(mpm_ctx* c, const mpm_deck* d, mpm_output* out, const doub
     int field, ncomp;
   } want[] = {{MPM_P_XP, 3},   {MPM_P_VXP, 3},  {MPM_P_FXP, 3},     {MPM_P_MASS, 1}, {MPM_P_SEQV, 1},
               {MPM_P_EPEFF, 1}, {MPM_P_SM, 1},   {MPM_P_VOL, 1},     {MPM_P_IE, 1},   {MPM_P_CELSIUS, 1},
-              {MPM_P_CP, 1},    {MPM_P_DMG, 1},  {MPM_P_SD, 6},      {MPM_P_FAILURE, 1}, {MPM_P_ICELL, 1}};
+              {MPM_P_CP, 1},    {MPM_P_DMG, 1},  {MPM_P_SD, 6},      {MPM_P_FAILURE, 1}, {MPM_P_ICELL, 1},
+              {MPM_P_SPRE, 1}};
   enum { NW = sizeof want / sizeof want[0] };
   double* a[NW];
   for (int k = 0; k < NW; ++k) {
@@ -49,7 +50,8 @@ static int anim_frame(mpm_ctx* c, const mpm_deck* d, mpm_output* out, const doub
       a[k] = NULL;
     }
   }
-  mpm_particle_view v = {a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10], a[11], a[12], a[13], a[14]};
+  mpm_particle_view v = {a[0], a[1], a[2],  a[3],  a[4],  a[5],  a[6], a[7],
+                         a[8], a[9], a[10], a[11], a[12], a[13], a[14], a[15]};
   int st = mpm_output_anim(out, s, &v);
   for (int k = 0; k < NW; ++k) free(a[k]);
   if (st) fprintf(stderr, "animation output error %d\n", st);

@@ -35,7 +35,7 @@ FIELDS = {
     "Xp": 1, "XX": 2, "VXp": 3, "FXp": 4, "XN": 5, "XXN": 6, "VOL": 7, "VOL0": 8, "sig_y": 9,
     "SM": 10, "Seqv": 11, "SD": 12, "Fp": 13, "epeff": 14, "celsius_t": 15, "DMG": 16, "LT": 17,
     "ie": 18, "mass": 19, "cp": 20, "q": 21, "failure": 22, "icell": 23, "centericell": 24,
-    "inode": 25, "Mg": 40, "PXg": 41, "FXg": 42, "Cmg": 50, "Cpxg": 51,
+    "inode": 25, "Spre": 26, "Mg": 40, "PXg": 41, "FXg": 42, "Cmg": 50, "Cpxg": 51,
 }
 COMPONENTS = {"Xp": 3, "XX": 3, "VXp": 3, "FXp": 3, "XN": 3, "XXN": 3, "SD": 6, "Fp": 9,
               "PXg": 3, "FXg": 3, "Cpxg": 3}
@@ -46,7 +46,7 @@ PHASES = {
     "GridMomentumInitial": 1, "ApplyBoundaryConditions": 2, "ParticleStressUpdate": 3,
     "GridMomentumUpdate": 4, "IntegrateMomentum": 5, "ParticlePositionUpdate": 6,
     "GridMomentumMUSL": 7, "calcEnergy": 8, "UpdateDT": 9, "dynamicRelaxationDamping": 10,
-    "BeginStep": 11,
+    "BeginStep": 11, "SmoothStressbyGrid": 12,
 }
 
 SCALARS = ("istep", "CurrentTime", "DT", "EngKinetic", "EngInternal", "Momentum_x",
@@ -305,6 +305,9 @@ class MpmStep:
     def dynamicRelaxationDamping(self):
         self.phase("dynamicRelaxationDamping")
 
+    def SmoothStressbyGrid(self):
+        self.phase("SmoothStressbyGrid")
+
     # -- whole steps
     def step(self) -> None:
         self._check(library().mpm_step(self._h))
@@ -520,7 +523,7 @@ class Batch:
 class _ParticleView(ctypes.Structure):
     _fields_ = [(n, ctypes.POINTER(ctypes.c_double)) for n in
                 ("xp", "vxp", "fxp", "mass", "seqv", "epeff", "sm", "vol", "ie", "celsius", "cp", "dmg", "sd",
-                 "failure", "icell")]
+                 "failure", "icell", "spre")]
 
 
 def format_e(w: int, d: int, x: float) -> str:
@@ -536,7 +539,7 @@ class Output:
 
     VIEW_FIELDS = {"xp": "Xp", "vxp": "VXp", "fxp": "FXp", "mass": "mass", "seqv": "Seqv", "epeff": "epeff",
                    "sm": "SM", "vol": "VOL", "ie": "ie", "celsius": "celsius_t", "cp": "cp", "dmg": "DMG",
-                   "sd": "SD", "failure": "failure", "icell": "icell"}
+                   "sd": "SD", "failure": "failure", "icell": "icell", "spre": "Spre"}
 
     def __init__(self, deck: Deck, job: str, plot_dir: Optional[str] = None):
         h = ctypes.c_void_p()

@@ -9,8 +9,9 @@
  *
  * Scope: the updated-Lagrangian step (MPM3D.f90:68-160) with linear, GIMP,
  * B-spline and SGMP shape functions, USF / USL / MUSL, material types 1-11
- * and EOS 1-4. Contact (Lagr_NodContact), stress smoothing and TLMPM are not
- * restated; orc_create rejects decks that switch them on.
+ * and EOS 1-4, and the stress smoothing of SmoothStressbyGrid. Contact
+ * (Lagr_NodContact) and TLMPM are not restated; orc_create rejects decks that
+ * switch them on.
  */
 #include "mpm_oracle.h"
 
@@ -32,6 +33,7 @@ typedef struct opart {
   double epeff, celsius_t;
   int failure, icell, centericell;
   double DMG, LT, ie, mass, cp, q;
+  double Spre; /* smoothed pressure (Particle.f90:40) */
 } opart;
 
 typedef struct onode {
@@ -42,10 +44,13 @@ typedef struct onode {
 
 typedef struct ogrid {
   double Mg, PXg[3], FXg[3];
+  double Gpre, GV_all; /* stress smoothing (Grid.f90:41-43) */
+  int mapped;
 } ogrid;
 
 typedef struct ocellp {
   double Cmg, Cpxg[3], Cfint[6], Cfext[3], Cvx[3], Cax[3], Co[6], Cw[3], CdeFp[3][3];
+  double CGpre, CGV_all; /* stress smoothing (Grid.f90:62-64) */
 } ocellp;
 
 struct orc {
@@ -56,7 +61,7 @@ struct orc {
   mpm_body* body;
   int nb_mat;
   mpm_material* mat;
-  int MUSL, USL, USF, GIMP, Bspline, SGMP, QuasiLoad, QuasiDamp, UpdateVbyFp, Gravity, DR_DAMPING;
+  int MUSL, USL, USF, GIMP, Bspline, SGMP, QuasiLoad, QuasiDamp, UpdateVbyFp, Gravity, DR_DAMPING, SmoothStress;
   int istep;
   double DT, QuasiLoadTime, DampFactor, CurrentTime, EndTime, DTScale;
   double EngInternal, EngKinetic, EngKinetic_prev, Momentum[3];
@@ -1710,6 +1715,93 @@ static void update_dt(orc* o) {
   o->DT = o->DT * o->DTScale;
 }
 
+/* SmoothStressbyGrid, update_step.f90:1876-2055: the particles' pressure
+ * -SM mapped to the grid with volume weights, normalised by the mapped
+ * volume, and interpolated back (Spre). The shapes are those of the
+ * step's cells: GIMP and B-spline weights use the current Xp against the
+ * cell found at the start of the step, linear ones XN, SGMP ones XXN. With
+ * SGMP the map goes through the centre nodes (every grid node counts as
+ * mapped, so a node without volume gets 0/0) and back through nodes above
+ * the cut-off mass. */
+static void smooth_stress(orc* o) {
+  for (int n = 0; n < o->nb_gridnode; ++n) {
+    o->grid[n].Gpre = 0.0;
+    o->grid[n].GV_all = 0.0;
+    o->grid[n].mapped = 0;
+  }
+  if (o->SGMP)
+    for (int c = 0; c < o->nb_centernode; ++c) {
+      o->cellp[c].CGpre = 0.0;
+      o->cellp[c].CGV_all = 0.0;
+    }
+  for (int b = 0; b < o->nb_body; ++b)
+    for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
+      opart* p = &o->pt[ip];
+      if (o->SGMP) {
+        if (p->centericell < 0) continue;
+        for (int n = 0; n < 8; ++n) o->CenterInflNode[n] = o->CenterCellNode[p->centericell - 1][n];
+        sg_nshape(o, p->XXN);
+        for (int n = 0; n < 8; ++n) {
+          if (!center_valid(o, o->CenterInflNode[n])) continue;
+          ocellp* cd = &o->cellp[o->CenterInflNode[n] - 1];
+          double SHPn = o->SHP[n];
+          cd->CGpre = cd->CGpre + SHPn * (-1 * p->SM) * p->VOL;
+          cd->CGV_all = cd->CGV_all + SHPn * p->VOL;
+        }
+      } else {
+        if (p->icell < 0) continue;
+        particle_shape(o, p, p->icell);
+        for (int n = 0; n < o->nb_InflNode; ++n) {
+          if (!node_valid(o, o->InflNode[n])) continue;
+          ogrid* gd = &o->grid[o->InflNode[n] - 1];
+          gd->mapped = 1;
+          double SHPn = o->SHP[n];
+          gd->Gpre = gd->Gpre + SHPn * (-1 * p->SM) * p->VOL;
+          gd->GV_all = gd->GV_all + SHPn * p->VOL;
+        }
+      }
+    }
+  if (o->SGMP)
+    for (int i = 0; i < o->nb_centernode; ++i)
+      for (int j = 0; j < 8; ++j) {
+        ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
+        gd->mapped = 1;
+        gd->Gpre = gd->Gpre + 0.125 * o->cellp[i].CGpre;
+        gd->GV_all = gd->GV_all + 0.125 * o->cellp[i].CGV_all;
+      }
+  for (int n = 0; n < o->nb_gridnode; ++n)
+    if (o->grid[n].mapped) o->grid[n].Gpre = o->grid[n].Gpre / o->grid[n].GV_all;
+  if (o->SGMP) {
+    for (int i = 0; i < o->nb_centernode; ++i) o->cellp[i].CGpre = 0.0;
+    for (int i = 0; i < o->nb_centernode; ++i)
+      for (int j = 0; j < 8; ++j) {
+        const ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
+        if (gd->Mg > o->CutOff) o->cellp[i].CGpre = o->cellp[i].CGpre + 0.125 * gd->Gpre;
+      }
+  }
+  for (int b = 0; b < o->nb_body; ++b)
+    for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
+      opart* p = &o->pt[ip];
+      p->Spre = 0;
+      if (o->SGMP) {
+        if (p->centericell < 0) continue;
+        for (int n = 0; n < 8; ++n) o->CenterInflNode[n] = o->CenterCellNode[p->centericell - 1][n];
+        sg_nshape(o, p->XXN);
+        for (int n = 0; n < 8; ++n) {
+          if (!center_valid(o, o->CenterInflNode[n])) continue;
+          p->Spre = p->Spre + o->SHP[n] * o->cellp[o->CenterInflNode[n] - 1].CGpre;
+        }
+      } else {
+        if (p->icell < 0) continue;
+        particle_shape(o, p, p->icell);
+        for (int n = 0; n < o->nb_InflNode; ++n) {
+          if (!node_valid(o, o->InflNode[n])) continue;
+          p->Spre = p->Spre + o->SHP[n] * o->grid[o->InflNode[n] - 1].Gpre;
+        }
+      }
+    }
+}
+
 /* ====================================================================
  * driver
  * ==================================================================== */
@@ -1732,6 +1824,7 @@ int orc_phase(orc* o, int phase) {
     case MPM_PHASE_CALC_ENERGY: calc_energy(o); return MPM_OK;
     case MPM_PHASE_UPDATE_DT: update_dt(o); return MPM_OK;
     case MPM_PHASE_DR_DAMPING: dr_damping(o); return MPM_OK;
+    case MPM_PHASE_SMOOTH_STRESS: smooth_stress(o); return MPM_OK;
     default: return oerr(o, MPM_ERR_ARG, "unknown phase %d", phase);
   }
 }
@@ -1757,6 +1850,7 @@ int orc_step(orc* o) {
   }
   calc_energy(o);
   update_dt(o);
+  if (o->SmoothStress) smooth_stress(o);
   if (o->DR_DAMPING) dr_damping(o);
   return MPM_OK;
 }
@@ -1775,11 +1869,8 @@ int orc_create(const mpm_deck* d, int libm_mode, orc** out) {
   orc* o = (orc*)calloc(1, sizeof(orc));
   if (!o) return MPM_ERR_OOM;
   *out = o;
-  if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM | MPM_F_SMOOTH)) {
-    /* smoothing only writes the plotted Spre; contact and TLMPM change the step */
-    if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM))
-      return oerr(o, MPM_ERR_UNSUPPORTED, "contact / TLMPM are outside the restated step");
-  }
+  if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM))
+    return oerr(o, MPM_ERR_UNSUPPORTED, "contact / TLMPM are outside the restated step");
   if (libm_mode == ORC_LIBM_PROJECT) {
     o->f_log = proj_log; o->f_exp = proj_exp; o->f_pow = proj_pow;
   } else {
@@ -1791,6 +1882,7 @@ int orc_create(const mpm_deck* d, int libm_mode, orc** out) {
   o->QuasiLoad = !!(f & MPM_F_QUASILOAD); o->QuasiDamp = !!(f & MPM_F_QUASIDAMP);
   o->UpdateVbyFp = !!(f & MPM_F_UVFP); o->Gravity = !!(f & MPM_F_GRAVITY);
   o->DR_DAMPING = !!(f & MPM_F_DRDAMP);
+  o->SmoothStress = !!(f & MPM_F_SMOOTH);
   o->QuasiLoadTime = d->quasi_load_time;
   o->DampFactor = d->damp_factor;
   o->EndTime = d->endtime;
@@ -1892,6 +1984,7 @@ static int field_io(orc* o, int field, double* out, const double* in, int set) {
     case MPM_P_MASS: PFIELD1(mass); break;
     case MPM_P_CP: PFIELD1(cp); break;
     case MPM_P_Q: PFIELD1(q); break;
+    case MPM_P_SPRE: PFIELD1(Spre); break;
     case MPM_P_SD:
       for (int64_t p = 0; p < np; ++p) {
         opart* t = &o->pt[p];

@@ -15,6 +15,10 @@ CASES = {
     "beam_musl_neoh_sgmp": (lambda: decks.soft_beam(), 60),
     "beam_usl_neoh_linear": (lambda: decks.soft_beam(shape="mpm", scheme="usl"), 60),
     "cook_musl_neoh_quasistatic": (lambda: decks.cook_membrane(), 60),
+    # Cook panels carry 'smoo': stress smoothing every step, one per shape family
+    "cook_smooth_gimp": (lambda: decks.cook_membrane("gimp", spacing=1.0), 40),
+    "cook_smooth_bspline": (lambda: decks.cook_membrane("bimp", spacing=1.0), 40),
+    "cook_smooth_sgmp": (lambda: decks.cook_membrane("sgmp", spacing=1.0), 40),
     "block_usf_elastic": (lambda: decks.generic_block("1 elas 1000 1e7 0.3"), 60),
     "block_musl_pla1_gimp": (lambda: decks.generic_block("1 pla1 1000 1e7 0.3 2e4", shape="gimp",
                                                          scheme="musl", velocity=(1.0, 0.0, -20.0)), 60),

@@ -25,6 +25,9 @@ MIXED_TOL = {
     "block_usf_sjcf_gruneisen": 5e-2,
 }
 DEFAULT_TOL = 1e-4
+# Spre is SM smoothed through the grid: it carries SM's error and the FP32
+# shape weights of the two transfers
+SMOOTH_TOL = 1e-4
 FIELDS = ["PXg", "Mg", "SM", "SD", "Xp", "VXp"]
 
 
@@ -195,3 +198,28 @@ def test_serving_shortest_first(built):
         done_big = srv.result(tb)["latency_ms"]
         for t in ts:
             assert srv.result(t)["latency_ms"] < done_big
+
+
+@pytest.mark.parametrize("variant", ["mpm", "gimp", "bimp", "sgmp"])
+def test_mixed_stress_smoothing(built, variant):
+    """Spre of the mixed form (computed from the state after the last step
+    when read) against the FP64 form, and the same alone or in a batch."""
+    from mpm3d_gb300 import Batch, Deck, MpmStep, decks
+    d = Deck.parse(decks.cook_membrane(variant, spacing=1.0))
+    a = MpmStep(d, "fp64")
+    b = MpmStep(d, "mixed")
+    a.run(40)
+    b.run(40)
+    sa, sb = a.download("Spre"), b.download("Spre")
+    assert np.all(np.isfinite(sb)) and np.any(sa != 0.0)
+    err = _rel(sa, sb)
+    assert err <= SMOOTH_TOL, f"cook {variant} Spre: {err:.3g}"
+    # with a scene of another material (the batch then runs one stress
+    # instantiation per material type): the same state and Spre
+    other = Deck.parse(CASES["slope_small_usf_dp_gimp"][0]())
+    with Batch() as bt:
+        bt.add(other, steps=40)
+        sid = bt.add(d, steps=40)
+        bt.run(40)
+        for f in ["Xp", "SD", "Spre"]:
+            np.testing.assert_array_equal(bt.download(sid, f), b.download(f), err_msg=f)

@@ -150,3 +150,26 @@ def test_oracle_matches_golden_digests(oracle_mod):
         o.run(entry["steps"])
         for field, dig in entry["digests"].items():
             assert _digest(o.download(field)) == dig, (name, field)
+
+
+@pytest.mark.parametrize("variant", ["mpm", "gimp", "bimp", "sgmp"])
+def test_stress_smoothing_reproduces_uniform_pressure(oracle_mod, variant):
+    """SmoothStressbyGrid maps -SM * VOL and VOL to the grid and back with the
+    same shape functions; the shapes sum to one, so a uniform mean stress comes
+    back as its pressure at every particle (SGMP: at every particle whose
+    centre nodes see only nodes with mass). Spre is zero before the first
+    smoothing and follows the deck's own stresses after steps."""
+    from mpm3d_gb300 import decks
+    o = oracle_mod.Oracle(deck_text=decks.cook_membrane(variant, spacing=1.0), libm="project")
+    n = o.nb_particle
+    assert np.all(o.download("Spre") == 0.0)
+    o.run(3)
+    assert np.all(np.isfinite(o.download("Spre"))) and np.any(o.download("Spre") != 0.0)
+    o.upload("SM", np.full(n, 5.0))
+    o.phase("SmoothStressbyGrid")
+    spre = o.download("Spre")
+    exact = np.abs(spre + 5.0) <= 1e-14 * 5.0 * 8
+    if variant == "sgmp":
+        assert exact.mean() > 0.95 and np.all(np.abs(spre + 5.0) <= 1e-8 * 5.0)
+    else:
+        assert exact.all(), (variant, spre.min(), spre.max())

@@ -53,7 +53,7 @@ def test_tecplot_and_paraview_frames(gpu_mod, tmp_path):
     p = d.particles()
     f = {"xp": p["Xp"], "vxp": p["VXp"], "fxp": p["FXp"], "mass": p["mass"], "seqv": np.arange(n, dtype=float),
          "sm": -np.ones(n), "vol": np.ones(n), "celsius": np.zeros(n), "dmg": np.zeros(n), "sd": np.zeros(6 * n),
-         "epeff": np.zeros(n)}
+         "epeff": np.zeros(n), "spre": np.full(n, 2.5)}
     job = str(tmp_path / "run")
     sc = np.zeros(16)
     with Output(d, job) as out:
@@ -71,6 +71,11 @@ def test_tecplot_and_paraview_frames(gpu_mod, tmp_path):
     assert len(row) == 3 * 12 + 3 + 12 + 12  # X Y Z, material (I3), seqv, pressure
     assert row[36:39] == "  1" and row[-12:] == "  0.1000E+01"
     assert os.path.exists(job + "_anim_1.vtu") and os.path.exists(job + "_anim_2.vtu")
+    vtu = open(job + "_anim_1.vtu").read().splitlines()
+    k = vtu.index('            <DataArray type="Float32" Name="Smoothpressure" Format="ascii">')
+    assert vtu[k + 1] == "                  0.2500E+01"
+    k = vtu.index('            <DataArray type="Float32" Name="SmoothMeanNormalStress" Format="ascii">')
+    assert vtu[k + 1] == "                 -0.2500E+01"
     pvd = open(job + "_anim.pvd").read().splitlines()
     assert pvd[-2:] == ["    </Collection>", "</VTKFile>"]
     assert pvd[3] == f'    <DataSet timestep="  0.0000E+00" group="" part="0" file="{job}_anim_1.vtu"/>'
