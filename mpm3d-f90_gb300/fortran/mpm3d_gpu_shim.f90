@@ -7,8 +7,9 @@
 ! keep the time loop as it is: the step subroutines of update_step.f90
 ! (GridMomentumInitial, ApplyBoundaryConditions, ParticleStressUpdate,
 ! GridMomentumUpdate, IntegrateMomentum, ParticlePositionUpdate,
-! GridMomentumMUSL, UpdateDT) and calcEnergy / dynamicRelaxationDamping of
-! Particle.f90 are replaced by the gpu_* routines below, one C call each.
+! GridMomentumMUSL, UpdateDT, SmoothStressbyGrid) and calcEnergy /
+! dynamicRelaxationDamping of Particle.f90 are replaced by the gpu_* routines
+! below, one C call each.
 ! gpu_sync_scalars copies DT, CurrentTime, energies and momentum back into
 ! the ParticleData globals; gpu_fetch_particles refreshes particle_list
 ! before OutCurve / OutAnim.
@@ -26,9 +27,10 @@ module mpm3d_gpu
        PH_PARTICLE_STRESS_UPDATE = 3, PH_GRID_MOMENTUM_UPDATE = 4, &
        PH_INTEGRATE_MOMENTUM = 5, PH_PARTICLE_POSITION_UPDATE = 6, &
        PH_GRID_MOMENTUM_MUSL = 7, PH_CALC_ENERGY = 8, PH_UPDATE_DT = 9, &
-       PH_DR_DAMPING = 10, PH_BEGIN_STEP = 11
+       PH_DR_DAMPING = 10, PH_BEGIN_STEP = 11, PH_SMOOTH_STRESS = 12
   integer(c_int), parameter :: F_XP = 1, F_VXP = 3, F_VOL = 7, F_SM = 10, F_SEQV = 11, &
-       F_SD = 12, F_EPEFF = 14, F_CELSIUS = 15, F_IE = 18, F_CP = 20, F_FAILURE = 22
+       F_SD = 12, F_EPEFF = 14, F_CELSIUS = 15, F_IE = 18, F_CP = 20, F_FAILURE = 22, &
+       F_SPRE = 26
 
   type(c_ptr), save :: ctx = c_null_ptr
   type(c_ptr), save :: deck = c_null_ptr
@@ -145,6 +147,9 @@ contains
   subroutine gpu_dynamicRelaxationDamping()
     call check(mpm_step_phase(ctx, PH_DR_DAMPING), 'dynamicRelaxationDamping')
   end subroutine
+  subroutine gpu_SmoothStressbyGrid()
+    call check(mpm_step_phase(ctx, PH_SMOOTH_STRESS), 'SmoothStressbyGrid')
+  end subroutine
 
   ! One whole step (the fused kernel sequence) instead of the phases above.
   subroutine gpu_step()
@@ -199,6 +204,8 @@ contains
     particle_list(:)%ie = buf(1:n)
     call check(mpm_download(ctx, F_CELSIUS, buf), 'celsius_t')
     particle_list(:)%celsius_t = buf(1:n)
+    call check(mpm_download(ctx, F_SPRE, buf), 'Spre')
+    particle_list(:)%Spre = buf(1:n)
     deallocate(buf)
   end subroutine gpu_fetch_particles
 
