@@ -170,19 +170,21 @@ def kernel_bytes(kernel: str, np_: int, nn_active: float, usf: bool = True) -> f
     return np_ * 100.0
 
 
-def profiled_traffic(kernel: str):
+def profiled_traffic(workload: str, kernel: str, particles: int):
     """DRAM bytes per launch (dram__bytes_read + write) of a step category,
-    as recorded from one ncu capture in profiles/ ('traffic_bytes: <name> <bytes>'
-    lines); None if not recorded."""
+    from one ncu capture summarised in profiles/ (lines 'traffic_bytes:
+    <workload> <category> <bytes> <particles>'), scaled to this run's particle
+    count (the per-particle traffic of these kernels does not depend on the
+    count); None when the workload has no capture."""
     import glob
     import re
 
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
         with open(path) as f:
             for line in f:
-                m = re.match(r"traffic_bytes:\s+(\S+)\s+([0-9.eE+]+)", line.strip())
-                if m and m.group(1) == kernel:
-                    return float(m.group(2))
+                m = re.match(r"traffic_bytes:\s+(\S+)\s+(\S+)\s+([0-9.eE+]+)\s+([0-9]+)", line.strip())
+                if m and m.group(1) == workload and m.group(2) == kernel:
+                    return float(m.group(3)) * particles / float(m.group(4))
     return None
 
 
@@ -323,7 +325,7 @@ def run_ours(args) -> dict:
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                     "traffic": profiled_traffic(dom["kernel"]), "algorithmic_bytes": kb,
+                     "traffic": profiled_traffic(args.workload, dom["kernel"], npart), "algorithmic_bytes": kb,
                      "avg_launch_ms": dom["avg_ms"]},
         "step_alg_gbs": mixed["alg_bytes_step"] / (mixed["ms"] / args.steps / 1e3) / 1e9,
         "kernels_mixed": {k["kernel"]: round(k["total_ms"] / args.steps, 4) for k in mixed["kernels"] if k["launches"]},
