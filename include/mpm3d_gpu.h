@@ -52,7 +52,8 @@ enum mpm_phase {
   MPM_PHASE_UPDATE_DT = 9,                /* update_step.f90:1833 UpdateDT                */
   MPM_PHASE_DR_DAMPING = 10,              /* Particle.f90:172     dynamicRelaxationDamping*/
   MPM_PHASE_BEGIN_STEP = 11,              /* MPM3D.f90:72-74: istep+1, time += DT         */
-  MPM_PHASE_SMOOTH_STRESS = 12            /* update_step.f90:1876 SmoothStressbyGrid      */
+  MPM_PHASE_SMOOTH_STRESS = 12,           /* update_step.f90:1876 SmoothStressbyGrid      */
+  MPM_PHASE_CONTACT = 13                  /* update_step.f90:1241 Lagr_NodContact         */
 };
 
 /* Field identifiers for mpm_download / oracle accessors. Particle fields are
@@ -134,6 +135,14 @@ int mpm_upload(mpm_ctx* ctx, int field, const double* in);
 int64_t mpm_nb_particle(const mpm_ctx* ctx);
 int64_t mpm_nb_gridnode(const mpm_ctx* ctx);
 int64_t mpm_nb_cell(const mpm_ctx* ctx);
+/* Grid components (nbco): grid fields hold nb_component * nb_gridnode
+ * nodes per vector component, component-major (DataIn.f90 'nbco',
+ * Grid.f90:284 grid_list(nb_component, nb_gridnode)). */
+int mpm_nb_component(const mpm_ctx* ctx);
+/* Total contact force of the last step (tot_cont_for of Lagr_NodContact,
+ * update_step.f90:1241-1376; written to ContforcPlot.dat by OutCurve); zero
+ * without 'cont'. */
+int mpm_contact_force(mpm_ctx* ctx, double f[3]);
 
 /* ---------------------------------------------------- measurement hooks */
 /* Time nsteps full steps with CUDA events on the context's stream;

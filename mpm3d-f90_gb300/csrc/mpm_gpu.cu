@@ -121,7 +121,7 @@ const char* const kKernelNames[K_COUNT] = {
     "stress_update", "depeff_tail", "force_prep", "p2g_force_integrate", "integrate", "g2p_position",
     "p2g_musl", "reduce_energy_dt", "dr_damping", "permute",
     "p2g_mass_scatter", "p2g_force_scatter", "p2g_musl_scatter", "sgmp_centre_clear",
-    "sgmp_centre_gradient", "sgmp_centre_velocity", "stress_smoothing"};
+    "sgmp_centre_gradient", "sgmp_centre_velocity", "stress_smoothing", "contact"};
 
 static thread_local Profiler* t_prof = nullptr;
 void prof_set_current(Profiler* p) { t_prof = p; }
@@ -352,6 +352,7 @@ int enqueue_step(mpm_ctx* c) {
     if ((r = stress_pass(c))) return r;
   o->force_prep(st, g, s);
   o->p2g_force(st, g, 1, s);
+  if (g.contact && g.contact_type == 1) o->contact(st, g, s);
   o->position(st, g, s);
   if (g.musl) o->p2g_momentum(st, g, !g.usf, s);
   if (!g.usf)
@@ -410,9 +411,7 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
   if (!out) return set_err(nullptr, MPM_ERR_ARG, "out is NULL");
   *out = nullptr;
   if (!d) return set_err(nullptr, MPM_ERR_ARG, "deck is NULL");
-  if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM))
-    return set_err(nullptr, MPM_ERR_UNSUPPORTED, "contact and TLMPM are outside the explicit-step path");
-  if (d->nb_component != 1) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "only one grid component");
+  if (d->flags & MPM_F_TLMPM) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "TLMPM is outside the explicit-step path");
   if (d->nb_particle <= 0 || d->nb_body <= 0 || d->nb_mat <= 0)
     return set_err(nullptr, MPM_ERR_ARG, "deck defines no particles / bodies / materials");
   if (d->nb_body > 65535) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "more than 65535 bodies");
@@ -485,9 +484,9 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     return r;
   }
   Geometry& g = c->g;
-  const long long np = g.np, nn = g.nn, nc = g.ncell;
+  const long long np = g.np, nn = g.nn, nc = g.ncell, nnt = g.nnt;
   const int K = g.K;
-  c->nkeys = g.shape == 3 ? (int)nc : (int)nn;
+  c->nkeys = g.shape == 3 ? (int)nc : (int)nnt;  // pair keys: (component, node) or centre node
   c->npairs = np * K;
   c->key_bits = 1;
   while ((1LL << c->key_bits) <= (long long)c->nkeys) c->key_bits++;
@@ -516,8 +515,9 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     AL(s.key, unsigned, c->npairs); AL(s.val, unsigned, c->npairs);
     AL(s.key_sorted, unsigned, c->npairs); AL(s.val_sorted, unsigned, c->npairs);
     AL(s.seg, int, (long long)c->nkeys + 1);
-    AL(s.mg, double, nn); AL(s.px, double, 3 * nn); AL(s.fx, double, 3 * nn); AL(s.vg, double, 3 * nn);
+    AL(s.mg, double, nnt); AL(s.px, double, 3 * nnt); AL(s.fx, double, 3 * nnt); AL(s.vg, double, 3 * nnt);
     AL(s.fix, uint8_t, nn); AL(s.bd, uint8_t, nn);
+    if (g.contact) { AL(s.ndir, double, 3 * nnt); AL(s.cforce, double, 3 * nn); }
     if (g.shape == 3) {
       AL(s.cmg, double, nc); AL(s.cpx, double, 3 * nc); AL(s.cfext, double, 3 * nc); AL(s.cfint, double, 6 * nc);
       AL(s.co, double, 6 * nc); AL(s.cw, double, 3 * nc); AL(s.cdefp, double, 9 * nc);
@@ -586,10 +586,12 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
                         c->stream));
     CKF(cudaMemcpyAsync(s.bodies, c->bodies.data(), sizeof(DevBody) * c->bodies.size(), cudaMemcpyHostToDevice,
                         c->stream));
-    CKF(cudaMemsetAsync(s.mg, 0, sizeof(double) * nn, c->stream));
-    CKF(cudaMemsetAsync(s.px, 0, sizeof(double) * 3 * nn, c->stream));
-    CKF(cudaMemsetAsync(s.fx, 0, sizeof(double) * 3 * nn, c->stream));
-    CKF(cudaMemsetAsync(s.vg, 0, sizeof(double) * 3 * nn, c->stream));
+    CKF(cudaMemsetAsync(s.mg, 0, sizeof(double) * nnt, c->stream));
+    CKF(cudaMemsetAsync(s.px, 0, sizeof(double) * 3 * nnt, c->stream));
+    CKF(cudaMemsetAsync(s.fx, 0, sizeof(double) * 3 * nnt, c->stream));
+    CKF(cudaMemsetAsync(s.vg, 0, sizeof(double) * 3 * nnt, c->stream));
+    if (s.ndir) CKF(cudaMemsetAsync(s.ndir, 0, sizeof(double) * 3 * nnt, c->stream));
+    if (s.cforce) CKF(cudaMemsetAsync(s.cforce, 0, sizeof(double) * 3 * nn, c->stream));
     CKF(cudaMemsetAsync(s.red_count, 0, sizeof(unsigned), c->stream));
     if (s.spre) CKF(cudaMemsetAsync(s.spre, 0, sizeof(double) * np, c->stream));
     DevScalars sc0;
@@ -657,6 +659,9 @@ int mpm_step_phase(mpm_ctx* c, int phase) {
     case MPM_PHASE_DR_DAMPING: o->dr_damping(st, g, s); break;
     case MPM_PHASE_SMOOTH_STRESS:
       if ((r = smooth_pass(c))) return r;
+      break;
+    case MPM_PHASE_CONTACT:
+      if (g.contact && g.contact_type == 1) o->contact(st, g, s);
       break;
     default: return set_err(c, MPM_ERR_ARG, "unknown phase %d", phase);
   }
@@ -752,6 +757,21 @@ int mpm_get_scalars(mpm_ctx* c, double* o) {
 int64_t mpm_nb_particle(const mpm_ctx* c) { return c ? c->g.np : -1; }
 int64_t mpm_nb_gridnode(const mpm_ctx* c) { return c ? c->g.nn : -1; }
 int64_t mpm_nb_cell(const mpm_ctx* c) { return c ? c->g.ncell : -1; }
+int mpm_nb_component(const mpm_ctx* c) { return c ? (c->batch ? 1 : c->g.ncomp) : -1; }
+
+int mpm_contact_force(mpm_ctx* c, double f[3]) {
+  if (!c || !f) return set_err(c, MPM_ERR_ARG, "bad argument");
+  if (c->batch || !c->g.contact) {
+    f[0] = f[1] = f[2] = 0.0;
+    return MPM_OK;
+  }
+  DevScalars sc;
+  CK(cudaMemcpyAsync(&sc, c->st.sc, sizeof sc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 3; ++k) f[k] = sc.cont_for[k];
+  return MPM_OK;
+}
+
 int64_t mpm_device_bytes(const mpm_ctx* c) { return c ? (c->batch ? mpm_batch_device_bytes(c->batch) : c->bytes) : -1; }
 
 static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long* count) {
@@ -788,9 +808,9 @@ static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long*
     case MPM_P_CENTERICELL: *ptr = s.centericell; *elem = 4; break;
     case MPM_P_INODE: *ptr = s.inode; *elem = 4; break;
     case MPM_P_SPRE: *ptr = s.spre; break;  // null without 'smoo': reads as zeros
-    case MPM_G_MG: *ptr = s.mg; *count = nn; break;
-    case MPM_G_PX: *ptr = s.px; *count = 3 * nn; break;
-    case MPM_G_FX: *ptr = s.fx; *count = 3 * nn; break;
+    case MPM_G_MG: *ptr = s.mg; *count = c->g.nnt; break;  // every grid component, component-major
+    case MPM_G_PX: *ptr = s.px; *count = 3 * c->g.nnt; break;
+    case MPM_G_FX: *ptr = s.fx; *count = 3 * c->g.nnt; break;
     case MPM_C_MG:
       if (!s.cmg) return set_err(c, MPM_ERR_ARG, "no auxiliary grid (not SGMP)");
       *ptr = s.cmg; *count = nc; break;

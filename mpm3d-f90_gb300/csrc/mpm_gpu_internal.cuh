@@ -17,7 +17,10 @@
 //     the reference's summation order (ascending particle, then slot);
 //     seg[n] = end of node n's slice (inclusive prefix sum of the counts).
 //   grid, FP64, flat reference node order: mg[Nn], px[3][Nn], fx[3][Nn],
-//     vg[3][Nn] (= px/mg), uint8 fix[Nn] (bit c = DOF c fixed), uint8 bd[Nn]
+//     vg[3][Nn] (= px/mg), uint8 fix[Nn] (bit c = DOF c fixed), uint8 bd[Nn];
+//     with several grid components (contact) the value arrays hold ncomp
+//     grids back to back (Nn = ncomp * nodes), a particle reaching its body's
+//     component through the node index of its shape cache
 //   SGMP auxiliary grid (one centre node per cell), FP64: cmg, cpx[3],
 //     cfext[3], cfint[6], co[6], cw[3], cdefp[9], cvx[3], cax[3].
 //   stress smoothing (decks with 'smoo'), FP64: spre[Np], gpre[Nn],
@@ -53,7 +56,8 @@ struct DevMaterial {
 };
 
 struct DevBody {
-  int mat;  // 0-based material index
+  int mat;   // 0-based material index
+  int comp;  // 0-based grid component of the body's particles (comID with contact, else 0)
   double gravp[3];
 };
 
@@ -66,6 +70,7 @@ struct DevScalars {
   double ke, ie, mom[3], ke_prev;
   double depeff_carry;  // MaterialModel's module-level depeff after the last particle
   double max_vp;
+  double cont_for[3];  // total contact force of the last step (Lagr_NodContact)
   unsigned long long active_nodes;
   unsigned status;
   unsigned pad2_;
@@ -74,7 +79,9 @@ struct DevScalars {
 // Everything a kernel needs besides the arrays.
 struct Geometry {
   long long np;       // particles
-  int nn;             // grid nodes
+  int nn;             // grid nodes (of one grid component)
+  int ncomp;          // grid components (nbco); node arrays hold ncomp * nn nodes, component-major
+  long long nnt;      // ncomp * nn
   int ncell;          // cells (= SGMP centre nodes)
   int NGx, NGy, NGz, NGxy;
   int NCx, NCy, NCz, NCxy;        // NumCellx..
@@ -88,6 +95,8 @@ struct Geometry {
   int usf, usl, musl, uvfp, qload, qdamp, gravity;
   int nb_mat, nb_body;
   int has_jc;         // a Johnson-Cook material (types 4, 7) is present
+  int contact, contact_type, normbody;  // 'cont': bodies on their own components; type 1 = Lagr_NodContact
+  double fricfa;      // friction coefficient of the contact
 };
 
 template <class B, class R>
@@ -114,6 +123,8 @@ struct DevState {
   // stress smoothing (decks with 'smoo'): Spre per particle, Gpre per node,
   // CGpre / CGV_all per centre node
   double *spre, *gpre, *cgpre, *cgvall;
+  // contact: mass-gradient normals [3][ncomp * nn], contact force per node [3][nn]
+  double *ndir, *cforce;
   // Johnson-Cook depeff carry
   int *setter, *setter_scan;
   double *dep;
@@ -154,6 +165,8 @@ struct StepOps {
   // maps to the grid and back
   void (*smooth_locate)(void* st, const Geometry& g, cudaStream_t s);
   void (*smooth)(void* st, const Geometry& g, cudaStream_t s);
+  // Lagr_NodContact after IntegrateMomentum, with the total contact force
+  void (*contact)(void* st, const Geometry& g, cudaStream_t s);
 };
 
 extern const StepOps kOpsStrict;   // MPM_FP64_STRICT
@@ -167,7 +180,7 @@ enum KernelId {
   K_BEGIN = 0, K_LOCATE, K_SORT, K_SEG, K_P2G_MASS, K_NODE_VEL, K_BC, K_STRESS, K_DEPEFF,
   K_FORCE_PREP, K_P2G_FORCE, K_INTEGRATE, K_POSITION, K_P2G_MOM, K_REDUCE, K_DR, K_PERMUTE,
   K_SCATTER_MASS, K_SCATTER_FORCE, K_SCATTER_MOM, K_SG_CLEAR, K_SG_GRADIENT, K_SG_VELOCITY, K_SMOOTH,
-  K_COUNT
+  K_CONTACT, K_COUNT
 };
 extern const char* const kKernelNames[K_COUNT];
 

@@ -197,14 +197,15 @@ __device__ __forceinline__ int slot_shapes(St<P>& s, const Geometry& g, long lon
 
 // pair keys of particle p's slots (node-sorted list; pair j = p*K + k keeps
 // (particle, slot) order for the stable sort; invalid slots get the
-// sentinel key nkeys) and the per-node pair counts
+// sentinel key nkeys) and the per-node pair counts; cbase = the first node
+// of the particle's grid component
 template <class P>
 __device__ __forceinline__ void write_pairs(St<P>& s, const Geometry& g, long long p, int nvalid,
-                                            const int slot_node[27], int nkeys) {
+                                            const int slot_node[27], int nkeys, int cbase) {
   const long long np = g.np;
   const int K = g.K;
   for (int k = 0; k < K; ++k) {
-    int nd = k < nvalid ? slot_node[k] : -1;
+    int nd = k < nvalid && slot_node[k] >= 0 ? cbase + slot_node[k] : -1;
     s.snode[k * np + p] = nd;
     long long j = p * K + k;
     s.key[j] = nd >= 0 ? (unsigned)nd : (unsigned)nkeys;
@@ -267,7 +268,7 @@ __global__ void k_locate(St<P> s, Geometry g, int nkeys) {
   }
   int slot_node[27];
   const int nvalid = slot_shapes<P>(s, g, p, x, icell, xn, cc, xxn, slot_node);
-  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys);
+  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys, g.shape == 3 ? 0 : s.bodies[s.body[p]].comp * g.nn);
 }
 
 __device__ __forceinline__ void decode_pair(unsigned v, long long np, long long* p, long long* idx) {
@@ -278,7 +279,7 @@ __device__ __forceinline__ void decode_pair(unsigned v, long long np, long long*
 }
 
 // ----------------------------------------------------- node-level helpers
-__device__ __forceinline__ void node_bc(const uint8_t fix, double* px, double* fx, int n, int nn) {
+__device__ __forceinline__ void node_bc(const uint8_t fix, double* px, double* fx, long long n, long long nn) {
   for (int c = 0; c < 3; ++c)
     if (fix & (1 << c)) {
       px[(long long)c * nn + n] = 0.0;
@@ -286,7 +287,7 @@ __device__ __forceinline__ void node_bc(const uint8_t fix, double* px, double* f
     }
 }
 
-__device__ __forceinline__ void node_vel(const double* mg, const double* px, double* vg, int n, int nn,
+__device__ __forceinline__ void node_vel(const double* mg, const double* px, double* vg, long long n, long long nn,
                                          double cutoff) {
   double m = mg[n];
   if (m > cutoff)
@@ -304,7 +305,7 @@ __device__ __forceinline__ void count_active(bool active, unsigned long long* ou
 template <class P>
 __global__ void k_p2g_mass(St<P> s, Geometry g, int bc, int vel) {
   const long long n = gtid();
-  const int nn = g.nn;
+  const long long nn = g.nnt;  // every grid component
   bool act = false;
   if (n < nn) {
     const long long np = g.np;
@@ -324,8 +325,8 @@ __global__ void k_p2g_mass(St<P> s, Geometry g, int bc, int vel) {
     s.px[nn + n] = py;
     s.px[2LL * nn + n] = pz;
     act = m > 0.0;
-    if (bc) node_bc(s.fix[n], s.px, s.fx, (int)n, nn);
-    if (vel) node_vel(s.mg, s.px, s.vg, (int)n, nn, g.cutoff);
+    if (bc) node_bc(s.fix[n % g.nn], s.px, s.fx, n, nn);
+    if (vel) node_vel(s.mg, s.px, s.vg, n, nn, g.cutoff);
   }
   count_active(act, &s.sc->active_nodes);
 }
@@ -336,15 +337,15 @@ __global__ void k_p2g_mass(St<P> s, Geometry g, int bc, int vel) {
 template <class P>
 __global__ void k_node_velocity(St<P> s, Geometry g) {
   const long long n = gtid();
-  if (n >= g.nn) return;
-  node_vel(s.mg, s.px, s.vg, (int)n, g.nn, g.cutoff);
+  if (n >= g.nnt) return;
+  node_vel(s.mg, s.px, s.vg, n, g.nnt, g.cutoff);
 }
 
 template <class P>
 __global__ void k_apply_bc(St<P> s, Geometry g) {
   const long long n = gtid();
-  if (n >= g.nn) return;
-  node_bc(s.fix[n], s.px, s.fx, (int)n, g.nn);
+  if (n >= g.nnt) return;
+  node_bc(s.fix[n % g.nn], s.px, s.fx, n, g.nnt);
 }
 
 // ---------------------------------------------------------- stress update
@@ -681,7 +682,7 @@ __global__ void k_stress(St<P> s, Geometry g) {
   const long long p = gtid();
   if (p >= g.np) return;
   const long long np = g.np;
-  const int nn = g.nn;
+  const long long nn = g.nnt;  // node arrays of every grid component
   if (g.has_jc) {
     s.setter[p] = -1;
     s.deferred[p] = 0;
@@ -891,7 +892,7 @@ __global__ void k_force_prep(St<P> s, Geometry g) {
 // integ != 0, IntegrateMomentum (1194-1239) and the node velocity.
 template <class P>
 __device__ __forceinline__ void node_integrate(St<P>& s, const Geometry& g, long long n, double fxn[3]) {
-  const int nn = g.nn;
+  const long long nn = g.nnt;
   const DevScalars& sc = *s.sc;
   const double dt = sc.dt;
   for (int c = 0; c < 3; ++c) {
@@ -902,23 +903,30 @@ __device__ __forceinline__ void node_integrate(St<P>& s, const Geometry& g, long
       pxc = pxc + fxn[c] * dt;
     s.px[(long long)c * nn + n] = pxc;
   }
-  node_bc(s.fix[n], s.px, s.fx, (int)n, nn);
-  node_vel(s.mg, s.px, s.vg, (int)n, nn, g.cutoff);
+  node_bc(s.fix[n % g.nn], s.px, s.fx, n, nn);
+  node_vel(s.mg, s.px, s.vg, n, nn, g.cutoff);
 }
 
 template <class P>
 __global__ void k_p2g_force(St<P> s, Geometry g, int integ) {
   using R = typename P::R;
   const long long n = gtid();
-  const int nn = g.nn;
+  const long long nn = g.nnt;  // every grid component
   if (n >= nn) return;
   const long long np = g.np;
   double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+  double nd0 = 0.0, nd1 = 0.0, nd2 = 0.0;  // contact normal: mass gradient (update_step.f90:977-982)
   const int j0 = n == 0 ? 0 : s.seg[n - 1], j1 = s.seg[n];
   for (int j = j0; j < j1; ++j) {
     long long p, idx;
     decode_pair(s.val_sorted[j], np, &p, &idx);
     R sk = s.shp[idx], dx = s.dndx[idx], dy = s.dndy[idx], dz = s.dndz[idx];
+    if (g.contact) {
+      const double mp = s.mass[p];
+      nd0 = nd0 + (double)dx * mp;
+      nd1 = nd1 + (double)dy * mp;
+      nd2 = nd2 + (double)dz * mp;
+    }
     R sxx = (R)s.sdiag[p], syy = (R)s.sdiag[np + p], szz = (R)s.sdiag[2 * np + p];
     R sxy = (R)s.sd[3 * np + p], syz = (R)s.sd[4 * np + p], sxz = (R)s.sd[5 * np + p];
     R vol = (R)s.vol[p];
@@ -938,6 +946,11 @@ __global__ void k_p2g_force(St<P> s, Geometry g, int integ) {
   s.fx[n] = f0;
   s.fx[nn + n] = f1;
   s.fx[2LL * nn + n] = f2;
+  if (g.contact) {
+    s.ndir[n] = nd0;
+    s.ndir[nn + n] = nd1;
+    s.ndir[2LL * nn + n] = nd2;
+  }
   if (integ) {
     double fxn[3] = {f0, f1, f2};
     node_integrate<P>(s, g, n, fxn);
@@ -947,10 +960,108 @@ __global__ void k_p2g_force(St<P> s, Geometry g, int integ) {
 template <class P>
 __global__ void k_integrate(St<P> s, Geometry g) {
   const long long n = gtid();
-  if (n >= g.nn) return;
-  const int nn = g.nn;
+  if (n >= g.nnt) return;
+  const long long nn = g.nnt;
   double fxn[3] = {s.fx[n], s.fx[nn + n], s.fx[2LL * nn + n]};
   node_integrate<P>(s, g, n, fxn);
+}
+
+// ---------------------------------------------------------------- contact
+// Lagr_NodContact (update_step.f90:1241-1376), Bardenhagen's method between
+// grid components 1 and 2, after IntegrateMomentum: per node, the contact
+// normal from the components' mass gradients (normbody 0: their
+// difference, 1: component 1's, 2: minus component 2's), unitised; where
+// both components have mass above the cut-off and approach along the normal
+// (crit > epsilon), the normal contact force crit / ((Mg1 + Mg2) DT) -- with
+// friction, the full sticking force limited to fricfa |normal force|
+// tangentially -- is taken from component 1 and given to component 2, in
+// force and momentum, on the node's free directions. The node velocities of
+// both components are refreshed for the position update; the force per node
+// is kept for the total.
+template <class P>
+__global__ void k_contact(St<P> s, Geometry g) {
+  const long long n = gtid();
+  const long long nn = g.nn, nt = g.nnt;
+  if (n >= nn) return;
+  const double eps = 2.220446049250313e-16;  // epsilon(1d0)
+  const long long n2 = nn + n;               // the node in component 2
+  double nx = 0.0, ny = 0.0, nz = 0.0;
+  if (g.normbody == 0) {
+    nx = s.ndir[n] - s.ndir[n2];
+    ny = s.ndir[nt + n] - s.ndir[nt + n2];
+    nz = s.ndir[2 * nt + n] - s.ndir[2 * nt + n2];
+  } else if (g.normbody == 1) {
+    nx = s.ndir[n];
+    ny = s.ndir[nt + n];
+    nz = s.ndir[2 * nt + n];
+  } else {
+    nx = -s.ndir[n2];
+    ny = -s.ndir[nt + n2];
+    nz = -s.ndir[2 * nt + n2];
+  }
+  double tt = sqrt(nx * nx + ny * ny + nz * nz);
+  if (tt > eps) {
+    nx = nx / tt;
+    ny = ny / tt;
+    nz = nz / tt;
+  }
+  const double nd[3] = {nx, ny, nz};
+  const double m1 = s.mg[n], m2 = s.mg[n2];
+  double p1[3], p2[3], cforce[3] = {0.0, 0.0, 0.0};
+  for (int c = 0; c < 3; ++c) {
+    p1[c] = s.px[c * nt + n];
+    p2[c] = s.px[c * nt + n2];
+  }
+  double crit = 0.0;
+  if (m1 > g.cutoff && m2 > g.cutoff)
+    crit = (p1[0] * m2 - p2[0] * m1) * nx + (p1[1] * m2 - p2[1] * m1) * ny + (p1[2] * m2 - p2[2] * m1) * nz;
+  if (crit > eps) {
+    const double dt = s.sc->dt;
+    tt = (m1 + m2) * dt;
+    const double nomforce = crit / tt;
+    if (g.fricfa > eps) {
+      double fstick[3];
+      for (int c = 0; c < 3; ++c) cforce[c] = (p1[c] * m2 - p2[c] * m1) / tt;
+      for (int c = 0; c < 3; ++c) fstick[c] = cforce[c] - nomforce * nd[c];
+      const double val_fstick = sqrt(fstick[0] * fstick[0] + fstick[1] * fstick[1] + fstick[2] * fstick[2]);
+      const double val_fslip = g.fricfa * fabs(nomforce);
+      if (val_fslip < val_fstick)
+        for (int c = 0; c < 3; ++c) cforce[c] = nomforce * nd[c] + val_fslip * (fstick[c] / val_fstick);
+    } else {
+      for (int c = 0; c < 3; ++c) cforce[c] = nomforce * nd[c];
+    }
+    const uint8_t fix = s.fix[n];
+    for (int c = 0; c < 3; ++c) {
+      if (fix & (1 << c)) continue;
+      s.fx[c * nt + n] = s.fx[c * nt + n] - cforce[c];
+      s.fx[c * nt + n2] = s.fx[c * nt + n2] + cforce[c];
+      s.px[c * nt + n] = p1[c] - cforce[c] * dt;
+      s.px[c * nt + n2] = p2[c] + cforce[c] * dt;
+    }
+    node_vel(s.mg, s.px, s.vg, n, nt, g.cutoff);
+    node_vel(s.mg, s.px, s.vg, n2, nt, g.cutoff);
+  }
+  for (int c = 0; c < 3; ++c) s.cforce[c * nn + n] = cforce[c];
+}
+
+// the total contact force (tot_cont_for): one block, fixed summation tree
+template <class P>
+__global__ void k_contact_sum(St<P> s, Geometry g) {
+  __shared__ double part[3][kBlock];
+  const int t = threadIdx.x;
+  const long long nn = g.nn;
+  double a[3] = {0.0, 0.0, 0.0};
+  for (long long n = t; n < nn; n += kBlock)
+    for (int c = 0; c < 3; ++c) a[c] = a[c] + s.cforce[c * nn + n];
+  for (int c = 0; c < 3; ++c) part[c][t] = a[c];
+  __syncthreads();
+  for (int w = kBlock / 2; w > 0; w >>= 1) {
+    if (t < w)
+      for (int c = 0; c < 3; ++c) part[c][t] = part[c][t] + part[c][t + w];
+    __syncthreads();
+  }
+  if (t == 0)
+    for (int c = 0; c < 3; ++c) s.sc->cont_for[c] = part[c][0];
 }
 
 // ------------------------------------------------------ position update
@@ -961,7 +1072,7 @@ __global__ void k_position(St<P> s, Geometry g) {
   const long long p = gtid();
   if (p >= g.np) return;
   const long long np = g.np;
-  const int nn = g.nn;
+  const long long nn = g.nnt;  // node arrays of every grid component
   const DevScalars& sc = *s.sc;
   double vx[3] = {0, 0, 0}, ax[3] = {0, 0, 0};
   if (g.shape == 3) {
@@ -1051,7 +1162,7 @@ __global__ void k_position(St<P> s, Geometry g) {
 template <class P>
 __global__ void k_p2g_momentum(St<P> s, Geometry g, int vel) {
   const long long n = gtid();
-  const int nn = g.nn;
+  const long long nn = g.nnt;  // every grid component
   if (n >= nn) return;
   const long long np = g.np;
   double px = 0.0, py = 0.0, pz = 0.0;
@@ -1067,8 +1178,8 @@ __global__ void k_p2g_momentum(St<P> s, Geometry g, int vel) {
   s.px[n] = px;
   s.px[nn + n] = py;
   s.px[2LL * nn + n] = pz;
-  node_bc(s.fix[n], s.px, s.fx, (int)n, nn);
-  if (vel) node_vel(s.mg, s.px, s.vg, (int)n, nn, g.cutoff);
+  node_bc(s.fix[n % g.nn], s.px, s.fx, n, nn);
+  if (vel) node_vel(s.mg, s.px, s.vg, n, nn, g.cutoff);
 }
 
 // ================================================================ SGMP
@@ -1366,7 +1477,7 @@ __global__ void k_smooth_locate(St<P> s, Geometry g, int nkeys) {
   const int cc = g.shape == 3 ? s.centericell[p] : 0;
   int slot_node[27];
   const int nvalid = slot_shapes<P>(s, g, p, x, g.shape == 3 ? 0 : icell, xn, cc, xxn, slot_node);
-  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys);
+  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys, 0);  // SmoothStressbyGrid maps to component 1
 }
 
 // pressure * volume and volume of one (node or centre node) slice of pairs,

@@ -19,7 +19,7 @@ struct Ops {
   }
   static void locate(void* st, const Geometry& g, cudaStream_t s) {
     prof_begin(K_LOCATE, s);
-    k_locate<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g, g.shape == 3 ? g.ncell : g.nn);
+    k_locate<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g, g.shape == 3 ? g.ncell : (int)g.nnt);
     prof_end(K_LOCATE, s);
   }
   static void node_offsets(void*, const Geometry&, long long, cudaStream_t) {}
@@ -29,18 +29,18 @@ struct Ops {
       k_sg_cell_mass<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
       k_sg_node_mass<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, bc, vel);
     } else {
-      k_p2g_mass<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, bc, vel);
+      k_p2g_mass<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g, bc, vel);
     }
     prof_end(K_P2G_MASS, s);
   }
   static void node_velocity(void* st, const Geometry& g, cudaStream_t s) {
     prof_begin(K_NODE_VEL, s);
-    k_node_velocity<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g);
+    k_node_velocity<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g);
     prof_end(K_NODE_VEL, s);
   }
   static void apply_bc(void* st, const Geometry& g, cudaStream_t s) {
     prof_begin(K_BC, s);
-    k_apply_bc<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g);
+    k_apply_bc<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g);
     prof_end(K_BC, s);
   }
   static void stress(void* st, const Geometry& g, cudaStream_t s) {
@@ -66,13 +66,13 @@ struct Ops {
       k_sg_cell_force<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
       k_sg_node_force<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, integ);
     } else {
-      k_p2g_force<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, integ);
+      k_p2g_force<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g, integ);
     }
     prof_end(K_P2G_FORCE, s);
   }
   static void integrate(void* st, const Geometry& g, cudaStream_t s) {
     prof_begin(K_INTEGRATE, s);
-    k_integrate<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g);
+    k_integrate<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g);
     prof_end(K_INTEGRATE, s);
   }
   static void position(void* st, const Geometry& g, cudaStream_t s) {
@@ -87,7 +87,7 @@ struct Ops {
       k_sg_cell_momentum<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
       k_sg_node_momentum<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, vel);
     } else {
-      k_p2g_momentum<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, vel);
+      k_p2g_momentum<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g, vel);
     }
     prof_end(K_P2G_MOM, s);
   }
@@ -121,6 +121,13 @@ struct Ops {
     prof_end(K_SMOOTH, s);
   }
 
+  static void contact(void* st, const Geometry& g, cudaStream_t s) {
+    prof_begin(K_CONTACT, s);
+    k_contact<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g);
+    k_contact_sum<P><<<1, kBlock, 0, s>>>(S(st), g);
+    prof_end(K_CONTACT, s);
+  }
+
   static StepOps table(const char* name) {
     StepOps o;
     o.name = name;
@@ -143,6 +150,7 @@ struct Ops {
     o.dr_damping = dr_damping;
     o.smooth_locate = smooth_locate;
     o.smooth = smooth;
+    o.contact = contact;
     return o;
   }
 };

@@ -145,6 +145,23 @@ int scene_setup(const mpm_deck* d, SceneSetup& out) {
   g.has_jc = 0;
   for (auto& m : out.mats)
     if (m.mat_type == 4 || m.mat_type == 7) g.has_jc = 1;
+  // grid components and contact (Particle.f90:69-92, DataIn.f90:1348-1393)
+  g.ncomp = d->nb_component > 0 ? d->nb_component : 1;
+  g.nnt = (long long)g.ncomp * nn;
+  if (g.nnt > 2000000000LL) return fail(out, MPM_ERR_UNSUPPORTED, "grid too large for 32-bit node ids");
+  g.contact = !!(f & MPM_F_CONTACT);
+  g.contact_type = d->contact_type;
+  g.normbody = d->normbody;
+  g.fricfa = d->fricfa;
+  if (sgmp && g.ncomp > 1)
+    return fail(out, MPM_ERR_UNSUPPORTED, "SGMP with several grid components (the reference shares its centre grid)");
+  if (g.contact && g.contact_type == 1 && (g.ncomp < 2 || g.normbody < 0 || g.normbody > 2))
+    return fail(out, MPM_ERR_ARG, "contact needs two grid components and normbody 0, 1 or 2");
+  for (int b = 0; b < d->nb_body; ++b) {
+    const int com = d->bodies[b].comID;
+    if (g.contact && (com < 1 || com > g.ncomp)) return fail(out, MPM_ERR_ARG, "body component out of range");
+    out.bodies[b].comp = g.contact ? com - 1 : 0;
+  }
   // fixities and SGMP boundary types (Grid.f90:291-359)
   fix.assign(nn, 0);
   bd.assign(nn, 0);

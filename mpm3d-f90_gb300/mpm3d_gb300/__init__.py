@@ -46,7 +46,7 @@ PHASES = {
     "GridMomentumInitial": 1, "ApplyBoundaryConditions": 2, "ParticleStressUpdate": 3,
     "GridMomentumUpdate": 4, "IntegrateMomentum": 5, "ParticlePositionUpdate": 6,
     "GridMomentumMUSL": 7, "calcEnergy": 8, "UpdateDT": 9, "dynamicRelaxationDamping": 10,
-    "BeginStep": 11, "SmoothStressbyGrid": 12,
+    "BeginStep": 11, "SmoothStressbyGrid": 12, "Lagr_NodContact": 13,
 }
 
 SCALARS = ("istep", "CurrentTime", "DT", "EngKinetic", "EngInternal", "Momentum_x",
@@ -100,6 +100,8 @@ def library() -> ctypes.CDLL:
         "mpm_nb_particle": (i64, [vp]),
         "mpm_nb_gridnode": (i64, [vp]),
         "mpm_nb_cell": (i64, [vp]),
+        "mpm_nb_component": (i, [vp]),
+        "mpm_contact_force": (i, [vp, P(d)]),
         "mpm_time_steps": (i, [vp, i, i, P(d)]),
         "mpm_profile_enable": (i, [vp, i]),
         "mpm_kernel_count": (i, [vp]),
@@ -245,6 +247,7 @@ class MpmStep:
         self.nb_particle = int(lib.mpm_nb_particle(h))
         self.nb_gridnode = int(lib.mpm_nb_gridnode(h))
         self.nb_cell = int(lib.mpm_nb_cell(h))
+        self.nb_component = int(lib.mpm_nb_component(h))
 
     # -- plumbing
     def _check(self, st: int) -> None:
@@ -308,6 +311,9 @@ class MpmStep:
     def SmoothStressbyGrid(self):
         self.phase("SmoothStressbyGrid")
 
+    def Lagr_NodContact(self):
+        self.phase("Lagr_NodContact")
+
     # -- whole steps
     def step(self) -> None:
         self._check(library().mpm_step(self._h))
@@ -332,7 +338,7 @@ class MpmStep:
     def download(self, field: str) -> np.ndarray:
         ncomp = COMPONENTS.get(field, 1)
         if field in GRID_FIELDS:
-            n = self.nb_gridnode
+            n = self.nb_gridnode * self.nb_component  # every grid component, component-major
         elif field in CELL_FIELDS:
             n = self.nb_cell
         else:
@@ -340,6 +346,12 @@ class MpmStep:
         out = np.zeros(ncomp * n)
         self._check(library().mpm_download(self._h, FIELDS[field], _dptr(out)))
         return out.reshape(ncomp, n) if ncomp > 1 else out
+
+    def contact_force(self) -> np.ndarray:
+        """Total contact force of the last step (Lagr_NodContact's tot_cont_for)."""
+        f = np.zeros(3)
+        self._check(library().mpm_contact_force(self._h, _dptr(f)))
+        return f
 
     def upload(self, field: str, values: np.ndarray) -> None:
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()

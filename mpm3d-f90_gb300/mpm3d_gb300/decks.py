@@ -53,6 +53,7 @@ class DeckWriter:
         self.tail: list[str] = []
         self.nbmp = 0
         self.nbbo = 0
+        self.nbco = 1
 
     def kw(self, line: str) -> None:
         self.head.append(line)
@@ -76,7 +77,7 @@ class DeckWriter:
         return first, first + nx * ny * nz - 1
 
     def text(self) -> str:
-        out = [f"mpm3d *** {self.title}", "nbco 1", f"nbbo {self.nbbo}", f"nbmp {self.nbmp}"]
+        out = [f"mpm3d *** {self.title}", f"nbco {self.nbco}", f"nbbo {self.nbbo}", f"nbmp {self.nbmp}"]
         out += self.head
         out += self.bodies
         out += self.tail
@@ -254,6 +255,34 @@ def generic_block(material_line: str, eos_line: Optional[str] = None, *, dp: flo
     w.tail += ["velo", "body 1 %s %s %s" % tuple(f32s(v) for v in velocity), "endv"]
     if gravity is not None:
         w.tail += ["load", f"grav 1 0 0 {f32s(gravity)}", "endl"]
+    return w.text()
+
+
+def contact_blocks(shape: Optional[str] = None, scheme: str = "usf", fricfa: float = 0.0, normbody: int = 0,
+                   dp: float = 0.25, speed: float = 4.0, counts=(6, 4, 4), gap_cells: float = 1.0) -> str:
+    """Two elastic blocks on separate grid components driven into each other
+    along x (block 1 at +speed, block 2 at -speed, a gap of `gap_cells` cells),
+    with Bardenhagen's contact ('cont lagr fricfa normbody'); block 2 also
+    slides in y so that friction acts. Cell = 2 dp (8 particles per cell)."""
+    h = 2 * dp
+    w = DeckWriter(f"contact of two blocks, {shape or 'linear'}, {scheme}")
+    w.nbco = 2
+    w.kw("nmat 1")
+    lx, ly, lz = (counts[i] * dp for i in range(3))
+    x2 = lx + gap_cells * h
+    w.head += _grid_lines(((-2 * h, x2 + lx + 2 * h), (-2 * h, ly + 2 * h), (-2 * h, lz + 2 * h)), h)
+    w.kw("dtsc 0.4")
+    w.kw("endt 100.0")
+    w.kw(f"{scheme} on")
+    if shape:
+        w.kw(shape)
+    w.kw(f"cont lagr {f32s(fricfa)} {normbody}")
+    w.kw("fixe 0 0 0 0 0 0")
+    w.kw("mate")
+    w.kw("1 elas 1000 1e6 0.3")
+    w.block(1, 1000.0, dp, (0.0, 0.0, 0.0), counts, com=1)
+    w.block(1, 1000.0, dp, (x2, 0.0, 0.0), counts, com=2)
+    w.tail += ["velo", f"body 1 {f32s(speed)} 0 0", f"body 2 {f32s(-speed)} {f32s(speed * 0.5)} 0", "endv"]
     return w.text()
 
 

@@ -9,9 +9,10 @@
  *
  * Scope: the updated-Lagrangian step (MPM3D.f90:68-160) with linear, GIMP,
  * B-spline and SGMP shape functions, USF / USL / MUSL, material types 1-11
- * and EOS 1-4, and the stress smoothing of SmoothStressbyGrid. Contact
- * (Lagr_NodContact) and TLMPM are not restated; orc_create rejects decks that
- * switch them on.
+ * and EOS 1-4, the stress smoothing of SmoothStressbyGrid, and grid
+ * components with the Lagrangian contact of Lagr_NodContact. TLMPM, and SGMP
+ * with several grid components, are not restated; orc_create rejects decks
+ * that ask for them.
  */
 #include "mpm_oracle.h"
 
@@ -62,6 +63,12 @@ struct orc {
   int nb_mat;
   mpm_material* mat;
   int MUSL, USL, USF, GIMP, Bspline, SGMP, QuasiLoad, QuasiDamp, UpdateVbyFp, Gravity, DR_DAMPING, SmoothStress;
+  /* grid components and contact (Particle.f90:69-92, Grid.f90:66-80): grid
+   * component c (0-based) holds nodes c*nb_gridnode .. ; a body's particles
+   * map to its component (comID) when contact is on, to component 0 otherwise */
+  int nb_component, contact, contact_type, normbody;
+  double fricfa, tot_cont_for[3];
+  double (*ndir)[3]; /* CP_list%ndir per component node */
   int istep;
   double DT, QuasiLoadTime, DampFactor, CurrentTime, EndTime, DTScale;
   double EngInternal, EngKinetic, EngKinetic_prev, Momentum[3];
@@ -180,6 +187,12 @@ static void cnshape(orc* o) {
 }
 
 static int node_valid(const orc* o, int n) { return n <= o->nb_gridnode && n > 0; }
+
+/* first node of body b's grid component (comID when contact is on) */
+static int64_t comp_base(const orc* o, int b) {
+  return o->contact ? (int64_t)(o->body[b].comID - 1) * o->nb_gridnode : 0;
+}
+static int64_t all_nodes(const orc* o) { return (int64_t)o->nb_gridnode * o->nb_component; }
 
 /* NShape_GIMP, Grid.f90:546-599 */
 static void nshape_gimp(orc* o) {
@@ -425,7 +438,11 @@ static int set_grid_data(orc* o) {
   o->nb_gridnode = o->NGxy * o->NGz;
 
   o->node = (onode*)calloc((size_t)o->nb_gridnode, sizeof(onode));
-  o->grid = (ogrid*)calloc((size_t)o->nb_gridnode, sizeof(ogrid));
+  o->grid = (ogrid*)calloc((size_t)o->nb_gridnode * (size_t)o->nb_component, sizeof(ogrid));
+  if (o->contact) {
+    o->ndir = (double(*)[3])calloc((size_t)o->nb_gridnode * (size_t)o->nb_component, sizeof(double[3]));
+    if (!o->ndir) return oerr(o, MPM_ERR_OOM, "out of memory");
+  }
   o->Cxg = (double(*)[3])calloc((size_t)o->NumCell, sizeof(double[3]));
   o->CellsNode = (int(*)[8])calloc((size_t)o->NumCell, sizeof(int[8]));
   if (!o->node || !o->grid || !o->Cxg || !o->CellsNode) return oerr(o, MPM_ERR_OOM, "out of memory");
@@ -1231,7 +1248,7 @@ static int center_valid(const orc* o, int c) { return c <= o->nb_centernode && c
 
 /* GridMomentumInitial, update_step.f90:288-406 */
 static void grid_momentum_initial(orc* o) {
-  for (int n = 0; n < o->nb_gridnode; ++n) {
+  for (int64_t n = 0; n < all_nodes(o); ++n) {
     o->grid[n].Mg = 0.0;
     o->grid[n].PXg[0] = o->grid[n].PXg[1] = o->grid[n].PXg[2] = 0.0;
   }
@@ -1243,6 +1260,7 @@ static void grid_momentum_initial(orc* o) {
     }
   }
   for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
     for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
       opart* p = &o->pt[ip];
       if (o->SGMP) {
@@ -1263,7 +1281,7 @@ static void grid_momentum_initial(orc* o) {
         particle_shape(o, p, p->icell);
         for (int n = 0; n < o->nb_InflNode; ++n) {
           if (!node_valid(o, o->InflNode[n])) continue;
-          ogrid* gd = &o->grid[o->InflNode[n] - 1];
+          ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
           double shm = o->SHP[n] * mp_;
           gd->Mg = gd->Mg + shm;
           for (int c = 0; c < 3; ++c) gd->PXg[c] = gd->PXg[c] + p->VXp[c] * shm;
@@ -1282,7 +1300,7 @@ static void grid_momentum_initial(orc* o) {
     }
   }
   int64_t act = 0;
-  for (int n = 0; n < o->nb_gridnode; ++n) act += o->grid[n].Mg > 0;
+  for (int64_t n = 0; n < all_nodes(o); ++n) act += o->grid[n].Mg > 0;
   o->active_nodes = act;
 }
 
@@ -1290,11 +1308,12 @@ static void grid_momentum_initial(orc* o) {
  * update_step.f90:1795-1830; the same loop closes IntegrateMomentum and
  * GridMomentumMUSL) */
 static void apply_bc(orc* o) {
-  for (int n = 0; n < o->nb_gridnode; ++n) {
+  for (int64_t k = 0; k < all_nodes(o); ++k) {
+    const int64_t n = k % o->nb_gridnode;
     for (int c = 0; c < 3; ++c) {
       if (o->node[n].fix[c]) {
-        o->grid[n].PXg[c] = 0.0;
-        o->grid[n].FXg[c] = 0.0;
+        o->grid[k].PXg[c] = 0.0;
+        o->grid[k].FXg[c] = 0.0;
       }
     }
   }
@@ -1336,6 +1355,7 @@ static int particle_stress_update(orc* o) {
     }
   }
   for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
     for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
       opart* p = &o->pt[ip];
       double de[6] = {0, 0, 0, 0, 0, 0}, vort[3] = {0, 0, 0}, deFp[3][3];
@@ -1361,7 +1381,7 @@ static int particle_stress_update(orc* o) {
         particle_shape(o, p, p->icell);
         for (int n = 0; n < o->nb_InflNode; ++n) {
           if (!node_valid(o, o->InflNode[n])) continue;
-          const ogrid* gd = &o->grid[o->InflNode[n] - 1];
+          const ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
           if (!(gd->Mg > o->CutOff)) continue;
           double v[3];
           for (int c = 0; c < 3; ++c) v[c] = gd->PXg[c] / gd->Mg;
@@ -1424,11 +1444,14 @@ static void grid_momentum_update(orc* o) {
       memset(o->cellp[i].Cfext, 0, sizeof o->cellp[i].Cfext);
     }
   }
-  for (int n = 0; n < o->nb_gridnode; ++n) o->grid[n].FXg[0] = o->grid[n].FXg[1] = o->grid[n].FXg[2] = 0.0;
+  for (int64_t n = 0; n < all_nodes(o); ++n) o->grid[n].FXg[0] = o->grid[n].FXg[1] = o->grid[n].FXg[2] = 0.0;
+  if (o->contact) memset(o->ndir, 0, sizeof(double[3]) * (size_t)all_nodes(o));
   for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
     for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
       opart* p = &o->pt[ip];
       double fx[3];
+      const double mp_ = p->mass;
       particle_fx(o, p, b, fx);
       double vol_ = p->VOL;
       double sxx = p->SM - p->q + p->SDxx;
@@ -1456,13 +1479,19 @@ static void grid_momentum_update(orc* o) {
         particle_shape(o, p, p->icell);
         for (int n = 0; n < o->nb_InflNode; ++n) {
           if (!node_valid(o, o->InflNode[n])) continue;
-          ogrid* gd = &o->grid[o->InflNode[n] - 1];
+          ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
           double s = o->SHP[n], dx = o->DNDX[n], dy = o->DNDY[n], dz = o->DNDZ[n];
           double fi[3];
           fi[0] = -(sxx * dx + sxy * dy + sxz * dz) * vol_;
           fi[1] = -(sxy * dx + syy * dy + syz * dz) * vol_;
           fi[2] = -(sxz * dx + syz * dy + szz * dz) * vol_;
           for (int c = 0; c < 3; ++c) gd->FXg[c] = gd->FXg[c] + fi[c] + fx[c] * s;
+          if (o->contact) { /* mass-gradient normal of the component's node (update_step.f90:977-982) */
+            double* nd = o->ndir[cb + o->InflNode[n] - 1];
+            nd[0] = nd[0] + dx * mp_;
+            nd[1] = nd[1] + dy * mp_;
+            nd[2] = nd[2] + dz * mp_;
+          }
         }
       }
     }
@@ -1486,8 +1515,9 @@ static void grid_momentum_update(orc* o) {
 
 /* IntegrateMomentum, update_step.f90:1194-1239 */
 static void integrate_momentum(orc* o) {
-  for (int n = 0; n < o->nb_gridnode; ++n) {
-    ogrid* gd = &o->grid[n];
+  for (int64_t k = 0; k < all_nodes(o); ++k) {
+    const int64_t n = k % o->nb_gridnode;
+    ogrid* gd = &o->grid[k];
     for (int c = 0; c < 3; ++c) {
       if (o->istep == 1)
         gd->PXg[c] = gd->PXg[c] + gd->FXg[c] * o->DT * 0.5;
@@ -1500,6 +1530,82 @@ static void integrate_momentum(orc* o) {
         gd->FXg[c] = 0.0;
       }
     }
+  }
+}
+
+/* Lagr_NodContact, update_step.f90:1241-1376 (Bardenhagen's method between
+ * grid components 1 and 2): per node, the contact normal from the two
+ * components' mass gradients (normbody 0: their difference, 1: body a's,
+ * 2: minus body b's), unitised; where both components have mass above the
+ * cut-off and approach along the normal (crit > epsilon), the normal contact
+ * force crit / ((Mg1 + Mg2) DT) -- with friction, the full sticking force
+ * limited to fricfa |normal force| tangentially -- is taken from component 1
+ * and given to component 2 in force and momentum, on the free directions of
+ * the node; the forces add up to the plotted total contact force. */
+static void lagr_contact(orc* o) {
+  const double eps = 2.220446049250313e-16; /* epsilon(1d0) */
+  const int64_t nn = o->nb_gridnode;
+  o->tot_cont_for[0] = o->tot_cont_for[1] = o->tot_cont_for[2] = 0.0;
+  for (int64_t n = 0; n < nn; ++n) {
+    double* cp1 = o->ndir[n];
+    double* cp2 = o->ndir[nn + n];
+    ogrid* gd1 = &o->grid[n];
+    ogrid* gd2 = &o->grid[nn + n];
+    double nx = 0, ny = 0, nz = 0;
+    if (o->normbody == 0) {
+      nx = cp1[0] - cp2[0];
+      ny = cp1[1] - cp2[1];
+      nz = cp1[2] - cp2[2];
+    }
+    if (o->normbody == 1) {
+      nx = cp1[0];
+      ny = cp1[1];
+      nz = cp1[2];
+    }
+    if (o->normbody == 2) {
+      nx = -cp2[0];
+      ny = -cp2[1];
+      nz = -cp2[2];
+    }
+    double tt = sqrt(nx * nx + ny * ny + nz * nz);
+    if (tt > eps) {
+      nx = nx / tt;
+      ny = ny / tt;
+      nz = nz / tt;
+    }
+    cp1[0] = nx;
+    cp1[1] = ny;
+    cp1[2] = nz;
+    cp2[0] = -cp1[0];
+    cp2[1] = -cp1[1];
+    cp2[2] = -cp1[2];
+    double crit = 0.0;
+    if (gd1->Mg > o->CutOff && gd2->Mg > o->CutOff)
+      crit = (gd1->PXg[0] * gd2->Mg - gd2->PXg[0] * gd1->Mg) * nx + (gd1->PXg[1] * gd2->Mg - gd2->PXg[1] * gd1->Mg) * ny +
+             (gd1->PXg[2] * gd2->Mg - gd2->PXg[2] * gd1->Mg) * nz;
+    if (!(crit > eps)) continue;
+    tt = (gd1->Mg + gd2->Mg) * o->DT;
+    const double nomforce = crit / tt;
+    double cforce[3];
+    if (o->fricfa > eps) {
+      double fstick[3];
+      for (int c = 0; c < 3; ++c) cforce[c] = (gd1->PXg[c] * gd2->Mg - gd2->PXg[c] * gd1->Mg) / tt;
+      for (int c = 0; c < 3; ++c) fstick[c] = cforce[c] - nomforce * cp1[c];
+      const double val_fstick = sqrt(fstick[0] * fstick[0] + fstick[1] * fstick[1] + fstick[2] * fstick[2]);
+      const double val_fslip = o->fricfa * fabs(nomforce);
+      if (val_fslip < val_fstick)
+        for (int c = 0; c < 3; ++c) cforce[c] = nomforce * cp1[c] + val_fslip * (fstick[c] / val_fstick);
+    } else {
+      for (int c = 0; c < 3; ++c) cforce[c] = nomforce * cp1[c];
+    }
+    for (int c = 0; c < 3; ++c) {
+      if (o->node[n].fix[c]) continue;
+      gd1->FXg[c] = gd1->FXg[c] - cforce[c];
+      gd2->FXg[c] = gd2->FXg[c] + cforce[c];
+      gd1->PXg[c] = gd1->PXg[c] - cforce[c] * o->DT;
+      gd2->PXg[c] = gd2->PXg[c] + cforce[c] * o->DT;
+    }
+    for (int c = 0; c < 3; ++c) o->tot_cont_for[c] = o->tot_cont_for[c] + cforce[c];
   }
 }
 
@@ -1595,6 +1701,7 @@ static void particle_position_update(orc* o) {
     boundary_aux_update(o);
   }
   for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
     for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
       opart* p = &o->pt[ip];
       double xx[3], vx[3] = {0, 0, 0}, ax[3] = {0, 0, 0};
@@ -1626,7 +1733,7 @@ static void particle_position_update(orc* o) {
         particle_shape(o, p, p->icell);
         for (int n = 0; n < o->nb_InflNode; ++n) {
           if (!node_valid(o, o->InflNode[n])) continue;
-          const ogrid* gd = &o->grid[o->InflNode[n] - 1];
+          const ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
           if (!(gd->Mg > o->CutOff)) continue;
           double s = o->SHP[n];
           for (int c = 0; c < 3; ++c) {
@@ -1649,10 +1756,11 @@ static void particle_position_update(orc* o) {
 
 /* GridMomentumMUSL, update_step.f90:1668-1793 */
 static void grid_momentum_musl(orc* o) {
-  for (int n = 0; n < o->nb_gridnode; ++n) o->grid[n].PXg[0] = o->grid[n].PXg[1] = o->grid[n].PXg[2] = 0.0;
+  for (int64_t n = 0; n < all_nodes(o); ++n) o->grid[n].PXg[0] = o->grid[n].PXg[1] = o->grid[n].PXg[2] = 0.0;
   if (o->SGMP)
     for (int i = 0; i < o->nb_centernode; ++i) memset(o->cellp[i].Cpxg, 0, sizeof o->cellp[i].Cpxg);
   for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
     for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
       opart* p = &o->pt[ip];
       if (o->SGMP) {
@@ -1672,7 +1780,7 @@ static void grid_momentum_musl(orc* o) {
         particle_shape(o, p, p->icell);
         for (int n = 0; n < o->nb_InflNode; ++n) {
           if (!node_valid(o, o->InflNode[n])) continue;
-          ogrid* gd = &o->grid[o->InflNode[n] - 1];
+          ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
           double shm = o->SHP[n] * mp_;
           for (int c = 0; c < 3; ++c) gd->PXg[c] = gd->PXg[c] + p->VXp[c] * shm;
         }
@@ -1825,6 +1933,9 @@ int orc_phase(orc* o, int phase) {
     case MPM_PHASE_UPDATE_DT: update_dt(o); return MPM_OK;
     case MPM_PHASE_DR_DAMPING: dr_damping(o); return MPM_OK;
     case MPM_PHASE_SMOOTH_STRESS: smooth_stress(o); return MPM_OK;
+    case MPM_PHASE_CONTACT:
+      if (o->contact && o->contact_type == 1) lagr_contact(o);
+      return MPM_OK;
     default: return oerr(o, MPM_ERR_ARG, "unknown phase %d", phase);
   }
 }
@@ -1840,6 +1951,7 @@ int orc_step(orc* o) {
   }
   grid_momentum_update(o);
   integrate_momentum(o);
+  if (o->contact && o->contact_type == 1) lagr_contact(o);
   particle_position_update(o);
   if (o->MUSL) {
     grid_momentum_musl(o);
@@ -1869,8 +1981,19 @@ int orc_create(const mpm_deck* d, int libm_mode, orc** out) {
   orc* o = (orc*)calloc(1, sizeof(orc));
   if (!o) return MPM_ERR_OOM;
   *out = o;
-  if (d->flags & (MPM_F_CONTACT | MPM_F_TLMPM))
-    return oerr(o, MPM_ERR_UNSUPPORTED, "contact / TLMPM are outside the restated step");
+  if (d->flags & MPM_F_TLMPM) return oerr(o, MPM_ERR_UNSUPPORTED, "TLMPM is outside the restated step");
+  o->nb_component = d->nb_component > 0 ? d->nb_component : 1;
+  o->contact = !!(d->flags & MPM_F_CONTACT);
+  o->contact_type = d->contact_type;
+  o->normbody = d->normbody;
+  o->fricfa = d->fricfa;
+  if ((d->flags & MPM_F_SGMP) && o->nb_component > 1)
+    return oerr(o, MPM_ERR_UNSUPPORTED, "SGMP with several grid components is outside the restated step");
+  if (o->contact && o->contact_type == 1 && (o->nb_component < 2 || o->normbody < 0 || o->normbody > 2))
+    return oerr(o, MPM_ERR_ARG, "contact needs two grid components and normbody 0, 1 or 2");
+  for (int b = 0; b < d->nb_body; ++b)
+    if (o->contact && (d->bodies[b].comID < 1 || d->bodies[b].comID > o->nb_component))
+      return oerr(o, MPM_ERR_ARG, "body %d: component %d out of 1..%d", b + 1, d->bodies[b].comID, o->nb_component);
   if (libm_mode == ORC_LIBM_PROJECT) {
     o->f_log = proj_log; o->f_exp = proj_exp; o->f_pow = proj_pow;
   } else {
@@ -1932,7 +2055,7 @@ int orc_create(const mpm_deck* d, int libm_mode, orc** out) {
 
 void orc_destroy(orc* o) {
   if (!o) return;
-  free(o->pt); free(o->body); free(o->mat); free(o->node); free(o->grid); free(o->Cxg);
+  free(o->pt); free(o->body); free(o->mat); free(o->node); free(o->grid); free(o->ndir); free(o->Cxg);
   free(o->cellp); free(o->CellsNode); free(o->CenterCellNode);
   free(o);
 }
@@ -1940,6 +2063,12 @@ void orc_destroy(orc* o) {
 const char* orc_error(const orc* o) { return o ? o->err : "null oracle"; }
 int64_t orc_nb_particle(const orc* o) { return o ? o->np : -1; }
 int64_t orc_nb_gridnode(const orc* o) { return o ? o->nb_gridnode : -1; }
+int orc_nb_component(const orc* o) { return o ? o->nb_component : -1; }
+int orc_contact_force(const orc* o, double f[3]) {
+  if (!o || !f) return MPM_ERR_ARG;
+  for (int c = 0; c < 3; ++c) f[c] = o->tot_cont_for[c];
+  return MPM_OK;
+}
 int64_t orc_nb_cell(const orc* o) { return o ? o->NumCell : -1; }
 
 int orc_get_scalars(orc* o, double* s) {
@@ -2020,12 +2149,12 @@ static int field_io(orc* o, int field, double* out, const double* in, int set) {
       break;
     case MPM_G_MG:
       if (set) return MPM_ERR_ARG;
-      for (int n = 0; n < o->nb_gridnode; ++n) out[n] = o->grid[n].Mg;
+      for (int64_t n = 0; n < all_nodes(o); ++n) out[n] = o->grid[n].Mg;
       break;
     case MPM_G_PX:
     case MPM_G_FX: {
       if (set) return MPM_ERR_ARG;
-      const int64_t nn = o->nb_gridnode;
+      const int64_t nn = all_nodes(o);
       for (int64_t n = 0; n < nn; ++n)
         for (int c = 0; c < 3; ++c)
           out[c * nn + n] = field == MPM_G_PX ? o->grid[n].PXg[c] : o->grid[n].FXg[c];

@@ -46,6 +46,10 @@ int orc_download(orc* o, int field, double* out);
 int orc_upload(orc* o, int field, const double* in);
 int64_t orc_nb_particle(const orc* o);
 int64_t orc_nb_gridnode(const orc* o);
+/* grid components (grid fields hold nb_component * nb_gridnode nodes,
+ * component-major) and the total contact force of the last step */
+int orc_nb_component(const orc* o);
+int orc_contact_force(const orc* o, double f[3]);
 int64_t orc_nb_cell(const orc* o);
 
 #ifdef __cplusplus

@@ -33,7 +33,7 @@ PHASES = {
     "GridMomentumInitial": 1, "ApplyBoundaryConditions": 2, "ParticleStressUpdate": 3,
     "GridMomentumUpdate": 4, "IntegrateMomentum": 5, "ParticlePositionUpdate": 6,
     "GridMomentumMUSL": 7, "calcEnergy": 8, "UpdateDT": 9, "dynamicRelaxationDamping": 10,
-    "BeginStep": 11, "SmoothStressbyGrid": 12,
+    "BeginStep": 11, "SmoothStressbyGrid": 12, "Lagr_NodContact": 13,
 }
 SCALARS = ("istep", "CurrentTime", "DT", "EngKinetic", "EngInternal", "Momentum_x",
            "Momentum_y", "Momentum_z", "EngKinetic_prev", "nb_gridnode", "nb_particle",
@@ -66,6 +66,8 @@ def library() -> ctypes.CDLL:
             ("orc_nb_particle", i64, [vp]),
             ("orc_nb_gridnode", i64, [vp]),
             ("orc_nb_cell", i64, [vp]),
+            ("orc_nb_component", i, [vp]),
+            ("orc_contact_force", i, [vp, P(d)]),
         ]:
             f = getattr(lib, name)
             f.restype = res
@@ -103,6 +105,7 @@ class Oracle:
         self.nb_particle = int(lib.orc_nb_particle(h))
         self.nb_gridnode = int(lib.orc_nb_gridnode(h))
         self.nb_cell = int(lib.orc_nb_cell(h))
+        self.nb_component = int(lib.orc_nb_component(h))
 
     def close(self):
         if self._h and self._h.value:
@@ -135,10 +138,17 @@ class Oracle:
 
     def download(self, field: str) -> np.ndarray:
         ncomp = COMPONENTS.get(field, 1)
-        n = self.nb_gridnode if field in GRID_FIELDS else (self.nb_cell if field in CELL_FIELDS else self.nb_particle)
+        n = (self.nb_gridnode * self.nb_component if field in GRID_FIELDS
+             else (self.nb_cell if field in CELL_FIELDS else self.nb_particle))
         out = np.zeros(ncomp * n)
         self._check(library().orc_download(self._h, FIELDS[field], _dptr(out)))
         return out.reshape(ncomp, n) if ncomp > 1 else out
+
+    def contact_force(self) -> np.ndarray:
+        """Total contact force of the last step (Lagr_NodContact's tot_cont_for)."""
+        f = np.zeros(3)
+        self._check(library().orc_contact_force(self._h, _dptr(f)))
+        return f
 
     def upload(self, field: str, values):
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()

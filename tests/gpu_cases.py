@@ -19,6 +19,10 @@ CASES = {
     "cook_smooth_gimp": (lambda: decks.cook_membrane("gimp", spacing=1.0), 40),
     "cook_smooth_bspline": (lambda: decks.cook_membrane("bimp", spacing=1.0), 40),
     "cook_smooth_sgmp": (lambda: decks.cook_membrane("sgmp", spacing=1.0), 40),
+    # two blocks on separate grid components meeting head-on (Lagr_NodContact)
+    "contact_linear_usf": (lambda: decks.contact_blocks(None, "usf", fricfa=0.0, normbody=0), 50),
+    "contact_gimp_musl_friction": (lambda: decks.contact_blocks("gimp", "musl", fricfa=0.3, normbody=1), 50),
+    "contact_bspline_usl_friction": (lambda: decks.contact_blocks("bimp", "usl", fricfa=0.3, normbody=2), 50),
     "block_usf_elastic": (lambda: decks.generic_block("1 elas 1000 1e7 0.3"), 60),
     "block_musl_pla1_gimp": (lambda: decks.generic_block("1 pla1 1000 1e7 0.3 2e4", shape="gimp",
                                                          scheme="musl", velocity=(1.0, 0.0, -20.0)), 60),

@@ -46,6 +46,10 @@ def test_strict_bit_identical(gpu_mod, oracle_mod, name):
     g, o = _run_pair(gpu_mod, oracle_mod, text, steps, "fp64", "project")
     gs, os_ = g.scalars(), o.scalars()
     assert gs["istep"] == os_["istep"] == steps
+    # the total contact force is summed over nodes in a fixed tree order on the
+    # GPU, node by node on the CPU
+    fg, fo = g.contact_force(), o.contact_force()
+    assert np.all(np.abs(fg - fo) <= 1e-12 * max(np.abs(fo).max(), 1e-300)), (fg, fo)
     assert gs["DT"] == os_["DT"], (gs["DT"], os_["DT"])
     assert gs["CurrentTime"] == os_["CurrentTime"]
     bad = []

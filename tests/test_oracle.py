@@ -173,3 +173,41 @@ def test_stress_smoothing_reproduces_uniform_pressure(oracle_mod, variant):
         assert exact.mean() > 0.95 and np.all(np.abs(spre + 5.0) <= 1e-8 * 5.0)
     else:
         assert exact.all(), (variant, spre.min(), spre.max())
+
+
+@pytest.mark.parametrize("shape", [None, "gimp", "bimp"])
+@pytest.mark.parametrize("fricfa,normbody", [(0.0, 0), (0.3, 1), (0.3, 2)])
+def test_contact_blocks_exchange_and_rebound(oracle_mod, shape, fricfa, normbody):
+    """Lagr_NodContact between two blocks on their own grid components, driven
+    into each other with no fixed node: the contact step moves momentum from
+    one grid to the other at each contact node, so the summed grid momentum is
+    the same before and after it; the blocks do not pass through each other
+    (they separate again, moving apart); the plotted contact force is non-zero
+    while they touch."""
+    from mpm3d_gb300 import decks
+    o = oracle_mod.Oracle(deck_text=decks.contact_blocks(shape, "usf", fricfa=fricfa, normbody=normbody),
+                          libm="project")
+    assert o.nb_component == 2 and o.download("Mg").shape == (2 * o.nb_gridnode,)
+    mass = o.download("mass")
+    p0 = (mass * o.download("VXp")).sum(axis=1)
+    touching = 0
+    for _ in range(60):
+        for ph in ["BeginStep", "GridMomentumInitial", "ApplyBoundaryConditions", "ParticleStressUpdate",
+                   "GridMomentumUpdate", "IntegrateMomentum"]:
+            o.phase(ph)
+        before = o.download("PXg").sum(axis=1)
+        o.phase("Lagr_NodContact")
+        after = o.download("PXg").sum(axis=1)
+        scale = np.abs(o.download("PXg")).sum()
+        assert np.all(np.abs(after - before) <= 1e-12 * scale), (before, after)
+        touching += bool(np.any(o.contact_force() != 0.0))
+        for ph in ["ParticlePositionUpdate", "calcEnergy", "UpdateDT"]:
+            o.phase(ph)
+    assert touching >= 10
+    n = o.nb_particle
+    vx = o.download("VXp")[0]
+    assert vx[: n // 2].mean() < 0 < vx[n // 2:].mean()
+    # on separate grids each block's interface nodes carry only part of a
+    # cell's mass, and those below the cut-off keep back their internal force
+    p1 = (mass * o.download("VXp")).sum(axis=1)
+    assert np.all(np.abs(p1 - p0) <= 5e-4 * np.abs(mass * o.download("VXp")).sum()), (p0, p1)
