@@ -1,14 +1,13 @@
 /* mpm_output.h -- result files of MPM3D-F90 (DataOut.f90) written from host
  * arrays: the time-history curves (OutCurve: <job>_curv.dat, EnergyPlot.dat,
- * MomentumPlot.dat), the Tecplot animation (OutAnim: <job>_anim.dat) and the
- * ParaView animation (OutAnimPV: <job>_anim_<k>.vtu listed in <job>_anim.pvd,
+ * MomentumPlot.dat, ContforcPlot.dat with contact), the Tecplot animation
+ * (OutAnim: <job>_anim.dat) and the ParaView animation (OutAnimPV: <job>_anim_<k>.vtu listed in <job>_anim.pvd,
  * plus the grid <job>_Grid.vtu from OutGrid), in the reference's file names,
  * layouts and Fortran edit descriptors (E12.4, E10.3, I3, I10, ...).
  *
  * The writer takes plain host arrays, so the same calls serve the GPU
  * library (curve values gathered from the device, mpm_gather*) and any other
- * producer of the step's state. Not written: the contact-force plot (contact
- * is outside the explicit-step path).
+ * producer of the step's state.
  */
 #ifndef MPM_OUTPUT_H
 #define MPM_OUTPUT_H
@@ -62,6 +61,11 @@ int mpm_output_curve_items(const mpm_output* o, int64_t* particle, int* field, i
  * first), EnergyPlot.dat and MomentumPlot.dat. scalars16 as mpm_get_scalars
  * (time, energies, momentum); values as listed by mpm_output_curve_items. */
 int mpm_output_curve(mpm_output* o, const double* scalars16, const double* values);
+
+/* The contact-force row of OutCurve (DataOut.f90:148-152): with contact on,
+ * a row of ContforcPlot.dat (next to EnergyPlot.dat) with the time and the
+ * total contact force (mpm_contact_force); a no-op otherwise. */
+int mpm_output_contact(mpm_output* o, double time, const double* force3);
 
 /* One animation frame at an output time: OutAnim with 'tecp', OutAnimPV with
  * 'para' (DataOut.f90:157-247, 250-530). */

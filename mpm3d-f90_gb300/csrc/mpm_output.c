@@ -20,7 +20,7 @@ enum { kMaxCurves = 15 + 2, kMaxAnim = 10 + 1 };
 
 struct mpm_output {
   const mpm_deck* d;
-  FILE *curv, *energy, *momentum, *tec, *pvd;
+  FILE *curv, *energy, *momentum, *contact, *tec, *pvd;
   char job[1024];
   int ncurves, curve_option[kMaxCurves];
   int64_t curve_point[kMaxCurves]; /* 0-based */
@@ -136,7 +136,11 @@ int mpm_output_open(const mpm_deck* d, const char* job, const char* plot_dir, mp
   o->energy = open_w(path);
   snprintf(path, sizeof path, "%s%sMomentumPlot.dat", dir, need_sep ? "/" : "");
   o->momentum = open_w(path);
-  if (!o->curv || !o->energy || !o->momentum) {
+  if (d->flags & MPM_F_CONTACT) { /* DataIn.f90:89 */
+    snprintf(path, sizeof path, "%s%sContforcPlot.dat", dir, need_sep ? "/" : "");
+    o->contact = open_w(path);
+  }
+  if (!o->curv || !o->energy || !o->momentum || ((d->flags & MPM_F_CONTACT) && !o->contact)) {
     mpm_output_close(o);
     return MPM_ERR_IO;
   }
@@ -176,6 +180,7 @@ void mpm_output_close(mpm_output* o) {
   if (o->curv) fclose(o->curv);
   if (o->energy) fclose(o->energy);
   if (o->momentum) fclose(o->momentum);
+  if (o->contact) fclose(o->contact);
   free(o->xo);
   free(o);
 }
@@ -257,6 +262,15 @@ int mpm_output_curve(mpm_output* o, const double* s, const double* v) {
   fputc('\n', o->momentum);
   o->ncurve_rows++;
   return ferror(f) || ferror(o->energy) || ferror(o->momentum) ? MPM_ERR_IO : MPM_OK;
+}
+
+int mpm_output_contact(mpm_output* o, double time, const double* force3) {
+  if (!o || !force3) return MPM_ERR_ARG;
+  if (!o->contact) return MPM_OK;
+  put_e(o->contact, 12, 4, time);
+  for (int a = 0; a < 3; ++a) put_e(o->contact, 12, 4, force3[a]);
+  fputc('\n', o->contact);
+  return ferror(o->contact) ? MPM_ERR_IO : MPM_OK;
 }
 
 /* ----------------------------------------------------------- OutAnim */

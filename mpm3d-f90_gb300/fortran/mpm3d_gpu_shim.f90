@@ -7,7 +7,7 @@
 ! keep the time loop as it is: the step subroutines of update_step.f90
 ! (GridMomentumInitial, ApplyBoundaryConditions, ParticleStressUpdate,
 ! GridMomentumUpdate, IntegrateMomentum, ParticlePositionUpdate,
-! GridMomentumMUSL, UpdateDT, SmoothStressbyGrid) and calcEnergy /
+! GridMomentumMUSL, UpdateDT, SmoothStressbyGrid, Lagr_NodContact) and calcEnergy /
 ! dynamicRelaxationDamping of Particle.f90 are replaced by the gpu_* routines
 ! below, one C call each.
 ! gpu_sync_scalars copies DT, CurrentTime, energies and momentum back into
@@ -27,7 +27,7 @@ module mpm3d_gpu
        PH_PARTICLE_STRESS_UPDATE = 3, PH_GRID_MOMENTUM_UPDATE = 4, &
        PH_INTEGRATE_MOMENTUM = 5, PH_PARTICLE_POSITION_UPDATE = 6, &
        PH_GRID_MOMENTUM_MUSL = 7, PH_CALC_ENERGY = 8, PH_UPDATE_DT = 9, &
-       PH_DR_DAMPING = 10, PH_BEGIN_STEP = 11, PH_SMOOTH_STRESS = 12
+       PH_DR_DAMPING = 10, PH_BEGIN_STEP = 11, PH_SMOOTH_STRESS = 12, PH_CONTACT = 13
   integer(c_int), parameter :: F_XP = 1, F_VXP = 3, F_VOL = 7, F_SM = 10, F_SEQV = 11, &
        F_SD = 12, F_EPEFF = 14, F_CELSIUS = 15, F_IE = 18, F_CP = 20, F_FAILURE = 22, &
        F_SPRE = 26
@@ -149,6 +149,9 @@ contains
   end subroutine
   subroutine gpu_SmoothStressbyGrid()
     call check(mpm_step_phase(ctx, PH_SMOOTH_STRESS), 'SmoothStressbyGrid')
+  end subroutine
+  subroutine gpu_Lagr_NodContact()
+    call check(mpm_step_phase(ctx, PH_CONTACT), 'Lagr_NodContact')
   end subroutine
 
   ! One whole step (the fused kernel sequence) instead of the phases above.

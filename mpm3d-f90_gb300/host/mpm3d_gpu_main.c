@@ -129,6 +129,10 @@ int main(int argc, char** argv) {
     if (out) {
       if (ncur > 0 && (st = mpm_gather_wait(c, cv_))) break;
       if ((st = mpm_output_curve(out, s, cv_))) break;
+      if (d->flags & MPM_F_CONTACT) {
+        double cf[3];
+        if ((st = mpm_contact_force(c, cf)) || (st = mpm_output_contact(out, s[1], cf))) break;
+      }
       if (s[1] >= (double)plt) {
         plt = plt + (float)d->outtime;
         if ((st = anim_frame(c, d, out, s))) break;

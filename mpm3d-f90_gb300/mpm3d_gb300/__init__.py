@@ -140,6 +140,7 @@ def library() -> ctypes.CDLL:
         "mpm_output_curve_count": (i, [vp]),
         "mpm_output_curve_items": (i, [vp, P(i64), P(i), P(i), i]),
         "mpm_output_curve": (i, [vp, P(d), P(d)]),
+        "mpm_output_contact": (i, [vp, d, P(d)]),
         "mpm_output_anim": (i, [vp, P(d), vp]),
         "mpm_format_e": (i, [c, i, i, i, d]),
         "mpm_serve_create": (i, [vp, P(vp)]),
@@ -587,6 +588,13 @@ class Output:
         st = library().mpm_output_curve(self._h, _dptr(s), _dptr(v))
         if st:
             raise MpmError(st, "curve output")
+
+    def contact(self, time: float, force) -> None:
+        """A row of ContforcPlot.dat (decks with contact)."""
+        f = np.ascontiguousarray(force, dtype=np.float64)
+        st = library().mpm_output_contact(self._h, float(time), _dptr(f))
+        if st:
+            raise MpmError(st, "contact output")
 
     def anim(self, scalars, fields: dict) -> None:
         """fields: name (as in the view: xp, vxp, ..., icell) -> array in deck order."""

@@ -83,3 +83,15 @@ def test_tecplot_and_paraview_frames(gpu_mod, tmp_path):
     assert f'<Piece NumberOfPoints="{n}" NumberOfCells="{n}">' in vtu and vtu.count("<DataArray") == 1 + 20 + 3
     grid = open(job + "_Grid.vtu").read()
     assert 'Name="connectivity"' in grid and grid.rstrip().endswith("</VTKFile>")
+
+
+def test_contact_force_plot(gpu_mod, tmp_path):
+    """With contact on, OutCurve also writes ContforcPlot.dat (time and the
+    total contact force, 4E12.4) next to EnergyPlot.dat."""
+    from mpm3d_gb300 import Deck, Output, decks
+    d = Deck.parse(decks.contact_blocks())
+    job = str(tmp_path / "blocks")
+    with Output(d, job) as out:
+        out.contact(2e-3, [1.5, -0.25, 0.0])
+    rows = open(str(tmp_path / "ContforcPlot.dat")).read().splitlines()
+    assert rows == ["  0.2000E-02  0.1500E+01 -0.2500E+00  0.0000E+00"]
