@@ -87,6 +87,7 @@ enum mpm_field {
   MPM_P_CENTERICELL = 24,
   MPM_P_INODE = 25,
   MPM_P_SPRE = 26,   /* smoothed pressure (SmoothStressbyGrid; 0 without 'smoo') */
+  MPM_P_PK = 27,     /* 9: first Piola-Kirchhoff stress of TLMPM, xx yy zz yz xz xy zy zx yx */
   MPM_G_MG = 40,
   MPM_G_PX = 41,     /* 3 */
   MPM_G_FX = 42,     /* 3 */

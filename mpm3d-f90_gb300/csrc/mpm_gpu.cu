@@ -326,7 +326,7 @@ int smooth_pass(mpm_ctx* c) {
   if (!c->st.spre) return set_err(c, MPM_ERR_ARG, "stress smoothing is off for this deck (no 'smoo')");
   cudaError_t e = cudaMemsetAsync(c->st.seg, 0, sizeof(int) * ((size_t)c->nkeys + 1), c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "memset seg");
-  c->ops->smooth_locate(&c->st, c->g, c->stream);
+  c->ops->fixed_locate(&c->st, c->g, 0, c->stream);
   int r = sort_pairs(c);
   if (r) return r;
   c->ops->smooth(&c->st, c->g, c->stream);
@@ -338,8 +338,38 @@ int stress_pass(mpm_ctx* c) {
   return depeff_pass(c);
 }
 
+// one step of the total Lagrangian form, MPM3D.f90:164-226
+int enqueue_step_tl(mpm_ctx* c) {
+  const Geometry& g = c->g;
+  const StepOps* o = c->ops;
+  void* st = &c->st;
+  cudaStream_t s = c->stream;
+  int r;
+  o->begin_step(st, g, s);
+  cudaError_t e = cudaMemsetAsync(c->st.seg, 0, sizeof(int) * ((size_t)c->nkeys + 1), s);
+  if (e != cudaSuccess) return cuda_err(c, e, "memset seg");
+  o->fixed_locate(st, g, 1, s);
+  if ((r = sort_pairs(c))) return r;
+  o->tl_momentum(st, g, g.usf, s);
+  if (g.usf) o->tl_stress(st, g, s);
+  o->force_prep(st, g, s);
+  o->tl_force(st, g, 1, s);
+  if (g.contact && g.contact_type == 1) o->contact(st, g, s);
+  o->position(st, g, s);
+  if (g.musl) o->p2g_momentum(st, g, !g.usf, s);
+  if (!g.usf) o->tl_stress(st, g, s);
+  o->reduce(st, g, 3, c->red_blocks, s);
+  if (c->smooth)
+    if ((r = smooth_pass(c))) return r;
+  if (c->drdamp) o->dr_damping(st, g, s);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_err(c, e, "kernel launch");
+  return MPM_OK;
+}
+
 // one full step, MPM3D.f90:69-118, enqueued without synchronisation
 int enqueue_step(mpm_ctx* c) {
+  if (c->g.tlmpm) return enqueue_step_tl(c);
   const Geometry& g = c->g;
   const StepOps* o = c->ops;
   void* st = &c->st;
@@ -395,7 +425,7 @@ int mpm_field_components(int f) {
     case MPM_G_PX: case MPM_G_FX: case MPM_C_PX:
       return 3;
     case MPM_P_SD: return 6;
-    case MPM_P_FP: return 9;
+    case MPM_P_FP: case MPM_P_PK: return 9;
     case MPM_P_VOL: case MPM_P_VOL0: case MPM_P_SIG_Y: case MPM_P_SM: case MPM_P_SEQV: case MPM_P_EPEFF:
     case MPM_P_CELSIUS: case MPM_P_DMG: case MPM_P_LT: case MPM_P_IE: case MPM_P_MASS: case MPM_P_CP:
     case MPM_P_Q: case MPM_P_FAILURE: case MPM_P_ICELL: case MPM_P_CENTERICELL: case MPM_P_INODE: case MPM_P_SPRE:
@@ -411,7 +441,6 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
   if (!out) return set_err(nullptr, MPM_ERR_ARG, "out is NULL");
   *out = nullptr;
   if (!d) return set_err(nullptr, MPM_ERR_ARG, "deck is NULL");
-  if (d->flags & MPM_F_TLMPM) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "TLMPM is outside the explicit-step path");
   if (d->nb_particle <= 0 || d->nb_body <= 0 || d->nb_mat <= 0)
     return set_err(nullptr, MPM_ERR_ARG, "deck defines no particles / bodies / materials");
   if (d->nb_body > 65535) return set_err(nullptr, MPM_ERR_UNSUPPORTED, "more than 65535 bodies");
@@ -518,6 +547,10 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     AL(s.mg, double, nnt); AL(s.px, double, 3 * nnt); AL(s.fx, double, 3 * nnt); AL(s.vg, double, 3 * nnt);
     AL(s.fix, uint8_t, nn); AL(s.bd, uint8_t, nn);
     if (g.contact) { AL(s.ndir, double, 3 * nnt); AL(s.cforce, double, 3 * nn); }
+    if (g.tlmpm) {
+      AL(s.pk, double, 9 * np); AL(s.vol0, double, np);
+      if (g.shape == 3) AL(s.cpk, double, 9 * nc);
+    }
     if (g.shape == 3) {
       AL(s.cmg, double, nc); AL(s.cpx, double, 3 * nc); AL(s.cfext, double, 3 * nc); AL(s.cfint, double, 6 * nc);
       AL(s.co, double, 6 * nc); AL(s.cw, double, 3 * nc); AL(s.cdefp, double, 9 * nc);
@@ -604,6 +637,17 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
     }
     // calcEnergy before the loop (MPM3D.f90:42)
     c->ops->reduce(&c->st, g, 1, c->red_blocks, c->stream);
+    if (g.tlmpm) {
+      // GridMassInitial (MPM3D.f90:162): cells of the initial positions kept
+      // for the run, the grid mass mapped once
+      CKF(cudaMemsetAsync(s.pk, 0, sizeof(double) * 9 * np, c->stream));
+      CKF(cudaMemcpyAsync(s.vol0, s.vol, sizeof(double) * np, cudaMemcpyDeviceToDevice, c->stream));
+      c->ops->tl_initial(&c->st, g, c->stream);
+      CKF(cudaMemsetAsync(s.seg, 0, sizeof(int) * ((size_t)c->nkeys + 1), c->stream));
+      c->ops->fixed_locate(&c->st, g, 1, c->stream);
+      if ((r = sort_pairs(c))) goto fail;
+      c->ops->p2g_mass(&c->st, g, 0, 0, c->stream);
+    }
     CKF(cudaStreamSynchronize(c->stream));
     CKF(cudaGetLastError());
 #undef UPB
@@ -636,17 +680,27 @@ int mpm_step_phase(mpm_ctx* c, int phase) {
   switch (phase) {
     case MPM_PHASE_BEGIN_STEP: o->begin_step(st, g, s); break;
     case MPM_PHASE_GRID_MOMENTUM_INITIAL:
+      if (g.tlmpm) {  // TLGridMomentumInitial: momentum with the cells of the initial positions
+        cudaError_t e = cudaMemsetAsync(c->st.seg, 0, sizeof(int) * ((size_t)c->nkeys + 1), s);
+        if (e != cudaSuccess) return cuda_err(c, e, "memset seg");
+        o->fixed_locate(st, g, 1, s);
+        if ((r = sort_pairs(c))) return r;
+        o->tl_momentum(st, g, 0, s);
+        break;
+      }
       if ((r = build_pairs(c))) return r;
       o->p2g_mass(st, g, 0, 0, s);
       break;
     case MPM_PHASE_APPLY_BOUNDARY: o->apply_bc(st, g, s); break;
     case MPM_PHASE_PARTICLE_STRESS_UPDATE:
       o->node_velocity(st, g, s);
-      if ((r = stress_pass(c))) return r;
+      if (g.tlmpm) o->tl_stress(st, g, s);
+      else if ((r = stress_pass(c))) return r;
       break;
     case MPM_PHASE_GRID_MOMENTUM_UPDATE:
       o->force_prep(st, g, s);
-      o->p2g_force(st, g, 0, s);
+      if (g.tlmpm) o->tl_force(st, g, 0, s);
+      else o->p2g_force(st, g, 0, s);
       break;
     case MPM_PHASE_INTEGRATE_MOMENTUM: o->integrate(st, g, s); break;
     case MPM_PHASE_PARTICLE_POSITION_UPDATE:
@@ -808,6 +862,10 @@ static int field_ptr(mpm_ctx* c, int field, void** ptr, size_t* elem, long long*
     case MPM_P_CENTERICELL: *ptr = s.centericell; *elem = 4; break;
     case MPM_P_INODE: *ptr = s.inode; *elem = 4; break;
     case MPM_P_SPRE: *ptr = s.spre; break;  // null without 'smoo': reads as zeros
+    case MPM_P_PK: *ptr = s.pk; break;      // null without 'TLmp': reads as zeros
+    case MPM_P_VOL0:
+      if (!s.vol0) return set_err(c, MPM_ERR_ARG, "initial volume is kept by TLMPM contexts only");
+      *ptr = s.vol0; break;
     case MPM_G_MG: *ptr = s.mg; *count = c->g.nnt; break;  // every grid component, component-major
     case MPM_G_PX: *ptr = s.px; *count = 3 * c->g.nnt; break;
     case MPM_G_FX: *ptr = s.fx; *count = 3 * c->g.nnt; break;
@@ -863,6 +921,7 @@ int mpm_upload(mpm_ctx* c, int field, const double* in) {
   long long n = 0;
   int r = field_ptr(c, field, &p, &elem, &n);
   if (r) return r;
+  if (!p) return set_err(c, MPM_ERR_ARG, "field %d is not kept by this context", field);
   CK(cudaStreamSynchronize(c->stream));
   if (elem == 8) {
     CK(cudaMemcpy(p, in, (size_t)n * 8, cudaMemcpyHostToDevice));
@@ -925,7 +984,7 @@ int mpm_kernel_stats(mpm_ctx* c, int k, char* name, int namelen, int64_t* launch
 static const int kSnapFields[] = {MPM_P_XP,  MPM_P_XX,      MPM_P_VXP, MPM_P_FXP, MPM_P_XN,    MPM_P_XXN,
                                   MPM_P_VOL, MPM_P_SIG_Y,   MPM_P_SM,  MPM_P_SEQV, MPM_P_SD,   MPM_P_FP,
                                   MPM_P_EPEFF, MPM_P_CELSIUS, MPM_P_DMG, MPM_P_LT, MPM_P_IE,   MPM_P_MASS,
-                                  MPM_P_CP,  MPM_P_Q,       MPM_P_FAILURE};
+                                  MPM_P_CP,  MPM_P_Q,       MPM_P_FAILURE, MPM_P_PK};
 static const char kSnapMagic[8] = {'M', 'P', 'M', '3', 'D', 'S', 'N', '1'};
 
 struct SnapHeader {
@@ -983,7 +1042,7 @@ int mpm_snapshot_save(mpm_ctx* c, const char* path) {
   std::vector<unsigned char> buf;
   for (int k = 0; ok && k < h.nfields; ++k) {
     const int fld = kSnapFields[k];
-    if (fld == MPM_P_FP && !c->g.uvfp) continue;
+    if ((fld == MPM_P_FP && !c->g.uvfp) || (fld == MPM_P_PK && !c->g.tlmpm)) continue;
     void* p = nullptr;
     size_t elem = 0;
     long long n = 0;
@@ -1025,7 +1084,7 @@ int mpm_snapshot_load(mpm_ctx* c, const char* path) {
   std::vector<unsigned char> buf;
   for (int k = 0; r == MPM_OK && k < h.nfields; ++k) {
     const int fld = kSnapFields[k];
-    if (fld == MPM_P_FP && !c->g.uvfp) continue;
+    if ((fld == MPM_P_FP && !c->g.uvfp) || (fld == MPM_P_PK && !c->g.tlmpm)) continue;
     void* p = nullptr;
     size_t elem = 0;
     long long n = 0;

@@ -96,6 +96,7 @@ struct Geometry {
   int nb_mat, nb_body;
   int has_jc;         // a Johnson-Cook material (types 4, 7) is present
   int contact, contact_type, normbody;  // 'cont': bodies on their own components; type 1 = Lagr_NodContact
+  int tlmpm;          // 'TLmp': the total Lagrangian form
   double fricfa;      // friction coefficient of the contact
 };
 
@@ -125,6 +126,9 @@ struct DevState {
   double *spre, *gpre, *cgpre, *cgvall;
   // contact: mass-gradient normals [3][ncomp * nn], contact force per node [3][nn]
   double *ndir, *cforce;
+  // TLMPM: first Piola-Kirchhoff stress [9][Np] (xx yy zz yz xz xy zy zx yx),
+  // initial volume [Np], centre-node PK sums [9][Nc] (SGMP)
+  double *pk, *vol0, *cpk;
   // Johnson-Cook depeff carry
   int *setter, *setter_scan;
   double *dep;
@@ -161,12 +165,18 @@ struct StepOps {
   // mode bit 0: energies and momentum (calcEnergy), bit 1: next DT (UpdateDT)
   void (*reduce)(void* st, const Geometry& g, int mode, int nblocks, cudaStream_t s);
   void (*dr_damping)(void* st, const Geometry& g, cudaStream_t s);
-  // SmoothStressbyGrid: shapes + pair keys, then (after the pair sort) the
-  // maps to the grid and back
-  void (*smooth_locate)(void* st, const Geometry& g, cudaStream_t s);
+  // SmoothStressbyGrid (after fixed_locate and the pair sort): the maps to
+  // the grid and back
   void (*smooth)(void* st, const Geometry& g, cudaStream_t s);
   // Lagr_NodContact after IntegrateMomentum, with the total contact force
   void (*contact)(void* st, const Geometry& g, cudaStream_t s);
+  // shapes and pair keys from the cells the particles hold (smoothing: with_comp 0)
+  void (*fixed_locate)(void* st, const Geometry& g, int with_comp, cudaStream_t s);
+  // TLMPM: initial cells, momentum transfer, stress, force (+ integrate)
+  void (*tl_initial)(void* st, const Geometry& g, cudaStream_t s);
+  void (*tl_momentum)(void* st, const Geometry& g, int vel, cudaStream_t s);
+  void (*tl_stress)(void* st, const Geometry& g, cudaStream_t s);
+  void (*tl_force)(void* st, const Geometry& g, int integ, cudaStream_t s);
 };
 
 extern const StepOps kOpsStrict;   // MPM_FP64_STRICT

@@ -1450,6 +1450,273 @@ __global__ void k_sg_node_momentum(St<P> s, Geometry g, int vel) {
   if (vel) node_vel(s.mg, s.px, s.vg, (int)n, nn, g.cutoff);
 }
 
+// ================================================================= TLMPM
+// The total Lagrangian form (MPM3D.f90:161-244): the grid mass is mapped
+// once from the initial positions (GridMassInitial), each particle keeps the
+// cell of its initial position for the whole run (TLParticleInitial; shapes
+// as k_fixed_locate), the deformation gradient grows by the velocity
+// gradient, the stress is the neo-Hookean first Piola-Kirchhoff stress
+// (TLConstitution, M3DM11) and the internal forces come from it on the
+// initial volume (TLGridMomentumUpdate). Position update, MUSL re-map and
+// contact are those of the updated form.
+
+// TLParticleInitial (update_step.f90:127-172) at the initial positions;
+// XN is not set there for non-SGMP shapes and keeps its initial value 0
+template <class P>
+__global__ void k_tl_initial(St<P> s, Geometry g) {
+  using B = typename P::B;
+  const long long p = gtid();
+  if (p >= g.np) return;
+  const long long np = g.np;
+  const double x[3] = {s.xp[p], s.xp[np + p], s.xp[2 * np + p]};
+  const int icell = in_which_cell(g, x);
+  s.icell[p] = icell;
+  for (int d = 0; d < 3; ++d) s.xn[d * np + p] = (B)0;
+  if (g.shape != 3) return;
+  s.centericell[p] = center_in_which_cell(g, x);
+  const int ix = (int)((x[0] - g.span0[0]) / g.dcell + 0.5) + 1;
+  const int iy = (int)((x[1] - g.span0[1]) / g.dcell + 0.5) + 1;
+  const int iz = (int)((x[2] - g.span0[2]) / g.dcell + 0.5) + 1;
+  const long long inode = (long long)(iz - 1) * g.NGxy + (long long)(iy - 1) * g.NGx + ix;
+  s.inode[p] = (int)inode;
+  if (inode < 1 || inode > g.nn || icell < 1) return;  // outside the grid
+  const int bd = s.bd[inode - 1];
+  const int n1 = cell_node1(g, icell);
+  for (int d = 0; d < 3; ++d) {
+    double xxn = (x[d] - node_coord(g, (int)inode - 1, d)) * g.iJacobi;
+    if ((bd >> (2 * d)) & 3) xxn = xxn > 0 ? 1.0 : (xxn < 0 ? -1.0 : xxn);
+    s.xxn[d * np + p] = (B)xxn;
+    s.xn[d * np + p] = (B)((x[d] - (node_coord(g, n1, d) + g.dcell / 2.0)) * g.iJacobi);
+  }
+}
+
+// TLGridMomentumInitial, SGMP: centre nodes -> nodes, momentum of the cells
+// above the cut-off mass (the mass stays that of GridMassInitial)
+template <class P>
+__global__ void k_tl_sg_node_momentum(St<P> s, Geometry g, int vel) {
+  const long long n = gtid();
+  const int nn = g.nn;
+  if (n >= nn) return;
+  const long long nc = g.ncell;
+  double px = 0.0, py = 0.0, pz = 0.0;
+  for_adjacent_cells(g, n, [&](int c, int) {
+    if (!(s.cmg[c] > g.cutoff)) return;
+    px = px + 0.125 * s.cpx[c];
+    py = py + 0.125 * s.cpx[nc + c];
+    pz = pz + 0.125 * s.cpx[2 * nc + c];
+  });
+  s.px[n] = px;
+  s.px[nn + n] = py;
+  s.px[2LL * nn + n] = pz;
+  node_bc(s.fix[n], s.px, s.fx, n, nn);
+  if (vel) node_vel(s.mg, s.px, s.vg, n, nn, g.cutoff);
+}
+
+// TLParticleStressUpdate + TLConstitution / M3DM11 (update_step.f90:649-828,
+// Constitution.f90:370-523, 782-882) for one particle. Like the reference,
+// sig_y and epeff are written from the constitutive module's state, which
+// the TL update never loads (0 in a TL run).
+template <class P>
+__global__ void k_tl_stress(St<P> s, Geometry g) {
+  using R = typename P::R;
+  using B = typename P::B;
+  const long long p = gtid();
+  if (p >= g.np) return;
+  const long long np = g.np, nn = g.nnt;
+  R deFp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  if (g.shape == 3) {
+    if (s.centericell[p] < 0) return;
+    const long long nc = g.ncell;
+    for (int k = 0; k < 8; ++k) {
+      int c = s.snode[k * np + p];
+      if (c < 0) continue;
+      R sk = s.shp[k * np + p];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] + sk * (R)s.cdefp[(i * 3 + j) * nc + c];
+    }
+  } else {
+    if (s.icell[p] < 0) return;
+    for (int k = 0; k < g.K; ++k) {
+      int n = s.snode[k * np + p];
+      if (n < 0) continue;
+      if (!(s.mg[n] > g.cutoff)) continue;
+      R v[3] = {(R)s.vg[n], (R)s.vg[nn + n], (R)s.vg[2LL * nn + n]};
+      const long long idx = k * np + p;
+      R dx = s.dndx[idx], dy = s.dndy[idx], dz = s.dndz[idx];
+      for (int i = 0; i < 3; ++i) {
+        deFp[i][0] = deFp[i][0] + dx * v[i];
+        deFp[i][1] = deFp[i][1] + dy * v[i];
+        deFp[i][2] = deFp[i][2] + dz * v[i];
+      }
+    }
+  }
+  const DevScalars& sc = *s.sc;
+  const R DT = (R)sc.dt;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] * DT;
+  if (g.uvfp)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) s.fp[(i * 3 + j) * np + p] = (B)((R)s.fp[(i * 3 + j) * np + p] + deFp[i][j]);
+  // ---- TLConstitution
+  R ppk_old[9], ppk_new[9];
+  for (int i = 0; i < 9; ++i) ppk_old[i] = (R)s.pk[i * np + p];
+  const R vold = (R)s.vol[p];
+  R F3[3][3];
+  for (int i = 0; i < 9; ++i) F3[i / 3][i % 3] = (R)s.fp[i * np + p];
+  for (int i = 0; i < 3; ++i) F3[i][i] = F3[i][i] + (R)1.0;
+  const R detF = F3[0][0] * F3[1][1] * F3[2][2] - F3[0][0] * F3[1][2] * F3[2][1] -
+                 F3[1][0] * F3[0][1] * F3[2][2] + F3[1][0] * F3[0][2] * F3[2][1] +
+                 F3[2][0] * F3[0][1] * F3[1][2] - F3[2][0] * F3[0][2] * F3[1][1];
+  const R vol = detF * (R)s.vol0[p];
+  const DevMaterial& mt = s.mats[s.bodies[s.body[p]].mat];
+  const R young = (R)mt.young * ((R)1.0 - (R)s.dmg[p] + (R)2.220446049250313e-16);
+  const R nu = (R)mt.poisson;
+  const R G2 = young / (1 + nu);
+  const R lamda = (young * nu) / ((1 + nu) * (1 - 2 * nu));
+  const R G = (R)0.5 * G2, J = detF;
+  // F and its transposed inverse in the order 11 22 33 23 13 12 32 31 21
+  const R F[9] = {F3[0][0], F3[1][1], F3[2][2], F3[1][2], F3[0][2], F3[0][1], F3[2][1], F3[2][0], F3[1][0]};
+  R FIT[9];
+  FIT[0] = (F[1] * F[2] - F[3] * F[6]) / J;
+  FIT[1] = (F[0] * F[2] - F[4] * F[7]) / J;
+  FIT[2] = (F[0] * F[1] - F[5] * F[8]) / J;
+  FIT[3] = (F[5] * F[7] - F[0] * F[6]) / J;
+  FIT[4] = (F[8] * F[6] - F[1] * F[7]) / J;
+  FIT[5] = (F[3] * F[7] - F[2] * F[8]) / J;
+  FIT[6] = (F[4] * F[8] - F[3] * F[0]) / J;
+  FIT[7] = (F[3] * F[5] - F[4] * F[1]) / J;
+  FIT[8] = (F[4] * F[6] - F[5] * F[2]) / J;
+  const R lnJ = m_log<P>(J);
+  for (int i = 0; i < 9; ++i) ppk_new[i] = G * (F[i] - FIT[i]) + lamda * lnJ * FIT[i];
+  const R FT[9] = {F[0], F[1], F[2], F[6], F[7], F[8], F[3], F[4], F[5]};
+  R sig[6];
+  sig[0] = (ppk_new[0] * FT[0] + ppk_new[5] * FT[8] + ppk_new[4] * FT[7]) / J;
+  sig[1] = (ppk_new[8] * FT[5] + ppk_new[1] * FT[1] + ppk_new[3] * FT[6]) / J;
+  sig[2] = (ppk_new[7] * FT[4] + ppk_new[6] * FT[3] + ppk_new[2] * FT[2]) / J;
+  sig[3] = (ppk_new[8] * FT[4] + ppk_new[1] * FT[3] + ppk_new[3] * FT[2]) / J;  // yz
+  sig[4] = (ppk_new[0] * FT[4] + ppk_new[5] * FT[3] + ppk_new[4] * FT[2]) / J;  // xz
+  sig[5] = (ppk_new[0] * FT[5] + ppk_new[5] * FT[1] + ppk_new[4] * FT[6]) / J;  // xy
+  const R sm = (sig[0] + sig[1] + sig[2]) / (R)3.0;
+  const R sd[6] = {sig[0] - sm, sig[1] - sm, sig[2] - sm, sig[3], sig[4], sig[5]};
+  R J2 = (R)0.5 * (sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2]) + sd[3] * sd[3] + sd[4] * sd[4] + sd[5] * sd[5];
+  J2 = J2 * (R)3.0;
+  const R seqv = (R)(float)sqrt(J2);  // EquivalentStress: a default-REAL result
+  // increment of F in the same order as F
+  const R dF[9] = {deFp[0][0], deFp[1][1], deFp[2][2], deFp[1][2], deFp[0][2], deFp[0][1], deFp[2][1], deFp[2][0],
+                   deFp[1][0]};
+  R ieinc = 0;
+  for (int i = 0; i < 9; ++i) ieinc = ieinc + (R)0.5 * (ppk_old[i] + ppk_new[i]) * dF[i];
+  const R iener = (R)s.ie[p] + ieinc * (R)0.5 * (vol + vold);
+  for (int i = 0; i < 9; ++i) s.pk[i * np + p] = (double)ppk_new[i];
+  s.vol[p] = (B)vol;
+  s.sm[p] = (B)sm;
+  s.seqv[p] = (B)seqv;
+  s.sd[p] = (B)sd[0];
+  s.sd[np + p] = (B)sd[1];
+  s.sd[2 * np + p] = (B)sd[2];
+  s.sd[3 * np + p] = (B)sd[5];  // xy
+  s.sd[4 * np + p] = (B)sd[3];  // yz
+  s.sd[5 * np + p] = (B)sd[4];  // xz
+  s.sig_y[p] = (B)0;
+  s.epeff[p] = (B)0;
+  s.ie[p] = (double)iener;
+  s.q[p] = (B)0;
+  if (!g.usf)
+    for (int d = 0; d < 3; ++d) s.xp[d * np + p] = s.xx[d * np + p];
+}
+
+// TLGridMomentumUpdate (update_step.f90:1015-1191): nodal force from the
+// PK stress on the initial volume, then optionally IntegrateMomentum
+template <class P>
+__global__ void k_tl_p2g_force(St<P> s, Geometry g, int integ) {
+  using R = typename P::R;
+  const long long n = gtid();
+  const long long nn = g.nnt;
+  if (n >= nn) return;
+  const long long np = g.np;
+  double f0 = 0.0, f1 = 0.0, f2 = 0.0, nd0 = 0.0, nd1 = 0.0, nd2 = 0.0;
+  const int j0 = n == 0 ? 0 : s.seg[n - 1], j1 = s.seg[n];
+  for (int j = j0; j < j1; ++j) {
+    long long p, idx;
+    decode_pair(s.val_sorted[j], np, &p, &idx);
+    const R sk = s.shp[idx], dx = s.dndx[idx], dy = s.dndy[idx], dz = s.dndz[idx];
+    R K[9];
+    for (int k = 0; k < 9; ++k) K[k] = (R)s.pk[k * np + p];  // xx yy zz yz xz xy zy zx yx
+    const R vol = (R)s.vol0[p];
+    const R fi0 = -(K[0] * dx + K[5] * dy + K[4] * dz) * vol;
+    const R fi1 = -(K[8] * dx + K[1] * dy + K[3] * dz) * vol;
+    const R fi2 = -(K[7] * dx + K[6] * dy + K[2] * dz) * vol;
+    f0 = f0 + fi0 + s.fext[p] * sk;
+    f1 = f1 + fi1 + s.fext[np + p] * sk;
+    f2 = f2 + fi2 + s.fext[2 * np + p] * sk;
+    if (g.contact) {
+      const double mp = s.mass[p];
+      nd0 = nd0 + (double)dx * mp;
+      nd1 = nd1 + (double)dy * mp;
+      nd2 = nd2 + (double)dz * mp;
+    }
+  }
+  s.fx[n] = f0;
+  s.fx[nn + n] = f1;
+  s.fx[2LL * nn + n] = f2;
+  if (g.contact) {
+    s.ndir[n] = nd0;
+    s.ndir[nn + n] = nd1;
+    s.ndir[2LL * nn + n] = nd2;
+  }
+  if (integ) {
+    double fxn[3] = {f0, f1, f2};
+    node_integrate<P>(s, g, n, fxn);
+  }
+}
+
+// ... SGMP: particles -> cells (external force, PK * VOL0)
+template <class P>
+__global__ void k_tl_sg_cell_force(St<P> s, Geometry g) {
+  const long long c = gtid();
+  const int nc = g.ncell;
+  if (c >= nc) return;
+  const long long np = g.np;
+  double fe[3] = {0, 0, 0}, fk[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const int j0 = c == 0 ? 0 : s.seg[c - 1], j1 = s.seg[c];
+  for (int j = j0; j < j1; ++j) {
+    long long p, idx;
+    decode_pair(s.val_sorted[j], np, &p, &idx);
+    const double sk = (double)s.shp[idx], vol = (double)s.vol0[p];
+    for (int d = 0; d < 3; ++d) fe[d] = fe[d] + s.fext[d * np + p] * sk;
+    for (int k = 0; k < 9; ++k) fk[k] = fk[k] + sk * s.pk[k * np + p] * vol;
+  }
+  for (int d = 0; d < 3; ++d) s.cfext[(long long)d * nc + c] = fe[d];
+  for (int k = 0; k < 9; ++k) s.cpk[(long long)k * nc + c] = fk[k];
+}
+
+// ... cells -> nodes (every cell), then optionally integrate
+template <class P>
+__global__ void k_tl_sg_node_force(St<P> s, Geometry g, int integ) {
+  const long long n = gtid();
+  const int nn = g.nn;
+  if (n >= nn) return;
+  const long long nc = g.ncell;
+  double f[3] = {0.0, 0.0, 0.0};
+  for_adjacent_cells(g, n, [&](int c, int j) {
+    double dx = (double)kSN[0][j] * 1.0 * 1.0 * g.iJacobi4;
+    double dy = (double)kSN[1][j] * 1.0 * 1.0 * g.iJacobi4;
+    double dz = (double)kSN[2][j] * 1.0 * 1.0 * g.iJacobi4;
+    double C[9];
+    for (int k = 0; k < 9; ++k) C[k] = s.cpk[k * nc + c];
+    double fi0 = -(C[0] * dx + C[5] * dy + C[4] * dz);
+    double fi1 = -(C[8] * dx + C[1] * dy + C[3] * dz);
+    double fi2 = -(C[7] * dx + C[6] * dy + C[2] * dz);
+    f[0] = f[0] + 0.125 * s.cfext[c] + fi0;
+    f[1] = f[1] + 0.125 * s.cfext[nc + c] + fi1;
+    f[2] = f[2] + 0.125 * s.cfext[2 * nc + c] + fi2;
+  });
+  s.fx[n] = f[0];
+  s.fx[nn + n] = f[1];
+  s.fx[2LL * nn + n] = f[2];
+  if (integ) node_integrate<P>(s, g, n, f);
+}
+
 // ====================================================== stress smoothing
 // SmoothStressbyGrid (update_step.f90:1876-2055): the particles' pressure
 // -SM mapped to the grid with volume weights, normalised by the mapped
@@ -1461,9 +1728,12 @@ __global__ void k_sg_node_momentum(St<P> s, Geometry g, int vel) {
 // order (ascending particle per node or centre node; ascending cell per node;
 // slot order per particle).
 
-// the smoothing shapes and pair keys of every particle
+// shapes and pair keys of every particle with the cells it holds (those of
+// the start of the step for the smoothing, those of the start of the run for
+// TLMPM): GIMP / B-spline weights at the current position, linear ones at
+// XN, SGMP ones at XXN; with_comp: keys in the particle's grid component
 template <class P>
-__global__ void k_smooth_locate(St<P> s, Geometry g, int nkeys) {
+__global__ void k_fixed_locate(St<P> s, Geometry g, int nkeys, int with_comp) {
   const long long p = gtid();
   if (p >= g.np) return;
   const long long np = g.np;
@@ -1477,19 +1747,22 @@ __global__ void k_smooth_locate(St<P> s, Geometry g, int nkeys) {
   const int cc = g.shape == 3 ? s.centericell[p] : 0;
   int slot_node[27];
   const int nvalid = slot_shapes<P>(s, g, p, x, g.shape == 3 ? 0 : icell, xn, cc, xxn, slot_node);
-  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys, 0);  // SmoothStressbyGrid maps to component 1
+  const int cbase = with_comp && g.shape != 3 ? s.bodies[s.body[p]].comp * g.nn : 0;  // smoothing: component 1
+  write_pairs<P>(s, g, p, nvalid, slot_node, nkeys, cbase);
 }
 
 // pressure * volume and volume of one (node or centre node) slice of pairs,
 // in particle order; returns false for an empty slice
 template <class P>
-__device__ __forceinline__ bool smooth_sums(const St<P>& s, long long np, int j0, int j1, double& gp, double& gv) {
+__device__ __forceinline__ bool smooth_sums(const St<P>& s, const Geometry& g, int j0, int j1, double& gp, double& gv) {
+  const long long np = g.np;
   gp = 0.0;
   gv = 0.0;
   for (int j = j0; j < j1; ++j) {
     long long p, idx;
     decode_pair(s.val_sorted[j], np, &p, &idx);
-    const double shp = (double)s.shp[idx], sm = (double)s.sm[p], vol = (double)s.vol[p];
+    const double shp = (double)s.shp[idx], sm = (double)s.sm[p];
+    const double vol = g.tlmpm ? (double)s.vol0[p] : (double)s.vol[p];  // TLSmoothStressbyGrid: VOL0
     gp = gp + shp * (-1 * sm) * vol;
     gv = gv + shp * vol;
   }
@@ -1502,7 +1775,7 @@ __global__ void k_smooth_node(St<P> s, Geometry g) {
   const long long n = gtid();
   if (n >= g.nn) return;
   double gp, gv;
-  const bool mapped = smooth_sums<P>(s, g.np, n == 0 ? 0 : s.seg[n - 1], s.seg[n], gp, gv);
+  const bool mapped = smooth_sums<P>(s, g, n == 0 ? 0 : s.seg[n - 1], s.seg[n], gp, gv);
   s.gpre[n] = mapped ? gp / gv : gp;
 }
 
@@ -1512,7 +1785,7 @@ __global__ void k_smooth_cell(St<P> s, Geometry g) {
   const long long c = gtid();
   if (c >= g.ncell) return;
   double gp, gv;
-  smooth_sums<P>(s, g.np, c == 0 ? 0 : s.seg[c - 1], s.seg[c], gp, gv);
+  smooth_sums<P>(s, g, c == 0 ? 0 : s.seg[c - 1], s.seg[c], gp, gv);
   s.cgpre[c] = gp;
   s.cgvall[c] = gv;
 }

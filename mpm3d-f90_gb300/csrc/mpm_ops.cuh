@@ -103,10 +103,39 @@ struct Ops {
     prof_end(K_DR, s);
   }
 
-  static void smooth_locate(void* st, const Geometry& g, cudaStream_t s) {
-    prof_begin(K_SMOOTH, s);
-    k_smooth_locate<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g, g.shape == 3 ? g.ncell : g.nn);
-    prof_end(K_SMOOTH, s);
+  static void fixed_locate(void* st, const Geometry& g, int with_comp, cudaStream_t s) {
+    prof_begin(K_LOCATE, s);
+    k_fixed_locate<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g, g.shape == 3 ? g.ncell : (int)g.nnt, with_comp);
+    prof_end(K_LOCATE, s);
+  }
+  static void tl_initial(void* st, const Geometry& g, cudaStream_t s) {
+    k_tl_initial<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g);
+  }
+  static void tl_momentum(void* st, const Geometry& g, int vel, cudaStream_t s) {
+    prof_begin(K_P2G_MASS, s);
+    if (g.shape == 3) {
+      k_sg_cell_momentum<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
+      k_tl_sg_node_momentum<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, vel);
+    } else {
+      k_p2g_momentum<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g, vel);
+    }
+    prof_end(K_P2G_MASS, s);
+  }
+  static void tl_stress(void* st, const Geometry& g, cudaStream_t s) {
+    prof_begin(K_STRESS, s);
+    if (g.shape == 3) k_sg_cell_gradient<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
+    k_tl_stress<P><<<grid_for(g.np), kBlock, 0, s>>>(S(st), g);
+    prof_end(K_STRESS, s);
+  }
+  static void tl_force(void* st, const Geometry& g, int integ, cudaStream_t s) {
+    prof_begin(K_P2G_FORCE, s);
+    if (g.shape == 3) {
+      k_tl_sg_cell_force<P><<<grid_for(g.ncell), kBlock, 0, s>>>(S(st), g);
+      k_tl_sg_node_force<P><<<grid_for(g.nn), kBlock, 0, s>>>(S(st), g, integ);
+    } else {
+      k_tl_p2g_force<P><<<grid_for(g.nnt), kBlock, 0, s>>>(S(st), g, integ);
+    }
+    prof_end(K_P2G_FORCE, s);
   }
   static void smooth(void* st, const Geometry& g, cudaStream_t s) {
     prof_begin(K_SMOOTH, s);
@@ -148,7 +177,11 @@ struct Ops {
     o.p2g_momentum = p2g_momentum;
     o.reduce = reduce;
     o.dr_damping = dr_damping;
-    o.smooth_locate = smooth_locate;
+    o.fixed_locate = fixed_locate;
+    o.tl_initial = tl_initial;
+    o.tl_momentum = tl_momentum;
+    o.tl_stress = tl_stress;
+    o.tl_force = tl_force;
     o.smooth = smooth;
     o.contact = contact;
     return o;

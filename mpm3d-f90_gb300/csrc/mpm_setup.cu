@@ -153,6 +153,10 @@ int scene_setup(const mpm_deck* d, SceneSetup& out) {
   g.contact_type = d->contact_type;
   g.normbody = d->normbody;
   g.fricfa = d->fricfa;
+  g.tlmpm = !!(f & MPM_F_TLMPM);
+  if (g.tlmpm)
+    for (const auto& m : out.mats)
+      if (m.mat_type != 11) return fail(out, MPM_ERR_UNSUPPORTED, "TLMPM supports the neo-Hookean material only");
   if (sgmp && g.ncomp > 1)
     return fail(out, MPM_ERR_UNSUPPORTED, "SGMP with several grid components (the reference shares its centre grid)");
   if (g.contact && g.contact_type == 1 && (g.ncomp < 2 || g.normbody < 0 || g.normbody > 2))

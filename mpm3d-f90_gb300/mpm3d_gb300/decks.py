@@ -204,10 +204,11 @@ def dam_break(dp: float = 0.01, h: float = 0.02, water=(4.0, 2.0, 2.0), tank=(10
 
 def soft_beam(dp: float = 0.25, length: float = 6.0, depth: float = 1.0, thick: float = 1.0,
               young: float = 1e7, nu: float = 0.3, rho: float = 1000.0, dtscale: float = 0.5,
-              shape: str = "sgmp", scheme: str = "musl", gravity: float = -9.81) -> str:
+              shape: str = "sgmp", scheme: str = "musl", gravity: float = -9.81, tlmpm: bool = False) -> str:
     """Cantilever soft beam clamped at x = 0 (neo-Hookean). With SGMP the grid
     has one extra layer beyond the clamped face (the reference's rule for
-    fixed boundaries under SGMP)."""
+    fixed boundaries under SGMP). tlmpm: the total Lagrangian form ('TLmp',
+    with the deformation gradient tracked, 'UVFp')."""
     h = 2 * dp
     nx, ny, nz = int(round(length / dp)), int(round(thick / dp)), int(round(depth / dp))
     w = DeckWriter(f"soft beam, neo-Hookean, {shape}, {scheme}")
@@ -220,6 +221,9 @@ def soft_beam(dp: float = 0.25, length: float = 6.0, depth: float = 1.0, thick: 
     w.kw(f"{scheme} on")
     if shape in ("sgmp", "gimp", "bimp"):
         w.kw(shape)
+    if tlmpm:
+        w.kw("TLmp")
+        w.kw("UVFp")
     w.kw("fixe 1 0 2 2 0 0")
     w.kw("mate")
     w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")

@@ -9,10 +9,10 @@
  *
  * Scope: the updated-Lagrangian step (MPM3D.f90:68-160) with linear, GIMP,
  * B-spline and SGMP shape functions, USF / USL / MUSL, material types 1-11
- * and EOS 1-4, the stress smoothing of SmoothStressbyGrid, and grid
- * components with the Lagrangian contact of Lagr_NodContact. TLMPM, and SGMP
- * with several grid components, are not restated; orc_create rejects decks
- * that ask for them.
+ * and EOS 1-4, the stress smoothing of SmoothStressbyGrid, grid components
+ * with the Lagrangian contact of Lagr_NodContact, and the total Lagrangian
+ * form (TLMPM, neo-Hookean). SGMP with several grid components is not
+ * restated; orc_create rejects decks that ask for it.
  */
 #include "mpm_oracle.h"
 
@@ -35,6 +35,7 @@ typedef struct opart {
   int failure, icell, centericell;
   double DMG, LT, ie, mass, cp, q;
   double Spre; /* smoothed pressure (Particle.f90:40) */
+  double PK[9]; /* first Piola-Kirchhoff stress of TLMPM: xx yy zz yz xz xy zy zx yx (Particle.f90:29) */
 } opart;
 
 typedef struct onode {
@@ -52,6 +53,7 @@ typedef struct ogrid {
 typedef struct ocellp {
   double Cmg, Cpxg[3], Cfint[6], Cfext[3], Cvx[3], Cax[3], Co[6], Cw[3], CdeFp[3][3];
   double CGpre, CGV_all; /* stress smoothing (Grid.f90:62-64) */
+  double CPKint[9];      /* TLMPM internal-force sums (Grid.f90:61) */
 } ocellp;
 
 struct orc {
@@ -63,6 +65,7 @@ struct orc {
   int nb_mat;
   mpm_material* mat;
   int MUSL, USL, USF, GIMP, Bspline, SGMP, QuasiLoad, QuasiDamp, UpdateVbyFp, Gravity, DR_DAMPING, SmoothStress;
+  int TLMPM; /* total Lagrangian form (MPM3D.f90:161-244) */
   /* grid components and contact (Particle.f90:69-92, Grid.f90:66-80): grid
    * component c (0-based) holds nodes c*nb_gridnode .. ; a body's particles
    * map to its component (comID) when contact is on, to component 0 otherwise */
@@ -1319,41 +1322,46 @@ static void apply_bc(orc* o) {
   }
 }
 
-/* ParticleStressUpdate, update_step.f90:456-647 */
-static int particle_stress_update(orc* o) {
-  if (o->SGMP) {
-    for (int i = 0; i < o->nb_centernode; ++i) {
-      ocellp* cd = &o->cellp[i];
-      memset(cd->Co, 0, sizeof cd->Co);
-      memset(cd->Cw, 0, sizeof cd->Cw);
-      memset(cd->CdeFp, 0, sizeof cd->CdeFp);
-    }
-    for (int i = 0; i < o->nb_centernode; ++i) {
-      ocellp* cd = &o->cellp[i];
-      cnshape(o);
-      for (int j = 0; j < 8; ++j) {
-        const ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
-        if (!(gd->Mg > o->CutOff)) continue;
-        double v[3];
-        for (int c = 0; c < 3; ++c) v[c] = gd->PXg[c] / gd->Mg;
-        double dx = o->CDNDX[j], dy = o->CDNDY[j], dz = o->CDNDZ[j];
-        cd->Co[0] = cd->Co[0] + dx * v[0];
-        cd->Co[1] = cd->Co[1] + dy * v[1];
-        cd->Co[2] = cd->Co[2] + dz * v[2];
-        cd->Co[3] = cd->Co[3] + dz * v[1] + dy * v[2];
-        cd->Co[4] = cd->Co[4] + dz * v[0] + dx * v[2];
-        cd->Co[5] = cd->Co[5] + dy * v[0] + dx * v[1];
-        cd->Cw[0] = cd->Cw[0] + dy * v[2] - dz * v[1];
-        cd->Cw[1] = cd->Cw[1] + dz * v[0] - dx * v[2];
-        cd->Cw[2] = cd->Cw[2] + dx * v[1] - dy * v[0];
-        for (int n = 0; n < 3; ++n) {
-          cd->CdeFp[n][0] = cd->CdeFp[n][0] + dx * v[n];
-          cd->CdeFp[n][1] = cd->CdeFp[n][1] + dy * v[n];
-          cd->CdeFp[n][2] = cd->CdeFp[n][2] + dz * v[n];
-        }
+/* centre-node strain rate, spin and velocity gradient from the cell nodes
+ * (the SGMP part of ParticleStressUpdate, update_step.f90:478-523, and of
+ * TLParticleStressUpdate, 671-716) */
+static void sg_cell_gradients(orc* o) {
+  for (int i = 0; i < o->nb_centernode; ++i) {
+    ocellp* cd = &o->cellp[i];
+    memset(cd->Co, 0, sizeof cd->Co);
+    memset(cd->Cw, 0, sizeof cd->Cw);
+    memset(cd->CdeFp, 0, sizeof cd->CdeFp);
+  }
+  for (int i = 0; i < o->nb_centernode; ++i) {
+    ocellp* cd = &o->cellp[i];
+    cnshape(o);
+    for (int j = 0; j < 8; ++j) {
+      const ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
+      if (!(gd->Mg > o->CutOff)) continue;
+      double v[3];
+      for (int c = 0; c < 3; ++c) v[c] = gd->PXg[c] / gd->Mg;
+      double dx = o->CDNDX[j], dy = o->CDNDY[j], dz = o->CDNDZ[j];
+      cd->Co[0] = cd->Co[0] + dx * v[0];
+      cd->Co[1] = cd->Co[1] + dy * v[1];
+      cd->Co[2] = cd->Co[2] + dz * v[2];
+      cd->Co[3] = cd->Co[3] + dz * v[1] + dy * v[2];
+      cd->Co[4] = cd->Co[4] + dz * v[0] + dx * v[2];
+      cd->Co[5] = cd->Co[5] + dy * v[0] + dx * v[1];
+      cd->Cw[0] = cd->Cw[0] + dy * v[2] - dz * v[1];
+      cd->Cw[1] = cd->Cw[1] + dz * v[0] - dx * v[2];
+      cd->Cw[2] = cd->Cw[2] + dx * v[1] - dy * v[0];
+      for (int n = 0; n < 3; ++n) {
+        cd->CdeFp[n][0] = cd->CdeFp[n][0] + dx * v[n];
+        cd->CdeFp[n][1] = cd->CdeFp[n][1] + dy * v[n];
+        cd->CdeFp[n][2] = cd->CdeFp[n][2] + dz * v[n];
       }
     }
   }
+}
+
+/* ParticleStressUpdate, update_step.f90:456-647 */
+static int particle_stress_update(orc* o) {
+  if (o->SGMP) sg_cell_gradients(o);
   for (int b = 0; b < o->nb_body; ++b) {
     const int64_t cb = comp_base(o, b);
     for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
@@ -1797,6 +1805,343 @@ static void grid_momentum_musl(orc* o) {
   apply_bc(o);
 }
 
+/* ====================================================================
+ * Total Lagrangian MPM (MPM3D.f90:161-244): the grid mass is mapped once,
+ * cells are those of the initial positions for the whole run, the
+ * deformation gradient grows by the velocity gradient, and the internal
+ * forces come from the first Piola-Kirchhoff stress on the initial volume.
+ * Shapes are evaluated as the reference does: GIMP and B-spline at the
+ * current Xp against the initial cell, SGMP at the initial XXN, linear at
+ * XN -- which TLParticleInitial does not set for linear shapes, so it keeps
+ * its initial value (0 here: the cell centre).
+ * ==================================================================== */
+
+/* TLParticleInitial, update_step.f90:127-172 */
+static void tl_particle_initial(orc* o) {
+  for (int64_t ip = 0; ip < o->np; ++ip) {
+    opart* p = &o->pt[ip];
+    p->icell = in_which_cell(o, p->Xo);
+    if (!o->SGMP) continue;
+    p->centericell = center_in_which_cell(o, p->Xo);
+    int ix = (int)((p->Xo[0] - o->SpanX[0]) / o->DCell + 0.5) + 1;
+    int iy = (int)((p->Xo[1] - o->SpanY[0]) / o->DCell + 0.5) + 1;
+    int iz = (int)((p->Xo[2] - o->SpanZ[0]) / o->DCell + 0.5) + 1;
+    p->inode = (iz - 1) * o->NGxy + (iy - 1) * o->NGx + ix;
+    if (p->inode < 1 || p->inode > o->nb_gridnode || p->icell < 1) continue; /* outside the grid */
+    const onode* nd = &o->node[p->inode - 1];
+    for (int d = 0; d < 3; ++d) p->XXN[d] = (p->Xo[d] - nd->Xg[d]) * o->iJacobi;
+    for (int d = 0; d < 3; ++d) p->XN[d] = (p->Xo[d] - o->Cxg[p->icell - 1][d]) * o->iJacobi;
+    for (int d = 0; d < 3; ++d)
+      if (nd->bd_type[d] != 0) {
+        if (p->XXN[d] > 0) p->XXN[d] = 1;
+        else if (p->XXN[d] < 0) p->XXN[d] = -1;
+      }
+  }
+}
+
+/* GridMassInitial, update_step.f90:22-125 (once, before the time loop) */
+static void grid_mass_initial(orc* o) {
+  for (int64_t n = 0; n < all_nodes(o); ++n) o->grid[n].Mg = 0.0;
+  tl_particle_initial(o);
+  if (o->SGMP)
+    for (int c = 0; c < o->NumCell; ++c) o->cellp[c].Cmg = 0.0;
+  for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
+    for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
+      opart* p = &o->pt[ip];
+      double mp_ = p->mass;
+      if (o->SGMP) {
+        if (p->centericell < 0) continue;
+        for (int n = 0; n < 8; ++n) o->CenterInflNode[n] = o->CenterCellNode[p->centericell - 1][n];
+        sg_nshape(o, p->XXN);
+        for (int n = 0; n < 8; ++n) {
+          if (!center_valid(o, o->CenterInflNode[n])) continue;
+          ocellp* cd = &o->cellp[o->CenterInflNode[n] - 1];
+          cd->Cmg = cd->Cmg + o->SHP[n] * mp_;
+        }
+      } else {
+        if (p->icell < 0) continue;
+        particle_shape(o, p, p->icell);
+        for (int n = 0; n < o->nb_InflNode; ++n) {
+          if (!node_valid(o, o->InflNode[n])) continue;
+          ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
+          gd->Mg = gd->Mg + o->SHP[n] * mp_;
+        }
+      }
+    }
+  }
+  if (o->SGMP)
+    for (int i = 0; i < o->nb_centernode; ++i) {
+      if (!(o->cellp[i].Cmg > o->CutOff)) continue;
+      for (int j = 0; j < 8; ++j) {
+        ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
+        gd->Mg = gd->Mg + 0.125 * o->cellp[i].Cmg;
+      }
+    }
+  int64_t act = 0;
+  for (int64_t n = 0; n < all_nodes(o); ++n) act += o->grid[n].Mg > 0;
+  o->active_nodes = act;
+}
+
+/* TLGridMomentumInitial, update_step.f90:174-286 (momentum only) */
+static void tl_grid_momentum_initial(orc* o) {
+  for (int64_t n = 0; n < all_nodes(o); ++n) o->grid[n].PXg[0] = o->grid[n].PXg[1] = o->grid[n].PXg[2] = 0.0;
+  if (o->SGMP)
+    for (int c = 0; c < o->NumCell; ++c) o->cellp[c].Cpxg[0] = o->cellp[c].Cpxg[1] = o->cellp[c].Cpxg[2] = 0.0;
+  for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
+    for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
+      opart* p = &o->pt[ip];
+      double mp_ = p->mass;
+      if (o->SGMP) {
+        if (p->centericell < 0) continue;
+        for (int n = 0; n < 8; ++n) o->CenterInflNode[n] = o->CenterCellNode[p->centericell - 1][n];
+        sg_nshape(o, p->XXN);
+        for (int n = 0; n < 8; ++n) {
+          if (!center_valid(o, o->CenterInflNode[n])) continue;
+          ocellp* cd = &o->cellp[o->CenterInflNode[n] - 1];
+          double shm = o->SHP[n] * mp_;
+          for (int c = 0; c < 3; ++c) cd->Cpxg[c] = cd->Cpxg[c] + p->VXp[c] * shm;
+        }
+      } else {
+        if (p->icell < 0) continue;
+        particle_shape(o, p, p->icell);
+        for (int n = 0; n < o->nb_InflNode; ++n) {
+          if (!node_valid(o, o->InflNode[n])) continue;
+          ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
+          double shm = o->SHP[n] * mp_;
+          for (int c = 0; c < 3; ++c) gd->PXg[c] = gd->PXg[c] + p->VXp[c] * shm;
+        }
+      }
+    }
+  }
+  if (o->SGMP)
+    for (int i = 0; i < o->nb_centernode; ++i) {
+      if (!(o->cellp[i].Cmg > o->CutOff)) continue;
+      for (int j = 0; j < 8; ++j) {
+        ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
+        for (int c = 0; c < 3; ++c) gd->PXg[c] = gd->PXg[c] + 0.125 * o->cellp[i].Cpxg[c];
+      }
+    }
+}
+
+/* TLConstitution + M3DM11 (neo-Hookean), Constitution.f90:370-523, 782-882:
+ * the first Piola-Kirchhoff stress from F = I + Fp, the Cauchy stress from
+ * it, the volume det(F) VOL0, and the internal energy from the mid-step PK
+ * stress on the increment of F. Like the reference, sig_y and epeff are
+ * written from the constitutive module's state, which the TL update does
+ * not load from the particle. */
+static int tl_constitution(orc* o, int b, int64_t pidx, const double deFp[3][3]) {
+  opart* p = &o->pt[pidx];
+  double ppk_old[9], ppk_new[9];
+  memcpy(ppk_old, p->PK, sizeof ppk_old);
+  memcpy(o->deF, deFp, sizeof o->deF);
+  o->vold = p->VOL;
+  memcpy(o->Fp, p->Fp, sizeof o->Fp);
+  for (int i = 0; i < 3; ++i) o->Fp[i][i] = o->Fp[i][i] + 1.0;
+  double (*F3)[3] = o->Fp;
+  const double detF = F3[0][0] * F3[1][1] * F3[2][2] - F3[0][0] * F3[1][2] * F3[2][1] -
+                      F3[1][0] * F3[0][1] * F3[2][2] + F3[1][0] * F3[0][2] * F3[2][1] +
+                      F3[2][0] * F3[0][1] * F3[1][2] - F3[2][0] * F3[0][2] * F3[1][1];
+  p->VOL = detF * p->VOL0;
+  o->vol_ = p->VOL;
+  o->dvol = 0.5 * (o->vol_ - o->vold);
+  o->mid = o->body[b].mat;
+  const mpm_material* m = &o->mat[o->mid - 1];
+  if (m->mat_type != 11) return oerr(o, MPM_ERR_UNSUPPORTED, "TLMPM supports the neo-Hookean material only");
+  o->seqv = p->Seqv;
+  o->mtype_ = m->mat_type;
+  o->etype_ = m->eos_type;
+  o->miu2 = 2 * m->miu;
+  o->young_ = m->young;
+  o->poisson_ = m->poisson;
+  o->yield0_ = m->yield0;
+  o->tangmod_ = m->tangmod;
+  o->den0_ = m->density;
+  o->DMG = p->DMG;
+  o->oldDMG = o->DMG;
+  o->young_ = o->young_ * (1.0 - o->DMG + 2.220446049250313e-16);
+  o->G2 = o->young_ / (1 + o->poisson_);
+  o->K3 = o->young_ / (1 - 2 * o->poisson_);
+  o->lamda = (o->young_ * o->poisson_) / ((1 + o->poisson_) * (1 - 2 * o->poisson_));
+  o->PlaMod = o->young_ * o->tangmod_ / (o->young_ - o->tangmod_);
+  o->cp = p->cp;
+  o->sm = p->SM;
+  o->smold = p->SM;
+  o->iener = p->ie;
+  o->bqf = 0.0;
+  /* M3DM11: F / transposed inverse in the order 11 22 33 23 13 12 32 31 21 */
+  const double G = 0.5 * o->G2;
+  const double J = detF;
+  const double F[9] = {F3[0][0], F3[1][1], F3[2][2], F3[1][2], F3[0][2], F3[0][1], F3[2][1], F3[2][0], F3[1][0]};
+  double FIT[9];
+  FIT[0] = (F[1] * F[2] - F[3] * F[6]) / J;
+  FIT[1] = (F[0] * F[2] - F[4] * F[7]) / J;
+  FIT[2] = (F[0] * F[1] - F[5] * F[8]) / J;
+  FIT[3] = (F[5] * F[7] - F[0] * F[6]) / J;
+  FIT[4] = (F[8] * F[6] - F[1] * F[7]) / J;
+  FIT[5] = (F[3] * F[7] - F[2] * F[8]) / J;
+  FIT[6] = (F[4] * F[8] - F[3] * F[0]) / J;
+  FIT[7] = (F[3] * F[5] - F[4] * F[1]) / J;
+  FIT[8] = (F[4] * F[6] - F[5] * F[2]) / J;
+  const double lnJ = o->f_log(J);
+  for (int i = 0; i < 9; ++i) ppk_new[i] = G * (F[i] - FIT[i]) + o->lamda * lnJ * FIT[i];
+  const double FT[9] = {F[0], F[1], F[2], F[6], F[7], F[8], F[3], F[4], F[5]};
+  double* sig = o->sig;
+  sig[0] = (ppk_new[0] * FT[0] + ppk_new[5] * FT[8] + ppk_new[4] * FT[7]) / J;
+  sig[1] = (ppk_new[8] * FT[5] + ppk_new[1] * FT[1] + ppk_new[3] * FT[6]) / J;
+  sig[2] = (ppk_new[7] * FT[4] + ppk_new[6] * FT[3] + ppk_new[2] * FT[2]) / J;
+  sig[3] = (ppk_new[8] * FT[4] + ppk_new[1] * FT[3] + ppk_new[3] * FT[2]) / J;
+  sig[4] = (ppk_new[0] * FT[4] + ppk_new[5] * FT[3] + ppk_new[4] * FT[2]) / J;
+  sig[5] = (ppk_new[0] * FT[5] + ppk_new[5] * FT[1] + ppk_new[4] * FT[6]) / J;
+  o->sm = (sig[0] + sig[1] + sig[2]) / 3.0;
+  o->sd[0] = sig[0] - o->sm;
+  o->sd[1] = sig[1] - o->sm;
+  o->sd[2] = sig[2] - o->sm;
+  o->sd[3] = sig[3];
+  o->sd[4] = sig[4];
+  o->sd[5] = sig[5];
+  o->seqv = equivalent_stress(o);
+  const double* dF = &o->deF[0][0];
+  const double deltaFp[9] = {dF[0], dF[4], dF[8], dF[5], dF[2], dF[1], dF[7], dF[6], dF[3]};
+  o->ieinc = 0.0;
+  for (int i = 0; i < 9; ++i) o->ieinc = o->ieinc + 0.5 * (ppk_old[i] + ppk_new[i]) * deltaFp[i];
+  o->iener = o->iener + o->ieinc * 0.5 * (o->vol_ + o->vold);
+  memcpy(p->PK, ppk_new, sizeof p->PK);
+  p->SM = o->sm;
+  p->Seqv = o->seqv;
+  p->SDxx = o->sd[0]; p->SDyy = o->sd[1]; p->SDzz = o->sd[2];
+  p->SDyz = o->sd[3]; p->SDxz = o->sd[4]; p->SDxy = o->sd[5];
+  p->sig_y = o->sig_y_;
+  p->epeff = o->epeff_;
+  p->ie = o->iener;
+  p->cp = o->cp;
+  p->q = o->bqf;
+  return MPM_OK;
+}
+
+/* TLParticleStressUpdate, update_step.f90:649-828 (the strain-rate and spin
+ * sums of the reference are not used by TLConstitution) */
+static int tl_particle_stress_update(orc* o) {
+  if (o->SGMP) sg_cell_gradients(o);
+  for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
+    for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
+      opart* p = &o->pt[ip];
+      double deFp[3][3];
+      memset(deFp, 0, sizeof deFp);
+      if (o->SGMP) {
+        if (p->centericell < 0) continue;
+        for (int n = 0; n < 8; ++n) o->CenterInflNode[n] = o->CenterCellNode[p->centericell - 1][n];
+        sg_nshape(o, p->XXN);
+        for (int n = 0; n < 8; ++n) {
+          if (!center_valid(o, o->CenterInflNode[n])) continue;
+          const ocellp* cd = &o->cellp[o->CenterInflNode[n] - 1];
+          double s = o->SHP[n];
+          for (int i = 0; i < 3; ++i) {
+            deFp[i][0] = deFp[i][0] + s * cd->CdeFp[i][0];
+            deFp[i][1] = deFp[i][1] + s * cd->CdeFp[i][1];
+            deFp[i][2] = deFp[i][2] + s * cd->CdeFp[i][2];
+          }
+        }
+      } else {
+        if (p->icell < 0) continue;
+        particle_shape(o, p, p->icell);
+        for (int n = 0; n < o->nb_InflNode; ++n) {
+          if (!node_valid(o, o->InflNode[n])) continue;
+          const ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
+          if (!(gd->Mg > o->CutOff)) continue;
+          double v[3];
+          for (int c = 0; c < 3; ++c) v[c] = gd->PXg[c] / gd->Mg;
+          double dx = o->DNDX[n], dy = o->DNDY[n], dz = o->DNDZ[n];
+          for (int i = 0; i < 3; ++i) {
+            deFp[i][0] = deFp[i][0] + dx * v[i];
+            deFp[i][1] = deFp[i][1] + dy * v[i];
+            deFp[i][2] = deFp[i][2] + dz * v[i];
+          }
+        }
+      }
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) deFp[i][j] = deFp[i][j] * o->DT;
+      if (o->UpdateVbyFp)
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) p->Fp[i][j] = p->Fp[i][j] + deFp[i][j];
+      int st = tl_constitution(o, b, ip, (const double (*)[3])deFp);
+      if (st) return st;
+      if (!o->USF) memcpy(p->Xp, p->XX, sizeof p->Xp);
+    }
+  }
+  return MPM_OK;
+}
+
+/* TLGridMomentumUpdate, update_step.f90:1015-1191 */
+static void tl_grid_momentum_update(orc* o) {
+  if (o->SGMP)
+    for (int i = 0; i < o->nb_centernode; ++i) {
+      memset(o->cellp[i].CPKint, 0, sizeof o->cellp[i].CPKint);
+      memset(o->cellp[i].Cfext, 0, sizeof o->cellp[i].Cfext);
+    }
+  for (int64_t n = 0; n < all_nodes(o); ++n) o->grid[n].FXg[0] = o->grid[n].FXg[1] = o->grid[n].FXg[2] = 0.0;
+  if (o->contact) memset(o->ndir, 0, sizeof(double[3]) * (size_t)all_nodes(o));
+  for (int b = 0; b < o->nb_body; ++b) {
+    const int64_t cb = comp_base(o, b);
+    for (int64_t ip = o->body[b].par_begin; ip < o->body[b].par_end; ++ip) {
+      opart* p = &o->pt[ip];
+      const double* K = p->PK; /* xx yy zz yz xz xy zy zx yx */
+      const double vol_ = p->VOL0, mp_ = p->mass;
+      double fx[3];
+      particle_fx(o, p, b, fx);
+      if (o->SGMP) {
+        if (p->centericell < 0) continue;
+        for (int n = 0; n < 8; ++n) o->CenterInflNode[n] = o->CenterCellNode[p->centericell - 1][n];
+        sg_nshape(o, p->XXN);
+        for (int n = 0; n < 8; ++n) {
+          if (!center_valid(o, o->CenterInflNode[n])) continue;
+          ocellp* cd = &o->cellp[o->CenterInflNode[n] - 1];
+          double s = o->SHP[n];
+          for (int c = 0; c < 3; ++c) cd->Cfext[c] = cd->Cfext[c] + fx[c] * s;
+          for (int k = 0; k < 9; ++k) cd->CPKint[k] = cd->CPKint[k] + s * K[k] * vol_;
+        }
+      } else {
+        if (p->icell < 0) continue;
+        particle_shape(o, p, p->icell);
+        for (int n = 0; n < o->nb_InflNode; ++n) {
+          if (!node_valid(o, o->InflNode[n])) continue;
+          ogrid* gd = &o->grid[cb + o->InflNode[n] - 1];
+          double s = o->SHP[n], dx = o->DNDX[n], dy = o->DNDY[n], dz = o->DNDZ[n];
+          double fi[3];
+          fi[0] = -(K[0] * dx + K[5] * dy + K[4] * dz) * vol_;
+          fi[1] = -(K[8] * dx + K[1] * dy + K[3] * dz) * vol_;
+          fi[2] = -(K[7] * dx + K[6] * dy + K[2] * dz) * vol_;
+          for (int c = 0; c < 3; ++c) gd->FXg[c] = gd->FXg[c] + fi[c] + fx[c] * s;
+          if (o->contact) {
+            double* nd = o->ndir[cb + o->InflNode[n] - 1];
+            nd[0] = nd[0] + dx * mp_;
+            nd[1] = nd[1] + dy * mp_;
+            nd[2] = nd[2] + dz * mp_;
+          }
+        }
+      }
+    }
+  }
+  if (o->SGMP) {
+    cnshape(o);
+    for (int i = 0; i < o->nb_centernode; ++i) {
+      const ocellp* cd = &o->cellp[i];
+      const double* C = cd->CPKint;
+      for (int j = 0; j < 8; ++j) {
+        ogrid* gd = &o->grid[o->CellsNode[i][j] - 1];
+        double dx = o->CDNDX[j], dy = o->CDNDY[j], dz = o->CDNDZ[j];
+        double fi[3];
+        fi[0] = -(C[0] * dx + C[5] * dy + C[4] * dz);
+        fi[1] = -(C[8] * dx + C[1] * dy + C[3] * dz);
+        fi[2] = -(C[7] * dx + C[6] * dy + C[2] * dz);
+        for (int c = 0; c < 3; ++c) gd->FXg[c] = gd->FXg[c] + 0.125 * cd->Cfext[c] + fi[c];
+      }
+    }
+  }
+}
+
 /* UpdateDT, update_step.f90:1833-1874 */
 static void update_dt(orc* o) {
   double max_vp = 0;
@@ -1853,8 +2198,9 @@ static void smooth_stress(orc* o) {
           if (!center_valid(o, o->CenterInflNode[n])) continue;
           ocellp* cd = &o->cellp[o->CenterInflNode[n] - 1];
           double SHPn = o->SHP[n];
-          cd->CGpre = cd->CGpre + SHPn * (-1 * p->SM) * p->VOL;
-          cd->CGV_all = cd->CGV_all + SHPn * p->VOL;
+          const double v = o->TLMPM ? p->VOL0 : p->VOL; /* TLSmoothStressbyGrid: VOL0 */
+          cd->CGpre = cd->CGpre + SHPn * (-1 * p->SM) * v;
+          cd->CGV_all = cd->CGV_all + SHPn * v;
         }
       } else {
         if (p->icell < 0) continue;
@@ -1864,8 +2210,9 @@ static void smooth_stress(orc* o) {
           ogrid* gd = &o->grid[o->InflNode[n] - 1];
           gd->mapped = 1;
           double SHPn = o->SHP[n];
-          gd->Gpre = gd->Gpre + SHPn * (-1 * p->SM) * p->VOL;
-          gd->GV_all = gd->GV_all + SHPn * p->VOL;
+          const double v = o->TLMPM ? p->VOL0 : p->VOL;
+          gd->Gpre = gd->Gpre + SHPn * (-1 * p->SM) * v;
+          gd->GV_all = gd->GV_all + SHPn * v;
         }
       }
     }
@@ -1922,10 +2269,16 @@ int orc_phase(orc* o, int phase) {
       o->CurrentTime = o->CurrentTime + o->DT;
       o->EngInternal = 0.0;
       return MPM_OK;
-    case MPM_PHASE_GRID_MOMENTUM_INITIAL: grid_momentum_initial(o); return MPM_OK;
+    case MPM_PHASE_GRID_MOMENTUM_INITIAL:
+      if (o->TLMPM) tl_grid_momentum_initial(o);
+      else grid_momentum_initial(o);
+      return MPM_OK;
     case MPM_PHASE_APPLY_BOUNDARY: apply_bc(o); return MPM_OK;
-    case MPM_PHASE_PARTICLE_STRESS_UPDATE: return particle_stress_update(o);
-    case MPM_PHASE_GRID_MOMENTUM_UPDATE: grid_momentum_update(o); return MPM_OK;
+    case MPM_PHASE_PARTICLE_STRESS_UPDATE: return o->TLMPM ? tl_particle_stress_update(o) : particle_stress_update(o);
+    case MPM_PHASE_GRID_MOMENTUM_UPDATE:
+      if (o->TLMPM) tl_grid_momentum_update(o);
+      else grid_momentum_update(o);
+      return MPM_OK;
     case MPM_PHASE_INTEGRATE_MOMENTUM: integrate_momentum(o); return MPM_OK;
     case MPM_PHASE_PARTICLE_POSITION_UPDATE: particle_position_update(o); return MPM_OK;
     case MPM_PHASE_GRID_MOMENTUM_MUSL: grid_momentum_musl(o); return MPM_OK;
@@ -1944,12 +2297,14 @@ int orc_phase(orc* o, int phase) {
 int orc_step(orc* o) {
   int st;
   orc_phase(o, MPM_PHASE_BEGIN_STEP);
-  grid_momentum_initial(o);
+  if (o->TLMPM) tl_grid_momentum_initial(o); /* MPM3D.f90:168-244 */
+  else grid_momentum_initial(o);
   if (o->USF) {
     apply_bc(o);
-    if ((st = particle_stress_update(o))) return st;
+    if ((st = o->TLMPM ? tl_particle_stress_update(o) : particle_stress_update(o))) return st;
   }
-  grid_momentum_update(o);
+  if (o->TLMPM) tl_grid_momentum_update(o);
+  else grid_momentum_update(o);
   integrate_momentum(o);
   if (o->contact && o->contact_type == 1) lagr_contact(o);
   particle_position_update(o);
@@ -1958,7 +2313,7 @@ int orc_step(orc* o) {
     apply_bc(o);
   }
   if (!o->USF) {
-    if ((st = particle_stress_update(o))) return st;
+    if ((st = o->TLMPM ? tl_particle_stress_update(o) : particle_stress_update(o))) return st;
   }
   calc_energy(o);
   update_dt(o);
@@ -1981,7 +2336,11 @@ int orc_create(const mpm_deck* d, int libm_mode, orc** out) {
   orc* o = (orc*)calloc(1, sizeof(orc));
   if (!o) return MPM_ERR_OOM;
   *out = o;
-  if (d->flags & MPM_F_TLMPM) return oerr(o, MPM_ERR_UNSUPPORTED, "TLMPM is outside the restated step");
+  o->TLMPM = !!(d->flags & MPM_F_TLMPM);
+  if (o->TLMPM)
+    for (int m = 0; m < d->nb_mat; ++m)
+      if (d->mats[m].mat_type != 11)
+        return oerr(o, MPM_ERR_UNSUPPORTED, "TLMPM supports the neo-Hookean material only (TLConstitution)");
   o->nb_component = d->nb_component > 0 ? d->nb_component : 1;
   o->contact = !!(d->flags & MPM_F_CONTACT);
   o->contact_type = d->contact_type;
@@ -2050,6 +2409,7 @@ int orc_create(const mpm_deck* d, int libm_mode, orc** out) {
   if (st) return st;
   set_dt(o);
   calc_energy(o); /* MPM3D.f90:42 */
+  if (o->TLMPM) grid_mass_initial(o); /* MPM3D.f90:162 */
   return MPM_OK;
 }
 
@@ -2114,6 +2474,13 @@ static int field_io(orc* o, int field, double* out, const double* in, int set) {
     case MPM_P_CP: PFIELD1(cp); break;
     case MPM_P_Q: PFIELD1(q); break;
     case MPM_P_SPRE: PFIELD1(Spre); break;
+    case MPM_P_PK:
+      for (int64_t p = 0; p < np; ++p)
+        for (int c = 0; c < 9; ++c) {
+          if (set) o->pt[p].PK[c] = in[c * np + p];
+          else out[c * np + p] = o->pt[p].PK[c];
+        }
+      break;
     case MPM_P_SD:
       for (int64_t p = 0; p < np; ++p) {
         opart* t = &o->pt[p];

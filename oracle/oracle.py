@@ -23,9 +23,9 @@ FIELDS = {
     "Xp": 1, "XX": 2, "VXp": 3, "FXp": 4, "XN": 5, "XXN": 6, "VOL": 7, "VOL0": 8, "sig_y": 9,
     "SM": 10, "Seqv": 11, "SD": 12, "Fp": 13, "epeff": 14, "celsius_t": 15, "DMG": 16, "LT": 17,
     "ie": 18, "mass": 19, "cp": 20, "q": 21, "failure": 22, "icell": 23, "centericell": 24,
-    "inode": 25, "Spre": 26, "Mg": 40, "PXg": 41, "FXg": 42, "Cmg": 50, "Cpxg": 51,
+    "inode": 25, "Spre": 26, "PK": 27, "Mg": 40, "PXg": 41, "FXg": 42, "Cmg": 50, "Cpxg": 51,
 }
-COMPONENTS = {"Xp": 3, "XX": 3, "VXp": 3, "FXp": 3, "XN": 3, "XXN": 3, "SD": 6, "Fp": 9,
+COMPONENTS = {"Xp": 3, "XX": 3, "VXp": 3, "FXp": 3, "XN": 3, "XXN": 3, "SD": 6, "Fp": 9, "PK": 9,
               "PXg": 3, "FXg": 3, "Cpxg": 3}
 GRID_FIELDS = {"Mg", "PXg", "FXg"}
 CELL_FIELDS = {"Cmg", "Cpxg"}

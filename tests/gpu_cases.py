@@ -23,6 +23,11 @@ CASES = {
     "contact_linear_usf": (lambda: decks.contact_blocks(None, "usf", fricfa=0.0, normbody=0), 50),
     "contact_gimp_musl_friction": (lambda: decks.contact_blocks("gimp", "musl", fricfa=0.3, normbody=1), 50),
     "contact_bspline_usl_friction": (lambda: decks.contact_blocks("bimp", "usl", fricfa=0.3, normbody=2), 50),
+    # total Lagrangian form (neo-Hookean soft beam under gravity), one per shape family
+    "tl_beam_linear_usf": (lambda: decks.soft_beam(shape="mpm", scheme="usf", tlmpm=True), 40),
+    "tl_beam_gimp_musl": (lambda: decks.soft_beam(shape="gimp", scheme="musl", tlmpm=True), 40),
+    "tl_beam_bspline_usl": (lambda: decks.soft_beam(shape="bimp", scheme="usl", tlmpm=True), 40),
+    "tl_beam_sgmp_musl": (lambda: decks.soft_beam(shape="sgmp", scheme="musl", tlmpm=True), 40),
     "block_usf_elastic": (lambda: decks.generic_block("1 elas 1000 1e7 0.3"), 60),
     "block_musl_pla1_gimp": (lambda: decks.generic_block("1 pla1 1000 1e7 0.3 2e4", shape="gimp",
                                                          scheme="musl", velocity=(1.0, 0.0, -20.0)), 60),

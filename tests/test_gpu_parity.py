@@ -17,7 +17,7 @@ import pytest
 from gpu_cases import CASES
 
 PARTICLE_FIELDS = ["Xp", "XX", "VXp", "VOL", "SM", "Seqv", "SD", "epeff", "sig_y", "ie", "q",
-                   "celsius_t", "failure", "icell", "XN", "cp", "Spre"]
+                   "celsius_t", "failure", "icell", "XN", "cp", "Spre", "PK"]
 GRID_FIELDS = ["Mg", "PXg", "FXg"]
 
 

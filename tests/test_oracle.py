@@ -211,3 +211,28 @@ def test_contact_blocks_exchange_and_rebound(oracle_mod, shape, fricfa, normbody
     # cell's mass, and those below the cut-off keep back their internal force
     p1 = (mass * o.download("VXp")).sum(axis=1)
     assert np.all(np.abs(p1 - p0) <= 5e-4 * np.abs(mass * o.download("VXp")).sum()), (p0, p1)
+
+
+@pytest.mark.parametrize("shape", ["mpm", "gimp", "bimp", "sgmp"])
+def test_tlmpm_invariants(oracle_mod, shape):
+    """Total Lagrangian form: the grid mass is mapped once (GridMassInitial)
+    and stays the same over the run; the volume is det(I + Fp) VOL0; the mean
+    stress is the trace of the Cauchy stress P F^T / J built from the stored
+    first Piola-Kirchhoff stress; the beam sags under its weight."""
+    from mpm3d_gb300 import decks
+    o = oracle_mod.Oracle(deck_text=decks.soft_beam(shape=shape, scheme="musl", tlmpm=True), libm="project")
+    z0 = o.download("Xp")[2].copy()
+    o.run(5)
+    mg5 = o.download("Mg").copy()
+    o.run(25)
+    assert np.array_equal(o.download("Mg"), mg5)
+    F = o.download("Fp").reshape(3, 3, -1) + np.eye(3)[:, :, None]
+    J = np.linalg.det(np.moveaxis(F, 2, 0))
+    vol0 = o.download("VOL0")
+    assert np.allclose(o.download("VOL"), J * vol0, rtol=1e-13, atol=0)
+    K = o.download("PK")  # xx yy zz yz xz xy zy zx yx
+    P = np.array([[K[0], K[5], K[4]], [K[8], K[1], K[3]], [K[7], K[6], K[2]]])
+    tr = np.einsum("ijp,ijp->p", P, F)  # tr(P F^T)
+    sm = o.download("SM")
+    assert np.allclose(sm, tr / (3 * J), rtol=1e-9, atol=1e-9 * np.abs(sm).max())
+    assert (o.download("Xp")[2] - z0).min() < 0
