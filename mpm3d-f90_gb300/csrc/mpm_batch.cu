@@ -67,6 +67,7 @@ struct HostScene {
   SceneState st{};
   int drdamp = 0;
   int smooth = 0;  // 'smoo': Spre is computed when read
+  DetoPoints deto{};  // detonation points (lighting time of explosives)
 };
 
 }  // namespace mpm
@@ -76,15 +77,38 @@ namespace {
 // particle state of a newly admitted scene from its uploaded inputs:
 // scr = vol, sig_y, cp, lt (FP64, np each); the rest of the state starts at
 // zero, the temperature at 293 (Particle.f90:131)
-__global__ void kb_init_scene(BState s, int scene, int body0, const double* scr) {
+// Initial (DataIn.f90:1211-1267) for the particles of a new scene, from
+// their mass and position and their body's material: volume, yield stress,
+// internal energy, sound speed, lighting time (sqrt(...)/D a default-REAL
+// temporary); bodies of material type 12 keep zeros
+__global__ void kb_init_scene(BState s, int scene, int body0, DetoPoints deto) {
   const Scene& sc = s.scenes[scene];
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sc.np) return;
-  const long long NP = s.NP, np = sc.np, i = sc.p0 + k;
-  s.vol[i] = (float)scr[k];
-  s.sig_y[i] = (float)scr[np + k];
-  s.cp[i] = (float)scr[2 * np + k];
-  s.lt[i] = (float)scr[3 * np + k];
+  const long long NP = s.NP, i = sc.p0 + k;
+  const DevMaterial& m = s.mats[s.bodies[body0 + s.body[i]].mat];
+  double vol = 0.0, sig_y = 0.0, ie = 0.0, cp = 0.0, lt = 0.0;
+  if (m.mat_type != 12) {
+    vol = s.mass[i] / m.density;
+    sig_y = m.yield0;
+    ie = m.cEos[9] * vol;
+    if (m.mat_type == 1 || m.mat_type == 11) {
+      const double E = m.young, nu = m.poisson, ro = m.density;
+      cp = sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
+    }
+    if (m.mat_type == 9) cp = m.wavespd;
+    lt = (double)10e6f;
+    for (int j = 0; j < deto.n; ++j) {
+      const double dx = s.x[i] - deto.p[j][0], dy = s.x[NP + i] - deto.p[j][1], dz = s.x[2 * NP + i] - deto.p[j][2];
+      const float t = (float)(sqrt(dx * dx + dy * dy + dz * dz) / m.D);
+      if ((double)t < lt) lt = (double)t;
+    }
+  }
+  s.vol[i] = (float)vol;
+  s.sig_y[i] = (float)sig_y;
+  s.ie[i] = ie;
+  s.cp[i] = (float)cp;
+  s.lt[i] = (float)lt;
   s.celsius[i] = 293.0f;
   s.sm[i] = 0.f;
   s.evol[i] = 0.f;
@@ -165,6 +189,8 @@ struct mpm_batch {
   size_t arena_cap = 0;
   char* spare = nullptr;
   size_t spare_cap = 0;
+  double* dl = nullptr;  // particle-field download buffer (all components of one field)
+  size_t dl_cap = 0;
   long long bytes = 0;
   int* d_target = nullptr;
   void* cub_tmp = nullptr;
@@ -285,17 +311,8 @@ int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
     BCK(upd(s.fxp + a * NP + p0, fxp + a * np, np));
   }
   BCK(upd(s.mass + p0, h->in_mass(), np));
-  BCK(upd(s.ie + p0, h->su.ie.data(), np));
-  // FP64 set-up values through the force staging scratch (idle outside a
-  // step; 9 floats per particle hold 4 doubles), converted and completed by
-  // one kernel
-  double* scr = reinterpret_cast<double*>(s.fs);
-  BCK(upd(scr, h->su.vol.data(), np));
-  BCK(upd(scr + np, h->su.sig_y.data(), np));
-  BCK(upd(scr + 2 * np, h->su.cp.data(), np));
-  BCK(upd(scr + 3 * np, h->su.lt.data(), np));
   BCK(cudaMemcpyAsync(s.body + p0, h->body_local.data(), sizeof(uint16_t) * np, cudaMemcpyHostToDevice, st));
-  kb_init_scene<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(s, h->index, h->body0, scr);
+  kb_init_scene<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(s, h->index, h->body0, h->deto);
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(st));  // the host arrays may go away after this
   return MPM_OK;
@@ -807,6 +824,7 @@ void mpm_batch_destroy(mpm_batch* b) {
   if (b->g_items_d) cudaFree(b->g_items_d);
   if (b->g_out_d) cudaFree(b->g_out_d);
   if (b->g_done) cudaEventDestroy(b->g_done);
+  if (b->dl) cudaFree(b->dl);
   for (auto& kv : b->by_id) delete kv.second;
   prof_free(&b->prof);
   cudaStreamDestroy(b->stream);
@@ -1018,20 +1036,25 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
     if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "centre field: %s", cudaGetErrorString(e));
     return MPM_OK;
   }
-  // particle fields: un-permuted on the device into a per-step scratch (the
-  // force staging array, idle between steps), one copy per component
+  // particle fields: every component un-permuted on the device by one kernel
+  // into a download buffer kept by the batch, then one copy
   const bool ok = field >= MPM_P_XP && field <= MPM_P_FAILURE && field != MPM_P_XN && field != MPM_P_XXN &&
                   field != MPM_P_VOL0 && nc > 0 && (field != MPM_P_FP || b->any_uvfp);
   if (!ok) return berr(b, MPM_ERR_ARG, "field %d is not available for batched scenes", field);
-  double* scratch = reinterpret_cast<double*>(s.fs);  // 9 floats per particle >= one double per particle
   (void)NP;
   (void)p0;
-  for (int a = 0; a < nc; ++a) {
-    kb_unpermute<<<gridn(np, 256), 256, 0, b->stream>>>(s, h->index, field, a, scratch);
-    BCK(cudaGetLastError());
-    BCK(cudaMemcpyAsync(out + a * np, scratch, sizeof(double) * np, cudaMemcpyDeviceToHost, b->stream));
-    BCK(cudaStreamSynchronize(b->stream));
+  const size_t bytes = sizeof(double) * (size_t)np * (size_t)nc;
+  if (bytes > b->dl_cap) {
+    if (b->dl) cudaFree(b->dl);
+    b->dl = nullptr;
+    b->dl_cap = 0;
+    BCK(cudaMalloc(&b->dl, bytes));
+    b->dl_cap = bytes;
   }
+  kb_unpermute<<<gridn(np * nc, 256), 256, 0, b->stream>>>(s, h->index, field, nc, b->dl);
+  BCK(cudaGetLastError());
+  BCK(cudaMemcpyAsync(out, b->dl, bytes, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
   return MPM_OK;
 }
 
@@ -1147,13 +1170,16 @@ HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code
     return nullptr;
   }
   HostScene* h = new HostScene();
-  int r = scene_setup(d, h->su);
+  int r = scene_setup(d, h->su, false);  // per-particle set-up values are derived on the device
   if (r) {
     *code = r;
     err = h->su.err;
     delete h;
     return nullptr;
   }
+  h->deto.n = d->n_deto;
+  for (int j = 0; j < d->n_deto; ++j)
+    for (int a = 0; a < 3; ++a) h->deto.p[j][a] = d->deto[j][a];
   h->steps = steps > 0 ? steps : 0x7fffffff;
   h->np = d->nb_particle;
   h->nn = h->su.g.nn;

@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "mpm_deck.h"
 #include "mpm_gpu_internal.cuh"
 
 namespace mpm {
@@ -107,6 +108,12 @@ struct BState {
 };
 
 constexpr int kChunk = 2048;  // particles per reduction chunk
+
+// detonation points of a scene (the lighting time of explosive particles)
+struct DetoPoints {
+  int n;
+  double p[MPM_MAX_DETO][3];
+};
 
 // SGMP centre accumulator channels (cacc[channel * NC + cell]): mass and
 // momentum (CenterNode Mg / PXg, the MUSL momentum reuses the momentum

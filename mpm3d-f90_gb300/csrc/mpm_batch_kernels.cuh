@@ -1473,11 +1473,13 @@ __global__ void kb_gather(BState b, int scene, const GatherItem* it, int n, doub
 }
 
 // one component of a particle field of a scene in deck order (downloads)
-__global__ void kb_unpermute(BState b, int scene, int field, int comp, double* dst) {
+__global__ void kb_unpermute(BState b, int scene, int field, int ncomp, double* dst) {
   const Scene& sc = b.scenes[scene];
-  const long long k = btid();
-  if (k >= sc.np) return;
-  dst[k] = field_value(b, field, comp, b.inv[sc.p0 + k]);
+  const long long t = btid();
+  if (t >= sc.np * ncomp) return;
+  const int a = (int)(t / sc.np);
+  const long long k = t - (long long)a * sc.np;
+  dst[t] = field_value(b, field, a, b.inv[sc.p0 + k]);  // component-major, input order
 }
 
 // ----------------------------------------------------- stress smoothing

@@ -21,7 +21,7 @@ static int fail(SceneSetup& out, int code, const char* fmt, ...) {
   return code;
 }
 
-int scene_setup(const mpm_deck* d, SceneSetup& out) {
+int scene_setup(const mpm_deck* d, SceneSetup& out, bool particle_fields) {
   Geometry& g = out.g;
   std::vector<double>& host_vol = out.vol;
   std::vector<double>& sig_y = out.sig_y;
@@ -64,21 +64,27 @@ int scene_setup(const mpm_deck* d, SceneSetup& out) {
   }
   // Initial: per-particle volume, yield stress, internal energy, sound speed,
   // lighting time (sqrt(...)/D is a default-REAL temporary)
-  host_vol.assign(np, 0.0); sig_y.assign(np, 0.0); ie.assign(np, 0.0); cp.assign(np, 0.0);
-  lt.assign(np, 0.0);
-  for (int b = 0; b < d->nb_body; ++b) {
+  if (particle_fields) {
+    host_vol.assign(np, 0.0); sig_y.assign(np, 0.0); ie.assign(np, 0.0); cp.assign(np, 0.0);
+    lt.assign(np, 0.0);
+  }
+  for (int b = 0; b < (particle_fields ? d->nb_body : 0); ++b) {
     const DevMaterial& m = out.mats[out.bodies[b].mat];
     if (m.mat_type == 12) continue;
+    // the body's material constants (the same for each of its particles)
+    double cp_b = 0.0;
+    if (m.mat_type == 1 || m.mat_type == 11) {
+      double E = m.young, nu = m.poisson, ro = m.density;
+      cp_b = std::sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
+    }
+    if (m.mat_type == 9) cp_b = m.wavespd;
+    const double e0 = d->mats[out.bodies[b].mat].cEos[9];
     for (long long p = d->bodies[b].par_begin; p < d->bodies[b].par_end; ++p) {
       double vol = d->mass[p] / m.density;
       host_vol[p] = vol;
       sig_y[p] = m.yield0;
-      ie[p] = d->mats[out.bodies[b].mat].cEos[9] * vol;
-      if (m.mat_type == 1 || m.mat_type == 11) {
-        double E = m.young, nu = m.poisson, ro = m.density;
-        cp[p] = std::sqrt(E * (1 - nu) / (1 + nu) / (1 - 2 * nu) / ro);
-      }
-      if (m.mat_type == 9) cp[p] = m.wavespd;
+      ie[p] = e0 * vol;
+      cp[p] = cp_b;
       double ltv = (double)10e6f;
       for (int j = 0; j < d->n_deto; ++j) {
         double dx = d->xp[p] - d->deto[j][0];

@@ -18,8 +18,10 @@ struct SceneSetup {
   std::string err;
 };
 
-// Initial + SetGridData of a deck; returns an mpm_status.
-int scene_setup(const mpm_deck* d, SceneSetup& out);
+// Initial + SetGridData of a deck; returns an mpm_status. particle_fields:
+// also fill the per-particle vol / sig_y / ie / cp / lt (the batched engine
+// derives them on the device instead).
+int scene_setup(const mpm_deck* d, SceneSetup& out, bool particle_fields = true);
 // SetDT: the first time step of a material set.
 double set_dt(const std::vector<DevMaterial>& mats, double dcell, double dtscale);
 

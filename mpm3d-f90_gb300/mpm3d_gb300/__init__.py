@@ -344,7 +344,7 @@ class MpmStep:
             n = self.nb_cell
         else:
             n = self.nb_particle
-        out = np.zeros(ncomp * n)
+        out = np.empty(ncomp * n)
         self._check(library().mpm_download(self._h, FIELDS[field], _dptr(out)))
         return out.reshape(ncomp, n) if ncomp > 1 else out
 
@@ -498,7 +498,7 @@ class Batch:
             raise MpmError(1, "cell fields are read per scene through MpmStep")
         else:
             n = int(sc["nb_particle"])
-        out = np.zeros(ncomp * n)
+        out = np.empty(ncomp * n)
         self._check(library().mpm_batch_scene_download(self._h, int(scene), FIELDS[field], _dptr(out)))
         return out.reshape(ncomp, n) if ncomp > 1 else out
 
@@ -710,7 +710,7 @@ class Server:
     def field(self, ticket: int, name: str) -> np.ndarray:
         ncomp = COMPONENTS.get(name, 1)
         n = self._np[ticket]
-        out = np.zeros(ncomp * n)
+        out = np.empty(ncomp * n)
         self._check(library().mpm_serve_field(self._h, int(ticket), FIELDS[name], _dptr(out)))
         return out.reshape(ncomp, n) if ncomp > 1 else out
 
