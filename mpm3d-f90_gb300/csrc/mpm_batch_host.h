@@ -10,6 +10,9 @@
 
 namespace mpm {
 
+// touch every page of a host buffer once (before a device-to-host copy into it)
+void prefault_host(void* p, size_t bytes);
+
 struct HostScene;
 // stage a scene from a deck on any thread (nullptr + code/err on failure);
 // with borrow the deck's particle arrays are used in place, so the scene must

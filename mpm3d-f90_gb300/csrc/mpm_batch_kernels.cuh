@@ -99,25 +99,30 @@ __device__ __forceinline__ long long dual_cell(const Scene& sc, const double x[3
 // contiguous, which the transfers rely on for locality (and the SGMP centre
 // gathers for their particle ranges).
 __global__ void kb_keys(BState b) {
-  long long i = btid();
-  if (i >= b.NP) return;
-  const long long NP = b.NP;
-  const Scene& sc = b.scenes[b.scene[i]];
-  double x[3] = {b.x[i], b.x[NP + i], b.x[2 * NP + i]};
-  long long c = -1;
-  if (sc.shape == 3) {
-    c = dual_cell(sc, x);
-  } else {
-    int cc[3];
-    float off[3];
-    if (cell_of(sc, x, cc, off)) {
-      c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+  const long long i = btid();
+  long long key = -1;
+  if (i < b.NP) {
+    const long long NP = b.NP;
+    const Scene& sc = b.scenes[b.scene[i]];
+    double x[3] = {b.x[i], b.x[NP + i], b.x[2 * NP + i]};
+    long long c = -1;
+    if (sc.shape == 3) {
+      c = dual_cell(sc, x);
+    } else {
+      int cc[3];
+      float off[3];
+      if (cell_of(sc, x, cc, off)) {
+        c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+      }
     }
+    key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
+    b.key[i] = (unsigned)key;
+    b.val[i] = (int)i;
   }
-  long long key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
-  b.key[i] = (unsigned)key;
-  b.val[i] = (int)i;
-  atomicAdd(&b.seg[key], 1);
+  // per-key counts: the particles arrive sorted by the last step's keys, so
+  // a warp's lanes mostly share a few keys -- one atomic per key and warp
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&b.seg[key], __popc(grp));
 }
 
 // ---------------------------------------------------- permutation + derived
@@ -1442,7 +1447,7 @@ __device__ __forceinline__ double field_value(const BState& b, int field, long l
   double v = 0.0;
   switch (field) {
     case MPM_P_XP: v = b.x[c * NP + i]; break;
-    case MPM_P_XX: v = b.xx[c * NP + i]; break;
+    case MPM_P_XX: v = b.x[c * NP + i]; break;  // XX equals Xp between steps
     case MPM_P_VXP: v = b.v[c * NP + i]; break;
     case MPM_P_FXP: v = b.fxp[c * NP + i]; break;
     case MPM_P_VOL: v = b.vol[i]; break;

@@ -894,6 +894,7 @@ int mpm_download(mpm_ctx* c, int field, double* out) {
     return MPM_OK;
   }
   if (elem == 8) {
+    mpm::prefault_host(out, (size_t)n * 8);
     CK(cudaMemcpy(out, p, (size_t)n * 8, cudaMemcpyDeviceToHost));
     return MPM_OK;
   }
