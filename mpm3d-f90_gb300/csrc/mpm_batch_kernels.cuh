@@ -252,31 +252,29 @@ __device__ __forceinline__ float q_scale(int sh) { return __int_as_float((sh + 1
 __device__ __forceinline__ long long quant(float c, float scale) { return __float2ll_rn(c * scale); }
 __device__ __forceinline__ double q_unit(int sh) { return __longlong_as_double((long long)(1023 - sh) << 52); }  // 2^-sh
 
-// influence nodes of a particle along one direction: node = cell + t[k],
-// weight w[k] and derivative d[k] (per cell) -- NShape / the cpGIMP quarter
-// rule of FindInflNode with NShape_GIMP / NShape_Bspline
-__device__ __forceinline__ int dim_nodes(int shape, float off, int t[4], float w[4], float d[4]) {
+// influence nodes of a particle along one direction: node = cell + t0 + k
+// for k < the returned count (at most 3), weight w[k] and derivative d[k]
+// (per cell) -- NShape / the cpGIMP quarter rule of FindInflNode with
+// NShape_GIMP / NShape_Bspline. Fixed-size arrays with constant indices (the
+// gathers unroll their node loops) stay in registers.
+__device__ __forceinline__ int dim_nodes(int shape, float off, int& t0, float w[3], float d[3]) {
   if (shape == 0) {
-    t[0] = 0;
-    t[1] = 1;
+    t0 = 0;
     lin1(0, off, w[0], d[0]);
     lin1(1, off, w[1], d[1]);
+    w[2] = d[2] = 0.f;
     return 2;
   }
   if (shape == 2) {
-    for (int k = 0; k < 3; ++k) {
-      t[k] = k - 1;
-      bsp1(k - 1, off, w[k], d[k]);
-    }
+    t0 = -1;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) bsp1(k - 1, off, w[k], d[k]);
     return 3;
   }
-  int n = 0;
-  if (off < 0.25f) t[n++] = -1;
-  t[n++] = 0;
-  t[n++] = 1;
-  if (off > 0.75f) t[n++] = 2;
-  for (int k = 0; k < n; ++k) gimp1((float)(-t[k]) + off, w[k], d[k]);
-  return n;
+  t0 = off < 0.25f ? -1 : 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gimp1((float)(-(t0 + k)) + off, w[k], d[k]);
+  return 2 + (off < 0.25f) + (off > 0.75f);
 }
 
 // permutation kernel; it also takes the mass and momentum bounds of the
@@ -757,8 +755,9 @@ __host__ __device__ constexpr bool stress_specialised(int mat_type) {
   return mat_type == 1 || mat_type == 9 || mat_type == 10 || mat_type == 11;
 }
 
+// (the common types capped at 64 registers: four 256-thread blocks per SM)
 template <int MT>
-__global__ void kb_stress(BState b, int usf_pass, int filter) {
+__global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_pass, int filter) {
   using P = PMixed;
   using R = float;
   long long i = btid();
@@ -806,14 +805,18 @@ __global__ void kb_stress(BState b, int usf_pass, int filter) {
     c[1] = rem / sc.NCx;
     c[0] = rem - c[1] * sc.NCx;
     float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-    int t[3][4], nt[3];
-    float wd[3][4], dd[3][4];
-    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], wd[a], dd[a]);
+    int t0[3], nt[3];
+    float wd[3][3], dd[3][3];
+    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t0[a], wd[a], dd[a]);
     const float idc = (float)sc.idcell;
-    for (int az = 0; az < nt[2]; ++az)
-      for (int ay = 0; ay < nt[1]; ++ay)
-        for (int ax = 0; ax < nt[0]; ++ax) {
-          int j[3] = {c[0] + t[0][ax], c[1] + t[1][ay], c[2] + t[2][az]};
+#pragma unroll
+    for (int az = 0; az < 3; ++az)
+#pragma unroll
+      for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          if (ax >= nt[0] || ay >= nt[1] || az >= nt[2]) continue;
+          int j[3] = {c[0] + t0[0] + ax, c[1] + t0[1] + ay, c[2] + t0[2] + az};
           if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
           long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
           const float4 v4 = b.nvel[n];  // zero below the cut-off mass
@@ -1239,13 +1242,17 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
     c[1] = rem / sc.NCx;
     c[0] = rem - c[1] * sc.NCx;
     float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
-    int t[3][4], nt[3];
-    float wd[3][4], dd[3][4];
-    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t[a], wd[a], dd[a]);
-    for (int az = 0; az < nt[2]; ++az)
-      for (int ay = 0; ay < nt[1]; ++ay)
-        for (int ax = 0; ax < nt[0]; ++ax) {
-          int j[3] = {c[0] + t[0][ax], c[1] + t[1][ay], c[2] + t[2][az]};
+    int t0[3], nt[3];
+    float wd[3][3], dd[3][3];
+    for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t0[a], wd[a], dd[a]);
+#pragma unroll
+    for (int az = 0; az < 3; ++az)
+#pragma unroll
+      for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          if (ax >= nt[0] || ay >= nt[1] || az >= nt[2]) continue;
+          int j[3] = {c[0] + t0[0] + ax, c[1] + t0[1] + ay, c[2] + t0[2] + az};
           if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
           long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
           const float w = wd[0][ax] * wd[1][ay] * wd[2][az];
