@@ -350,7 +350,8 @@ __device__ __forceinline__ long long sg_corner_cell(const Scene& sc, int dx, int
 // (CenterNode Mg, PXg), 1 momentum with the updated velocities, 2 external
 // force then internal force (Cfext, Cfint).
 template <int MODE>
-__device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int s, int i0, int i1, int d, float* ws) {
+__device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int i0, int i1, int dx, int dy, int dz,
+                                                float sA, float sB, float* ws) {
   constexpr int NQ = ScatterShape<MODE>::NQ;      // staged quantities, then 8 corner weights, then 1
   constexpr int SROW = ScatterShape<MODE>::SROW;
   constexpr int NV = MODE == 0 ? 4 : (MODE == 1 ? 3 : 9);  // channels
@@ -358,9 +359,6 @@ __device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int 
   constexpr int CH0 = MODE == 2 ? CQ_FE : (MODE == 1 ? CQ_P : CQ_M);  // first accumulator channel
   static_assert(NQ + 9 <= SROW, "staging row");
   const int lane = threadIdx.x & 31;
-  if (d < 0) return;  // the scene's off-grid bucket
-  const int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
-  const SceneState& st = b.sst[s];
   const long long NP = b.NP, NC = b.NC;
   // per slot: corner weight index, the staged factors (mass / force value,
   // velocity or the 1 at the end of the row), scale, target cell
@@ -377,11 +375,11 @@ __device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int 
     if (MODE == 2) {
       f0[k] = ch[k] < 3 ? 6 + ch[k] : ch[k] - 3;  // fs: sigma*vol xx..xz (0..5), external force (6..8)
       f1[k] = NQ + 8;
-      scale[k] = q_scale(q_shift(sc, st.qmax[Q_FORCE]));
+      scale[k] = sA;
     } else {
       f0[k] = 0;  // mass
       f1[k] = MODE == 0 ? (ch[k] == 0 ? NQ + 8 : ch[k]) : ch[k] + 1;
-      scale[k] = q_scale(q_shift(sc, st.qmax[MODE == 1 ? Q_MOM_MUSL : (ch[k] == 0 ? Q_MASS : Q_MOM)]));
+      scale[k] = MODE == 0 && ch[k] != 0 ? sB : sA;
     }
     acc[k] = 0.f;
   }
@@ -423,36 +421,26 @@ __device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int 
   }
 }
 
-// the scatter of one cell's particles [i0, i1) of a linear / GIMP /
-// B-spline scene by one warp; ws = the warp's shared workspace
-template <int MODE>
-__device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int s, int i0, int i1, int cl, float* ws) {
+// the scatter of one cell's particles [i0, i1) of a linear (SH 0), GIMP (1)
+// or B-spline (2) scene by one warp; cell (c0, c1, c2); sA, sB: the
+// quantisation scales (mode 0: mass, momentum; else the mode's one);
+// ws = the warp's shared workspace
+template <int MODE, int SH>
+__device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int i0, int i1, int c0, int c1, int c2,
+                                                 float sA, float sB, float* ws) {
   using SS = ScatterShape<MODE>;
   constexpr int NV = SS::NV, NQ = SS::NQ, PC = SS::PC, NPQ = SS::NPQ;
   float* pq = ws;                                   // [PC][16][NPQ], 16-byte aligned
   float2* tab = reinterpret_cast<float2*>(ws + SS::PQ);  // [PC][3][4]
   float* val = ws + SS::PQ + SS::TAB;               // [NQ][PC]
   const int lane = threadIdx.x & 31;
-  int c[3];
-  c[2] = cl / sc.NCxy;
-  {
-    const int rem = cl - c[2] * sc.NCxy;
-    c[1] = rem / sc.NCx;
-    c[0] = rem - c[1] * sc.NCx;
-  }
+  const int c[3] = {c0, c1, c2};
   const long long NP = b.NP;
-  const SceneState& st = b.sst[s];
   float scale[NV];
-  if (MODE == 0) {
-    scale[0] = q_scale(q_shift(sc, st.qmax[Q_MASS]));
-    scale[1] = scale[2] = scale[3] = q_scale(q_shift(sc, st.qmax[Q_MOM]));
-  } else {
-    const float sv = q_scale(q_shift(sc, st.qmax[MODE == 1 ? Q_MOM_MUSL : Q_FORCE]));
-    for (int v = 0; v < NV; ++v) scale[v] = sv;
-  }
-  const int shape = sc.shape;
-  const int tlo = shape == 0 ? 0 : -1, nt = shape == 1 ? 4 : (shape == 2 ? 3 : 2);
-  const int ns = nt * nt * nt;
+  scale[0] = sA;
+  for (int v = 1; v < NV; ++v) scale[v] = MODE == 0 ? sB : sA;
+  constexpr int tlo = SH == 0 ? 0 : -1, nt = SH == 1 ? 4 : (SH == 2 ? 3 : 2);
+  constexpr int ns = nt * nt * nt;
   // this lane's slots (box offsets sx, sy, sz)
   int sx[2], syz[2], sy[2], sz[2];
   bool use[2];
@@ -485,8 +473,8 @@ __device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int
       if (p >= cnt || t >= nt) continue;
       const float off = b.off[a * NP + base + p];
       float w, d;
-      if (shape == 0) lin1(tlo + t, off, w, d);
-      else if (shape == 2) bsp1(tlo + t, off, w, d);
+      if (SH == 0) lin1(tlo + t, off, w, d);
+      else if (SH == 2) bsp1(tlo + t, off, w, d);
       else gimp1((float)(-(tlo + t)) + off, w, d);
       tab[(p * 3 + a) * 4 + t] = make_float2(w, d * idc);
     }
@@ -559,12 +547,17 @@ __device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int
 
 // the scatter of one sort key by one warp: particles [i0, i1) of scene s in
 // cell cl (dual cell d for SGMP)
+// (cell or dual cell (x, y, z), scales sA, sB as box_scatter_cell)
 template <int MODE>
-__device__ __forceinline__ void scatter_cell(BState& b, int i0, int i1, int s, int cl, int d, float* ws) {
+__device__ __forceinline__ void scatter_cell(BState& b, int i0, int i1, int s, int x, int y, int z, float sA,
+                                             float sB, float* ws) {
   const Scene& sc = b.scenes[s];
-  if (!scene_live(b, s) || (MODE == 1 && !sc.musl)) return;
-  if (sc.shape == 3) sg_scatter_cell<MODE>(b, sc, s, i0, i1, d, ws);
-  else if (cl >= 0) box_scatter_cell<MODE>(b, sc, s, i0, i1, cl, ws);  // cl < 0: the off-grid bucket
+  switch (sc.shape) {
+    case 0: box_scatter_cell<MODE, 0>(b, sc, i0, i1, x, y, z, sA, sB, ws); break;
+    case 1: box_scatter_cell<MODE, 1>(b, sc, i0, i1, x, y, z, sA, sB, ws); break;
+    case 2: box_scatter_cell<MODE, 2>(b, sc, i0, i1, x, y, z, sA, sB, ws); break;
+    default: sg_scatter_cell<MODE>(b, sc, i0, i1, x, y, z, sA, sB, ws);
+  }
 }
 
 // Persistent scatter over the occupied sort keys (the run-length encoding of
@@ -583,21 +576,40 @@ __global__ void __launch_bounds__(32 * kCellWarps, 4) kb_cell_scatter(BState b, 
   const long long nw = (long long)gridDim.x * kCellWarps;
   const int chunk = (int)max(1LL, min(32LL, (n + nw - 1) / nw));
   for (long long r0 = ((long long)blockIdx.x * kCellWarps + warp) * chunk; r0 < n; r0 += nw * chunk) {
-    int i0 = 0, i1 = 0, s = -1, cl = -1, d = -1;
+    // lane j: key r0 + j -- its particles, scene, cell (dual cell for SGMP)
+    // coordinates and quantisation scales (s = -1: nothing to scatter)
+    int i0 = 0, i1 = 0, s = -1, x = 0, y = 0, z = 0;
+    float sA = 0.f, sB = 0.f;
     if (lane < chunk && r0 + lane < n) {
       key_range(b, runs[r0 + lane], i0, i1);
       if (i0 < i1) {
         s = b.scene[i0];
-        cl = b.cell[i0];
-        d = b.dual[i0];
+        const Scene& sc = b.scenes[s];
+        const int sg = sc.shape == 3;
+        const int cl = sg ? b.dual[i0] : b.cell[i0];
+        if (cl < 0 || !scene_live(b, s) || (MODE == 1 && !sc.musl)) {
+          s = -1;  // the scene's off-grid bucket, or no transfer this step
+        } else {
+          const int nx = sg ? sc.CNCx : sc.NCx, nxy = sg ? sc.CNCxy : sc.NCxy;
+          z = cl / nxy;
+          const int rem = cl - z * nxy;
+          y = rem / nx;
+          x = rem - y * nx;
+          const SceneState& st = b.sst[s];
+          sA = q_scale(q_shift(sc, st.qmax[MODE == 0 ? Q_MASS : (MODE == 1 ? Q_MOM_MUSL : Q_FORCE)]));
+          sB = MODE == 0 ? q_scale(q_shift(sc, st.qmax[Q_MOM])) : sA;
+        }
       }
     }
     const int m = (int)min((long long)chunk, n - r0);
     for (int j = 0; j < m; ++j) {
       const int sj = __shfl_sync(0xffffffffu, s, j);
+      if (sj < 0) continue;
       const int a = __shfl_sync(0xffffffffu, i0, j), e = __shfl_sync(0xffffffffu, i1, j);
-      const int cj = __shfl_sync(0xffffffffu, cl, j), dj = __shfl_sync(0xffffffffu, d, j);
-      if (sj >= 0) scatter_cell<MODE>(b, a, e, sj, cj, dj, reinterpret_cast<float*>(wsp[warp]));
+      const int xj = __shfl_sync(0xffffffffu, x, j), yj = __shfl_sync(0xffffffffu, y, j),
+                zj = __shfl_sync(0xffffffffu, z, j);
+      const float aj = __shfl_sync(0xffffffffu, sA, j), bj = __shfl_sync(0xffffffffu, sB, j);
+      scatter_cell<MODE>(b, a, e, sj, xj, yj, zj, aj, bj, reinterpret_cast<float*>(wsp[warp]));
     }
   }
 }
