@@ -193,6 +193,7 @@ struct mpm_batch {
   size_t spare_cap = 0;
   double* dl = nullptr;  // particle-field download buffer (all components of one field)
   size_t dl_cap = 0;
+  bool inv_stale = false;  // steps ran since the inverse permutation was last built
   long long bytes = 0;
   int* d_target = nullptr;
   void* cub_tmp = nullptr;
@@ -752,9 +753,10 @@ int commit(mpm_batch* b) {
       int r = upload_scene_particles(b, h, A);
       if (r) return r;
     }
-  // inverse permutation of the new layout (the permutation kernel keeps it
-  // up to date from the first step on)
+  // inverse permutation of the new layout (rebuilt before the first
+  // download or probe after later steps)
   kb_inverse<<<gridn(NP, 256), 256, 0, st>>>(A);
+  b->inv_stale = false;
   // calcEnergy of the new scenes (MPM3D.f90:42)
   kb_reduce_chunks<<<(unsigned)NR, 256, 0, st>>>(A);
   kb_reduce_scenes<<<(unsigned)A.nscene, 256, 0, st>>>(A, 1);
@@ -886,6 +888,7 @@ int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph) {
   int r = ensure_committed(b);
   if (r) return r;
   if (b->order.empty()) return MPM_OK;
+  b->inv_stale = true;
   BProfScope ps(b);
   if (!use_graph) {
     for (int i = 0; i < nsteps; ++i)
@@ -1004,6 +1007,16 @@ static int scene_spre(mpm_batch* b, HostScene* h, double* out) {
   return MPM_OK;
 }
 
+namespace {
+// the inverse permutation (deck index -> position) of the current order,
+// rebuilt on the batch stream when steps ran since it was last built
+void fresh_inverse(mpm_batch* b) {
+  if (!b->inv_stale) return;
+  kb_inverse<<<gridn(b->A.NP, 256), 256, 0, b->stream>>>(b->A);
+  b->inv_stale = false;
+}
+}  // namespace
+
 int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
   if (!b || !out) return MPM_ERR_ARG;
   int r = ensure_committed(b);
@@ -1053,6 +1066,7 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
     BCK(cudaMalloc(&b->dl, bytes));
     b->dl_cap = bytes;
   }
+  fresh_inverse(b);
   kb_unpermute<<<gridn(np * nc, 256), 256, 0, b->stream>>>(s, h->index, field, nc, b->dl);
   BCK(cudaGetLastError());
   mpm::prefault_host(out, bytes);  // while the kernel runs
@@ -1089,6 +1103,7 @@ int mpm_batch_scene_gather_async(mpm_batch* b, int id, int n, const int64_t* par
   b->g_n = n;
   if (n > 0) {
     BCK(cudaMemcpyAsync(b->g_items_d, b->g_items_h, sizeof(GatherItem) * n, cudaMemcpyHostToDevice, b->stream));
+    fresh_inverse(b);
     kb_gather<<<(n + 127) / 128, 128, 0, b->stream>>>(b->A, h->index, b->g_items_d, n, b->g_out_d);
     BCK(cudaGetLastError());
     BCK(cudaMemcpyAsync(b->g_out_h, b->g_out_d, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));

@@ -74,7 +74,7 @@ struct BState {
   uint8_t* failure;
   uint16_t *body, *scene;
   int* orig;
-  int* inv;  // position of a particle by scene p0 + deck index (written by the permutation)
+  int* inv;  // position of a particle by scene p0 + deck index (rebuilt before downloads and probes)
   // per-step derived (written by the permutation)
   int *cell, *dual, *inode;
   float *off, *xxn, *xn;

@@ -129,39 +129,60 @@ __global__ void kb_keys(BState b) {
 // dst[i] = src[perm[i]] for every persistent particle field, then the per-step
 // derived data of the particle at its new position (ParticleInitial,
 // update_step.f90:408-453, in FP32 form).
-__device__ __forceinline__ void permute_one(const BState& src, BState& dst, long long i) {
+// returns the particle's scene; mass and velocity for the transfer bounds
+__device__ __forceinline__ int permute_one(const BState& src, BState& dst, long long i, double& m_out,
+                                           double (&v_out)[3]) {
+  // every value is loaded before the first store: the stores could alias the
+  // loads as far as the compiler knows, so interleaving them would serialise
+  // one memory round trip per field
   const long long NP = src.NP;
   const long long j = src.perm[i];
+  double x[3], v[3], f[3];
   for (int a = 0; a < 3; ++a) {
-    dst.x[a * NP + i] = src.x[a * NP + j];
-    dst.v[a * NP + i] = src.v[a * NP + j];
-    dst.fxp[a * NP + i] = src.fxp[a * NP + j];
+    x[a] = src.x[a * NP + j];
+    v[a] = src.v[a * NP + j];
+    f[a] = src.fxp[a * NP + j];
   }
-  dst.mass[i] = src.mass[j];
-  dst.ie[i] = src.ie[j];
-  dst.vol[i] = src.vol[j];
-  dst.evol[i] = src.evol[j];
-  dst.sig_y[i] = src.sig_y[j];
-  dst.sm[i] = src.sm[j];
-  dst.seqv[i] = src.seqv[j];
-  for (int a = 0; a < 6; ++a) dst.sd[a * NP + i] = src.sd[a * NP + j];
-  if (src.any_uvfp)
-    for (int a = 0; a < 9; ++a) dst.fp[a * NP + i] = src.fp[a * NP + j];
-  dst.epeff[i] = src.epeff[j];
-  dst.celsius[i] = src.celsius[j];
-  dst.dmg[i] = src.dmg[j];
-  dst.lt[i] = src.lt[j];
-  dst.cp[i] = src.cp[j];
-  dst.q[i] = src.q[j];
-  dst.failure[i] = src.failure[j];
-  dst.body[i] = src.body[j];
+  const double mass = src.mass[j], ie = src.ie[j];
+  const float vol = src.vol[j], evol = src.evol[j], sig_y = src.sig_y[j], sm = src.sm[j], seqv = src.seqv[j];
+  float sd[6];
+  for (int a = 0; a < 6; ++a) sd[a] = src.sd[a * NP + j];
+  const float epeff = src.epeff[j], celsius = src.celsius[j], dmg = src.dmg[j], lt = src.lt[j], cp = src.cp[j],
+              q = src.q[j];
+  const uint8_t failure = src.failure[j];
+  const uint16_t body = src.body[j];
   const int s = src.scene[j];
+  const int orig = src.orig[j];
+  if (src.any_uvfp) {
+    float fp[9];
+    for (int a = 0; a < 9; ++a) fp[a] = src.fp[a * NP + j];
+    for (int a = 0; a < 9; ++a) dst.fp[a * NP + i] = fp[a];
+  }
+  for (int a = 0; a < 3; ++a) {
+    dst.x[a * NP + i] = x[a];
+    dst.v[a * NP + i] = v[a];
+    dst.fxp[a * NP + i] = f[a];
+  }
+  dst.mass[i] = mass;
+  dst.ie[i] = ie;
+  dst.vol[i] = vol;
+  dst.evol[i] = evol;
+  dst.sig_y[i] = sig_y;
+  dst.sm[i] = sm;
+  dst.seqv[i] = seqv;
+  for (int a = 0; a < 6; ++a) dst.sd[a * NP + i] = sd[a];
+  dst.epeff[i] = epeff;
+  dst.celsius[i] = celsius;
+  dst.dmg[i] = dmg;
+  dst.lt[i] = lt;
+  dst.cp[i] = cp;
+  dst.q[i] = q;
+  dst.failure[i] = failure;
+  dst.body[i] = body;
   dst.scene[i] = (uint16_t)s;
-  dst.orig[i] = src.orig[j];
-  dst.inv[src.scenes[s].p0 + src.orig[j]] = (int)i;
+  dst.orig[i] = orig;
   // derived
   const Scene& sc = src.scenes[s];
-  double x[3] = {dst.x[i], dst.x[NP + i], dst.x[2 * NP + i]};
   int cc[3];
   float off[3];
   const bool in = cell_of(sc, x, cc, off);
@@ -184,6 +205,9 @@ __device__ __forceinline__ void permute_one(const BState& src, BState& dst, long
       dst.xn[a * NP + i] = off[a] * 2.f - 1.f;
     }
   }
+  m_out = mass;
+  for (int a = 0; a < 3; ++a) v_out[a] = v[a];
+  return s;
 }
 
 // ------------------------------------------- deterministic P2G scatter
@@ -284,13 +308,11 @@ __global__ void kb_permute(BState src, BState dst) {
   int s = -1;
   float bm = 0.f, bv = 0.f;
   if (i < src.NP) {
-    permute_one(src, dst, i);
-    s = dst.scene[i];
+    double m, v[3];
+    s = permute_one(src, dst, i, m, v);
     if (scene_live(dst, s)) {
-      const long long NP = dst.NP;
-      bm = (float)dst.mass[i];
-      bv = bm * fmaxf(fabsf((float)dst.v[i]), fmaxf(fabsf((float)dst.v[NP + i]), fabsf((float)dst.v[2 * NP + i]))) *
-           1.0001f;
+      bm = (float)m;
+      bv = bm * fmaxf(fabsf((float)v[0]), fmaxf(fabsf((float)v[1]), fabsf((float)v[2]))) * 1.0001f;
     } else {
       s = -1;
     }
