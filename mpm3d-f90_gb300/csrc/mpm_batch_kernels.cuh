@@ -1032,20 +1032,19 @@ __device__ __forceinline__ float force_prep_one(BState& b, long long i) {
     const DevBody& bd = b.bodies[b.body[i]];
     for (int a = 0; a < 3; ++a) f[a] = f[a] + m * (float)bd.gravp[a];
   }
-  float vol = b.vol[i];
-  float smq = b.sm[i] - b.q[i];
-  b.fs[i] = (smq + b.sd[i]) * vol;
-  b.fs[NP + i] = (smq + b.sd[NP + i]) * vol;
-  b.fs[2 * NP + i] = (smq + b.sd[2 * NP + i]) * vol;
-  b.fs[3 * NP + i] = b.sd[3 * NP + i] * vol;
-  b.fs[4 * NP + i] = b.sd[4 * NP + i] * vol;
-  b.fs[5 * NP + i] = b.sd[5 * NP + i] * vol;
+  // (every value loaded before the first store, which could alias them)
+  const float vol = b.vol[i];
+  const float smq = b.sm[i] - b.q[i];
+  float sd[6];
+  for (int a = 0; a < 6; ++a) sd[a] = b.sd[a * NP + i];
+  float fs[6];
+  for (int a = 0; a < 3; ++a) fs[a] = (smq + sd[a]) * vol;
+  for (int a = 3; a < 6; ++a) fs[a] = sd[a] * vol;
+  for (int a = 0; a < 6; ++a) b.fs[a * NP + i] = fs[a];
   for (int a = 0; a < 3; ++a) b.fs[(6 + a) * NP + i] = f[a];
   // bound of one contribution: node force (|grad N| <= 1 / h per component,
   // N <= 1), or for SGMP one centre-node channel (N times a staged value)
-  const float* fs = b.fs;
-  const float sig = fabsf(fs[i]) + fabsf(fs[NP + i]) + fabsf(fs[2 * NP + i]) +
-                    2.f * (fabsf(fs[3 * NP + i]) + fabsf(fs[4 * NP + i]) + fabsf(fs[5 * NP + i]));
+  const float sig = fabsf(fs[0]) + fabsf(fs[1]) + fabsf(fs[2]) + 2.f * (fabsf(fs[3]) + fabsf(fs[4]) + fabsf(fs[5]));
   const float gscale = sc.shape == 3 ? 1.f : (float)sc.idcell;
   return (sig * gscale + fabsf(f[0]) + fabsf(f[1]) + fabsf(f[2])) * 1.0001f;
 }
@@ -1235,7 +1234,7 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
   if (!scene_live(b, s)) return -1.f;
   const Scene& sc = b.scenes[s];
   const SceneState& st = b.sst[s];
-  const long long NP = b.NP, NN = b.NN;
+  const long long NP = b.NP;
   float v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
   if (sc.shape == 3) {
     int d = b.dual[i];
@@ -1300,18 +1299,19 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
         }
   }
   const double dt = st.dt;
+  double pv[3];
   for (int a = 0; a < 3; ++a) {
-    double xx = b.x[a * NP + i] + (double)v[a] * dt;
+    const double xx = b.x[a * NP + i] + (double)v[a] * dt;
     b.xx[a * NP + i] = xx;
-    double vv = b.v[a * NP + i];
-    vv = st.istep == 1 ? vv + (double)acc[a] * dt * 0.5 : vv + (double)acc[a] * dt;
-    b.v[a * NP + i] = vv;
+    const double vv = b.v[a * NP + i];
+    pv[a] = st.istep == 1 ? vv + (double)acc[a] * dt * 0.5 : vv + (double)acc[a] * dt;
+    b.v[a * NP + i] = pv[a];
     if (sc.usf) b.x[a * NP + i] = xx;
   }
   if (!sc.musl) return -1.f;
   // bound of GridMomentumMUSL's contributions with the updated velocity
   const float m = (float)b.mass[i];
-  return m * fmaxf(fabsf((float)b.v[i]), fmaxf(fabsf((float)b.v[NP + i]), fabsf((float)b.v[2 * NP + i]))) * 1.0001f;
+  return m * fmaxf(fabsf((float)pv[0]), fmaxf(fabsf((float)pv[1]), fabsf((float)pv[2]))) * 1.0001f;
 }
 
 __global__ void kb_position(BState b) {
