@@ -205,6 +205,7 @@ struct mpm_batch {
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
   int scatter_blocks = 9728;  // scatter grid cap (64 blocks per SM; warps stride over the occupied cells)
+  int scatter_wave = 4864;    // scatter warps resident at once (4 blocks per SM)
   Profiler prof;
   // particle value gather (curve output)
   GatherItem *g_items_h = nullptr, *g_items_d = nullptr;
@@ -367,7 +368,7 @@ int enqueue_step(mpm_batch* b) {
     prof_end(K_SG_CLEAR, st);
   }
   prof_begin(K_SCATTER_MASS, st);
-  kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
+  kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
   prof_end(K_SCATTER_MASS, st);
   prof_begin(K_P2G_MASS, st);
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
@@ -406,7 +407,7 @@ int enqueue_step(mpm_batch* b) {
   kb_force_prep<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_FORCE_PREP, st);
   prof_begin(K_SCATTER_FORCE, st);
-  kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
+  kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
   prof_end(K_SCATTER_FORCE, st);
   prof_begin(K_P2G_FORCE, st);
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
@@ -421,7 +422,7 @@ int enqueue_step(mpm_batch* b) {
   prof_end(K_POSITION, st);
   if (b->any_musl) {
     prof_begin(K_SCATTER_MOM, st);
-    kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns);
+    kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
     prof_end(K_SCATTER_MOM, st);
     prof_begin(K_P2G_MOM, st);
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
@@ -807,7 +808,10 @@ int mpm_batch_create(int device, mpm_batch** out) {
   cudaGetDevice(&b->device);
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) == cudaSuccess && sms > 0)
+  {
     b->scatter_blocks = 64 * sms;
+    b->scatter_wave = 4 * sms * kCellWarps;
+  }
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete b;
     return MPM_ERR_CUDA;

@@ -489,46 +489,56 @@ __device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int
       if (MODE == 2) val[e] = b.fs[q * NP + i];
       else val[e] = q == 0 ? (float)b.mass[i] : (float)b.v[(q - 1) * NP + i];
     }
-    // 1-D weights and derivatives (per unit length) at offsets tlo + t
-    for (int e = lane; e < 12 * PC; e += 32) {
-      const int p = e % PC, r = e / PC, a = r >> 2, t = r & 3;
-      if (p >= cnt || t >= nt) continue;
-      const float off = b.off[a * NP + base + p];
-      float w, d;
-      if (SH == 0) lin1(tlo + t, off, w, d);
-      else if (SH == 2) bsp1(tlo + t, off, w, d);
-      else gimp1((float)(-(tlo + t)) + off, w, d);
-      tab[(p * 3 + a) * 4 + t] = make_float2(w, d * idc);
+    // 1-D weights and derivatives (per unit length) at offsets tlo + t: lane
+    // a * PC + p takes direction a of particle p
+    if (lane < 3 * PC) {
+      const int p = lane % PC, a = lane / PC;
+      if (p < cnt) {
+        const float off = b.off[a * NP + base + p];
+#pragma unroll
+        for (int t = 0; t < nt; ++t) {
+          float w, d;
+          if (SH == 0) lin1(tlo + t, off, w, d);
+          else if (SH == 2) bsp1(tlo + t, off, w, d);
+          else gimp1((float)(-(tlo + t)) + off, w, d);
+          tab[(p * 3 + a) * 4 + t] = make_float2(w, d * idc);
+        }
+      }
     }
     __syncwarp();
-    // y-z factors per particle and (ty, tz)
-    for (int e = lane; e < 16 * PC; e += 32) {
-      const int p = e >> 4, yz = e & 15, ty = yz & 3, tz = yz >> 2;
-      if (p >= cnt || ty >= nt || tz >= nt) continue;
-      const float2 y = tab[(p * 3 + 1) * 4 + ty], z = tab[(p * 3 + 2) * 4 + tz];
-      const float A = y.x * z.x;
-      float* o = pq + (p * 16 + yz) * NPQ;
-      if (MODE == 2) {
-        const float B = y.y * z.x, C = y.x * z.y;
-        const float sxx = val[0 * PC + p], syy = val[1 * PC + p], szz = val[2 * PC + p];
-        const float sxy = val[3 * PC + p], syz_ = val[4 * PC + p], sxz = val[5 * PC + p];
-        o[0] = -sxx * A;
-        o[1] = val[6 * PC + p] * A - sxy * B - sxz * C;
-        o[2] = -sxy * A;
-        o[3] = val[7 * PC + p] * A - syy * B - syz_ * C;
-        o[4] = -sxz * A;
-        o[5] = val[8 * PC + p] * A - syz_ * B - szz * C;
-      } else {
-        const float M = val[p] * A;
-        if (MODE == 0) {
-          o[0] = M;
-          o[1] = M * val[PC + p];
-          o[2] = M * val[2 * PC + p];
-          o[3] = M * val[3 * PC + p];
-        } else {
-          o[0] = M * val[PC + p];
-          o[1] = M * val[2 * PC + p];
-          o[2] = M * val[3 * PC + p];
+    // y-z factors per particle and (ty, tz): lane l takes particle l / 4 and
+    // the pairs yz = l % 4 + 4 u (ty = yz % nt, tz = yz / nt), stored at
+    // [p][tz * 4 + ty]
+    {
+      static_assert(PC == 8, "four lanes per staged particle");
+      constexpr int NYZ = nt * nt, NU = (NYZ + 3) / 4;
+      const int p = lane >> 2;
+      if (p < cnt) {
+        float pv[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) pv[q] = val[q * PC + p];
+#pragma unroll
+        for (int u = 0; u < NU; ++u) {
+          const int yz = (lane & 3) + 4 * u;
+          if (yz < NYZ) {
+            const int ty = yz % nt, tz = yz / nt;
+            const float2 y = tab[(p * 3 + 1) * 4 + ty], z = tab[(p * 3 + 2) * 4 + tz];
+            const float A = y.x * z.x;
+            float* o = pq + (p * 16 + tz * 4 + ty) * NPQ;
+            if (MODE == 2) {
+              const float B = y.y * z.x, C = y.x * z.y;
+              const float sxx = pv[0], syy = pv[1], szz = pv[2], sxy = pv[3], syz_ = pv[4], sxz = pv[5];
+              reinterpret_cast<float2*>(o)[0] = make_float2(-sxx * A, pv[6] * A - sxy * B - sxz * C);
+              reinterpret_cast<float2*>(o)[1] = make_float2(-sxy * A, pv[7] * A - syy * B - syz_ * C);
+              reinterpret_cast<float2*>(o)[2] = make_float2(-sxz * A, pv[8] * A - syz_ * B - szz * C);
+            } else {
+              const float M = pv[0] * A;
+              if (MODE == 0)
+                *reinterpret_cast<float4*>(o) = make_float4(M, M * pv[1], M * pv[2], M * pv[3]);
+              else
+                *reinterpret_cast<float4*>(o) = make_float4(M * pv[1], M * pv[2], M * pv[3], 0.f);
+            }
+          }
         }
       }
     }
@@ -582,21 +592,24 @@ __device__ __forceinline__ void scatter_cell(BState& b, int i0, int i1, int s, i
   }
 }
 
-// Persistent scatter over the occupied sort keys (the run-length encoding of
-// the sorted keys, count on the device): a fixed grid, each warp taking
-// chunks of up to 32 consecutive keys (fewer when there are few keys, so
-// that every warp has work). The lanes first load one key's particle range,
-// scene and cell each -- one round of dependent loads for the whole chunk
-// instead of one per key -- then the warp scatters the keys in turn. Empty
-// cells cost nothing, which matters on sparse grids (a granular column fills
-// a fifth of its grid).
+// Scatter over the occupied sort keys (the run-length encoding of the sorted
+// keys, count on the device): a fixed grid, each warp taking chunks of up to
+// 32 consecutive keys. The lanes first load one key's particle range, scene
+// and cell each -- one round of dependent loads for the whole chunk instead
+// of one per key -- then the warp scatters the keys in turn. The chunk is
+// sized for the warps of one resident wave (wave), so that the chain of
+// metadata loads is paid once per up to 32 keys while every resident warp
+// has work; warps of later blocks past the keys exit at once. Empty cells
+// cost nothing, which matters on sparse grids (a granular column fills a
+// fifth of its grid).
 template <int MODE>
-__global__ void __launch_bounds__(32 * kCellWarps, 4) kb_cell_scatter(BState b, const unsigned* runs, const int* nruns) {
+__global__ void __launch_bounds__(32 * kCellWarps, 4)
+    kb_cell_scatter(BState b, const unsigned* runs, const int* nruns, int wave) {
   __shared__ float4 wsp[kCellWarps][ScatterShape<MODE>::WS / 4];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long n = *nruns;
   const long long nw = (long long)gridDim.x * kCellWarps;
-  const int chunk = (int)max(1LL, min(32LL, (n + nw - 1) / nw));
+  const int chunk = (int)max(1LL, min(32LL, (n + wave - 1) / wave));
   for (long long r0 = ((long long)blockIdx.x * kCellWarps + warp) * chunk; r0 < n; r0 += nw * chunk) {
     // lane j: key r0 + j -- its particles, scene, cell (dual cell for SGMP)
     // coordinates and quantisation scales (s = -1: nothing to scatter)
