@@ -1327,7 +1327,10 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
   return m * fmaxf(fabsf((float)pv[0]), fmaxf(fabsf((float)pv[1]), fabsf((float)pv[2]))) * 1.0001f;
 }
 
-__global__ void kb_position(BState b) {
+// (capped at 40 registers: six 256-thread blocks per SM hide the node
+// gathers' latency better than fewer blocks with more registers; a pblock of
+// 512 still launches)
+__global__ void __launch_bounds__(512, 3) kb_position(BState b) {
   const long long i = btid();
   float bound = -1.f;
   if (i < b.NP) bound = position_one(b, i);
