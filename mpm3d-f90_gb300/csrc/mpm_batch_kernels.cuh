@@ -855,37 +855,53 @@ __global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_p
     int t0[3], nt[3];
     float wd[3][3], dd[3][3];
     for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t0[a], wd[a], dd[a]);
-    const float idc = (float)sc.idcell;
+    // velocity gradient L[a][k] = sum_n v_a(n) dN_n / dx_k; the shape is a
+    // tensor product, so the node velocities are first summed along x with
+    // the x weights and x derivatives, and each (y, z) row then adds its two
+    // sums times the y-z factors: 6 multiply-adds per node instead of the 24
+    // of forming de, vort and deFp node by node
+    float L[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll
     for (int az = 0; az < 3; ++az)
 #pragma unroll
-      for (int ay = 0; ay < 3; ++ay)
+      for (int ay = 0; ay < 3; ++ay) {
+        if (ay >= nt[1] || az >= nt[2]) continue;
+        const int jy = c[1] + t0[1] + ay, jz = c[2] + t0[2] + az;
+        if (jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
+        const long long row = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx;
+        float S[3] = {0, 0, 0}, D[3] = {0, 0, 0};
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
-          if (ax >= nt[0] || ay >= nt[1] || az >= nt[2]) continue;
-          int j[3] = {c[0] + t0[0] + ax, c[1] + t0[1] + ay, c[2] + t0[2] + az};
-          if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
-          long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
-          const float4 v4 = b.nvel[n];  // zero below the cut-off mass
-          float dx = dd[0][ax] * wd[1][ay] * wd[2][az] * idc;
-          float dy = wd[0][ax] * dd[1][ay] * wd[2][az] * idc;
-          float dz = wd[0][ax] * wd[1][ay] * dd[2][az] * idc;
-          float v[3] = {v4.x, v4.y, v4.z};
-          de[0] += dx * v[0];
-          de[1] += dy * v[1];
-          de[2] += dz * v[2];
-          de[3] += dy * v[2] + dz * v[1];
-          de[4] += dz * v[0] + dx * v[2];
-          de[5] += dx * v[1] + dy * v[0];
-          vort[0] += dy * v[2] - dz * v[1];
-          vort[1] += dz * v[0] - dx * v[2];
-          vort[2] += dx * v[1] - dy * v[0];
-          for (int a = 0; a < 3; ++a) {
-            deFp[a][0] += dx * v[a];
-            deFp[a][1] += dy * v[a];
-            deFp[a][2] += dz * v[a];
-          }
+          if (ax >= nt[0]) continue;
+          const int jx = c[0] + t0[0] + ax;
+          if (jx < 0 || jx >= sc.NGx) continue;
+          const float4 v4 = b.nvel[row + jx];  // zero below the cut-off mass
+          S[0] += wd[0][ax] * v4.x;
+          S[1] += wd[0][ax] * v4.y;
+          S[2] += wd[0][ax] * v4.z;
+          D[0] += dd[0][ax] * v4.x;
+          D[1] += dd[0][ax] * v4.y;
+          D[2] += dd[0][ax] * v4.z;
         }
+        const float fx = wd[1][ay] * wd[2][az], fy = dd[1][ay] * wd[2][az], fz = wd[1][ay] * dd[2][az];
+        for (int a = 0; a < 3; ++a) {
+          L[a][0] += D[a] * fx;
+          L[a][1] += S[a] * fy;
+          L[a][2] += S[a] * fz;
+        }
+      }
+    const float idc = (float)sc.idcell;
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < 3; ++k) deFp[a][k] = L[a][k] * idc;
+    de[0] = deFp[0][0];
+    de[1] = deFp[1][1];
+    de[2] = deFp[2][2];
+    de[3] = deFp[2][1] + deFp[1][2];
+    de[4] = deFp[0][2] + deFp[2][0];
+    de[5] = deFp[1][0] + deFp[0][1];
+    vort[0] = deFp[2][1] - deFp[1][2];
+    vort[1] = deFp[0][2] - deFp[2][0];
+    vort[2] = deFp[1][0] - deFp[0][1];
   }
   const SceneState& st = b.sst[s];
   const R DT = (R)st.dt;
