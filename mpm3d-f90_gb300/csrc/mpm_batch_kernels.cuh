@@ -1307,18 +1307,24 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
     int t0[3], nt[3];
     float wd[3][3], dd[3][3];
     for (int a = 0; a < 3; ++a) nt[a] = dim_nodes(sc.shape, off[a], t0[a], wd[a], dd[a]);
+    // node rows along x: bounds and row index once per row, one multiply
+    // per node for its weight (the shape is a tensor product)
 #pragma unroll
     for (int az = 0; az < 3; ++az)
 #pragma unroll
-      for (int ay = 0; ay < 3; ++ay)
+      for (int ay = 0; ay < 3; ++ay) {
+        if (ay >= nt[1] || az >= nt[2]) continue;
+        const int jy = c[1] + t0[1] + ay, jz = c[2] + t0[2] + az;
+        if (jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
+        const long long row = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx;
+        const float wyz = wd[1][ay] * wd[2][az];
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
-          if (ax >= nt[0] || ay >= nt[1] || az >= nt[2]) continue;
-          int j[3] = {c[0] + t0[0] + ax, c[1] + t0[1] + ay, c[2] + t0[2] + az};
-          if (j[0] < 0 || j[0] >= sc.NGx || j[1] < 0 || j[1] >= sc.NGy || j[2] < 0 || j[2] >= sc.NGz) continue;
-          long long n = sc.n0 + ((long long)j[2] * sc.NGy + j[1]) * sc.NGx + j[0];
-          const float w = wd[0][ax] * wd[1][ay] * wd[2][az];
-          const float4 vn = b.nvel[n], an = b.nacc[n];  // zero below the cut-off mass
+          if (ax >= nt[0]) continue;
+          const int jx = c[0] + t0[0] + ax;
+          if (jx < 0 || jx >= sc.NGx) continue;
+          const float4 vn = b.nvel[row + jx], an = b.nacc[row + jx];  // zero below the cut-off mass
+          const float w = wd[0][ax] * wyz;
           v[0] += w * vn.x;
           v[1] += w * vn.y;
           v[2] += w * vn.z;
@@ -1326,6 +1332,7 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
           acc[1] += w * an.y;
           acc[2] += w * an.z;
         }
+      }
   }
   const double dt = st.dt;
   double pv[3];
