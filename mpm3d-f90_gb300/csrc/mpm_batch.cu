@@ -200,6 +200,7 @@ struct mpm_batch {
   size_t cub_bytes = 0;
   int key_bits = 1;
   int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
+  int any_prep = 0;  // scenes whose force input is not staged by their stress kernel (USL / MUSL, Johnson-Cook)
   unsigned stress_types = 0;  // stress instantiations to launch: bit MT per specialised type, bit 0 for the rest
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
@@ -287,12 +288,14 @@ long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bo
 
 void layout_flags(mpm_batch* b) {
   b->any_sgmp = b->any_nonsgmp = b->any_usf = b->any_later = b->any_musl = b->any_jc = b->any_dr = b->any_uvfp = 0;
+  b->any_prep = 0;
   for (HostScene* h : b->order) {
     const Geometry& g = h->su.g;
     if (g.shape == 3) b->any_sgmp = 1; else b->any_nonsgmp = 1;
     if (g.usf) b->any_usf = 1; else b->any_later = 1;
     if (g.musl) b->any_musl = 1;
     if (g.has_jc) b->any_jc = 1;
+    if (!g.usf || g.has_jc) b->any_prep = 1;
     if (g.uvfp) b->any_uvfp = 1;
     if (h->drdamp) b->any_dr = 1;
   }
@@ -403,9 +406,11 @@ int enqueue_step(mpm_batch* b) {
   };
   int r;
   if (b->any_usf && (r = stress(1))) return r;
-  prof_begin(K_FORCE_PREP, st);
-  kb_force_prep<<<gridn(s.NP, pb), pb, 0, st>>>(s);
-  prof_end(K_FORCE_PREP, st);
+  if (b->any_prep) {  // (USF scenes without Johnson-Cook tails are staged by their stress kernel)
+    prof_begin(K_FORCE_PREP, st);
+    kb_force_prep<<<gridn(s.NP, pb), pb, 0, st>>>(s);
+    prof_end(K_FORCE_PREP, st);
+  }
   prof_begin(K_SCATTER_FORCE, st);
   kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
   prof_end(K_SCATTER_FORCE, st);

@@ -803,22 +803,26 @@ __host__ __device__ constexpr bool stress_specialised(int mat_type) {
 }
 
 // (the common types capped at 64 registers: four 256-thread blocks per SM)
+__device__ __forceinline__ float force_stage(BState& b, const Scene& sc, const SceneState& st, long long i, float vol,
+                                             float smq, const float (&sd)[6]);
+
+// stages the particle's force input when its scene's USF pass has its final
+// stress here (no Johnson-Cook tail after this kernel) and returns that
+// contribution's bound; -1 otherwise
 template <int MT>
-__global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_pass, int filter) {
+__device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass, int filter) {
   using P = PMixed;
   using R = float;
-  long long i = btid();
-  if (i >= b.NP) return;
   const int s = b.scene[i];
-  if (!scene_live(b, s)) return;
+  if (!scene_live(b, s)) return -1.f;
   const Scene& sc = b.scenes[s];
-  if (sc.usf != usf_pass) return;
+  if (sc.usf != usf_pass) return -1.f;
   const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
   // every particle goes through the instantiation of its own material type
   // (or the general one), whatever else shares the batch: the compiled FP32
   // arithmetic, and so the result, is the same alone or in a batch (filter
   // 0: the batch needs this instantiation only)
-  if (filter && (MT ? mt.mat_type != MT : stress_specialised(mt.mat_type))) return;
+  if (filter && (MT ? mt.mat_type != MT : stress_specialised(mt.mat_type))) return -1.f;
   const long long NP = b.NP;
   const long long o = sc.p0 + b.orig[i];  // position in the reference processing order
   if (sc.has_jc) {
@@ -828,7 +832,7 @@ __global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_p
   R de[6] = {0, 0, 0, 0, 0, 0}, vort[3] = {0, 0, 0}, deFp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   if (sc.shape == 3) {
     int d = b.dual[i];
-    if (d < 0) return;
+    if (d < 0) return -1.f;
     int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
     float xx[3] = {b.xxn[i], b.xxn[NP + i], b.xxn[2 * NP + i]};
     for (int k = 0; k < 8; ++k) {
@@ -845,7 +849,7 @@ __global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_p
     }
   } else {
     const int cl = b.cell[i];
-    if (cl < 0) return;
+    if (cl < 0) return -1.f;
     int c[3];
     c[2] = cl / sc.NCxy;
     int rem = cl - c[2] * sc.NCxy;
@@ -969,6 +973,19 @@ __global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_p
   if (!isfinite(ps.sm) || !isfinite(ps.ie)) atomicOr(&b.sst[s].status, (unsigned)ST_NONFINITE);
   if (!sc.usf)
     for (int a = 0; a < 3; ++a) b.x[a * NP + i] = b.xx[a * NP + i];
+  // GridMomentumUpdate follows a USF stress update directly: stage its
+  // force input from the registers (the stress state is final unless a
+  // Johnson-Cook tail still runs)
+  if (!sc.usf || sc.has_jc) return -1.f;
+  return force_stage(b, sc, st, i, ps.vol, ps.sm - ps.q, ps.sd);
+}
+
+template <int MT>
+__global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_pass, int filter) {
+  const long long i = btid();
+  float bound = -1.f;
+  if (i < b.NP) bound = stress_one<MT>(b, i, usf_pass, filter);
+  if (usf_pass) block_scene_max<1>(b, bound >= 0.f ? (int)b.scene[i] : -1, {Q_FORCE}, {fmaxf(bound, 0.f)});
 }
 
 // Johnson-Cook tails waiting for the depeff carried from the previous particle
@@ -1042,12 +1059,10 @@ __global__ void kb_depeff_carry(BState b, int usf_pass) {
 
 // ------------------------------------------------------------ force input
 // external force (QuLo ramp, Damp, gravity; update_step.f90:889-903) and
-// sigma * vol, staged per particle in FP32 for the force gather
-__device__ __forceinline__ float force_prep_one(BState& b, long long i) {
-  const int s = b.scene[i];
-  if (!scene_live(b, s)) return -1.f;
-  const Scene& sc = b.scenes[s];
-  const SceneState& st = b.sst[s];
+// sigma * vol, staged per particle in FP32 for the force gather, from the
+// particle's volume, SM - q and SD; returns the bound of one contribution
+__device__ __forceinline__ float force_stage(BState& b, const Scene& sc, const SceneState& st, long long i, float vol,
+                                             float smq, const float (&sd)[6]) {
   const long long NP = b.NP;
   // external force in FP32 (the staged force is FP32): load ramp, mass
   // damping, gravity
@@ -1061,11 +1076,6 @@ __device__ __forceinline__ float force_prep_one(BState& b, long long i) {
     const DevBody& bd = b.bodies[b.body[i]];
     for (int a = 0; a < 3; ++a) f[a] = f[a] + m * (float)bd.gravp[a];
   }
-  // (every value loaded before the first store, which could alias them)
-  const float vol = b.vol[i];
-  const float smq = b.sm[i] - b.q[i];
-  float sd[6];
-  for (int a = 0; a < 6; ++a) sd[a] = b.sd[a * NP + i];
   float fs[6];
   for (int a = 0; a < 3; ++a) fs[a] = (smq + sd[a]) * vol;
   for (int a = 3; a < 6; ++a) fs[a] = sd[a] * vol;
@@ -1076,6 +1086,23 @@ __device__ __forceinline__ float force_prep_one(BState& b, long long i) {
   const float sig = fabsf(fs[0]) + fabsf(fs[1]) + fabsf(fs[2]) + 2.f * (fabsf(fs[3]) + fabsf(fs[4]) + fabsf(fs[5]));
   const float gscale = sc.shape == 3 ? 1.f : (float)sc.idcell;
   return (sig * gscale + fabsf(f[0]) + fabsf(f[1]) + fabsf(f[2])) * 1.0001f;
+}
+
+// the staging of the particles whose stress kernel did not stage them (scenes
+// updating stresses after the position update, and Johnson-Cook scenes, whose
+// tails run after the stress kernel)
+__device__ __forceinline__ float force_prep_one(BState& b, long long i) {
+  const int s = b.scene[i];
+  if (!scene_live(b, s)) return -1.f;
+  const Scene& sc = b.scenes[s];
+  if (sc.usf && !sc.has_jc) return -1.f;
+  const long long NP = b.NP;
+  // (every value loaded before the first store, which could alias them)
+  const float vol = b.vol[i];
+  const float smq = b.sm[i] - b.q[i];
+  float sd[6];
+  for (int a = 0; a < 6; ++a) sd[a] = b.sd[a * NP + i];
+  return force_stage(b, sc, b.sst[s], i, vol, smq, sd);
 }
 
 __global__ void kb_force_prep(BState b) {
