@@ -160,8 +160,11 @@ def kernel_bytes(kernel: str, np_: int, nn_active: float, usf: bool = True) -> f
         return nn_active * (32 + 24 + 24 + 24)
     if kernel == "stress_update":
         # read x, vol, SM, SD, q, ie, cp, epeff, sig_y; write vol, SM, SD, q,
-        # ie, seqv, epeff; node velocity read once
-        return np_ * (24 + 4 * 13 + 8) + np_ * (4 * 11 + 8) + nn_active * 12
+        # ie, seqv, epeff; node velocity read once; under USF the kernel also
+        # stages the force input (read mass, point loads; write sigma * vol
+        # and the external force)
+        staged = np_ * (8 + 24 + 36) if usf else 0
+        return np_ * (24 + 4 * 13 + 8) + np_ * (4 * 11 + 8) + nn_active * 12 + staged
     if kernel == "g2p_position":
         # read x, v; write x, v; node velocity and acceleration read once
         return np_ * 96 + nn_active * 24
