@@ -218,12 +218,15 @@ int mpm_gather_wait(mpm_ctx* ctx, double* out);
 int mpm_gather(mpm_ctx* ctx, int n, const int64_t* particle, const int* field, const int* component, double* out);
 
 /* ------------------------------------------------------ restart snapshot */
-/* No counterpart in the reference: a full-precision restart file of an FP64
+/* No counterpart in the reference: a full-precision restart file of a
  * context -- the device images of every persistent particle field and the
  * step's scalars (istep, time, DT, energies, the carried Johnson-Cook
- * depeff). Loading it into a context created from the same deck and
- * precision continues the run bit-identically. MPM_ERR_UNSUPPORTED for the
- * mixed form; MPM_ERR_STATE for a file of another deck size / precision. */
+ * depeff). For the mixed form the particle fields are stored at their
+ * stored widths (FP64 positions, velocities, mass, energy; FP32 stress
+ * state) in the batched engine's storage order, with the scene's step state.
+ * Loading it into a context created from the same deck and precision
+ * continues the run bit-identically. MPM_ERR_STATE for a file of another
+ * deck or precision. */
 int mpm_snapshot_save(mpm_ctx* ctx, const char* path);
 int mpm_snapshot_load(mpm_ctx* ctx, const char* path);
 

@@ -1040,6 +1040,8 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
     const double* src = field == MPM_G_MG ? s.mg : (field == MPM_G_PX ? s.px : s.fx);
     for (int a = 0; a < nc; ++a)
       BCK(cudaMemcpy(out + a * h->nn, src + a * s.NN + h->n0, sizeof(double) * h->nn, cudaMemcpyDeviceToHost));
+    if (field == MPM_G_MG)  // -0 marks a massless node with a force or momentum (the idle test)
+      for (long long k = 0; k < h->nn; ++k) out[k] = out[k] + 0.0;
     return MPM_OK;
   }
   if (field == MPM_P_SPRE) return scene_spre(b, h, out);
@@ -1083,6 +1085,86 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
   BCK(cudaStreamSynchronize(b->stream));
   return MPM_OK;
 }
+
+}  // extern "C"
+
+namespace {
+// the particle arrays a restart of a scene needs (the rest is rebuilt by the
+// next step): device array, bytes per element, components
+struct RestartField {
+  void* p;
+  size_t elem;
+  int nc;
+};
+std::vector<RestartField> restart_fields(const BState& s, bool uvfp) {
+  std::vector<RestartField> f = {{s.x, 8, 3},     {s.v, 8, 3},       {s.fxp, 8, 3},   {s.mass, 8, 1},  {s.ie, 8, 1},
+                                 {s.vol, 4, 1},   {s.evol, 4, 1},    {s.sig_y, 4, 1}, {s.sm, 4, 1},    {s.seqv, 4, 1},
+                                 {s.sd, 4, 6},    {s.epeff, 4, 1},   {s.celsius, 4, 1}, {s.dmg, 4, 1}, {s.lt, 4, 1},
+                                 {s.cp, 4, 1},    {s.q, 4, 1},       {s.failure, 1, 1}, {s.body, 2, 1}, {s.scene, 2, 1},
+                                 {s.orig, 4, 1}};
+  if (uvfp) f.push_back({s.fp, 4, 9});
+  return f;
+}
+}  // namespace
+
+namespace mpm {
+
+int mpm_batch_scene_snapshot(mpm_batch* b, int id, std::vector<unsigned char>& out) {
+  if (!b) return MPM_ERR_ARG;
+  int r = ensure_committed(b);
+  if (r) return r;
+  HostScene* h = find(b, id);
+  if (!h) return berr(b, MPM_ERR_ARG, "no scene %d", id);
+  BCK(cudaStreamSynchronize(b->stream));
+  const BState& s = b->A;
+  const long long NP = s.NP, np = h->np, p0 = h->p0;
+  SceneState st;
+  BCK(cudaMemcpy(&st, s.sst + h->index, sizeof st, cudaMemcpyDeviceToHost));
+  out.assign(reinterpret_cast<const unsigned char*>(&st), reinterpret_cast<const unsigned char*>(&st) + sizeof st);
+  for (const RestartField& f : restart_fields(s, h->su.g.uvfp != 0))
+    for (int a = 0; a < f.nc; ++a) {
+      const size_t at = out.size(), n = (size_t)np * f.elem;
+      out.resize(at + n);
+      BCK(cudaMemcpy(out.data() + at, static_cast<const char*>(f.p) + ((size_t)a * NP + p0) * f.elem, n,
+                     cudaMemcpyDeviceToHost));
+    }
+  return MPM_OK;
+}
+
+int mpm_batch_scene_restore(mpm_batch* b, int id, const unsigned char* in, size_t bytes) {
+  if (!b || !in) return MPM_ERR_ARG;
+  int r = ensure_committed(b);
+  if (r) return r;
+  HostScene* h = find(b, id);
+  if (!h) return berr(b, MPM_ERR_ARG, "no scene %d", id);
+  BCK(cudaStreamSynchronize(b->stream));
+  const BState& s = b->A;
+  const long long NP = s.NP, np = h->np, p0 = h->p0;
+  const std::vector<RestartField> fields = restart_fields(s, h->su.g.uvfp != 0);
+  size_t need = sizeof(SceneState);
+  for (const RestartField& f : fields) need += (size_t)f.nc * (size_t)np * f.elem;
+  if (bytes != need) return berr(b, MPM_ERR_STATE, "restart image of %zu bytes, the scene needs %zu", bytes, need);
+  SceneState st;
+  memcpy(&st, in, sizeof st);
+  size_t at = sizeof st;
+  for (const RestartField& f : fields)
+    for (int a = 0; a < f.nc; ++a) {
+      const size_t n = (size_t)np * f.elem;
+      BCK(cudaMemcpy(static_cast<char*>(f.p) + ((size_t)a * NP + p0) * f.elem, in + at, n, cudaMemcpyHostToDevice));
+      at += n;
+    }
+  // positions and their copy agree at the end of every step
+  for (int a = 0; a < 3; ++a)
+    BCK(cudaMemcpy(s.xx + a * NP + p0, s.x + a * NP + p0, sizeof(double) * np, cudaMemcpyDeviceToDevice));
+  BCK(cudaMemcpy(s.sst + h->index, &st, sizeof st, cudaMemcpyHostToDevice));
+  h->st = st;
+  b->inv_stale = true;
+  return MPM_OK;
+}
+
+}  // namespace mpm
+
+extern "C" {
 
 int mpm_batch_scene_gather_async(mpm_batch* b, int id, int n, const int64_t* particle, const int* field,
                                  const int* component) {

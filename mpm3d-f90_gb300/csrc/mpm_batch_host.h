@@ -38,6 +38,11 @@ struct BatchProgress {
 // progress of every resident scene, read from the device in one copy
 // (synchronises the batch stream)
 int batch_progress(mpm_batch* b, std::vector<BatchProgress>& out);
+// restart image of a resident scene (its persistent particle arrays in the
+// batch's storage order and its step state) and its restoration into a scene
+// of the same deck and layout; the next steps continue bit-identically
+int mpm_batch_scene_snapshot(mpm_batch* b, int id, std::vector<unsigned char>& out);
+int mpm_batch_scene_restore(mpm_batch* b, int id, const unsigned char* in, size_t bytes);
 // particles of all resident scenes
 long long batch_particles(const mpm_batch* b);
 // particle-steps still to run over the resident scenes, and the smallest

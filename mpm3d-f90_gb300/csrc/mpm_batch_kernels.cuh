@@ -651,10 +651,13 @@ __global__ void __launch_bounds__(32 * kCellWarps, 4)
 
 // Accumulated channels 0..nv-1 of node n in FP64 (the accumulators cleared
 // for the next transfer). Returns false for an idle node: nothing
-// accumulated and no mass at the node already, so every node field is still
-// zero from the last time the node was written and nothing needs writing --
-// on sparse grids most nodes are idle. (A node that no particle reaches is
-// never read by a particle, and one whose mass drops to zero is written once.)
+// accumulated and a node mass of +0, so every node field is still zero from
+// the last time the node was written and nothing needs writing -- on sparse
+// grids most nodes are idle. (A node that no particle reaches is never read
+// by a particle, and one whose mass drops to zero is written once.) A
+// massless node that received a force or a momentum (IntegrateMomentum
+// integrates every node, so its momentum is F * DT) carries a mass of -0 as
+// the mark that its fields are not zero, and the next transfer clears them.
 __device__ __forceinline__ bool take_acc(BState& b, long long n, int nv, const double* unit, double* out) {
   unsigned long long q[4];
   unsigned long long any = 0ull;
@@ -662,7 +665,7 @@ __device__ __forceinline__ bool take_acc(BState& b, long long n, int nv, const d
     q[v] = b.acc[v * b.NN + n];
     any |= q[v];
   }
-  if (any == 0ull && b.mg[n] == 0.0) return false;
+  if (any == 0ull && __double_as_longlong(b.mg[n]) == 0ll) return false;
   for (int v = 0; v < nv; ++v) {
     out[v] = (double)(long long)q[v] * unit[v];
     if (q[v]) b.acc[v * b.NN + n] = 0ull;
@@ -765,6 +768,9 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
           for (int a = 0; a < 3; ++a) b.fx[a * NN + n] = 0.0;
           b.nvel[n] = make_float4(0.f, 0.f, 0.f, 0.f);
           b.nacc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+          // a momentum without mass (the mass contributions quantised to
+          // zero, the momentum ones not) keeps the node marked (take_acc)
+          if (b.px[n] != 0.0 || b.px[NN + n] != 0.0 || b.px[2 * NN + n] != 0.0) b.mg[n] = -0.0;
         }
       }
     }
@@ -1125,6 +1131,7 @@ __device__ __forceinline__ void node_integrate(BState& b, const Scene& sc, long 
   }
   node_finish(b, sc, n, 1, 1);
   const double m = b.mg[n];
+  if (m == 0.0 && sc.shape != 3) b.mg[n] = -0.0;  // fields not zero at a massless node (take_acc)
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   if (m > sc.cutoff) {
     const float m32 = (float)m;
@@ -1432,6 +1439,8 @@ __global__ void kb_p2g_momentum(BState b) {
   b.px[n] = P0;
   b.px[NN + n] = P1;
   b.px[2 * NN + n] = P2;
+  if (sc.shape != 3 && b.mg[n] == 0.0 && (P0 != 0.0 || P1 != 0.0 || P2 != 0.0))
+    b.mg[n] = -0.0;  // momentum at a massless node (take_acc)
   node_finish(b, sc, n, 1, !sc.usf);
 }
 

@@ -1011,14 +1011,69 @@ static int deck_hash(mpm_ctx* c, uint64_t* out) {
   h = fnv1a(h, &c->g, sizeof c->g);
   h = fnv1a(h, c->mats.data(), sizeof(DevMaterial) * c->mats.size());
   std::vector<double> m((size_t)c->g.np);
-  CK(cudaMemcpy(m.data(), c->st.mass, sizeof(double) * m.size(), cudaMemcpyDeviceToHost));
+  if (c->batch) {  // the masses in the deck's particle order
+    if (int r = batch_status(c, mpm_batch_scene_download(c->batch, c->batch_scene, MPM_P_MASS, m.data()))) return r;
+  } else {
+    CK(cudaMemcpy(m.data(), c->st.mass, sizeof(double) * m.size(), cudaMemcpyDeviceToHost));
+  }
   *out = fnv1a(h, m.data(), sizeof(double) * m.size());
   return MPM_OK;
 }
 
+// Mixed form: the header (nfields 0) is followed by the byte count and the
+// scene's restart image from the batched engine (its persistent particle
+// arrays in the engine's storage order and its step state).
+static int snapshot_save_mixed(mpm_ctx* c, const char* path) {
+  SnapHeader h;
+  memset(&h, 0, sizeof h);
+  memcpy(h.magic, kSnapMagic, 8);
+  h.precision = c->precision;
+  h.np = c->g.np;
+  h.nn = c->g.nn;
+  h.ncell = c->g.ncell;
+  h.uvfp = c->g.uvfp;
+  if (int r = deck_hash(c, &h.deck_hash)) return r;
+  std::vector<unsigned char> img;
+  if (int r = batch_status(c, mpm::mpm_batch_scene_snapshot(c->batch, c->batch_scene, img))) return r;
+  h.scalars_bytes = 0;
+  FILE* f = fopen(path, "wb");
+  if (!f) return set_err(c, MPM_ERR_IO, "cannot write %s", path);
+  const int64_t n = (int64_t)img.size();
+  bool ok = fwrite(&h, sizeof h, 1, f) == 1 && fwrite(&n, sizeof n, 1, f) == 1 &&
+            fwrite(img.data(), 1, img.size(), f) == img.size();
+  ok = (fclose(f) == 0) && ok;
+  if (!ok) return set_err(c, MPM_ERR_IO, "writing %s failed", path);
+  return MPM_OK;
+}
+
+static int snapshot_load_mixed(mpm_ctx* c, const char* path) {
+  uint64_t mine = 0;
+  if (int r = deck_hash(c, &mine)) return r;
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_err(c, MPM_ERR_IO, "cannot read %s", path);
+  SnapHeader h;
+  int64_t n = 0;
+  int r = MPM_OK;
+  std::vector<unsigned char> img;
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, kSnapMagic, 8) != 0) {
+    r = set_err(c, MPM_ERR_IO, "%s is not a snapshot", path);
+  } else if (h.precision != c->precision || h.np != c->g.np || h.nn != c->g.nn || h.ncell != c->g.ncell ||
+             h.uvfp != c->g.uvfp || h.nfields != 0 || h.deck_hash != mine) {
+    r = set_err(c, MPM_ERR_STATE, "snapshot of another deck or precision");
+  } else if (fread(&n, sizeof n, 1, f) != 1 || n <= 0 || n > (int64_t)1 << 40) {
+    r = set_err(c, MPM_ERR_IO, "truncated snapshot");
+  } else {
+    img.resize((size_t)n);
+    if (fread(img.data(), 1, img.size(), f) != img.size()) r = set_err(c, MPM_ERR_IO, "truncated snapshot");
+  }
+  fclose(f);
+  if (r) return r;
+  return batch_status(c, mpm::mpm_batch_scene_restore(c->batch, c->batch_scene, img.data(), img.size()));
+}
+
 int mpm_snapshot_save(mpm_ctx* c, const char* path) {
   if (!c || !path) return set_err(c, MPM_ERR_ARG, "bad argument");
-  if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "snapshots cover the FP64 forms");
+  if (c->batch) return snapshot_save_mixed(c, path);
   CK(cudaStreamSynchronize(c->stream));
   FILE* f = fopen(path, "wb");
   if (!f) return set_err(c, MPM_ERR_IO, "cannot write %s", path);
@@ -1063,7 +1118,7 @@ int mpm_snapshot_save(mpm_ctx* c, const char* path) {
 
 int mpm_snapshot_load(mpm_ctx* c, const char* path) {
   if (!c || !path) return set_err(c, MPM_ERR_ARG, "bad argument");
-  if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "snapshots cover the FP64 forms");
+  if (c->batch) return snapshot_load_mixed(c, path);
   FILE* f = fopen(path, "rb");
   if (!f) return set_err(c, MPM_ERR_IO, "cannot read %s", path);
   SnapHeader h;

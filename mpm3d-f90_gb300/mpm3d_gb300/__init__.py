@@ -378,7 +378,7 @@ class MpmStep:
         self._check(library().mpm_algorithmic_bytes(self._h, ctypes.byref(b)))
         return b.value
 
-    # -- restart snapshot (FP64 forms)
+    # -- restart snapshot (every form)
     def save(self, path: str) -> None:
         self._check(library().mpm_snapshot_save(self._h, path.encode()))
 
