@@ -543,7 +543,8 @@ __device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int
       }
     }
     __syncwarp();
-    for (int p = 0; p < cnt; ++p) {
+    // particle p's contributions to this lane's slots, in particle order
+    auto add_particle = [&](int p) {
       for (int k = 0; k < 2; ++k) {
         if (!use[k]) continue;
         const float2 x = tab[p * 12 + sx[k]];
@@ -562,6 +563,12 @@ __device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int
           if (MODE == 0) acc[k][3] += x.x * m4.w;
         }
       }
+    };
+    if (cnt == PC) {  // a full round (the common case): unrolled, shared-memory offsets constant
+#pragma unroll
+      for (int p = 0; p < PC; ++p) add_particle(p);
+    } else {
+      for (int p = 0; p < cnt; ++p) add_particle(p);
     }
     __syncwarp();
   }
