@@ -11,10 +11,10 @@ functions, USF. A "step" is one explicit time step of the whole scene.
              stream (inputs are larger than L2, no flush needed);
   fp64       the plain FP64 form (bit-identical to the CPU oracle) on the same
              steps, and the mixed form's error against it;
-  e2e        the same metric through the C ABI from host arrays: context
-             creation (host->device upload of the particle state), the steps
-             with the per-step scalar read-back the host loop needs for its
-             exit test, and the read-back of the particle state;
+  e2e        the same metric through the C ABI from page-locked host arrays:
+             context creation (host->device upload of the particle state), the
+             steps with the per-step scalar read-back the host loop needs for
+             its exit test, and the read-back of the particle state;
   roofline   the dominant kernel's algorithmic bytes / its event-timed duration;
   cpu_baseline  the CPU oracle (a restatement of the reference step) on a
              bounded sample of the same workload on this host's cores.
@@ -66,7 +66,11 @@ def make_deck(workload: str, scale: float = 1.0) -> str:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled during the timed region:
+    the sampler runs every 20 ms from before the region (the first sample is
+    awaited, so sampling is live when the region starts), each line is
+    stamped with the host clock when it arrives, and only the lines that
+    arrived between the region's start and shortly after its end are kept."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -75,33 +79,41 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.perf_counter() + 5.0
+            while not self.lines and time.perf_counter() < deadline and self.proc.poll() is None:
+                time.sleep(0.005)
         except OSError:
             self.proc = None
+        self.t0 = time.perf_counter()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def stop(self) -> dict:
+        self.t1 = time.perf_counter()
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.05)  # a sample taken at the end of the region is still in the pipe
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        inside = [ln for t, ln in self.lines if self.t0 <= t <= self.t1 + 0.05]
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in inside:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -114,7 +126,8 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": 20,
+                "region_ms": round((self.t1 - self.t0) * 1e3, 1)}
 
 
 def rel_err(a, b) -> float:
@@ -280,20 +293,26 @@ def run_ours(args) -> dict:
                                           rel_err(states["mixed"]["SD"], states["fp64"]["SD"])),
                "position_rel": rel_err(states["mixed"]["Xp"], states["fp64"]["Xp"])}
 
-    # end to end through the C ABI from host buffers
+    # end to end through the C ABI from host buffers: the deck's particle
+    # arrays and the result buffers are page-locked once, before the timed
+    # region, as a host program would allocate them
     if args.no_e2e:
         t_e2e, h2d, d2h = float("nan"), 0, 0
-    t0 = time.perf_counter()
     if not args.no_e2e:
+        res_fields = ("Xp", "VXp", "SM", "SD")
+        deck.pin(True)
+        bufs = {f: m.pinned_empty(m.COMPONENTS.get(f, 1) * npart) for f in res_fields}
+        t0 = time.perf_counter()
         e2 = m.MpmStep(deck, precision="mixed", device=local)
         h2d = npart * 8 * (1 + 3 + 3 + 3)  # mass, Xp, VXp, FXp uploaded
         for _ in range(args.steps):
             e2.step()
             e2.scalars()  # the host loop's exit test needs CurrentTime every step
-        out = [e2.download(f) for f in ("Xp", "VXp", "SM", "SD")]
+        out = [e2.download(f, out=bufs[f]) for f in res_fields]
         t_e2e = time.perf_counter() - t0
         d2h = args.steps * 16 * 8 + sum(o.nbytes for o in out)
         e2.close()
+        deck.pin(False)
         t_e2e = max_over_ranks(t_e2e)
 
     mixed, fp64 = results["mixed"], results.get("fp64")

@@ -133,6 +133,18 @@ int mpm_get_scalars(mpm_ctx* ctx, double* out16);
 int mpm_download(mpm_ctx* ctx, int field, double* out);
 /* Replace a particle field (component-major, nb_particle per component). */
 int mpm_upload(mpm_ctx* ctx, int field, const double* in);
+/* Page-locked host memory (no counterpart in the reference). Copies between
+ * the device and page-locked buffers run at the link's bandwidth; pageable
+ * buffers go through the driver's staging. mpm_host_alloc returns NULL on
+ * failure (message in mpm_last_error); mpm_host_register locks an existing
+ * buffer in place (undone by mpm_host_unregister, before the buffer is
+ * freed); mpm_deck_pin locks (on != 0) or unlocks the particle arrays of a
+ * deck, which mpm_create then uploads from. */
+void* mpm_host_alloc(int64_t bytes);
+void mpm_host_free(void* p);
+int mpm_host_register(void* p, int64_t bytes);
+int mpm_host_unregister(void* p);
+int mpm_deck_pin(mpm_deck* deck, int on);
 int64_t mpm_nb_particle(const mpm_ctx* ctx);
 int64_t mpm_nb_gridnode(const mpm_ctx* ctx);
 int64_t mpm_nb_cell(const mpm_ctx* ctx);

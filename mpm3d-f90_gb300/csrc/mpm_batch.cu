@@ -1312,11 +1312,15 @@ HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code
   return h;
 }
 
-// Touches every page of a host destination buffer once from the CPU: a
-// device-to-host copy into pageable pages that were never touched waits for
-// the driver to fault them in one by one, several times slower than the CPU
-// does it (a fresh 28 MB array: 28 ms against under 1 ms touched first).
+// Touches every page of a pageable host destination buffer once from the
+// CPU: a device-to-host copy into pageable pages that were never touched
+// waits for the driver to fault them in one by one, several times slower
+// than the CPU does it (a fresh 28 MB array: 28 ms against under 1 ms touched
+// first). Page-locked buffers are resident already and are left alone.
 void prefault_host(void* p, size_t bytes) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost) return;  // page-locked
+  cudaGetLastError();
   static const size_t page = (size_t)std::max(4096L, sysconf(_SC_PAGESIZE));
   volatile char* c = static_cast<volatile char*>(p);
   for (size_t k = 0; k < bytes; k += page) c[k] = 0;

@@ -911,6 +911,56 @@ int mpm_download(mpm_ctx* c, int field, double* out) {
   return MPM_OK;
 }
 
+void* mpm_host_alloc(int64_t bytes) {
+  if (bytes <= 0) {
+    set_err(nullptr, MPM_ERR_ARG, "page-locked allocation of %lld bytes", (long long)bytes);
+    return nullptr;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    set_err(nullptr, MPM_ERR_OOM, "page-locked allocation of %lld bytes: %s", (long long)bytes, cudaGetErrorString(e));
+    return nullptr;
+  }
+  return p;
+}
+
+void mpm_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+int mpm_host_register(void* p, int64_t bytes) {
+  if (!p || bytes <= 0) return set_err(nullptr, MPM_ERR_ARG, "bad argument");
+  cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) return set_err(nullptr, MPM_ERR_CUDA, "host register: %s", cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+int mpm_host_unregister(void* p) {
+  if (!p) return set_err(nullptr, MPM_ERR_ARG, "bad argument");
+  cudaError_t e = cudaHostUnregister(p);
+  if (e != cudaSuccess) return set_err(nullptr, MPM_ERR_CUDA, "host unregister: %s", cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+int mpm_deck_pin(mpm_deck* d, int on) {
+  if (!d) return set_err(nullptr, MPM_ERR_ARG, "deck is NULL");
+  const int64_t np = d->nb_particle;
+  double* a[4] = {d->mass, d->xp, d->vxp, d->fxp};
+  const int64_t n[4] = {np, 3 * np, 3 * np, 3 * np};
+  for (int k = 0; k < 4; ++k) {
+    if (!a[k] || n[k] <= 0) continue;
+    const int r = on ? mpm_host_register(a[k], n[k] * 8) : mpm_host_unregister(a[k]);
+    if (r && on) {  // leave nothing half locked
+      for (int u = 0; u < k; ++u)
+        if (a[u] && n[u] > 0) cudaHostUnregister(a[u]);
+      return r;
+    }
+    if (r) return r;
+  }
+  return MPM_OK;
+}
+
 int mpm_upload(mpm_ctx* c, int field, const double* in) {
   if (!c || !in) return set_err(c, MPM_ERR_ARG, "bad argument");
   if (c->batch) return set_err(c, MPM_ERR_UNSUPPORTED, "the mixed form takes its state from the deck only");

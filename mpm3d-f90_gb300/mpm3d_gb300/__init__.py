@@ -97,6 +97,11 @@ def library() -> ctypes.CDLL:
         "mpm_get_scalars": (i, [vp, P(d)]),
         "mpm_download": (i, [vp, i, P(d)]),
         "mpm_upload": (i, [vp, i, P(d)]),
+        "mpm_host_alloc": (vp, [i64]),
+        "mpm_host_free": (None, [vp]),
+        "mpm_host_register": (i, [vp, i64]),
+        "mpm_host_unregister": (i, [vp]),
+        "mpm_deck_pin": (i, [vp, i]),
         "mpm_nb_particle": (i64, [vp]),
         "mpm_nb_gridnode": (i64, [vp]),
         "mpm_nb_cell": (i64, [vp]),
@@ -167,6 +172,50 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+class _PinnedBuffer:
+    """Owner of a page-locked host allocation (mpm_host_alloc), freed when
+    the last array viewing it goes away."""
+
+    def __init__(self, nbytes: int):
+        lib = library()
+        self.p = lib.mpm_host_alloc(int(nbytes))
+        if not self.p:
+            raise MpmError(2, lib.mpm_last_error(None).decode(errors="replace"))
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            library().mpm_host_free(self.p)
+            self.p = None
+
+
+class _PinnedArray(np.ndarray):
+    """ndarray in page-locked host memory; its views keep it (and so the
+    allocation) alive through their base."""
+    _owner = None
+
+
+def _out_buffer(out: Optional[np.ndarray], n: int) -> np.ndarray:
+    if out is None:
+        return np.empty(n)
+    if out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
+        raise MpmError(1, f"out must be a contiguous float64 array of {n} values")
+    return out.reshape(n)
+
+
+def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
+    """An uninitialised array in page-locked host memory: device copies into
+    and out of it run at the link's bandwidth (downloads accept it as out=)."""
+    shape = (int(shape),) if np.isscalar(shape) else tuple(int(x) for x in shape)
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape))
+    nbytes = max(1, n * dt.itemsize)
+    buf = _PinnedBuffer(nbytes)
+    raw = (ctypes.c_char * nbytes).from_address(buf.p)
+    a = np.frombuffer(raw, dtype=dt, count=n).reshape(shape).view(_PinnedArray)
+    a._owner = buf
+    return a
+
+
 class Deck:
     """A parsed .mpm deck (the reference's input format, FFI.f90 / DataIn.f90)."""
 
@@ -222,8 +271,21 @@ class Deck:
                  "EndTime", "OutTime", "ReportTime", "QuasiLoadTime", "DampFactor", "bq1", "bq2")
         return dict(zip(names, o.tolist()))
 
+    def pin(self, on: bool = True) -> None:
+        """Page-lock (or unlock) the deck's particle arrays, from which a
+        context is uploaded: the upload then runs at the link's bandwidth."""
+        if bool(on) == getattr(self, "_pinned", False):
+            return
+        st = library().mpm_deck_pin(self._h, int(bool(on)))
+        if st:
+            raise MpmError(st, library().mpm_last_error(None).decode(errors="replace"))
+        self._pinned = bool(on)
+
     def close(self) -> None:
         if self._h and self._h.value:
+            if getattr(self, "_pinned", False):
+                library().mpm_deck_pin(self._h, 0)
+                self._pinned = False
             library().mpm_deck_free(self._h)
             self._h = ctypes.c_void_p()
 
@@ -336,7 +398,9 @@ class MpmStep:
         self._check(library().mpm_get_scalars(self._h, _dptr(o)))
         return dict(zip(SCALARS, o.tolist()))
 
-    def download(self, field: str) -> np.ndarray:
+    def download(self, field: str, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """A field in host memory; out (contiguous float64 of the field's size,
+        e.g. from pinned_empty) receives it in place of a new array."""
         ncomp = COMPONENTS.get(field, 1)
         if field in GRID_FIELDS:
             n = self.nb_gridnode * self.nb_component  # every grid component, component-major
@@ -344,9 +408,9 @@ class MpmStep:
             n = self.nb_cell
         else:
             n = self.nb_particle
-        out = np.empty(ncomp * n)
+        out = _out_buffer(out, ncomp * n)
         self._check(library().mpm_download(self._h, FIELDS[field], _dptr(out)))
-        return out.reshape(ncomp, n) if ncomp > 1 else out
+        return out.reshape(ncomp, n) if ncomp > 1 else out.reshape(n)
 
     def contact_force(self) -> np.ndarray:
         """Total contact force of the last step (Lagr_NodContact's tot_cont_for)."""
@@ -489,7 +553,7 @@ class Batch:
         self._check(library().mpm_batch_scene_scalars(self._h, int(scene), _dptr(o)))
         return dict(zip(SCALARS, o.tolist()))
 
-    def download(self, scene: int, field: str) -> np.ndarray:
+    def download(self, scene: int, field: str, out: Optional[np.ndarray] = None) -> np.ndarray:
         ncomp = COMPONENTS.get(field, 1)
         sc = self.scalars(scene)
         if field in GRID_FIELDS:
@@ -498,9 +562,9 @@ class Batch:
             raise MpmError(1, "cell fields are read per scene through MpmStep")
         else:
             n = int(sc["nb_particle"])
-        out = np.empty(ncomp * n)
+        out = _out_buffer(out, ncomp * n)
         self._check(library().mpm_batch_scene_download(self._h, int(scene), FIELDS[field], _dptr(out)))
-        return out.reshape(ncomp, n) if ncomp > 1 else out
+        return out.reshape(ncomp, n) if ncomp > 1 else out.reshape(n)
 
     def set_blocks(self, particle_block: int = 0, node_block: int = 0) -> None:
         self._check(library().mpm_batch_set_blocks(self._h, int(particle_block), int(node_block)))
@@ -731,5 +795,5 @@ class Server:
         return True
 
 
-__all__ = ["Deck", "MpmStep", "Batch", "Server", "Output", "format_e", "serve_plan", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
+__all__ = ["Deck", "pinned_empty", "MpmStep", "Batch", "Server", "Output", "format_e", "serve_plan", "MpmError", "library", "FIELDS", "PHASES", "PRECISION",
            "LIB_PATH"]

@@ -78,3 +78,30 @@ def test_curve_files_match_oracle(gpu_mod, oracle_mod, tmp_path):
         scale = np.abs(rb[:, 1:]).max()
         assert np.all(ra[:, 0] == rb[:, 0])
         assert np.abs(ra[:, 1:] - rb[:, 1:]).max() <= 1e-12 * scale
+
+
+def test_pinned_buffers_and_deck(built):
+    """Page-locked result buffers (download out=) and a page-locked deck give
+    the same fields as pageable ones, for the FP64 and the mixed form."""
+    import numpy as np
+    from mpm3d_gb300 import COMPONENTS, Deck, MpmStep, pinned_empty
+    from gpu_cases import CASES
+    mk, _ = CASES["slope_small_usf_dp_gimp"]
+    plain = Deck.parse(mk())
+    locked = Deck.parse(mk())
+    locked.pin(True)
+    for form in ("fp64", "mixed"):
+        a = MpmStep(plain, form)
+        b = MpmStep(locked, form)
+        a.run(3)
+        b.run(3)
+        for f in ("Xp", "VXp", "SD", "Mg"):
+            n = COMPONENTS.get(f, 1) * (a.nb_gridnode * a.nb_component if f == "Mg" else a.nb_particle)
+            buf = pinned_empty(n)
+            got = b.download(f, out=buf)
+            assert np.shares_memory(got, buf)
+            np.testing.assert_array_equal(a.download(f), got, err_msg=f"{form} {f}")
+        a.close()
+        b.close()
+    locked.pin(False)
+    locked.close()
