@@ -435,19 +435,28 @@ def cpu_baseline(text: str, steps: int, npart: int, cores: int = 1) -> dict:
 
 
 def _replica(args_tuple):
-    text, warm, steps = args_tuple
+    """One CPU replica of the reference arm: warm-up steps, then up to
+    `steps` timed steps, stopping early once `budget_s` seconds are spent."""
+    text, warm, steps, budget_s = args_tuple
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
     o = oracle.Oracle(deck_text=text)
     o.run(warm)
     t0 = time.perf_counter()
-    o.run(steps)
-    return time.perf_counter() - t0, o.nb_particle
+    done = 0
+    while done < steps:
+        o.run(1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return time.perf_counter() - t0, o.nb_particle, done
 
 
 def run_reference(args) -> dict:
-    """Reference arm: the CPU step (oracle port), one replica per host core."""
+    """Reference arm: the CPU step (oracle port), one replica per host core,
+    each running the --warmup / --steps of the workload (bounded: a replica
+    stops timing once --ref-budget seconds are spent)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
@@ -455,23 +464,27 @@ def run_reference(args) -> dict:
 
     text = make_deck(args.workload, args.scale)
     cores = args.ref_cores or os.cpu_count() or 1
+    steps = args.ref_steps or args.steps
+    warm = args.ref_warmup if args.ref_warmup >= 0 else args.warmup
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_replica, [(text, args.ref_warmup, args.ref_steps)] * cores)
+        res = pool.map(_replica, [(text, warm, steps, args.ref_budget)] * cores)
     t = max(r[0] for r in res)
     npart = res[0][1]
-    value = npart * cores * args.ref_steps / t
+    done = [r[2] for r in res]
+    value = npart * sum(done) / t
     return {
         "impl": "reference",
         "metric": "particle-steps/s (mixed precision vs plain FP64 GPU, stated error)",
         "value": value, "unit": "particle-steps/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.ref_steps * 1e3,
+        "steps": min(done), "warmup": warm, "ms_per_step": t / max(1, min(done)) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded deck generator)",
         "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
                    "parallelism": f"{cores} CPU replicas"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.ref_steps} steps per replica after {args.ref_warmup} warm-up steps, "
+                         "sample": f"{min(done)}-{max(done)} timed steps per replica (of {steps} asked, "
+                                   f"{args.ref_budget:.0f} s budget) after {warm} warm-up steps, "
                                    f"{cores} independent replicas of the full workload"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -489,8 +502,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 form (large workloads)")
-    ap.add_argument("--ref-steps", type=int, default=2)
-    ap.add_argument("--ref-warmup", type=int, default=1)
+    ap.add_argument("--ref-steps", type=int, default=0, help="reference arm steps (0 = --steps)")
+    ap.add_argument("--ref-warmup", type=int, default=-1, help="reference arm warm-up steps (-1 = --warmup)")
+    ap.add_argument("--ref-budget", type=float, default=90.0, help="reference arm: seconds of timed steps per replica")
     ap.add_argument("--ref-cores", type=int, default=0)
     ap.add_argument("--serve-scenes", type=int, default=256, help="serving workload scenes (0 = skip)")
     ap.add_argument("--serve-steps", type=int, default=500)
