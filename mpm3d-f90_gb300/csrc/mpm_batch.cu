@@ -196,13 +196,18 @@ struct mpm_batch {
   bool inv_stale = false;  // steps ran since the inverse permutation was last built
   long long bytes = 0;
   int* d_target = nullptr;
+  // second stream: the energy / DT reduction of a step runs there while the
+  // next step's keys are sorted (the two touch disjoint arrays)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
   int key_bits = 1;
   int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
   int any_prep = 0;  // scenes whose force input is not staged by their stress kernel (USL / MUSL, Johnson-Cook)
   unsigned stress_types = 0;  // stress instantiations to launch: bit MT per specialised type, bit 0 for the rest
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one step, per buffer parity
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // one step, per buffer parity and
+                                                                      // without / with the previous step's reduction
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
   int scatter_blocks = 9728;  // scatter grid cap (64 blocks per SM; warps stride over the occupied cells)
@@ -332,13 +337,16 @@ long long scene_keys(const Geometry& g) { return (long long)g.ncell + 1; }
 inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
 
 // one step of every live scene (MPM3D.f90:69-118 for each scene)
-int enqueue_step(mpm_batch* b) {
+// The step in three parts. The front (sort keys, sort, per-key counts,
+// occupied keys) reads the positions and scene ids only; the back (begin,
+// permutation, transfers, stress, position) does the rest; the reduction
+// (calcEnergy, UpdateDT, damping) reads the final velocities, masses and
+// energies. The front does not depend on the begin kernel (which advances
+// the step count and time), so it runs first.
+int enqueue_front(mpm_batch* b) {
   cudaStream_t st = b->stream;
   BState& a = b->A;
-  const int pb = b->pblock, nb = b->nblock;
-  prof_begin(K_BEGIN, st);
-  kb_begin<<<gridn(a.nscene, 128), 128, 0, st>>>(a, b->d_target);
-  prof_end(K_BEGIN, st);
+  const int pb = b->pblock;
   prof_begin(K_LOCATE, st);
   cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
   kb_keys<<<gridn(a.NP, pb), pb, 0, st>>>(a);
@@ -358,6 +366,16 @@ int enqueue_step(mpm_batch* b) {
     if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "run-length encode: %s", cudaGetErrorString(e));
   }
   prof_end(K_SORT, st);
+  return MPM_OK;
+}
+
+int enqueue_back(mpm_batch* b) {
+  cudaStream_t st = b->stream;
+  BState& a = b->A;
+  const int pb = b->pblock, nb = b->nblock;
+  prof_begin(K_BEGIN, st);
+  kb_begin<<<gridn(a.nscene, 128), 128, 0, st>>>(a, b->d_target);
+  prof_end(K_BEGIN, st);
   prof_begin(K_PERMUTE, st);
   kb_permute<<<gridn(a.NP, pb), pb, 0, st>>>(a, b->B);
   prof_end(K_PERMUTE, st);
@@ -434,6 +452,14 @@ int enqueue_step(mpm_batch* b) {
     prof_end(K_P2G_MOM, st);
   }
   if (b->any_later && (r = stress(0))) return r;
+  return MPM_OK;
+}
+
+// calcEnergy + UpdateDT (+ dynamic relaxation) of the step that just ran,
+// on stream st
+int enqueue_reduce(mpm_batch* b, cudaStream_t st) {
+  BState& s = b->A;
+  const int pb = b->pblock;
   prof_begin(K_REDUCE, st);
   kb_reduce_chunks<<<(unsigned)s.NR, 256, 0, st>>>(s);
   kb_reduce_scenes<<<(unsigned)s.nscene, 256, 0, st>>>(s, 3);
@@ -444,26 +470,60 @@ int enqueue_step(mpm_batch* b) {
     kb_dr_finish<<<gridn(s.nscene, 128), 128, 0, st>>>(s);
     prof_end(K_DR, st);
   }
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "launch: %s", cudaGetErrorString(e));
   return MPM_OK;
 }
 
-void drop_graph(mpm_batch* b) {
-  for (auto& g : b->graph) {
-    if (g) cudaGraphExecDestroy(g);
-    g = nullptr;
+// one whole step, in order
+int enqueue_step(mpm_batch* b) {
+  int r = enqueue_front(b);
+  if (!r) r = enqueue_back(b);
+  if (!r) r = enqueue_reduce(b, b->stream);
+  return r;
+}
+
+// one step whose front overlaps the previous step's reduction (lead), which
+// then runs on the side stream; without lead the step ends before its own
+// reduction, which the caller enqueues (the next step's lead, or the tail of
+// a run)
+int enqueue_step_overlapped(mpm_batch* b, bool lead) {
+  if (lead) {
+    BCK(cudaEventRecord(b->ev_fork, b->stream));
+    BCK(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+    if (int r = enqueue_reduce(b, b->side)) return r;
+    BCK(cudaEventRecord(b->ev_join, b->side));
   }
+  int r = enqueue_front(b);
+  if (lead) BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
+  if (!r) r = enqueue_back(b);
+  if (!r) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "launch: %s", cudaGetErrorString(e));
+  }
+  return r;
+}
+
+void drop_graph(mpm_batch* b) {
+  for (auto& gp : b->graph)
+    for (auto& g : gp) {
+      if (g) cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
 }
 
 // capture nsteps steps into an executable graph; the host-side buffer handles
-// end swapped nsteps times, as after running the steps eagerly
-int capture(mpm_batch* b, int nsteps, cudaGraphExec_t* out) {
+// end swapped nsteps times, as after running the steps eagerly. lead < 0:
+// whole steps in order; otherwise one overlapped step (with or without the
+// previous step's reduction)
+int capture(mpm_batch* b, int nsteps, cudaGraphExec_t* out, int lead = -1) {
   cudaGraph_t g;
   BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   b->prof.capturing = true;
   int r = MPM_OK;
-  for (int i = 0; i < nsteps && r == MPM_OK; ++i) r = enqueue_step(b);
+  if (lead >= 0) r = enqueue_step_overlapped(b, lead != 0);
+  else
+    for (int i = 0; i < nsteps && r == MPM_OK; ++i) r = enqueue_step(b);
   b->prof.capturing = false;
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (r) {
@@ -817,7 +877,13 @@ int mpm_batch_create(int device, mpm_batch** out) {
     b->scatter_blocks = 64 * sms;
     b->scatter_wave = 4 * sms * kCellWarps;
   }
-  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return MPM_ERR_CUDA;
   }
@@ -840,6 +906,10 @@ void mpm_batch_destroy(mpm_batch* b) {
   if (b->dl) cudaFree(b->dl);
   for (auto& kv : b->by_id) delete kv.second;
   prof_free(&b->prof);
+  cudaStreamSynchronize(b->side);
+  cudaEventDestroy(b->ev_fork);
+  cudaEventDestroy(b->ev_join);
+  cudaStreamDestroy(b->side);
   cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -900,9 +970,11 @@ int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph) {
   b->inv_stale = true;
   BProfScope ps(b);
   if (!use_graph) {
+    // each step's reduction overlaps the next step's sort; the last one ends
+    // the run, so nothing is pending between calls
     for (int i = 0; i < nsteps; ++i)
-      if ((r = enqueue_step(b))) return r;
-    return MPM_OK;
+      if ((r = enqueue_step_overlapped(b, i > 0))) return r;
+    return enqueue_reduce(b, b->stream);
   }
   if (b->prof.on) {
     // one graph over all the steps, with event nodes around every kernel
@@ -917,19 +989,22 @@ int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph) {
     return MPM_OK;
   }
   // one graph of one step per buffer parity (the step swaps the two particle
-  // buffer sets, so the graph captured from either set is replayed alternately)
+  // buffer sets, so the graph captured from either set is replayed
+  // alternately), the steps after the first of the run with the previous
+  // step's reduction overlapping their sort; the run's last reduction ends it
   for (int i = 0; i < nsteps; ++i) {
     const int par = b->A.x == b->set0_x ? 0 : 1;
-    if (!b->graph[par]) {
+    const int lead = i > 0 ? 1 : 0;
+    if (!b->graph[par][lead]) {
       cudaGraphExec_t ge = nullptr;
-      if ((r = capture(b, 1, &ge))) return r;
-      b->graph[par] = ge;
+      if ((r = capture(b, 1, &ge, lead))) return r;
+      b->graph[par][lead] = ge;
       std::swap(b->A, b->B);  // capture swapped the host handles; the launch below does the step
     }
-    BCK(cudaGraphLaunch(b->graph[par], b->stream));
+    BCK(cudaGraphLaunch(b->graph[par][lead], b->stream));
     std::swap(b->A, b->B);
   }
-  return MPM_OK;
+  return enqueue_reduce(b, b->stream);
 }
 
 int mpm_batch_sync(mpm_batch* b) {
