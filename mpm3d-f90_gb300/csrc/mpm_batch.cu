@@ -200,6 +200,10 @@ struct mpm_batch {
   // next step's keys are sorted (the two touch disjoint arrays)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // the per-key counts and the occupied keys of the sort run there too,
+  // beside the permutation; the first scatter waits for them
+  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;
+  bool counts_pending = false;
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
   int key_bits = 1;
@@ -343,7 +347,7 @@ inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / 
 // (calcEnergy, UpdateDT, damping) reads the final velocities, masses and
 // energies. The front does not depend on the begin kernel (which advances
 // the step count and time), so it runs first.
-int enqueue_front(mpm_batch* b) {
+int enqueue_front(mpm_batch* b, bool side_counts = false) {
   cudaStream_t st = b->stream;
   BState& a = b->A;
   const int pb = b->pblock;
@@ -356,6 +360,13 @@ int enqueue_front(mpm_batch* b) {
   cudaError_t e = cub::DeviceRadixSort::SortPairs(b->cub_tmp, tmp, a.key, a.key_sorted, a.val, a.perm, (int)a.NP, 0,
                                                   b->key_bits, st);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "sort: %s", cudaGetErrorString(e));
+  if (side_counts) {
+    prof_end(K_SORT, st);
+    BCK(cudaEventRecord(b->ev_fork2, st));
+    BCK(cudaStreamWaitEvent(b->side, b->ev_fork2, 0));
+    st = b->side;
+    prof_begin(K_SORT, st);
+  }
   tmp = b->cub_bytes;
   e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
@@ -366,6 +377,10 @@ int enqueue_front(mpm_batch* b) {
     if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "run-length encode: %s", cudaGetErrorString(e));
   }
   prof_end(K_SORT, st);
+  if (side_counts) {
+    BCK(cudaEventRecord(b->ev_join2, st));
+    b->counts_pending = true;
+  }
   return MPM_OK;
 }
 
@@ -387,6 +402,10 @@ int enqueue_back(mpm_batch* b) {
     prof_begin(K_SG_CLEAR, st);
     kb_sg_clear<<<gridn(s.NC, nb), nb, 0, st>>>(s);
     prof_end(K_SG_CLEAR, st);
+  }
+  if (b->counts_pending) {  // per-key counts and occupied keys from the side stream
+    BCK(cudaStreamWaitEvent(st, b->ev_join2, 0));
+    b->counts_pending = false;
   }
   prof_begin(K_SCATTER_MASS, st);
   kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
@@ -494,7 +513,7 @@ int enqueue_step_overlapped(mpm_batch* b, bool lead) {
     if (int r = enqueue_reduce(b, b->side)) return r;
     BCK(cudaEventRecord(b->ev_join, b->side));
   }
-  int r = enqueue_front(b);
+  int r = enqueue_front(b, true);
   if (lead) BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
   if (!r) r = enqueue_back(b);
   if (!r) {
@@ -880,8 +899,12 @@ int mpm_batch_create(int device, mpm_batch** out) {
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming) != cudaSuccess) {
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->ev_fork2) cudaEventDestroy(b->ev_fork2);
     if (b->side) cudaStreamDestroy(b->side);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -909,6 +932,8 @@ void mpm_batch_destroy(mpm_batch* b) {
   cudaStreamSynchronize(b->side);
   cudaEventDestroy(b->ev_fork);
   cudaEventDestroy(b->ev_join);
+  cudaEventDestroy(b->ev_fork2);
+  cudaEventDestroy(b->ev_join2);
   cudaStreamDestroy(b->side);
   cudaStreamDestroy(b->stream);
   delete b;
