@@ -231,3 +231,39 @@ def test_mixed_refuses_contact(built):
     from mpm3d_gb300 import Deck, MpmError, MpmStep, decks
     with pytest.raises(MpmError):
         MpmStep(Deck.parse(decks.contact_blocks()), "mixed")
+
+
+@pytest.mark.parametrize("name", ["slope_small_usf_dp_gimp", "beam_musl_neoh_sgmp", "block_usf_elastic_drda"])
+def test_run_splitting_and_energies(built, name):
+    """A step's energy / DT reduction overlaps the next step's sort on a
+    second stream, and the last reduction of a run ends it: one run of n
+    steps, n runs of one step and an eager run give the same state, energies,
+    momentum and DT -- with dynamic relaxation, whose damping reads the
+    kinetic energy of the step before."""
+    from mpm3d_gb300 import Batch, Deck
+    if name.endswith("_drda"):
+        text = CASES[name[: -len("_drda")]][0]().replace("usf on\n", "usf on\ndrda\n")
+        assert "drda" in text
+    else:
+        text = CASES[name][0]()
+    d = Deck.parse(text)
+    keys = ("istep", "CurrentTime", "DT", "EngKinetic", "EngInternal", "Momentum_x", "Momentum_y", "Momentum_z",
+            "EngKinetic_prev")
+    out = []
+    for mode in ("one_run", "split", "eager"):
+        with Batch() as bt:
+            sid = bt.add(d, steps=24)
+            if mode == "one_run":
+                bt.run(24)
+            elif mode == "split":
+                for _ in range(24):
+                    bt.run(1)
+            else:
+                bt.run(24, graph=False)
+            bt.sync()
+            sc = bt.scalars(sid)
+            out.append(({k: sc[k] for k in keys}, {f: bt.download(sid, f) for f in PFIELDS}))
+    for sc, fields in out[1:]:
+        assert sc == out[0][0]
+        for f in PFIELDS:
+            np.testing.assert_array_equal(fields[f], out[0][1][f], err_msg=f"{name} {f}")
