@@ -1209,6 +1209,15 @@ std::vector<RestartField> restart_fields(const BState& s, bool uvfp) {
 
 namespace mpm {
 
+long long mpm_batch_scene_restart_bytes(mpm_batch* b, int id) {
+  if (!b || ensure_committed(b)) return -1;
+  HostScene* h = find(b, id);
+  if (!h) return -1;
+  long long n = (long long)sizeof(SceneState);
+  for (const RestartField& f : restart_fields(b->A, h->su.g.uvfp != 0)) n += (long long)f.nc * h->np * (long long)f.elem;
+  return n;
+}
+
 int mpm_batch_scene_snapshot(mpm_batch* b, int id, std::vector<unsigned char>& out) {
   if (!b) return MPM_ERR_ARG;
   int r = ensure_committed(b);

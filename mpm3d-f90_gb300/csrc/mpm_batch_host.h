@@ -42,6 +42,8 @@ int batch_progress(mpm_batch* b, std::vector<BatchProgress>& out);
 // batch's storage order and its step state) and its restoration into a scene
 // of the same deck and layout; the next steps continue bit-identically
 int mpm_batch_scene_snapshot(mpm_batch* b, int id, std::vector<unsigned char>& out);
+// bytes of that image (-1 for no such scene)
+long long mpm_batch_scene_restart_bytes(mpm_batch* b, int id);
 int mpm_batch_scene_restore(mpm_batch* b, int id, const unsigned char* in, size_t bytes);
 // particles of all resident scenes
 long long batch_particles(const mpm_batch* b);

@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <new>
 #include <vector>
 
 #include "mpm3d_gpu.h"
@@ -1084,7 +1085,11 @@ static int snapshot_save_mixed(mpm_ctx* c, const char* path) {
   h.uvfp = c->g.uvfp;
   if (int r = deck_hash(c, &h.deck_hash)) return r;
   std::vector<unsigned char> img;
-  if (int r = batch_status(c, mpm::mpm_batch_scene_snapshot(c->batch, c->batch_scene, img))) return r;
+  try {
+    if (int r = batch_status(c, mpm::mpm_batch_scene_snapshot(c->batch, c->batch_scene, img))) return r;
+  } catch (const std::bad_alloc&) {
+    return set_err(c, MPM_ERR_OOM, "no host memory for the restart image");
+  }
   h.scalars_bytes = 0;
   FILE* f = fopen(path, "wb");
   if (!f) return set_err(c, MPM_ERR_IO, "cannot write %s", path);
@@ -1110,11 +1115,17 @@ static int snapshot_load_mixed(mpm_ctx* c, const char* path) {
   } else if (h.precision != c->precision || h.np != c->g.np || h.nn != c->g.nn || h.ncell != c->g.ncell ||
              h.uvfp != c->g.uvfp || h.nfields != 0 || h.deck_hash != mine) {
     r = set_err(c, MPM_ERR_STATE, "snapshot of another deck or precision");
-  } else if (fread(&n, sizeof n, 1, f) != 1 || n <= 0 || n > (int64_t)1 << 40) {
+  } else if (fread(&n, sizeof n, 1, f) != 1) {
     r = set_err(c, MPM_ERR_IO, "truncated snapshot");
+  } else if (n != mpm::mpm_batch_scene_restart_bytes(c->batch, c->batch_scene)) {
+    r = set_err(c, MPM_ERR_STATE, "snapshot image of %lld bytes does not fit this context", (long long)n);
   } else {
-    img.resize((size_t)n);
-    if (fread(img.data(), 1, img.size(), f) != img.size()) r = set_err(c, MPM_ERR_IO, "truncated snapshot");
+    try {
+      img.resize((size_t)n);
+    } catch (const std::bad_alloc&) {
+      r = set_err(c, MPM_ERR_OOM, "no host memory for the restart image");
+    }
+    if (!r && fread(img.data(), 1, img.size(), f) != img.size()) r = set_err(c, MPM_ERR_IO, "truncated snapshot");
   }
   fclose(f);
   if (r) return r;
