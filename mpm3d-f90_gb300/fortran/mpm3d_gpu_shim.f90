@@ -34,6 +34,9 @@ module mpm3d_gpu
 
   type(c_ptr), save :: ctx = c_null_ptr
   type(c_ptr), save :: deck = c_null_ptr
+  ! page-locked download buffer of gpu_fetch_particles (9 * nb_particle)
+  type(c_ptr), save :: hbuf = c_null_ptr
+  integer(c_int64_t), save :: hbuf_n = 0
 
   interface
      integer(c_int) function mpm_deck_load(path, out, errbuf, errlen) bind(C, name="mpm_deck_load")
@@ -77,6 +80,19 @@ module mpm3d_gpu
        integer(c_int), value :: field
        real(c_double), dimension(*) :: out
      end function
+     integer(c_int) function mpm_deck_pin(d, on) bind(C, name="mpm_deck_pin")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: d
+       integer(c_int), value :: on
+     end function
+     type(c_ptr) function mpm_host_alloc(bytes) bind(C, name="mpm_host_alloc")
+       import :: c_ptr, c_int64_t
+       integer(c_int64_t), value :: bytes
+     end function
+     subroutine mpm_host_free(p) bind(C, name="mpm_host_free")
+       import :: c_ptr
+       type(c_ptr), value :: p
+     end subroutine
      integer(c_int) function mpm_sync(c) bind(C, name="mpm_sync")
        import :: c_int, c_ptr
        type(c_ptr), value :: c
@@ -103,10 +119,16 @@ contains
     prec = MPM_FP64_STRICT
     if (present(precision)) prec = precision
     call check(mpm_deck_load(trim(fileinp)//c_null_char, deck, err, 256_c_int), 'mpm_deck_load')
+    ! the particle arrays page-locked for the upload in mpm_create
+    call check(mpm_deck_pin(deck, 1_c_int), 'mpm_deck_pin')
     call check(mpm_create(deck, prec, -1_c_int, ctx), 'mpm_create')
+    call check(mpm_deck_pin(deck, 0_c_int), 'mpm_deck_pin')
   end subroutine gpu_init
 
   subroutine gpu_finalize()
+    if (c_associated(hbuf)) call mpm_host_free(hbuf)
+    hbuf = c_null_ptr
+    hbuf_n = 0
     call mpm_destroy(ctx)
     call mpm_deck_free(deck)
     ctx = c_null_ptr
@@ -176,10 +198,18 @@ contains
   ! output writers of DataOut.f90.
   subroutine gpu_fetch_particles()
     use ParticleData, only: particle_list, nb_particle
-    real(c_double), allocatable :: buf(:)
+    real(c_double), pointer :: buf(:)
     integer :: n, c
     n = nb_particle
-    allocate(buf(9 * n))
+    ! a page-locked buffer, kept for the next fetch: the copies run at the
+    ! link's bandwidth instead of through the driver's staging
+    if (hbuf_n < 9_c_int64_t * n) then
+       if (c_associated(hbuf)) call mpm_host_free(hbuf)
+       hbuf = mpm_host_alloc(8_c_int64_t * 9_c_int64_t * n)
+       if (.not. c_associated(hbuf)) stop 'page-locked buffer allocation failed'
+       hbuf_n = 9_c_int64_t * n
+    end if
+    call c_f_pointer(hbuf, buf, [9 * n])
     call check(mpm_download(ctx, F_XP, buf), 'Xp')
     do c = 1, 3
        particle_list(:)%Xp(c) = buf((c - 1) * n + 1:c * n)
@@ -209,7 +239,7 @@ contains
     particle_list(:)%celsius_t = buf(1:n)
     call check(mpm_download(ctx, F_SPRE, buf), 'Spre')
     particle_list(:)%Spre = buf(1:n)
-    deallocate(buf)
+    nullify(buf)
   end subroutine gpu_fetch_particles
 
 end module mpm3d_gpu
