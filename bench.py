@@ -139,6 +139,38 @@ def rel_err(a, b) -> float:
     return float(np.max(np.abs(a - b)) / s) if s > 0 else float(np.max(np.abs(a - b)))
 
 
+def disp_err(xm, xf, x0) -> float:
+    """Position error relative to the motion: max |(Xm - X0) - (Xf - X0)| /
+    max |Xf - X0| (positions stay FP64 in the mixed form, so an error relative
+    to the coordinates themselves would say nothing)."""
+    import numpy as np
+
+    dm = np.asarray(xm, dtype=np.float64) - x0
+    df = np.asarray(xf, dtype=np.float64) - x0
+    s = float(np.max(np.abs(df)))
+    return float(np.max(np.abs(dm - df)) / s) if s > 0 else float(np.max(np.abs(dm - df)))
+
+
+def form_errors(mixed: dict, fp64: dict, x0) -> dict:
+    """Mixed-form error against the FP64 form on the same deck after the same
+    steps: nodal momentum, particle stress (mean and deviatoric), particle
+    displacement; each max |a - b| / max |b| over the field."""
+    return {"nodal_momentum_rel": rel_err(mixed["PXg"], fp64["PXg"]),
+            "particle_stress_rel": max(rel_err(mixed["SM"], fp64["SM"]), rel_err(mixed["SD"], fp64["SD"])),
+            "displacement_rel": disp_err(mixed["Xp"], fp64["Xp"], x0)}
+
+
+ERR_FIELDS = ("PXg", "Mg", "SM", "SD", "Xp", "VXp")
+
+
+def run_to(s, total: int) -> None:
+    """Advance a context to step `total` (graph replay) and wait for it."""
+    done = int(s.scalars()["istep"])
+    if total > done:
+        s.run(total - done, graph=True)
+    s.sync()
+
+
 def measured_peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -184,6 +216,45 @@ def kernel_bytes(kernel: str, np_: int, nn_active: float, usf: bool = True) -> f
     if kernel == "permute":
         return np_ * 2 * (6 * 8 + 6 * 8 + 16 * 4 + 1 + 2 + 2 + 4)
     return np_ * 100.0
+
+
+def profiled_fp64_ops(workload: str, kernel: str, particles: int):
+    """Executed FP64 operations per launch of an FP64-form kernel (adds and
+    multiplies count 1, fused multiply-adds 2), from one ncu capture
+    summarised in profiles/ (lines 'fp64_ops: <workload> <kernel> <ops>
+    <particles>'), scaled to this run's particle count; None without one."""
+    import glob
+    import re
+
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for line in f:
+                m = re.match(r"fp64_ops:\s+(\S+)\s+(\S+)\s+([0-9.eE+]+)\s+([0-9]+)", line.strip())
+                if m and m.group(1) == workload and m.group(2) == kernel:
+                    return float(m.group(3)) * particles / float(m.group(4))
+    return None
+
+
+def fp64_roofline(args, device: int, kernels: list, steps: int, npart: int) -> dict:
+    """The FP64 forms' ceiling is the FP64 pipe: the measured FMA rate of
+    this device (mpm_fp64_ceiling) and, per FP64 kernel, its executed FP64
+    flops per launch (ncu capture in profiles/) over its event-timed
+    duration."""
+    import mpm3d_gb300 as m
+
+    ceil = m.fp64_ceiling(device)
+    peak = ceil["fp64_tflops"]
+    per = {}
+    for k in kernels:
+        if not k["launches"]:
+            continue
+        avg_ms = k["total_ms"] / k["launches"]
+        ops = profiled_fp64_ops(args.workload, k["kernel"], npart)
+        ach = ops / (avg_ms / 1e3) / 1e12 if ops else None
+        per[k["kernel"]] = {"ms_per_step": round(k["total_ms"] / steps, 4),
+                            "fp64_tflops": ach, "frac": (ach / peak) if ach else None}
+    return {"bound": "fp64", "unit": "TFLOP/s", "peak": peak, "peak_source": "measured (mpm_fp64_ceiling)",
+            "ddiv_per_s": ceil["ddiv_per_s"], "kernels": per}
 
 
 def profiled_traffic(workload: str, kernel: str, particles: int):
@@ -245,6 +316,13 @@ def aggregate_rate(units_per_rank: float, world: int, steps: int, ms_max: float)
     return units_per_rank * world * steps / (ms_max / 1e3)
 
 
+def workload_config(args, npart: int, grid_nodes: int, world: int) -> dict:
+    """The config object of both arms (the same workload, so the same dict)."""
+    return {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
+            "grid_nodes": grid_nodes, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (no flush)"}
+
+
 def run_ours(args) -> dict:
     import numpy as np
     import mpm3d_gb300 as m
@@ -264,6 +342,8 @@ def run_ours(args) -> dict:
 
     results = {}
     states = {}
+    ctxs = {}
+    x0 = deck.particles()["Xp"]
     for form in (("mixed",) if args.no_fp64 else ("fp64", "mixed")):
         s = m.MpmStep(deck, precision=form, device=local)
         s.run(args.warmup, graph=True)
@@ -279,19 +359,41 @@ def run_ours(args) -> dict:
         barrier()
         results[form] = {"ms": ms, "clocks": clocks, "device_bytes": s.device_bytes(),
                          "alg_bytes_step": s.algorithmic_bytes(), "scalars": s.scalars()}
-        states[form] = {f: s.download(f) for f in ("PXg", "Mg", "SM", "SD", "Xp", "VXp")}
+        states[form] = {f: s.download(f) for f in ERR_FIELDS}
         # per-kernel timing over a second, profiled run of the same length
         s.profile(True)
         s.time_steps(args.steps, graph=True)
         results[form]["kernels"] = s.kernel_stats()
         s.profile(False)
-        s.close()
+        ctxs[form] = s
     err = None
     if "fp64" in states:
-        err = {"nodal_momentum_rel": rel_err(states["mixed"]["PXg"], states["fp64"]["PXg"]),
-               "particle_stress_rel": max(rel_err(states["mixed"]["SM"], states["fp64"]["SM"]),
-                                          rel_err(states["mixed"]["SD"], states["fp64"]["SD"])),
-               "position_rel": rel_err(states["mixed"]["Xp"], states["fp64"]["Xp"])}
+        err = dict(form_errors(states["mixed"], states["fp64"], x0), steps=args.warmup + args.steps)
+    # the FP64 form with CUDA's libm and contraction (within 1e-10 of the
+    # oracle on glibc): the faster of the two plain FP64 forms
+    native = None
+    if not args.no_fp64:
+        s = m.MpmStep(deck, precision="native", device=local)
+        s.run(args.warmup, graph=True)
+        s.sync()
+        barrier()
+        ms_n = max_over_ranks(s.time_steps(args.steps, graph=True))
+        s.close()
+        native = {"value": aggregate_rate(npart, world, args.steps, ms_n), "ms_per_step": ms_n / args.steps}
+    # error at the workload's own length: both forms advanced from the same
+    # deck to the same step, outside the timed regions
+    target_c2 = None
+    if "fp64" in ctxs and args.target_steps > 0:
+        t0 = time.perf_counter()
+        fin = {}
+        for form in ("fp64", "mixed"):
+            run_to(ctxs[form], args.target_steps)
+            fin[form] = {f: ctxs[form].download(f) for f in ERR_FIELDS}
+        target_c2 = {"steps": args.target_steps,
+                     "max_error": form_errors(fin["mixed"], fin["fp64"], x0),
+                     "wall_s": round(time.perf_counter() - t0, 1)}
+    for c in ctxs.values():
+        c.close()
 
     # end to end through the C ABI from host buffers: the deck's particle
     # arrays and the result buffers are page-locked once, before the timed
@@ -336,12 +438,14 @@ def run_ours(args) -> dict:
         "vs_baseline": None,
         "dtype": "f32 particle / f64 grid (mixed)",
         "data": "synthetic (seeded deck generator)",
-        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
-                   "grid_nodes": int(mixed["scalars"]["nb_gridnode"]), "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (no flush)", "graph": True},
+        "config": workload_config(args, npart, int(mixed["scalars"]["nb_gridnode"]), world),
+        "graph": True,
         "fp64": ({"value": fp64_value, "ms_per_step": fp64["ms"] / args.steps, "dtype": "f64",
                   "parity": "bit-identical to the CPU oracle (tests/test_gpu_parity.py)",
-                  "speedup_mixed_over_fp64": value / fp64_value} if fp64 else None),
+                  "speedup_mixed_over_fp64": value / fp64_value,
+                  "native": native,
+                  "speedup_mixed_over_fp64_native": value / native["value"] if native else None}
+                 if fp64 else None),
         "error_vs_fp64": err,
         "e2e": {"value": npart * world * args.steps / t_e2e, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
@@ -356,8 +460,20 @@ def run_ours(args) -> dict:
         "gpu_launches": sum(k["launches"] for k in mixed["kernels"]),
         "clocks": mixed["clocks"],
     }
+    target = {}
+    if target_c2 is not None:
+        fastest = max(fp64_value, native["value"]) if native else fp64_value
+        target[args.workload] = dict(target_c2, ratio_mixed_over_fp64=value / fastest,
+                                    fp64_form_compared="fastest of strict / native",
+                                    error_reference="FP64 strict form (bit-identical to the oracle)")
+    if fp64 is not None:
+        line["fp64"]["roofline"] = fp64_roofline(args, local, fp64["kernels"], args.steps, npart)
     if world == 1 and args.serve_scenes > 0:
-        line["serving"] = run_serving(args, local)
+        line["serving"], target_c4 = run_serving(args, local)
+        if target_c4 is not None:
+            target["serving_scenes"] = target_c4
+    if target:
+        line["target"] = target
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(text, args.cpu_steps, npart)
     rep.close()
@@ -384,7 +500,59 @@ def run_serving(args, device: int) -> dict:
     out = {"fifo": serve_scenes(args, device, dks, nps, arrivals, "fifo", 0)}
     if args.serve_cap > 0:
         out["shortest_capped"] = serve_scenes(args, device, dks, nps, arrivals, "shortest", args.serve_cap)
-    return out
+    target = None
+    if args.target_stride > 0:
+        target = serving_vs_fp64(args, device, dks, nps, out["fifo"]["particle_steps_per_s"])
+    return out, target
+
+
+def serving_vs_fp64(args, device: int, dks, nps, served_rate: float) -> dict:
+    """The serving scenes through the plain FP64 forms: every target_stride-th
+    scene of the stream, one context per scene, run for the scenes' step
+    count (CUDA events, graph replay); the FP64 rate of the scene mix is the
+    sampled particle-steps over the summed FP64 time. The same scenes run
+    alone in the mixed form (bit-identical to their results in the batch,
+    tests/test_gpu_batch.py) give the per-scene error against the FP64 strict
+    form after the full step count."""
+    import numpy as np
+    import mpm3d_gb300 as m
+
+    idx = list(range(0, len(dks), args.target_stride))
+    steps = args.serve_steps
+    work, t_strict, t_native = 0.0, 0.0, 0.0
+    worst = {"nodal_momentum_rel": 0.0, "particle_stress_rel": 0.0, "displacement_rel": 0.0}
+    per_scene = []
+    t0 = time.perf_counter()
+    for k in idx:
+        d = dks[k]
+        x0 = d.particles()["Xp"]
+        f = m.MpmStep(d, precision="fp64", device=device)
+        t_strict += f.time_steps(steps, graph=True)
+        f.sync()
+        ref = {fl: f.download(fl) for fl in ERR_FIELDS}
+        f.close()
+        nat = m.MpmStep(d, precision="native", device=device)
+        t_native += nat.time_steps(steps, graph=True)
+        nat.close()
+        mx = m.MpmStep(d, precision="mixed", device=device)
+        mx.run(steps, graph=True)
+        mx.sync()
+        got = {fl: mx.download(fl) for fl in ERR_FIELDS}
+        mx.close()
+        e = form_errors(got, ref, x0)
+        per_scene.append([int(nps[k])] + [float("%.3g" % e[q]) for q in worst])
+        for q in worst:
+            worst[q] = max(worst[q], e[q])
+        work += float(nps[k]) * steps
+    strict_rate = work / (t_strict / 1e3)
+    native_rate = work / (t_native / 1e3)
+    fastest = max(strict_rate, native_rate)
+    return {"scenes_sampled": len(idx), "of_scenes": len(dks), "stride": args.target_stride, "steps": steps,
+            "fp64_strict_particle_steps_per_s": strict_rate, "fp64_native_particle_steps_per_s": native_rate,
+            "served_particle_steps_per_s": served_rate, "ratio_served_over_fp64": served_rate / fastest,
+            "fp64_form_compared": "fastest of strict / native", "max_error": worst,
+            "error_reference": "FP64 strict form, each scene alone",
+            "per_scene_np_mom_stress_disp": per_scene, "wall_s": round(time.perf_counter() - t0, 1)}
 
 
 def serve_scenes(args, device: int, dks, nps, arrivals, policy: str, cap: int) -> dict:
@@ -450,7 +618,7 @@ def _replica(args_tuple):
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
-    return time.perf_counter() - t0, o.nb_particle, done
+    return time.perf_counter() - t0, o.nb_particle, done, o.nb_gridnode
 
 
 def run_reference(args) -> dict:
@@ -480,8 +648,7 @@ def run_reference(args) -> dict:
         "steps": min(done), "warmup": warm, "ms_per_step": t / max(1, min(done)) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded deck generator)",
-        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][0]}", "particles": npart,
-                   "parallelism": f"{cores} CPU replicas"},
+        "config": workload_config(args, npart, int(res[0][3]), int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{min(done)}-{max(done)} timed steps per replica (of {steps} asked, "
                                    f"{args.ref_budget:.0f} s budget) after {warm} warm-up steps, "
@@ -511,6 +678,10 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate (scenes/s)")
     ap.add_argument("--serve-cap", type=int, default=2_000_000,
                     help="resident particle cap of the shortest-work-first serving run (0 = FIFO run only)")
+    ap.add_argument("--target-steps", type=int, default=5000,
+                    help="mixed-vs-FP64 error after this many steps of the workload (0 = skip)")
+    ap.add_argument("--target-stride", type=int, default=8,
+                    help="serving scenes also run through the FP64 forms: every n-th scene (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -139,7 +139,9 @@ int mpm_upload(mpm_ctx* ctx, int field, const double* in);
  * failure (message in mpm_last_error); mpm_host_register locks an existing
  * buffer in place (undone by mpm_host_unregister, before the buffer is
  * freed); mpm_deck_pin locks (on != 0) or unlocks the particle arrays of a
- * deck, which mpm_create then uploads from. */
+ * deck, which mpm_create then uploads from. The locks are portable: they
+ * count as page-locked for every device of the process, whichever device is
+ * current when they are taken. */
 void* mpm_host_alloc(int64_t bytes);
 void mpm_host_free(void* p);
 int mpm_host_register(void* p, int64_t bytes);
@@ -301,6 +303,19 @@ int mpm_serve_plan(const mpm_serve_config* cfg, int nqueued, const int64_t* np, 
                    const int64_t* bytes, int resident_scenes, int64_t resident_particles, int64_t resident_bytes,
                    int* admit, int* reject, int* nreject);
 
+/* ------------------------------------------------ FP64 pipe ceiling */
+/* No counterpart in the reference: the measured FP64 arithmetic ceiling of a
+ * device, the roofline of the FP64 forms (their kernels are bound by the FP64
+ * pipe, not by HBM). A kernel of independent FP64 fused multiply-add chains
+ * and one of FP64 divisions fill every SM; each is timed with CUDA events
+ * (best of `repeats` launches after one warm-up launch). Outputs (any may be
+ * NULL): dfma_per_s -- FP64 FMA instructions per second summed over the
+ * device's threads (x 2 for flop/s); ddiv_per_s -- FP64 divisions (the
+ * compiler's correctly rounded division) per second. Changes no device
+ * setting; allocates 8 bytes of device memory per call for the kernels'
+ * results (so that they cannot be optimised away). */
+int mpm_fp64_ceiling(int device, int repeats, double* dfma_per_s, double* ddiv_per_s);
+
 /* ------------------------------------------------ allocation-free call */
 /* No counterpart in the reference: an extra entry point for hosts that may not
  * allocate device memory inside a solver call (a Fortran code passing device
@@ -320,8 +335,9 @@ int mpm_serve_plan(const mpm_serve_config* cfg, int nqueued, const int64_t* np, 
  * device current), so make the first call before any stream capture. All
  * calls share the array: calls that overlap on the GPU (different streams or
  * threads at the same time) race and must be serialised by the caller.
- * It uses the block tree and combine order of the context path's calcEnergy
- * (mpm_step_phase MPM_PHASE_CALC_ENERGY) on the same arrays. */
+ * It uses the block tree and combine order of the FP64 forms' calcEnergy
+ * (mpm_step_phase MPM_PHASE_CALC_ENERGY) and gives the same bits on the same
+ * arrays. */
 #define MPM_NOALLOC_MAX_PARTICLES (1LL << 27)
 int mpm_energy_reduce_noalloc(const double* vxp, const double* mass, const double* ie, int64_t np,
                               double* out6, void* stream);

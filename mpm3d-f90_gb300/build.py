@@ -7,7 +7,8 @@ Outputs (all git-ignored, built in-tree so that they travel with the tree):
   oracle/_build/mpm3d_oracle               -- oracle command-line driver
 
 Translation units are compiled in parallel; the FP64 step is compiled with
---fmad=false (no fused multiply-add contraction) and the host C code with
+--fmad=false (no fused multiply-add contraction) and the host C code (the
+oracle included, which is also the timed CPU baseline) with -O3
 -ffp-contract=off, so that both sides round every product and sum.
 """
 from __future__ import annotations
@@ -29,7 +30,7 @@ ORACLE_BUILD = os.path.join(ORACLE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                       "-Xcompiler", "-ffp-contract=off", "-I" + INC, "-I" + CSRC]
-CC_COMMON = ["-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-D_POSIX_C_SOURCE=200809L",
+CC_COMMON = ["-O3", "-fPIC", "-std=c11", "-ffp-contract=off", "-D_POSIX_C_SOURCE=200809L",
              "-Wall", "-I" + INC, "-I" + CSRC]
 
 
@@ -74,6 +75,7 @@ def build_library(force: bool = False) -> str:
         ("mpm_setup.cu", []),
         ("mpm_batch.cu", []),
         ("mpm_serve.cu", []),
+        ("mpm_probe.cu", []),
     ]
     jobs = []
     objs = []

@@ -918,7 +918,7 @@ void* mpm_host_alloc(int64_t bytes) {
     return nullptr;
   }
   void* p = nullptr;
-  cudaError_t e = cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault);
+  cudaError_t e = cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocPortable);
   if (e != cudaSuccess) {
     set_err(nullptr, MPM_ERR_OOM, "page-locked allocation of %lld bytes: %s", (long long)bytes, cudaGetErrorString(e));
     return nullptr;
@@ -932,7 +932,7 @@ void mpm_host_free(void* p) {
 
 int mpm_host_register(void* p, int64_t bytes) {
   if (!p || bytes <= 0) return set_err(nullptr, MPM_ERR_ARG, "bad argument");
-  cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterDefault);
+  cudaError_t e = cudaHostRegister(p, (size_t)bytes, cudaHostRegisterPortable);
   if (e != cudaSuccess) return set_err(nullptr, MPM_ERR_CUDA, "host register: %s", cudaGetErrorString(e));
   return MPM_OK;
 }
@@ -1110,6 +1110,13 @@ static int snapshot_load_mixed(mpm_ctx* c, const char* path) {
   int64_t n = 0;
   int r = MPM_OK;
   std::vector<unsigned char> img;
+  // the image size this context expects; negative when the context has no
+  // committed scene, so no file size can match it
+  const long long want = mpm::mpm_batch_scene_restart_bytes(c->batch, c->batch_scene);
+  if (want < 0) {
+    fclose(f);
+    return set_err(c, MPM_ERR_STATE, "the context holds no restartable scene");
+  }
   if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, kSnapMagic, 8) != 0) {
     r = set_err(c, MPM_ERR_IO, "%s is not a snapshot", path);
   } else if (h.precision != c->precision || h.np != c->g.np || h.nn != c->g.nn || h.ncell != c->g.ncell ||
@@ -1117,7 +1124,7 @@ static int snapshot_load_mixed(mpm_ctx* c, const char* path) {
     r = set_err(c, MPM_ERR_STATE, "snapshot of another deck or precision");
   } else if (fread(&n, sizeof n, 1, f) != 1) {
     r = set_err(c, MPM_ERR_IO, "truncated snapshot");
-  } else if (n != mpm::mpm_batch_scene_restart_bytes(c->batch, c->batch_scene)) {
+  } else if (n != want) {
     r = set_err(c, MPM_ERR_STATE, "snapshot image of %lld bytes does not fit this context", (long long)n);
   } else {
     try {

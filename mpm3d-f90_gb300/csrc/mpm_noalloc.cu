@@ -10,10 +10,11 @@
 // inputs and the output; the block partial sums live in a file-scope
 // __device__ array of fixed size instead of memory the library allocates.
 //
-// The arithmetic is that of the step's calcEnergy reduction (block tree of
-// 256 threads, min(1024, ceil(np/256)) blocks, block partials combined by the
-// last block in the same fixed order), so both give the same bits for the
-// same inputs.
+// The arithmetic is that of the FP64 forms' calcEnergy reduction (block tree
+// of 256 threads, min(1024, ceil(np/256)) blocks, block partials combined by
+// the last block in the same fixed order, both compiled without multiply-add
+// contraction), so both give the same bits for the same inputs. (The mixed
+// form reduces per scene in its own order.)
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -3,6 +3,7 @@
  * (MPM3D.f90:62-160) over the C ABI of libmpm3d_gpu.
  *
  *   mpm3d_gpu deck.mpm [--precision fp64|native|mixed] [--steps N] [--report K] [--no-output]
+ *             [--pinned] [--dump FILE]
  *
  * It writes the reference's result files next to the deck (job = the deck
  * path without its extension): <job>_curv.dat, EnergyPlot.dat and
@@ -16,6 +17,13 @@
  * and CurrentTime > 100; MPM3D.f90:152-158). It reports per K steps like the
  * reference's progress line and ends with the "time per particle cycle" of
  * MPM3D.f90:267, measured around the device step loop.
+ *
+ * --pinned follows the Fortran shim's memory sequence: the deck's particle
+ * arrays page-locked around mpm_create (mpm_deck_pin on, create, pin off)
+ * and the final read-back into a page-locked buffer from mpm_host_alloc,
+ * released with mpm_host_free. --dump FILE writes the final Xp (3), VXp (3),
+ * SM and SD (6) as raw doubles, component-major, in the input particle
+ * order.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -65,7 +73,8 @@ int main(int argc, char** argv) {
   }
   int precision = MPM_FP64_STRICT;
   long steps = -1, report = 100;
-  int write_output = 1;
+  int write_output = 1, pinned = 0;
+  const char* dump = NULL;
   for (int i = 2; i < argc; ++i) {
     if (!strcmp(argv[i], "--precision") && i + 1 < argc) {
       ++i;
@@ -76,6 +85,10 @@ int main(int argc, char** argv) {
       report = atol(argv[++i]);
     } else if (!strcmp(argv[i], "--no-output")) {
       write_output = 0;
+    } else if (!strcmp(argv[i], "--pinned")) {
+      pinned = 1;
+    } else if (!strcmp(argv[i], "--dump") && i + 1 < argc) {
+      dump = argv[++i];
     }
   }
   char err[256] = {0};
@@ -86,7 +99,15 @@ int main(int argc, char** argv) {
     return 1;
   }
   mpm_ctx* c = NULL;
+  if (pinned && (st = mpm_deck_pin(d, 1))) {
+    fprintf(stderr, "deck pin error %d: %s\n", st, mpm_last_error(NULL));
+    return 1;
+  }
   st = mpm_create(d, precision, -1, &c);
+  if (pinned) {
+    int st2 = mpm_deck_pin(d, 0);
+    if (!st && st2) st = st2;
+  }
   if (st) {
     fprintf(stderr, "create error %d: %s\n", st, mpm_last_error(NULL));
     return 1;
@@ -157,6 +178,29 @@ int main(int argc, char** argv) {
   const double np = (double)mpm_nb_particle(c);
   printf("** steps %ld  elapsed %.4f s\n** Time per particle cycle: %12.4f nanoseconds\n", n, t,
          1e9 * t / np / (double)(n > 0 ? n : 1));
+  if (dump) {
+    static const int fields[4] = {MPM_P_XP, MPM_P_VXP, MPM_P_SM, MPM_P_SD};
+    const int64_t npi = mpm_nb_particle(c);
+    const int64_t bytes = (int64_t)sizeof(double) * 6 * npi; /* the largest field */
+    double* buf = pinned ? (double*)mpm_host_alloc(bytes) : (double*)malloc((size_t)bytes);
+    FILE* f = buf ? fopen(dump, "wb") : NULL;
+    if (!f) {
+      fprintf(stderr, "cannot write %s\n", dump);
+      return 1;
+    }
+    for (int k = 0; k < 4 && !st; ++k) {
+      const int64_t cnt = (int64_t)mpm_field_components(fields[k]) * npi;
+      st = mpm_download(c, fields[k], buf);
+      if (!st && fwrite(buf, sizeof(double), (size_t)cnt, f) != (size_t)cnt) st = MPM_ERR_IO;
+    }
+    fclose(f);
+    if (pinned) mpm_host_free(buf);
+    else free(buf);
+    if (st) {
+      fprintf(stderr, "dump error %d: %s\n", st, mpm_last_error(c));
+      return 1;
+    }
+  }
   mpm_output_close(out);
   mpm_destroy(c);
   mpm_deck_free(d);

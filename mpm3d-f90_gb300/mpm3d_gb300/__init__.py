@@ -114,6 +114,7 @@ def library() -> ctypes.CDLL:
         "mpm_algorithmic_bytes": (i, [vp, P(d)]),
         "mpm_device_bytes": (i64, [vp]),
         "mpm_energy_reduce_noalloc": (i, [vp, vp, vp, i64, vp, vp]),
+        "mpm_fp64_ceiling": (i, [i, i, P(d), P(d)]),
         "mpm_batch_create": (i, [i, P(vp)]),
         "mpm_batch_destroy": (None, [vp]),
         "mpm_batch_add": (i, [vp, vp, i, P(i)]),
@@ -200,6 +201,17 @@ def _out_buffer(out: Optional[np.ndarray], n: int) -> np.ndarray:
     if out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
         raise MpmError(1, f"out must be a contiguous float64 array of {n} values")
     return out.reshape(n)
+
+
+def fp64_ceiling(device: int = 0, repeats: int = 5) -> dict:
+    """Measured FP64 arithmetic ceiling of a device (mpm_fp64_ceiling): FP64
+    fused multiply-adds per second (flop/s = 2 x) and FP64 divisions per
+    second, each the best of `repeats` timed launches."""
+    fma, div = ctypes.c_double(), ctypes.c_double()
+    st = library().mpm_fp64_ceiling(int(device), int(repeats), ctypes.byref(fma), ctypes.byref(div))
+    if st:
+        raise MpmError(st, "FP64 ceiling probe failed")
+    return {"dfma_per_s": fma.value, "fp64_tflops": 2.0 * fma.value / 1e12, "ddiv_per_s": div.value}
 
 
 def pinned_empty(shape, dtype=np.float64) -> np.ndarray:

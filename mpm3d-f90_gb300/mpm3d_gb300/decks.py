@@ -290,18 +290,35 @@ def contact_blocks(shape: Optional[str] = None, scheme: str = "usf", fricfa: flo
     return w.text()
 
 
+# Grid and run settings of the two published Cook-membrane resolutions
+# (VolumetricLockingEx/Cook_membrane/*5776p and *23072p): cell size, spans per
+# variant, time-step scale, damping factor and the number formats of the
+# particle mass and the edge loads. Other spacings use the 5776 settings.
+_COOK_LAYOUT = {
+    0.5: dict(dcell=1.0, dtscale="0.9", damp="0.3", mass_fmt="%.6f", load_fmt="%.6f",
+              spans={"mpm": ((0, 50), (0, 62), (-0.5, 0.5)), "gimp": ((-1, 50), (-1, 62), (-1, 1)),
+                     "bimp": ((-1, 50), (-1, 62), (-1, 1)), "sgmp": ((-1, 50), (-1, 62), (-0.5, 0.5))}),
+    0.25: dict(dcell=0.5, dtscale="0.8", damp="0.2", mass_fmt="%.6g", load_fmt="%.5g",
+               spans={"mpm": ((0, 48.5), (0, 61), (-0.25, 0.25)), "gimp": ((-0.5, 48.5), (-0.5, 61), (-0.5, 0.5)),
+                      "bimp": ((-0.5, 48.5), (-0.5, 61), (-0.5, 0.5)),
+                      "sgmp": ((-0.5, 48.5), (-0.5, 61), (-0.25, 0.25))}),
+}
+
+
 def cook_membrane(variant: str = "mpm", spacing: float = 0.5, young: float = 70.0, nu: float = 0.499,
-                  rho: float = 1.0, total_load: float = 1.0) -> str:
+                  rho: float = 1.0, total_load: float = 1.0, extra: Iterable[str] = ()) -> str:
     """Cook's tapered panel (corners (0,0), (48,44), (48,60), (0,44), unit
     thickness, plane strain through roller z faces), clamped at x = 0 and
     loaded by a vertical shear on the x = 48 edge, run quasi-statically (load
-    ramp 'QuLo 15', mass damping 'Damp 0.3'); neo-Hookean, MUSL.
+    ramp 'QuLo 15', mass damping 'Damp'); neo-Hookean, MUSL.
 
     variant: 'mpm' (linear), 'gimp', 'bimp' (B-spline) or 'sgmp'. Particles
-    sit on a regular lattice clipped to the panel, rows by increasing y; the
-    particle mass and the edge loads are written with six decimals (mass =
-    area/n; the edge particles carry 1/(m-1) of the load, the two corner
-    particles half of that)."""
+    sit on a regular lattice clipped to the panel, rows by increasing y
+    (mass = area/n; the edge particles carry 1/(m-1) of the load, the two
+    corner particles half of that). Spacing 0.5 and 0.25 give the two
+    published resolutions (5776 and 23072 particles: cell 1 and 0.5, their
+    spans, time-step scale, damping factor and number formats); extra:
+    further keyword lines (output settings)."""
     ds = spacing
     xs = (np.arange(int(round(48 / ds))) + 0.5) * ds
     ys = (np.arange(int(round(60 / ds))) + 0.5) * ds
@@ -313,21 +330,22 @@ def cook_membrane(variant: str = "mpm", spacing: float = 0.5, young: float = 70.
     xyz = np.array(pts)
     n = xyz.shape[0]
     area = 48.0 * (44.0 + 16.0) / 2.0
-    mass = "%.6f" % (rho * area / n)
-    spans = {"mpm": ((0, 50), (0, 62), (-0.5, 0.5)), "gimp": ((-1, 50), (-1, 62), (-1, 1)),
-             "bimp": ((-1, 50), (-1, 62), (-1, 1)), "sgmp": ((-1, 50), (-1, 62), (-0.5, 0.5))}[variant]
+    lay = _COOK_LAYOUT.get(spacing, _COOK_LAYOUT[0.5])
+    mass = lay["mass_fmt"] % (rho * area / n)
     w = DeckWriter(f"Cook membrane, neo-Hookean, {variant}")
     w.kw("nmat 1")
-    w.head += _grid_lines(spans, 1.0)
+    w.head += _grid_lines(lay["spans"][variant], lay["dcell"])
     w.kw("fixe 1 0 0 0 2 2")
-    w.kw("dtsc 0.9")
+    w.kw(f"dtsc {lay['dtscale']}")
     w.kw("endt 30")
     w.kw("musl on")
     if variant != "mpm":
         w.kw(variant)
     w.kw("smoo")
     w.kw("QuLo 15")
-    w.kw("Damp 0.3")
+    w.kw(f"Damp {lay['damp']}")
+    for e in extra:
+        w.kw(e)
     w.kw(f"curv disy {n}")
     w.kw("mate")
     w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
@@ -341,7 +359,7 @@ def cook_membrane(variant: str = "mpm", spacing: float = 0.5, young: float = 70.
     loads = ["load"]
     for k, i in enumerate(right):
         f = per * (0.5 if k in (0, len(right) - 1) else 1.0)
-        loads.append("part %d 0 %.6f 0" % (i + 1, f))
+        loads.append(("part %d 0 " + lay["load_fmt"] + " 0") % (i + 1, f))
     loads.append("endl")
     w.tail += loads
     return w.text()
@@ -350,6 +368,8 @@ def cook_membrane(variant: str = "mpm", spacing: float = 0.5, young: float = 70.
 # Published tip vertical displacement (m) of the Cook membrane with 5776
 # particles (VolumetricLockingEx/ExamplesResults.pdf, Table 1), by variant.
 COOK_TIP_PUBLISHED = {"mpm": 0.2489, "gimp": 0.2512, "bimp": 0.2620, "sgmp": 0.2678}
+# The same with 23072 particles (spacing 0.25, cell 0.5; same table).
+COOK_TIP_PUBLISHED_23072 = {"mpm": 0.2692, "gimp": 0.2688, "bimp": 0.2711, "sgmp": 0.2739}
 
 
 def _fast_points(ids_start: int, mat: int, mass: float, xyz: np.ndarray) -> str:

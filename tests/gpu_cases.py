@@ -1,7 +1,10 @@
 """Parity cases shared by the GPU tests: small decks that the oracle runs in
-seconds, each exercising one shape family / scheme / material path."""
+seconds, each exercising one shape family / scheme / material path; and the
+strict-form comparison the parity tests share."""
 import sys
 import os
+
+import numpy as np
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "mpm3d-f90_gb300"))
 
@@ -47,3 +50,54 @@ CASES = {
         velocity=(0.0, 0.0, 0.0), rho=1630.0, dtscale=0.1, gravity=None, scheme="musl",
         extra=["deto 0 0 0"]), 60),
 }
+
+
+PARTICLE_FIELDS = ["Xp", "XX", "VXp", "VOL", "SM", "Seqv", "SD", "epeff", "sig_y", "ie", "q",
+                   "celsius_t", "failure", "icell", "XN", "cp", "Spre", "PK"]
+GRID_FIELDS = ["Mg", "PXg", "FXg"]
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = max(np.max(np.abs(b)), 1e-300) if b.size else 1.0
+    return float(np.max(np.abs(a - b)) / scale) if a.size else 0.0
+
+
+def run_pair(gpu_mod, oracle_mod, text, steps, precision, libm):
+    """The GPU form `precision` and the oracle on libm `libm`, both advanced
+    `steps` steps from the same deck text."""
+    deck = gpu_mod.Deck.parse(text)
+    g = gpu_mod.MpmStep(deck, precision=precision, device=0)
+    o = oracle_mod.Oracle(deck_text=text, libm=libm)
+    g.run(steps, graph=False)
+    g.sync()
+    o.run(steps)
+    return g, o
+
+
+def check_strict(g, o, name, steps):
+    """The FP64 strict form against the oracle on the project libm: the same
+    step count, time and DT; every grid and particle field bit-identical; the
+    sums over particles (energies, momentum, contact force), which the GPU
+    reduces in a fixed tree and the oracle sequentially, equal to rounding."""
+    gs, os_ = g.scalars(), o.scalars()
+    assert gs["istep"] == os_["istep"] == steps
+    fg, fo = g.contact_force(), o.contact_force()
+    assert np.all(np.abs(fg - fo) <= 1e-12 * max(np.abs(fo).max(), 1e-300)), (fg, fo)
+    assert gs["DT"] == os_["DT"], (gs["DT"], os_["DT"])
+    assert gs["CurrentTime"] == os_["CurrentTime"]
+    bad = []
+    for f in GRID_FIELDS + PARTICLE_FIELDS:
+        a, b = g.download(f), o.download(f)
+        if not np.array_equal(a, b):
+            diff = np.argwhere(a != b)
+            bad.append((f, int(diff.shape[0]), rel(a, b)))
+    assert not bad, f"{name}: fields differ from the oracle: {bad}"
+    v = o.download("VXp")
+    mass = o.download("mass")
+    mom_scale = float(np.sum(mass * np.abs(v).max(axis=0)))
+    for k in ("EngKinetic", "EngInternal"):
+        assert abs(gs[k] - os_[k]) <= 1e-12 * max(abs(os_[k]), 1e-300), (k, gs[k], os_[k])
+    for k in ("Momentum_x", "Momentum_y", "Momentum_z"):
+        assert abs(gs[k] - os_[k]) <= 1e-12 * max(mom_scale, 1e-300), (k, gs[k], os_[k])

@@ -11,65 +11,17 @@ pow / log can flip a particle between the elastic and plastic branch. For
 those fields the bar is twice the spread between the oracle on the project
 libm and the oracle on glibc for the same deck and steps.
 """
-import numpy as np
 import pytest
 
-from gpu_cases import CASES
-
-PARTICLE_FIELDS = ["Xp", "XX", "VXp", "VOL", "SM", "Seqv", "SD", "epeff", "sig_y", "ie", "q",
-                   "celsius_t", "failure", "icell", "XN", "cp", "Spre", "PK"]
-GRID_FIELDS = ["Mg", "PXg", "FXg"]
-
-
-def _run_pair(gpu_mod, oracle_mod, text, steps, precision, libm):
-    deck = gpu_mod.Deck.parse(text)
-    g = gpu_mod.MpmStep(deck, precision=precision, device=0)
-    o = oracle_mod.Oracle(deck_text=text, libm=libm)
-    g.run(steps, graph=False)
-    g.sync()
-    o.run(steps)
-    return g, o
-
-
-def _rel(a, b):
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
-    scale = max(np.max(np.abs(b)), 1e-300)
-    return float(np.max(np.abs(a - b)) / scale) if a.size else 0.0
+from gpu_cases import CASES, check_strict, rel as _rel, run_pair as _run_pair
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_strict_bit_identical(gpu_mod, oracle_mod, name):
     make, steps = CASES[name]
-    text = make()
-    g, o = _run_pair(gpu_mod, oracle_mod, text, steps, "fp64", "project")
-    gs, os_ = g.scalars(), o.scalars()
-    assert gs["istep"] == os_["istep"] == steps
-    # the total contact force is summed over nodes in a fixed tree order on the
-    # GPU, node by node on the CPU
-    fg, fo = g.contact_force(), o.contact_force()
-    assert np.all(np.abs(fg - fo) <= 1e-12 * max(np.abs(fo).max(), 1e-300)), (fg, fo)
-    assert gs["DT"] == os_["DT"], (gs["DT"], os_["DT"])
-    assert gs["CurrentTime"] == os_["CurrentTime"]
-    bad = []
-    for f in GRID_FIELDS + PARTICLE_FIELDS:
-        if f == "XN" and "sgmp" in name:
-            pass
-        a, b = g.download(f), o.download(f)
-        if not np.array_equal(a, b):
-            diff = np.argwhere(a != b)
-            bad.append((f, int(diff.shape[0]), _rel(a, b)))
-    assert not bad, f"{name}: fields differ from the oracle: {bad}"
-    # energies are reduced in a fixed tree order on the GPU, sequentially on the
-    # CPU: equal to rounding, measured against the sum of the magnitudes
-    v = o.download("VXp")
-    mass = o.download("mass")
-    mom_scale = float(np.sum(mass * np.abs(v).max(axis=0)))
-    for k in ("EngKinetic", "EngInternal"):
-        assert abs(gs[k] - os_[k]) <= 1e-12 * max(abs(os_[k]), 1e-300), (k, gs[k], os_[k])
-    for k in ("Momentum_x", "Momentum_y", "Momentum_z"):
-        assert abs(gs[k] - os_[k]) <= 1e-12 * max(mom_scale, 1e-300), (k, gs[k], os_[k])
+    g, o = _run_pair(gpu_mod, oracle_mod, make(), steps, "fp64", "project")
+    check_strict(g, o, name, steps)
 
 
 @pytest.mark.gpu

@@ -11,7 +11,6 @@ import pytest
 from gpu_cases import CASES
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
 
 
 def test_project_libm_accuracy(built):
@@ -81,9 +80,8 @@ def test_p2g_conserves_mass_and_momentum(oracle_mod, name):
             assert abs(px[c].sum() - tot) <= 1e-11 * (np.abs(mass * v[c]).sum() + 1e-300)
 
 
-def test_reference_decks_parse_like_generated(gpu_mod):
-    if not os.path.isdir(REF):
-        pytest.skip("reference tree not present")
+def test_reference_decks_parse_like_generated(gpu_mod, reference_tree):
+    REF = reference_tree
     from mpm3d_gb300 import decks
 
     paths = {"mpm": "MPM5776p/Cookmo_MPM", "gimp": "GIMP5776p/Cookmo_Gimp", "bimp": "BSMPM5776p/Cookmo_Bimp",
@@ -101,9 +99,8 @@ def test_reference_decks_parse_like_generated(gpu_mod):
         assert a.flags == b.flags
 
 
-def test_reference_decks_run(oracle_mod):
-    if not os.path.isdir(REF):
-        pytest.skip("reference tree not present")
+def test_reference_decks_run(oracle_mod, reference_tree):
+    REF = reference_tree
     for deck in ("Data/Taylor.mpm", "Data/Slopefail.mpm", "Data/Deto1k.mpm", "Data/SGDeto1k.mpm",
                  "VolumetricLockingEx/DamBreak/SGMPM/Dam_SGR2.mpm"):
         o = oracle_mod.Oracle(deck_path=f"{REF}/{deck}")

@@ -4,8 +4,13 @@ It serves hosts that cannot allocate device memory inside a solver call: the
 caller owns every device array and passes pointers; the entry point's own
 scratch is a fixed __device__ array. This test calls it through the C ABI on
 device arrays the test allocates itself, twice in a row (the second call must
-not see the first call's leftovers), and checks both results against the
-context path (the step's calcEnergy reduction) on the same particle state.
+not see the first call's leftovers), and checks both results bit for bit
+against the context path (the FP64 strict form's calcEnergy reduction) on the
+same particle state. Two sizes: the small Taylor bar (66 blocks) and a block
+of 327,680 particles, which reaches the 1024-block cap, so that every thread
+loops over several particles and the last block combines four block partials
+per thread -- the paths that use the whole partial-sum area of the scratch
+array and its arrival counter.
 The file name makes pytest collect it last.
 """
 import ctypes
@@ -42,33 +47,43 @@ def _to_device(rt, a):
     return p
 
 
-@pytest.mark.gpu
-def test_noalloc_energy_matches_context(gpu_mod):
+def _decks():
     from mpm3d_gb300 import decks
 
+    return {
+        "taylor_bar_2080": decks.taylor_bar(dp=8e-4),
+        "elastic_block_327680": decks.generic_block("1 elas 1000 1e7 0.3", counts=(80, 64, 64),
+                                                    velocity=(1.0, -2.0, -5.0)),
+    }
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["taylor_bar_2080", "elastic_block_327680"])
+def test_noalloc_energy_matches_context(gpu_mod, case):
     lib = gpu_mod.library()
     rt = _cudart()
-    deck = gpu_mod.Deck.parse(decks.taylor_bar(dp=8e-4))
+    deck = gpu_mod.Deck.parse(_decks()[case])
     step = gpu_mod.MpmStep(deck, precision="fp64", device=0)
-    step.run(5, graph=False)
+    step.run(3, graph=False)
     step.calcEnergy()
     ref = step.scalars()
     vxp, mass, ie = step.download("VXp"), step.download("mass"), step.download("ie")
     np_ = mass.size
+    if case.startswith("elastic_block"):
+        assert np_ > 1024 * 256  # more particles than one pass of the capped grid
     d_v, d_m, d_e = _to_device(rt, vxp), _to_device(rt, mass), _to_device(rt, ie)
     d_out = ctypes.c_void_p()
     assert rt.cudaMalloc(ctypes.byref(d_out), 6 * 8) == 0
-    want = [ref["EngKinetic"], ref["EngInternal"], ref["Momentum_x"], ref["Momentum_y"], ref["Momentum_z"],
-            float(np.max(np.abs(vxp)))]
-    scale = [abs(want[0]), abs(want[1])] + [float(np.sum(mass * np.abs(vxp).max(axis=0)))] * 3 + [want[5]]
+    want = np.array([ref["EngKinetic"], ref["EngInternal"], ref["Momentum_x"], ref["Momentum_y"],
+                     ref["Momentum_z"], float(np.max(np.abs(vxp)))])
     try:
         for call in range(2):
             st = lib.mpm_energy_reduce_noalloc(d_v, d_m, d_e, np_, d_out, None)
             assert st == 0, f"call {call}: status {st}"
             got = np.zeros(6)
             assert rt.cudaMemcpy(got.ctypes.data, d_out, 6 * 8, 2) == 0  # device -> host
-            for k in range(6):
-                assert abs(got[k] - want[k]) <= 1e-12 * max(scale[k], 1e-300), (call, k, got[k], want[k])
+            # the same block tree and combine order as the step's reduction
+            np.testing.assert_array_equal(got, want, err_msg=f"call {call}")
         # sizes beyond the stated maximum are refused before any work
         assert lib.mpm_energy_reduce_noalloc(d_v, d_m, d_e, (1 << 27) + 1, d_out, None) == 1
         assert lib.mpm_energy_reduce_noalloc(d_v, d_m, d_e, 0, d_out, None) == 1
