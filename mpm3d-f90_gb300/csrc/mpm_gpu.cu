@@ -589,7 +589,11 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
 #define CKF(call)                                              \
   if ((e = (call)) != cudaSuccess) { r = cuda_err(c, e, #call); goto fail; }
     CKF(cudaMemcpyAsync(s.xp, d->xp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
-    CKF(cudaMemcpyAsync(s.xx, d->xp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
+    // XX (the position at t + DT) is written by ParticlePositionUpdate for
+    // the particles inside the grid only (update_step.f90:1477, 1515); the
+    // reference's freshly allocated particle list holds 0 until then, which
+    // a particle that starts outside the grid keeps
+    CKF(cudaMemsetAsync(s.xx, 0, sizeof(double) * 3 * np, c->stream));
     CKF(cudaMemcpyAsync(s.vxp, d->vxp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
     CKF(cudaMemcpyAsync(s.fxp, d->fxp, sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream));
     CKF(cudaMemcpyAsync(s.mass, d->mass, sizeof(double) * np, cudaMemcpyHostToDevice, c->stream));

@@ -409,7 +409,12 @@ def serving_scene(rng: np.random.Generator, np_min: int = 2000, np_max: int = 40
         w = DeckWriter("serving scene: soft beam, neo-Hookean, sgmp, musl")
         w.kw("nmat 1")
         lx, ly, lz = nx * dp, ny * dp, nz * dp
-        w.head += _grid_lines(((-h, lx + 2 * h), (0.0, ly), (0.0, lz + 4 * h)), h)
+        # the beam hangs 2 m above the grid floor: the free end of the
+        # softest beams falls about a metre in the 500 steps of a scene, and
+        # must stay inside the grid; SGMP wants one cell of grid beyond the
+        # clamped face and beyond the roller faces
+        z0 = 2.0
+        w.head += _grid_lines(((-h, lx + 2 * h), (-h, ly + h), (0.0, z0 + lz + 2 * h)), h)
         w.kw("dtsc 0.5")
         w.kw("endt 100.0")
         w.kw("musl on")
@@ -417,7 +422,7 @@ def serving_scene(rng: np.random.Generator, np_min: int = 2000, np_max: int = 40
         w.kw("fixe 1 0 2 2 0 0")
         w.kw("mate")
         w.kw(f"1 neoh {f32s(rho)} {f32s(young)} {f32s(nu)}")
-        w.block(1, rho, dp, (0.0, 0.0, 2 * h), (nx, ny, nz))
+        w.block(1, rho, dp, (0.0, 0.0, z0), (nx, ny, nz))
         w.tail += ["load", f"grav 1 0 0 {f32s(-9.81)}", "endl"]
         return w.text(), nx * ny * nz, kind
     # Cook panel (48 x 44..60 m), two particles through the thickness
