@@ -499,6 +499,10 @@ def run_serving(args, device: int) -> dict:
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=len(dks)))
     out = {"fifo": serve_scenes(args, device, dks, nps, arrivals, "fifo", 0)}
     if args.serve_cap > 0:
+        # a resident-particle cap bounds the batch a scene shares the device
+        # with: FIFO with the cap bounds the tail, least-work-first with it
+        # trades the tail for the median
+        out["fifo_capped"] = serve_scenes(args, device, dks, nps, arrivals, "fifo", args.serve_cap)
         out["shortest_capped"] = serve_scenes(args, device, dks, nps, arrivals, "shortest", args.serve_cap)
     target = None
     if args.target_stride > 0:
@@ -559,7 +563,9 @@ def serve_scenes(args, device: int, dks, nps, arrivals, policy: str, cap: int) -
     import numpy as np
     import mpm3d_gb300 as m
 
-    with m.Server(device=device, chunk_steps=25, autotune=True, policy=policy, max_resident_particles=cap) as srv:
+    # the device loop returns when a scene finishes or a submission arrives;
+    # chunk_steps only bounds a loop that neither ends
+    with m.Server(device=device, chunk_steps=500, autotune=True, policy=policy, max_resident_particles=cap) as srv:
         tickets = []
         t0 = time.perf_counter()
         for k, d in enumerate(dks):
@@ -572,6 +578,7 @@ def serve_scenes(args, device: int, dks, nps, arrivals, policy: str, cap: int) -
         wall = time.perf_counter() - t0
         res = [srv.result(t) for t in tickets]
         st = srv.stats()
+        shape = srv.launch_shape()
     lat = np.array([r["latency_ms"] for r in res])
     queue = np.array([r["queue_ms"] for r in res])
     return {
@@ -581,8 +588,8 @@ def serve_scenes(args, device: int, dks, nps, arrivals, policy: str, cap: int) -
         "p50_latency_ms": float(np.percentile(lat, 50)), "p99_latency_ms": float(np.percentile(lat, 99)),
         "mean_queue_ms": float(queue.mean()), "makespan_s": wall,
         "particle_steps_per_s": float(nps.sum() * args.serve_steps / wall),
-        "gpu_busy_frac": st["busy_ms"] / 1e3 / wall, "chunks": int(st["chunks"]),
-        "autotuned_blocks": [int(st["particle_block"]), int(st["node_block"])],
+        "gpu_busy_frac": st["busy_ms"] / 1e3 / wall, "device_loops": int(st["chunks"]),
+        "device_loop": True, "autotuned_launch_shape": shape,
         "peak_resident_bytes": int(st["peak_resident_bytes"]),
     }
 
@@ -657,6 +664,19 @@ def run_reference(args) -> dict:
     }
 
 
+def profile_run(args) -> None:
+    """A few steps of the workload in one form, launched kernel by kernel, for
+    ncu captures of single kernels (the timed bench replays graphs)."""
+    import mpm3d_gb300 as m
+
+    d = m.Deck.parse(make_deck(args.workload, args.scale))
+    s = m.MpmStep(d, precision=args.profile_form, device=0)
+    s.run(args.profile_steps, graph=False)
+    s.sync()
+    print(f"{args.workload} x{args.scale}: {d.nb_particle} particles, {args.profile_steps} {args.profile_form} steps")
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -682,7 +702,14 @@ def main():
                     help="mixed-vs-FP64 error after this many steps of the workload (0 = skip)")
     ap.add_argument("--target-stride", type=int, default=8,
                     help="serving scenes also run through the FP64 forms: every n-th scene (0 = skip)")
+    ap.add_argument("--profile-form", default="", choices=["", "mixed", "fp64", "native"],
+                    help="profiling harness for ncu: only run --profile-steps steps of the workload in this form, "
+                         "one kernel launch at a time (no graph), and exit; prints no bench line")
+    ap.add_argument("--profile-steps", type=int, default=4)
     args = ap.parse_args()
+    if args.profile_form:
+        profile_run(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     line = run_reference(args) if args.impl == "reference" else run_ours(args)

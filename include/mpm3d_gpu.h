@@ -199,6 +199,19 @@ int mpm_batch_scene_count(const mpm_batch* b);
 /* nsteps steps of every resident scene (a scene stops at its step count);
  * use_graph replays a CUDA graph captured once per batch composition. */
 int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph);
+/* Device-resident run loop (no counterpart in the reference, whose time
+ * loop is one scene on the host, MPM3D.f90:66-160): one launch of a CUDA
+ * graph whose WHILE node repeats two steps of the batch while a device-side
+ * test passes, so the device steps the batch without a host round trip per
+ * step or per chunk. The loop returns (and the call, after its last
+ * reduction) once a scene has taken its last step, once max_steps steps are
+ * taken, or after mpm_batch_interrupt; *steps receives the steps taken (at
+ * least 1, at most max_steps). */
+int mpm_batch_run_loop(mpm_batch* b, int max_steps, int* steps);
+/* Ask a running device loop to return at its next test (two steps at most);
+ * callable from any thread. The request is cleared when mpm_batch_run_loop
+ * returns. */
+int mpm_batch_interrupt(mpm_batch* b);
 int mpm_batch_sync(mpm_batch* b);
 int mpm_batch_time_steps(mpm_batch* b, int nsteps, int use_graph, double* ms);
 int mpm_batch_scene_scalars(mpm_batch* b, int scene_id, double* out16);
@@ -213,7 +226,11 @@ const char* mpm_batch_last_error(const mpm_batch* b);
  * kernels; 0 keeps the current value). */
 int mpm_batch_set_blocks(mpm_batch* b, int particle_block, int node_block);
 /* Batch options (launch shapes; they change no result). */
-enum mpm_batch_option { MPM_BATCH_PARTICLE_BLOCK = 1, MPM_BATCH_NODE_BLOCK = 2 };
+enum mpm_batch_option {
+  MPM_BATCH_PARTICLE_BLOCK = 1,
+  MPM_BATCH_NODE_BLOCK = 2,
+  MPM_BATCH_SCATTER_BLOCKS = 3 /* grid cap of the particle -> grid transfers, blocks per SM (1..64) */
+};
 int mpm_batch_set_option(mpm_batch* b, int option, int value);
 int mpm_batch_get_option(const mpm_batch* b, int option);
 int mpm_batch_profile_enable(mpm_batch* b, int on);
@@ -256,11 +273,14 @@ int mpm_snapshot_load(mpm_ctx* ctx, const char* path);
 typedef struct mpm_server mpm_server;
 typedef struct mpm_serve_config {
   int device;               /* CUDA device, -1 = current                        */
-  int chunk_steps;          /* steps between admission points (0 = 25)          */
+  int chunk_steps;          /* most steps the device loop takes before it returns
+                               to the server (0 = 25); it returns earlier when a
+                               scene finishes or a submission arrives          */
   int64_t hbm_budget_bytes; /* sum of the resident scenes' mpm_scene_device_bytes
                                (0 = 35% of free memory: a batch keeps two arenas) */
   int max_scenes;           /* resident scene cap (0 = 4096)                     */
-  int autotune;             /* 1 = pick the batch launch shape on the first chunks */
+  int autotune;             /* 1 = pick the batch launch shape by timing every
+                               candidate on one frozen composition            */
   int policy;               /* admission order: MPM_SERVE_FIFO or MPM_SERVE_SHORTEST */
   int64_t max_resident_particles; /* admit while the resident particles stay below
                                      this (0 = no cap; a lone scene is always admitted) */
@@ -290,6 +310,9 @@ int mpm_serve_release(mpm_server* s, int64_t ticket);
 /* out[10]: submitted, finished, queued, resident, chunks run, particle-steps
  * run, device busy ms, particle block, node block, peak resident bytes */
 int mpm_serve_stats(mpm_server* s, double* out10);
+/* the launch shape in use (autotuned or default): MPM_ERR_STATE until the
+ * autotuner has chosen */
+int mpm_serve_launch_shape(mpm_server* s, int* particle_block, int* node_block, int* scatter_blocks);
 /* block until no scene is queued or resident (or timeout_ms passes) */
 int mpm_serve_drain(mpm_server* s, int timeout_ms);
 /* The server's admission decision as a pure host function (no device needed;

@@ -8,9 +8,6 @@
 // all scenes by (scene, cell) and runs one launch per kernel for the batch.
 #include <cuda_runtime.h>
 
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_run_length_encode.cuh>
-#include <cub/device/device_scan.cuh>
 
 #include <unistd.h>
 
@@ -26,6 +23,7 @@
 #include "mpm3d_gpu.h"
 #include "mpm_batch_host.h"
 #include "mpm_batch_kernels.cuh"
+#include "mpm_sort.cuh"
 #include "mpm_setup.h"
 
 using namespace mpm;
@@ -120,7 +118,7 @@ __global__ void kb_init_scene(BState s, int scene, int body0, DetoPoints deto) {
   s.q[i] = 0.f;
   for (int a = 0; a < 6; ++a) s.sd[a * NP + i] = 0.f;
   if (s.any_uvfp)
-    for (int a = 0; a < 9; ++a) s.fp[a * NP + i] = 0.f;
+    for (int a = 0; a < 18; ++a) s.fp[a * NP + i] = 0.f;
   s.failure[i] = 0;
   s.body[i] = (uint16_t)(body0 + s.body[i]);
   s.scene[i] = (uint16_t)scene;
@@ -133,9 +131,6 @@ __global__ void kb_inverse(BState s) {
   s.inv[s.scenes[s.scene[i]].p0 + s.orig[i]] = (int)i;
 }
 
-struct MaxOpB {
-  __host__ __device__ int operator()(int a, int b) const { return a > b ? a : b; }
-};
 
 // relocation of resident particles into a new layout
 __global__ void kb_relocate(BState src, BState dst, const int* map, const uint16_t* scene_map,
@@ -160,7 +155,7 @@ __global__ void kb_relocate(BState src, BState dst, const int* map, const uint16
   dst.seqv[i] = src.seqv[j];
   for (int a = 0; a < 6; ++a) dst.sd[a * NP + i] = src.sd[a * SP + j];
   if (src.any_uvfp && dst.any_uvfp)
-    for (int a = 0; a < 9; ++a) dst.fp[a * NP + i] = src.fp[a * SP + j];
+    for (int a = 0; a < 18; ++a) dst.fp[a * NP + i] = src.fp[a * SP + j];
   dst.epeff[i] = src.epeff[j];
   dst.celsius[i] = src.celsius[j];
   dst.dmg[i] = src.dmg[j];
@@ -200,13 +195,6 @@ struct mpm_batch {
   // next step's keys are sorted (the two touch disjoint arrays)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  // the per-key counts and the occupied keys of the sort run there too,
-  // beside the permutation; the first scatter waits for them
-  cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;
-  bool counts_pending = false;
-  void* cub_tmp = nullptr;
-  size_t cub_bytes = 0;
-  int key_bits = 1;
   int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
   int any_prep = 0;  // scenes whose force input is not staged by their stress kernel (USL / MUSL, Johnson-Cook)
   unsigned stress_types = 0;  // stress instantiations to launch: bit MT per specialised type, bit 0 for the rest
@@ -216,6 +204,16 @@ struct mpm_batch {
   int pblock = 256, nblock = 256;
   int scatter_blocks = 9728;  // scatter grid cap (64 blocks per SM; warps stride over the occupied cells)
   int scatter_wave = 4864;    // scatter warps resident at once (4 blocks per SM)
+  int sort_blocks = 152;      // grid of the long-segment sort (one block per SM)
+  int sms = 152;              // multiprocessors of the device
+  long long ntask = 0;        // particle tasks of the linear / GIMP / B-spline scenes (32 particles each)
+  // device-resident run loop (mpm_batch_run_loop): its state, the host's
+  // request flag (page-locked, mapped into the device's address space) and
+  // one loop graph per buffer parity
+  LoopCtl* ctl = nullptr;
+  volatile int* loop_flag_h = nullptr;
+  int* loop_flag_d = nullptr;
+  cudaGraphExec_t loop_graph[2] = {nullptr, nullptr};
   Profiler prof;
   // particle value gather (curve output)
   GatherItem *g_items_h = nullptr, *g_items_d = nullptr;
@@ -271,7 +269,7 @@ void alloc_particles(Alloc& al, BState& s, long long NP, bool uvfp) {
   s.sm = al.get<float>(NP);
   s.seqv = al.get<float>(NP);
   s.sd = al.get<float>(6 * NP);
-  s.fp = al.get<float>(uvfp ? 9 * NP : 1);
+  s.fp = al.get<float>(uvfp ? 18 * NP : 1);
   s.epeff = al.get<float>(NP);
   s.celsius = al.get<float>(NP);
   s.dmg = al.get<float>(NP);
@@ -285,14 +283,14 @@ void alloc_particles(Alloc& al, BState& s, long long NP, bool uvfp) {
 }
 
 long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bool uvfp, bool jc) {
-  long long per_p = 2 * (16 * 8 + 17 * 4 + (uvfp ? 36 : 0) + 1 + 2 + 2 + 4);  // two particle buffer sets
+  long long per_p = 2 * (16 * 8 + 17 * 4 + (uvfp ? 72 : 0) + 1 + 2 + 2 + 4);  // two particle buffer sets
   per_p += 4 * 3 + 4 * 9 + 4 * 6 + 4 * 9;                                  // derived + force staging
-  per_p += 4 * 4;                                                         // sort keys / values
+  per_p += 4 * 4;                                                         // sort key, permutation, runs, inverse
   if (jc) per_p += 4 * 2 + 8 * 6 + 1;
   long long per_n = 8 * 13 + 4 + 8 * 4;
-  long long per_k = 4;
+  long long per_k = 4 * 2;                                                // segment ends, fill counters
   long long per_c = sgmp ? 8 * 39 + 2 : 0;
-  return np * per_p + nn * per_n + (ncell + 1) * per_k + ncell * per_c + 4096;
+  return np * per_p + nn * per_n + (std::max(nn, ncell) + 1) * per_k + ncell * per_c + 4096;
 }
 
 void layout_flags(mpm_batch* b) {
@@ -334,11 +332,23 @@ int upload_scene_particles(mpm_batch* b, HostScene* h, BState& s) {
   return MPM_OK;
 }
 
-// sort keys of a scene: its cells (dual cells for SGMP) plus one for the
-// particles off the grid
-long long scene_keys(const Geometry& g) { return (long long)g.ncell + 1; }
+// sort keys of a scene: one per cell (linear, B-spline), per node (GIMP: a
+// particle is binned with its nearest node, see kb_keys) or per dual cell
+// (SGMP, ncell of them), plus the bucket of the particles outside the grid
+long long scene_keys(const Geometry& g) { return (g.shape == 1 ? (long long)g.nn : (long long)g.ncell) + 1; }
 
 inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
+
+// inclusive scan in three passes over tiles (mpm_sort.cuh); tiles holds
+// scan_tiles(src.n) values of the source's type
+template <class S>
+void scan_tiles_enqueue(const S& src, typename S::T* tiles, cudaStream_t st) {
+  const long long nt = scan_tiles(src.n);
+  if (nt <= 0) return;
+  ks_tile_total<S><<<(unsigned)nt, kScanThreads, 0, st>>>(src, tiles);
+  ks_tile_prefix<typename S::T, typename S::Op><<<1, kScanThreads, 0, st>>>(tiles, nt);
+  ks_tile_scan<S><<<(unsigned)nt, kScanThreads, 0, st>>>(src, tiles);
+}
 
 // one step of every live scene (MPM3D.f90:69-118 for each scene)
 // The step in three parts. The front (sort keys, sort, per-key counts,
@@ -347,7 +357,7 @@ inline unsigned gridn(long long n, int blk) { return (unsigned)((n + blk - 1) / 
 // (calcEnergy, UpdateDT, damping) reads the final velocities, masses and
 // energies. The front does not depend on the begin kernel (which advances
 // the step count and time), so it runs first.
-int enqueue_front(mpm_batch* b, bool side_counts = false) {
+int enqueue_front(mpm_batch* b) {
   cudaStream_t st = b->stream;
   BState& a = b->A;
   const int pb = b->pblock;
@@ -355,32 +365,16 @@ int enqueue_front(mpm_batch* b, bool side_counts = false) {
   cudaMemsetAsync(a.seg, 0, sizeof(int) * (size_t)(a.NK + 1), st);
   kb_keys<<<gridn(a.NP, pb), pb, 0, st>>>(a);
   prof_end(K_LOCATE, st);
+  // counting sort by key (mpm_sort.cuh): segment ends and the occupied
+  // keys, placement, then the stable order inside each segment
   prof_begin(K_SORT, st);
-  size_t tmp = b->cub_bytes;
-  cudaError_t e = cub::DeviceRadixSort::SortPairs(b->cub_tmp, tmp, a.key, a.key_sorted, a.val, a.perm, (int)a.NP, 0,
-                                                  b->key_bits, st);
-  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "sort: %s", cudaGetErrorString(e));
-  if (side_counts) {
-    prof_end(K_SORT, st);
-    BCK(cudaEventRecord(b->ev_fork2, st));
-    BCK(cudaStreamWaitEvent(b->side, b->ev_fork2, 0));
-    st = b->side;
-    prof_begin(K_SORT, st);
-  }
-  tmp = b->cub_bytes;
-  e = cub::DeviceScan::InclusiveSum(b->cub_tmp, tmp, a.seg, a.seg, (int)a.NK, st);
-  if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "scan: %s", cudaGetErrorString(e));
-  {  // occupied cells (dual cells for SGMP) for the persistent scatters
-    tmp = b->cub_bytes;
-    e = cub::DeviceRunLengthEncode::Encode(b->cub_tmp, tmp, a.key_sorted, a.runs, a.run_counts, a.nruns, (int)a.NP,
-                                           st);
-    if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "run-length encode: %s", cudaGetErrorString(e));
-  }
+  scan_tiles_enqueue(SegScan{a.seg, a.runs, a.nruns, a.NK}, reinterpret_cast<long long*>(a.tiles), st);
+  BCK(cudaMemsetAsync(a.fill, 0, sizeof(int) * (size_t)a.NK, st));
+  BCK(cudaMemsetAsync(a.nbig, 0, sizeof(int), st));
+  ks_place<<<gridn(a.NP, 256), 256, 0, st>>>(a.key, a.seg, a.fill, a.perm, a.NP);
+  ks_segments<<<gridn(a.NK, 256), 256, 0, st>>>(a.seg, a.NK, a.perm, a.big, a.nbig);
+  ks_long_segments<<<b->sort_blocks, kSegThreads, 0, st>>>(a.seg, a.perm, a.big, a.nbig);
   prof_end(K_SORT, st);
-  if (side_counts) {
-    BCK(cudaEventRecord(b->ev_join2, st));
-    b->counts_pending = true;
-  }
   return MPM_OK;
 }
 
@@ -398,17 +392,31 @@ int enqueue_back(mpm_batch* b) {
   std::swap(b->A, b->B);
   BState& s = b->A;
   const unsigned sgrid = (unsigned)std::min<long long>(b->scatter_blocks, (s.NK + kCellWarps - 1) / kCellWarps);
+  auto pgrid = [&](int warps) {
+    return (unsigned)std::max<long long>(1, std::min<long long>(b->scatter_blocks, (b->ntask + warps - 1) / warps));
+  };
+  // particle -> grid transfers: particle tasks (linear, GIMP, B-spline) and
+  // the SGMP keys, each launched when the batch holds such scenes
+  auto scatter = [&](int mode) {
+    if (b->any_nonsgmp) {
+      constexpr int w0 = PartShape<0>::WARPS, w1 = PartShape<1>::WARPS, w2 = PartShape<2>::WARPS;
+      if (mode == 0) kb_part_scatter<0><<<pgrid(w0), 32 * w0, 0, st>>>(s);
+      else if (mode == 1) kb_part_scatter<1><<<pgrid(w1), 32 * w1, 0, st>>>(s);
+      else kb_part_scatter<2><<<pgrid(w2), 32 * w2, 0, st>>>(s);
+    }
+    if (b->any_sgmp) {
+      if (mode == 0) kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
+      else if (mode == 1) kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
+      else kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
+    }
+  };
   if (b->any_sgmp) {
     prof_begin(K_SG_CLEAR, st);
     kb_sg_clear<<<gridn(s.NC, nb), nb, 0, st>>>(s);
     prof_end(K_SG_CLEAR, st);
   }
-  if (b->counts_pending) {  // per-key counts and occupied keys from the side stream
-    BCK(cudaStreamWaitEvent(st, b->ev_join2, 0));
-    b->counts_pending = false;
-  }
   prof_begin(K_SCATTER_MASS, st);
-  kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
+  scatter(0);
   prof_end(K_SCATTER_MASS, st);
   prof_begin(K_P2G_MASS, st);
   kb_p2g_mass<<<gridn(s.NN, nb), nb, 0, st>>>(s, 1, 1);
@@ -432,9 +440,7 @@ int enqueue_back(mpm_batch* b) {
     prof_end(K_STRESS, st);
     if (b->any_jc) {
       prof_begin(K_DEPEFF, st);
-      size_t t2 = b->cub_bytes;
-      cudaError_t e2 = cub::DeviceScan::InclusiveScan(b->cub_tmp, t2, s.setter, s.setter_scan, MaxOpB(), (int)s.NP, st);
-      if (e2 != cudaSuccess) return berr(b, MPM_ERR_CUDA, "depeff scan: %s", cudaGetErrorString(e2));
+      scan_tiles_enqueue(IntScan<ScanMax>{s.setter, s.setter_scan, s.NP}, s.tiles, st);
       kb_depeff_apply<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass);
       kb_depeff_carry<<<gridn(s.nscene, 128), 128, 0, st>>>(s, usf_pass);
       prof_end(K_DEPEFF, st);
@@ -449,7 +455,7 @@ int enqueue_back(mpm_batch* b) {
     prof_end(K_FORCE_PREP, st);
   }
   prof_begin(K_SCATTER_FORCE, st);
-  kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
+  scatter(2);
   prof_end(K_SCATTER_FORCE, st);
   prof_begin(K_P2G_FORCE, st);
   kb_p2g_force<<<gridn(s.NN, nb), nb, 0, st>>>(s);
@@ -464,7 +470,7 @@ int enqueue_back(mpm_batch* b) {
   prof_end(K_POSITION, st);
   if (b->any_musl) {
     prof_begin(K_SCATTER_MOM, st);
-    kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
+    scatter(1);
     prof_end(K_SCATTER_MOM, st);
     prof_begin(K_P2G_MOM, st);
     kb_p2g_momentum<<<gridn(s.NN, nb), nb, 0, st>>>(s);
@@ -513,7 +519,7 @@ int enqueue_step_overlapped(mpm_batch* b, bool lead) {
     if (int r = enqueue_reduce(b, b->side)) return r;
     BCK(cudaEventRecord(b->ev_join, b->side));
   }
-  int r = enqueue_front(b, true);
+  int r = enqueue_front(b);
   if (lead) BCK(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
   if (!r) r = enqueue_back(b);
   if (!r) {
@@ -529,6 +535,10 @@ void drop_graph(mpm_batch* b) {
       if (g) cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  for (auto& g : b->loop_graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
 }
 
 // capture nsteps steps into an executable graph; the host-side buffer handles
@@ -553,6 +563,106 @@ int capture(mpm_batch* b, int nsteps, cudaGraphExec_t* out, int lead = -1) {
   e = cudaGraphInstantiate(out, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return berr(b, MPM_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+// ------------------------------------------------ device-resident loop
+// The loop test: iterate again while no scene has taken its last step since
+// the loop began, some scene still has steps to take, the host has not
+// asked the loop to return (flag, page-locked host memory read through its
+// device mapping) and the iteration budget is not spent. One block.
+__device__ __forceinline__ void loop_decide(const BState& b, const int* target, const volatile int* flag,
+                                            cudaGraphConditionalHandle h) {
+  bool pending = false;
+  for (int s = threadIdx.x; s < b.nscene; s += blockDim.x) pending = pending || b.sst[s].istep < target[s];
+  pending = __syncthreads_or(pending);
+  if (threadIdx.x == 0) {
+    const LoopCtl& c = *b.ctl;
+    const bool go = pending && c.finished == c.fin0 && *flag == 0 && c.iters < c.max_iters;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+  }
+}
+
+// before the loop's first step: budget, iteration count, finished-scene mark
+__global__ void kb_loop_arm(LoopCtl* c, int max_iters) {
+  c->fin0 = c->finished;
+  c->iters = 0;
+  c->max_iters = max_iters;
+}
+
+__global__ void kb_loop_start(BState b, const int* target, const volatile int* flag, cudaGraphConditionalHandle h) {
+  loop_decide(b, target, flag, h);
+}
+
+__global__ void kb_loop_test(BState b, const int* target, const volatile int* flag, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0) b.ctl->iters = b.ctl->iters + 1;
+  __syncthreads();
+  loop_decide(b, target, flag, h);
+}
+
+// The loop graph of the current buffer parity: a test kernel, then a WHILE
+// node whose body is two overlapped steps (each with the previous step's
+// reduction beside its sort) and the test again. Two steps per iteration
+// bring the particle buffer sets back to the parity the graph was built
+// for.
+int build_loop(mpm_batch* b, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  BCK(cudaGraphCreate(&g, 0));
+  int r = MPM_OK;
+  cudaGraphConditionalHandle h{};
+  cudaGraphNode_t kn = nullptr, cn = nullptr;
+  BState s0 = b->A;
+  const int* tgt = b->d_target;
+  const volatile int* flag = b->loop_flag_d;
+  void* args[] = {&s0, &tgt, &flag, &h};
+  cudaKernelNodeParams kp{};
+  kp.func = (void*)kb_loop_start;
+  kp.gridDim = dim3(1);
+  kp.blockDim = dim3(256);
+  kp.kernelParams = args;
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+  if (e == cudaSuccess) e = cudaGraphAddKernelNode(&kn, g, nullptr, 0, &kp);
+  if (e == cudaSuccess) {
+    cp.conditional.handle = h;
+    e = cudaGraphAddNode(&cn, g, &kn, nullptr, 1, &cp);
+  }
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(b->stream, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return berr(b, MPM_ERR_CUDA, "loop graph: %s", cudaGetErrorString(e));
+  }
+  r = enqueue_step_overlapped(b, true);
+  if (!r) r = enqueue_step_overlapped(b, true);
+  if (!r) kb_loop_test<<<1, 256, 0, b->stream>>>(b->A, tgt, flag, h);
+  cudaGraph_t body = nullptr;
+  e = cudaStreamEndCapture(b->stream, &body);
+  if (!r && e != cudaSuccess) r = berr(b, MPM_ERR_CUDA, "loop body capture: %s", cudaGetErrorString(e));
+  if (!r) {
+    e = cudaGraphInstantiate(out, g, 0);
+    if (e != cudaSuccess) r = berr(b, MPM_ERR_CUDA, "loop graph instantiate: %s", cudaGetErrorString(e));
+  }
+  cudaGraphDestroy(g);
+  return r;
+}
+
+// one step replayed from the graph of the current buffer parity (captured on
+// first use); lead: with the previous step's reduction beside the sort
+int replay_step(mpm_batch* b, int lead) {
+  const int par = b->A.x == b->set0_x ? 0 : 1;
+  if (!b->graph[par][lead]) {
+    cudaGraphExec_t ge = nullptr;
+    if (int r = capture(b, 1, &ge, lead)) return r;
+    b->graph[par][lead] = ge;
+    std::swap(b->A, b->B);  // capture swapped the host handles; the launch below does the step
+  }
+  BCK(cudaGraphLaunch(b->graph[par][lead], b->stream));
+  std::swap(b->A, b->B);
   return MPM_OK;
 }
 
@@ -622,23 +732,10 @@ int commit(mpm_batch* b) {
   if (NP >= (1LL << 31) || NK >= (1LL << 31) || NN >= (1LL << 31))
     return berr(b, MPM_ERR_UNSUPPORTED, "batch too large for 32-bit indices");
   layout_flags(b);
-  // CUB scratch sizes for this layout (size queries only)
-  size_t t1 = 0, t2 = 0, t3 = 0;
-  int bits = 1;
-  while ((1LL << bits) <= NK) ++bits;
-  cub::DeviceRadixSort::SortPairs(nullptr, t1, (unsigned*)nullptr, (unsigned*)nullptr, (int*)nullptr, (int*)nullptr,
-                                  (int)NP, 0, bits, st);
-  cub::DeviceScan::InclusiveSum(nullptr, t2, (int*)nullptr, (int*)nullptr, (int)NK, st);
-  if (b->any_jc) cub::DeviceScan::InclusiveScan(nullptr, t3, (int*)nullptr, (int*)nullptr, MaxOpB(), (int)NP, st);
-  size_t t4 = 0;
-  cub::DeviceRunLengthEncode::Encode(nullptr, t4, (unsigned*)nullptr, (unsigned*)nullptr, (int*)nullptr, (int*)nullptr,
-                                     (int)NP, st);
-  const size_t tb = std::max(std::max(t1, t4), std::max(t2, t3));
   BState A{}, B{}, shared{};
   int* d_target = nullptr;
   int* d_map = nullptr;
   uint16_t *d_smap = nullptr, *d_bmap = nullptr;
-  void* tmp = nullptr;
   auto carve = [&](Alloc& al) {
   A = BState{};
   B = BState{};
@@ -662,14 +759,15 @@ int commit(mpm_batch* b) {
   shared.xn = al.get<float>(3 * NP);
   shared.fs = al.get<float>(9 * NP);
   shared.key = al.get<unsigned>(NP);
-  shared.key_sorted = al.get<unsigned>(NP);
-  shared.val = al.get<int>(NP);
   shared.perm = al.get<int>(NP);
   shared.seg = al.get<int>(NK + 1);
   shared.runs = al.get<unsigned>(NP);
   shared.inv = al.get<int>(NP);
-  shared.run_counts = al.get<int>(NP);
   shared.nruns = al.get<int>(1);
+  shared.fill = al.get<int>(NK);
+  shared.tiles = al.get<int>(2 * (std::max(scan_tiles(NK), scan_tiles(NP)) + 1));  // 64-bit tile totals
+  shared.big = al.get<int>(NP / (kRegSeg + 1) + 1);
+  shared.nbig = al.get<int>(1);
   shared.mg = al.get<double>(NN);
   shared.px = al.get<double>(3 * NN);
   shared.fx = al.get<double>(3 * NN);
@@ -696,6 +794,7 @@ int commit(mpm_batch* b) {
   shared.red_part = al.get<double>(6 * NR);
   shared.rscene = al.get<uint16_t>(NR);
   shared.scenes = al.get<Scene>((long long)b->order.size());
+  shared.task0 = al.get<int>((long long)b->order.size() + 1);
   shared.sst = al.get<SceneState>((long long)b->order.size());
   shared.mats = al.get<DevMaterial>(nmat);
   shared.bodies = al.get<DevBody>(nbody);
@@ -703,7 +802,6 @@ int commit(mpm_batch* b) {
   d_map = al.get<int>(NP);
   d_smap = al.get<uint16_t>(b->A.nscene + 1);
   d_bmap = al.get<uint16_t>(65536);
-  tmp = al.get<char>((long long)tb);
   };
   Alloc measure;
   carve(measure);
@@ -729,13 +827,15 @@ int commit(mpm_batch* b) {
   carve(al);
   auto share = [&](BState& s) {
     s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
-    s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.key_sorted = shared.key_sorted; s.val = shared.val;
-    s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.inv = shared.inv; s.run_counts = shared.run_counts; s.nruns = shared.nruns; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
+    s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key;
+    s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.inv = shared.inv; s.nruns = shared.nruns;
+    s.fill = shared.fill; s.tiles = shared.tiles; s.big = shared.big; s.nbig = shared.nbig; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
     s.nvel = shared.nvel; s.nacc = shared.nacc; s.acc = shared.acc; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
     s.cacc = shared.cacc; s.co = shared.co;
     s.cw = shared.cw; s.cdefp = shared.cdefp; s.cvx = shared.cvx; s.cax = shared.cax; s.cscene = shared.cscene;
     s.setter = shared.setter; s.setter_scan = shared.setter_scan; s.dep = shared.dep; s.jc_aux = shared.jc_aux;
     s.deferred = shared.deferred; s.red_part = shared.red_part; s.rscene = shared.rscene; s.scenes = shared.scenes;
+    s.task0 = shared.task0;
     s.sst = shared.sst; s.mats = shared.mats; s.bodies = shared.bodies;
   };
   share(A);
@@ -769,8 +869,12 @@ int commit(mpm_batch* b) {
   std::vector<uint8_t> fix((size_t)NN), bd((size_t)NN);
   std::vector<int> target;
   std::vector<SceneState> sst;
+  std::vector<int> task0;  // first particle task of each scene (32 particles; SGMP scenes have none)
+  long long ntask = 0;
   for (HostScene* h : b->order) {
     const Geometry& g = h->su.g;
+    task0.push_back((int)ntask);
+    if (g.shape != 3) ntask += (h->np + 31) / 32;
     Scene sc;
     memset(&sc, 0, sizeof sc);
     sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = scene_keys(g);
@@ -810,6 +914,9 @@ int commit(mpm_batch* b) {
     s0.active = h->resident ? 0 : 1;  // the initial energy pass below runs for new scenes only
     sst.push_back(s0);
   }
+  task0.push_back((int)ntask);
+  b->ntask = ntask;
+  BCK(cudaMemcpyAsync(shared.task0, task0.data(), sizeof(int) * task0.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.scenes, scenes.data(), sizeof(Scene) * scenes.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.mats, mats.data(), sizeof(DevMaterial) * mats.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.bodies, bodies.data(), sizeof(DevBody) * bodies.size(), cudaMemcpyHostToDevice, st));
@@ -852,13 +959,11 @@ int commit(mpm_batch* b) {
   std::swap(b->arena, b->spare);
   std::swap(b->arena_cap, b->spare_cap);
   b->bytes = (long long)(b->arena_cap + b->spare_cap);
+  A.ctl = B.ctl = b->ctl;
   b->A = A;
   b->B = B;
   b->set0_x = A.x;
   b->d_target = d_target;
-  b->cub_tmp = tmp;
-  b->cub_bytes = tb;
-  b->key_bits = bits;
   for (HostScene* h : b->order) {
     if (!h->resident) h->release_inputs();  // the scene's inputs are on the device now
     h->resident = true;
@@ -895,16 +1000,22 @@ int mpm_batch_create(int device, mpm_batch** out) {
   {
     b->scatter_blocks = 64 * sms;
     b->scatter_wave = 4 * sms * kCellWarps;
+    b->sort_blocks = sms;
+    b->sms = sms;
   }
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev_join2, cudaEventDisableTiming) != cudaSuccess) {
+      cudaMalloc((void**)&b->ctl, sizeof(LoopCtl)) != cudaSuccess ||
+      cudaMemset(b->ctl, 0, sizeof(LoopCtl)) != cudaSuccess ||
+      cudaHostAlloc((void**)&b->loop_flag_h, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&b->loop_flag_d, (void*)b->loop_flag_h, 0) != cudaSuccess) {
+    if (b->ctl) cudaFree(b->ctl);
+    if (b->loop_flag_h) cudaFreeHost((void*)b->loop_flag_h);
+
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
-    if (b->ev_fork2) cudaEventDestroy(b->ev_fork2);
     if (b->side) cudaStreamDestroy(b->side);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -932,8 +1043,8 @@ void mpm_batch_destroy(mpm_batch* b) {
   cudaStreamSynchronize(b->side);
   cudaEventDestroy(b->ev_fork);
   cudaEventDestroy(b->ev_join);
-  cudaEventDestroy(b->ev_fork2);
-  cudaEventDestroy(b->ev_join2);
+  cudaFree(b->ctl);
+  cudaFreeHost((void*)b->loop_flag_h);
   cudaStreamDestroy(b->side);
   cudaStreamDestroy(b->stream);
   delete b;
@@ -1017,19 +1128,44 @@ int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph) {
   // buffer sets, so the graph captured from either set is replayed
   // alternately), the steps after the first of the run with the previous
   // step's reduction overlapping their sort; the run's last reduction ends it
-  for (int i = 0; i < nsteps; ++i) {
-    const int par = b->A.x == b->set0_x ? 0 : 1;
-    const int lead = i > 0 ? 1 : 0;
-    if (!b->graph[par][lead]) {
-      cudaGraphExec_t ge = nullptr;
-      if ((r = capture(b, 1, &ge, lead))) return r;
-      b->graph[par][lead] = ge;
-      std::swap(b->A, b->B);  // capture swapped the host handles; the launch below does the step
-    }
-    BCK(cudaGraphLaunch(b->graph[par][lead], b->stream));
-    std::swap(b->A, b->B);
-  }
+  for (int i = 0; i < nsteps; ++i)
+    if ((r = replay_step(b, i > 0 ? 1 : 0))) return r;
   return enqueue_reduce(b, b->stream);
+}
+
+int mpm_batch_run_loop(mpm_batch* b, int max_steps, int* steps) {
+  if (!b || !steps || max_steps < 1) return MPM_ERR_ARG;
+  *steps = 0;
+  cudaSetDevice(b->device);
+  int r = ensure_committed(b);
+  if (r) return r;
+  if (b->order.empty()) return MPM_OK;
+  b->inv_stale = true;
+  *b->loop_flag_h = 0;
+  // the first step (its reduction overlaps the loop's first step), then the
+  // loop's iterations of two steps, then the last step's reduction
+  kb_loop_arm<<<1, 1, 0, b->stream>>>(b->ctl, (max_steps - 1) / 2);
+  if ((r = replay_step(b, 0))) return r;
+  const int par = b->A.x == b->set0_x ? 0 : 1;
+  if (!b->loop_graph[par]) {
+    cudaGraphExec_t ge = nullptr;
+    if ((r = build_loop(b, &ge))) return r;
+    b->loop_graph[par] = ge;
+  }
+  BCK(cudaGraphLaunch(b->loop_graph[par], b->stream));
+  if ((r = enqueue_reduce(b, b->stream))) return r;
+  LoopCtl c{};
+  BCK(cudaMemcpyAsync(&c, b->ctl, sizeof c, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  *b->loop_flag_h = 0;  // an interrupt is consumed by the loop it ended (or the next one)
+  *steps = 1 + 2 * c.iters;
+  return MPM_OK;
+}
+
+int mpm_batch_interrupt(mpm_batch* b) {
+  if (!b) return MPM_ERR_ARG;
+  *b->loop_flag_h = 1;  // read by the loop test through the device mapping
+  return MPM_OK;
 }
 
 int mpm_batch_sync(mpm_batch* b) {
@@ -1202,7 +1338,7 @@ std::vector<RestartField> restart_fields(const BState& s, bool uvfp) {
                                  {s.sd, 4, 6},    {s.epeff, 4, 1},   {s.celsius, 4, 1}, {s.dmg, 4, 1}, {s.lt, 4, 1},
                                  {s.cp, 4, 1},    {s.q, 4, 1},       {s.failure, 1, 1}, {s.body, 2, 1}, {s.scene, 2, 1},
                                  {s.orig, 4, 1}};
-  if (uvfp) f.push_back({s.fp, 4, 9});
+  if (uvfp) f.push_back({s.fp, 4, 18});
   return f;
 }
 }  // namespace
@@ -1335,6 +1471,13 @@ int mpm_batch_set_option(mpm_batch* b, int option, int value) {
   switch (option) {
     case MPM_BATCH_PARTICLE_BLOCK: return mpm_batch_set_blocks(b, value, 0);
     case MPM_BATCH_NODE_BLOCK: return mpm_batch_set_blocks(b, 0, value);
+    case MPM_BATCH_SCATTER_BLOCKS:
+      if (value < 1 || value > 64) return berr(b, MPM_ERR_ARG, "scatter blocks per SM %d not in 1..64", value);
+      if (b->scatter_blocks != value * b->sms) {
+        b->scatter_blocks = value * b->sms;
+        drop_graph(b);
+      }
+      return MPM_OK;
     default: return berr(b, MPM_ERR_ARG, "unknown batch option %d", option);
   }
 }
@@ -1344,6 +1487,7 @@ int mpm_batch_get_option(const mpm_batch* b, int option) {
   switch (option) {
     case MPM_BATCH_PARTICLE_BLOCK: return b->pblock;
     case MPM_BATCH_NODE_BLOCK: return b->nblock;
+    case MPM_BATCH_SCATTER_BLOCKS: return b->scatter_blocks / b->sms;
     default: return -1;
   }
 }

@@ -18,8 +18,9 @@
 //     force[6]); FP32 co[6], cw[3], cdefp[9], cvx[3], cax[3]
 //   sort keys: scene s owns keys [k0, k0 + nk), the last one collects the
 //     particles outside its grid; seg[k] = end of key k's particle range
-//     (kept for SGMP scenes). Linear / GIMP / B-spline: one key per cell;
-//     SGMP: one key per dual cell.
+//     (kept for SGMP scenes). Linear / B-spline: one key per cell; GIMP:
+//     one key per node (the particle's nearest node); SGMP: one key per dual
+//     cell.
 //   P2G accumulators: acc[4][NN] 64-bit fixed point (see the scatter kernels).
 //
 // Transfers particle -> grid are scatters of FP32 per-cell partial sums
@@ -43,7 +44,7 @@ namespace bm {
 struct Scene {
   long long p0, np;  // particles
   long long n0, nn;  // grid nodes
-  long long k0, nk;  // sort keys (ncell + 1)
+  long long k0, nk;  // sort keys (ncell + 1; GIMP nn + 1)
   long long c0, nc;  // SGMP centre nodes
   long long r0, nr;  // reduction chunks
   int NGx, NGy, NGz, NGxy, NCx, NCy, NCz, NCxy, CNCx, CNCy, CNCz, CNCxy, CNC;
@@ -64,6 +65,14 @@ struct SceneState {
   unsigned pad_;
 };
 
+// State of the device-resident run loop (mpm_batch_run_loop).
+struct LoopCtl {
+  int finished;   // scenes that took their last step (counted by kb_begin, never reset)
+  int fin0;       // finished when the loop began
+  int iters;      // loop iterations taken (two steps each)
+  int max_iters;  // iteration budget
+};
+
 struct BState {
   long long NP, NN, NK, NC, NR;
   int nscene;
@@ -79,11 +88,14 @@ struct BState {
   int *cell, *dual, *inode;
   float *off, *xxn, *xn;
   float* fs;  // force staging [9][NP]: sigma*vol (xx, yy, zz, xy, yz, xz), fext (3)
-  // sort
-  unsigned *key, *key_sorted;
-  int *val, *perm, *seg;
-  unsigned* runs;    // occupied sort keys of the step (run-length encoding of key_sorted)
-  int *run_counts, *nruns;
+  // sort (mpm_sort.cuh)
+  unsigned* key;
+  int *perm, *seg;
+  unsigned* runs;  // occupied sort keys of the step (in no particular order)
+  int* nruns;
+  int *fill, *tiles, *big, *nbig;  // per-key slots taken, scan tile totals, long segments
+  LoopCtl* ctl;  // run-loop state (one per batch, outside the layout arena)
+  int* task0;  // first particle task (32 sorted particles) of each scene, nscene + 1 entries; SGMP scenes have none
   // grid
   double *mg, *px, *fx;
   float4 *nvel, *nacc;             // FP32 px / mg and fx / mg for the gathers (zero at or below the cut-off)

@@ -58,6 +58,7 @@ __global__ void kb_begin(BState b, const int* target) {
   t.active = t.istep < target[s] ? 1 : 0;
   if (!t.active) return;
   t.istep = t.istep + 1;
+  if (t.istep == target[s]) atomicAdd(&b.ctl->finished, 1);  // the scene's last step
   t.time = t.time + t.dt;
   t.ie = 0.0;
   t.active_nodes = 0;
@@ -93,11 +94,15 @@ __device__ __forceinline__ long long dual_cell(const Scene& sc, const double x[3
 }
 
 // ------------------------------------------------------------------ keys
-// Sort key of a particle: its scene's key base plus its cell (linear, GIMP,
-// B-spline) or its dual cell (SGMP); the scene's last key collects the
-// particles outside the grid. Sorting keeps the particles of a cell
-// contiguous, which the transfers rely on for locality (and the SGMP centre
-// gathers for their particle ranges).
+// Sort key of a particle: its scene's key base plus its cell (linear,
+// B-spline), its nearest node (GIMP) or its dual cell (SGMP); the scene's
+// last key collects the particles outside the grid. Sorting keeps the
+// particles of a key contiguous, which the transfers rely on for locality
+// (and the SGMP centre gathers for their particle ranges). A GIMP particle
+// reaches the nodes within 1.25 cells of it (the cpGIMP quarter rule of
+// FindInflNode), i.e. at most one node either side of its nearest node in
+// each direction: binned by nearest node, a key's particles reach a 3 x 3 x
+// 3 box of nodes instead of the 4 x 4 x 4 box of a cell's particles.
 __global__ void kb_keys(BState b) {
   const long long i = btid();
   long long key = -1;
@@ -112,12 +117,16 @@ __global__ void kb_keys(BState b) {
       int cc[3];
       float off[3];
       if (cell_of(sc, x, cc, off)) {
-        c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+        if (sc.shape == 1) {  // nearest node: the cell's lower node, or the upper one from half a cell on
+          for (int a = 0; a < 3; ++a) cc[a] += off[a] >= 0.5f;
+          c = ((long long)cc[2] * sc.NGy + cc[1]) * sc.NGx + cc[0];
+        } else {
+          c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
+        }
       }
     }
     key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
     b.key[i] = (unsigned)key;
-    b.val[i] = (int)i;
   }
   // per-key counts: the particles arrive sorted by the last step's keys, so
   // a warp's lanes mostly share a few keys -- one atomic per key and warp
@@ -154,9 +163,9 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   const int s = src.scene[j];
   const int orig = src.orig[j];
   if (src.any_uvfp) {
-    float fp[9];
-    for (int a = 0; a < 9; ++a) fp[a] = src.fp[a * NP + j];
-    for (int a = 0; a < 9; ++a) dst.fp[a * NP + i] = fp[a];
+    float fp[18];
+    for (int a = 0; a < 18; ++a) fp[a] = src.fp[a * NP + j];
+    for (int a = 0; a < 18; ++a) dst.fp[a * NP + i] = fp[a];
   }
   for (int a = 0; a < 3; ++a) {
     dst.x[a * NP + i] = x[a];
@@ -320,36 +329,17 @@ __global__ void kb_permute(BState src, BState dst) {
   block_scene_max<2>(dst, s, {Q_MASS, Q_MOM}, {bm, bv});
 }
 
-// Cell-centric form of the scatter: one warp per sort key (cell), over the
-// box of node offsets t = tlo .. tlo + nt - 1 per direction that the shape
-// reaches from a cell (linear 0..1, B-spline -1..1, GIMP -1..2). Lane l owns
-// box slots l and l + 32 and sums their contributions over the cell's
-// particles in storage order (FP32); each nonzero slot sum is quantised and
-// added to the node's fixed-point accumulator. A cell's sums depend only on
-// its own particle list, so they are the same alone or in a batch.
-// The shape functions are tensor products, N = Wx Wy Wz, so the work is
-// split by direction: the particles' 1-D tables (w, dw/dx) per offset, then
-// per particle and (ty, tz) the y-z factors of every channel, e.g. for the
-// force  f_x = Dx * (-s_xx Wy Wz) + Wx * (b_x Wy Wz - s_xy Dy Wz - s_xz Wy Dz),
-// shared by the nt slots that differ in tx; a slot then costs 2 multiply-adds
-// per channel and particle. Particles go 8 at a time through the warp's
-// shared workspace.
+// SGMP scatter workspace: one warp per sort key (a dual cell); per mode the
+// staged particle quantities and the warp's staging rows.
 // mode 0: mass + momentum (GridMomentumInitial), 1: momentum with the updated
 // velocities (GridMomentumMUSL), 2: force (GridMomentumUpdate).
-constexpr int kCellWarps = 8;  // warps (cells) per block
+constexpr int kCellWarps = 8;  // warps (keys) per block
 
 template <int MODE>
 struct ScatterShape {
-  static constexpr int NV = MODE == 0 ? 4 : 3;   // channels
-  static constexpr int NQ = MODE == 2 ? 9 : 4;   // per-particle quantities staged
-  static constexpr int PC = 8;                   // particles per staging round (box shapes)
-  static constexpr int NPQ = MODE == 2 ? 6 : 4;  // y-z factors per (particle, ty, tz)
-  static constexpr int PQ = PC * 16 * NPQ;       // floats: y-z factors [PC][tz * 4 + ty][NPQ]
-  static constexpr int TAB = PC * 3 * 4 * 2;     // floats: (w, dw/dx) [PC][direction][t - tlo]
-  static constexpr int VAL = NQ * PC;            // floats: particle values [NQ][PC]
-  static constexpr int SROW = MODE == 2 ? 19 : 13;  // SGMP staging row: NQ values, 8 weights, 1 (odd length)
-  static constexpr int BOX = PQ + TAB + VAL;
-  static constexpr int WS = ((BOX > 32 * SROW ? BOX : 32 * SROW) + 3) / 4 * 4;  // floats per warp
+  static constexpr int NQ = MODE == 2 ? 9 : 4;      // per-particle quantities staged
+  static constexpr int SROW = MODE == 2 ? 19 : 13;  // staging row: NQ values, 8 weights, 1 (odd length)
+  static constexpr int WS = (32 * SROW + 3) / 4 * 4;  // floats per warp
 };
 
 // Corner k of the dual cell (dx, dy, dz) as a scene cell (its centre node),
@@ -443,165 +433,233 @@ __device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int 
   }
 }
 
-// the scatter of one cell's particles [i0, i1) of a linear (SH 0), GIMP (1)
-// or B-spline (2) scene by one warp; cell (c0, c1, c2); sA, sB: the
-// quantisation scales (mode 0: mass, momentum; else the mode's one);
-// ws = the warp's shared workspace
-template <int MODE, int SH>
-__device__ __forceinline__ void box_scatter_cell(BState& b, const Scene& sc, int i0, int i1, int c0, int c1, int c2,
-                                                 float sA, float sB, float* ws) {
-  using SS = ScatterShape<MODE>;
-  constexpr int NV = SS::NV, NQ = SS::NQ, PC = SS::PC, NPQ = SS::NPQ;
-  float* pq = ws;                                   // [PC][16][NPQ], 16-byte aligned
-  float2* tab = reinterpret_cast<float2*>(ws + SS::PQ);  // [PC][3][4]
-  float* val = ws + SS::PQ + SS::TAB;               // [NQ][PC]
-  const int lane = threadIdx.x & 31;
-  const int c[3] = {c0, c1, c2};
-  const long long NP = b.NP;
-  float scale[NV];
-  scale[0] = sA;
-  for (int v = 1; v < NV; ++v) scale[v] = MODE == 0 ? sB : sA;
-  constexpr int tlo = SH == 0 ? 0 : -1, nt = SH == 1 ? 4 : (SH == 2 ? 3 : 2);
-  constexpr int ns = nt * nt * nt;
-  // this lane's slots (box offsets sx, sy, sz)
-  int sx[2], syz[2], sy[2], sz[2];
-  bool use[2];
-  for (int k = 0; k < 2; ++k) {
-    const int slot = lane + 32 * k;
-    use[k] = slot < ns;
-    sz[k] = slot / (nt * nt);
-    const int r2 = slot - sz[k] * nt * nt;
-    sy[k] = r2 / nt;
-    sx[k] = r2 - sy[k] * nt;
-    syz[k] = sz[k] * 4 + sy[k];
-  }
-  const float idc = (float)sc.idcell;
-  float acc[2][NV];
-  for (int k = 0; k < 2; ++k)
-    for (int v = 0; v < NV; ++v) acc[k][v] = 0.f;
-  for (int base = i0; base < i1; base += PC) {
-    const int cnt = min(PC, i1 - base);
-    // particle values, component-major
-    for (int e = lane; e < NQ * PC; e += 32) {
-      const int q = e / PC, p = e % PC;
-      if (p >= cnt) continue;
-      const long long i = base + p;
-      if (MODE == 2) val[e] = b.fs[q * NP + i];
-      else val[e] = q == 0 ? (float)b.mass[i] : (float)b.v[(q - 1) * NP + i];
-    }
-    // 1-D weights and derivatives (per unit length) at offsets tlo + t: lane
-    // a * PC + p takes direction a of particle p
-    if (lane < 3 * PC) {
-      const int p = lane % PC, a = lane / PC;
-      if (p < cnt) {
-        const float off = b.off[a * NP + base + p];
+// -------------------------------------------- particle-parallel scatter
+// Linear, GIMP and B-spline scenes scatter in tasks of 32 consecutive
+// particles of one scene (task t of a scene: its sorted particles 32 t ..
+// 32 t + 31). The lanes of a task that share a sort key (the key's cell, or
+// for GIMP its nearest node) form a segment, and every segment's particles
+// reach the same box of node offsets (2^3 linear, 3^3 GIMP / B-spline). The
+// shapes are tensor products, N = Wx Wy Wz, so a slot's contribution splits
+// into an x factor and a (y, z) factor per channel, e.g. for the force
+//   f_x = Dx (-s_xx Wy Wz) + Wx (b_x Wy Wz - s_xy Dy Wz - s_xz Wy Dz).
+// Two phases through the warp's shared workspace:
+//   1. lane = particle: its x factors (W, and D for the force) per x offset
+//      and its (y, z) factors per channel, one column per lane;
+//   2. lane = box slot: the walk along the task's particles in storage order
+//      (FP32 sums of x factor times (y, z) factor, every channel at once),
+//      flushed at every segment end -- quantised and added to the node's
+//      64-bit accumulators with one integer atomic per channel.
+// The task boundaries are fixed by the scene's own sorted order (32 t from
+// the scene's first particle), so a scene's sums are the same alone or in a
+// batch. Phase 2's walk and its segment ends are the same for every lane
+// (the segment mask comes from a warp vote), so the warp never diverges
+// there.
+template <int MODE>
+struct PartShape {
+  static constexpr int NV = MODE == 0 ? 4 : 3;          // channels
+  static constexpr int NX = MODE == 2 ? 6 : 3;          // x-factor rows (W, and D, per x offset)
+  static constexpr int NK = MODE == 2 ? 2 : 1;          // (y, z) factors per channel and (ty, tz)
+  static constexpr int ROWS = NX + 9 * NV * NK;         // workspace rows (one column per lane)
+  static constexpr int STRIDE = 33;                     // row stride: conflict-free in both phases
+  static constexpr int WARPS = MODE == 2 ? 4 : 8;       // warps (tasks) per block (static shared memory)
+};
+
+// 1-D weight w[t] and derivative d[t] (per unit length) of node offset t
+// from the key's base (linear: 0..1 from the cell; B-spline: -1..1 from the
+// cell; GIMP: -1..1 from the nearest node)
+template <int SH>
+__device__ __forceinline__ void part_tab(float off, float idc, float (&w)[3], float (&d)[3]) {
 #pragma unroll
-        for (int t = 0; t < nt; ++t) {
-          float w, d;
-          if (SH == 0) lin1(tlo + t, off, w, d);
-          else if (SH == 2) bsp1(tlo + t, off, w, d);
-          else gimp1((float)(-(tlo + t)) + off, w, d);
-          tab[(p * 3 + a) * 4 + t] = make_float2(w, d * idc);
-        }
-      }
-    }
-    __syncwarp();
-    // y-z factors per particle and (ty, tz): lane l takes particle l / 4 and
-    // the pairs yz = l % 4 + 4 u (ty = yz % nt, tz = yz / nt), stored at
-    // [p][tz * 4 + ty]
-    {
-      static_assert(PC == 8, "four lanes per staged particle");
-      constexpr int NYZ = nt * nt, NU = (NYZ + 3) / 4;
-      const int p = lane >> 2;
-      if (p < cnt) {
-        float pv[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) pv[q] = val[q * PC + p];
-#pragma unroll
-        for (int u = 0; u < NU; ++u) {
-          const int yz = (lane & 3) + 4 * u;
-          if (yz < NYZ) {
-            const int ty = yz % nt, tz = yz / nt;
-            const float2 y = tab[(p * 3 + 1) * 4 + ty], z = tab[(p * 3 + 2) * 4 + tz];
-            const float A = y.x * z.x;
-            float* o = pq + (p * 16 + tz * 4 + ty) * NPQ;
-            if (MODE == 2) {
-              const float B = y.y * z.x, C = y.x * z.y;
-              const float sxx = pv[0], syy = pv[1], szz = pv[2], sxy = pv[3], syz_ = pv[4], sxz = pv[5];
-              reinterpret_cast<float2*>(o)[0] = make_float2(-sxx * A, pv[6] * A - sxy * B - sxz * C);
-              reinterpret_cast<float2*>(o)[1] = make_float2(-sxy * A, pv[7] * A - syy * B - syz_ * C);
-              reinterpret_cast<float2*>(o)[2] = make_float2(-sxz * A, pv[8] * A - syz_ * B - szz * C);
-            } else {
-              const float M = pv[0] * A;
-              if (MODE == 0)
-                *reinterpret_cast<float4*>(o) = make_float4(M, M * pv[1], M * pv[2], M * pv[3]);
-              else
-                *reinterpret_cast<float4*>(o) = make_float4(M * pv[1], M * pv[2], M * pv[3], 0.f);
-            }
-          }
-        }
-      }
-    }
-    __syncwarp();
-    // particle p's contributions to this lane's slots, in particle order
-    auto add_particle = [&](int p) {
-      for (int k = 0; k < 2; ++k) {
-        if (!use[k]) continue;
-        const float2 x = tab[p * 12 + sx[k]];
-        const float* o = pq + (p * 16 + syz[k]) * NPQ;
-        if (MODE == 2) {
-          const float2 o01 = *reinterpret_cast<const float2*>(o), o23 = *reinterpret_cast<const float2*>(o + 2),
-                       o45 = *reinterpret_cast<const float2*>(o + 4);
-          acc[k][0] += x.y * o01.x + x.x * o01.y;
-          acc[k][1] += x.y * o23.x + x.x * o23.y;
-          acc[k][2] += x.y * o45.x + x.x * o45.y;
-        } else {
-          const float4 m4 = *reinterpret_cast<const float4*>(o);
-          acc[k][0] += x.x * m4.x;
-          acc[k][1] += x.x * m4.y;
-          acc[k][2] += x.x * m4.z;
-          if (MODE == 0) acc[k][3] += x.x * m4.w;
-        }
-      }
-    };
-    if (cnt == PC) {  // a full round (the common case): unrolled, shared-memory offsets constant
-#pragma unroll
-      for (int p = 0; p < PC; ++p) add_particle(p);
+  for (int t = 0; t < 3; ++t) {
+    if (SH == 0) {
+      if (t < 2) lin1(t, off, w[t], d[t]);
+      else w[t] = d[t] = 0.f;
+    } else if (SH == 2) {
+      bsp1(t - 1, off, w[t], d[t]);
     } else {
-      for (int p = 0; p < cnt; ++p) add_particle(p);
+      gimp1(off - (float)(t - 1 + (off >= 0.5f)), w[t], d[t]);  // node = nearest - 1 + t
     }
-    __syncwarp();
+    d[t] *= idc;
   }
-  for (int k = 0; k < 2; ++k) {
-    if (!use[k]) continue;
-    const int jx = c[0] + tlo + sx[k], jy = c[1] + tlo + sy[k], jz = c[2] + tlo + sz[k];
-    if (jx < 0 || jx >= sc.NGx || jy < 0 || jy >= sc.NGy || jz < 0 || jz >= sc.NGz) continue;
-    const long long n = sc.n0 + ((long long)jz * sc.NGy + jy) * sc.NGx + jx;
-    for (int v = 0; v < NV; ++v) {
-      const long long q = quant(acc[k][v], scale[v]);
-      if (q) atomicAdd(&b.acc[v * b.NN + n], (unsigned long long)q);
+}
+
+template <int MODE, int SH>
+__device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, long long i0, int cnt, float sA,
+                                                  float sB, float* ws) {
+  using PS = PartShape<MODE>;
+  constexpr int NV = PS::NV, NX = PS::NX, NK = PS::NK, ST = PS::STRIDE;
+  constexpr int nt = SH == 0 ? 2 : 3, tlo = SH == 0 ? 0 : -1, NS = nt * nt * nt;
+  const int lane = threadIdx.x & 31;
+  const long long NP = b.NP, i = i0 + lane;
+  const int cl = lane < cnt ? b.cell[i] : -1;
+  int c[3] = {0, 0, 0};
+  float off[3] = {0.f, 0.f, 0.f};
+  int key = -1;
+  if (cl >= 0) {
+    c[2] = cl / sc.NCxy;
+    const int rem = cl - c[2] * sc.NCxy;
+    c[1] = rem / sc.NCx;
+    c[0] = rem - c[1] * sc.NCx;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) off[a] = b.off[a * NP + i];
+    if (SH == 1) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) c[a] += off[a] >= 0.5f;
+      key = (c[2] * sc.NGy + c[1]) * sc.NGx + c[0];
+    } else {
+      key = cl;
+    }
+  }
+  // segment ends: the last lane of every run of equal keys
+  const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+  const unsigned lasts = __ballot_sync(0xffffffffu, key >= 0 && (lane == 31 || knext != key));
+  if (lasts == 0u) return;  // (uniform) nothing of this task on the grid
+  const int jend = 32 - __clz(lasts);  // one past the last segment end
+  // the segment's first box node (scene-local flat index) and whether the
+  // whole box lies inside the grid
+  const int nbase = ((c[2] + tlo) * sc.NGy + (c[1] + tlo)) * sc.NGx + (c[0] + tlo);
+  const bool inner = c[0] + tlo >= 0 && c[0] + tlo + nt <= sc.NGx && c[1] + tlo >= 0 && c[1] + tlo + nt <= sc.NGy &&
+                     c[2] + tlo >= 0 && c[2] + tlo + nt <= sc.NGz;
+  // phase 1: the particle's factors (zero for a lane without a key)
+  {
+    constexpr int NQ = MODE == 2 ? 9 : 4;
+    float pv[NQ];
+    float w[3][3], d[3][3];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) pv[q] = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int t = 0; t < 3; ++t) w[a][t] = d[a][t] = 0.f;
+    if (key >= 0) {
+      if (MODE == 2) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) pv[q] = b.fs[q * NP + i];
+      } else {
+        pv[0] = (float)b.mass[i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) pv[1 + a] = (float)b.v[a * NP + i];
+      }
+      const float idc = (float)sc.idcell;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) part_tab<SH>(off[a], idc, w[a], d[a]);
+    }
+    float* col = ws + lane;
+#pragma unroll
+    for (int t = 0; t < nt; ++t) {
+      col[t * ST] = w[0][t];
+      if (MODE == 2) col[(3 + t) * ST] = d[0][t];
+    }
+#pragma unroll
+    for (int tz = 0; tz < nt; ++tz)
+#pragma unroll
+      for (int ty = 0; ty < nt; ++ty) {
+        const int yz = tz * nt + ty;
+        const float A = w[1][ty] * w[2][tz];
+        if (MODE == 2) {
+          const float B = d[1][ty] * w[2][tz], C = w[1][ty] * d[2][tz];
+          // per channel: o0 (times D) and o1 (times W)
+          col[(NX + 0 * 9 + yz) * ST] = -pv[0] * A;
+          col[(NX + 1 * 9 + yz) * ST] = pv[6] * A - pv[3] * B - pv[5] * C;
+          col[(NX + 2 * 9 + yz) * ST] = -pv[3] * A;
+          col[(NX + 3 * 9 + yz) * ST] = pv[7] * A - pv[1] * B - pv[4] * C;
+          col[(NX + 4 * 9 + yz) * ST] = -pv[5] * A;
+          col[(NX + 5 * 9 + yz) * ST] = pv[8] * A - pv[4] * B - pv[2] * C;
+        } else {
+          const float M = pv[0] * A;
+          if (MODE == 0) col[(NX + yz) * ST] = M;
+#pragma unroll
+          for (int a = 0; a < 3; ++a) col[(NX + (MODE == 0 ? 1 + a : a) * 9 + yz) * ST] = M * pv[1 + a];
+        }
+      }
+  }
+  __syncwarp();
+  // phase 2: lane = box slot (sx, sy, sz), the walk along the particles
+  const int sz = lane / (nt * nt), sy = (lane / nt) % nt, sx = lane % nt;
+  const int yz = lane < NS ? sz * nt + sy : 0;
+  const int soff = (sz * sc.NGy + sy) * sc.NGx + sx;
+  const float* xw = ws + (lane < NS ? sx : 0) * ST;
+  const float* xd = ws + (lane < NS ? 3 + sx : 0) * ST;
+  const float* fr = ws + (NX + yz) * ST;
+  float acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = 0.f;
+  for (int j = 0; j < jend; ++j) {
+    const float x = xw[j];
+    if (MODE == 2) {
+      const float dx = xd[j];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) acc[v] += dx * fr[(2 * v) * 9 * ST + j] + x * fr[(2 * v + 1) * 9 * ST + j];
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v] += x * fr[v * 9 * ST + j];
+    }
+    if ((lasts >> j) & 1u) {  // (uniform) segment end: flush its sums into the nodes
+      const int nb = __shfl_sync(0xffffffffu, nbase, j);
+      bool ok = lane < NS;
+      if (!__shfl_sync(0xffffffffu, (int)inner, j)) {  // (uniform) a box at the grid's edge
+        const int jx = __shfl_sync(0xffffffffu, c[0], j) + tlo + sx, jy = __shfl_sync(0xffffffffu, c[1], j) + tlo + sy,
+                  jz = __shfl_sync(0xffffffffu, c[2], j) + tlo + sz;
+        ok = ok && jx >= 0 && jx < sc.NGx && jy >= 0 && jy < sc.NGy && jz >= 0 && jz < sc.NGz;
+      }
+      if (ok) {
+        const long long n = sc.n0 + nb + soff;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const long long q = quant(acc[v], MODE == 0 && v > 0 ? sB : sA);
+          if (q) atomicAdd(&b.acc[v * b.NN + n], (unsigned long long)q);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v] = 0.f;
+    }
+  }
+  __syncwarp();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * PartShape<MODE>::WARPS, MODE == 2 ? 6 : 4) kb_part_scatter(BState b) {
+  using PS = PartShape<MODE>;
+  __shared__ float wsp[PS::WARPS][PS::ROWS * PS::STRIDE];
+  const int warp = threadIdx.x >> 5;
+  const int nt = b.task0[b.nscene];
+  for (int t = blockIdx.x * PS::WARPS + warp; t < nt; t += gridDim.x * PS::WARPS) {
+    // the scene of the task: the last scene whose first task is at or before t
+    int lo = 0, hi = b.nscene - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (b.task0[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const int s = lo;
+    const Scene& sc = b.scenes[s];
+    if (!scene_live(b, s) || (MODE == 1 && !sc.musl)) continue;
+    const long long first = (long long)(t - b.task0[s]) * 32;
+    const int cnt = (int)min(32LL, sc.np - first);
+    const SceneState& st = b.sst[s];
+    const float sA = q_scale(q_shift(sc, st.qmax[MODE == 0 ? Q_MASS : (MODE == 1 ? Q_MOM_MUSL : Q_FORCE)]));
+    const float sB = MODE == 0 ? q_scale(q_shift(sc, st.qmax[Q_MOM])) : sA;
+    float* ws = wsp[warp];
+    switch (sc.shape) {
+      case 0: part_scatter_task<MODE, 0>(b, sc, sc.p0 + first, cnt, sA, sB, ws); break;
+      case 1: part_scatter_task<MODE, 1>(b, sc, sc.p0 + first, cnt, sA, sB, ws); break;
+      default: part_scatter_task<MODE, 2>(b, sc, sc.p0 + first, cnt, sA, sB, ws);
     }
   }
 }
 
-// the scatter of one sort key by one warp: particles [i0, i1) of scene s in
-// cell cl (dual cell d for SGMP)
-// (cell or dual cell (x, y, z), scales sA, sB as box_scatter_cell)
+// the scatter of one SGMP sort key (a dual cell (x, y, z)) by one warp:
+// particles [i0, i1) of scene s, scales sA, sB as sg_scatter_cell
 template <int MODE>
 __device__ __forceinline__ void scatter_cell(BState& b, int i0, int i1, int s, int x, int y, int z, float sA,
                                              float sB, float* ws) {
-  const Scene& sc = b.scenes[s];
-  switch (sc.shape) {
-    case 0: box_scatter_cell<MODE, 0>(b, sc, i0, i1, x, y, z, sA, sB, ws); break;
-    case 1: box_scatter_cell<MODE, 1>(b, sc, i0, i1, x, y, z, sA, sB, ws); break;
-    case 2: box_scatter_cell<MODE, 2>(b, sc, i0, i1, x, y, z, sA, sB, ws); break;
-    default: sg_scatter_cell<MODE>(b, sc, i0, i1, x, y, z, sA, sB, ws);
-  }
+  sg_scatter_cell<MODE>(b, b.scenes[s], i0, i1, x, y, z, sA, sB, ws);
 }
 
-// Scatter over the occupied sort keys (the run-length encoding of the sorted
-// keys, count on the device): a fixed grid, each warp taking chunks of up to
-// 32 consecutive keys. The lanes first load one key's particle range, scene
+// SGMP scatter over the occupied sort keys (listed in ascending order by the
+// sort, count on the device): a fixed grid, each warp taking chunks of up to
+// 32 consecutive keys; keys of the other shape families are skipped (their
+// scenes scatter by particle tasks, kb_part_scatter). The lanes first load one key's particle range, scene
 // and cell each -- one round of dependent loads for the whole chunk instead
 // of one per key -- then the warp scatters the keys in turn. The chunk is
 // sized for the warps of one resident wave (wave), so that the chain of
@@ -627,12 +685,11 @@ __global__ void __launch_bounds__(32 * kCellWarps, 4)
       if (i0 < i1) {
         s = b.scene[i0];
         const Scene& sc = b.scenes[s];
-        const int sg = sc.shape == 3;
-        const int cl = sg ? b.dual[i0] : b.cell[i0];
+        const int cl = sc.shape == 3 ? b.dual[i0] : -1;  // the key's dual cell
         if (cl < 0 || !scene_live(b, s) || (MODE == 1 && !sc.musl)) {
-          s = -1;  // the scene's off-grid bucket, or no transfer this step
+          s = -1;  // another shape family, the off-grid bucket, or no transfer this step
         } else {
-          const int nx = sg ? sc.CNCx : sc.NCx, nxy = sg ? sc.CNCxy : sc.NCxy;
+          const int nx = sc.CNCx, nxy = sc.CNCxy;
           z = cl / nxy;
           const int rem = cl - z * nxy;
           y = rem / nx;
@@ -926,14 +983,28 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   for (int a = 0; a < 3; ++a) vort[a] = vort[a] * DT / 2.f;
   for (int a = 0; a < 3; ++a)
     for (int k = 0; k < 3; ++k) deFp[a][k] *= DT;
-  R Fpn[3][3];
+  R Fpn[3][3], Fpn_lo[3][3];
   if (sc.uvfp) {
-    R F0[3][3];
-    for (int a = 0; a < 9; ++a) F0[a / 3][a % 3] = b.fp[a * NP + i];
+    // Fp(n+1) = (I + dF) Fp(n), i.e. H += dF + dF H for H = Fp - I, with H
+    // carried as a pair hi + lo of FP32 values: the increment in FP32 from
+    // the rounded H, added to the pair without rounding error (TwoSum), so
+    // that H keeps the precision of the increments instead of losing an
+    // FP32 rounding of its whole size every step (a rotated body has |H|
+    // far above its strain)
+    R F0[3][3], L0[3][3];
+    for (int a = 0; a < 9; ++a) {
+      F0[a / 3][a % 3] = b.fp[a * NP + i];
+      L0[a / 3][a % 3] = b.fp[(9 + a) * NP + i];
+    }
     for (int a = 0; a < 3; ++a)
       for (int k = 0; k < 3; ++k) {
-        Fpn[a][k] = F0[a][k] + deFp[a][k] + deFp[a][0] * F0[0][k] + deFp[a][1] * F0[1][k] + deFp[a][2] * F0[2][k];
-        b.fp[(a * 3 + k) * NP + i] = Fpn[a][k];
+        const R inc = deFp[a][k] + (deFp[a][0] * F0[0][k] + deFp[a][1] * F0[1][k] + deFp[a][2] * F0[2][k]);
+        const F2 t = two_sum(F0[a][k], inc);
+        const F2 h = two_sum(t.hi, t.lo + L0[a][k]);
+        Fpn[a][k] = h.hi;
+        Fpn_lo[a][k] = h.lo;
+        b.fp[(a * 3 + k) * NP + i] = h.hi;
+        b.fp[(9 + a * 3 + k) * NP + i] = h.lo;
       }
   }
   PState<R> ps;
@@ -954,7 +1025,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   ps.evol = b.evol[i];
   CResult<R> res;
   constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2,
-                      res);
+                      res, sc.uvfp ? Fpn_lo : nullptr);
   if (res.negative_volume) atomicOr(&b.sst[s].status, (unsigned)ST_NEGATIVE_VOLUME);
   if (!res.eos_ok) atomicOr(&b.sst[s].status, (unsigned)ST_BAD_EOS);
   if (sc.has_jc) {
@@ -1578,7 +1649,7 @@ __device__ __forceinline__ double field_value(const BState& b, int field, long l
     case MPM_P_SM: v = b.sm[i]; break;
     case MPM_P_SEQV: v = b.seqv[i]; break;
     case MPM_P_SD: v = b.sd[c * NP + i]; break;
-    case MPM_P_FP: v = b.fp[c * NP + i]; break;
+    case MPM_P_FP: v = (double)b.fp[c * NP + i] + (double)b.fp[(9 + c) * NP + i]; break;
     case MPM_P_EPEFF: v = b.epeff[i]; break;
     case MPM_P_CELSIUS: v = b.celsius[i]; break;
     case MPM_P_DMG: v = b.dmg[i]; break;

@@ -518,6 +518,14 @@ int mpm_create(const mpm_deck* d, int precision, int device, mpm_ctx** out) {
   const int K = g.K;
   c->nkeys = g.shape == 3 ? (int)nc : (int)nnt;  // pair keys: (component, node) or centre node
   c->npairs = np * K;
+  if (c->npairs >= (1LL << 31) || np >= (1LL << 27) || nnt >= (1LL << 31)) {
+    // pair values hold particle * 32 + slot in 32 bits, segment ends and the
+    // sort's item count are 32-bit ints
+    set_err(c, MPM_ERR_UNSUPPORTED, "FP64 forms: %lld particles x %d slots exceed the 32-bit pair indices", np, K);
+    g_lib_error = c->err;
+    free_ctx(c);
+    return MPM_ERR_UNSUPPORTED;
+  }
   c->key_bits = 1;
   while ((1LL << c->key_bits) <= (long long)c->nkeys) c->key_bits++;
   c->red_blocks = (int)std::min<long long>(1024, (np + kBlock - 1) / kBlock);

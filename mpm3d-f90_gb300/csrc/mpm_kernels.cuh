@@ -411,10 +411,12 @@ __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const De
                                              const typename P::R deFp[3][3], const typename P::R Fpn[3][3],
                                              bool uvfp, typename P::R DT, double time, typename P::R dcell,
                                              typename P::R bq1, typename P::R bq2,
-                                             CResult<typename P::R>& res) {
+                                             CResult<typename P::R>& res,
+                                             const typename P::R (*Fpn_lo)[3] = nullptr) {
   using R = typename P::R;
   Mm<R> m;
   m.dep_set = false;
+  m.has_hlo = Fpn_lo != nullptr;
   m.depeff = (R)0;
   m.bfac = (R)0;
   for (int i = 0; i < 6; ++i) m.dinc[i] = de[i];
@@ -427,6 +429,7 @@ __device__ __forceinline__ void constitution(PState<typename P::R>& ps, const De
         dF[i][j] = deFp[i][j];
         m.Fp[i][j] = Fpn[i][j];
         m.H[i][j] = Fpn[i][j];
+        m.Hlo[i][j] = Fpn_lo ? Fpn_lo[i][j] : (R)0;
       }
     for (int i = 0; i < 3; ++i) {
       dF[i][i] = dF[i][i] + (R)1.0;

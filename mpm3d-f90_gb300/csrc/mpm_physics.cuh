@@ -169,8 +169,90 @@ struct Mm {
   R G2, K3, PlaMod, lamda, miu2, young_, poisson_, yield0_, tmprt, cp, DMG, oldDMG, bfac;
   R Fp[3][3];
   R H[3][3];     // Fp - I as stored per particle (the mixed form works from it)
+  R Hlo[3][3];   // mixed form: the remainder of Fp - I beyond H (Fp - I = H + Hlo)
+  bool has_hlo;  // Hlo is set
   bool dep_set;  // this particle assigned the module variable depeff
 };
+
+// ---------------------------------------- compensated FP32 arithmetic
+// Error-free transformations for the mixed form where the FP64 reference
+// cancels: TwoSum (Knuth) gives s + e = a + b exactly; TwoProduct (one fused
+// multiply-add) gives p + e = a * b exactly. An FFAcc sums terms as an
+// unevaluated pair hi + lo.
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ F2 two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+struct FFAcc {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const F2 t = two_sum(hi, x);
+    hi = t.hi;
+    lo += t.lo;
+  }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const F2 p = two_prod(a, b);
+    add(p.hi);
+    lo += p.lo;
+  }
+  __device__ __forceinline__ float value() const { return hi + lo; }
+};
+
+// B - I (xx, yy, zz, xy, yz, xz) and J - 1 of F = I + H for H carried as
+// Hh + Hl: B - I = H + H^T + H H^T and J - 1 = tr H + I2(H) + det H, the
+// leading terms summed in compensated FP32 and the first-order terms of Hl
+// added to the remainder. A rotation makes H + H^T cancel against H H^T and
+// tr H against I2(H): a body turned by 0.3 rad at strains of 1e-4 would lose
+// three more digits there than FP32 holds.
+__device__ __forceinline__ void bmi_jm1_compensated(const float (*Hh)[3], const float (*Hl)[3], float B[6],
+                                                    float& jm1) {
+  const int bi[6] = {0, 1, 2, 0, 1, 0}, bj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    const int i = bi[e], j = bj[e];
+    FFAcc a;
+    a.add(Hh[i][j]);
+    a.add(Hh[j][i]);
+    a.lo += Hl[i][j] + Hl[j][i];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      a.add_prod(Hh[i][k], Hh[j][k]);
+      a.lo += Hh[i][k] * Hl[j][k] + Hl[i][k] * Hh[j][k];
+    }
+    B[e] = a.value();
+  }
+  FFAcc t;
+  t.add(Hh[0][0]);
+  t.add(Hh[1][1]);
+  t.add(Hh[2][2]);
+  t.lo += Hl[0][0] + Hl[1][1] + Hl[2][2];
+  const int pi[3] = {0, 1, 0}, pj[3] = {1, 2, 2};
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const int i = pi[e], j = pj[e];
+    t.add_prod(Hh[i][i], Hh[j][j]);
+    t.add_prod(-Hh[i][j], Hh[j][i]);
+    t.lo += Hh[i][i] * Hl[j][j] + Hl[i][i] * Hh[j][j] - Hh[i][j] * Hl[j][i] - Hl[i][j] * Hh[j][i];
+  }
+  // det H and its first-order change cof(H) : Hl
+  const float c00 = Hh[1][1] * Hh[2][2] - Hh[1][2] * Hh[2][1], c01 = Hh[1][2] * Hh[2][0] - Hh[1][0] * Hh[2][2],
+              c02 = Hh[1][0] * Hh[2][1] - Hh[1][1] * Hh[2][0];
+  const float c10 = Hh[0][2] * Hh[2][1] - Hh[0][1] * Hh[2][2], c11 = Hh[0][0] * Hh[2][2] - Hh[0][2] * Hh[2][0],
+              c12 = Hh[0][1] * Hh[2][0] - Hh[0][0] * Hh[2][1];
+  const float c20 = Hh[0][1] * Hh[1][2] - Hh[0][2] * Hh[1][1], c21 = Hh[0][2] * Hh[1][0] - Hh[0][0] * Hh[1][2],
+              c22 = Hh[0][0] * Hh[1][1] - Hh[0][1] * Hh[1][0];
+  t.add(Hh[0][0] * c00 + Hh[0][1] * c01 + Hh[0][2] * c02);
+  t.lo += c00 * Hl[0][0] + c01 * Hl[0][1] + c02 * Hl[0][2] + c10 * Hl[1][0] + c11 * Hl[1][1] + c12 * Hl[1][2] +
+          c20 * Hl[2][0] + c21 * Hl[2][1] + c22 * Hl[2][2];
+  jm1 = t.value();
+}
 
 template <class P>
 __device__ __forceinline__ typename P::R equivalent_stress(const Mm<typename P::R>& m) {
@@ -430,6 +512,12 @@ __device__ __forceinline__ void m3dm10(Mm<typename P::R>& m) {
     // B - I = H + H^T + H H^T;  J - 1 = tr H + I2(H) + det H;  ln J = log1p(J - 1)
     const R (*H)[3] = m.H;
     auto hh = [&](int i, int j) { return H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2]; };
+    if (m.has_hlo) {  // H carried as H + Hlo (the batched engine's UpdateVbyFp state)
+      R jm1;
+      bmi_jm1_compensated(m.H, m.Hlo, B, jm1);
+      iJ = (R)1.0 / ((R)1.0 + jm1);
+      lj = log1pf(jm1);
+    } else {
     B[0] = (R)2 * H[0][0] + hh(0, 0);
     B[1] = (R)2 * H[1][1] + hh(1, 1);
     B[2] = (R)2 * H[2][2] + hh(2, 2);
@@ -441,6 +529,7 @@ __device__ __forceinline__ void m3dm10(Mm<typename P::R>& m) {
     R jm1 = (H[0][0] + H[1][1] + H[2][2]) + i2 + det3(H);
     iJ = (R)1.0 / ((R)1.0 + jm1);
     lj = log1pf(jm1);
+    }
   }
   m.ieinc = sig_work(m);
   R* sig = m.sig;

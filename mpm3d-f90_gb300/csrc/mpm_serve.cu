@@ -9,13 +9,18 @@
 //   1. admit queued scenes -- in submission order, or least work first --
 //      while the estimated device bytes of the resident scenes stay within the
 //      budget (and their particles within the optional cap);
-//   2. run min(chunk_steps, steps until the next scene finishes) steps of the
-//      batch (graph replays; the batch recaptures after a composition change);
+//   2. hand the batch to the device loop (mpm_batch_run_loop): one graph
+//      launch in which the device repeats steps until a resident scene takes
+//      its last step, chunk_steps steps are taken, or a submission raises the
+//      batch's interrupt flag (a page-locked word the device reads once per
+//      two steps);
 //   3. read every resident scene's progress in one copy, snapshot the fields
 //      of the finished ones, retire them and wake their waiters.
-// The launch shape autotuner times the candidate (particle block, node block)
-// pairs on the first chunks (a launch shape changes no result) and keeps the
-// fastest per particle-step.
+// The launch shape autotuner times every candidate (particle block, node
+// block, scatter blocks per SM) on one frozen composition -- the first whose
+// scenes all have the steps for the sweep left -- two rounds in opposite
+// orders (a launch shape changes no result), and keeps the fastest per
+// particle-step.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -63,7 +68,7 @@ struct Ticket {
 };
 
 struct Tune {
-  int pb, nb;
+  int pb, nb, sb;           // particle block, node block, scatter blocks per SM
   double ms = 0, work = 0;  // accumulated time and particle-steps
 };
 
@@ -84,10 +89,8 @@ struct mpm_server {
   // statistics
   long long submitted = 0, finished = 0, chunks = 0;
   double particle_steps = 0, busy_ms = 0;
-  int pb = 256, nb = 256;
+  int pb = 256, nb = 256, sb = 64;
   std::vector<Tune> tune;
-  size_t tune_next = 0;
-  int tune_rounds = 0;
   bool tuned = false;
   std::string err;
 };
@@ -221,43 +224,67 @@ void serve_loop(mpm_server* s) {
         s->cv_work.wait(lk);
       }
     }
-    // 2. a chunk of steps (server thread only touches the batch)
+    // 2. the device loop (server thread only touches the batch): the device
+    // steps the batch until a resident scene takes its last step, the step
+    // budget is spent, or a submission interrupts it
     int r = mpm_batch_commit(s->batch);
-    if (r == MPM_OK) r = mpm::batch_progress(s->batch, prog);
-    int left = 0;
-    if (r == MPM_OK) mpm::batch_remaining(s->batch, prog, &left);
-    int k = std::max(1, std::min(s->cfg.chunk_steps, left > 0 ? left : 1));
-    double work = 0;  // particle-steps this chunk runs (parked scenes do no work)
-    for (const BatchProgress& q : prog) work += (double)q.np * std::max(0, std::min(k, q.target - q.istep));
-    Tune* trial = nullptr;
+    std::vector<BatchProgress> before;
+    if (r == MPM_OK) r = mpm::batch_progress(s->batch, before);
+    auto work_since = [&](const std::vector<BatchProgress>& a, const std::vector<BatchProgress>& b2) {
+      double w = 0;  // particle-steps taken between two progress reads (parked scenes take none)
+      for (const BatchProgress& q : b2)
+        for (const BatchProgress& p0 : a)
+          if (p0.id == q.id) w += (double)q.np * std::max(0, q.istep - p0.istep);
+      return w;
+    };
     if (r == MPM_OK && s->cfg.autotune && !s->tuned) {
-      trial = &s->tune[s->tune_next];
-      r = mpm_batch_set_blocks(s->batch, trial->pb, trial->nb);
-    }
-    double ms = 0;
-    if (r == MPM_OK) r = mpm_batch_time_steps(s->batch, k, 1, &ms);
-    if (r == MPM_OK && trial) {
-      trial->ms += ms;
-      trial->work += work;
-      s->tune_next++;
-      if (s->tune_next == s->tune.size()) {
-        // two rounds over the candidates, then keep the best
-        bool measured = true;
-        for (auto& c : s->tune) measured = measured && c.work > 0;
-        if (measured && ++s->tune_rounds >= 2) {
+      // every candidate timed on this one composition (no admission or
+      // retirement between the trials), two rounds in opposite orders; only
+      // when every resident scene has the steps for the whole sweep left
+      const int per = 2;
+      int left = 1 << 30;
+      for (const BatchProgress& q : before) left = std::min(left, q.target - q.istep);
+      if (left >= (int)(2 * per * s->tune.size() + 1)) {
+        for (int round = 0; round < 2 && r == MPM_OK; ++round)
+          for (size_t n = 0; n < s->tune.size() && r == MPM_OK; ++n) {
+            Tune& c = s->tune[round ? s->tune.size() - 1 - n : n];
+            r = mpm_batch_set_blocks(s->batch, c.pb, c.nb);
+            if (r == MPM_OK) r = mpm_batch_set_option(s->batch, MPM_BATCH_SCATTER_BLOCKS, c.sb);
+            std::vector<BatchProgress> a, z;
+            if (r == MPM_OK) r = mpm::batch_progress(s->batch, a);
+            double tms = 0;
+            if (r == MPM_OK) r = mpm_batch_time_steps(s->batch, per, 1, &tms);
+            if (r == MPM_OK) r = mpm::batch_progress(s->batch, z);
+            if (r == MPM_OK) {
+              const double w = work_since(a, z);
+              c.ms += tms;
+              c.work += w;
+              std::lock_guard<std::mutex> lk(s->mu);
+              s->particle_steps += w;
+              s->busy_ms += tms;
+            }
+          }
+        if (r == MPM_OK) {
           const Tune* best = &s->tune[0];
           for (auto& c : s->tune)
-            if (c.ms / c.work < best->ms / best->work) best = &c;
+            if (c.work > 0 && (best->work <= 0 || c.ms / c.work < best->ms / best->work)) best = &c;
           s->pb = best->pb;
           s->nb = best->nb;
+          s->sb = best->sb;
           s->tuned = true;
           r = mpm_batch_set_blocks(s->batch, s->pb, s->nb);
+          if (r == MPM_OK) r = mpm_batch_set_option(s->batch, MPM_BATCH_SCATTER_BLOCKS, s->sb);
         }
-        s->tune_next = 0;
+        if (r == MPM_OK) r = mpm::batch_progress(s->batch, before);
       }
     }
-    // 3. retirement
+    int taken = 0;
+    Clock::time_point t0 = Clock::now();
+    if (r == MPM_OK) r = mpm_batch_run_loop(s->batch, s->cfg.chunk_steps, &taken);
+    const double ms = ms_since(t0, Clock::now());
     if (r == MPM_OK) r = mpm::batch_progress(s->batch, prog);
+    const double work = r == MPM_OK ? work_since(before, prog) : 0.0;
+    // 3. retirement
     retire.clear();
     std::vector<Ticket*> done;
     if (r == MPM_OK) {
@@ -308,6 +335,7 @@ void serve_loop(mpm_server* s) {
           s->err = "batch lost after error: " + msg;
         } else {
           mpm_batch_set_blocks(s->batch, s->pb, s->nb);
+          mpm_batch_set_option(s->batch, MPM_BATCH_SCATTER_BLOCKS, s->sb);
         }
       }
     }
@@ -341,9 +369,10 @@ int mpm_serve_create(const mpm_serve_config* cfg, mpm_server** out) {
     s->cfg.hbm_budget_bytes = (int64_t)(0.35 * (double)fr);
   }
   if (s->cfg.autotune) {
-    const int cand[3] = {128, 256, 512};
-    for (int a : cand)
-      for (int b2 : cand) s->tune.push_back(Tune{a, b2});
+    const int blk[2] = {256, 512}, sbs[3] = {8, 32, 64};
+    for (int a : blk)
+      for (int b2 : blk)
+        for (int c : sbs) s->tune.push_back(Tune{a, b2, c});
   }
   s->thr = std::thread(serve_loop, s);
   *out = s;
@@ -394,6 +423,9 @@ int mpm_serve_submit(mpm_server* s, const mpm_deck* d, int steps, uint32_t field
     s->queue.push_back(t->id);
     s->submitted++;
     *ticket = t->id;
+    // a running device loop returns at its next test, so that the server
+    // can admit the scene (the flag is a page-locked word, no CUDA call)
+    if (s->batch) mpm_batch_interrupt(s->batch);
   }
   s->cv_work.notify_all();
   return MPM_OK;
@@ -457,6 +489,15 @@ int mpm_serve_release(mpm_server* s, int64_t ticket) {
   delete t;
   s->tickets.erase(it);
   return MPM_OK;
+}
+
+int mpm_serve_launch_shape(mpm_server* s, int* particle_block, int* node_block, int* scatter_blocks) {
+  if (!s || !particle_block || !node_block || !scatter_blocks) return MPM_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  *particle_block = s->pb;
+  *node_block = s->nb;
+  *scatter_blocks = s->sb;
+  return s->tuned ? MPM_OK : MPM_ERR_STATE;
 }
 
 int mpm_serve_stats(mpm_server* s, double* o) {

@@ -124,6 +124,9 @@ def library() -> ctypes.CDLL:
         "mpm_batch_device_bytes": (i64, [vp]),
         "mpm_batch_scene_count": (i, [vp]),
         "mpm_batch_run": (i, [vp, i, i]),
+        "mpm_batch_run_loop": (i, [vp, i, P(i)]),
+        "mpm_serve_launch_shape": (i, [vp, P(i), P(i), P(i)]),
+        "mpm_batch_interrupt": (i, [vp]),
         "mpm_batch_sync": (i, [vp]),
         "mpm_batch_time_steps": (i, [vp, i, i, P(d)]),
         "mpm_batch_scene_scalars": (i, [vp, i, P(d)]),
@@ -490,7 +493,7 @@ class MpmStep:
         return int(library().mpm_device_bytes(self._h))
 
 
-BATCH_OPTIONS = {"particle_block": 1, "node_block": 2}
+BATCH_OPTIONS = {"particle_block": 1, "node_block": 2, "scatter_blocks": 3}
 
 
 class Batch:
@@ -554,6 +557,18 @@ class Batch:
 
     def sync(self) -> None:
         self._check(library().mpm_batch_sync(self._h))
+
+    def run_loop(self, max_steps: int) -> int:
+        """Device-resident run: the device repeats steps until a scene takes
+        its last step, max_steps are taken, or :meth:`interrupt` is called;
+        returns the steps taken."""
+        n = ctypes.c_int()
+        self._check(library().mpm_batch_run_loop(self._h, int(max_steps), ctypes.byref(n)))
+        return n.value
+
+    def interrupt(self) -> None:
+        """Ask a running :meth:`run_loop` (on another thread) to return."""
+        self._check(library().mpm_batch_interrupt(self._h))
 
     def time_steps(self, nsteps: int, graph: bool = True) -> float:
         ms = ctypes.c_double()
@@ -798,6 +813,15 @@ class Server:
         o = np.zeros(10)
         self._check(library().mpm_serve_stats(self._h, _dptr(o)))
         return dict(zip(SERVE_STATS, o.tolist()))
+
+    def launch_shape(self) -> Optional[dict]:
+        """The autotuned launch shape, None before the tuner has chosen."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        st = library().mpm_serve_launch_shape(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        if st == 9:
+            return None
+        self._check(st)
+        return {"particle_block": a.value, "node_block": b.value, "scatter_blocks_per_sm": c.value}
 
     def drain(self, timeout_ms: int = -1) -> bool:
         st = library().mpm_serve_drain(self._h, int(timeout_ms))

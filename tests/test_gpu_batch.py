@@ -153,6 +153,9 @@ def test_serving_runtime(built):
             assert srv.wait(t, 300000)
         st = srv.stats()
         assert st["finished"] == 16 and st["resident"] == 0 and st["queued"] == 0
+        # the autotuner timed its candidates on one composition and chose
+        shape = srv.launch_shape()
+        assert shape is not None and shape["scatter_blocks_per_sm"] in (8, 32, 64)
         for t in tickets:
             r = srv.result(t)
             assert r["istep"] == 60
@@ -267,3 +270,105 @@ def test_run_splitting_and_energies(built, name):
         assert sc == out[0][0]
         for f in PFIELDS:
             np.testing.assert_array_equal(fields[f], out[0][1][f], err_msg=f"{name} {f}")
+
+
+def _outlier_deck(outlier: bool) -> str:
+    """A GIMP elastic block drifting at 0.05 m/s and, with outlier, one more
+    particle of the same mass two cells above it moving at 5 m/s -- 100 times
+    the block's speed, so that its momentum alone sets the scene's
+    fixed-point bound for the momentum transfers. The two share no node."""
+    from mpm3d_gb300.decks import DeckWriter, _grid_lines, f32s
+    dp, h = 0.5, 1.0
+    w = DeckWriter("elastic block with an outlier particle")
+    w.kw("nmat 1")
+    w.head += _grid_lines(((-2.0, 6.0), (-2.0, 4.0), (0.0, 9.0)), h)
+    w.kw("dtsc 0.5")
+    w.kw("endt 100.0")
+    w.kw("usf on")
+    w.kw("gimp")
+    w.kw("fixe 0 0 0 0 1 0")
+    w.kw("mate")
+    w.kw("1 elas 1000 1e7 0.3")
+    w.block(1, 1000.0, dp, (0.0, 0.0, h), (8, 4, 6))
+    velo = ["velo", "body 1 0 0 %s" % f32s(-0.05)]
+    if outlier:
+        w.block(1, 1000.0, dp, (1.0, 1.0, 6.5), (1, 1, 1))
+        velo.append("body 2 %s 0 0" % f32s(5.0))
+    w.tail += velo + ["endv"]
+    return w.text()
+
+
+def test_mixed_outlier_particle(built):
+    """The fixed-point scale of a scene's grid sums comes from its largest
+    single contribution. One particle 100 times faster than the rest must not
+    coarsen the others' sums: the block's particle fields keep the same
+    error against FP64 with the outlier present as without it."""
+    from mpm3d_gb300 import Deck, MpmStep
+    errs = {}
+    for outlier in (False, True):
+        d = Deck.parse(_outlier_deck(outlier))
+        a = MpmStep(d, "fp64")
+        b = MpmStep(d, "mixed")
+        a.run(60)
+        b.run(60)
+        nb = 8 * 4 * 6
+        e = {}
+        for f in ("SM", "SD", "VXp"):
+            fa, fb = a.download(f), b.download(f)
+            fa = fa.reshape(-1, d.nb_particle)[:, :nb]
+            fb = fb.reshape(-1, d.nb_particle)[:, :nb]
+            e[f] = _rel(fa, fb)
+        errs[outlier] = e
+        if outlier:  # the outlier really dominates the momentum bound
+            v = a.download("VXp").reshape(3, -1)
+            assert np.max(np.abs(v[:, nb:])) > 50 * np.max(np.abs(v[:, :nb]))
+        a.close()
+        b.close()
+    # (the outlier also shortens DT by a few per cent, so the two runs do not
+    # take the same steps: the bound is an order of magnitude, not equality)
+    for f, e in errs[True].items():
+        assert e <= 1e-5, f"{f}: {e:.3g} with the outlier"
+        assert e <= 10 * max(errs[False][f], 1e-7), f"{f}: {e:.3g} with the outlier, {errs[False][f]:.3g} without"
+
+
+def test_batch_device_loop(built):
+    """The device-resident run loop: the device repeats steps until a scene
+    takes its last step (or the step budget is spent, or the host interrupts
+    it), with the same results as host-driven runs."""
+    import threading
+    from mpm3d_gb300 import Batch, Deck, decks
+    dk = [Deck.parse(decks.soft_beam()), Deck.parse(decks.soil_slope(dp=0.5, width=2.0))]
+    with Batch() as ref:
+        a = ref.add(dk[0], steps=40)
+        b = ref.add(dk[1], steps=25)
+        ref.run(41)
+        ref.sync()
+        want = {s: {f: ref.download(s, f) for f in PFIELDS} for s in (a, b)}
+    with Batch() as bt:
+        a = bt.add(dk[0], steps=40)
+        b = bt.add(dk[1], steps=25)
+        assert bt.run_loop(7) == 7  # the budget
+        # steps 8.. in one launch: the loop test after each pair of steps sees
+        # scene b take its last step (25) in the pair (25, 26)
+        assert bt.run_loop(1000) == 19
+        assert bt.scalars(b)["istep"] == 25 and bt.scalars(a)["istep"] == 26
+        assert bt.run_loop(1000) == 15  # scene a's last step (40) in the pair (40, 41)
+        assert bt.scalars(a)["istep"] == 40
+        assert bt.run_loop(1000) == 1  # nothing left to do: the first step only
+        bt.sync()
+        for s in (a, b):
+            for f in PFIELDS:
+                assert np.array_equal(bt.download(s, f), want[s][f]), (s, f)
+    # the host interrupts a loop that would otherwise run for 10^6 steps
+    with Batch() as bt:
+        s = bt.add(dk[0], steps=1_000_000)
+        bt.commit()
+        got = {}
+        th = threading.Thread(target=lambda: got.setdefault("n", bt.run_loop(1_000_000)))
+        th.start()
+        time.sleep(0.3)
+        bt.interrupt()
+        th.join(timeout=60)
+        assert not th.is_alive() and 1 <= got["n"] < 1_000_000
+        assert bt.scalars(s)["istep"] == got["n"]
+        assert bt.run_loop(5) == 5  # the request was consumed
