@@ -507,7 +507,26 @@ def run_serving(args, device: int) -> dict:
     target = None
     if args.target_stride > 0:
         target = serving_vs_fp64(args, device, dks, nps, out["fifo"]["particle_steps_per_s"])
+    if not args.no_cpu_baseline:
+        out["cpu_baseline_per_scene"] = serving_cpu_baseline()
     return out, target
+
+
+def serving_cpu_baseline(steps: int = 2) -> list:
+    """The oracle (the CPU port of the reference step, one core) on serving
+    scenes of each kind at 2k, 40k and 400k particles: a bounded sample of
+    `steps` timed steps after one untimed step, per scene."""
+    import numpy as np
+    from mpm3d_gb300 import decks
+
+    out = []
+    for kind in ("cook", "beam"):
+        for n in (2000, 40000, 400000):
+            text, npart, _ = decks.serving_scene(np.random.default_rng(n), n, n, kind=kind)
+            cb = cpu_baseline(text, steps, npart)
+            out.append({"kind": kind, "particles": npart, "particle_steps_per_s": cb["value"], "cores": 1,
+                        "sample": cb["sample"]})
+    return out
 
 
 def serving_vs_fp64(args, device: int, dks, nps, served_rate: float) -> dict:
@@ -563,9 +582,9 @@ def serve_scenes(args, device: int, dks, nps, arrivals, policy: str, cap: int) -
     import numpy as np
     import mpm3d_gb300 as m
 
-    # the device loop returns when a scene finishes or a submission arrives;
-    # chunk_steps only bounds a loop that neither ends
-    with m.Server(device=device, chunk_steps=500, autotune=True, policy=policy, max_resident_particles=cap) as srv:
+    # the device loop returns when a scene finishes, or after at least
+    # chunk_steps steps when a submission is waiting
+    with m.Server(device=device, chunk_steps=25, autotune=True, policy=policy, max_resident_particles=cap) as srv:
         tickets = []
         t0 = time.perf_counter()
         for k, d in enumerate(dks):

@@ -208,9 +208,9 @@ int mpm_batch_run(mpm_batch* b, int nsteps, int use_graph);
  * taken, or after mpm_batch_interrupt; *steps receives the steps taken (at
  * least 1, at most max_steps). */
 int mpm_batch_run_loop(mpm_batch* b, int max_steps, int* steps);
-/* Ask a running device loop to return at its next test (two steps at most);
- * callable from any thread. The request is cleared when mpm_batch_run_loop
- * returns. */
+/* Ask a running device loop to return at its next test (two steps at most,
+ * once MPM_BATCH_LOOP_MIN_STEPS steps are taken); callable from any thread.
+ * The request is cleared when mpm_batch_run_loop returns. */
 int mpm_batch_interrupt(mpm_batch* b);
 int mpm_batch_sync(mpm_batch* b);
 int mpm_batch_time_steps(mpm_batch* b, int nsteps, int use_graph, double* ms);
@@ -229,7 +229,8 @@ int mpm_batch_set_blocks(mpm_batch* b, int particle_block, int node_block);
 enum mpm_batch_option {
   MPM_BATCH_PARTICLE_BLOCK = 1,
   MPM_BATCH_NODE_BLOCK = 2,
-  MPM_BATCH_SCATTER_BLOCKS = 3 /* grid cap of the particle -> grid transfers, blocks per SM (1..64) */
+  MPM_BATCH_SCATTER_BLOCKS = 3, /* grid cap of the particle -> grid transfers, blocks per SM (1..64) */
+  MPM_BATCH_LOOP_MIN_STEPS = 4  /* steps a device loop takes before it honours mpm_batch_interrupt (0) */
 };
 int mpm_batch_set_option(mpm_batch* b, int option, int value);
 int mpm_batch_get_option(const mpm_batch* b, int option);
@@ -273,9 +274,10 @@ int mpm_snapshot_load(mpm_ctx* ctx, const char* path);
 typedef struct mpm_server mpm_server;
 typedef struct mpm_serve_config {
   int device;               /* CUDA device, -1 = current                        */
-  int chunk_steps;          /* most steps the device loop takes before it returns
-                               to the server (0 = 25); it returns earlier when a
-                               scene finishes or a submission arrives          */
+  int chunk_steps;          /* steps between admission points (0 = 25): the device
+                               loop returns when a scene finishes, or when a
+                               submission is waiting and it has taken this many
+                               steps                                            */
   int64_t hbm_budget_bytes; /* sum of the resident scenes' mpm_scene_device_bytes
                                (0 = 35% of free memory: a batch keeps two arenas) */
   int max_scenes;           /* resident scene cap (0 = 4096)                     */

@@ -206,6 +206,7 @@ struct mpm_batch {
   int scatter_wave = 4864;    // scatter warps resident at once (4 blocks per SM)
   int sort_blocks = 152;      // grid of the long-segment sort (one block per SM)
   int sms = 152;              // multiprocessors of the device
+  int loop_min_steps = 0;     // steps a device loop takes before it honours an interrupt
   long long ntask = 0;        // particle tasks of the linear / GIMP / B-spline scenes (32 particles each)
   // device-resident run loop (mpm_batch_run_loop): its state, the host's
   // request flag (page-locked, mapped into the device's address space) and
@@ -578,16 +579,17 @@ __device__ __forceinline__ void loop_decide(const BState& b, const int* target, 
   pending = __syncthreads_or(pending);
   if (threadIdx.x == 0) {
     const LoopCtl& c = *b.ctl;
-    const bool go = pending && c.finished == c.fin0 && *flag == 0 && c.iters < c.max_iters;
+    const bool go = pending && c.finished == c.fin0 && (*flag == 0 || c.iters < c.min_iters) && c.iters < c.max_iters;
     cudaGraphSetConditional(h, go ? 1u : 0u);
   }
 }
 
 // before the loop's first step: budget, iteration count, finished-scene mark
-__global__ void kb_loop_arm(LoopCtl* c, int max_iters) {
+__global__ void kb_loop_arm(LoopCtl* c, int max_iters, int min_iters) {
   c->fin0 = c->finished;
   c->iters = 0;
   c->max_iters = max_iters;
+  c->min_iters = min_iters;
 }
 
 __global__ void kb_loop_start(BState b, const int* target, const volatile int* flag, cudaGraphConditionalHandle h) {
@@ -1144,7 +1146,7 @@ int mpm_batch_run_loop(mpm_batch* b, int max_steps, int* steps) {
   *b->loop_flag_h = 0;
   // the first step (its reduction overlaps the loop's first step), then the
   // loop's iterations of two steps, then the last step's reduction
-  kb_loop_arm<<<1, 1, 0, b->stream>>>(b->ctl, (max_steps - 1) / 2);
+  kb_loop_arm<<<1, 1, 0, b->stream>>>(b->ctl, (max_steps - 1) / 2, b->loop_min_steps / 2);
   if ((r = replay_step(b, 0))) return r;
   const int par = b->A.x == b->set0_x ? 0 : 1;
   if (!b->loop_graph[par]) {
@@ -1478,6 +1480,10 @@ int mpm_batch_set_option(mpm_batch* b, int option, int value) {
         drop_graph(b);
       }
       return MPM_OK;
+    case MPM_BATCH_LOOP_MIN_STEPS:
+      if (value < 0) return berr(b, MPM_ERR_ARG, "loop minimum steps %d < 0", value);
+      b->loop_min_steps = value;
+      return MPM_OK;
     default: return berr(b, MPM_ERR_ARG, "unknown batch option %d", option);
   }
 }
@@ -1488,6 +1494,7 @@ int mpm_batch_get_option(const mpm_batch* b, int option) {
     case MPM_BATCH_PARTICLE_BLOCK: return b->pblock;
     case MPM_BATCH_NODE_BLOCK: return b->nblock;
     case MPM_BATCH_SCATTER_BLOCKS: return b->scatter_blocks / b->sms;
+    case MPM_BATCH_LOOP_MIN_STEPS: return b->loop_min_steps;
     default: return -1;
   }
 }

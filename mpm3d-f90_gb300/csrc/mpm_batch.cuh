@@ -71,6 +71,8 @@ struct LoopCtl {
   int fin0;       // finished when the loop began
   int iters;      // loop iterations taken (two steps each)
   int max_iters;  // iteration budget
+  int min_iters;  // iterations before an interrupt is honoured
+  int pad_;
 };
 
 struct BState {

@@ -66,9 +66,9 @@ __global__ void kb_begin(BState b, const int* target) {
 }
 
 // cell of a position (InWhichCell, Grid.f90:123-155) and the offset in it, in
-// cells (FP32); false off the grid. The sort keys and the per-step particle
-// data use this one routine, so that a particle's key and its shape-function
-// offsets agree exactly.
+// cells (FP32); false off the grid. Every transfer and gather takes a
+// particle's cell and shape-function offsets from this one routine (through
+// the per-step data the permutation writes).
 __device__ __forceinline__ bool cell_of(const Scene& sc, const double x[3], int cc[3], float off[3]) {
   bool in = true;
   for (int a = 0; a < 3; ++a) {
@@ -105,7 +105,7 @@ __device__ __forceinline__ long long dual_cell(const Scene& sc, const double x[3
 // 3 box of nodes instead of the 4 x 4 x 4 box of a cell's particles.
 __global__ void kb_keys(BState b) {
   const long long i = btid();
-  long long key = -1;
+  unsigned key = 0xffffffffu;
   if (i < b.NP) {
     const long long NP = b.NP;
     const Scene& sc = b.scenes[b.scene[i]];
@@ -114,24 +114,39 @@ __global__ void kb_keys(BState b) {
     if (sc.shape == 3) {
       c = dual_cell(sc, x);
     } else {
+      // The coordinate in cells is formed in FP64 and rounded to FP32 once;
+      // the rest is FP32 / integer work (GB300's FP64 pipe is narrow). The
+      // sort only groups particles: the transfers take every particle's cell
+      // and offsets from the permutation's exact routine (cell_of), so a
+      // particle that this rounding puts on the other side of a cell face
+      // (or of the grid's edge) is still transferred exactly, in a segment
+      // of its own.
       int cc[3];
-      float off[3];
-      if (cell_of(sc, x, cc, off)) {
+      float u[3];
+      bool in = true;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        u[a] = (float)((x[a] - sc.span0[a]) * sc.idcell);
+        in = in && u[a] >= 0.f;
+        cc[a] = (int)u[a];
+      }
+      if (in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz) {
         if (sc.shape == 1) {  // nearest node: the cell's lower node, or the upper one from half a cell on
-          for (int a = 0; a < 3; ++a) cc[a] += off[a] >= 0.5f;
+#pragma unroll
+          for (int a = 0; a < 3; ++a) cc[a] += u[a] - (float)cc[a] >= 0.5f;
           c = ((long long)cc[2] * sc.NGy + cc[1]) * sc.NGx + cc[0];
         } else {
           c = ((long long)cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0];
         }
       }
     }
-    key = sc.k0 + (c >= 0 ? c : sc.nk - 1);
-    b.key[i] = (unsigned)key;
+    key = (unsigned)(sc.k0 + (c >= 0 ? c : sc.nk - 1));
+    b.key[i] = key;
   }
   // per-key counts: the particles arrive sorted by the last step's keys, so
   // a warp's lanes mostly share a few keys -- one atomic per key and warp
   const unsigned grp = __match_any_sync(0xffffffffu, key);
-  if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&b.seg[key], __popc(grp));
+  if (key != 0xffffffffu && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&b.seg[key], __popc(grp));
 }
 
 // ---------------------------------------------------- permutation + derived

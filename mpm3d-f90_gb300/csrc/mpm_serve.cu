@@ -11,9 +11,9 @@
 //      budget (and their particles within the optional cap);
 //   2. hand the batch to the device loop (mpm_batch_run_loop): one graph
 //      launch in which the device repeats steps until a resident scene takes
-//      its last step, chunk_steps steps are taken, or a submission raises the
-//      batch's interrupt flag (a page-locked word the device reads once per
-//      two steps);
+//      its last step or, once chunk_steps steps are taken, a submission has
+//      raised the batch's interrupt flag (a page-locked word the device reads
+//      once per two steps);
 //   3. read every resident scene's progress in one copy, snapshot the fields
 //      of the finished ones, retire them and wake their waiters.
 // The launch shape autotuner times every candidate (particle block, node
@@ -45,6 +45,10 @@ using mpm::HostScene;
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+// steps a device loop may take at most (it ends earlier when a scene
+// finishes or, after chunk_steps steps, when a submission arrives)
+constexpr int kLoopBudget = 1 << 20;
 
 double ms_since(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
@@ -278,9 +282,12 @@ void serve_loop(mpm_server* s) {
         if (r == MPM_OK) r = mpm::batch_progress(s->batch, before);
       }
     }
+    // submissions are admitted at most every chunk_steps steps: the loop
+    // honours their interrupt only after that many steps
     int taken = 0;
     Clock::time_point t0 = Clock::now();
-    if (r == MPM_OK) r = mpm_batch_run_loop(s->batch, s->cfg.chunk_steps, &taken);
+    if (r == MPM_OK) r = mpm_batch_set_option(s->batch, MPM_BATCH_LOOP_MIN_STEPS, s->cfg.chunk_steps);
+    if (r == MPM_OK) r = mpm_batch_run_loop(s->batch, kLoopBudget, &taken);
     const double ms = ms_since(t0, Clock::now());
     if (r == MPM_OK) r = mpm::batch_progress(s->batch, prog);
     const double work = r == MPM_OK ? work_since(before, prog) : 0.0;

@@ -493,7 +493,7 @@ class MpmStep:
         return int(library().mpm_device_bytes(self._h))
 
 
-BATCH_OPTIONS = {"particle_block": 1, "node_block": 2, "scatter_blocks": 3}
+BATCH_OPTIONS = {"particle_block": 1, "node_block": 2, "scatter_blocks": 3, "loop_min_steps": 4}
 
 
 class Batch:

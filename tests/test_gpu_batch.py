@@ -10,24 +10,42 @@ from gpu_cases import CASES
 
 pytestmark = pytest.mark.gpu
 
-# Relative error bound of the mixed form against FP64 (max |a - b| / max |a|
-# per field) after the case's step count. Elastic, hyperelastic, Drucker-
-# Prager, J2-plastic and fluid cases stay near FP32 rounding (< 1e-4; most
-# are ~1e-6). Johnson-Cook cases amplify rounding through the plastic return
-# map and the rate term (the FP64 form itself moves by ~1e-2 in SD over 1000
-# Taylor steps when only the libm changes), so they get a looser bound; with
-# failure ('sjcf') a particle's failure flag flips on a threshold, so
-# rounding-level differences switch individual particles between failed and
-# intact and the fields differ locally by O(1) of those particles' share.
+# Relative error bound of the mixed form against FP64 strict (max |a - b| /
+# max |a| per field) after the case's step count: 1e-5, the bound the mixed
+# form is held to. Where a case cannot meet it, the bound below says why, with
+# the numbers measured on a GB300 beside it -- the mixed error and the spread
+# of the FP64 strict form itself when its initial positions are perturbed by
+# 1e-12 (relative, seeded), which measures how much the case amplifies any
+# perturbation:
+# * Johnson-Cook cases: the plastic threshold switches particles between
+#   elastic and plastic steps, which amplifies rounding-size differences by
+#   orders of magnitude. Taylor bar ('jcf', 100 steps): SD 5.4e-2 mixed, 6.8e-5
+#   from a 1e-12 FP64 perturbation; the other fields 1.3e-5..5.6e-5.
+#   Simplified Johnson-Cook + Gruneisen (80 steps): mixed 1.0e-3 / 4.0e-3 /
+#   3.4e-3 (PXg / SM / SD), the 1e-12 FP64 perturbation 8.2e-4 / 4.9e-3 /
+#   2.4e-3 -- the case is chaotic at any precision. With failure ('sjcf'),
+#   rounding flips individual particles' failure flags: PXg 2.0e-2 mixed, 1.2e-3
+#   from the FP64 perturbation.
+# * Nearly incompressible neo-Hookean Cook membranes (nu = 0.499): the mean
+#   stress is lamda ln J with lamda = 499 G, and the trace of the FP32 velocity
+#   gradient that drives J cancels about 500:1, so SM keeps FP32 rounding
+#   times ~500: 1.3e-5 after 300 B-spline steps (other fields <= 6e-7).
 MIXED_TOL = {
-    "taylor_small_usf_jcf_linear": 0.1,
-    "block_musl_sjc_gruneisen": 2e-2,
-    "block_usf_sjcf_gruneisen": 5e-2,
+    "taylor_small_usf_jcf_linear": {"SD": 0.1, "*": 1e-4},
+    "block_musl_sjc_gruneisen": {"*": 2e-2},
+    "block_usf_sjcf_gruneisen": {"*": 5e-2},
 }
-DEFAULT_TOL = 1e-4
+DEFAULT_TOL = 1e-5
+COOK_TOL = {"SM": 3e-5, "*": DEFAULT_TOL}
 # Spre is SM smoothed through the grid: it carries SM's error and the FP32
 # shape weights of the two transfers
 SMOOTH_TOL = 1e-4
+
+
+def _tol(table, field):
+    return table.get(field, table.get("*", DEFAULT_TOL))
+
+
 FIELDS = ["PXg", "Mg", "SM", "SD", "Xp", "VXp"]
 
 
@@ -48,8 +66,8 @@ def test_mixed_vs_fp64(built, name):
     b = MpmStep(d, "mixed")
     b.run(steps)
     b.sync()
-    tol = MIXED_TOL.get(name, DEFAULT_TOL)
     for f in FIELDS:
+        tol = _tol(MIXED_TOL.get(name, {}), f)
         err = _rel(a.download(f), b.download(f))
         assert err <= tol, f"{name} {f}: mixed vs FP64 relative error {err:.3g} > {tol}"
     sa, sb = a.scalars(), b.scalars()
@@ -68,7 +86,7 @@ def test_mixed_cook_vs_fp64(built, variant):
     b.run(300)
     for f in FIELDS:
         err = _rel(a.download(f), b.download(f))
-        assert err <= DEFAULT_TOL, f"cook {variant} {f}: {err:.3g}"
+        assert err <= _tol(COOK_TOL, f), f"cook {variant} {f}: {err:.3g}"
 
 
 MIX = ["slope_small_usf_dp_gimp", "beam_musl_neoh_sgmp", "block_usf_john", "dam_small_musl_null_bspline"]

@@ -29,7 +29,7 @@ def test_column_mixed_vs_fp64(column):
     b.run(20)
     for f in ["PXg", "Mg", "SM", "SD", "Xp", "VXp"]:
         err = _rel(a.download(f), b.download(f))
-        assert err <= 1e-4, f"{f}: {err:.3g}"
+        assert err <= 1e-5, f"{f}: {err:.3g}"
 
 
 def test_column_grid_mass_equals_particle_mass(column):
