@@ -373,13 +373,20 @@ def run_ours(args) -> dict:
     # oracle on glibc): the faster of the two plain FP64 forms
     native = None
     if not args.no_fp64:
-        s = m.MpmStep(deck, precision="native", device=local)
-        s.run(args.warmup, graph=True)
-        s.sync()
-        barrier()
-        ms_n = max_over_ranks(s.time_steps(args.steps, graph=True))
-        s.close()
-        native = {"value": aggregate_rate(npart, world, args.steps, ms_n), "ms_per_step": ms_n / args.steps}
+        if args.target_steps <= 0:  # the strict context is not needed again: free its memory first
+            ctxs.pop("fp64").close()
+        try:
+            s = m.MpmStep(deck, precision="native", device=local)
+        except m.MpmError as e:  # (a workload that fits one FP64 context, not two)
+            s = None
+            native = {"skipped": str(e)}
+        if s is not None:
+            s.run(args.warmup, graph=True)
+            s.sync()
+            barrier()
+            ms_n = max_over_ranks(s.time_steps(args.steps, graph=True))
+            s.close()
+            native = {"value": aggregate_rate(npart, world, args.steps, ms_n), "ms_per_step": ms_n / args.steps}
     # error at the workload's own length: both forms advanced from the same
     # deck to the same step, outside the timed regions
     target_c2 = None
@@ -389,8 +396,18 @@ def run_ours(args) -> dict:
         for form in ("fp64", "mixed"):
             run_to(ctxs[form], args.target_steps)
             fin[form] = {f: ctxs[form].download(f) for f in ERR_FIELDS}
+        # the FP64 form's own response to input noise the size of one FP32
+        # rounding: the same deck with every initial coordinate perturbed by
+        # a seeded relative 1e-7, run to the same step
+        pert = m.MpmStep(deck, precision="fp64", device=local)
+        xp = pert.download("Xp")
+        pert.upload("Xp", xp * (1.0 + 1e-7 * np.random.default_rng(7).uniform(-1.0, 1.0, size=xp.shape)))
+        run_to(pert, args.target_steps)
+        fin["perturbed"] = {f: pert.download(f) for f in ERR_FIELDS}
+        pert.close()
         target_c2 = {"steps": args.target_steps,
                      "max_error": form_errors(fin["mixed"], fin["fp64"], x0),
+                     "fp64_perturbed_1e-7": form_errors(fin["perturbed"], fin["fp64"], x0),
                      "wall_s": round(time.perf_counter() - t0, 1)}
     for c in ctxs.values():
         c.close()
@@ -444,7 +461,7 @@ def run_ours(args) -> dict:
                   "parity": "bit-identical to the CPU oracle (tests/test_gpu_parity.py)",
                   "speedup_mixed_over_fp64": value / fp64_value,
                   "native": native,
-                  "speedup_mixed_over_fp64_native": value / native["value"] if native else None}
+                  "speedup_mixed_over_fp64_native": value / native["value"] if native and "value" in native else None}
                  if fp64 else None),
         "error_vs_fp64": err,
         "e2e": {"value": npart * world * args.steps / t_e2e, "unit": "particle-steps/s",
@@ -462,7 +479,7 @@ def run_ours(args) -> dict:
     }
     target = {}
     if target_c2 is not None:
-        fastest = max(fp64_value, native["value"]) if native else fp64_value
+        fastest = max(fp64_value, native["value"]) if native and "value" in native else fp64_value
         target[args.workload] = dict(target_c2, ratio_mixed_over_fp64=value / fastest,
                                     fp64_form_compared="fastest of strict / native",
                                     error_reference="FP64 strict form (bit-identical to the oracle)")

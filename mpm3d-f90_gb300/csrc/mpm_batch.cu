@@ -203,7 +203,6 @@ struct mpm_batch {
   const double* set0_x = nullptr;                   // identifies particle buffer set 0
   int pblock = 256, nblock = 256;
   int scatter_blocks = 9728;  // scatter grid cap (64 blocks per SM; warps stride over the occupied cells)
-  int scatter_wave = 4864;    // scatter warps resident at once (4 blocks per SM)
   int sort_blocks = 152;      // grid of the long-segment sort (one block per SM)
   int sms = 152;              // multiprocessors of the device
   int loop_min_steps = 0;     // steps a device loop takes before it honours an interrupt
@@ -285,8 +284,8 @@ void alloc_particles(Alloc& al, BState& s, long long NP, bool uvfp) {
 
 long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bool uvfp, bool jc) {
   long long per_p = 2 * (16 * 8 + 17 * 4 + (uvfp ? 72 : 0) + 1 + 2 + 2 + 4);  // two particle buffer sets
-  per_p += 4 * 3 + 4 * 9 + 4 * 6 + 4 * 9;                                  // derived + force staging
-  per_p += 4 * 4;                                                         // sort key, permutation, runs, inverse
+  per_p += 4 * 3 + 4 * 9 + 4 * 6 + 4 * 9 + 4 * 4;                          // derived + force staging + FP32 m, v
+  per_p += 4 * 3;                                                         // sort key, permutation, inverse
   if (jc) per_p += 4 * 2 + 8 * 6 + 1;
   long long per_n = 8 * 13 + 4 + 8 * 4;
   long long per_k = 4 * 2;                                                // segment ends, fill counters
@@ -369,7 +368,7 @@ int enqueue_front(mpm_batch* b) {
   // counting sort by key (mpm_sort.cuh): segment ends and the occupied
   // keys, placement, then the stable order inside each segment
   prof_begin(K_SORT, st);
-  scan_tiles_enqueue(SegScan{a.seg, a.runs, a.nruns, a.NK}, reinterpret_cast<long long*>(a.tiles), st);
+  scan_tiles_enqueue(IntScan<ScanSum>{a.seg, a.seg, a.NK}, a.tiles, st);
   BCK(cudaMemsetAsync(a.fill, 0, sizeof(int) * (size_t)a.NK, st));
   BCK(cudaMemsetAsync(a.nbig, 0, sizeof(int), st));
   ks_place<<<gridn(a.NP, 256), 256, 0, st>>>(a.key, a.seg, a.fill, a.perm, a.NP);
@@ -392,24 +391,15 @@ int enqueue_back(mpm_batch* b) {
   // swap the particle buffer sets (node and scene arrays are shared)
   std::swap(b->A, b->B);
   BState& s = b->A;
-  const unsigned sgrid = (unsigned)std::min<long long>(b->scatter_blocks, (s.NK + kCellWarps - 1) / kCellWarps);
   auto pgrid = [&](int warps) {
     return (unsigned)std::max<long long>(1, std::min<long long>(b->scatter_blocks, (b->ntask + warps - 1) / warps));
   };
-  // particle -> grid transfers: particle tasks (linear, GIMP, B-spline) and
-  // the SGMP keys, each launched when the batch holds such scenes
+  // particle -> grid transfers: particle tasks of every scene
   auto scatter = [&](int mode) {
-    if (b->any_nonsgmp) {
-      constexpr int w0 = PartShape<0>::WARPS, w1 = PartShape<1>::WARPS, w2 = PartShape<2>::WARPS;
-      if (mode == 0) kb_part_scatter<0><<<pgrid(w0), 32 * w0, 0, st>>>(s);
-      else if (mode == 1) kb_part_scatter<1><<<pgrid(w1), 32 * w1, 0, st>>>(s);
-      else kb_part_scatter<2><<<pgrid(w2), 32 * w2, 0, st>>>(s);
-    }
-    if (b->any_sgmp) {
-      if (mode == 0) kb_cell_scatter<0><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
-      else if (mode == 1) kb_cell_scatter<1><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
-      else kb_cell_scatter<2><<<sgrid, 32 * kCellWarps, 0, st>>>(s, s.runs, s.nruns, b->scatter_wave);
-    }
+    constexpr int w0 = PartShape<0>::WARPS, w1 = PartShape<1>::WARPS, w2 = PartShape<2>::WARPS;
+    if (mode == 0) kb_part_scatter<0><<<pgrid(w0), 32 * w0, 0, st>>>(s);
+    else if (mode == 1) kb_part_scatter<1><<<pgrid(w1), 32 * w1, 0, st>>>(s);
+    else kb_part_scatter<2><<<pgrid(w2), 32 * w2, 0, st>>>(s);
   };
   if (b->any_sgmp) {
     prof_begin(K_SG_CLEAR, st);
@@ -760,14 +750,14 @@ int commit(mpm_batch* b) {
   shared.xxn = al.get<float>(3 * NP);
   shared.xn = al.get<float>(3 * NP);
   shared.fs = al.get<float>(9 * NP);
+  shared.m32 = al.get<float>(NP);
+  shared.v32 = al.get<float>(3 * NP);
   shared.key = al.get<unsigned>(NP);
   shared.perm = al.get<int>(NP);
   shared.seg = al.get<int>(NK + 1);
-  shared.runs = al.get<unsigned>(NP);
   shared.inv = al.get<int>(NP);
-  shared.nruns = al.get<int>(1);
   shared.fill = al.get<int>(NK);
-  shared.tiles = al.get<int>(2 * (std::max(scan_tiles(NK), scan_tiles(NP)) + 1));  // 64-bit tile totals
+  shared.tiles = al.get<int>(std::max(scan_tiles(NK), scan_tiles(NP)) + 1);
   shared.big = al.get<int>(NP / (kRegSeg + 1) + 1);
   shared.nbig = al.get<int>(1);
   shared.mg = al.get<double>(NN);
@@ -829,8 +819,8 @@ int commit(mpm_batch* b) {
   carve(al);
   auto share = [&](BState& s) {
     s.cell = shared.cell; s.dual = shared.dual; s.inode = shared.inode; s.off = shared.off; s.xxn = shared.xxn;
-    s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key;
-    s.perm = shared.perm; s.seg = shared.seg; s.runs = shared.runs; s.inv = shared.inv; s.nruns = shared.nruns;
+    s.xn = shared.xn; s.fs = shared.fs; s.key = shared.key; s.m32 = shared.m32; s.v32 = shared.v32;
+    s.perm = shared.perm; s.seg = shared.seg; s.inv = shared.inv;
     s.fill = shared.fill; s.tiles = shared.tiles; s.big = shared.big; s.nbig = shared.nbig; s.mg = shared.mg; s.px = shared.px; s.fx = shared.fx;
     s.nvel = shared.nvel; s.nacc = shared.nacc; s.acc = shared.acc; s.fix = shared.fix; s.bd = shared.bd; s.node_scene = shared.node_scene;
     s.cacc = shared.cacc; s.co = shared.co;
@@ -871,12 +861,12 @@ int commit(mpm_batch* b) {
   std::vector<uint8_t> fix((size_t)NN), bd((size_t)NN);
   std::vector<int> target;
   std::vector<SceneState> sst;
-  std::vector<int> task0;  // first particle task of each scene (32 particles; SGMP scenes have none)
+  std::vector<int> task0;  // first particle task of each scene (32 particles)
   long long ntask = 0;
   for (HostScene* h : b->order) {
     const Geometry& g = h->su.g;
     task0.push_back((int)ntask);
-    if (g.shape != 3) ntask += (h->np + 31) / 32;
+    ntask += (h->np + 31) / 32;
     Scene sc;
     memset(&sc, 0, sizeof sc);
     sc.p0 = h->p0; sc.np = h->np; sc.n0 = h->n0; sc.nn = h->nn; sc.k0 = h->k0; sc.nk = scene_keys(g);
@@ -1001,7 +991,6 @@ int mpm_batch_create(int device, mpm_batch** out) {
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) == cudaSuccess && sms > 0)
   {
     b->scatter_blocks = 64 * sms;
-    b->scatter_wave = 4 * sms * kCellWarps;
     b->sort_blocks = sms;
     b->sms = sms;
   }

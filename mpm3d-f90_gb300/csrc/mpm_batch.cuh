@@ -90,11 +90,10 @@ struct BState {
   int *cell, *dual, *inode;
   float *off, *xxn, *xn;
   float* fs;  // force staging [9][NP]: sigma*vol (xx, yy, zz, xy, yz, xz), fext (3)
+  float *m32, *v32;  // FP32 mass and velocity [3][NP] for the momentum transfers (permutation; position update)
   // sort (mpm_sort.cuh)
   unsigned* key;
   int *perm, *seg;
-  unsigned* runs;  // occupied sort keys of the step (in no particular order)
-  int* nruns;
   int *fill, *tiles, *big, *nbig;  // per-key slots taken, scan tile totals, long segments
   LoopCtl* ctl;  // run-loop state (one per batch, outside the layout arena)
   int* task0;  // first particle task (32 sorted particles) of each scene, nscene + 1 entries; SGMP scenes have none

@@ -45,10 +45,6 @@ __device__ __forceinline__ void bsp1(int t, float off, float& w, float& d) {
   }
 }
 
-__device__ __forceinline__ void key_range(const BState& b, long long key, int& i0, int& i1) {
-  i0 = key == 0 ? 0 : b.seg[key - 1];
-  i1 = b.seg[key];
-}
 
 // ------------------------------------------------------------- begin step
 __global__ void kb_begin(BState b, const int* target) {
@@ -334,28 +330,20 @@ __global__ void kb_permute(BState src, BState dst) {
   if (i < src.NP) {
     double m, v[3];
     s = permute_one(src, dst, i, m, v);
+    // FP32 mass and velocity for the first transfer (the conversions run
+    // once per particle here, not in every transfer lane)
+    const float m32 = (float)m, v32[3] = {(float)v[0], (float)v[1], (float)v[2]};
+    dst.m32[i] = m32;
+    for (int a = 0; a < 3; ++a) dst.v32[a * dst.NP + i] = v32[a];
     if (scene_live(dst, s)) {
-      bm = (float)m;
-      bv = bm * fmaxf(fabsf((float)v[0]), fmaxf(fabsf((float)v[1]), fabsf((float)v[2]))) * 1.0001f;
+      bm = m32;
+      bv = bm * fmaxf(fabsf(v32[0]), fmaxf(fabsf(v32[1]), fabsf(v32[2]))) * 1.0001f;
     } else {
       s = -1;
     }
   }
   block_scene_max<2>(dst, s, {Q_MASS, Q_MOM}, {bm, bv});
 }
-
-// SGMP scatter workspace: one warp per sort key (a dual cell); per mode the
-// staged particle quantities and the warp's staging rows.
-// mode 0: mass + momentum (GridMomentumInitial), 1: momentum with the updated
-// velocities (GridMomentumMUSL), 2: force (GridMomentumUpdate).
-constexpr int kCellWarps = 8;  // warps (keys) per block
-
-template <int MODE>
-struct ScatterShape {
-  static constexpr int NQ = MODE == 2 ? 9 : 4;      // per-particle quantities staged
-  static constexpr int SROW = MODE == 2 ? 19 : 13;  // staging row: NQ values, 8 weights, 1 (odd length)
-  static constexpr int WS = (32 * SROW + 3) / 4 * 4;  // floats per warp
-};
 
 // Corner k of the dual cell (dx, dy, dz) as a scene cell (its centre node),
 // with the reference's flat arithmetic (CenterCellNode, Grid.f90:380-418:
@@ -366,86 +354,6 @@ __device__ __forceinline__ long long sg_corner_cell(const Scene& sc, int dx, int
   const long long c1 = ((long long)dz * sc.NCy + dy) * sc.NCx + dx;
   const long long cid = c1 + kCorner[k][0] + (long long)kCorner[k][1] * sc.NCx + (long long)kCorner[k][2] * sc.NCxy;
   return cid < (long long)sc.NCxy * sc.NCz ? cid : -1;
-}
-
-// SGMP form of the scatter: the sort key is a dual cell, whose particles
-// reach the centre nodes of its 8 corners with the SGNShape weights
-// 0.125 (1 +- xi)(1 +- eta)(1 +- zeta). Lane l sums slots l, l + 32, l + 64
-// (slot = corner * channels + channel) over the dual cell's particles in
-// storage order (FP32) and adds each nonzero sum, quantised, to the centre
-// node's fixed-point accumulator (cacc). Channels: mode 0 mass and momentum
-// (CenterNode Mg, PXg), 1 momentum with the updated velocities, 2 external
-// force then internal force (Cfext, Cfint).
-template <int MODE>
-__device__ __forceinline__ void sg_scatter_cell(BState& b, const Scene& sc, int i0, int i1, int dx, int dy, int dz,
-                                                float sA, float sB, float* ws) {
-  constexpr int NQ = ScatterShape<MODE>::NQ;      // staged quantities, then 8 corner weights, then 1
-  constexpr int SROW = ScatterShape<MODE>::SROW;
-  constexpr int NV = MODE == 0 ? 4 : (MODE == 1 ? 3 : 9);  // channels
-  constexpr int NS = 8 * NV, KS = (NS + 31) / 32;           // slots, slots per lane
-  constexpr int CH0 = MODE == 2 ? CQ_FE : (MODE == 1 ? CQ_P : CQ_M);  // first accumulator channel
-  static_assert(NQ + 9 <= SROW, "staging row");
-  const int lane = threadIdx.x & 31;
-  const long long NP = b.NP, NC = b.NC;
-  // per slot: corner weight index, the staged factors (mass / force value,
-  // velocity or the 1 at the end of the row), scale, target cell
-  int wi[KS], f0[KS], f1[KS], ch[KS];
-  long long cell[KS];
-  float scale[KS], acc[KS];
-#pragma unroll
-  for (int k = 0; k < KS; ++k) {
-    const int slot = lane + 32 * k;
-    const int corner = slot / NV;
-    ch[k] = slot - corner * NV;
-    wi[k] = NQ + (corner & 7);
-    cell[k] = slot < NS ? sg_corner_cell(sc, dx, dy, dz, corner) : -1;
-    if (MODE == 2) {
-      f0[k] = ch[k] < 3 ? 6 + ch[k] : ch[k] - 3;  // fs: sigma*vol xx..xz (0..5), external force (6..8)
-      f1[k] = NQ + 8;
-      scale[k] = sA;
-    } else {
-      f0[k] = 0;  // mass
-      f1[k] = MODE == 0 ? (ch[k] == 0 ? NQ + 8 : ch[k]) : ch[k] + 1;
-      scale[k] = MODE == 0 && ch[k] != 0 ? sB : sA;
-    }
-    acc[k] = 0.f;
-  }
-  float* row = ws + lane * SROW;
-  for (int base = i0; base < i1; base += 32) {
-    const int cnt = min(32, i1 - base);
-    if (lane < cnt) {
-      const long long i = base + lane;
-      const float xx[3] = {b.xxn[i], b.xxn[NP + i], b.xxn[2 * NP + i]};
-      if (MODE == 2) {
-        for (int q = 0; q < 9; ++q) row[q] = b.fs[q * NP + i];
-      } else {
-        row[0] = (float)b.mass[i];
-        row[1] = (float)b.v[i];
-        row[2] = (float)b.v[NP + i];
-        row[3] = (float)b.v[2 * NP + i];
-      }
-      for (int k = 0; k < 8; ++k) {
-        float w = 0.125f;
-        for (int a = 0; a < 3; ++a) w *= kCorner[k][a] ? 1.f + xx[a] : 1.f - xx[a];
-        row[NQ + k] = w;
-      }
-      row[NQ + 8] = 1.f;
-    }
-    __syncwarp();
-    for (int p = 0; p < cnt; ++p) {
-      const float* r = ws + p * SROW;
-#pragma unroll
-      for (int k = 0; k < KS; ++k)
-        if (cell[k] >= 0) acc[k] += MODE == 2 ? r[wi[k]] * r[f0[k]] : (r[wi[k]] * r[f0[k]]) * r[f1[k]];
-    }
-    __syncwarp();
-  }
-#pragma unroll
-  for (int k = 0; k < KS; ++k) {
-    if (cell[k] < 0) continue;
-    const long long q = quant(acc[k], scale[k]);
-    if (q) atomicAdd(&b.cacc[(long long)(CH0 + ch[k]) * NC + sc.c0 + cell[k]], (unsigned long long)q);
-  }
 }
 
 // -------------------------------------------- particle-parallel scatter
@@ -551,9 +459,9 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
 #pragma unroll
         for (int q = 0; q < 9; ++q) pv[q] = b.fs[q * NP + i];
       } else {
-        pv[0] = (float)b.mass[i];
+        pv[0] = b.m32[i];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) pv[1 + a] = (float)b.v[a * NP + i];
+        for (int a = 0; a < 3; ++a) pv[1 + a] = b.v32[a * NP + i];
       }
       const float idc = (float)sc.idcell;
 #pragma unroll
@@ -632,6 +540,95 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
   __syncwarp();
 }
 
+// The SGMP form of a particle task: the key is the particle's dual cell,
+// whose 8 corners are centre nodes with the SGNShape weights
+// 0.125 (1 +- xi)(1 +- eta)(1 +- zeta). Phase 1 (lane = particle) writes the
+// 8 corner weights -- times the mass for the momentum transfers -- and the
+// transferred values; phase 2 (lane = corner and channel) walks the task's
+// particles and flushes each segment's sums, quantised, into the centre
+// nodes' 64-bit accumulators. Channels: mode 0 mass and momentum (CenterNode
+// Mg, PXg), 1 momentum with the updated velocities, 2 external then internal
+// force (Cfext, Cfint); a lane takes the corner lane / 4 (mode 0) or lane / 3
+// (modes 1, 2: one channel, or three force channels g, g + 3, g + 6).
+template <int MODE>
+__device__ __forceinline__ void sg_part_task(BState& b, const Scene& sc, long long i0, int cnt, float sA, float sB,
+                                             float* ws) {
+  constexpr int ST = PartShape<MODE>::STRIDE;
+  constexpr int CH0 = MODE == 2 ? CQ_FE : (MODE == 1 ? CQ_P : CQ_M);  // first accumulator channel
+  const int lane = threadIdx.x & 31;
+  const long long NP = b.NP, i = i0 + lane;
+  const int d = lane < cnt ? b.dual[i] : -1;
+  const int knext = __shfl_down_sync(0xffffffffu, d, 1);
+  const unsigned lasts = __ballot_sync(0xffffffffu, d >= 0 && (lane == 31 || knext != d));
+  if (lasts == 0u) return;  // (uniform) nothing of this task on the dual grid
+  const int jend = 32 - __clz(lasts);
+  // phase 1: rows 0..7 the corner weights (times the mass for modes 0, 1),
+  // then the values (velocity, or the 9 force inputs)
+  {
+    float* col = ws + lane;
+    float xx[3] = {0.f, 0.f, 0.f}, m = 0.f;
+    if (d >= 0) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) xx[a] = b.xxn[a * NP + i];
+      if (MODE != 2) m = b.m32[i];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float w = 0.125f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) w *= kCorner[k][a] ? 1.f + xx[a] : 1.f - xx[a];
+      col[k * ST] = d < 0 ? 0.f : (MODE == 2 ? w : w * m);
+    }
+    if (MODE == 2) {
+#pragma unroll
+      for (int c = 0; c < 9; ++c) col[(8 + c) * ST] = d < 0 ? 0.f : b.fs[(c < 3 ? 6 + c : c - 3) * NP + i];
+    } else {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) col[(8 + a) * ST] = d < 0 ? 0.f : b.v32[a * NP + i];
+    }
+  }
+  __syncwarp();
+  // phase 2
+  constexpr int NPER = MODE == 0 ? 4 : 3;  // lanes per corner
+  const int k = lane / NPER, g = lane - k * NPER;
+  const bool active = k < 8;
+  const float* wr = ws + (active ? k : 0) * ST;
+  const float* vr = ws + (8 + (MODE == 0 ? (g > 0 ? g - 1 : 0) : g)) * ST;
+  constexpr int NA = MODE == 2 ? 3 : 1;  // accumulators per lane
+  float acc[NA];
+#pragma unroll
+  for (int a = 0; a < NA; ++a) acc[a] = 0.f;
+  for (int j = 0; j < jend; ++j) {
+    const float w = wr[j];
+    if (MODE == 2) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a] += w * vr[3 * a * ST + j];
+    } else if (MODE == 0) {
+      acc[0] += g == 0 ? w : w * vr[j];
+    } else {
+      acc[0] += w * vr[j];
+    }
+    if ((lasts >> j) & 1u) {  // (uniform) segment end: flush into the centre nodes
+      const int dj = __shfl_sync(0xffffffffu, d, j);
+      if (active) {
+        const int dz = dj / sc.CNCxy, rem = dj - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+        const long long cid = sg_corner_cell(sc, dx, dy, dz, k);
+        if (cid >= 0) {
+#pragma unroll
+          for (int a = 0; a < NA; ++a) {
+            const int ch = MODE == 2 ? g + 3 * a : g;
+            const long long q = quant(acc[a], MODE == 0 && ch != 0 ? sB : sA);
+            if (q) atomicAdd(&b.cacc[(long long)(CH0 + ch) * b.NC + sc.c0 + cid], (unsigned long long)q);
+          }
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < NA; ++a) acc[a] = 0.f;
+    }
+  }
+  __syncwarp();
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(32 * PartShape<MODE>::WARPS, MODE == 2 ? 6 : 4) kb_part_scatter(BState b) {
   using PS = PartShape<MODE>;
@@ -658,72 +655,8 @@ __global__ void __launch_bounds__(32 * PartShape<MODE>::WARPS, MODE == 2 ? 6 : 4
     switch (sc.shape) {
       case 0: part_scatter_task<MODE, 0>(b, sc, sc.p0 + first, cnt, sA, sB, ws); break;
       case 1: part_scatter_task<MODE, 1>(b, sc, sc.p0 + first, cnt, sA, sB, ws); break;
-      default: part_scatter_task<MODE, 2>(b, sc, sc.p0 + first, cnt, sA, sB, ws);
-    }
-  }
-}
-
-// the scatter of one SGMP sort key (a dual cell (x, y, z)) by one warp:
-// particles [i0, i1) of scene s, scales sA, sB as sg_scatter_cell
-template <int MODE>
-__device__ __forceinline__ void scatter_cell(BState& b, int i0, int i1, int s, int x, int y, int z, float sA,
-                                             float sB, float* ws) {
-  sg_scatter_cell<MODE>(b, b.scenes[s], i0, i1, x, y, z, sA, sB, ws);
-}
-
-// SGMP scatter over the occupied sort keys (listed in ascending order by the
-// sort, count on the device): a fixed grid, each warp taking chunks of up to
-// 32 consecutive keys; keys of the other shape families are skipped (their
-// scenes scatter by particle tasks, kb_part_scatter). The lanes first load one key's particle range, scene
-// and cell each -- one round of dependent loads for the whole chunk instead
-// of one per key -- then the warp scatters the keys in turn. The chunk is
-// sized for the warps of one resident wave (wave), so that the chain of
-// metadata loads is paid once per up to 32 keys while every resident warp
-// has work; warps of later blocks past the keys exit at once. Empty cells
-// cost nothing, which matters on sparse grids (a granular column fills a
-// fifth of its grid).
-template <int MODE>
-__global__ void __launch_bounds__(32 * kCellWarps, 4)
-    kb_cell_scatter(BState b, const unsigned* runs, const int* nruns, int wave) {
-  __shared__ float4 wsp[kCellWarps][ScatterShape<MODE>::WS / 4];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long n = *nruns;
-  const long long nw = (long long)gridDim.x * kCellWarps;
-  const int chunk = (int)max(1LL, min(32LL, (n + wave - 1) / wave));
-  for (long long r0 = ((long long)blockIdx.x * kCellWarps + warp) * chunk; r0 < n; r0 += nw * chunk) {
-    // lane j: key r0 + j -- its particles, scene, cell (dual cell for SGMP)
-    // coordinates and quantisation scales (s = -1: nothing to scatter)
-    int i0 = 0, i1 = 0, s = -1, x = 0, y = 0, z = 0;
-    float sA = 0.f, sB = 0.f;
-    if (lane < chunk && r0 + lane < n) {
-      key_range(b, runs[r0 + lane], i0, i1);
-      if (i0 < i1) {
-        s = b.scene[i0];
-        const Scene& sc = b.scenes[s];
-        const int cl = sc.shape == 3 ? b.dual[i0] : -1;  // the key's dual cell
-        if (cl < 0 || !scene_live(b, s) || (MODE == 1 && !sc.musl)) {
-          s = -1;  // another shape family, the off-grid bucket, or no transfer this step
-        } else {
-          const int nx = sc.CNCx, nxy = sc.CNCxy;
-          z = cl / nxy;
-          const int rem = cl - z * nxy;
-          y = rem / nx;
-          x = rem - y * nx;
-          const SceneState& st = b.sst[s];
-          sA = q_scale(q_shift(sc, st.qmax[MODE == 0 ? Q_MASS : (MODE == 1 ? Q_MOM_MUSL : Q_FORCE)]));
-          sB = MODE == 0 ? q_scale(q_shift(sc, st.qmax[Q_MOM])) : sA;
-        }
-      }
-    }
-    const int m = (int)min((long long)chunk, n - r0);
-    for (int j = 0; j < m; ++j) {
-      const int sj = __shfl_sync(0xffffffffu, s, j);
-      if (sj < 0) continue;
-      const int a = __shfl_sync(0xffffffffu, i0, j), e = __shfl_sync(0xffffffffu, i1, j);
-      const int xj = __shfl_sync(0xffffffffu, x, j), yj = __shfl_sync(0xffffffffu, y, j),
-                zj = __shfl_sync(0xffffffffu, z, j);
-      const float aj = __shfl_sync(0xffffffffu, sA, j), bj = __shfl_sync(0xffffffffu, sB, j);
-      scatter_cell<MODE>(b, a, e, sj, xj, yj, zj, aj, bj, reinterpret_cast<float*>(wsp[warp]));
+      case 2: part_scatter_task<MODE, 2>(b, sc, sc.p0 + first, cnt, sA, sB, ws); break;
+      default: sg_part_task<MODE>(b, sc, sc.p0 + first, cnt, sA, sB, ws);
     }
   }
 }
@@ -1469,6 +1402,7 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
     const double vv = b.v[a * NP + i];
     pv[a] = st.istep == 1 ? vv + (double)acc[a] * dt * 0.5 : vv + (double)acc[a] * dt;
     b.v[a * NP + i] = pv[a];
+    b.v32[a * NP + i] = (float)pv[a];  // for GridMomentumMUSL's transfer
     if (sc.usf) b.x[a * NP + i] = xx;
   }
   if (!sc.musl) return -1.f;

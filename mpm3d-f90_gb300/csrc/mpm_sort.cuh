@@ -146,7 +146,8 @@ __global__ void __launch_bounds__(kScanThreads) ks_tile_scan(S src, const typena
 }
 
 // an int array scanned into another (or itself); store(g, v, prev) receives
-// the inclusive prefixes of items g and g - 1
+// the inclusive prefixes of items g and g - 1 (sources that also derive
+// something from each item's own value use prev)
 template <class O>
 struct IntScan {
   using T = int;
@@ -156,30 +157,6 @@ struct IntScan {
   long long n;
   __device__ __forceinline__ int load(long long g) const { return in[g]; }
   __device__ __forceinline__ void store(long long g, int v, int) const { out[g] = v; }
-};
-
-// The per-key particle counts (seg) scanned into segment ends, and the
-// occupied keys listed in ascending order (runs, count in *nruns), in one
-// scan of the pairs (count, count > 0) packed into one 64-bit sum: the low
-// half counts occupied keys (fewer than 2^31), so it never carries into the
-// high half.
-struct SegScan {
-  using T = long long;
-  using Op = ScanSum;
-  int* seg;
-  unsigned* runs;
-  int* nruns;
-  long long n;
-  __device__ __forceinline__ long long load(long long g) const {
-    const int c = seg[g];
-    return ((long long)c << 32) | (long long)(c > 0);
-  }
-  __device__ __forceinline__ void store(long long g, long long v, long long prev) const {
-    const int occ = (int)(v & 0xffffffffLL);
-    seg[g] = (int)(v >> 32);
-    if (occ != (int)(prev & 0xffffffffLL)) runs[occ - 1] = (unsigned)g;  // key g is occupied
-    if (g == n - 1) *nruns = occ;
-  }
 };
 
 // ---------------------------------------------------------- counting sort

@@ -390,3 +390,56 @@ def test_batch_device_loop(built):
         assert not th.is_alive() and 1 <= got["n"] < 1_000_000
         assert bt.scalars(s)["istep"] == got["n"]
         assert bt.run_loop(5) == 5  # the request was consumed
+
+
+def _dense_deck() -> str:
+    """An elastic block of ordinary density (8 particles per cell) beside a
+    cluster of 22^3 = 10648 particles inside one cell: the counting sort's
+    segments then have every length class -- up to 32 particles (one thread),
+    33..8192 (a block in shared memory: the cluster's neighbouring keys) and
+    beyond 8192 (a block in global memory: the cluster's own key)."""
+    from mpm3d_gb300.decks import DeckWriter, _grid_lines, f32s
+    h = 1.0
+    w = DeckWriter("block and a dense cluster")
+    w.kw("nmat 1")
+    w.head += _grid_lines(((-2.0, 10.0), (-2.0, 4.0), (0.0, 6.0)), h)
+    w.kw("dtsc 0.5")
+    w.kw("endt 100.0")
+    w.kw("usf on")
+    w.kw("fixe 0 0 0 0 1 0")
+    w.kw("mate")
+    w.kw("1 elas 1000 1e7 0.3")
+    w.block(1, 1000.0, 0.5, (0.0, 0.0, 1.0), (8, 4, 6))
+    dp = h / 22
+    w.block(1, 1000.0, dp, (6.0 + dp / 2, 1.0 + dp / 2, 2.0 + dp / 2), (22, 22, 22))
+    w.tail += ["velo", "body 1 0 0 %s" % f32s(-1.0), "body 2 %s 0 0" % f32s(0.5), "endv"]
+    return w.text()
+
+
+def test_mixed_sort_long_segments(built):
+    """Segments of every length sort into the same order each run (results
+    bit-identical run to run and alone vs in a batch) and the step stays
+    within the mixed form's bound of FP64."""
+    from mpm3d_gb300 import Batch, Deck, MpmStep
+    d = Deck.parse(_dense_deck())
+    runs = []
+    for _ in range(2):
+        m = MpmStep(d, "mixed")
+        m.run(30)
+        runs.append({f: m.download(f) for f in PFIELDS})
+        m.close()
+    for f in PFIELDS:
+        assert np.array_equal(runs[0][f], runs[1][f]), f
+    with Batch() as bt:
+        bt.add(Deck.parse(CASES["slope_small_usf_dp_gimp"][0]()), steps=30)  # another scene in the batch
+        sid = bt.add(d, steps=30)
+        bt.run(30)
+        bt.sync()
+        for f in ["Xp", "VXp", "SM", "SD"]:
+            assert np.array_equal(bt.download(sid, f), runs[0][f]), f
+    a = MpmStep(d, "fp64")
+    a.run(30)
+    for f in ["PXg", "SM", "SD", "VXp"]:
+        err = _rel(a.download(f), runs[0][f])
+        assert err <= DEFAULT_TOL, f"{f}: {err:.3g}"
+    a.close()
