@@ -28,6 +28,18 @@ __device__ __forceinline__ void lin1(int t, float off, float& w, float& d) {
   d = t ? 1.f : -1.f;
 }
 __device__ __forceinline__ void gimp1(float r, float& w, float& d) { gimp_1d<float>(r, w, d); }
+// the same values as gimp1, every branch evaluated and the result selected:
+// a warp's particles sit in different pieces of the shape, and the branches
+// of gimp1 would run one after another
+__device__ __forceinline__ void gimp1_select(float r, float& w, float& d) {
+  const float a = r < 0.f ? -r : r, sg = copysignf(1.f, r);
+  const float w1 = (7.f - 16.f * a * a) * 0.125f, d1 = -(4.f * r);
+  const float w2 = 1.f - a, d2 = -sg;
+  const float t = (5.f - 4.f * a) * 0.25f;
+  const float w3 = t * t, d3 = 2.f * r - sg * 2.5f;
+  w = a < 0.25f ? w1 : (a < 0.75f ? w2 : (a < 1.25f ? w3 : 0.f));
+  d = a < 0.25f ? d1 : (a < 0.75f ? d2 : (a < 1.25f ? d3 : 0.f));
+}
 __device__ __forceinline__ void bsp1(int t, float off, float& w, float& d) {
   // NShape_Bspline pieces (Grid.f90:927-962) with r = off * 0.2 + 0.4
   float r = off * 0.2f + 0.4f;
@@ -209,17 +221,25 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   for (int a = 0; a < 3; ++a) dst.off[a * NP + i] = off[a];
   dst.cell[i] = in ? (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0] : -1;
   if (sc.shape == 3) {
-    // dual (cell-centre) grid: CenterInWhichCell and the nearest node
+    // dual (cell-centre) grid: CenterInWhichCell (FP64, as the sort keys) and
+    // the nearest node with the particle's coordinates about it. The node is
+    // the cell's upper one from half a cell on, decided on the exact FP64
+    // offset (the node must stay the one above the dual cell: deciding on
+    // the FP32 offset would move particles within 3e-8 of the half onto the
+    // other node); XXN = 2 off - 2 (upper node) or 2 off in FP32 -- no
+    // further FP64 arithmetic (the narrow FP64 pipe bounds this kernel)
     int nd[3];
-    for (int a = 0; a < 3; ++a) nd[a] = (int)((x[a] - sc.span0[a]) * sc.idcell + 0.5);
+    for (int a = 0; a < 3; ++a) {
+      const double u = (x[a] - sc.span0[a]) * sc.idcell;  // (as in cell_of)
+      nd[a] = cc[a] + (u - (double)cc[a] >= 0.5);
+    }
     dst.dual[i] = (int)dual_cell(sc, x);
     bool nin = nd[0] >= 0 && nd[0] < sc.NGx && nd[1] >= 0 && nd[1] < sc.NGy && nd[2] >= 0 && nd[2] < sc.NGz;
     int ln = nin ? (nd[2] * sc.NGy + nd[1]) * sc.NGx + nd[0] : -1;
     dst.inode[i] = ln;
     int bd = ln >= 0 ? src.bd[sc.n0 + ln] : 0;
     for (int a = 0; a < 3; ++a) {
-      double u = (x[a] - sc.span0[a]) * sc.idcell;
-      float xxn = (float)((u - (double)nd[a]) * 2.0);
+      float xxn = off[a] * 2.f - (nd[a] > cc[a] ? 2.f : 0.f);
       if ((bd >> (2 * a)) & 3) xxn = xxn > 0.f ? 1.f : (xxn < 0.f ? -1.f : 0.f);
       dst.xxn[a * NP + i] = xxn;
       dst.xn[a * NP + i] = off[a] * 2.f - 1.f;
@@ -400,7 +420,7 @@ __device__ __forceinline__ void part_tab(float off, float idc, float (&w)[3], fl
     } else if (SH == 2) {
       bsp1(t - 1, off, w[t], d[t]);
     } else {
-      gimp1(off - (float)(t - 1 + (off >= 0.5f)), w[t], d[t]);  // node = nearest - 1 + t
+      gimp1_select(off - (float)(t - 1 + (off >= 0.5f)), w[t], d[t]);  // node = nearest - 1 + t
     }
     d[t] *= idc;
   }
@@ -437,7 +457,6 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
   const int knext = __shfl_down_sync(0xffffffffu, key, 1);
   const unsigned lasts = __ballot_sync(0xffffffffu, key >= 0 && (lane == 31 || knext != key));
   if (lasts == 0u) return;  // (uniform) nothing of this task on the grid
-  const int jend = 32 - __clz(lasts);  // one past the last segment end
   // the segment's first box node (scene-local flat index) and whether the
   // whole box lies inside the grid
   const int nbase = ((c[2] + tlo) * sc.NGy + (c[1] + tlo)) * sc.NGx + (c[0] + tlo);
@@ -504,37 +523,42 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
   const float* xw = ws + (lane < NS ? sx : 0) * ST;
   const float* xd = ws + (lane < NS ? 3 + sx : 0) * ST;
   const float* fr = ws + (NX + yz) * ST;
-  float acc[NV];
+  // segment by segment: the segment ends come from a warp vote, so the walk
+  // and its flushes are the same for every lane
+  unsigned rem = lasts;
+  int j = 0;
+  while (rem) {
+    const int e = __ffs(rem) - 1;  // the segment's last lane
+    rem &= rem - 1;
+    float acc[NV];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) acc[v] = 0.f;
-  for (int j = 0; j < jend; ++j) {
-    const float x = xw[j];
-    if (MODE == 2) {
-      const float dx = xd[j];
+    for (int v = 0; v < NV; ++v) acc[v] = 0.f;
+    for (; j <= e; ++j) {
+      const float x = xw[j];
+      if (MODE == 2) {
+        const float dx = xd[j];
 #pragma unroll
-      for (int v = 0; v < 3; ++v) acc[v] += dx * fr[(2 * v) * 9 * ST + j] + x * fr[(2 * v + 1) * 9 * ST + j];
-    } else {
+        for (int v = 0; v < 3; ++v) acc[v] += dx * fr[(2 * v) * 9 * ST + j] + x * fr[(2 * v + 1) * 9 * ST + j];
+      } else {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) acc[v] += x * fr[v * 9 * ST + j];
+        for (int v = 0; v < NV; ++v) acc[v] += x * fr[v * 9 * ST + j];
+      }
     }
-    if ((lasts >> j) & 1u) {  // (uniform) segment end: flush its sums into the nodes
-      const int nb = __shfl_sync(0xffffffffu, nbase, j);
-      bool ok = lane < NS;
-      if (!__shfl_sync(0xffffffffu, (int)inner, j)) {  // (uniform) a box at the grid's edge
-        const int jx = __shfl_sync(0xffffffffu, c[0], j) + tlo + sx, jy = __shfl_sync(0xffffffffu, c[1], j) + tlo + sy,
-                  jz = __shfl_sync(0xffffffffu, c[2], j) + tlo + sz;
-        ok = ok && jx >= 0 && jx < sc.NGx && jy >= 0 && jy < sc.NGy && jz >= 0 && jz < sc.NGz;
-      }
-      if (ok) {
-        const long long n = sc.n0 + nb + soff;
+    // flush the segment's sums into the nodes
+    const int nb = __shfl_sync(0xffffffffu, nbase, e);
+    bool ok = lane < NS;
+    if (!__shfl_sync(0xffffffffu, (int)inner, e)) {  // (uniform) a box at the grid's edge
+      const int jx = __shfl_sync(0xffffffffu, c[0], e) + tlo + sx, jy = __shfl_sync(0xffffffffu, c[1], e) + tlo + sy,
+                jz = __shfl_sync(0xffffffffu, c[2], e) + tlo + sz;
+      ok = ok && jx >= 0 && jx < sc.NGx && jy >= 0 && jy < sc.NGy && jz >= 0 && jz < sc.NGz;
+    }
+    if (ok) {
+      const long long n = sc.n0 + nb + soff;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const long long q = quant(acc[v], MODE == 0 && v > 0 ? sB : sA);
-          if (q) atomicAdd(&b.acc[v * b.NN + n], (unsigned long long)q);
-        }
+      for (int v = 0; v < NV; ++v) {
+        const long long q = quant(acc[v], MODE == 0 && v > 0 ? sB : sA);
+        if (q) atomicAdd(&b.acc[v * b.NN + n], (unsigned long long)q);
       }
-#pragma unroll
-      for (int v = 0; v < NV; ++v) acc[v] = 0.f;
     }
   }
   __syncwarp();
@@ -561,7 +585,6 @@ __device__ __forceinline__ void sg_part_task(BState& b, const Scene& sc, long lo
   const int knext = __shfl_down_sync(0xffffffffu, d, 1);
   const unsigned lasts = __ballot_sync(0xffffffffu, d >= 0 && (lane == 31 || knext != d));
   if (lasts == 0u) return;  // (uniform) nothing of this task on the dual grid
-  const int jend = 32 - __clz(lasts);
   // phase 1: rows 0..7 the corner weights (times the mass for modes 0, 1),
   // then the values (velocity, or the 9 force inputs)
   {
@@ -595,35 +618,37 @@ __device__ __forceinline__ void sg_part_task(BState& b, const Scene& sc, long lo
   const float* wr = ws + (active ? k : 0) * ST;
   const float* vr = ws + (8 + (MODE == 0 ? (g > 0 ? g - 1 : 0) : g)) * ST;
   constexpr int NA = MODE == 2 ? 3 : 1;  // accumulators per lane
-  float acc[NA];
+  unsigned rem = lasts;
+  int j = 0;
+  while (rem) {  // segment by segment (uniform: the segment ends come from a warp vote)
+    const int e = __ffs(rem) - 1;
+    rem &= rem - 1;
+    float acc[NA];
 #pragma unroll
-  for (int a = 0; a < NA; ++a) acc[a] = 0.f;
-  for (int j = 0; j < jend; ++j) {
-    const float w = wr[j];
-    if (MODE == 2) {
+    for (int a = 0; a < NA; ++a) acc[a] = 0.f;
+    for (; j <= e; ++j) {
+      const float w = wr[j];
+      if (MODE == 2) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) acc[a] += w * vr[3 * a * ST + j];
-    } else if (MODE == 0) {
-      acc[0] += g == 0 ? w : w * vr[j];
-    } else {
-      acc[0] += w * vr[j];
+        for (int a = 0; a < 3; ++a) acc[a] += w * vr[3 * a * ST + j];
+      } else if (MODE == 0) {
+        acc[0] += g == 0 ? w : w * vr[j];
+      } else {
+        acc[0] += w * vr[j];
+      }
     }
-    if ((lasts >> j) & 1u) {  // (uniform) segment end: flush into the centre nodes
-      const int dj = __shfl_sync(0xffffffffu, d, j);
-      if (active) {
-        const int dz = dj / sc.CNCxy, rem = dj - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
-        const long long cid = sg_corner_cell(sc, dx, dy, dz, k);
-        if (cid >= 0) {
+    const int dj = __shfl_sync(0xffffffffu, d, e);  // flush into the centre nodes
+    if (active) {
+      const int dz = dj / sc.CNCxy, rm = dj - dz * sc.CNCxy, dy = rm / sc.CNCx, dx = rm - dy * sc.CNCx;
+      const long long cid = sg_corner_cell(sc, dx, dy, dz, k);
+      if (cid >= 0) {
 #pragma unroll
-          for (int a = 0; a < NA; ++a) {
-            const int ch = MODE == 2 ? g + 3 * a : g;
-            const long long q = quant(acc[a], MODE == 0 && ch != 0 ? sB : sA);
-            if (q) atomicAdd(&b.cacc[(long long)(CH0 + ch) * b.NC + sc.c0 + cid], (unsigned long long)q);
-          }
+        for (int a = 0; a < NA; ++a) {
+          const int ch = MODE == 2 ? g + 3 * a : g;
+          const long long q = quant(acc[a], MODE == 0 && ch != 0 ? sB : sA);
+          if (q) atomicAdd(&b.cacc[(long long)(CH0 + ch) * b.NC + sc.c0 + cid], (unsigned long long)q);
         }
       }
-#pragma unroll
-      for (int a = 0; a < NA; ++a) acc[a] = 0.f;
     }
   }
   __syncwarp();
@@ -1012,8 +1037,10 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   return force_stage(b, sc, st, i, ps.vol, ps.sm - ps.q, ps.sd);
 }
 
+// (Drucker-Prager runs best at three 512-thread blocks per SM -- 42
+// registers, some spilled -- the other specialised models at two)
 template <int MT>
-__global__ void __launch_bounds__(512, MT ? 2 : 1) kb_stress(BState b, int usf_pass, int filter) {
+__global__ void __launch_bounds__(512, MT == 10 ? 3 : (MT ? 2 : 1)) kb_stress(BState b, int usf_pass, int filter) {
   const long long i = btid();
   float bound = -1.f;
   if (i < b.NP) bound = stress_one<MT>(b, i, usf_pass, filter);
