@@ -67,6 +67,7 @@ struct HostScene {
   SceneState st{};
   int drdamp = 0;
   int smooth = 0;  // 'smoo': Spre is computed when read
+  int any_fxp = 1;  // some particle carries an external force (FXP)
   DetoPoints deto{};  // detonation points (lighting time of explosives)
 };
 
@@ -789,6 +790,7 @@ int commit(mpm_batch* b) {
   shared.task0 = al.get<int>((long long)b->order.size() + 1);
   shared.sst = al.get<SceneState>((long long)b->order.size());
   shared.mats = al.get<DevMaterial>(nmat);
+  shared.fmats = al.get<DevMaterialF>(nmat);
   shared.bodies = al.get<DevBody>(nbody);
   d_target = al.get<int>((long long)b->order.size());
   d_map = al.get<int>(NP);
@@ -828,7 +830,7 @@ int commit(mpm_batch* b) {
     s.setter = shared.setter; s.setter_scan = shared.setter_scan; s.dep = shared.dep; s.jc_aux = shared.jc_aux;
     s.deferred = shared.deferred; s.red_part = shared.red_part; s.rscene = shared.rscene; s.scenes = shared.scenes;
     s.task0 = shared.task0;
-    s.sst = shared.sst; s.mats = shared.mats; s.bodies = shared.bodies;
+    s.sst = shared.sst; s.mats = shared.mats; s.fmats = shared.fmats; s.bodies = shared.bodies;
   };
   share(A);
   share(B);
@@ -881,6 +883,14 @@ int commit(mpm_batch* b) {
     for (int k = 0; k < 3; ++k) { sc.span0[k] = g.span0[k]; sc.span1[k] = g.span1[k]; }
     sc.dcell = g.dcell; sc.idcell = g.iDCell; sc.cutoff = g.cutoff; sc.iJacobi = g.iJacobi; sc.iJacobi4 = g.iJacobi4;
     sc.dtscale = g.dtscale; sc.qload_time = g.qload_time; sc.damp_factor = g.damp_factor; sc.bq1 = g.bq1; sc.bq2 = g.bq2;
+    sc.fdcell = (float)g.dcell; sc.fidcell = (float)g.iDCell; sc.fbq1 = (float)g.bq1; sc.fbq2 = (float)g.bq2;
+    sc.fdamp = (float)g.damp_factor; sc.fiJacobi4 = (float)g.iJacobi4; sc.fnp = (float)h->np;
+    sc.has_fxp = h->any_fxp;
+    for (int k = 0; k < 3; ++k) {
+      sc.fspan0[k] = (float)g.span0[k];
+      sc.fspan0_lo[k] = (float)(g.span0[k] - (double)sc.fspan0[k]);
+    }
+    sc.fidcell_lo = (float)(g.iDCell - (double)sc.fidcell);
     scenes.push_back(sc);
     for (auto m : h->su.mats) mats.push_back(m);
     for (auto bo : h->su.bodies) {
@@ -903,6 +913,9 @@ int commit(mpm_batch* b) {
       memset(&s0, 0, sizeof s0);
       s0.dt = set_dt(h->su.mats, g.dcell, g.dtscale);
     }
+    s0.fdt = (float)s0.dt;
+    s0.fdt_lo = (float)(s0.dt - (double)s0.fdt);
+    s0.ftime = (float)s0.time;
     s0.active = h->resident ? 0 : 1;  // the initial energy pass below runs for new scenes only
     sst.push_back(s0);
   }
@@ -911,6 +924,9 @@ int commit(mpm_batch* b) {
   BCK(cudaMemcpyAsync(shared.task0, task0.data(), sizeof(int) * task0.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.scenes, scenes.data(), sizeof(Scene) * scenes.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.mats, mats.data(), sizeof(DevMaterial) * mats.size(), cudaMemcpyHostToDevice, st));
+  std::vector<DevMaterialF> fmats;
+  for (const DevMaterial& m : mats) fmats.push_back(material_f32(m));
+  BCK(cudaMemcpyAsync(shared.fmats, fmats.data(), sizeof(DevMaterialF) * fmats.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.bodies, bodies.data(), sizeof(DevBody) * bodies.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.node_scene, nscene.data(), 2 * NN, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.fix, fix.data(), NN, cudaMemcpyHostToDevice, st));
@@ -1555,6 +1571,8 @@ HostScene* scene_stage(const mpm_deck* d, int steps, std::string& err, int* code
     h->v.assign(d->vxp, d->vxp + 3 * h->np);
     h->fxp.assign(d->fxp, d->fxp + 3 * h->np);
   }
+  h->any_fxp = 0;
+  for (long long k = 0; d->fxp && k < 3 * h->np && !h->any_fxp; ++k) h->any_fxp = d->fxp[k] != 0.0;
   h->body_local.assign((size_t)h->np, 0);
   for (int bo = 0; bo < d->nb_body; ++bo)
     for (long long p = d->bodies[bo].par_begin; p < d->bodies[bo].par_end; ++p) h->body_local[p] = (uint16_t)bo;

@@ -53,6 +53,11 @@ struct Scene {
   int mat0, nmat;
   double span0[3], span1[3], dcell, idcell, cutoff, iJacobi, iJacobi4;
   double dtscale, qload_time, damp_factor, bq1, bq2;
+  // FP32 copies for the mixed-precision kernels (a conversion from FP64 runs
+  // on GB300's narrow FP64 pipe, once per thread that makes it)
+  float fdcell, fidcell, fbq1, fbq2, fdamp, fiJacobi4, fnp, fspan0[3];
+  float fidcell_lo, fspan0_lo[3];  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
+  int has_fxp;  // some particle of the scene carries an external force
 };
 
 struct SceneState {
@@ -62,7 +67,7 @@ struct SceneState {
   unsigned long long active_nodes;
   unsigned status;
   unsigned qmax[4];  // per-step contribution bounds of the P2G scatters (float bits)
-  unsigned pad_;
+  float fdt, fdt_lo, ftime;  // FP32 dt, dt - fdt and time (written with dt and time)
 };
 
 // State of the device-resident run loop (mpm_batch_run_loop).
@@ -117,6 +122,7 @@ struct BState {
   Scene* scenes;
   SceneState* sst;
   DevMaterial* mats;
+  DevMaterialF* fmats;  // FP32 mirror of mats (the stress update's material constants)
   DevBody* bodies;   // gravp; mat = global material index
 };
 

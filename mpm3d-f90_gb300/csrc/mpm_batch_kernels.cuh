@@ -68,9 +68,59 @@ __global__ void kb_begin(BState b, const int* target) {
   t.istep = t.istep + 1;
   if (t.istep == target[s]) atomicAdd(&b.ctl->finished, 1);  // the scene's last step
   t.time = t.time + t.dt;
+  t.ftime = (float)t.time;
   t.ie = 0.0;
   t.active_nodes = 0;
   for (int k = 0; k < 4; ++k) t.qmax[k] = 0u;
+}
+
+// ---------------------------------------------- FP64 <-> FP32 off the FP64 pipe
+// GB300 runs FP64 arithmetic and every conversion to or from a 64-bit type
+// on a narrow pipe (1/64 of the FP32 rate); the mixed-precision kernels
+// convert between FP64 storage and FP32 arithmetic with integer operations.
+// Magnitudes below the FP32 normal range give 0 (sign kept), above it (and
+// NaN) infinity; positions, velocities and masses lie far inside it.
+
+// FP32 value of x truncated toward zero (its leading 24 bits)
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned mag = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : ((unsigned)e << 23) | mant);
+  return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
+// FP32 rounding of x, to nearest even (the value of (float)x)
+__device__ __forceinline__ float f32_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  // round bit: mantissa bit 28 of the low word; sticky: bits 0..27 (ties to
+  // even on the kept last bit); a carry out of the mantissa steps the exponent
+  const unsigned inc = ((lo >> 28) & 1u) & (((lo & 0x0fffffffu) != 0u) | (mant & 1u));
+  unsigned mag = (((unsigned)e << 23) | mant) + inc;
+  mag = e <= 0 ? 0u : (e >= 255 || mag >= 0x7f800000u ? 0x7f800000u : mag);
+  return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
+// exact FP64 value of an FP32 value (normal or zero)
+__device__ __forceinline__ double f64_of(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned hi = (u & 0x80000000u) | (e ? ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3) : 0u);
+  const unsigned lo = e ? u << 29 : 0u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// x as hi + lo: hi its leading 24 bits, lo the remaining 29 rounded to FP32
+// (one 32-bit integer conversion), so hi + lo = x to 2^-47 relative
+__device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
+  hi = f32_trunc(x);
+  const unsigned w = (unsigned)__double2hiint(x), l = (unsigned)__double2loint(x);
+  const int eb = (int)((w >> 20) & 0x7ffu);
+  // lo = (l mod 2^29) * 2^(e - 52), e = eb - 1023: FP32 biased exponent eb - 948
+  const float r = __uint2float_rn(l & 0x1fffffffu) * __uint_as_float(eb > 948 ? (unsigned)(eb - 948) << 23 : 0u);
+  lo = (w & 0x80000000u) ? -r : r;
 }
 
 // cell of a position (InWhichCell, Grid.f90:123-155) and the offset in it, in
@@ -86,6 +136,44 @@ __device__ __forceinline__ bool cell_of(const Scene& sc, const double x[3], int 
     off[a] = (float)(u - (double)cc[a]);
   }
   return in && cc[0] < sc.NCx && cc[1] < sc.NCy && cc[2] < sc.NCz;
+}
+
+// cell_of for the linear, GIMP and B-spline scenes without FP64
+// instructions: x - span0 and its product with 1 / dcell carried as FP32
+// hi + lo pairs (to about 2^-46), so the offset is exact to far below its
+// FP32 rounding. The cell can differ from cell_of's only for a position
+// within about 1e-12 cells of a face (or of the grid's edge), where the
+// shape functions of the two cells agree.
+__device__ __forceinline__ bool cell_of_df(const Scene& sc, const double x[3], int cc[3], float off[3]) {
+  bool in = true;
+  const int nc[3] = {sc.NCx, sc.NCy, sc.NCz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float xh, xl;
+    f32_split(x[a], xh, xl);
+    // d = x - span0: TwoSum of the leading parts, the trailing parts added
+    const float s = xh - sc.fspan0[a];
+    const float bb = s - xh;
+    const float err = (xh - (s - bb)) + (-sc.fspan0[a] - bb);
+    const float t = err + (xl - sc.fspan0_lo[a]);
+    const float dh = s + t, dl = t - (dh - s);
+    // u = d * idcell (the lo * lo term is below the pair's precision)
+    const float uh = dh * sc.fidcell;
+    const float ul = fmaf(dh, sc.fidcell, -uh) + fmaf(dh, sc.fidcell_lo, dl * sc.fidcell);
+    float c = floorf(uh);
+    float f = (uh - c) + ul;  // uh - c is exact
+    if (f < 0.f) {
+      c -= 1.f;
+      f += 1.f;
+    } else if (f >= 1.f) {
+      c += 1.f;
+      f -= 1.f;
+    }
+    in = in && c >= 0.f && c < (float)nc[a];
+    cc[a] = in ? (int)c : 0;
+    off[a] = f;
+  }
+  return in;
 }
 
 // SGMP dual (cell-centre) cell of a position, CenterInWhichCell
@@ -122,8 +210,10 @@ __global__ void kb_keys(BState b) {
     if (sc.shape == 3) {
       c = dual_cell(sc, x);
     } else {
-      // The coordinate in cells is formed in FP64 and rounded to FP32 once;
-      // the rest is FP32 / integer work (GB300's FP64 pipe is narrow). The
+      // The coordinate in cells is formed in FP32 from the positions
+      // truncated to FP32 by integer operations (GB300's FP64 pipe is
+      // narrow), so it can put a particle within a few FP32 roundings of
+      // the coordinate (about 1e-7 of it) on the other side of a face. The
       // sort only groups particles: the transfers take every particle's cell
       // and offsets from the permutation's exact routine (cell_of), so a
       // particle that this rounding puts on the other side of a cell face
@@ -134,7 +224,7 @@ __global__ void kb_keys(BState b) {
       bool in = true;
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        u[a] = (float)((x[a] - sc.span0[a]) * sc.idcell);
+        u[a] = (f32_trunc(x[a]) - sc.fspan0[a]) * sc.fidcell;
         in = in && u[a] >= 0.f;
         cc[a] = (int)u[a];
       }
@@ -217,7 +307,7 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   const Scene& sc = src.scenes[s];
   int cc[3];
   float off[3];
-  const bool in = cell_of(sc, x, cc, off);
+  const bool in = sc.shape == 3 ? cell_of(sc, x, cc, off) : cell_of_df(sc, x, cc, off);
   for (int a = 0; a < 3; ++a) dst.off[a * NP + i] = off[a];
   dst.cell[i] = in ? (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0] : -1;
   if (sc.shape == 3) {
@@ -301,19 +391,38 @@ __device__ __forceinline__ void block_scene_max(BState& b, int s, const int (&sl
 }
 
 // Fixed-point shift sh of a scene's channel: contributions are rounded to
-// integers after scaling by 2^sh, sh = 62 - E with np * bound < 2^E (clamped
-// to the FP32 exponent range; 0 when the bound is 0 and every contribution
-// is 0). Quantisation is one FP32 multiply by 2^sh (exact) and a conversion
-// to int64 -- no FP64 arithmetic on the particle side.
+// integers after scaling by 2^sh, sh = 61 - E with np * bound < 2^E, so no
+// sum of a scene's contributions overflows, and at most 47 - Eb with
+// bound < 2^Eb, so that one flushed sum (at most 32 contributions) stays
+// below 2^53 for quant (this limit binds below 16384 particles only);
+// clamped to the FP32 exponent range, 0 when the bound is 0 and every
+// contribution is 0.
 __device__ __forceinline__ int q_shift(const Scene& sc, unsigned bound_bits) {
   const float bound = __uint_as_float(bound_bits);
   if (!(bound > 0.f)) return 0;
-  int E;
-  frexpf((float)sc.np * bound, &E);  // np < 2^31: the product is exact up to one rounding, covered by E + 1
-  return max(-126, min(127, 61 - E));
+  int E, Eb;
+  frexpf(sc.fnp * bound, &E);  // np < 2^31: the product is exact up to one rounding, covered by E + 1
+  frexpf(bound, &Eb);
+  return max(-126, min(127, min(61 - E, 47 - Eb)));
 }
 __device__ __forceinline__ float q_scale(int sh) { return __int_as_float((sh + 127) << 23); }
-__device__ __forceinline__ long long quant(float c, float scale) { return __float2ll_rn(c * scale); }
+// f = c * 2^sh rounded to the nearest 64-bit integer (ties to even) for
+// |f| <= 2^53, without the FP64 pipe (GB300 converts float to int64 there,
+// at a small fraction of the 32-bit conversion rate). f splits exactly into
+// h * 2^31 + r: the FP32 sum f + 1.5 * 2^54 lies in the binade whose ulp is
+// 2^31, so it is 1.5 * 2^54 + h * 2^31 with h = f / 2^31 rounded to
+// nearest, and h is the difference of the two bit patterns; the remainder
+// r = f - h * 2^31 has |r| <= 2^30 and is exact (a multiple of f's ulp no
+// larger than f), so one 32-bit conversion rounds it. h * 2^31 is an
+// integer, so the result equals __float2ll_rn(f).
+__device__ __forceinline__ long long quant(float c, float scale) {
+  constexpr float M = 0x1.8p54f;
+  const float f = c * scale;
+  const float t = f + M;
+  const int h = __float_as_int(t) - __float_as_int(M);
+  const int r = __float2int_rn(f - (t - M));
+  return (long long)h * 2147483648LL + r;
+}
 __device__ __forceinline__ double q_unit(int sh) { return __longlong_as_double((long long)(1023 - sh) << 52); }  // 2^-sh
 
 // influence nodes of a particle along one direction: node = cell + t0 + k
@@ -352,7 +461,7 @@ __global__ void kb_permute(BState src, BState dst) {
     s = permute_one(src, dst, i, m, v);
     // FP32 mass and velocity for the first transfer (the conversions run
     // once per particle here, not in every transfer lane)
-    const float m32 = (float)m, v32[3] = {(float)v[0], (float)v[1], (float)v[2]};
+    const float m32 = f32_rn(m), v32[3] = {f32_rn(v[0]), f32_rn(v[1]), f32_rn(v[2])};
     dst.m32[i] = m32;
     for (int a = 0; a < 3; ++a) dst.v32[a * dst.NP + i] = v32[a];
     if (scene_live(dst, s)) {
@@ -482,7 +591,7 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
 #pragma unroll
         for (int a = 0; a < 3; ++a) pv[1 + a] = b.v32[a * NP + i];
       }
-      const float idc = (float)sc.idcell;
+      const float idc = sc.fidcell;
 #pragma unroll
       for (int a = 0; a < 3; ++a) part_tab<SH>(off[a], idc, w[a], d[a]);
     }
@@ -860,7 +969,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   if (!scene_live(b, s)) return -1.f;
   const Scene& sc = b.scenes[s];
   if (sc.usf != usf_pass) return -1.f;
-  const DevMaterial& mt = b.mats[b.bodies[b.body[i]].mat];
+  const DevMaterialF& mt = b.fmats[b.bodies[b.body[i]].mat];
   // every particle goes through the instantiation of its own material type
   // (or the general one), whatever else shares the batch: the compiled FP32
   // arithmetic, and so the result, is the same alone or in a batch (filter
@@ -937,7 +1046,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
           L[a][2] += S[a] * fz;
         }
       }
-    const float idc = (float)sc.idcell;
+    const float idc = sc.fidcell;
     for (int a = 0; a < 3; ++a)
       for (int k = 0; k < 3; ++k) deFp[a][k] = L[a][k] * idc;
     de[0] = deFp[0][0];
@@ -951,7 +1060,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
     vort[2] = deFp[1][0] - deFp[0][1];
   }
   const SceneState& st = b.sst[s];
-  const R DT = (R)st.dt;
+  const R DT = st.fdt;
   for (int a = 0; a < 6; ++a) de[a] *= DT;
   for (int a = 0; a < 3; ++a) vort[a] = vort[a] * DT / 2.f;
   for (int a = 0; a < 3; ++a)
@@ -988,7 +1097,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   ps.lt = b.lt[i];
   ps.celsius = b.celsius[i];
   ps.ie = (R)b.ie[i];
-  ps.mass = (R)b.mass[i];
+  ps.mass = b.m32[i];
   ps.dmg = b.dmg[i];
   ps.cp = b.cp[i];
   ps.sm = b.sm[i];
@@ -997,7 +1106,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   ps.failure = b.failure[i] != 0;
   ps.evol = b.evol[i];
   CResult<R> res;
-  constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, (R)sc.dcell, (R)sc.bq1, (R)sc.bq2,
+  constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, sc.fdcell, sc.fbq1, sc.fbq2,
                       res, sc.uvfp ? Fpn_lo : nullptr);
   if (res.negative_volume) atomicOr(&b.sst[s].status, (unsigned)ST_NEGATIVE_VOLUME);
   if (!res.eos_ok) atomicOr(&b.sst[s].status, (unsigned)ST_BAD_EOS);
@@ -1126,14 +1235,18 @@ __device__ __forceinline__ float force_stage(BState& b, const Scene& sc, const S
   // external force in FP32 (the staged force is FP32): load ramp, mass
   // damping, gravity
   float f[3];
-  const float m = (float)b.mass[i];
-  const float ramp = (sc.qload && !(st.time >= sc.qload_time)) ? (float)(st.time / sc.qload_time) : 1.f;
-  for (int a = 0; a < 3; ++a) f[a] = (float)b.fxp[a * NP + i] * ramp;
+  const float m = b.m32[i];
+  if (sc.has_fxp) {
+    const float ramp = (sc.qload && !(st.time >= sc.qload_time)) ? (float)(st.time / sc.qload_time) : 1.f;
+    for (int a = 0; a < 3; ++a) f[a] = (float)b.fxp[a * NP + i] * ramp;
+  } else {
+    f[0] = f[1] = f[2] = 0.f;
+  }
   if (sc.qdamp)
-    for (int a = 0; a < 3; ++a) f[a] = f[a] - (float)sc.damp_factor * m * (float)b.v[a * NP + i];
+    for (int a = 0; a < 3; ++a) f[a] = f[a] - sc.fdamp * m * b.v32[a * NP + i];
   if (sc.gravity) {
     const DevBody& bd = b.bodies[b.body[i]];
-    for (int a = 0; a < 3; ++a) f[a] = f[a] + m * (float)bd.gravp[a];
+    for (int a = 0; a < 3; ++a) f[a] = f[a] + m * bd.fgravp[a];
   }
   float fs[6];
   for (int a = 0; a < 3; ++a) fs[a] = (smq + sd[a]) * vol;
@@ -1143,7 +1256,7 @@ __device__ __forceinline__ float force_stage(BState& b, const Scene& sc, const S
   // bound of one contribution: node force (|grad N| <= 1 / h per component,
   // N <= 1), or for SGMP one centre-node channel (N times a staged value)
   const float sig = fabsf(fs[0]) + fabsf(fs[1]) + fabsf(fs[2]) + 2.f * (fabsf(fs[3]) + fabsf(fs[4]) + fabsf(fs[5]));
-  const float gscale = sc.shape == 3 ? 1.f : (float)sc.idcell;
+  const float gscale = sc.shape == 3 ? 1.f : sc.fidcell;
   return (sig * gscale + fabsf(f[0]) + fabsf(f[1]) + fabsf(f[2])) * 1.0001f;
 }
 
@@ -1259,7 +1372,7 @@ __global__ void kb_sg_centre_gradient(BState b, int usf_pass) {
   q[1] = rem / sc.NCx;
   q[0] = rem - q[1] * sc.NCx;
   float co[6] = {0, 0, 0, 0, 0, 0}, cw[3] = {0, 0, 0}, cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  const float j4 = (float)sc.iJacobi4;
+  const float j4 = sc.fiJacobi4;
   for (int k = 0; k < 8; ++k) {
     long long n = sc.n0 + ((long long)(q[2] + kCorner[k][2]) * sc.NGy + q[1] + kCorner[k][1]) * sc.NGx + q[0] +
                   kCorner[k][0];
@@ -1421,21 +1534,24 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
         }
       }
   }
-  const double dt = st.dt;
-  double pv[3];
+  // the increments v dt and a dt (a dt / 2 on the first step) in FP32 with
+  // dt as the pair fdt + fdt_lo, added to the FP64 position and velocity:
+  // one FP64 add each (the conversions are integer operations)
+  const float dth = st.fdt, dtl = st.fdt_lo, ah = st.istep == 1 ? 0.5f * dth : dth, al = st.istep == 1 ? 0.5f * dtl : dtl;
+  float pv[3];
   for (int a = 0; a < 3; ++a) {
-    const double xx = b.x[a * NP + i] + (double)v[a] * dt;
+    const double xx = b.x[a * NP + i] + f64_of(fmaf(v[a], dtl, v[a] * dth));
     b.xx[a * NP + i] = xx;
-    const double vv = b.v[a * NP + i];
-    pv[a] = st.istep == 1 ? vv + (double)acc[a] * dt * 0.5 : vv + (double)acc[a] * dt;
-    b.v[a * NP + i] = pv[a];
-    b.v32[a * NP + i] = (float)pv[a];  // for GridMomentumMUSL's transfer
+    const double vv = b.v[a * NP + i] + f64_of(fmaf(acc[a], al, acc[a] * ah));
+    b.v[a * NP + i] = vv;
+    pv[a] = f32_rn(vv);
+    b.v32[a * NP + i] = pv[a];  // for GridMomentumMUSL's transfer
     if (sc.usf) b.x[a * NP + i] = xx;
   }
   if (!sc.musl) return -1.f;
   // bound of GridMomentumMUSL's contributions with the updated velocity
-  const float m = (float)b.mass[i];
-  return m * fmaxf(fabsf((float)pv[0]), fmaxf(fabsf((float)pv[1]), fabsf((float)pv[2]))) * 1.0001f;
+  const float m = b.m32[i];
+  return m * fmaxf(fabsf(pv[0]), fmaxf(fabsf(pv[1]), fabsf(pv[2]))) * 1.0001f;
 }
 
 // (capped at 40 registers: six 256-thread blocks per SM hide the node
@@ -1509,22 +1625,25 @@ __global__ void kb_reduce_chunks(BState b) {
   const int s = b.rscene[r];
   const Scene& sc = b.scenes[s];
   const long long NP = b.NP;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  // a thread's particles (kChunk / blockDim.x of them) summed in FP32 from
+  // the FP32 roundings of the FP64 fields (the mixed form's velocities and
+  // internal energies carry FP32 precision), the thread sums in FP64
+  float acc[6] = {0, 0, 0, 0, 0, 0};
   if (scene_live(b, s)) {
     long long p_begin = sc.p0 + (r - sc.r0) * kChunk;
     long long p_end = min(p_begin + kChunk, sc.p0 + sc.np);
     for (long long i = p_begin + threadIdx.x; i < p_end; i += blockDim.x) {
-      double v0 = b.v[i], v1 = b.v[NP + i], v2 = b.v[2 * NP + i], m = b.mass[i];
-      acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5;
-      acc[1] += b.ie[i];
+      const float v0 = f32_rn(b.v[i]), v1 = f32_rn(b.v[NP + i]), v2 = f32_rn(b.v[2 * NP + i]);
+      const float m = f32_rn(b.mass[i]);
+      acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5f;
+      acc[1] += f32_rn(b.ie[i]);
       acc[2] += m * v0;
       acc[3] += m * v1;
       acc[4] += m * v2;
-      double a = fmax(fabs(v0), fmax(fabs(v1), fabs(v2)));
-      acc[5] = fmax(acc[5], a);
+      acc[5] = fmaxf(acc[5], fmaxf(fabsf(v0), fmaxf(fabsf(v1), fabsf(v2))));
     }
   }
-  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = acc[k];
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = f64_of(acc[k]);
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
@@ -1580,6 +1699,8 @@ __global__ void kb_reduce_scenes(BState b, int mode) {
       dt = fmin(dt, sc.dcell / vv);
     }
     st.dt = dt * sc.dtscale;
+    st.fdt = (float)st.dt;
+    st.fdt_lo = (float)(st.dt - (double)st.fdt);
   }
 }
 

@@ -55,10 +55,39 @@ struct DevMaterial {
   double wavespd, q_fai, k_fai, q_psi, ten_f;
 };
 
+// FP32 mirror of DevMaterial for the mixed-precision kernels: the same
+// field names, so the material models (templated on the material struct)
+// read either; every value is the FP32 rounding of its DevMaterial field,
+// which is what each FP32 use of that field converts it to, without a
+// conversion on the FP64 pipe per particle.
+struct DevMaterialF {
+  int mat_type, eos_type;
+  float density, miu, young, poisson, yield0, tangmod, roomt, melt, specheat;
+  float B_jc, n_jc, C_jc, m_jc, epso, epf, D;
+  float cEos[10];
+  float wavespd, q_fai, k_fai, q_psi, ten_f;
+};
+
+inline DevMaterialF material_f32(const DevMaterial& m) {
+  DevMaterialF f;
+  f.mat_type = m.mat_type;
+  f.eos_type = m.eos_type;
+  f.density = (float)m.density; f.miu = (float)m.miu; f.young = (float)m.young; f.poisson = (float)m.poisson;
+  f.yield0 = (float)m.yield0; f.tangmod = (float)m.tangmod; f.roomt = (float)m.roomt; f.melt = (float)m.melt;
+  f.specheat = (float)m.specheat;
+  f.B_jc = (float)m.B_jc; f.n_jc = (float)m.n_jc; f.C_jc = (float)m.C_jc; f.m_jc = (float)m.m_jc;
+  f.epso = (float)m.epso; f.epf = (float)m.epf; f.D = (float)m.D;
+  for (int k = 0; k < 10; ++k) f.cEos[k] = (float)m.cEos[k];
+  f.wavespd = (float)m.wavespd; f.q_fai = (float)m.q_fai; f.k_fai = (float)m.k_fai; f.q_psi = (float)m.q_psi;
+  f.ten_f = (float)m.ten_f;
+  return f;
+}
+
 struct DevBody {
   int mat;   // 0-based material index
   int comp;  // 0-based grid component of the body's particles (comID with contact, else 0)
   double gravp[3];
+  float fgravp[3];  // FP32 copy for the mixed-precision kernels
 };
 
 // Scalars that stay on the device across steps (MPM3D.f90 loop state).

@@ -353,8 +353,8 @@ __global__ void k_apply_bc(St<P> s, Geometry g) {
 // "depeff assigned" flag through m.dep_set; *deferred is set for the
 // Johnson-Cook particles whose tail must wait for the depeff carried from the
 // particle processed before them.
-template <class P>
-__device__ __forceinline__ void jc7_tail(Mm<typename P::R>& m, const DevMaterial& mt, bool& failure,
+template <class P, class Mat>
+__device__ __forceinline__ void jc7_tail(Mm<typename P::R>& m, const Mat& mt, bool& failure,
                                          typename P::R D, typename P::R& vol_out) {
   using R = typename P::R;
   const R epf = (R)mt.epf;
@@ -405,8 +405,8 @@ struct CResult {
 // material constants, the material model of the particle's material and the
 // write-back of Constitution.f90:351-366. MT != 0 compiles the model of
 // material type MT only (the caller guarantees mt.mat_type == MT).
-template <class P, int MT = 0>
-__device__ __forceinline__ void constitution(PState<typename P::R>& ps, const DevMaterial& mt,
+template <class P, int MT = 0, class Mat>
+__device__ __forceinline__ void constitution(PState<typename P::R>& ps, const Mat& mt,
                                              const typename P::R de[6], const typename P::R vort[3],
                                              const typename P::R deFp[3][3], const typename P::R Fpn[3][3],
                                              bool uvfp, typename P::R DT, double time, typename P::R dcell,

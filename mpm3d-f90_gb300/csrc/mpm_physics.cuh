@@ -373,8 +373,8 @@ __device__ __forceinline__ R det3(const R F[3][3]) {
 }
 
 // plastic return shared by M3DM4 / M3DM5 / M3DM8 (Johnson-Cook family)
-template <class P>
-__device__ __forceinline__ void jc_return(Mm<typename P::R>& m, const DevMaterial& mt, typename P::R DT,
+template <class P, class Mat>
+__device__ __forceinline__ void jc_return(Mm<typename P::R>& m, const Mat& mt, typename P::R DT,
                                           int variant, bool* failure) {
   using R = typename P::R;
   const R e4 = f32<R>(0.0001f);
@@ -432,8 +432,8 @@ __device__ __forceinline__ void m3dm7(Mm<R>& m, R DT) {
   m.sd[5] = (R)0.5 * m.miu2 * d[5] / DT;
 }
 
-template <class P>
-__device__ __forceinline__ void m3dm9(Mm<typename P::R>& m, const DevMaterial& mt) {
+template <class P, class Mat>
+__device__ __forceinline__ void m3dm9(Mm<typename P::R>& m, const Mat& mt) {
   using R = typename P::R;
   const R sqrt3f = (R)sqrtf(3.0f);
   const R third_f = (R)(1.0f / 3.0f);
@@ -552,8 +552,8 @@ __device__ __forceinline__ void m3dm10(Mm<typename P::R>& m) {
 
 // seleos + eos1..4 (Constitution.f90:1333-1541). Returns false for a material
 // without an EOS.
-template <class P>
-__device__ __forceinline__ bool seleos(Mm<typename P::R>& m, const DevMaterial& mt, bool failure,
+template <class P, class Mat>
+__device__ __forceinline__ bool seleos(Mm<typename P::R>& m, const Mat& mt, bool failure,
                                        typename P::R DT, typename P::R dcell, typename P::R bq1,
                                        typename P::R bq2) {
   using R = typename P::R;

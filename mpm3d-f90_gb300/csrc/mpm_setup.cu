@@ -60,7 +60,10 @@ int scene_setup(const mpm_deck* d, SceneSetup& out, bool particle_fields) {
     if (d->bodies[b].mat < 1 || d->bodies[b].mat > d->nb_mat)
       return fail(out, MPM_ERR_ARG, "body %d has no material", b + 1);
     out.bodies[b].mat = d->bodies[b].mat - 1;
-    for (int k = 0; k < 3; ++k) out.bodies[b].gravp[k] = d->bodies[b].gravp[k];
+    for (int k = 0; k < 3; ++k) {
+      out.bodies[b].gravp[k] = d->bodies[b].gravp[k];
+      out.bodies[b].fgravp[k] = (float)d->bodies[b].gravp[k];
+    }
   }
   // Initial: per-particle volume, yield stress, internal energy, sound speed,
   // lighting time (sqrt(...)/D is a default-REAL temporary)

@@ -31,7 +31,10 @@ pytestmark = pytest.mark.gpu
 #   gradient that drives J cancels about 500:1, so SM keeps FP32 rounding
 #   times ~500: 1.3e-5 after 300 B-spline steps (other fields <= 6e-7).
 MIXED_TOL = {
-    "taylor_small_usf_jcf_linear": {"SD": 0.1, "*": 1e-4},
+    # the FP32 Johnson-Cook return moves SD by up to 5e-2 and, through it,
+    # VXp by 6e-5 .. 1.4e-4 depending on the order of FP32 roundings (sort
+    # keys, increments, the energy / DT partial sums)
+    "taylor_small_usf_jcf_linear": {"SD": 0.1, "VXp": 2e-4, "*": 1e-4},
     "block_musl_sjc_gruneisen": {"*": 2e-2},
     "block_usf_sjcf_gruneisen": {"*": 5e-2},
 }
