@@ -197,6 +197,7 @@ struct mpm_batch {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int any_sgmp = 0, any_nonsgmp = 0, any_usf = 0, any_later = 0, any_musl = 0, any_jc = 0, any_dr = 0, any_uvfp = 0;
+  int any_nonuvfp = 0;
   int any_prep = 0;  // scenes whose force input is not staged by their stress kernel (USL / MUSL, Johnson-Cook)
   unsigned stress_types = 0;  // stress instantiations to launch: bit MT per specialised type, bit 0 for the rest
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // one step, per buffer parity and
@@ -296,6 +297,7 @@ long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bo
 
 void layout_flags(mpm_batch* b) {
   b->any_sgmp = b->any_nonsgmp = b->any_usf = b->any_later = b->any_musl = b->any_jc = b->any_dr = b->any_uvfp = 0;
+  b->any_nonuvfp = 0;
   b->any_prep = 0;
   for (HostScene* h : b->order) {
     const Geometry& g = h->su.g;
@@ -305,6 +307,7 @@ void layout_flags(mpm_batch* b) {
     if (g.has_jc) b->any_jc = 1;
     if (!g.usf || g.has_jc) b->any_prep = 1;
     if (g.uvfp) b->any_uvfp = 1;
+    else b->any_nonuvfp = 1;
     if (h->drdamp) b->any_dr = 1;
   }
   b->stress_types = 0;
@@ -422,13 +425,24 @@ int enqueue_back(mpm_batch* b) {
     prof_begin(K_STRESS, st);
     // one launch per material instantiation present (each takes its own
     // particles); usually a single one
+    // (and per volume update: by Fp or not)
     const unsigned ty = b->stress_types;
-    const int f = __builtin_popcount(ty) > 1;
-    if (ty & (1u << 1)) kb_stress<1><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
-    if (ty & (1u << 9)) kb_stress<9><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
-    if (ty & (1u << 10)) kb_stress<10><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
-    if (ty & (1u << 11)) kb_stress<11><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
-    if (ty & 1u) kb_stress<0><<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f);
+    const int f = __builtin_popcount(ty) > 1, uvf = b->any_uvfp && b->any_nonuvfp;
+    auto launch = [&](auto kern) { kern<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f, uvf); };
+    if (b->any_nonuvfp) {
+      if (ty & (1u << 1)) launch(kb_stress<1, 0>);
+      if (ty & (1u << 9)) launch(kb_stress<9, 0>);
+      if (ty & (1u << 10)) launch(kb_stress<10, 0>);
+      if (ty & (1u << 11)) launch(kb_stress<11, 0>);
+      if (ty & 1u) launch(kb_stress<0, 0>);
+    }
+    if (b->any_uvfp) {
+      if (ty & (1u << 1)) launch(kb_stress<1, 1>);
+      if (ty & (1u << 9)) launch(kb_stress<9, 1>);
+      if (ty & (1u << 10)) launch(kb_stress<10, 1>);
+      if (ty & (1u << 11)) launch(kb_stress<11, 1>);
+      if (ty & 1u) launch(kb_stress<0, 1>);
+    }
     prof_end(K_STRESS, st);
     if (b->any_jc) {
       prof_begin(K_DEPEFF, st);

@@ -259,11 +259,15 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   // one memory round trip per field
   const long long NP = src.NP;
   const long long j = src.perm[i];
-  double x[3], v[3], f[3];
+  const int s = src.scene[j];
+  const Scene& sc = src.scenes[s];
+  // (the external forces move only in scenes that have some: elsewhere
+  // they are zero and nothing reads them)
+  double x[3], v[3], f[3] = {0.0, 0.0, 0.0};
   for (int a = 0; a < 3; ++a) {
     x[a] = src.x[a * NP + j];
     v[a] = src.v[a * NP + j];
-    f[a] = src.fxp[a * NP + j];
+    if (sc.has_fxp) f[a] = src.fxp[a * NP + j];
   }
   const double mass = src.mass[j], ie = src.ie[j];
   const float vol = src.vol[j], evol = src.evol[j], sig_y = src.sig_y[j], sm = src.sm[j], seqv = src.seqv[j];
@@ -273,7 +277,6 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
               q = src.q[j];
   const uint8_t failure = src.failure[j];
   const uint16_t body = src.body[j];
-  const int s = src.scene[j];
   const int orig = src.orig[j];
   if (src.any_uvfp) {
     float fp[18];
@@ -283,7 +286,7 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   for (int a = 0; a < 3; ++a) {
     dst.x[a * NP + i] = x[a];
     dst.v[a * NP + i] = v[a];
-    dst.fxp[a * NP + i] = f[a];
+    if (sc.has_fxp) dst.fxp[a * NP + i] = f[a];
   }
   dst.mass[i] = mass;
   dst.ie[i] = ie;
@@ -304,7 +307,6 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   dst.scene[i] = (uint16_t)s;
   dst.orig[i] = orig;
   // derived
-  const Scene& sc = src.scenes[s];
   int cc[3];
   float off[3];
   const bool in = sc.shape == 3 ? cell_of(sc, x, cc, off) : cell_of_df(sc, x, cc, off);
@@ -642,6 +644,7 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
     float acc[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) acc[v] = 0.f;
+#pragma unroll 4
     for (; j <= e; ++j) {
       const float x = xw[j];
       if (MODE == 2) {
@@ -735,6 +738,7 @@ __device__ __forceinline__ void sg_part_task(BState& b, const Scene& sc, long lo
     float acc[NA];
 #pragma unroll
     for (int a = 0; a < NA; ++a) acc[a] = 0.f;
+#pragma unroll 4
     for (; j <= e; ++j) {
       const float w = wr[j];
       if (MODE == 2) {
@@ -960,15 +964,17 @@ __device__ __forceinline__ float force_stage(BState& b, const Scene& sc, const S
 
 // stages the particle's force input when its scene's USF pass has its final
 // stress here (no Johnson-Cook tail after this kernel) and returns that
-// contribution's bound; -1 otherwise
-template <int MT>
-__device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass, int filter) {
+// contribution's bound; -1 otherwise. UV: the instantiation for scenes that
+// update volumes by Fp (1) or not (0) -- without the Fp state's registers
+// when not; uvf: the batch holds both kinds, so each launch takes its own.
+template <int MT, int UV>
+__device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass, int filter, int uvf) {
   using P = PMixed;
   using R = float;
   const int s = b.scene[i];
   if (!scene_live(b, s)) return -1.f;
   const Scene& sc = b.scenes[s];
-  if (sc.usf != usf_pass) return -1.f;
+  if (sc.usf != usf_pass || (uvf && sc.uvfp != UV)) return -1.f;
   const DevMaterialF& mt = b.fmats[b.bodies[b.body[i]].mat];
   // every particle goes through the instantiation of its own material type
   // (or the general one), whatever else shares the batch: the compiled FP32
@@ -1066,7 +1072,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   for (int a = 0; a < 3; ++a)
     for (int k = 0; k < 3; ++k) deFp[a][k] *= DT;
   R Fpn[3][3], Fpn_lo[3][3];
-  if (sc.uvfp) {
+  if (UV) {
     // Fp(n+1) = (I + dF) Fp(n), i.e. H += dF + dF H for H = Fp - I, with H
     // carried as a pair hi + lo of FP32 values: the increment in FP32 from
     // the rounded H, added to the pair without rounding error (TwoSum), so
@@ -1106,8 +1112,8 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   ps.failure = b.failure[i] != 0;
   ps.evol = b.evol[i];
   CResult<R> res;
-  constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, sc.uvfp != 0, DT, st.time, sc.fdcell, sc.fbq1, sc.fbq2,
-                      res, sc.uvfp ? Fpn_lo : nullptr);
+  constitution<P, MT>(ps, mt, de, vort, deFp, Fpn, UV != 0, DT, st.time, sc.fdcell, sc.fbq1, sc.fbq2, res,
+                      UV ? Fpn_lo : nullptr);
   if (res.negative_volume) atomicOr(&b.sst[s].status, (unsigned)ST_NEGATIVE_VOLUME);
   if (!res.eos_ok) atomicOr(&b.sst[s].status, (unsigned)ST_BAD_EOS);
   if (sc.has_jc) {
@@ -1148,11 +1154,12 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
 
 // (Drucker-Prager runs best at three 512-thread blocks per SM -- 42
 // registers, some spilled -- the other specialised models at two)
-template <int MT>
-__global__ void __launch_bounds__(512, MT == 10 ? 3 : (MT ? 2 : 1)) kb_stress(BState b, int usf_pass, int filter) {
+template <int MT, int UV>
+__global__ void __launch_bounds__(512, MT == 10 ? 3 : (MT ? 2 : 1))
+    kb_stress(BState b, int usf_pass, int filter, int uvf) {
   const long long i = btid();
   float bound = -1.f;
-  if (i < b.NP) bound = stress_one<MT>(b, i, usf_pass, filter);
+  if (i < b.NP) bound = stress_one<MT, UV>(b, i, usf_pass, filter, uvf);
   if (usf_pass) block_scene_max<1>(b, bound >= 0.f ? (int)b.scene[i] : -1, {Q_FORCE}, {fmaxf(bound, 0.f)});
 }
 
@@ -1740,7 +1747,7 @@ __device__ __forceinline__ double field_value(const BState& b, int field, long l
     case MPM_P_XP: v = b.x[c * NP + i]; break;
     case MPM_P_XX: v = b.x[c * NP + i]; break;  // XX equals Xp between steps
     case MPM_P_VXP: v = b.v[c * NP + i]; break;
-    case MPM_P_FXP: v = b.fxp[c * NP + i]; break;
+    case MPM_P_FXP: v = b.scenes[b.scene[i]].has_fxp ? b.fxp[c * NP + i] : 0.0; break;
     case MPM_P_VOL: v = b.vol[i]; break;
     case MPM_P_SIG_Y: v = b.sig_y[i]; break;
     case MPM_P_SM: v = b.sm[i]; break;
