@@ -428,7 +428,7 @@ int enqueue_back(mpm_batch* b) {
     // (and per volume update: by Fp or not)
     const unsigned ty = b->stress_types;
     const int f = __builtin_popcount(ty) > 1, uvf = b->any_uvfp && b->any_nonuvfp;
-    auto launch = [&](auto kern) { kern<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f, uvf); };
+    auto launch = [&](auto kern) { kern<<<gridn(s.NP, kStressThreads), kStressThreads, 0, st>>>(s, usf_pass, f, uvf); };
     if (b->any_nonuvfp) {
       if (ty & (1u << 1)) launch(kb_stress<1, 0>);
       if (ty & (1u << 9)) launch(kb_stress<9, 0>);
@@ -472,7 +472,7 @@ int enqueue_back(mpm_batch* b) {
     prof_end(K_SG_VELOCITY, st);
   }
   prof_begin(K_POSITION, st);
-  kb_position<<<gridn(s.NP, pb), pb, 0, st>>>(s);
+  kb_position<<<gridn(s.NP, kPosThreads), kPosThreads, 0, st>>>(s);
   prof_end(K_POSITION, st);
   if (b->any_musl) {
     prof_begin(K_SCATTER_MOM, st);
@@ -775,9 +775,9 @@ int commit(mpm_batch* b) {
   shared.tiles = al.get<int>(std::max(scan_tiles(NK), scan_tiles(NP)) + 1);
   shared.big = al.get<int>(NP / (kRegSeg + 1) + 1);
   shared.nbig = al.get<int>(1);
-  shared.mg = al.get<double>(NN);
-  shared.px = al.get<double>(3 * NN);
-  shared.fx = al.get<double>(3 * NN);
+  shared.mg = al.get<float>(NN);
+  shared.px = al.get<float>(3 * NN);
+  shared.fx = al.get<float>(3 * NN);
   shared.nvel = al.get<float4>(NN);
   shared.nacc = al.get<float4>(NN);
   shared.acc = al.get<unsigned long long>(4 * NN);
@@ -905,6 +905,7 @@ int commit(mpm_batch* b) {
       sc.fspan0_lo[k] = (float)(g.span0[k] - (double)sc.fspan0[k]);
     }
     sc.fidcell_lo = (float)(g.iDCell - (double)sc.fidcell);
+    sc.fcutoff = (float)g.cutoff;
     scenes.push_back(sc);
     for (auto m : h->su.mats) mats.push_back(m);
     for (auto bo : h->su.bodies) {
@@ -949,9 +950,9 @@ int commit(mpm_batch* b) {
   BCK(cudaMemcpyAsync(shared.rscene, rscene.data(), 2 * NR, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(d_target, target.data(), sizeof(int) * target.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.sst, sst.data(), sizeof(SceneState) * sst.size(), cudaMemcpyHostToDevice, st));
-  BCK(cudaMemsetAsync(shared.mg, 0, sizeof(double) * NN, st));
-  BCK(cudaMemsetAsync(shared.px, 0, sizeof(double) * 3 * NN, st));
-  BCK(cudaMemsetAsync(shared.fx, 0, sizeof(double) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.mg, 0, sizeof(float) * NN, st));
+  BCK(cudaMemsetAsync(shared.px, 0, sizeof(float) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.fx, 0, sizeof(float) * 3 * NN, st));
   BCK(cudaMemsetAsync(shared.nvel, 0, sizeof(float4) * NN, st));
   BCK(cudaMemsetAsync(shared.nacc, 0, sizeof(float4) * NN, st));
   BCK(cudaMemsetAsync(shared.acc, 0, sizeof(unsigned long long) * 4 * NN, st));
@@ -1294,9 +1295,12 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
   const long long NP = s.NP, np = h->np, p0 = h->p0;
   const int nc = mpm_field_components(field);
   if (field == MPM_G_MG || field == MPM_G_PX || field == MPM_G_FX) {
-    const double* src = field == MPM_G_MG ? s.mg : (field == MPM_G_PX ? s.px : s.fx);
-    for (int a = 0; a < nc; ++a)
-      BCK(cudaMemcpy(out + a * h->nn, src + a * s.NN + h->n0, sizeof(double) * h->nn, cudaMemcpyDeviceToHost));
+    const float* src = field == MPM_G_MG ? s.mg : (field == MPM_G_PX ? s.px : s.fx);
+    std::vector<float> tmp((size_t)h->nn);
+    for (int a = 0; a < nc; ++a) {
+      BCK(cudaMemcpy(tmp.data(), src + a * s.NN + h->n0, sizeof(float) * h->nn, cudaMemcpyDeviceToHost));
+      for (long long k = 0; k < h->nn; ++k) out[a * h->nn + k] = (double)tmp[k];
+    }
     if (field == MPM_G_MG)  // -0 marks a massless node with a force or momentum (the idle test)
       for (long long k = 0; k < h->nn; ++k) out[k] = out[k] + 0.0;
     return MPM_OK;

@@ -56,7 +56,7 @@ struct Scene {
   // FP32 copies for the mixed-precision kernels (a conversion from FP64 runs
   // on GB300's narrow FP64 pipe, once per thread that makes it)
   float fdcell, fidcell, fbq1, fbq2, fdamp, fiJacobi4, fnp, fspan0[3];
-  float fidcell_lo, fspan0_lo[3];  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
+  float fidcell_lo, fspan0_lo[3], fcutoff;  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
   int has_fxp;  // some particle of the scene carries an external force
 };
 
@@ -103,7 +103,7 @@ struct BState {
   LoopCtl* ctl;  // run-loop state (one per batch, outside the layout arena)
   int* task0;  // first particle task (32 sorted particles) of each scene, nscene + 1 entries; SGMP scenes have none
   // grid
-  double *mg, *px, *fx;
+  float *mg, *px, *fx;  // FP32 node state: mass, momentum, force (from the exact fixed-point sums)
   float4 *nvel, *nacc;             // FP32 px / mg and fx / mg for the gathers (zero at or below the cut-off)
   unsigned long long* acc;         // [4][NN] fixed-point P2G sums, zero between transfers
   uint8_t *fix, *bd;
