@@ -350,8 +350,12 @@ void scan_tiles_enqueue(const S& src, typename S::T* tiles, cudaStream_t st) {
   const long long nt = scan_tiles(src.n);
   if (nt <= 0) return;
   ks_tile_total<S><<<(unsigned)nt, kScanThreads, 0, st>>>(src, tiles);
-  ks_tile_prefix<typename S::T, typename S::Op><<<1, kScanThreads, 0, st>>>(tiles, nt);
-  ks_tile_scan<S><<<(unsigned)nt, kScanThreads, 0, st>>>(src, tiles);
+  if (nt <= kFusedTiles) {
+    ks_tile_scan<S, true><<<(unsigned)nt, kScanThreads, 0, st>>>(src, tiles);
+  } else {
+    ks_tile_prefix<typename S::T, typename S::Op><<<1, kScanThreads, 0, st>>>(tiles, nt);
+    ks_tile_scan<S, false><<<(unsigned)nt, kScanThreads, 0, st>>>(src, tiles);
+  }
 }
 
 // one step of every live scene (MPM3D.f90:69-118 for each scene)
@@ -492,8 +496,7 @@ int enqueue_reduce(mpm_batch* b, cudaStream_t st) {
   BState& s = b->A;
   const int pb = b->pblock;
   prof_begin(K_REDUCE, st);
-  kb_reduce_chunks<<<(unsigned)s.NR, 256, 0, st>>>(s);
-  kb_reduce_scenes<<<(unsigned)s.nscene, 256, 0, st>>>(s, 3);
+  kb_reduce_chunks<1><<<(unsigned)s.NR, 256, 0, st>>>(s, 3);
   prof_end(K_REDUCE, st);
   if (b->any_dr) {
     prof_begin(K_DR, st);
@@ -973,8 +976,7 @@ int commit(mpm_batch* b) {
   kb_inverse<<<gridn(NP, 256), 256, 0, st>>>(A);
   b->inv_stale = false;
   // calcEnergy of the new scenes (MPM3D.f90:42)
-  kb_reduce_chunks<<<(unsigned)NR, 256, 0, st>>>(A);
-  kb_reduce_scenes<<<(unsigned)A.nscene, 256, 0, st>>>(A, 1);
+  kb_reduce_chunks<0><<<(unsigned)NR, 256, 0, st>>>(A, 1);
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(st));
   // swap in the new layout: its arena becomes current, the old one spare

@@ -68,6 +68,7 @@ struct SceneState {
   unsigned status;
   unsigned qmax[4];  // per-step contribution bounds of the P2G scatters (float bits)
   float fdt, fdt_lo, ftime;  // FP32 dt, dt - fdt and time (written with dt and time)
+  unsigned red_done;          // chunks of the energy reduction done this step (reset by the last)
 };
 
 // State of the device-resident run loop (mpm_batch_run_loop).

@@ -1634,52 +1634,16 @@ __global__ void kb_p2g_momentum(BState b) {
 // one scene (chunks are fixed relative to the scene start, so the sums of a
 // scene do not depend on the other scenes of the batch), then a block per
 // scene combining its chunks in order.
-__global__ void kb_reduce_chunks(BState b) {
-  __shared__ double sh[6][256];
-  const long long r = blockIdx.x;
-  const int s = b.rscene[r];
+// the scene totals from its chunks' partial sums (FP64; fixed tree order)
+// and, with mode & 2, UpdateDT; every thread of the block calls it
+__device__ __forceinline__ void reduce_scene_finish(BState& b, int s, int mode, double (*sh)[256]) {
   const Scene& sc = b.scenes[s];
-  const long long NP = b.NP;
-  // a thread's particles (kChunk / blockDim.x of them) summed in FP32 from
-  // the FP32 roundings of the FP64 fields (the mixed form's velocities and
-  // internal energies carry FP32 precision), the thread sums in FP64
-  float acc[6] = {0, 0, 0, 0, 0, 0};
-  if (scene_live(b, s)) {
-    long long p_begin = sc.p0 + (r - sc.r0) * kChunk;
-    long long p_end = min(p_begin + kChunk, sc.p0 + sc.np);
-    for (long long i = p_begin + threadIdx.x; i < p_end; i += blockDim.x) {
-      const float v0 = f32_rn(b.v[i]), v1 = f32_rn(b.v[NP + i]), v2 = f32_rn(b.v[2 * NP + i]);
-      const float m = f32_rn(b.mass[i]);
-      acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5f;
-      acc[1] += f32_rn(b.ie[i]);
-      acc[2] += m * v0;
-      acc[3] += m * v1;
-      acc[4] += m * v2;
-      acc[5] = fmaxf(acc[5], fmaxf(fabsf(v0), fmaxf(fabsf(v1), fabsf(v2))));
-    }
-  }
-  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = f64_of(acc[k]);
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      for (int k = 0; k < 5; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
-      sh[5][threadIdx.x] = fmax(sh[5][threadIdx.x], sh[5][threadIdx.x + w]);
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 6; ++k) b.red_part[k * b.NR + r] = sh[k][0];
-}
-
-__global__ void kb_reduce_scenes(BState b, int mode) {
-  __shared__ double sh[6][256];
-  const int s = blockIdx.x;
-  const Scene& sc = b.scenes[s];
-  if (!scene_live(b, s)) return;
   double acc[6] = {0, 0, 0, 0, 0, 0};
   for (long long r = sc.r0 + threadIdx.x; r < sc.r0 + sc.nr; r += blockDim.x) {
-    for (int k = 0; k < 5; ++k) acc[k] += b.red_part[k * b.NR + r];
-    acc[5] = fmax(acc[5], b.red_part[5 * b.NR + r]);
+    // (L2 loads: another SM wrote the partials, and this SM's L1 may hold
+    // the last step's)
+    for (int k = 0; k < 5; ++k) acc[k] += __ldcg(&b.red_part[k * b.NR + r]);
+    acc[5] = fmax(acc[5], __ldcg(&b.red_part[5 * b.NR + r]));
   }
   for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = acc[k];
   __syncthreads();
@@ -1717,6 +1681,65 @@ __global__ void kb_reduce_scenes(BState b, int mode) {
     st.fdt = (float)st.dt;
     st.fdt_lo = (float)(st.dt - (double)st.fdt);
   }
+}
+
+// calcEnergy / UpdateDT: one block per chunk of kChunk particles of a live
+// scene writes the chunk's partial sums; the scene's last chunk block to
+// finish (a per-scene counter, reset by that block) forms the scene totals.
+// SRC 1: the FP32 velocity and mass copies the step wrote (the mixed form's
+// velocities carry FP32 precision); SRC 0: the FP64 fields rounded to FP32
+// (a new scene's first energies, before any step). A thread's particles
+// (kChunk / blockDim.x of them) are summed in FP32, the thread sums in FP64.
+template <int SRC>
+__global__ void __launch_bounds__(256) kb_reduce_chunks(BState b, int mode) {
+  __shared__ double sh[6][256];
+  __shared__ int last;
+  const long long r = blockIdx.x;
+  const int s = b.rscene[r];
+  if (!scene_live(b, s)) return;  // (uniform: every block of the scene returns)
+  const Scene& sc = b.scenes[s];
+  const long long NP = b.NP;
+  float acc[6] = {0, 0, 0, 0, 0, 0};
+  const long long p_begin = sc.p0 + (r - sc.r0) * kChunk;
+  const long long p_end = min(p_begin + kChunk, sc.p0 + sc.np);
+  for (long long i = p_begin + threadIdx.x; i < p_end; i += blockDim.x) {
+    float v0, v1, v2, m;
+    if (SRC) {
+      v0 = b.v32[i];
+      v1 = b.v32[NP + i];
+      v2 = b.v32[2 * NP + i];
+      m = b.m32[i];
+    } else {
+      v0 = f32_rn(b.v[i]);
+      v1 = f32_rn(b.v[NP + i]);
+      v2 = f32_rn(b.v[2 * NP + i]);
+      m = f32_rn(b.mass[i]);
+    }
+    acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5f;
+    acc[1] += f32_rn(b.ie[i]);
+    acc[2] += m * v0;
+    acc[3] += m * v1;
+    acc[4] += m * v2;
+    acc[5] = fmaxf(acc[5], fmaxf(fabsf(v0), fmaxf(fabsf(v1), fabsf(v2))));
+  }
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = f64_of(acc[k]);
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      for (int k = 0; k < 5; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+      sh[5][threadIdx.x] = fmax(sh[5][threadIdx.x], sh[5][threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) b.red_part[k * b.NR + r] = sh[k][0];
+    __threadfence();
+    last = atomicAdd(&b.sst[s].red_done, 1u) == (unsigned)(sc.nr - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  if (threadIdx.x == 0) b.sst[s].red_done = 0u;
+  reduce_scene_finish(b, s, mode, sh);
 }
 
 __global__ void kb_dr_damping(BState b) {

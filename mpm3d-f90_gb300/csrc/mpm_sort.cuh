@@ -119,12 +119,25 @@ __global__ void __launch_bounds__(kScanThreads) ks_tile_prefix(T* tiles, long lo
   }
 }
 
-template <class S>
+// FUSED: tiles hold the tile totals themselves (no ks_tile_prefix launch):
+// every block reduces the totals of the tiles before it (for up to
+// kFusedTiles tiles, a few loads per thread)
+constexpr long long kFusedTiles = 4096;
+template <class S, bool FUSED>
 __global__ void __launch_bounds__(kScanThreads) ks_tile_scan(S src, const typename S::T* tiles) {
   using T = typename S::T;
   using Op = typename S::Op;
   __shared__ T tile[kScanTile];
   __shared__ T thr[kScanThreads], wsum[32];
+  T carry;
+  if (FUSED) {
+    T v = Op::template id<T>();
+    for (long long t = threadIdx.x; t < blockIdx.x; t += blockDim.x) v = Op::op(v, tiles[t]);
+    block_scan<T, Op>(v, thr, wsum);
+    carry = thr[kScanThreads - 1];  // (thr is rewritten only after the next scan's first barrier)
+  } else {
+    carry = tiles[blockIdx.x];
+  }
   load_tile(src, blockIdx.x, tile);
   T r[kScanItems];
   T v = Op::template id<T>();
@@ -133,12 +146,11 @@ __global__ void __launch_bounds__(kScanThreads) ks_tile_scan(S src, const typena
     v = Op::op(v, tile[threadIdx.x * kScanItems + k]);
     r[k] = v;
   }
-  const T pre = Op::op(tiles[blockIdx.x], block_scan<T, Op>(v, thr, wsum));
+  const T pre = Op::op(carry, block_scan<T, Op>(v, thr, wsum));
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) tile[threadIdx.x * kScanItems + k] = Op::op(pre, r[k]);
   __syncthreads();
   const long long base = (long long)blockIdx.x * kScanTile;
-  const T carry = tiles[blockIdx.x];
   for (int e = threadIdx.x; e < kScanTile; e += blockDim.x) {
     const long long g = base + e;
     if (g < src.n) src.store(g, tile[e], e ? tile[e - 1] : carry);
