@@ -295,6 +295,12 @@ long long scene_bytes(long long np, long long nn, long long ncell, bool sgmp, bo
   return np * per_p + nn * per_n + (std::max(nn, ncell) + 1) * per_k + ncell * per_c + 4096;
 }
 
+// multiplier of div_by for the divisor d (>= 1): floor(2^64 / d) + 1, exact
+// for every 32-bit dividend since n * (m - 2^64 / d) < 2^64 / d; 0 for d = 1
+unsigned long long div_magic(long long d) {
+  return d > 1 ? ~0ull / (unsigned long long)d + 1ull : 0ull;
+}
+
 void layout_flags(mpm_batch* b) {
   b->any_sgmp = b->any_nonsgmp = b->any_usf = b->any_later = b->any_musl = b->any_jc = b->any_dr = b->any_uvfp = 0;
   b->any_nonuvfp = 0;
@@ -909,6 +915,8 @@ int commit(mpm_batch* b) {
     }
     sc.fidcell_lo = (float)(g.iDCell - (double)sc.fidcell);
     sc.fcutoff = (float)g.cutoff;
+    sc.mNGx = div_magic(g.NGx); sc.mNGxy = div_magic(g.NGxy); sc.mNCx = div_magic(g.NCx);
+    sc.mNCxy = div_magic(g.NCxy); sc.mCNCx = div_magic(g.CNCx); sc.mCNCxy = div_magic(g.CNCxy);
     scenes.push_back(sc);
     for (auto m : h->su.mats) mats.push_back(m);
     for (auto bo : h->su.bodies) {

@@ -56,7 +56,10 @@ struct Scene {
   // FP32 copies for the mixed-precision kernels (a conversion from FP64 runs
   // on GB300's narrow FP64 pipe, once per thread that makes it)
   float fdcell, fidcell, fbq1, fbq2, fdamp, fiJacobi4, fnp, fspan0[3];
-  float fidcell_lo, fspan0_lo[3], fcutoff;  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
+  float fidcell_lo, fspan0_lo[3], fcutoff;
+  // division by the grid's row and layer sizes: n / d = the high 64 bits of
+  // n * m for 0 <= n < 2^32, m = floor(2^64 / d) + 1 (0 for d = 1), see div_by
+  unsigned long long mNGx, mNGxy, mNCx, mNCxy, mCNCx, mCNCxy;  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
   int has_fxp;  // some particle of the scene carries an external force
 };
 

@@ -13,10 +13,16 @@ __device__ __forceinline__ long long btid() { return (long long)blockIdx.x * blo
 __device__ __forceinline__ bool scene_live(const BState& b, int s) { return b.sst[s].active != 0; }
 
 // local node (jx, jy, jz) of a global node index
+// n / d for 0 <= n < 2^32 by the multiplier m of d (Scene::m*; 0: d = 1),
+// a 64-bit high multiply instead of an integer division
+__device__ __forceinline__ int div_by(long long n, unsigned long long m) {
+  return m ? (int)__umul64hi((unsigned long long)n, m) : (int)n;
+}
+
 __device__ __forceinline__ void node_xyz(const Scene& sc, long long ln, int& jx, int& jy, int& jz) {
-  jz = (int)(ln / sc.NGxy);
+  jz = div_by(ln, sc.mNGxy);
   int rem = (int)(ln - (long long)jz * sc.NGxy);
-  jy = rem / sc.NGx;
+  jy = div_by(rem, sc.mNGx);
   jx = rem - jy * sc.NGx;
 }
 
@@ -550,9 +556,9 @@ __device__ __forceinline__ void part_scatter_task(BState& b, const Scene& sc, lo
   float off[3] = {0.f, 0.f, 0.f};
   int key = -1;
   if (cl >= 0) {
-    c[2] = cl / sc.NCxy;
+    c[2] = div_by(cl, sc.mNCxy);
     const int rem = cl - c[2] * sc.NCxy;
-    c[1] = rem / sc.NCx;
+    c[1] = div_by(rem, sc.mNCx);
     c[0] = rem - c[1] * sc.NCx;
 #pragma unroll
     for (int a = 0; a < 3; ++a) off[a] = b.off[a * NP + i];
@@ -752,7 +758,7 @@ __device__ __forceinline__ void sg_part_task(BState& b, const Scene& sc, long lo
     }
     const int dj = __shfl_sync(0xffffffffu, d, e);  // flush into the centre nodes
     if (active) {
-      const int dz = dj / sc.CNCxy, rm = dj - dz * sc.CNCxy, dy = rm / sc.CNCx, dx = rm - dy * sc.CNCx;
+      const int dz = div_by(dj, sc.mCNCxy), rm = dj - dz * sc.CNCxy, dy = div_by(rm, sc.mCNCx), dx = rm - dy * sc.CNCx;
       const long long cid = sg_corner_cell(sc, dx, dy, dz, k);
       if (cid >= 0) {
 #pragma unroll
@@ -997,7 +1003,7 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   if (sc.shape == 3) {
     int d = b.dual[i];
     if (d < 0) return -1.f;
-    int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+    int dz = div_by(d, sc.mCNCxy), rem = d - dz * sc.CNCxy, dy = div_by(rem, sc.mCNCx), dx = rem - dy * sc.CNCx;
     float xx[3] = {b.xxn[i], b.xxn[NP + i], b.xxn[2 * NP + i]};
     for (int k = 0; k < 8; ++k) {
       int oc[3] = {kCorner[k][0], kCorner[k][1], kCorner[k][2]};
@@ -1015,9 +1021,9 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
     const int cl = b.cell[i];
     if (cl < 0) return -1.f;
     int c[3];
-    c[2] = cl / sc.NCxy;
+    c[2] = div_by(cl, sc.mNCxy);
     int rem = cl - c[2] * sc.NCxy;
-    c[1] = rem / sc.NCx;
+    c[1] = div_by(rem, sc.mNCx);
     c[0] = rem - c[1] * sc.NCx;
     float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
     int t0[3], nt[3];
@@ -1380,9 +1386,9 @@ __global__ void kb_sg_centre_gradient(BState b, int usf_pass) {
   const long long NC = b.NC;
   long long lc = c - sc.c0;
   int q[3];
-  q[2] = (int)(lc / sc.NCxy);
+  q[2] = div_by(lc, sc.mNCxy);
   int rem = (int)(lc - (long long)q[2] * sc.NCxy);
-  q[1] = rem / sc.NCx;
+  q[1] = div_by(rem, sc.mNCx);
   q[0] = rem - q[1] * sc.NCx;
   float co[6] = {0, 0, 0, 0, 0, 0}, cw[3] = {0, 0, 0}, cf[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   const float j4 = sc.fiJacobi4;
@@ -1422,9 +1428,9 @@ __global__ void kb_sg_centre_velocity(BState b) {
   const Scene& sc = b.scenes[s];
   long long lc = c - sc.c0;
   int q[3];
-  q[2] = (int)(lc / sc.NCxy);
+  q[2] = div_by(lc, sc.mNCxy);
   int rem = (int)(lc - (long long)q[2] * sc.NCxy);
-  q[1] = rem / sc.NCx;
+  q[1] = div_by(rem, sc.mNCx);
   q[0] = rem - q[1] * sc.NCx;
   const int NCd[3] = {sc.NCx, sc.NCy, sc.NCz};
   const long long NC = b.NC;
@@ -1481,7 +1487,7 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
   if (sc.shape == 3) {
     int d = b.dual[i];
     if (d < 0) return -1.f;
-    int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+    int dz = div_by(d, sc.mCNCxy), rem = d - dz * sc.CNCxy, dy = div_by(rem, sc.mCNCx), dx = rem - dy * sc.CNCx;
     int ln = b.inode[i];
     int bd = ln >= 0 ? b.bd[sc.n0 + ln] : 0;
     float xx[3];
@@ -1512,9 +1518,9 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
     const int cl = b.cell[i];
     if (cl < 0) return -1.f;
     int c[3];
-    c[2] = cl / sc.NCxy;
+    c[2] = div_by(cl, sc.mNCxy);
     int rem = cl - c[2] * sc.NCxy;
-    c[1] = rem / sc.NCx;
+    c[1] = div_by(rem, sc.mNCx);
     c[0] = rem - c[1] * sc.NCx;
     float off[3] = {b.off[i], b.off[NP + i], b.off[2 * NP + i]};
     int t0[3], nt[3];
@@ -1849,7 +1855,7 @@ __global__ void kb_smooth_p2g(BState b, int scene, const unsigned* bnd, unsigned
   if (sc.shape == 3) {
     const int d = b.dual[i];
     if (d < 0) return;
-    const int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+    const int dz = div_by(d, sc.mCNCxy), rem = d - dz * sc.CNCxy, dy = div_by(rem, sc.mCNCx), dx = rem - dy * sc.CNCx;
     const long long nc = sc.nc;
     for (int c = 0; c < 8; ++c) {
       const long long cid = sg_corner_cell(sc, dx, dy, dz, c);
@@ -1865,8 +1871,8 @@ __global__ void kb_smooth_p2g(BState b, int scene, const unsigned* bnd, unsigned
   const int cl = b.cell[i];
   if (cl < 0) return;
   int c[3];
-  c[2] = cl / sc.NCxy;
-  c[1] = (cl - c[2] * sc.NCxy) / sc.NCx;
+  c[2] = div_by(cl, sc.mNCxy);
+  c[1] = div_by(cl - c[2] * sc.NCxy, sc.mNCx);
   c[0] = cl - c[2] * sc.NCxy - c[1] * sc.NCx;
   float off[3];
   for (int a = 0; a < 3; ++a)
@@ -1930,7 +1936,7 @@ __global__ void kb_smooth_back(BState b, int scene, const double* gpre, double* 
   const Scene& sc = b.scenes[scene];
   const long long c = btid();
   if (c >= sc.nc) return;
-  const int cz = (int)(c / sc.NCxy), rem = (int)(c - (long long)cz * sc.NCxy), cy = rem / sc.NCx, cx = rem - cy * sc.NCx;
+  const int cz = div_by(c, sc.mNCxy), rem = (int)(c - (long long)cz * sc.NCxy), cy = div_by(rem, sc.mNCx), cx = rem - cy * sc.NCx;
   double g = 0.0;
   for (int k = 0; k < 8; ++k) {
     const long long ln = ((long long)(cz + kCorner[k][2]) * sc.NGy + cy + kCorner[k][1]) * sc.NGx + cx + kCorner[k][0];
@@ -1949,7 +1955,7 @@ __global__ void kb_smooth_g2p(BState b, int scene, const double* gpre, const dou
   if (sc.shape == 3) {
     const int d = b.dual[i];
     if (d >= 0) {
-      const int dz = d / sc.CNCxy, rem = d - dz * sc.CNCxy, dy = rem / sc.CNCx, dx = rem - dy * sc.CNCx;
+      const int dz = div_by(d, sc.mCNCxy), rem = d - dz * sc.CNCxy, dy = div_by(rem, sc.mCNCx), dx = rem - dy * sc.CNCx;
       for (int c = 0; c < 8; ++c) {
         const long long cid = sg_corner_cell(sc, dx, dy, dz, c);
         if (cid < 0) continue;
@@ -1961,8 +1967,8 @@ __global__ void kb_smooth_g2p(BState b, int scene, const double* gpre, const dou
   } else if (b.cell[i] >= 0) {
     const int cl = b.cell[i];
     int c[3];
-    c[2] = cl / sc.NCxy;
-    c[1] = (cl - c[2] * sc.NCxy) / sc.NCx;
+    c[2] = div_by(cl, sc.mNCxy);
+    c[1] = div_by(cl - c[2] * sc.NCxy, sc.mNCx);
     c[0] = cl - c[2] * sc.NCxy - c[1] * sc.NCx;
     float off[3];
     for (int a = 0; a < 3; ++a)
