@@ -438,7 +438,7 @@ int enqueue_back(mpm_batch* b) {
     // (and per volume update: by Fp or not)
     const unsigned ty = b->stress_types;
     const int f = __builtin_popcount(ty) > 1, uvf = b->any_uvfp && b->any_nonuvfp;
-    auto launch = [&](auto kern) { kern<<<gridn(s.NP, kStressThreads), kStressThreads, 0, st>>>(s, usf_pass, f, uvf); };
+    auto launch = [&](auto kern) { kern<<<gridn(s.NP, pb), pb, 0, st>>>(s, usf_pass, f, uvf); };
     if (b->any_nonuvfp) {
       if (ty & (1u << 1)) launch(kb_stress<1, 0>);
       if (ty & (1u << 9)) launch(kb_stress<9, 0>);
@@ -482,7 +482,7 @@ int enqueue_back(mpm_batch* b) {
     prof_end(K_SG_VELOCITY, st);
   }
   prof_begin(K_POSITION, st);
-  kb_position<<<gridn(s.NP, kPosThreads), kPosThreads, 0, st>>>(s);
+  kb_position<<<gridn(s.NP, pb), pb, 0, st>>>(s);
   prof_end(K_POSITION, st);
   if (b->any_musl) {
     prof_begin(K_SCATTER_MOM, st);
@@ -502,7 +502,7 @@ int enqueue_reduce(mpm_batch* b, cudaStream_t st) {
   BState& s = b->A;
   const int pb = b->pblock;
   prof_begin(K_REDUCE, st);
-  kb_reduce_chunks<1><<<(unsigned)s.NR, 256, 0, st>>>(s, 3);
+  kb_reduce_chunks<<<(unsigned)s.NR, 256, 0, st>>>(s, 3);
   prof_end(K_REDUCE, st);
   if (b->any_dr) {
     prof_begin(K_DR, st);
@@ -784,9 +784,9 @@ int commit(mpm_batch* b) {
   shared.tiles = al.get<int>(std::max(scan_tiles(NK), scan_tiles(NP)) + 1);
   shared.big = al.get<int>(NP / (kRegSeg + 1) + 1);
   shared.nbig = al.get<int>(1);
-  shared.mg = al.get<float>(NN);
-  shared.px = al.get<float>(3 * NN);
-  shared.fx = al.get<float>(3 * NN);
+  shared.mg = al.get<double>(NN);
+  shared.px = al.get<double>(3 * NN);
+  shared.fx = al.get<double>(3 * NN);
   shared.nvel = al.get<float4>(NN);
   shared.nacc = al.get<float4>(NN);
   shared.acc = al.get<unsigned long long>(4 * NN);
@@ -914,7 +914,6 @@ int commit(mpm_batch* b) {
       sc.fspan0_lo[k] = (float)(g.span0[k] - (double)sc.fspan0[k]);
     }
     sc.fidcell_lo = (float)(g.iDCell - (double)sc.fidcell);
-    sc.fcutoff = (float)g.cutoff;
     sc.mNGx = div_magic(g.NGx); sc.mNGxy = div_magic(g.NGxy); sc.mNCx = div_magic(g.NCx);
     sc.mNCxy = div_magic(g.NCxy); sc.mCNCx = div_magic(g.CNCx); sc.mCNCxy = div_magic(g.CNCxy);
     scenes.push_back(sc);
@@ -940,7 +939,6 @@ int commit(mpm_batch* b) {
       s0.dt = set_dt(h->su.mats, g.dcell, g.dtscale);
     }
     s0.fdt = (float)s0.dt;
-    s0.fdt_lo = (float)(s0.dt - (double)s0.fdt);
     s0.ftime = (float)s0.time;
     s0.active = h->resident ? 0 : 1;  // the initial energy pass below runs for new scenes only
     sst.push_back(s0);
@@ -961,9 +959,9 @@ int commit(mpm_batch* b) {
   BCK(cudaMemcpyAsync(shared.rscene, rscene.data(), 2 * NR, cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(d_target, target.data(), sizeof(int) * target.size(), cudaMemcpyHostToDevice, st));
   BCK(cudaMemcpyAsync(shared.sst, sst.data(), sizeof(SceneState) * sst.size(), cudaMemcpyHostToDevice, st));
-  BCK(cudaMemsetAsync(shared.mg, 0, sizeof(float) * NN, st));
-  BCK(cudaMemsetAsync(shared.px, 0, sizeof(float) * 3 * NN, st));
-  BCK(cudaMemsetAsync(shared.fx, 0, sizeof(float) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.mg, 0, sizeof(double) * NN, st));
+  BCK(cudaMemsetAsync(shared.px, 0, sizeof(double) * 3 * NN, st));
+  BCK(cudaMemsetAsync(shared.fx, 0, sizeof(double) * 3 * NN, st));
   BCK(cudaMemsetAsync(shared.nvel, 0, sizeof(float4) * NN, st));
   BCK(cudaMemsetAsync(shared.nacc, 0, sizeof(float4) * NN, st));
   BCK(cudaMemsetAsync(shared.acc, 0, sizeof(unsigned long long) * 4 * NN, st));
@@ -984,7 +982,7 @@ int commit(mpm_batch* b) {
   kb_inverse<<<gridn(NP, 256), 256, 0, st>>>(A);
   b->inv_stale = false;
   // calcEnergy of the new scenes (MPM3D.f90:42)
-  kb_reduce_chunks<0><<<(unsigned)NR, 256, 0, st>>>(A, 1);
+  kb_reduce_chunks<<<(unsigned)NR, 256, 0, st>>>(A, 1);
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(st));
   // swap in the new layout: its arena becomes current, the old one spare
@@ -1305,12 +1303,9 @@ int mpm_batch_scene_download(mpm_batch* b, int id, int field, double* out) {
   const long long NP = s.NP, np = h->np, p0 = h->p0;
   const int nc = mpm_field_components(field);
   if (field == MPM_G_MG || field == MPM_G_PX || field == MPM_G_FX) {
-    const float* src = field == MPM_G_MG ? s.mg : (field == MPM_G_PX ? s.px : s.fx);
-    std::vector<float> tmp((size_t)h->nn);
-    for (int a = 0; a < nc; ++a) {
-      BCK(cudaMemcpy(tmp.data(), src + a * s.NN + h->n0, sizeof(float) * h->nn, cudaMemcpyDeviceToHost));
-      for (long long k = 0; k < h->nn; ++k) out[a * h->nn + k] = (double)tmp[k];
-    }
+    const double* src = field == MPM_G_MG ? s.mg : (field == MPM_G_PX ? s.px : s.fx);
+    for (int a = 0; a < nc; ++a)
+      BCK(cudaMemcpy(out + a * h->nn, src + a * s.NN + h->n0, sizeof(double) * h->nn, cudaMemcpyDeviceToHost));
     if (field == MPM_G_MG)  // -0 marks a massless node with a force or momentum (the idle test)
       for (long long k = 0; k < h->nn; ++k) out[k] = out[k] + 0.0;
     return MPM_OK;

@@ -56,10 +56,10 @@ struct Scene {
   // FP32 copies for the mixed-precision kernels (a conversion from FP64 runs
   // on GB300's narrow FP64 pipe, once per thread that makes it)
   float fdcell, fidcell, fbq1, fbq2, fdamp, fiJacobi4, fnp, fspan0[3];
-  float fidcell_lo, fspan0_lo[3], fcutoff;
+  float fidcell_lo, fspan0_lo[3];  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
   // division by the grid's row and layer sizes: n / d = the high 64 bits of
   // n * m for 0 <= n < 2^32, m = floor(2^64 / d) + 1 (0 for d = 1), see div_by
-  unsigned long long mNGx, mNGxy, mNCx, mNCxy, mCNCx, mCNCxy;  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
+  unsigned long long mNGx, mNGxy, mNCx, mNCxy, mCNCx, mCNCxy;
   int has_fxp;  // some particle of the scene carries an external force
 };
 
@@ -70,7 +70,7 @@ struct SceneState {
   unsigned long long active_nodes;
   unsigned status;
   unsigned qmax[4];  // per-step contribution bounds of the P2G scatters (float bits)
-  float fdt, fdt_lo, ftime;  // FP32 dt, dt - fdt and time (written with dt and time)
+  float fdt, ftime;  // FP32 dt and time (written with dt and time)
   unsigned red_done;          // chunks of the energy reduction done this step (reset by the last)
 };
 
@@ -107,7 +107,7 @@ struct BState {
   LoopCtl* ctl;  // run-loop state (one per batch, outside the layout arena)
   int* task0;  // first particle task (32 sorted particles) of each scene, nscene + 1 entries; SGMP scenes have none
   // grid
-  float *mg, *px, *fx;  // FP32 node state: mass, momentum, force (from the exact fixed-point sums)
+  double *mg, *px, *fx;
   float4 *nvel, *nacc;             // FP32 px / mg and fx / mg for the gathers (zero at or below the cut-off)
   unsigned long long* acc;         // [4][NN] fixed-point P2G sums, zero between transfers
   uint8_t *fix, *bd;

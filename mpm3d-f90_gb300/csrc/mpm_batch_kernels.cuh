@@ -814,23 +814,16 @@ __global__ void __launch_bounds__(32 * PartShape<MODE>::WARPS, MODE == 2 ? 6 : 4
 // massless node that received a force or a momentum (IntegrateMomentum
 // integrates every node, so its momentum is F * DT) carries a mass of -0 as
 // the mark that its fields are not zero, and the next transfer clears them.
-// The value q * 2^-sh of a fixed-point sum in FP32: its two 32-bit halves
-// converted (32-bit conversions; a 64-bit one runs on GB300's narrow FP64
-// pipe) and combined, within an FP32 rounding or two of the exact value.
-__device__ __forceinline__ float q_value(long long q, int sh) {
-  return ldexpf(fmaf((float)(int)(q >> 32), 0x1p32f, (float)(unsigned)q), -sh);
-}
-
-__device__ __forceinline__ bool take_acc(BState& b, long long n, int nv, const int* sh, float* out) {
+__device__ __forceinline__ bool take_acc(BState& b, long long n, int nv, const double* unit, double* out) {
   unsigned long long q[4];
   unsigned long long any = 0ull;
   for (int v = 0; v < nv; ++v) {
     q[v] = b.acc[v * b.NN + n];
     any |= q[v];
   }
-  if (any == 0ull && __float_as_int(b.mg[n]) == 0) return false;
+  if (any == 0ull && __double_as_longlong(b.mg[n]) == 0ll) return false;
   for (int v = 0; v < nv; ++v) {
-    out[v] = q_value((long long)q[v], sh[v]);
+    out[v] = (double)(long long)q[v] * unit[v];
     if (q[v]) b.acc[v * b.NN + n] = 0ull;
   }
   return true;
@@ -842,19 +835,20 @@ __device__ __forceinline__ void node_finish(BState& b, const Scene& sc, long lon
     uint8_t f = b.fix[n];
     for (int a = 0; a < 3; ++a)
       if (f & (1 << a)) {
-        b.px[a * NN + n] = 0.f;
-        b.fx[a * NN + n] = 0.f;
+        b.px[a * NN + n] = 0.0;
+        b.fx[a * NN + n] = 0.0;
       }
   }
   if (vel) {
     // node velocity for the FP32 particle gathers; nodes at or below the
     // cut-off mass contribute nothing, so they hold zero
-    const float m = b.mg[n];
+    const double m = b.mg[n];
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (m > sc.fcutoff) {
-      v.x = b.px[n] / m;
-      v.y = b.px[NN + n] / m;
-      v.z = b.px[2 * NN + n] / m;
+    if (m > sc.cutoff) {
+      const float m32 = (float)m;
+      v.x = (float)b.px[n] / m32;
+      v.y = (float)b.px[NN + n] / m32;
+      v.z = (float)b.px[2 * NN + n] / m32;
     }
     b.nvel[n] = v;
   }
@@ -869,7 +863,7 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
     if (scene_live(b, s)) {
       const Scene& sc = b.scenes[s];
       const long long NN = b.NN;
-      float M = 0.f, P0 = 0.f, P1 = 0.f, P2 = 0.f;
+      double M = 0, P0 = 0, P1 = 0, P2 = 0;
       bool live = true;
       int j[3];
       node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
@@ -902,16 +896,16 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
             }
           }
         }
-        M = (float)(0.125 * ((double)QM * um));
-        P0 = (float)(0.125 * ((double)Q0 * up));
-        P1 = (float)(0.125 * ((double)Q1 * up));
-        P2 = (float)(0.125 * ((double)Q2 * up));
+        M = 0.125 * ((double)QM * um);
+        P0 = 0.125 * ((double)Q0 * up);
+        P1 = 0.125 * ((double)Q1 * up);
+        P2 = 0.125 * ((double)Q2 * up);
       } else {
         const SceneState& st = b.sst[s];
-        const int shp = q_shift(sc, st.qmax[Q_MOM]);
-        const int sh[4] = {q_shift(sc, st.qmax[Q_MASS]), shp, shp, shp};
-        float o[4];
-        live = take_acc(b, n, 4, sh, o);
+        const double up = q_unit(q_shift(sc, st.qmax[Q_MOM]));
+        const double unit[4] = {q_unit(q_shift(sc, st.qmax[Q_MASS])), up, up, up};
+        double o[4];
+        live = take_acc(b, n, 4, unit, o);
         M = o[0];
         P0 = o[1];
         P1 = o[2];
@@ -922,17 +916,17 @@ __global__ void kb_p2g_mass(BState b, int bc_usf, int vel_usf) {
         b.px[n] = P0;
         b.px[NN + n] = P1;
         b.px[2 * NN + n] = P2;
-        act = M > 0.f;
+        act = M > 0.0;
         node_finish(b, sc, n, bc_usf && sc.usf, vel_usf && sc.usf);
-        if (!(M != 0.f) && sc.shape != 3) {
+        if (!(M != 0.0) && sc.shape != 3) {
           // the node goes idle: clear the rest of its fields once (the idle
           // test of the later transfers skips it from now on)
-          for (int a = 0; a < 3; ++a) b.fx[a * NN + n] = 0.f;
+          for (int a = 0; a < 3; ++a) b.fx[a * NN + n] = 0.0;
           b.nvel[n] = make_float4(0.f, 0.f, 0.f, 0.f);
           b.nacc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
           // a momentum without mass (the mass contributions quantised to
           // zero, the momentum ones not) keeps the node marked (take_acc)
-          if (b.px[n] != 0.f || b.px[NN + n] != 0.f || b.px[2 * NN + n] != 0.f) b.mg[n] = -0.f;
+          if (b.px[n] != 0.0 || b.px[NN + n] != 0.0 || b.px[2 * NN + n] != 0.0) b.mg[n] = -0.0;
         }
       }
     }
@@ -1164,12 +1158,10 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   return force_stage(b, sc, st, i, ps.vol, ps.sm - ps.q, ps.sd);
 }
 
-// 256-thread blocks; Drucker-Prager at kStressBlocksDP blocks per SM, the
-// other specialised models at four (64 registers), the general one at two
-constexpr int kStressThreads = 256;
-constexpr int kStressBlocksDP = 6;
+// (Drucker-Prager runs best at three 512-thread blocks per SM -- 42
+// registers, some spilled -- the other specialised models at two)
 template <int MT, int UV>
-__global__ void __launch_bounds__(kStressThreads, MT == 10 ? kStressBlocksDP : (MT ? 4 : 2))
+__global__ void __launch_bounds__(512, MT == 10 ? 3 : (MT ? 2 : 1))
     kb_stress(BState b, int usf_pass, int filter, int uvf) {
   const long long i = btid();
   float bound = -1.f;
@@ -1306,23 +1298,25 @@ __global__ void kb_force_prep(BState b) {
 }
 
 // GridMomentumUpdate + IntegrateMomentum for one node
-__device__ __forceinline__ void node_integrate(BState& b, const Scene& sc, long long n, const float f[3]) {
+__device__ __forceinline__ void node_integrate(BState& b, const Scene& sc, long long n, const double f[3]) {
   const long long NN = b.NN;
   const SceneState& st = b.sst[b.node_scene[n]];
-  // p += f dt (f dt / 2 on the first step), dt as the pair fdt + fdt_lo
-  const float dth = st.istep == 1 ? 0.5f * st.fdt : st.fdt, dtl = st.istep == 1 ? 0.5f * st.fdt_lo : st.fdt_lo;
+  const double dt = st.dt;
   for (int a = 0; a < 3; ++a) {
     b.fx[a * NN + n] = f[a];
-    b.px[a * NN + n] = b.px[a * NN + n] + fmaf(f[a], dtl, f[a] * dth);
+    double p = b.px[a * NN + n];
+    p = st.istep == 1 ? p + f[a] * dt * 0.5 : p + f[a] * dt;
+    b.px[a * NN + n] = p;
   }
   node_finish(b, sc, n, 1, 1);
-  const float m = b.mg[n];
-  if (m == 0.f && sc.shape != 3) b.mg[n] = -0.f;  // fields not zero at a massless node (take_acc)
+  const double m = b.mg[n];
+  if (m == 0.0 && sc.shape != 3) b.mg[n] = -0.0;  // fields not zero at a massless node (take_acc)
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (m > sc.fcutoff) {
-    acc.x = b.fx[n] / m;
-    acc.y = b.fx[NN + n] / m;
-    acc.z = b.fx[2 * NN + n] / m;
+  if (m > sc.cutoff) {
+    const float m32 = (float)m;
+    acc.x = (float)b.fx[n] / m32;
+    acc.y = (float)b.fx[NN + n] / m32;
+    acc.z = (float)b.fx[2 * NN + n] / m32;
   }
   b.nacc[n] = acc;
 }
@@ -1335,7 +1329,7 @@ __global__ void kb_p2g_force(BState b) {
   const Scene& sc = b.scenes[s];
   int j[3];
   node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
-  float F[3] = {0.f, 0.f, 0.f};
+  double F[3] = {0, 0, 0};
   if (sc.shape == 3) {
     // centre nodes -> node (GridMomentumUpdate of SGMP): 1/8 of the cells'
     // external force minus Cfint . dN, dN = +-1 / (4 Jacobi) per direction
@@ -1366,11 +1360,11 @@ __global__ void kb_p2g_force(BState b) {
       }
     }
     const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
-    for (int a = 0; a < 3; ++a) F[a] = (float)((0.125 * (double)E[a] - sc.iJacobi4 * (double)T[a]) * u);
+    for (int a = 0; a < 3; ++a) F[a] = (0.125 * (double)E[a] - sc.iJacobi4 * (double)T[a]) * u;
   } else {
-    const int sf = q_shift(sc, b.sst[s].qmax[Q_FORCE]);
-    const int sh[3] = {sf, sf, sf};
-    if (!take_acc(b, n, 3, sh, F)) return;  // idle node
+    const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_FORCE]));
+    const double unit[3] = {u, u, u};
+    if (!take_acc(b, n, 3, unit, F)) return;  // idle node
   }
   node_integrate(b, sc, n, F);
 }
@@ -1553,17 +1547,18 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
         }
       }
   }
-  // the increments v dt and a dt (a dt / 2 on the first step) in FP32 with
-  // dt as the pair fdt + fdt_lo, added to the FP64 position and velocity:
-  // one FP64 add each (the conversions are integer operations)
-  const float dth = st.fdt, dtl = st.fdt_lo, ah = st.istep == 1 ? 0.5f * dth : dth, al = st.istep == 1 ? 0.5f * dtl : dtl;
+  // position and velocity integrated in FP64 (the FP32 interpolants
+  // converted exactly by integer operations; the FP32 velocity copy
+  // likewise)
+  const double dt = st.dt;
   float pv[3];
   for (int a = 0; a < 3; ++a) {
-    const double xx = b.x[a * NP + i] + f64_of(fmaf(v[a], dtl, v[a] * dth));
+    const double xx = b.x[a * NP + i] + f64_of(v[a]) * dt;
     b.xx[a * NP + i] = xx;
-    const double vv = b.v[a * NP + i] + f64_of(fmaf(acc[a], al, acc[a] * ah));
-    b.v[a * NP + i] = vv;
-    pv[a] = f32_rn(vv);
+    const double vv = b.v[a * NP + i];
+    const double vn = st.istep == 1 ? vv + f64_of(acc[a]) * dt * 0.5 : vv + f64_of(acc[a]) * dt;
+    b.v[a * NP + i] = vn;
+    pv[a] = f32_rn(vn);
     b.v32[a * NP + i] = pv[a];  // for GridMomentumMUSL's transfer
     if (sc.usf) b.x[a * NP + i] = xx;
   }
@@ -1576,9 +1571,7 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
 // (capped at 40 registers: six 256-thread blocks per SM hide the node
 // gathers' latency better than fewer blocks with more registers; a pblock of
 // 512 still launches)
-constexpr int kPosThreads = 256;
-constexpr int kPosBlocks = 6;
-__global__ void __launch_bounds__(kPosThreads, kPosBlocks) kb_position(BState b) {
+__global__ void __launch_bounds__(512, 3) kb_position(BState b) {
   const long long i = btid();
   float bound = -1.f;
   if (i < b.NP) bound = position_one(b, i);
@@ -1596,7 +1589,7 @@ __global__ void kb_p2g_momentum(BState b) {
   const long long NN = b.NN;
   int j[3];
   node_xyz(sc, n - sc.n0, j[0], j[1], j[2]);
-  float P0 = 0.f, P1 = 0.f, P2 = 0.f;
+  double P0 = 0, P1 = 0, P2 = 0;
   if (sc.shape == 3) {
     // centre nodes -> node (GridMomentumMUSL of SGMP), exact sums of the
     // cells' fixed-point momenta
@@ -1615,14 +1608,14 @@ __global__ void kb_p2g_momentum(BState b) {
       }
     }
     const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]));
-    P0 = (float)(0.125 * ((double)Q[0] * u));
-    P1 = (float)(0.125 * ((double)Q[1] * u));
-    P2 = (float)(0.125 * ((double)Q[2] * u));
+    P0 = 0.125 * ((double)Q[0] * u);
+    P1 = 0.125 * ((double)Q[1] * u);
+    P2 = 0.125 * ((double)Q[2] * u);
   } else {
-    const int sm = q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]);
-    const int sh[3] = {sm, sm, sm};
-    float o[3];
-    if (!take_acc(b, n, 3, sh, o)) return;  // idle node
+    const double u = q_unit(q_shift(sc, b.sst[s].qmax[Q_MOM_MUSL]));
+    const double unit[3] = {u, u, u};
+    double o[3];
+    if (!take_acc(b, n, 3, unit, o)) return;  // idle node
     P0 = o[0];
     P1 = o[1];
     P2 = o[2];
@@ -1630,8 +1623,8 @@ __global__ void kb_p2g_momentum(BState b) {
   b.px[n] = P0;
   b.px[NN + n] = P1;
   b.px[2 * NN + n] = P2;
-  if (sc.shape != 3 && b.mg[n] == 0.f && (P0 != 0.f || P1 != 0.f || P2 != 0.f))
-    b.mg[n] = -0.f;  // momentum at a massless node (take_acc)
+  if (sc.shape != 3 && b.mg[n] == 0.0 && (P0 != 0.0 || P1 != 0.0 || P2 != 0.0))
+    b.mg[n] = -0.0;  // momentum at a massless node (take_acc)
   node_finish(b, sc, n, 1, !sc.usf);
 }
 
@@ -1685,18 +1678,13 @@ __device__ __forceinline__ void reduce_scene_finish(BState& b, int s, int mode, 
     }
     st.dt = dt * sc.dtscale;
     st.fdt = (float)st.dt;
-    st.fdt_lo = (float)(st.dt - (double)st.fdt);
   }
 }
 
 // calcEnergy / UpdateDT: one block per chunk of kChunk particles of a live
-// scene writes the chunk's partial sums; the scene's last chunk block to
-// finish (a per-scene counter, reset by that block) forms the scene totals.
-// SRC 1: the FP32 velocity and mass copies the step wrote (the mixed form's
-// velocities carry FP32 precision); SRC 0: the FP64 fields rounded to FP32
-// (a new scene's first energies, before any step). A thread's particles
-// (kChunk / blockDim.x of them) are summed in FP32, the thread sums in FP64.
-template <int SRC>
+// scene sums the chunk in FP64 (the energy balance stays in FP64) and writes
+// its partial sums; the scene's last chunk block to finish (a per-scene
+// counter, reset by that block) forms the scene totals.
 __global__ void __launch_bounds__(256) kb_reduce_chunks(BState b, int mode) {
   __shared__ double sh[6][256];
   __shared__ int last;
@@ -1705,30 +1693,19 @@ __global__ void __launch_bounds__(256) kb_reduce_chunks(BState b, int mode) {
   if (!scene_live(b, s)) return;  // (uniform: every block of the scene returns)
   const Scene& sc = b.scenes[s];
   const long long NP = b.NP;
-  float acc[6] = {0, 0, 0, 0, 0, 0};
+  double acc[6] = {0, 0, 0, 0, 0, 0};
   const long long p_begin = sc.p0 + (r - sc.r0) * kChunk;
   const long long p_end = min(p_begin + kChunk, sc.p0 + sc.np);
   for (long long i = p_begin + threadIdx.x; i < p_end; i += blockDim.x) {
-    float v0, v1, v2, m;
-    if (SRC) {
-      v0 = b.v32[i];
-      v1 = b.v32[NP + i];
-      v2 = b.v32[2 * NP + i];
-      m = b.m32[i];
-    } else {
-      v0 = f32_rn(b.v[i]);
-      v1 = f32_rn(b.v[NP + i]);
-      v2 = f32_rn(b.v[2 * NP + i]);
-      m = f32_rn(b.mass[i]);
-    }
-    acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5f;
-    acc[1] += f32_rn(b.ie[i]);
+    const double v0 = b.v[i], v1 = b.v[NP + i], v2 = b.v[2 * NP + i], m = b.mass[i];
+    acc[0] += (v0 * v0 + v1 * v1 + v2 * v2) * m * 0.5;
+    acc[1] += b.ie[i];
     acc[2] += m * v0;
     acc[3] += m * v1;
     acc[4] += m * v2;
-    acc[5] = fmaxf(acc[5], fmaxf(fabsf(v0), fmaxf(fabsf(v1), fabsf(v2))));
+    acc[5] = fmax(acc[5], fmax(fabs(v0), fmax(fabs(v1), fabs(v2))));
   }
-  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = f64_of(acc[k]);
+  for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = acc[k];
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) {
@@ -1940,7 +1917,7 @@ __global__ void kb_smooth_back(BState b, int scene, const double* gpre, double* 
   double g = 0.0;
   for (int k = 0; k < 8; ++k) {
     const long long ln = ((long long)(cz + kCorner[k][2]) * sc.NGy + cy + kCorner[k][1]) * sc.NGx + cx + kCorner[k][0];
-    if (b.mg[sc.n0 + ln] > sc.fcutoff) g = g + 0.125 * gpre[ln];
+    if (b.mg[sc.n0 + ln] > sc.cutoff) g = g + 0.125 * gpre[ln];
   }
   cgpre[c] = g;
 }
