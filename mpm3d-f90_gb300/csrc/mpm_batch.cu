@@ -912,6 +912,8 @@ int commit(mpm_batch* b) {
     for (int k = 0; k < 3; ++k) {
       sc.fspan0[k] = (float)g.span0[k];
       sc.fspan0_lo[k] = (float)(g.span0[k] - (double)sc.fspan0[k]);
+      sc.fspan1[k] = (float)g.span1[k];
+      sc.fspan1_lo[k] = (float)(g.span1[k] - (double)sc.fspan1[k]);
     }
     sc.fidcell_lo = (float)(g.iDCell - (double)sc.fidcell);
     sc.mNGx = div_magic(g.NGx); sc.mNGxy = div_magic(g.NGxy); sc.mNCx = div_magic(g.NCx);

@@ -57,6 +57,7 @@ struct Scene {
   // on GB300's narrow FP64 pipe, once per thread that makes it)
   float fdcell, fidcell, fbq1, fbq2, fdamp, fiJacobi4, fnp, fspan0[3];
   float fidcell_lo, fspan0_lo[3];  // idcell - fidcell, span0 - fspan0 (FP32 double-float pairs)
+  float fspan1[3], fspan1_lo[3];    // span1 as an FP32 pair
   // division by the grid's row and layer sizes: n / d = the high 64 bits of
   // n * m for 0 <= n < 2^32, m = floor(2^64 / d) + 1 (0 for d = 1), see div_by
   unsigned long long mNGx, mNGxy, mNCx, mNCxy, mCNCx, mCNCxy;

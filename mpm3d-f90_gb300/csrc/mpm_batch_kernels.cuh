@@ -195,6 +195,58 @@ __device__ __forceinline__ long long dual_cell(const Scene& sc, const double x[3
   return (d >= 0 && d < sc.CNC) ? d : -1;
 }
 
+// (xh + xl) - (sh + sl) as a pair dh + dl: TwoSum of the leading parts, the
+// trailing parts added
+__device__ __forceinline__ void df_diff(float xh, float xl, float sh, float sl, float& dh, float& dl) {
+  const float s = xh - sh;
+  const float bb = s - xh;
+  const float err = (xh - (s - bb)) + (-sh - bb);
+  const float t = err + (xl - sl);
+  dh = s + t;
+  dl = t - (dh - s);
+}
+
+// The SGMP decisions of a position -- its cell and offsets (cell_of), its
+// nearest node (the cell's upper one from half a cell on) and its dual cell
+// (dual_cell) -- in FP32 double-float arithmetic: x - span0 and x - span1
+// as pairs, the coordinate in cells to about 2^-45. Returns false, leaving
+// the decisions to the FP64 routines, for a position outside the grid or
+// within 2^-40 (relative) of a grid face, a cell face or a half cell, where
+// the roundings of the FP64 arithmetic could decide otherwise; every
+// decision it returns is the FP64 one. (The nearest node and the dual cell
+// are discontinuous at the half cell, so they must be the FP64 ones.)
+__device__ __forceinline__ bool sg_locate_df(const Scene& sc, const double x[3], int cc[3], float off[3], int nd[3],
+                                             long long& dual) {
+  const int nc[3] = {sc.NCx, sc.NCy, sc.NCz};
+  int dc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float xh, xl, dh, dl, eh, el;
+    f32_split(x[a], xh, xl);
+    df_diff(xh, xl, sc.fspan0[a], sc.fspan0_lo[a], dh, dl);
+    df_diff(xh, xl, sc.fspan1[a], sc.fspan1_lo[a], eh, el);
+    const float gtol = 0x1p-40f * fabsf(xh);
+    if (!(dh > gtol && eh < -gtol)) return false;  // outside or at a grid face
+    const float uh = dh * sc.fidcell;
+    const float ul = fmaf(dh, sc.fidcell, -uh) + fmaf(dh, sc.fidcell_lo, dl * sc.fidcell);
+    const float cf = floorf(uh), fh = uh - cf;  // (exact)
+    // distances to the cell's faces and its half (a rounded sum keeps the
+    // sign of the exact one)
+    const float r0 = fh + ul, r1 = (fh - 1.f) + ul, rh = (fh - 0.5f) + ul;
+    const float tol = 0x1p-40f * fmaxf(1.f, uh);
+    if (!(r0 > tol && r1 < -tol && fabsf(rh) > tol)) return false;
+    const int c = (int)cf;
+    if (c >= nc[a]) return false;
+    cc[a] = c;
+    off[a] = r0;
+    nd[a] = c + (rh > 0.f);
+    dc[a] = max(nd[a] - 1, 0);  // trunc(u - 1/2): 0 below half a cell
+  }
+  const long long d = ((long long)dc[2] * sc.CNCy + dc[1]) * sc.CNCx + dc[0];
+  dual = (d >= 0 && d < sc.CNC) ? d : -1;
+  return true;
+}
+
 // ------------------------------------------------------------------ keys
 // Sort key of a particle: its scene's key base plus its cell (linear,
 // B-spline), its nearest node (GIMP) or its dual cell (SGMP); the scene's
@@ -214,7 +266,9 @@ __global__ void kb_keys(BState b) {
     double x[3] = {b.x[i], b.x[NP + i], b.x[2 * NP + i]};
     long long c = -1;
     if (sc.shape == 3) {
-      c = dual_cell(sc, x);
+      int cc[3], nd[3];
+      float off[3];
+      if (!sg_locate_df(sc, x, cc, off, nd, c)) c = dual_cell(sc, x);
     } else {
       // The coordinate in cells is formed in FP32 from the positions
       // truncated to FP32 by integer operations (GB300's FP64 pipe is
@@ -315,23 +369,31 @@ __device__ __forceinline__ int permute_one(const BState& src, BState& dst, long 
   // derived
   int cc[3];
   float off[3];
-  const bool in = sc.shape == 3 ? cell_of(sc, x, cc, off) : cell_of_df(sc, x, cc, off);
-  for (int a = 0; a < 3; ++a) dst.off[a * NP + i] = off[a];
-  dst.cell[i] = in ? (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0] : -1;
-  if (sc.shape == 3) {
-    // dual (cell-centre) grid: CenterInWhichCell (FP64, as the sort keys) and
-    // the nearest node with the particle's coordinates about it. The node is
-    // the cell's upper one from half a cell on, decided on the exact FP64
-    // offset (the node must stay the one above the dual cell: deciding on
-    // the FP32 offset would move particles within 3e-8 of the half onto the
-    // other node); XXN = 2 off - 2 (upper node) or 2 off in FP32 -- no
-    // further FP64 arithmetic (the narrow FP64 pipe bounds this kernel)
-    int nd[3];
+  int nd[3];
+  long long dualc = -1;
+  bool in;
+  if (sc.shape != 3) {
+    in = cell_of_df(sc, x, cc, off);
+  } else if (sg_locate_df(sc, x, cc, off, nd, dualc)) {
+    in = true;
+  } else {
+    in = cell_of(sc, x, cc, off);
     for (int a = 0; a < 3; ++a) {
       const double u = (x[a] - sc.span0[a]) * sc.idcell;  // (as in cell_of)
       nd[a] = cc[a] + (u - (double)cc[a] >= 0.5);
     }
-    dst.dual[i] = (int)dual_cell(sc, x);
+    dualc = dual_cell(sc, x);
+  }
+  for (int a = 0; a < 3; ++a) dst.off[a * NP + i] = off[a];
+  dst.cell[i] = in ? (cc[2] * sc.NCy + cc[1]) * sc.NCx + cc[0] : -1;
+  if (sc.shape == 3) {
+    // dual (cell-centre) grid: CenterInWhichCell (as the sort keys) and the
+    // nearest node with the particle's coordinates about it, both decided
+    // as in FP64 (sg_locate_df or the FP64 routines above: the node must
+    // stay the one above the dual cell, deciding on the FP32 offset would
+    // move particles within 3e-8 of the half onto the other node);
+    // XXN = 2 off - 2 (upper node) or 2 off in FP32
+    dst.dual[i] = (int)dualc;
     bool nin = nd[0] >= 0 && nd[0] < sc.NGx && nd[1] >= 0 && nd[1] < sc.NGy && nd[2] >= 0 && nd[2] < sc.NGz;
     int ln = nin ? (nd[2] * sc.NGy + nd[1]) * sc.NGx + nd[0] : -1;
     dst.inode[i] = ln;
