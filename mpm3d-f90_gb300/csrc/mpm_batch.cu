@@ -382,9 +382,7 @@ int enqueue_front(mpm_batch* b) {
   // counting sort by key (mpm_sort.cuh): segment ends and the occupied
   // keys, placement, then the stable order inside each segment
   prof_begin(K_SORT, st);
-  scan_tiles_enqueue(IntScan<ScanSum>{a.seg, a.seg, a.NK}, a.tiles, st);
-  BCK(cudaMemsetAsync(a.fill, 0, sizeof(int) * (size_t)a.NK, st));
-  BCK(cudaMemsetAsync(a.nbig, 0, sizeof(int), st));
+  scan_tiles_enqueue(SegScan{a.seg, a.fill, a.NK}, a.tiles, st);  // (zeroes the fill counters; kb_keys the long-segment count)
   ks_place<<<gridn(a.NP, 256), 256, 0, st>>>(a.key, a.seg, a.fill, a.perm, a.NP);
   ks_segments<<<gridn(a.NK, 256), 256, 0, st>>>(a.seg, a.NK, a.perm, a.big, a.nbig);
   ks_long_segments<<<b->sort_blocks, kSegThreads, 0, st>>>(a.seg, a.perm, a.big, a.nbig);

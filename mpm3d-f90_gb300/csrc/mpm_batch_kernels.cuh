@@ -259,6 +259,7 @@ __device__ __forceinline__ bool sg_locate_df(const Scene& sc, const double x[3],
 // 3 box of nodes instead of the 4 x 4 x 4 box of a cell's particles.
 __global__ void kb_keys(BState b) {
   const long long i = btid();
+  if (i == 0) *b.nbig = 0;  // long-segment count of this step's sort
   unsigned key = 0xffffffffu;
   if (i < b.NP) {
     const long long NP = b.NP;
@@ -1539,6 +1540,13 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
   const Scene& sc = b.scenes[s];
   const SceneState& st = b.sst[s];
   const long long NP = b.NP;
+  // the particle's FP64 position and velocity, loaded before the node
+  // gathers so that their latency overlaps the gathers'
+  double x0[3], v0[3];
+  for (int a = 0; a < 3; ++a) {
+    x0[a] = b.x[a * NP + i];
+    v0[a] = b.v[a * NP + i];
+  }
   float v[3] = {0, 0, 0}, acc[3] = {0, 0, 0};
   if (sc.shape == 3) {
     int d = b.dual[i];
@@ -1615,9 +1623,9 @@ __device__ __forceinline__ float position_one(BState& b, long long i) {
   const double dt = st.dt;
   float pv[3];
   for (int a = 0; a < 3; ++a) {
-    const double xx = b.x[a * NP + i] + f64_of(v[a]) * dt;
+    const double xx = x0[a] + f64_of(v[a]) * dt;
     b.xx[a * NP + i] = xx;
-    const double vv = b.v[a * NP + i];
+    const double vv = v0[a];
     const double vn = st.istep == 1 ? vv + f64_of(acc[a]) * dt * 0.5 : vv + f64_of(acc[a]) * dt;
     b.v[a * NP + i] = vn;
     pv[a] = f32_rn(vn);

@@ -171,6 +171,21 @@ struct IntScan {
   __device__ __forceinline__ void store(long long g, int v, int) const { out[g] = v; }
 };
 
+// the per-key counts scanned in place into segment ends, the keys' fill
+// counters zeroed on the way (the placement's slots start at zero)
+struct SegScan {
+  using T = int;
+  using Op = ScanSum;
+  int* seg;
+  int* fill;
+  long long n;
+  __device__ __forceinline__ int load(long long g) const { return seg[g]; }
+  __device__ __forceinline__ void store(long long g, int v, int) const {
+    seg[g] = v;
+    fill[g] = 0;
+  }
+};
+
 // ---------------------------------------------------------- counting sort
 constexpr int kRegSeg = 32;         // segments up to this length are ordered by one thread
 constexpr int kSegThreads = 256;    // threads of the long-segment blocks
