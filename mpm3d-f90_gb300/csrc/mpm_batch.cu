@@ -1400,6 +1400,10 @@ int mpm_batch_scene_snapshot(mpm_batch* b, int id, std::vector<unsigned char>& o
     for (int a = 0; a < f.nc; ++a) {
       const size_t at = out.size(), n = (size_t)np * f.elem;
       out.resize(at + n);
+      if (f.p == static_cast<const void*>(s.fxp) && !h->any_fxp) {
+        memset(out.data() + at, 0, n);  // (not moved by the permutation: zero in the deck, never read)
+        continue;
+      }
       BCK(cudaMemcpy(out.data() + at, static_cast<const char*>(f.p) + ((size_t)a * NP + p0) * f.elem, n,
                      cudaMemcpyDeviceToHost));
     }
