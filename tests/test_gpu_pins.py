@@ -12,7 +12,7 @@
    still creeping at the exit test and match the table at that instant: the
    table's 23072 figures come from settings other than the shipped decks'.
    Those four are held to 0.6% of the table.
-2. The spec case: the full Taylor bar (16 k particles, Johnson-Cook with
+2. The 1000-step Taylor bar: the full bar (16 k particles, Johnson-Cook with
    failure + linear EOS, USF) for 1000 steps. The strict FP64 form must be bit
    identical to the oracle with the same libm; against the oracle on glibc the
    nodal momentum and particle stress must agree to 1e-10 relative, or to the
@@ -61,7 +61,7 @@ def _rel(a, b):
 
 
 @pytest.mark.gpu
-def test_taylor_bar_1000_steps_north_star(gpu_mod, oracle_mod):
+def test_taylor_bar_1000_steps_vs_oracle(gpu_mod, oracle_mod):
     from mpm3d_gb300 import decks
 
     text = decks.taylor_bar()
