@@ -1221,8 +1221,9 @@ __device__ __forceinline__ float stress_one(BState& b, long long i, int usf_pass
   return force_stage(b, sc, st, i, ps.vol, ps.sm - ps.q, ps.sd);
 }
 
-// (Drucker-Prager runs best at three 512-thread blocks per SM -- 42
-// registers, some spilled -- the other specialised models at two)
+// (Drucker-Prager runs best at 1536 threads per SM -- 40 registers, some
+// spilled -- faster than at 1024 threads without spills; the other
+// specialised models at 1024)
 template <int MT, int UV>
 __global__ void __launch_bounds__(512, MT == 10 ? 3 : (MT ? 2 : 1))
     kb_stress(BState b, int usf_pass, int filter, int uvf) {
